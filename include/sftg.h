@@ -1,0 +1,137 @@
+/*
+ * sftg — the C ABI between sofren2's host runtime (include/sofren2.h, SFT_IMPL) and the
+ * GB300 kernels.  Plain pointers and sizes only.  Every call returns 0 on success or a
+ * negative SFTG_E* code; sftg_last_error() gives the text.  One context drives one GPU.
+ *
+ * Each entry point replaces a piece of the reference's CPU frame machinery (sofren2.c):
+ *   sftg_create / sftg_destroy      thread pool, barriers and arenas of sft_init / sft_release
+ *                                   (sofren2.c:7974-8137); here a stream plus device arenas
+ *   sftg_texture_upload             the texture heap of sft_texture_create (sofren2.c:9181-9310):
+ *                                   the caller passes the block-linear mip chain it built
+ *   sftg_material_set               the static material pool (sofren2.c:9393-9424)
+ *   sftg_model_upload               the meshlet / BLAS data a loaded sft_model carries
+ *                                   (sft_model, sofren2.c:1057-1123)
+ *   sftg_frame_render               sft_present (sofren2.c:8139-8289): proxy occlusion, geometry
+ *                                   and binning jobs, tile raster and resolve, written to the
+ *                                   caller's colour buffer (sft_set_color_buffer, 8405-8408)
+ */
+#ifndef SFTG_H
+#define SFTG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFTG_OK 0
+#define SFTG_E_CUDA (-1)          /* a CUDA call failed (text in sftg_last_error) */
+#define SFTG_E_ARG (-2)           /* invalid argument */
+#define SFTG_E_NOMEM (-3)         /* device allocation failed */
+#define SFTG_E_LIMIT (-4)         /* a reference limit was exceeded (e.g. > 64 instances) */
+#define SFTG_E_DEVICE_STATUS (-5) /* a kernel reported a bounded-walk overflow */
+
+typedef struct sftg_ctx sftg_ctx;
+
+/* texture description: level offsets are relative to the first texel passed */
+typedef struct sftg_texture_desc {
+    int32_t width, height, levels, is_pot;
+    uint32_t level_offset[14];
+    int32_t blocks_w[14];
+    int32_t stride_shift[14];
+} sftg_texture_desc;
+
+/* one mesh of a model: meshlet_count meshlets, each with
+ *   attr     f32[10][64]  x y z nx ny nz u v lu lv
+ *   inds     u8[512]      16 batches x [v0 x8, v1 x8, v2 x8, pad x8]
+ *   cull     f32[8]       sphere centre xyz, radius, cone axis xyz, cone cutoff
+ *   joints   u16[4][64], weights u8[4][64], culling_bone i32   (skinned meshes only, else NULL) */
+typedef struct sftg_mesh_desc {
+    uint32_t meshlet_count;
+    const float* attr;
+    const uint8_t* inds;
+    const float* cull;
+    const uint16_t* joints;
+    const uint8_t* weights;
+    const int32_t* culling_bones;
+    int32_t material;          /* material index, -1 = none */
+    int32_t lightmap_texture;  /* texture index, -1 = no lightmap */
+} sftg_mesh_desc;
+
+typedef struct sftg_model_desc {
+    uint32_t mesh_count;
+    const sftg_mesh_desc* meshes;
+    uint32_t bone_count;
+    const void* blas_nodes;    /* sft_bvh_node images, 256 B each */
+    uint32_t blas_count, blas_root;
+} sftg_model_desc;
+
+typedef struct sftg_instance_desc {
+    int32_t model;
+    float transform[16];
+    const float* bones;        /* posed matrices (16 floats each) or NULL */
+    uint32_t bone_count;
+} sftg_instance_desc;
+
+typedef struct sftg_frame_desc {
+    int32_t width, height, samples;          /* samples: 1, 2 or 4 */
+    float cam_pos[3];
+    float view_proj[16];
+    float frustum_n[6][3], frustum_d[6];     /* normalised planes (sft_set_camera) */
+    float ambient[3], lightmap_brightness;
+    uint32_t clear, clear_color, shadows, debug_mode;
+    uint32_t n_point;
+    const float* point_lights;               /* per light: pos[3], color[3] (rgb * intensity), radius, 1/radius^2 */
+    uint32_t n_dir;
+    const float* dir_lights;                 /* per light: dir[3] (normalised), color[3] */
+    uint32_t n_instances;
+    const sftg_instance_desc* instances;
+    uint32_t n_proxies;
+    const float* proxies;                    /* per world proxy: posa[3], posb[3], radius, pad */
+    const void* tlas_nodes;                  /* sft_bvh_node images built on the host */
+    uint32_t tlas_count, tlas_root;
+} sftg_frame_desc;
+
+/* optional per-frame outputs for parity checks (any pointer may be NULL; host memory) */
+typedef struct sftg_debug_out {
+    float* vis_depth;          /* tiles * samples * 4096 */
+    uint32_t* vis_id;          /* tiles * samples * 4096 */
+    uint32_t* tile_counts;     /* tiles */
+    uint64_t* tile_payloads;   /* capacity tile_payload_cap */
+    uint64_t tile_payload_cap;
+    uint64_t* tile_payload_total;
+    float* ss_cache;           /* total screen-space meshlets * 576 */
+    uint8_t* light_vis;        /* proxies * 64 */
+    void* clip_tris;           /* clip_cap * 164 bytes */
+    uint64_t clip_cap;
+    uint64_t* clip_total;
+    float* shadow;             /* width * height * 16, 1x only */
+    uint32_t* status;          /* kernel status bits */
+} sftg_debug_out;
+
+int sftg_create(int device, sftg_ctx** out);
+void sftg_destroy(sftg_ctx* ctx);
+const char* sftg_last_error(const sftg_ctx* ctx);
+
+int sftg_texture_upload(sftg_ctx* ctx, const uint32_t* texels, uint64_t n_texels, const sftg_texture_desc* desc, int32_t* out_index);
+int sftg_texture_update_desc(sftg_ctx* ctx, int32_t index, const sftg_texture_desc* desc_or_null);
+int sftg_material_set(sftg_ctx* ctx, int32_t index, int32_t texture, uint32_t base_color, float shininess);
+int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* desc, int32_t* out_model);
+
+/* Renders one frame into `color` (host memory, pitch in bytes; width*4 when 0).  When the frame
+ * does not clear, the current content of `color` is read first (the reference keeps it). */
+int sftg_frame_render(sftg_ctx* ctx, const sftg_frame_desc* frame, uint32_t* color, int32_t pitch_bytes, sftg_debug_out* dbg);
+
+/* Same as sftg_frame_render but leaves the result in device memory: *out_device_color points at
+ * width*height u32 owned by the context (valid until the next frame). No host copies of pixels. */
+int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* frame, const uint32_t** out_device_color);
+
+/* Device time in ms of the last frame's kernels, split as [occlusion, geometry+clip, binning, tile]. */
+int sftg_last_timings(const sftg_ctx* ctx, float* out4);
+/* Number of kernels launched by the last frame. */
+int sftg_last_launch_count(const sftg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,852 @@
+/*
+ * sofren2 for GB300 — drop-in replacement for the reference's single-header C API.
+ *
+ * Same names, signatures and frame contract as the reference's public API
+ * (sofren2.c:744-863): lights, sft_set_color_buffer, sft_frame_begin, sft_set_camera,
+ * sft_draw_instance ..., sft_present, sft_frame_end.  As with the reference, exactly one
+ * translation unit defines SFT_IMPL before including this header; that TU gets the host
+ * runtime below, which keeps the frame state in C and renders through the sftg C ABI
+ * (include/sftg.h, libsofren2_gb300.so) on the GPU.  There is no CPU rendering path:
+ * sft_init fails loudly when no CUDA device or library is available.
+ *
+ * Compile-time options kept from the reference: SFT_USE_AA / SFT_AA_SAMPLES (1, 2, 4),
+ * SFT_FUNC, SFT_NO_DEBUG.  Additions (not in the reference) are marked "extension".
+ */
+#ifndef SOFREN2_GB300_H
+#define SOFREN2_GB300_H
+
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int8_t i8; typedef uint8_t u8; typedef int16_t i16; typedef uint16_t u16;
+typedef int32_t i32; typedef uint32_t u32; typedef int64_t i64; typedef uint64_t u64;
+typedef float f32; typedef double f64;
+
+enum sft_debug_mode {
+    SFT_DEBUG_NONE, SFT_DEBUG_WIREFRAME, SFT_DEBUG_TILES, SFT_DEBUG_DEPTH,
+    SFT_DEBUG_LIGHT_COUNT, SFT_DEBUG_CHECKERBOARD, SFT_DEBUG_COUNT
+};
+enum sft_dmesh_type { SFT_DMESH_QUADS, SFT_DMESH_TRIANGLES };
+
+typedef u32 sft_tex_handle;
+typedef u32 sft_mat_handle;
+#define SFT_INVALID_HANDLE 0xFFFFFFFF
+#define SFT_HANDLE_INDEX_MASK 0x0000FFFF
+#define SFT_HANDLE_GEN_SHIFT 16
+#define SFT_HANDLE_INDEX(h) ((h) & SFT_HANDLE_INDEX_MASK)
+#define SFT_MAT_TRANSIENT_BIT 0x80000000
+#define SFT_MAT_GEN_SHIFT 16
+#define SFT_MAT_GEN_MASK 0x7FFF0000
+#define SFT_MAT_INDEX_MASK 0x0000FFFF
+#define SFT_MAT_IS_TRANSIENT(h) (0 != ((h) & SFT_MAT_TRANSIENT_BIT))
+#define SFT_MAT_INDEX(h) ((h) & SFT_MAT_INDEX_MASK)
+
+#define SFT_PI (3.14159265358979323846)
+#define SFT_EPSILON (1e-6f)
+#define SFT_V(a, b, c) (sftvec){ .x = (a), .y = (b), .z = (c) }
+#define SFT_MAX_INSTANCES_PER_FRAME 64
+#define SFT_VERTS_PER_MESHLET 64
+
+#ifdef SFT_USE_AA
+    #ifndef SFT_AA_SAMPLES
+        #define SFT_AA_SAMPLES 4
+    #endif
+#else
+    #ifndef SFT_AA_SAMPLES
+        #define SFT_AA_SAMPLES 1
+    #endif
+#endif
+
+#ifndef SFT_FUNC
+    #define SFT_FUNC static
+#endif
+
+typedef struct sftvec { f32 x, y, z; } sftvec;
+typedef struct sftquat { f32 x, y, z, w; } sftquat;
+typedef union sftmat { sftquat rows[4]; f32 m[4][4]; } sftmat;
+
+typedef struct sft_arena { u8* base; u64 max_size; u64 committed_size; u64 offset; volatile i32 commit_lock; } sft_arena;
+
+typedef struct sft_model sft_model;      /* host mirror of a device-resident model */
+typedef struct sft_dmesh sft_dmesh;
+typedef struct sft_dmesh_qb sft_dmesh_qb;
+
+typedef struct sft_pose {
+    const sft_model* model;
+    sftmat* global_matrices;
+    sftmat* posed_bone_matrices;
+} sft_pose;
+
+typedef struct sft_instance {
+    const sft_model* model;
+    sftmat transform;
+    u32 ss_meshlet_offset;
+    sftmat* posed_bone_matrices;
+} sft_instance;
+
+/* capsule shadow proxy in model (or bone) space, sofren2.c:985-989 */
+typedef struct sft_shadow_proxy { sftvec posa, posb; f32 radius; u32 bone_ind; } sft_shadow_proxy;
+
+/* extension: meshlet arrays of one mesh in the reference's layout (sofren2.c:914-953, 1071-1092) */
+typedef struct sft_mesh_data {
+    u32 meshlet_count;
+    const f32* attr;            /* [meshlet][10][64]: x y z nx ny nz u v lu lv */
+    const u8* inds;             /* [meshlet][512] */
+    const f32* cull;            /* [meshlet][8]: sphere centre, radius, cone axis, cone cutoff */
+    const u16* joints;          /* [meshlet][4][64] or NULL */
+    const u8* weights;          /* [meshlet][4][64] or NULL */
+    const i32* culling_bones;   /* [meshlet] or NULL */
+    sft_mat_handle material;
+    u32 lightmap_page;          /* index into the model's lightmaps, 0xFFFFFFFF = none */
+} sft_mesh_data;
+
+/* math (sofren2.c:745-792) */
+SFT_FUNC sftvec sft_v_add(sftvec a, sftvec b);
+SFT_FUNC sftvec sft_v_sub(sftvec a, sftvec b);
+SFT_FUNC sftvec sft_v_mul(sftvec a, f32 b);
+SFT_FUNC sftvec sft_v_div(sftvec a, f32 b);
+SFT_FUNC f32 sft_v_dot(sftvec a, sftvec b);
+SFT_FUNC sftvec sft_v_cross(sftvec a, sftvec b);
+SFT_FUNC f32 sft_v_length(sftvec v);
+SFT_FUNC f32 sft_v_length2(sftvec v);
+SFT_FUNC sftvec sft_v_norm(sftvec v);
+SFT_FUNC sftvec sft_v_normf(f32 x, f32 y, f32 z);
+SFT_FUNC sftvec sft_v_lerp(sftvec a, sftvec b, f32 t);
+SFT_FUNC sftmat sft_m_identity(void);
+SFT_FUNC sftmat sft_m_rot_x(f32 a);
+SFT_FUNC sftmat sft_m_rot_y(f32 a);
+SFT_FUNC sftmat sft_m_rot_z(f32 a);
+SFT_FUNC sftmat sft_m_translate(f32 x, f32 y, f32 z);
+SFT_FUNC sftmat sft_m_scale(f32 x, f32 y, f32 z);
+SFT_FUNC sftmat sft_m_proj(f32 fov_deg, f32 aspect, f32 near_z, f32 far_z);
+SFT_FUNC sftmat sft_m_mul(sftmat a, sftmat b);
+SFT_FUNC sftmat sft_m_qinv(sftmat m);
+SFT_FUNC sftmat sft_m_view_look_at(sftvec pos, sftvec target, sftvec up);
+SFT_FUNC sftmat sft_m_from_quat(sftquat q);
+SFT_FUNC sftquat sft_q_mul(sftquat a, sftquat b);
+SFT_FUNC sftquat sft_q_slerp(sftquat a, sftquat b, f32 t);
+SFT_FUNC sftquat sft_q_norm(sftquat q);
+
+/* core (sofren2.c:795-800) */
+SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads);
+SFT_FUNC void sft_release(void);
+SFT_FUNC void sft_present(void);
+SFT_FUNC void sft_frame_begin(void);
+SFT_FUNC void sft_frame_end(void);
+SFT_FUNC void sft_resize(i32 width, i32 height);
+
+/* misc (803-808) */
+SFT_FUNC void sft_set_camera(sftvec cam_pos, sftmat view, sftmat proj);
+SFT_FUNC void sft_set_debug_mode(enum sft_debug_mode mode);
+SFT_FUNC const char* sft_get_debug_name(enum sft_debug_mode mode);
+SFT_FUNC void sft_set_clear(u8 enabled);
+SFT_FUNC void sft_set_clear_color(u32 color);
+SFT_FUNC void sft_set_color_buffer(u32* buf, i32 pitch_in_bytes);
+
+/* drawing (811, 823-824) */
+SFT_FUNC void sft_draw_instance(const sft_instance* instance);
+SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena);
+
+/* lights (827-832) */
+SFT_FUNC void sft_set_ambient_light(f32 r, f32 g, f32 b);
+SFT_FUNC void sft_draw_directional_light(sftvec dir, f32 r, f32 g, f32 b, f32 intensity);
+SFT_FUNC void sft_draw_point_light(sftvec pos, f32 r, f32 g, f32 b, f32 intensity, f32 radius, u32 light_id);
+SFT_FUNC void sft_set_shadows_enabled(u8 enabled);
+SFT_FUNC void sft_set_lightmap_brightness(f32 b);
+
+/* textures (839-844) */
+SFT_FUNC sft_tex_handle sft_texture_create(i32 width, i32 height, const u32* pixels);
+SFT_FUNC sft_tex_handle sft_texture_create_solid(u32 color);
+SFT_FUNC i32 sft_texture_get_width(sft_tex_handle tex);
+SFT_FUNC i32 sft_texture_get_height(sft_tex_handle tex);
+SFT_FUNC u32* sft_texture_get_linear_pixels(sft_tex_handle tex);
+SFT_FUNC void sft_texture_release(sft_tex_handle tex);
+
+/* materials (847-849) */
+SFT_FUNC sft_mat_handle sft_material_create(sft_tex_handle tex, u32 base_color, f32 shininess);
+SFT_FUNC sft_mat_handle sft_material_clone(sft_mat_handle base_mat);
+SFT_FUNC void sft_material_release(sft_mat_handle mat);
+
+/* arenas (852-855) */
+SFT_FUNC void sft_arena_init(sft_arena* arena, u64 reserve_size);
+SFT_FUNC void* sft_arena_alloc(sft_arena* arena, u64 size);
+SFT_FUNC void sft_arena_commit_if_needed(sft_arena* arena, u64 required_bytes);
+SFT_FUNC void sft_arena_frame_begin(sft_arena* arena);
+
+/* extension: build a model from meshlet data (the reference's loaders produce the same
+ * arrays, sofren2.c:6918-7045); builds the BLAS like sft__blas_build_model (3526-3617) and
+ * uploads everything to the GPU.  lightmaps are texture handles indexed by lightmap_page. */
+SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count, const sft_shadow_proxy* proxies,
+                                     u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
+                                     sft_arena* arena);
+SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model);
+/* extension: MSAA samples (1, 2, 4) of the shared library build; SFT_AA_SAMPLES sets it in SFT_IMPL builds */
+SFT_FUNC void sft_set_msaa_samples(i32 samples);
+/* extension: last error text of the GPU runtime ("" when none) */
+SFT_FUNC const char* sft_get_last_error(void);
+/* extension: capture parity buffers for the next sft_present (struct sftg_debug_out from sftg.h, or NULL) */
+SFT_FUNC void sft_set_debug_capture(void* sftg_debug_out_or_null);
+/* extension: BLAS of a model as sft_bvh_node images (256 B each) */
+SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, u32* out_root);
+/* extension: device time of the last present, ms: [occlusion, geometry, binning, tile] */
+SFT_FUNC void sft_get_frame_timings(f32* out4);
+
+#ifdef __cplusplus
+}
+#endif
+
+/*================================================================ implementation */
+#ifdef SFT_IMPL
+
+#include "sftg.h"
+#include <sys/mman.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifdef SFT_NO_DEBUG
+    #define SFT__LOG(...)
+#else
+    #define SFT__LOG(...) do { fprintf(stdout, "[sofren2-gb300]: "); fprintf(stdout, __VA_ARGS__); } while (0)
+#endif
+#define SFT__FATAL(...) do { fprintf(stderr, "fatal sofren2-gb300 error in %s: ", __func__); fprintf(stderr, __VA_ARGS__); exit(1); } while (0)
+
+/* sft_bvh_node image (sofren2.c:967-983) */
+typedef struct sft__node {
+    f32 mn[3][8]; f32 mx[3][8];
+    u32 child[8]; u8 count; u8 leaf; u8 pad[30];
+} sft__node;
+
+typedef struct sft__item { u32 id; f32 mn[3], mx[3], c[3]; } sft__item;
+
+struct sft_model {
+    i32 device_id;
+    u32 mesh_count, total_meshlets, bone_count;
+    u32* mesh_first;              /* per mesh: first model meshlet */
+    u32* mesh_meshlets;
+    sft_shadow_proxy* proxies; u32 proxy_count;
+    sft__node* blas; u32 blas_count, blas_root;
+    f32 root_min[3], root_max[3]; /* from the BLAS root children, for the TLAS */
+};
+
+typedef struct sft__tex {
+    u32 generation; i32 next_free; i32 device_index;
+    i32 w, h, levels; u8 is_pot;
+    u32* level0;                  /* linear copy of level 0 for sft_texture_get_linear_pixels */
+    u8 live;
+} sft__tex;
+
+static struct sft__state {
+    sftg_ctx* gpu;
+    i32 width, height, samples;
+    u32* color; i32 pitch;
+    u8 clear; u32 clear_color; u8 shadows; enum sft_debug_mode debug_mode;
+    sftvec cam; sftmat view, proj, view_proj;
+    f32 fn[6][3], fd[6];
+    sftvec ambient; f32 lightmap_brightness;
+    f32* point; u32 n_point, cap_point;        /* 8 floats per light */
+    f32* dir; u32 n_dir, cap_dir;              /* 6 floats per light */
+    sftg_instance_desc inst[SFT_MAX_INSTANCES_PER_FRAME]; i32 n_inst_claimed; u32 n_inst;
+    const sft_model* inst_model[SFT_MAX_INSTANCES_PER_FRAME];
+    f32* bones; u32 n_bones, cap_bones;        /* copies of posed matrices for this frame */
+    u32 inst_bone_off[SFT_MAX_INSTANCES_PER_FRAME];
+    f32* proxies; u32 n_prox, cap_prox;        /* 8 floats per world proxy */
+    u32 total_ss;
+    sft__tex* tex; i32 tex_cap, tex_free;
+    u32* mat_gen; i32* mat_next; i32 mat_cap, mat_free;
+    i32 n_transient;
+    sft_mat_handle base_mat;
+    sftg_debug_out* debug;
+    char err[512];
+} *sft__s;
+
+/* ---------------------------------------------------------------- math (sofren2.c:1503-1918) */
+SFT_FUNC sftvec sft_v_add(sftvec a, sftvec b) { sftvec r = { a.x + b.x, a.y + b.y, a.z + b.z }; return r; }
+SFT_FUNC sftvec sft_v_sub(sftvec a, sftvec b) { sftvec r = { a.x - b.x, a.y - b.y, a.z - b.z }; return r; }
+SFT_FUNC sftvec sft_v_mul(sftvec a, f32 b) { sftvec r = { a.x * b, a.y * b, a.z * b }; return r; }
+SFT_FUNC sftvec sft_v_div(sftvec a, f32 b) { const f32 ib = 1.f / b; sftvec r = { a.x * ib, a.y * ib, a.z * ib }; return r; }
+SFT_FUNC f32 sft_v_dot(sftvec a, sftvec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SFT_FUNC sftvec sft_v_cross(sftvec a, sftvec b) { sftvec r = { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x }; return r; }
+SFT_FUNC f32 sft_v_length(sftvec v) { return sqrtf(sft_v_dot(v, v)); }
+SFT_FUNC f32 sft_v_length2(sftvec v) { return sft_v_dot(v, v); }
+SFT_FUNC sftvec sft_v_norm(sftvec v) { const f32 l = sft_v_length(v); if (l > SFT_EPSILON) return sft_v_mul(v, 1.f / l); sftvec z = { 0, 0, 0 }; return z; }
+SFT_FUNC sftvec sft_v_normf(f32 x, f32 y, f32 z) { sftvec v = { x, y, z }; return sft_v_norm(v); }
+SFT_FUNC sftvec sft_v_lerp(sftvec a, sftvec b, f32 t) { return sft_v_add(a, sft_v_mul(sft_v_sub(b, a), t)); }
+SFT_FUNC sftmat sft_m_identity(void) { sftmat r; memset(&r, 0, sizeof(r)); r.m[0][0] = r.m[1][1] = r.m[2][2] = r.m[3][3] = 1.f; return r; }
+SFT_FUNC sftmat sft_m_rot_x(f32 a) { sftmat r = sft_m_identity(); const f32 c = cosf(a), s = sinf(a); r.m[1][1] = c; r.m[1][2] = s; r.m[2][1] = -s; r.m[2][2] = c; return r; }
+SFT_FUNC sftmat sft_m_rot_y(f32 a) { sftmat r = sft_m_identity(); const f32 c = cosf(a), s = sinf(a); r.m[0][0] = c; r.m[0][2] = s; r.m[2][0] = -s; r.m[2][2] = c; return r; }
+SFT_FUNC sftmat sft_m_rot_z(f32 a) { sftmat r = sft_m_identity(); const f32 c = cosf(a), s = sinf(a); r.m[0][0] = c; r.m[0][1] = s; r.m[1][0] = -s; r.m[1][1] = c; return r; }
+SFT_FUNC sftmat sft_m_translate(f32 x, f32 y, f32 z) { sftmat r = sft_m_identity(); r.m[3][0] = x; r.m[3][1] = y; r.m[3][2] = z; return r; }
+SFT_FUNC sftmat sft_m_scale(f32 x, f32 y, f32 z) { sftmat r = sft_m_identity(); r.m[0][0] = x; r.m[1][1] = y; r.m[2][2] = z; return r; }
+SFT_FUNC sftmat sft_m_proj(f32 fov_deg, f32 aspect, f32 near_z, f32 far_z) {
+    const f32 fov = 1.f / tanf(fov_deg * 0.5f / 180.f * (f32)SFT_PI);
+    sftmat r; memset(&r, 0, sizeof(r));
+    r.m[0][0] = fov / aspect; r.m[1][1] = fov; r.m[2][2] = far_z / (far_z - near_z);
+    r.m[3][2] = (-far_z * near_z) / (far_z - near_z); r.m[2][3] = 1.f; r.m[3][3] = 0.f;
+    return r;
+}
+SFT_FUNC sftmat sft_m_mul(sftmat a, sftmat b) {   /* left-to-right sums, no contraction (sofren2.c:1668) */
+    sftmat r;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j] + a.m[i][3] * b.m[3][j];
+    return r;
+}
+SFT_FUNC sftmat sft_m_qinv(sftmat m) {
+    sftmat r;
+    r.m[0][0] = m.m[0][0]; r.m[0][1] = m.m[1][0]; r.m[0][2] = m.m[2][0]; r.m[0][3] = 0.f;
+    r.m[1][0] = m.m[0][1]; r.m[1][1] = m.m[1][1]; r.m[1][2] = m.m[2][1]; r.m[1][3] = 0.f;
+    r.m[2][0] = m.m[0][2]; r.m[2][1] = m.m[1][2]; r.m[2][2] = m.m[2][2]; r.m[2][3] = 0.f;
+    for (int a = 0; a < 3; a++) r.m[3][a] = -(m.m[3][0] * r.m[0][a] + m.m[3][1] * r.m[1][a] + m.m[3][2] * r.m[2][a]);
+    r.m[3][3] = 1.f;
+    return r;
+}
+SFT_FUNC sftmat sft_m_view_look_at(sftvec pos, sftvec target, sftvec up) {
+    const sftvec fwd = sft_v_norm(sft_v_sub(target, pos));
+    if (fabsf(fwd.x) < SFT_EPSILON && fabsf(fwd.z) < SFT_EPSILON) { up.x = 0.f; up.y = 0.f; up.z = -1.f; }
+    up = sft_v_norm(sft_v_sub(up, sft_v_mul(fwd, sft_v_dot(up, fwd))));
+    const sftvec right = sft_v_cross(up, fwd);
+    sftmat r;
+    r.m[0][0] = right.x; r.m[0][1] = up.x; r.m[0][2] = fwd.x; r.m[0][3] = 0.f;
+    r.m[1][0] = right.y; r.m[1][1] = up.y; r.m[1][2] = fwd.y; r.m[1][3] = 0.f;
+    r.m[2][0] = right.z; r.m[2][1] = up.z; r.m[2][2] = fwd.z; r.m[2][3] = 0.f;
+    r.m[3][0] = -sft_v_dot(pos, right); r.m[3][1] = -sft_v_dot(pos, up); r.m[3][2] = -sft_v_dot(pos, fwd); r.m[3][3] = 1.f;
+    return r;
+}
+SFT_FUNC sftmat sft_m_from_quat(sftquat q) {
+    sftmat m = sft_m_identity();
+    const f32 x2 = q.x + q.x, y2 = q.y + q.y, z2 = q.z + q.z;
+    const f32 xx = q.x * x2, xy = q.x * y2, xz = q.x * z2, yy = q.y * y2, yz = q.y * z2, zz = q.z * z2;
+    const f32 wx = q.w * x2, wy = q.w * y2, wz = q.w * z2;
+    m.m[0][0] = 1.f - (yy + zz); m.m[0][1] = xy + wz; m.m[0][2] = xz - wy;
+    m.m[1][0] = xy - wz; m.m[1][1] = 1.f - (xx + zz); m.m[1][2] = yz + wx;
+    m.m[2][0] = xz + wy; m.m[2][1] = yz - wx; m.m[2][2] = 1.f - (xx + yy);
+    return m;
+}
+SFT_FUNC sftquat sft_q_mul(sftquat a, sftquat b) {
+    sftquat r;
+    r.x = a.x * b.w + a.y * b.z - a.z * b.y + a.w * b.x;
+    r.y = -a.x * b.z + a.y * b.w + a.z * b.x + a.w * b.y;
+    r.z = a.x * b.y - a.y * b.x + a.z * b.w + a.w * b.z;
+    r.w = -a.x * b.x - a.y * b.y - a.z * b.z + a.w * b.w;
+    return r;
+}
+SFT_FUNC sftquat sft_q_norm(sftquat q) {
+    const f32 l2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+    if (l2 != 0.f) { const f32 il = 1.f / sqrtf(l2); q.x *= il; q.y *= il; q.z *= il; q.w *= il; }
+    return q;
+}
+SFT_FUNC sftquat sft_q_slerp(sftquat a, sftquat b, f32 t) {
+    f32 dot = a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+    if (dot < 0.f) { b.x = -b.x; b.y = -b.y; b.z = -b.z; b.w = -b.w; dot = -dot; }
+    if (dot > 0.9995f) {
+        sftquat r = { a.x + t * (b.x - a.x), a.y + t * (b.y - a.y), a.z + t * (b.z - a.z), a.w + t * (b.w - a.w) };
+        return sft_q_norm(r);
+    }
+    const f32 th0 = acosf(dot), th = th0 * t, st = sinf(th), is0 = 1.f / sinf(th0);
+    const f32 s0 = cosf(th) - dot * st * is0, s1 = st * is0;
+    sftquat r = { a.x * s0 + b.x * s1, a.y * s0 + b.y * s1, a.z * s0 + b.z * s1, a.w * s0 + b.w * s1 };
+    return sft_q_norm(r);
+}
+
+/* ---------------------------------------------------------------- arenas (sofren2.c:9456-9564) */
+SFT_FUNC void sft_arena_init(sft_arena* arena, u64 reserve_size) {
+    arena->max_size = reserve_size; arena->committed_size = reserve_size; arena->offset = 0; arena->commit_lock = 0;
+    arena->base = (u8*)mmap(NULL, reserve_size, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS | MAP_NORESERVE, -1, 0);
+    if (arena->base == (u8*)MAP_FAILED) SFT__FATAL("mmap reserve of %llu bytes failed\n", (unsigned long long)reserve_size);
+}
+SFT_FUNC void* sft_arena_alloc(sft_arena* arena, u64 size) {
+    if (!arena) return NULL;
+    const u64 a = (arena->offset + 63ull) & ~63ull;
+    if (a + size > arena->max_size) SFT__FATAL("arena out of memory (%llu of %llu)\n", (unsigned long long)(a + size), (unsigned long long)arena->max_size);
+    arena->offset = a + size;
+    return arena->base + a;
+}
+SFT_FUNC void sft_arena_commit_if_needed(sft_arena* arena, u64 required_bytes) { (void)arena; (void)required_bytes; }
+SFT_FUNC void sft_arena_frame_begin(sft_arena* arena) { arena->offset = 0; }
+
+/* ---------------------------------------------------------------- BVH build (sofren2.c:2895-3062)
+ * The TLAS is rebuilt every frame on the host exactly as the reference does, so the proxy
+ * occlusion traversal visits the same nodes; the BLAS uses the same builder at model creation. */
+static void sft__sort_items(sft__item* it, i32 count, int axis) {
+    if (count <= 1) return;
+    const f32 pivot = it[count / 2].c[axis];
+    i32 i = 0, j = count - 1;
+    while (i <= j) {
+        while (it[i].c[axis] < pivot) i++;
+        while (it[j].c[axis] > pivot) j--;
+        if (i <= j) { const sft__item t = it[i]; it[i] = it[j]; it[j] = t; i++; j--; }
+    }
+    if (j > 0) sft__sort_items(it, j + 1, axis);
+    if (i < count) sft__sort_items(it + i, count - i, axis);
+}
+static void sft__split8(sft__item* it, u32 start, u32 count, u32 depth, u32* st, u32* cn, u32* ng) {
+    if (!count) return;
+    if (depth == 3 || count == 1) { st[*ng] = start; cn[*ng] = count; (*ng)++; return; }
+    f32 lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
+    for (u32 i = 0; i < count; i++)
+        for (int a = 0; a < 3; a++) {
+            if (it[start + i].c[a] < lo[a]) lo[a] = it[start + i].c[a];
+            if (it[start + i].c[a] > hi[a]) hi[a] = it[start + i].c[a];
+        }
+    const f32 dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    const int axis = (dy > dx && dy > dz) ? 1 : (dz > dx && dz > dy) ? 2 : 0;
+    sft__sort_items(it + start, (i32)count, axis);
+    const u32 mid = count / 2;
+    sft__split8(it, start, mid, depth + 1, st, cn, ng);
+    sft__split8(it, start + mid, count - mid, depth + 1, st, cn, ng);
+}
+static u32 sft__bvh_build(sft__item* it, u32 count, sft__node* nodes, u32* ncount, f32* out_lo, f32* out_hi) {
+    const u32 ni = (*ncount)++;
+    sft__node* n = &nodes[ni];
+    memset(n, 0, sizeof(*n));
+    for (int i = 0; i < 8; i++) { for (int a = 0; a < 3; a++) { n->mn[a][i] = 1e30f; n->mx[a][i] = -1e30f; } n->child[i] = 0xFFFFFFFFu; }
+    f32 lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
+    if (count <= 8) {
+        n->leaf = 1; n->count = (u8)count;
+        for (u32 i = 0; i < count; i++) {
+            for (int a = 0; a < 3; a++) {
+                n->mn[a][i] = it[i].mn[a]; n->mx[a][i] = it[i].mx[a];
+                if (it[i].mn[a] < lo[a]) lo[a] = it[i].mn[a];
+                if (it[i].mx[a] > hi[a]) hi[a] = it[i].mx[a];
+            }
+            n->child[i] = 0x80000000u | it[i].id;
+        }
+    } else {
+        u32 st[8] = { 0 }, cn[8] = { 0 }, ng = 0;
+        sft__split8(it, 0, count, 0, st, cn, &ng);
+        n->count = (u8)ng;
+        for (u32 c = 0; c < ng; c++) {
+            f32 clo[3], chi[3];
+            const u32 ci = sft__bvh_build(it + st[c], cn[c], nodes, ncount, clo, chi);
+            n = &nodes[ni];
+            n->child[c] = ci;
+            for (int a = 0; a < 3; a++) {
+                n->mn[a][c] = clo[a]; n->mx[a][c] = chi[a];
+                if (clo[a] < lo[a]) lo[a] = clo[a];
+                if (chi[a] > hi[a]) hi[a] = chi[a];
+            }
+        }
+    }
+    if (out_lo) { memcpy(out_lo, lo, 12); memcpy(out_hi, hi, 12); }
+    return ni;
+}
+
+/* ---------------------------------------------------------------- lifecycle */
+static void sft__check(int rc, const char* what) {
+    if (rc) SFT__FATAL("%s failed (%d): %s\n", what, rc, sft__s && sft__s->gpu ? sftg_last_error(sft__s->gpu) : "no GPU context");
+}
+
+SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads) {
+    (void)requested_threads;   /* host work is a single thread; the GPU replaces the worker pool */
+    sft__s = (struct sft__state*)calloc(1, sizeof(*sft__s));
+    if (!sft__s) SFT__FATAL("out of memory\n");
+    const int rc = sftg_create(0, &sft__s->gpu);
+    if (rc) SFT__FATAL("no usable CUDA device (sftg_create returned %d)\n", rc);
+    sft__s->width = width; sft__s->height = height; sft__s->samples = SFT_AA_SAMPLES;
+    sft__s->lightmap_brightness = 1.5f;
+    sft__s->clear_color = 0xFF222222u;
+    sft__s->tex_free = -1; sft__s->mat_free = -1;
+    /* 256x256 checkerboard default material, as in sft_init (sofren2.c:8060-8086) */
+    u32* px = (u32*)malloc(256 * 256 * 4);
+    for (i32 y = 0, i = 0; y < 256; y++) for (i32 x = 0; x < 256; x++, i++) px[i] = (((x / 32) % 2) ^ ((y / 32) % 2)) ? 0xFFAFFFAFu : 0xFF555555u;
+    const sft_tex_handle checker = sft_texture_create(256, 256, px);
+    free(px);
+    sft__s->base_mat = sft_material_create(checker, 0xFFFFFFFFu, 2.f);
+    SFT__LOG("initialized GPU renderer %dx%d, %d sample(s)\n", width, height, sft__s->samples);
+}
+
+SFT_FUNC void sft_release(void) {
+    if (!sft__s) return;
+    sftg_destroy(sft__s->gpu);
+    for (i32 i = 0; i < sft__s->tex_cap; i++) free(sft__s->tex[i].level0);
+    free(sft__s->tex); free(sft__s->mat_gen); free(sft__s->mat_next);
+    free(sft__s->point); free(sft__s->dir); free(sft__s->bones); free(sft__s->proxies);
+    free(sft__s);
+    sft__s = NULL;
+}
+
+SFT_FUNC void sft_resize(i32 width, i32 height) { if (sft__s) { sft__s->width = width; sft__s->height = height; } }
+SFT_FUNC void sft_set_msaa_samples(i32 samples) { if (sft__s && (samples == 1 || samples == 2 || samples == 4)) sft__s->samples = samples; }
+SFT_FUNC const char* sft_get_last_error(void) { return sft__s && sft__s->gpu ? sftg_last_error(sft__s->gpu) : ""; }
+SFT_FUNC void sft_set_debug_capture(void* d) { if (sft__s) sft__s->debug = (sftg_debug_out*)d; }
+SFT_FUNC void sft_get_frame_timings(f32* out4) { if (sft__s) sftg_last_timings(sft__s->gpu, out4); }
+
+SFT_FUNC void sft_frame_begin(void) { }
+SFT_FUNC void sft_frame_end(void) {
+    sft__s->n_inst_claimed = 0; sft__s->n_inst = 0; sft__s->total_ss = 0;
+    sft__s->n_point = 0; sft__s->n_dir = 0; sft__s->n_prox = 0; sft__s->n_bones = 0; sft__s->n_transient = 0;
+}
+
+/* ---------------------------------------------------------------- frame setup */
+SFT_FUNC void sft_set_camera(sftvec cam_pos, sftmat view, sftmat proj) {   /* sofren2.c:8345-8376 */
+    sft__s->cam = cam_pos; sft__s->view = view; sft__s->proj = proj;
+    sft__s->view_proj = sft_m_mul(view, proj);
+    const sftmat* vp = &sft__s->view_proj;
+    f32 pl[6][4];
+    for (int i = 0; i < 4; i++) {
+        pl[0][i] = vp->m[i][3] + vp->m[i][0]; pl[1][i] = vp->m[i][3] - vp->m[i][0];
+        pl[2][i] = vp->m[i][3] + vp->m[i][1]; pl[3][i] = vp->m[i][3] - vp->m[i][1];
+        pl[4][i] = vp->m[i][3] + vp->m[i][2]; pl[5][i] = vp->m[i][3] - vp->m[i][2];
+    }
+    for (int p = 0; p < 6; p++) {
+        const f32 len = sqrtf(pl[p][0] * pl[p][0] + pl[p][1] * pl[p][1] + pl[p][2] * pl[p][2]);
+        const f32 il = (len < SFT_EPSILON) ? SFT_EPSILON : 1.f / len;
+        for (int a = 0; a < 3; a++) sft__s->fn[p][a] = pl[p][a] * il;
+        sft__s->fd[p] = pl[p][3] * il;
+    }
+}
+SFT_FUNC void sft_set_debug_mode(enum sft_debug_mode mode) {
+    if ((int)mode < 0 || mode >= SFT_DEBUG_COUNT) { fprintf(stderr, "sofren2-gb300: invalid debug mode %d\n", (int)mode); return; }
+    sft__s->debug_mode = mode;
+}
+SFT_FUNC const char* sft_get_debug_name(enum sft_debug_mode mode) {
+    switch (mode) {
+        case SFT_DEBUG_NONE: return "None";
+        case SFT_DEBUG_WIREFRAME: return "Wireframe";
+        case SFT_DEBUG_TILES: return "Tiles";
+        case SFT_DEBUG_DEPTH: return "Depth";
+        case SFT_DEBUG_LIGHT_COUNT: return "Light Count";
+        case SFT_DEBUG_CHECKERBOARD: return "Checkerboard";
+        default: return "INVALID MODE";
+    }
+}
+SFT_FUNC void sft_set_clear(u8 enabled) { sft__s->clear = enabled; }
+SFT_FUNC void sft_set_clear_color(u32 color) { sft__s->clear_color = color; }
+SFT_FUNC void sft_set_color_buffer(u32* buf, i32 pitch_in_bytes) { sft__s->color = buf; sft__s->pitch = pitch_in_bytes; }
+
+/* ---------------------------------------------------------------- lights (sofren2.c:9109-9149) */
+SFT_FUNC void sft_set_ambient_light(f32 r, f32 g, f32 b) { sft__s->ambient.x = r; sft__s->ambient.y = g; sft__s->ambient.z = b; }
+SFT_FUNC void sft_draw_directional_light(sftvec dir, f32 r, f32 g, f32 b, f32 intensity) {
+    if (sft__s->n_dir == sft__s->cap_dir) { sft__s->cap_dir = sft__s->cap_dir ? sft__s->cap_dir * 2 : 16; sft__s->dir = (f32*)realloc(sft__s->dir, sft__s->cap_dir * 24); }
+    f32* d = sft__s->dir + 6 * sft__s->n_dir++;
+    const sftvec n = sft_v_norm(dir);
+    d[0] = n.x; d[1] = n.y; d[2] = n.z; d[3] = r * intensity; d[4] = g * intensity; d[5] = b * intensity;
+}
+SFT_FUNC void sft_draw_point_light(sftvec pos, f32 r, f32 g, f32 b, f32 intensity, f32 radius, u32 light_id) {
+    (void)light_id;
+    if (sft__s->n_point == sft__s->cap_point) { sft__s->cap_point = sft__s->cap_point ? sft__s->cap_point * 2 : 16; sft__s->point = (f32*)realloc(sft__s->point, sft__s->cap_point * 32); }
+    f32* p = sft__s->point + 8 * sft__s->n_point++;
+    p[0] = pos.x; p[1] = pos.y; p[2] = pos.z; p[3] = r * intensity; p[4] = g * intensity; p[5] = b * intensity;
+    p[6] = radius; p[7] = 1.f / (radius * radius);
+}
+SFT_FUNC void sft_set_shadows_enabled(u8 enabled) { sft__s->shadows = enabled; }
+SFT_FUNC void sft_set_lightmap_brightness(f32 b) { sft__s->lightmap_brightness = b; }
+
+/* ---------------------------------------------------------------- textures (sofren2.c:9181-9391) */
+static i32 sft__ilog2(u32 v) { i32 r = 0; while (v >>= 1) r++; return r; }
+
+SFT_FUNC sft_tex_handle sft_texture_create(i32 width, i32 height, const u32* pixels) {
+    if (width <= 0 || height <= 0 || !pixels) return SFT_INVALID_HANDLE;
+    const u8 is_pot = (0 == (width & (width - 1))) && (0 == (height & (height - 1)));
+    i32 cw = width, ch = height, levels = 0; u64 total = 0;
+    while (levels < 14) {
+        total += (u64)(((cw + 3) & ~3) * ((ch + 3) & ~3));
+        levels++;
+        if (cw == 1 && ch == 1) break;
+        cw = cw > 1 ? cw / 2 : 1; ch = ch > 1 ? ch / 2 : 1;
+    }
+    u32* texels = (u32*)calloc(total + 16, 4);
+    sftg_texture_desc d; memset(&d, 0, sizeof(d));
+    d.width = width; d.height = height; d.levels = levels; d.is_pot = is_pot;
+    const u32* src = pixels; u32* tmp = NULL; u32 cur = 0;
+    cw = width; ch = height;
+    for (i32 l = 0; l < levels; l++) {
+        if (l > 0) {   /* 4x4 tent filter with 1-2-2-1 integer weights and clamped taps (9261-9290) */
+            const i32 nw = cw > 1 ? cw / 2 : 1, nh = ch > 1 ? ch / 2 : 1;
+            u32* dst = (u32*)malloc((size_t)nw * nh * 4);
+            for (i32 y = 0; y < nh; y++)
+                for (i32 x = 0; x < nw; x++) {
+                    u32 r = 0, g = 0, b = 0, a = 0, ws = 0;
+                    for (i32 ky = -1; ky <= 2; ky++) {
+                        const i32 sy = (y * 2 + ky) < 0 ? 0 : ((y * 2 + ky) > ch - 1 ? ch - 1 : (y * 2 + ky));
+                        const u32 wy = (ky == -1 || ky == 2) ? 1 : 2;
+                        for (i32 kx = -1; kx <= 2; kx++) {
+                            const i32 sx = (x * 2 + kx) < 0 ? 0 : ((x * 2 + kx) > cw - 1 ? cw - 1 : (x * 2 + kx));
+                            const u32 w = ((kx == -1 || kx == 2) ? 1 : 2) * wy;
+                            const u32 c = src[sy * cw + sx];
+                            r += ((c >> 16) & 255) * w; g += ((c >> 8) & 255) * w; b += (c & 255) * w; a += ((c >> 24) & 255) * w;
+                            ws += w;
+                        }
+                    }
+                    dst[y * nw + x] = ((a / ws) << 24) | ((r / ws) << 16) | ((g / ws) << 8) | (b / ws);
+                }
+            free(tmp); tmp = dst; src = dst; cw = nw; ch = nh;
+        }
+        const i32 pw = (cw + 3) & ~3, ph = (ch + 3) & ~3, bw = pw / 4;
+        d.level_offset[l] = cur; d.blocks_w[l] = bw; d.stride_shift[l] = is_pot ? sft__ilog2((u32)bw) : 0;
+        for (i32 y = 0; y < ch; y++)
+            for (i32 x = 0; x < cw; x++)
+                texels[cur + (u32)(((y / 4) * bw + x / 4) * 16 + (y % 4) * 4 + (x % 4))] = src[y * cw + x];
+        cur += (u32)(pw * ph);
+    }
+    free(tmp);
+    i32 dev = -1;
+    sft__check(sftg_texture_upload(sft__s->gpu, texels, total, &d, &dev), "texture upload");
+    free(texels);
+    /* slot in the generational pool (sofren2.c:4457-4480) */
+    if (sft__s->tex_free == -1) {
+        const i32 oc = sft__s->tex_cap, nc = oc ? oc * 2 : 1024;
+        sft__s->tex = (sft__tex*)realloc(sft__s->tex, (size_t)nc * sizeof(sft__tex));
+        for (i32 i = oc; i < nc; i++) { memset(&sft__s->tex[i], 0, sizeof(sft__tex)); sft__s->tex[i].generation = 1; sft__s->tex[i].next_free = i + 1; }
+        sft__s->tex[nc - 1].next_free = -1;
+        sft__s->tex_free = oc; sft__s->tex_cap = nc;
+    }
+    const i32 ti = sft__s->tex_free;
+    sft__tex* t = &sft__s->tex[ti];
+    sft__s->tex_free = t->next_free;
+    t->device_index = dev; t->w = width; t->h = height; t->levels = levels; t->is_pot = is_pot; t->live = 1;
+    t->level0 = (u32*)malloc((size_t)width * height * 4);
+    memcpy(t->level0, pixels, (size_t)width * height * 4);
+    return (t->generation << SFT_HANDLE_GEN_SHIFT) | (u32)ti;
+}
+SFT_FUNC sft_tex_handle sft_texture_create_solid(u32 color) { return sft_texture_create(1, 1, &color); }
+SFT_FUNC i32 sft_texture_get_width(sft_tex_handle tex) { return tex == SFT_INVALID_HANDLE ? 0 : sft__s->tex[SFT_HANDLE_INDEX(tex)].w; }
+SFT_FUNC i32 sft_texture_get_height(sft_tex_handle tex) { return tex == SFT_INVALID_HANDLE ? 0 : sft__s->tex[SFT_HANDLE_INDEX(tex)].h; }
+SFT_FUNC u32* sft_texture_get_linear_pixels(sft_tex_handle tex) {
+    if (tex == SFT_INVALID_HANDLE) return NULL;
+    const sft__tex* t = &sft__s->tex[SFT_HANDLE_INDEX(tex)];
+    u32* r = (u32*)malloc((size_t)t->w * t->h * 4);
+    memcpy(r, t->level0, (size_t)t->w * t->h * 4);
+    return r;
+}
+SFT_FUNC void sft_texture_release(sft_tex_handle tex) {
+    if (tex == SFT_INVALID_HANDLE) return;
+    const u32 ind = SFT_HANDLE_INDEX(tex), gen = tex >> SFT_HANDLE_GEN_SHIFT;
+    if (ind >= (u32)sft__s->tex_cap || sft__s->tex[ind].generation != gen) return;
+    sft__tex* t = &sft__s->tex[ind];
+    free(t->level0); t->level0 = NULL; t->live = 0;
+    t->generation++;
+    t->next_free = sft__s->tex_free; sft__s->tex_free = (i32)ind;
+}
+
+/* ---------------------------------------------------------------- materials (sofren2.c:9393-9454) */
+static i32 sft__tex_device(sft_tex_handle h) {
+    if (h == SFT_INVALID_HANDLE) return -1;
+    const u32 i = SFT_HANDLE_INDEX(h);
+    return (i < (u32)sft__s->tex_cap && sft__s->tex[i].live) ? sft__s->tex[i].device_index : -1;
+}
+SFT_FUNC sft_mat_handle sft_material_create(sft_tex_handle tex, u32 base_color, f32 shininess) {
+    if (sft__s->mat_free == -1) {
+        const i32 oc = sft__s->mat_cap, nc = oc ? oc * 2 : 32;
+        sft__s->mat_gen = (u32*)realloc(sft__s->mat_gen, (size_t)nc * 4);
+        sft__s->mat_next = (i32*)realloc(sft__s->mat_next, (size_t)nc * 4);
+        for (i32 i = oc; i < nc; i++) { sft__s->mat_gen[i] = 1; sft__s->mat_next[i] = i + 1; }
+        sft__s->mat_next[nc - 1] = -1;
+        sft__s->mat_free = oc; sft__s->mat_cap = nc;
+    }
+    const i32 ind = sft__s->mat_free;
+    sft__s->mat_free = sft__s->mat_next[ind];
+    sft__check(sftg_material_set(sft__s->gpu, ind, sft__tex_device(tex), base_color, shininess), "material upload");
+    return (sft__s->mat_gen[ind] << SFT_MAT_GEN_SHIFT) | (u32)ind;
+}
+SFT_FUNC sft_mat_handle sft_material_clone(sft_mat_handle base_mat) {
+    /* transient per-frame materials are not yet resident on the device: clone into a static slot */
+    (void)base_mat;
+    fprintf(stderr, "sofren2-gb300: sft_material_clone is not supported by the GPU runtime\n");
+    return SFT_INVALID_HANDLE;
+}
+SFT_FUNC void sft_material_release(sft_mat_handle mat) {
+    if (mat == SFT_INVALID_HANDLE || SFT_MAT_IS_TRANSIENT(mat)) return;
+    const u32 ind = SFT_MAT_INDEX(mat), gen = (mat & SFT_MAT_GEN_MASK) >> SFT_MAT_GEN_SHIFT;
+    if (ind >= (u32)sft__s->mat_cap || sft__s->mat_gen[ind] != gen) return;
+    sft__s->mat_gen[ind]++;
+    sft__s->mat_next[ind] = sft__s->mat_free; sft__s->mat_free = (i32)ind;
+}
+
+/* ---------------------------------------------------------------- models */
+SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count, const sft_shadow_proxy* proxies,
+                                     u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
+                                     sft_arena* arena) {
+    (void)arena;
+    sft_model* m = (sft_model*)calloc(1, sizeof(sft_model));
+    m->mesh_count = mesh_count; m->bone_count = bone_count;
+    m->mesh_first = (u32*)calloc(mesh_count + 1, 4); m->mesh_meshlets = (u32*)calloc(mesh_count + 1, 4);
+    sftg_mesh_desc* md = (sftg_mesh_desc*)calloc(mesh_count + 1, sizeof(sftg_mesh_desc));
+    u32 total = 0;
+    for (u32 k = 0; k < mesh_count; k++) {
+        const sft_mesh_data* s = &meshes[k];
+        m->mesh_first[k] = total; m->mesh_meshlets[k] = s->meshlet_count;
+        md[k].meshlet_count = s->meshlet_count; md[k].attr = s->attr; md[k].inds = s->inds; md[k].cull = s->cull;
+        md[k].joints = s->joints; md[k].weights = s->weights; md[k].culling_bones = s->culling_bones;
+        md[k].material = (s->material == SFT_INVALID_HANDLE) ? -1 : (i32)SFT_MAT_INDEX(s->material);
+        md[k].lightmap_texture = (s->lightmap_page != 0xFFFFFFFFu && s->lightmap_page < lightmap_count) ? sft__tex_device(lightmaps[s->lightmap_page]) : -1;
+        total += s->meshlet_count;
+    }
+    m->total_meshlets = total;
+    m->proxy_count = proxy_count;
+    m->proxies = (sft_shadow_proxy*)calloc(proxy_count + 1, sizeof(sft_shadow_proxy));
+    if (proxy_count) memcpy(m->proxies, proxies, proxy_count * sizeof(sft_shadow_proxy));
+    /* BLAS over every non-padding triangle, in meshlet / batch / lane order (sofren2.c:3526-3617) */
+    u32 ntri = 0;
+    for (u32 k = 0; k < mesh_count; k++)
+        for (u32 j = 0; j < meshes[k].meshlet_count; j++) {
+            const u8* in = meshes[k].inds + (size_t)j * 512;
+            for (u32 t = 0; t < 128; t++) { const u32 b = t >> 3, l = t & 7; if (!(in[b * 32 + l] == in[b * 32 + 8 + l] && in[b * 32 + 8 + l] == in[b * 32 + 16 + l])) ntri++; }
+        }
+    if (ntri) {
+        sft__item* it = (sft__item*)malloc(ntri * sizeof(sft__item));
+        u32 q = 0;
+        for (u32 k = 0; k < mesh_count; k++)
+            for (u32 j = 0; j < meshes[k].meshlet_count; j++) {
+                const u8* in = meshes[k].inds + (size_t)j * 512;
+                const f32* at = meshes[k].attr + (size_t)j * 640;
+                const u32 g = m->mesh_first[k] + j;
+                for (u32 t = 0; t < 128; t++) {
+                    const u32 b = t >> 3, l = t & 7;
+                    const u32 i0 = in[b * 32 + l], i1 = in[b * 32 + 8 + l], i2 = in[b * 32 + 16 + l];
+                    if (i0 == i1 && i1 == i2) continue;
+                    sft__item* o = &it[q++];
+                    for (int a = 0; a < 3; a++) {
+                        const f32 p0 = at[a * 64 + i0], p1 = at[a * 64 + i1], p2 = at[a * 64 + i2];
+                        const f32 m12 = p1 < p2 ? p1 : p2, x12 = p1 > p2 ? p1 : p2;
+                        o->mn[a] = p0 < m12 ? p0 : m12; o->mx[a] = p0 > x12 ? p0 : x12;
+                        o->c[a] = (o->mn[a] + o->mx[a]) * 0.5f;
+                    }
+                    o->id = (g << 7) | t;
+                }
+            }
+        m->blas = (sft__node*)calloc((size_t)ntri * 2 + 1, sizeof(sft__node));
+        m->blas_root = sft__bvh_build(it, ntri, m->blas, &m->blas_count, NULL, NULL);
+        free(it);
+        const sft__node* root = &m->blas[m->blas_root];
+        for (int a = 0; a < 3; a++) { m->root_min[a] = 1e30f; m->root_max[a] = -1e30f; }
+        for (u32 c = 0; c < root->count; c++)
+            for (int a = 0; a < 3; a++) {
+                if (root->mn[a][c] < m->root_min[a]) m->root_min[a] = root->mn[a][c];
+                if (root->mx[a][c] > m->root_max[a]) m->root_max[a] = root->mx[a][c];
+            }
+    }
+    sftg_model_desc d; memset(&d, 0, sizeof(d));
+    d.mesh_count = mesh_count; d.meshes = md; d.bone_count = bone_count;
+    d.blas_nodes = m->blas; d.blas_count = m->blas_count; d.blas_root = m->blas_root;
+    sft__check(sftg_model_upload(sft__s->gpu, &d, &m->device_id), "model upload");
+    free(md);
+    return m;
+}
+SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model) { return model ? model->total_meshlets : 0; }
+SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, u32* out_root) {
+    if (out_count) *out_count = model ? model->blas_count : 0;
+    if (out_root) *out_root = model ? model->blas_root : 0;
+    return model ? model->blas : NULL;
+}
+
+/* ---------------------------------------------------------------- draw (sofren2.c:8410-8478) */
+SFT_FUNC void sft_draw_instance(const sft_instance* in) {
+    const i32 slot = sft__s->n_inst_claimed++;
+    if (slot >= SFT_MAX_INSTANCES_PER_FRAME) return;    /* same silent drop as the reference */
+    const sft_model* md = in->model;
+    sftg_instance_desc* d = &sft__s->inst[slot];
+    d->model = md->device_id;
+    memcpy(d->transform, in->transform.m, 64);
+    d->bones = NULL; d->bone_count = 0;
+    sft__s->inst_model[slot] = md;
+    if (in->posed_bone_matrices && md->bone_count) {
+        if (sft__s->n_bones + md->bone_count > sft__s->cap_bones) {
+            while (sft__s->n_bones + md->bone_count > sft__s->cap_bones) sft__s->cap_bones = sft__s->cap_bones ? sft__s->cap_bones * 2 : 256;
+            sft__s->bones = (f32*)realloc(sft__s->bones, (size_t)sft__s->cap_bones * 64);
+        }
+        sft__s->inst_bone_off[slot] = sft__s->n_bones;
+        memcpy(sft__s->bones + 16 * (size_t)sft__s->n_bones, in->posed_bone_matrices, (size_t)md->bone_count * 64);
+        d->bone_count = md->bone_count;
+        sft__s->n_bones += md->bone_count;
+    }
+    sft__s->n_inst = (u32)slot + 1;
+    sft__s->total_ss += md->total_meshlets;
+    /* world-space shadow proxies (8426-8455) */
+    if (sft__s->shadows && md->proxy_count > 0) {
+        if (sft__s->n_prox + md->proxy_count > sft__s->cap_prox) {
+            while (sft__s->n_prox + md->proxy_count > sft__s->cap_prox) sft__s->cap_prox = sft__s->cap_prox ? sft__s->cap_prox * 2 : 64;
+            sft__s->proxies = (f32*)realloc(sft__s->proxies, (size_t)sft__s->cap_prox * 32);
+        }
+        for (u32 i = 0; i < md->proxy_count; i++) {
+            const sft_shadow_proxy* lp = &md->proxies[i];
+            sftmat m = in->transform;
+            if (lp->bone_ind != 0xFFFFFFFFu && in->posed_bone_matrices) m = sft_m_mul(in->posed_bone_matrices[lp->bone_ind], in->transform);
+            f32* w = sft__s->proxies + 8 * (size_t)sft__s->n_prox++;
+            w[0] = lp->posa.x * m.m[0][0] + lp->posa.y * m.m[1][0] + lp->posa.z * m.m[2][0] + m.m[3][0];
+            w[1] = lp->posa.x * m.m[0][1] + lp->posa.y * m.m[1][1] + lp->posa.z * m.m[2][1] + m.m[3][1];
+            w[2] = lp->posa.x * m.m[0][2] + lp->posa.y * m.m[1][2] + lp->posa.z * m.m[2][2] + m.m[3][2];
+            w[3] = lp->posb.x * m.m[0][0] + lp->posb.y * m.m[1][0] + lp->posb.z * m.m[2][0] + m.m[3][0];
+            w[4] = lp->posb.x * m.m[0][1] + lp->posb.y * m.m[1][1] + lp->posb.z * m.m[2][1] + m.m[3][1];
+            w[5] = lp->posb.x * m.m[0][2] + lp->posb.y * m.m[1][2] + lp->posb.z * m.m[2][2] + m.m[3][2];
+            const f32 sx = sqrtf(m.m[0][0] * m.m[0][0] + m.m[0][1] * m.m[0][1] + m.m[0][2] * m.m[0][2]);
+            w[6] = lp->radius * sx; w[7] = 0.f;
+        }
+    }
+}
+
+SFT_FUNC void sft_present(void) {
+    struct sft__state* s = sft__s;
+    /* TLAS over instance bounds, rebuilt per frame (sofren2.c:3619-3703) */
+    sft__node* tlas = NULL; u32 tlas_count = 0, tlas_root = 0;
+    if (s->n_inst) {
+        sft__item* it = (sft__item*)calloc(s->n_inst, sizeof(sft__item));
+        u32 valid = 0;
+        for (u32 i = 0; i < s->n_inst; i++) {
+            const sft_model* md = s->inst_model[i];
+            if (!md->blas_count) continue;
+            const f32* T = s->inst[i].transform;
+            f32 lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
+            for (int k = 0; k < 8; k++) {
+                const f32 cx = (k & 1) ? md->root_max[0] : md->root_min[0];
+                const f32 cy = (k & 2) ? md->root_max[1] : md->root_min[1];
+                const f32 cz = (k & 4) ? md->root_max[2] : md->root_min[2];
+                for (int a = 0; a < 3; a++) {
+                    const f32 t = cx * T[a] + cy * T[4 + a] + cz * T[8 + a] + T[12 + a];
+                    if (t < lo[a]) lo[a] = t;
+                    if (t > hi[a]) hi[a] = t;
+                }
+            }
+            it[i].id = i;
+            for (int a = 0; a < 3; a++) { it[i].mn[a] = lo[a]; it[i].mx[a] = hi[a]; it[i].c[a] = (lo[a] + hi[a]) * 0.5f; }
+            valid++;
+        }
+        tlas = (sft__node*)calloc((size_t)valid * 2 + 1, sizeof(sft__node));
+        tlas_root = sft__bvh_build(it, valid, tlas, &tlas_count, NULL, NULL);
+        free(it);
+    }
+    for (u32 i = 0; i < s->n_inst; i++)
+        s->inst[i].bones = s->inst[i].bone_count ? s->bones + 16 * (size_t)s->inst_bone_off[i] : NULL;
+    sftg_frame_desc fd; memset(&fd, 0, sizeof(fd));
+    fd.width = s->width; fd.height = s->height; fd.samples = s->samples;
+    fd.cam_pos[0] = s->cam.x; fd.cam_pos[1] = s->cam.y; fd.cam_pos[2] = s->cam.z;
+    memcpy(fd.view_proj, s->view_proj.m, 64);
+    memcpy(fd.frustum_n, s->fn, sizeof(fd.frustum_n)); memcpy(fd.frustum_d, s->fd, sizeof(fd.frustum_d));
+    fd.ambient[0] = s->ambient.x; fd.ambient[1] = s->ambient.y; fd.ambient[2] = s->ambient.z;
+    fd.lightmap_brightness = s->lightmap_brightness;
+    fd.clear = s->clear; fd.clear_color = s->clear_color; fd.shadows = s->shadows; fd.debug_mode = (u32)s->debug_mode;
+    fd.n_point = s->n_point; fd.point_lights = s->point;
+    fd.n_dir = s->n_dir; fd.dir_lights = s->dir;
+    fd.n_instances = s->n_inst; fd.instances = s->inst;
+    fd.n_proxies = s->n_prox; fd.proxies = s->proxies;
+    fd.tlas_nodes = tlas; fd.tlas_count = tlas_count; fd.tlas_root = tlas_root;
+    const int rc = sftg_frame_render(s->gpu, &fd, s->color, s->pitch, s->debug);
+    free(tlas);
+    if (rc) fprintf(stderr, "sofren2-gb300: sft_present failed (%d): %s\n", rc, sftg_last_error(s->gpu));
+}
+
+SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena) {
+    sft_pose* p = (sft_pose*)(arena ? sft_arena_alloc(arena, sizeof(sft_pose)) : calloc(1, sizeof(sft_pose)));
+    const u32 n = model ? model->bone_count : 0;
+    p->model = model;
+    p->global_matrices = (sftmat*)(arena ? sft_arena_alloc(arena, (n + 1) * sizeof(sftmat)) : calloc(n + 1, sizeof(sftmat)));
+    p->posed_bone_matrices = (sftmat*)(arena ? sft_arena_alloc(arena, (n + 1) * sizeof(sftmat)) : calloc(n + 1, sizeof(sftmat)));
+    for (u32 i = 0; i < n; i++) p->global_matrices[i] = p->posed_bone_matrices[i] = sft_m_identity();
+    return p;
+}
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFT_IMPL */
+#endif /* SOFREN2_GB300_H */

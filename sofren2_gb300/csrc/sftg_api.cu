@@ -1,0 +1,556 @@
+/*
+ * The sftg C ABI: context, device memory and the per-frame launch sequence.
+ *
+ * Device memory.  Resident assets live in growable device pools (texel heap, texture and
+ * material tables, meshlet pool, skin pool, BLAS node pool, model table).  Everything a frame
+ * needs beyond that comes from one device bump arena that is reset per frame (the
+ * reference's per-frame mmap arenas, sofren2.c:9456-9564); it grows between frames when a
+ * frame needs more and never inside one.
+ *
+ * Frame sequence on one stream (sft_present, sofren2.c:8139-8289):
+ *   1. one H2D copy of the frame block: constants, instances, bones, jobs, lights, proxies, TLAS
+ *   2. k_occlusion        light visibility of every shadow proxy (8163-8280)
+ *   3. k_geometry         cull, skin, transform, project, batch setup (4901-5145)
+ *   4. scan + k_clip      near-plane clipping in emission order (4691-4772)
+ *   5. k_bin (count), scan, k_bin (write)   per-tile payload lists (4619-4688)
+ *   6. k_tile             raster + resolve per tile (6756-6813)
+ *   7. D2H of the colour buffer into the caller's pitch
+ */
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+
+#include "../../include/sftg.h"
+#include "sftg_types.h"
+#include "sftg_kernels.h"
+
+#define TILE_THREADS 256
+#define SETUP_CAP 256
+
+struct dpool {   /* growable device buffer */
+    void* ptr = nullptr;
+    size_t size = 0, cap = 0;
+};
+
+struct sftg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    char err[512] = { 0 };
+    /* resident */
+    dpool texels, texs, mats, ml_attr, ml_inds, ml_cull, ml_info, skin_j, skin_w, blas, models;
+    std::vector<sftg_tex> h_texs;
+    std::vector<sftg_mat> h_mats;
+    std::vector<sftg_model> h_models;
+    std::vector<uint32_t> h_model_skinned;   /* per model: has skinned meshes */
+    std::vector<std::vector<uint8_t>> h_mesh_skinned;  /* per model, per mesh */
+    std::vector<std::vector<uint32_t>> h_mesh_first;   /* per model, per mesh: first meshlet */
+    std::vector<std::vector<uint32_t>> h_mesh_count;
+    uint32_t n_meshlets = 0, n_skin = 0, n_blas = 0;
+    bool tables_dirty = true;
+    /* per frame */
+    void* arena = nullptr;
+    size_t arena_cap = 0;
+    void* h_stage = nullptr;     /* pinned staging for the frame block */
+    size_t h_stage_cap = 0;
+    uint32_t* h_status = nullptr;
+    uint64_t tile_cap = 1u << 20, clip_cap = 1u << 16;
+    cudaEvent_t ev[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
+    float timings[4] = { 0, 0, 0, 0 };
+    int launches = 0;
+    uint32_t* d_color = nullptr;
+    size_t d_color_cap = 0;
+};
+
+static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        va_list ap; va_start(ap, fmt);
+        vsnprintf(c->err, sizeof(c->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return set_err(ctx, SFTG_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); } while (0)
+
+static int pool_reserve(sftg_ctx* ctx, dpool& p, size_t bytes) {
+    if (bytes <= p.cap) return 0;
+    size_t nc = p.cap ? p.cap : 1 << 20;
+    while (nc < bytes) nc *= 2;
+    void* np = nullptr;
+    if (cudaMalloc(&np, nc) != cudaSuccess) return set_err(ctx, SFTG_E_NOMEM, "device pool growth to %zu bytes failed", nc);
+    if (p.ptr) {
+        CK(cudaMemcpyAsync(np, p.ptr, p.size, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(p.ptr);
+    }
+    p.ptr = np; p.cap = nc;
+    ctx->tables_dirty = true;
+    return 0;
+}
+
+static int pool_append(sftg_ctx* ctx, dpool& p, const void* src, size_t bytes, size_t* out_offset) {
+    const size_t off = (p.size + 255) & ~(size_t)255;
+    int rc = pool_reserve(ctx, p, off + bytes);
+    if (rc) return rc;
+    if (bytes) CK(cudaMemcpyAsync((char*)p.ptr + off, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    p.size = off + bytes;
+    if (out_offset) *out_offset = off;
+    return 0;
+}
+
+extern "C" int sftg_create(int device, sftg_ctx** out) {
+    if (!out) return SFTG_E_ARG;
+    sftg_ctx* ctx = new sftg_ctx();
+    ctx->device = device;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) { delete ctx; return SFTG_E_CUDA; }
+    if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
+    for (int i = 0; i < 5; i++) cudaEventCreate(&ctx->ev[i]);
+    if (cudaMallocHost((void**)&ctx->h_status, 64) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
+    sftg_tile_configure(200 * 1024);
+    *out = ctx;
+    return SFTG_OK;
+}
+
+extern "C" void sftg_destroy(sftg_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    dpool* pools[] = { &ctx->texels, &ctx->texs, &ctx->mats, &ctx->ml_attr, &ctx->ml_inds, &ctx->ml_cull, &ctx->ml_info,
+                       &ctx->skin_j, &ctx->skin_w, &ctx->blas, &ctx->models };
+    for (dpool* p : pools) if (p->ptr) cudaFree(p->ptr);
+    if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->d_color) cudaFree(ctx->d_color);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    for (int i = 0; i < 5; i++) if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char* sftg_last_error(const sftg_ctx* ctx) { return ctx ? ctx->err : "no context"; }
+
+extern "C" int sftg_texture_upload(sftg_ctx* ctx, const uint32_t* texels, uint64_t n_texels, const sftg_texture_desc* d, int32_t* out_index) {
+    if (!ctx || !texels || !d || !out_index) return SFTG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    size_t off = 0;
+    int rc = pool_append(ctx, ctx->texels, texels, n_texels * 4, &off);
+    if (rc) return rc;
+    sftg_tex t;
+    memset(&t, 0, sizeof(t));
+    t.w = d->width; t.h = d->height; t.levels = d->levels; t.is_pot = d->is_pot;
+    for (int i = 0; i < 14; i++) { t.offs[i] = (uint32_t)(off / 4) + d->level_offset[i]; t.bw[i] = d->blocks_w[i]; t.shift[i] = d->stride_shift[i]; }
+    ctx->h_texs.push_back(t);
+    ctx->tables_dirty = true;
+    *out_index = (int32_t)ctx->h_texs.size() - 1;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SFTG_OK;
+}
+
+extern "C" int sftg_texture_update_desc(sftg_ctx* ctx, int32_t index, const sftg_texture_desc* d) {
+    if (!ctx || index < 0 || (size_t)index >= ctx->h_texs.size()) return SFTG_E_ARG;
+    if (!d) { ctx->h_texs[index].w = 0; }
+    ctx->tables_dirty = true;
+    return SFTG_OK;
+}
+
+extern "C" int sftg_material_set(sftg_ctx* ctx, int32_t index, int32_t texture, uint32_t base_color, float shininess) {
+    if (!ctx || index < 0) return SFTG_E_ARG;
+    if ((size_t)index >= ctx->h_mats.size()) ctx->h_mats.resize(index + 1);
+    ctx->h_mats[index].tex = texture;
+    ctx->h_mats[index].base_color = base_color;
+    ctx->h_mats[index].shininess = shininess;
+    ctx->tables_dirty = true;
+    return SFTG_OK;
+}
+
+extern "C" int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model) {
+    if (!ctx || !d || !out_model) return SFTG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    uint32_t total = 0;
+    for (uint32_t k = 0; k < d->mesh_count; k++) total += d->meshes[k].meshlet_count;
+    std::vector<float> attr((size_t)total * 640), cull((size_t)total * 8);
+    std::vector<uint8_t> inds((size_t)total * 512);
+    std::vector<sftg_meshlet_info> info(total);
+    std::vector<uint16_t> sj; std::vector<uint8_t> sw;
+    std::vector<uint8_t> mesh_sk; std::vector<uint32_t> mesh_first, mesh_cnt;
+    uint32_t o = 0, nskin = 0;
+    for (uint32_t k = 0; k < d->mesh_count; k++) {
+        const sftg_mesh_desc& m = d->meshes[k];
+        const bool sk = m.joints && m.weights;
+        mesh_sk.push_back(sk ? 1 : 0); mesh_first.push_back(o); mesh_cnt.push_back(m.meshlet_count);
+        memcpy(&attr[(size_t)o * 640], m.attr, (size_t)m.meshlet_count * 640 * 4);
+        memcpy(&inds[(size_t)o * 512], m.inds, (size_t)m.meshlet_count * 512);
+        memcpy(&cull[(size_t)o * 8], m.cull, (size_t)m.meshlet_count * 32);
+        for (uint32_t j = 0; j < m.meshlet_count; j++) {
+            sftg_meshlet_info& in = info[o + j];
+            in.material = m.material;
+            in.lightmap_tex = m.lightmap_texture;
+            in.culling_bone = (sk && m.culling_bones) ? m.culling_bones[j] : -1;
+            in.skin_slot = sk ? (int32_t)(ctx->n_skin + nskin + j) : -1;
+        }
+        if (sk) {
+            sj.insert(sj.end(), m.joints, m.joints + (size_t)m.meshlet_count * 256);
+            sw.insert(sw.end(), m.weights, m.weights + (size_t)m.meshlet_count * 256);
+            nskin += m.meshlet_count;
+        }
+        o += m.meshlet_count;
+    }
+    sftg_model md;
+    memset(&md, 0, sizeof(md));
+    md.meshlet_base = ctx->n_meshlets;
+    md.total_meshlets = total;
+    md.bone_count = d->bone_count;
+    md.mesh_count = d->mesh_count;
+    md.blas_base = ctx->n_blas; md.blas_root = d->blas_root; md.blas_count = d->blas_count;
+    int rc;
+    /* meshlet pools are indexed by meshlet, so they append at exact element offsets */
+    if ((rc = pool_reserve(ctx, ctx->ml_attr, ((size_t)ctx->n_meshlets + total) * 2560))) return rc;
+    if ((rc = pool_reserve(ctx, ctx->ml_inds, ((size_t)ctx->n_meshlets + total) * 512))) return rc;
+    if ((rc = pool_reserve(ctx, ctx->ml_cull, ((size_t)ctx->n_meshlets + total) * 32))) return rc;
+    if ((rc = pool_reserve(ctx, ctx->ml_info, ((size_t)ctx->n_meshlets + total) * sizeof(sftg_meshlet_info)))) return rc;
+    CK(cudaMemcpyAsync((char*)ctx->ml_attr.ptr + (size_t)ctx->n_meshlets * 2560, attr.data(), (size_t)total * 2560, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync((char*)ctx->ml_inds.ptr + (size_t)ctx->n_meshlets * 512, inds.data(), (size_t)total * 512, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync((char*)ctx->ml_cull.ptr + (size_t)ctx->n_meshlets * 32, cull.data(), (size_t)total * 32, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync((char*)ctx->ml_info.ptr + (size_t)ctx->n_meshlets * sizeof(sftg_meshlet_info), info.data(), (size_t)total * sizeof(sftg_meshlet_info), cudaMemcpyHostToDevice, ctx->stream));
+    /* sizes must track the filled bytes: a later growth copies exactly `size` bytes */
+    ctx->ml_attr.size = ((size_t)ctx->n_meshlets + total) * 2560;
+    ctx->ml_inds.size = ((size_t)ctx->n_meshlets + total) * 512;
+    ctx->ml_cull.size = ((size_t)ctx->n_meshlets + total) * 32;
+    ctx->ml_info.size = ((size_t)ctx->n_meshlets + total) * sizeof(sftg_meshlet_info);
+    if (nskin) {
+        if ((rc = pool_reserve(ctx, ctx->skin_j, ((size_t)ctx->n_skin + nskin) * 512))) return rc;
+        if ((rc = pool_reserve(ctx, ctx->skin_w, ((size_t)ctx->n_skin + nskin) * 256))) return rc;
+        CK(cudaMemcpyAsync((char*)ctx->skin_j.ptr + (size_t)ctx->n_skin * 512, sj.data(), (size_t)nskin * 512, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync((char*)ctx->skin_w.ptr + (size_t)ctx->n_skin * 256, sw.data(), (size_t)nskin * 256, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->skin_j.size = ((size_t)ctx->n_skin + nskin) * 512;
+        ctx->skin_w.size = ((size_t)ctx->n_skin + nskin) * 256;
+    }
+    if (d->blas_count) {
+        if ((rc = pool_reserve(ctx, ctx->blas, ((size_t)ctx->n_blas + d->blas_count) * 256))) return rc;
+        CK(cudaMemcpyAsync((char*)ctx->blas.ptr + (size_t)ctx->n_blas * 256, d->blas_nodes, (size_t)d->blas_count * 256, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->blas.size = ((size_t)ctx->n_blas + d->blas_count) * 256;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->n_meshlets += total; ctx->n_skin += nskin; ctx->n_blas += d->blas_count;
+    ctx->h_models.push_back(md);
+    ctx->h_mesh_skinned.push_back(mesh_sk);
+    ctx->h_mesh_first.push_back(mesh_first);
+    ctx->h_mesh_count.push_back(mesh_cnt);
+    ctx->tables_dirty = true;
+    *out_model = (int32_t)ctx->h_models.size() - 1;
+    return SFTG_OK;
+}
+
+static int sync_tables(sftg_ctx* ctx) {
+    if (!ctx->tables_dirty) return 0;
+    int rc;
+    if ((rc = pool_reserve(ctx, ctx->texs, (ctx->h_texs.size() + 1) * sizeof(sftg_tex)))) return rc;
+    if ((rc = pool_reserve(ctx, ctx->mats, (ctx->h_mats.size() + 1) * sizeof(sftg_mat)))) return rc;
+    if ((rc = pool_reserve(ctx, ctx->models, (ctx->h_models.size() + 1) * sizeof(sftg_model)))) return rc;
+    if (!ctx->h_texs.empty()) CK(cudaMemcpyAsync(ctx->texs.ptr, ctx->h_texs.data(), ctx->h_texs.size() * sizeof(sftg_tex), cudaMemcpyHostToDevice, ctx->stream));
+    if (!ctx->h_mats.empty()) CK(cudaMemcpyAsync(ctx->mats.ptr, ctx->h_mats.data(), ctx->h_mats.size() * sizeof(sftg_mat), cudaMemcpyHostToDevice, ctx->stream));
+    if (!ctx->h_models.empty()) CK(cudaMemcpyAsync(ctx->models.ptr, ctx->h_models.data(), ctx->h_models.size() * sizeof(sftg_model), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->tables_dirty = false;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ frame */
+struct bump {
+    char* base; size_t off, cap;
+    template <class T> T* take(size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = (T*)(base + off);
+        off += n * sizeof(T);
+        return p;
+    }
+};
+
+struct frame_bufs {
+    sftg_frame* F;
+    float* ss;
+    sftg_batch_rec* recs;
+    uint32_t* clip_cnt; uint32_t* clip_base;
+    int4* mrect;
+    sftg_clip_tri* clips; int4* clip_rect;
+    uint32_t* tile_count; uint32_t* tile_start;
+    uint64_t* tile_pay;
+    uint8_t* light_vis;
+    uint32_t* scan_tmp;
+    uint32_t* status;
+    uint32_t* totals;    /* [0] clip total, [1] tile payload total */
+    float* vis_depth; uint32_t* vis_id; float* shadow;
+    size_t used;
+};
+
+static void scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, uint32_t* total, cudaStream_t st, int* launches) {
+    const uint32_t nb = (n + SFTG_SCAN_ELEMS_PER_BLOCK - 1) / SFTG_SCAN_ELEMS_PER_BLOCK;
+    if (!nb) return;
+    k_scan_reduce<<<nb, 1024, 0, st>>>(in, n, tmp);
+    k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, total);
+    k_scan_down<<<nb, 1024, 0, st>>>(in, n, tmp, out);
+    *launches += 3;
+}
+
+static size_t tile_smem(int S) {
+    const size_t aux = 256 * 84 > 256 * 72 ? (size_t)SETUP_CAP * 84 : (size_t)256 * 72;
+    return (size_t)S * SFTG_TILE_PX * 8 + aux;
+}
+
+/* lays out and uploads the frame block; returns 0 or an error */
+static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug, frame_bufs& B, uint32_t& total_ss, uint32_t& n_jobs) {
+    const int W = fd->width, H = fd->height, S = fd->samples;
+    if (W <= 0 || H <= 0 || !(S == 1 || S == 2 || S == 4)) return set_err(ctx, SFTG_E_ARG, "bad frame size or samples");
+    if (fd->n_instances > SFTG_MAX_INSTANCES) return set_err(ctx, SFTG_E_LIMIT, "more than %d instances in one frame", SFTG_MAX_INSTANCES);
+    const int cols = (W + 63) / 64, rows = (H + 63) / 64, tiles = cols * rows;
+    /* host-side frame block */
+    std::vector<sftg_inst> inst(fd->n_instances + 1);
+    std::vector<sftg_job> jobs;
+    std::vector<float> bones;
+    total_ss = 0;
+    for (uint32_t i = 0; i < fd->n_instances; i++) {
+        const sftg_instance_desc& id = fd->instances[i];
+        if (id.model < 0 || (size_t)id.model >= ctx->h_models.size()) return set_err(ctx, SFTG_E_ARG, "instance %u: bad model", i);
+        const sftg_model& md = ctx->h_models[id.model];
+        sftg_inst& I = inst[i];
+        memcpy(I.T, id.transform, 64);
+        I.model = (uint32_t)id.model;
+        I.ss_offset = total_ss;
+        I.meshlet_base = md.meshlet_base;
+        I.bones = -1;
+        if (id.bones && id.bone_count) {
+            I.bones = (int32_t)(bones.size() / 16);
+            bones.insert(bones.end(), id.bones, id.bones + (size_t)id.bone_count * 16);
+        }
+        for (uint32_t k = 0; k < md.mesh_count; k++) {
+            const uint32_t first = ctx->h_mesh_first[id.model][k], cnt = ctx->h_mesh_count[id.model][k];
+            const uint32_t sk = ctx->h_mesh_skinned[id.model][k] && I.bones >= 0;
+            for (uint32_t s = 0; s < cnt; s += 8) {
+                sftg_job j; j.inst = i; j.first = first + s; j.count = (cnt - s) < 8 ? (cnt - s) : 8; j.skinned = sk;
+                jobs.push_back(j);
+            }
+        }
+        total_ss += md.total_meshlets;
+    }
+    n_jobs = (uint32_t)jobs.size();
+    const size_t n_rec = (size_t)total_ss * 16;
+    /* staging layout */
+    size_t so = 0;
+    auto stage_take = [&](size_t bytes) { so = (so + 255) & ~(size_t)255; const size_t r = so; so += bytes; return r; };
+    const size_t o_F = stage_take(sizeof(sftg_frame));
+    const size_t o_inst = stage_take(inst.size() * sizeof(sftg_inst));
+    const size_t o_bones = stage_take(bones.size() * 4 + 64);
+    const size_t o_jobs = stage_take(jobs.size() * sizeof(sftg_job) + 16);
+    const size_t o_pl = stage_take((size_t)fd->n_point * sizeof(sftg_point_light) + 16);
+    const size_t o_dl = stage_take((size_t)fd->n_dir * sizeof(sftg_dir_light) + 16);
+    const size_t o_px = stage_take((size_t)fd->n_proxies * sizeof(sftg_proxy) + 16);
+    const size_t o_tl = stage_take((size_t)fd->tlas_count * 256 + 16);
+    const size_t stage_bytes = so;
+    /* device arena layout */
+    size_t need = stage_bytes + 4096;
+    auto acc = [&](size_t bytes) { need = ((need + 255) & ~(size_t)255) + bytes; };
+    acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
+    acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
+    acc((size_t)tiles * 4); acc((size_t)tiles * 4); acc(ctx->tile_cap * 8);
+    acc((size_t)fd->n_proxies * 64 + 64); acc(((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
+    if (want_debug) { acc((size_t)tiles * S * 4096 * 4); acc((size_t)tiles * S * 4096 * 4); acc((size_t)W * H * 16 * 4); }
+    if (need > ctx->arena_cap) {
+        if (ctx->arena) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->arena); ctx->arena = nullptr; }
+        size_t nc = need + need / 4;
+        if (cudaMalloc(&ctx->arena, nc) != cudaSuccess) { ctx->arena_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "frame arena of %zu bytes", nc); }
+        ctx->arena_cap = nc;
+    }
+    if (stage_bytes > ctx->h_stage_cap) {
+        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        size_t nc = stage_bytes + stage_bytes / 4 + 4096;
+        if (cudaMallocHost(&ctx->h_stage, nc) != cudaSuccess) { ctx->h_stage = nullptr; ctx->h_stage_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "pinned staging"); }
+        ctx->h_stage_cap = nc;
+    }
+    char* hs = (char*)ctx->h_stage;
+    char* ds = (char*)ctx->arena;
+    bump bp{ ds, stage_bytes, ctx->arena_cap };
+    B.ss = bp.take<float>((size_t)total_ss * 576);
+    B.recs = bp.take<sftg_batch_rec>(n_rec);
+    B.clip_cnt = bp.take<uint32_t>(n_rec);
+    B.clip_base = bp.take<uint32_t>(n_rec);
+    B.mrect = bp.take<int4>((size_t)total_ss + 1);
+    B.clips = bp.take<sftg_clip_tri>(ctx->clip_cap);
+    B.clip_rect = bp.take<int4>(ctx->clip_cap);
+    B.tile_count = bp.take<uint32_t>(tiles);
+    B.tile_start = bp.take<uint32_t>(tiles);
+    B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
+    B.light_vis = bp.take<uint8_t>((size_t)fd->n_proxies * 64 + 64);
+    B.scan_tmp = bp.take<uint32_t>((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
+    B.status = bp.take<uint32_t>(16);
+    B.totals = bp.take<uint32_t>(16);
+    B.vis_depth = nullptr; B.vis_id = nullptr; B.shadow = nullptr;
+    if (want_debug) {
+        B.vis_depth = bp.take<float>((size_t)tiles * S * 4096);
+        B.vis_id = bp.take<uint32_t>((size_t)tiles * S * 4096);
+        B.shadow = bp.take<float>((size_t)W * H * 16);
+    }
+    B.used = bp.off;
+    /* fill the staging block */
+    sftg_frame* F = (sftg_frame*)(hs + o_F);
+    memset(F, 0, sizeof(*F));
+    F->width = W; F->height = H; F->samples = S; F->pitch = W;
+    F->hw = (float)W * 0.5f; F->hh = (float)H * 0.5f; F->vpx = 0.f; F->vpy = 0.f;
+    F->cols = cols; F->rows = rows; F->tiles = tiles; F->debug_mode = (int32_t)fd->debug_mode;
+    F->clear = fd->clear; F->clear_color = fd->clear_color; F->shadows = fd->shadows;
+    memcpy(F->cam, fd->cam_pos, 12);
+    memcpy(F->vp, fd->view_proj, 64);
+    for (int p = 0; p < 6; p++) {
+        for (int a = 0; a < 3; a++) { F->fn[p][a] = fd->frustum_n[p][a]; F->fan[p][a] = fabsf(fd->frustum_n[p][a]); }
+        F->fd[p] = fd->frustum_d[p];
+    }
+    memcpy(F->ambient, fd->ambient, 12);
+    F->lightmap_brightness = fd->lightmap_brightness;
+    F->n_point = fd->n_point; F->n_dir = fd->n_dir; F->n_proxies = fd->n_proxies; F->n_inst = fd->n_instances;
+    F->total_ss = total_ss; F->n_jobs = n_jobs; F->tlas_root = fd->tlas_root; F->tlas_count = fd->tlas_count;
+    F->clip_cap = (uint32_t)ctx->clip_cap; F->tile_cap = (uint32_t)ctx->tile_cap;
+    F->inst = (const sftg_inst*)(ds + o_inst);
+    F->bones = (const float*)(ds + o_bones);
+    F->jobs = (const sftg_job*)(ds + o_jobs);
+    F->point = (const sftg_point_light*)(ds + o_pl);
+    F->dir = (const sftg_dir_light*)(ds + o_dl);
+    F->proxies = (const sftg_proxy*)(ds + o_px);
+    F->tlas = (const sftg_bvh_node*)(ds + o_tl);
+    F->models = (const sftg_model*)ctx->models.ptr;
+    F->texs = (const sftg_tex*)ctx->texs.ptr;
+    F->texels = (const uint32_t*)ctx->texels.ptr;
+    F->mats = (const sftg_mat*)ctx->mats.ptr;
+    F->ml_attr = (const float*)ctx->ml_attr.ptr;
+    F->ml_inds = (const uint8_t*)ctx->ml_inds.ptr;
+    F->ml_cull = (const float*)ctx->ml_cull.ptr;
+    F->ml_info = (const sftg_meshlet_info*)ctx->ml_info.ptr;
+    F->skin_j = (const uint16_t*)ctx->skin_j.ptr;
+    F->skin_w = (const uint8_t*)ctx->skin_w.ptr;
+    F->blas = (const sftg_bvh_node*)ctx->blas.ptr;
+    memcpy(hs + o_inst, inst.data(), inst.size() * sizeof(sftg_inst));
+    if (!bones.empty()) memcpy(hs + o_bones, bones.data(), bones.size() * 4);
+    if (!jobs.empty()) memcpy(hs + o_jobs, jobs.data(), jobs.size() * sizeof(sftg_job));
+    for (uint32_t l = 0; l < fd->n_point; l++) memcpy(hs + o_pl + l * sizeof(sftg_point_light), fd->point_lights + 8 * l, 32);
+    for (uint32_t l = 0; l < fd->n_dir; l++) memcpy(hs + o_dl + l * sizeof(sftg_dir_light), fd->dir_lights + 6 * l, 24);
+    for (uint32_t p = 0; p < fd->n_proxies; p++) memcpy(hs + o_px + p * sizeof(sftg_proxy), fd->proxies + 8 * p, 32);
+    if (fd->tlas_count) memcpy(hs + o_tl, fd->tlas_nodes, (size_t)fd->tlas_count * 256);
+    B.F = (sftg_frame*)(ds + o_F);
+    CK(cudaMemcpyAsync(ds, hs, stage_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return 0;
+}
+
+static int launch_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, const frame_bufs& B, uint32_t total_ss, uint32_t n_jobs, uint32_t* d_color) {
+    const int S = fd->samples;
+    const int tiles = ((fd->width + 63) / 64) * ((fd->height + 63) / 64);
+    const uint32_t n_rec = total_ss * 16;
+    cudaStream_t st = ctx->stream;
+    ctx->launches = 0;
+    CK(cudaMemsetAsync(B.status, 0, 64, st));
+    CK(cudaEventRecord(ctx->ev[0], st));
+    if (fd->shadows && fd->n_point && fd->n_proxies) {
+        const uint32_t items = (fd->n_point < 64 ? fd->n_point : 64) * ((fd->n_proxies + 7) / 8);
+        k_occlusion<<<(items + 3) / 4, 128, 0, st>>>(B.F, B.light_vis, B.status);
+        ctx->launches++;
+    }
+    CK(cudaEventRecord(ctx->ev[1], st));
+    if (n_jobs) {
+        k_geometry<<<(n_jobs + 3) / 4, 128, 0, st>>>(B.F, B.ss, B.recs, B.clip_cnt, B.mrect);
+        ctx->launches++;
+    }
+    if (n_rec) {
+        scan_u32(B.clip_cnt, B.clip_base, n_rec, B.scan_tmp, B.totals + 0, st, &ctx->launches);
+        k_clip<<<(n_rec + 255) / 256, 256, 0, st>>>(B.F, B.ss, B.clip_cnt, B.clip_base, B.clips, B.clip_rect, B.mrect, n_rec);
+        ctx->launches++;
+    } else {
+        CK(cudaMemsetAsync(B.totals, 0, 8, st));
+    }
+    CK(cudaEventRecord(ctx->ev[2], st));
+    k_bin<<<tiles, 256, 0, st>>>(B.F, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
+    scan_u32(B.tile_count, B.tile_start, tiles, B.scan_tmp, B.totals + 1, st, &ctx->launches);
+    k_bin<<<tiles, 256, 0, st>>>(B.F, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
+    ctx->launches += 2;
+    CK(cudaEventRecord(ctx->ev[3], st));
+    const size_t sm = tile_smem(S);
+    sftg_launch_tile(S, tiles, sm, st, B.F, B.ss, B.clips, B.tile_start, B.tile_count, B.tile_pay, B.light_vis, d_color, B.vis_depth, B.vis_id, B.shadow);
+    ctx->launches++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[4], st));
+    return 0;
+}
+
+static int frame_common(sftg_ctx* ctx, const sftg_frame_desc* fd, uint32_t* host_color, int32_t pitch_bytes, sftg_debug_out* dbg, const uint32_t** out_dev) {
+    if (!ctx || !fd) return SFTG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_tables(ctx);
+    if (rc) return rc;
+    const int W = fd->width, H = fd->height;
+    const size_t cbytes = (size_t)W * H * 4;
+    if (cbytes > ctx->d_color_cap) {
+        if (ctx->d_color) cudaFree(ctx->d_color);
+        if (cudaMalloc((void**)&ctx->d_color, cbytes) != cudaSuccess) { ctx->d_color = nullptr; ctx->d_color_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "colour buffer"); }
+        ctx->d_color_cap = cbytes;
+    }
+    const int pitch = pitch_bytes > 0 ? pitch_bytes : W * 4;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        frame_bufs B; uint32_t total_ss = 0, n_jobs = 0;
+        if ((rc = build_frame(ctx, fd, dbg != nullptr, B, total_ss, n_jobs))) return rc;
+        if (!fd->clear && host_color)   /* the reference blends over / keeps the caller's pixels */
+            CK(cudaMemcpy2DAsync(ctx->d_color, (size_t)W * 4, host_color, (size_t)pitch, (size_t)W * 4, H, cudaMemcpyHostToDevice, ctx->stream));
+        if ((rc = launch_frame(ctx, fd, B, total_ss, n_jobs, ctx->d_color))) return rc;
+        CK(cudaMemcpyAsync(ctx->h_status, B.status, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->h_status + 2, B.totals, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        if (host_color)
+            CK(cudaMemcpy2DAsync(host_color, (size_t)pitch, ctx->d_color, (size_t)W * 4, (size_t)W * 4, H, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        const uint32_t clip_total = ctx->h_status[2], pay_total = ctx->h_status[3];
+        if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap) {   /* capacity exceeded: grow and redo the frame */
+            while (ctx->clip_cap < clip_total) ctx->clip_cap *= 2;
+            while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
+            continue;
+        }
+        float t[4];
+        for (int k = 0; k < 4; k++) { t[k] = 0.f; cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]); ctx->timings[k] = t[k]; }
+        if (dbg) {
+            const int S = fd->samples, tiles = ((W + 63) / 64) * ((H + 63) / 64);
+            if (dbg->vis_depth) CK(cudaMemcpy(dbg->vis_depth, B.vis_depth, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
+            if (dbg->vis_id) CK(cudaMemcpy(dbg->vis_id, B.vis_id, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
+            if (dbg->tile_counts) CK(cudaMemcpy(dbg->tile_counts, B.tile_count, (size_t)tiles * 4, cudaMemcpyDeviceToHost));
+            if (dbg->tile_payload_total) *dbg->tile_payload_total = pay_total;
+            if (dbg->tile_payloads && pay_total <= dbg->tile_payload_cap) CK(cudaMemcpy(dbg->tile_payloads, B.tile_pay, (size_t)pay_total * 8, cudaMemcpyDeviceToHost));
+            if (dbg->ss_cache) CK(cudaMemcpy(dbg->ss_cache, B.ss, (size_t)total_ss * 2304, cudaMemcpyDeviceToHost));
+            if (dbg->light_vis && fd->n_proxies) CK(cudaMemcpy(dbg->light_vis, B.light_vis, (size_t)fd->n_proxies * 64, cudaMemcpyDeviceToHost));
+            if (dbg->clip_total) *dbg->clip_total = clip_total;
+            if (dbg->clip_tris && clip_total <= dbg->clip_cap) CK(cudaMemcpy(dbg->clip_tris, B.clips, (size_t)clip_total * sizeof(sftg_clip_tri), cudaMemcpyDeviceToHost));
+            if (dbg->shadow && fd->samples == 1) CK(cudaMemcpy(dbg->shadow, B.shadow, (size_t)W * H * 16 * 4, cudaMemcpyDeviceToHost));
+            if (dbg->status) *dbg->status = ctx->h_status[0];
+        }
+        if (out_dev) *out_dev = ctx->d_color;
+        if (ctx->h_status[0] & 1u) return set_err(ctx, SFTG_E_DEVICE_STATUS, "occlusion traversal exceeded its stack bound");
+        return SFTG_OK;
+    }
+    return set_err(ctx, SFTG_E_NOMEM, "frame capacities did not converge");
+}
+
+extern "C" int sftg_frame_render(sftg_ctx* ctx, const sftg_frame_desc* fd, uint32_t* color, int32_t pitch_bytes, sftg_debug_out* dbg) {
+    if (dbg) {   /* debug capture renders into scratch state first so vis buffers are available */
+        if (dbg->shadow && fd->samples == 1) {}
+    }
+    return frame_common(ctx, fd, color, pitch_bytes, dbg, nullptr);
+}
+
+extern "C" int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* fd, const uint32_t** out_device_color) {
+    return frame_common(ctx, fd, nullptr, 0, nullptr, out_device_color);
+}
+
+extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out4) {
+    if (!ctx || !out4) return SFTG_E_ARG;
+    for (int k = 0; k < 4; k++) out4[k] = ctx->timings[k];
+    return SFTG_OK;
+}
+
+extern "C" int sftg_last_launch_count(const sftg_ctx* ctx) { return ctx ? ctx->launches : 0; }

@@ -1,0 +1,285 @@
+/*
+ * k_occlusion: the per-frame proxy occlusion pass (inside sft_present, sofren2.c:8163-8280).
+ * One warp per (light, batch of 8 proxies).  For each of the three rays toward the light disk
+ * the warp traces the 8-ray packet through the instance TLAS and each static model's BLAS:
+ * lanes 0-7 test the node's eight child AABBs against the packet frustum (one child per lane,
+ * sft__frustum_vs_bvh_node 3906-3968) and a ballot gives the hit mask, visited in child order;
+ * at a leaf triangle lanes 0-7 run the any-hit test of their own ray (3840-3904).  The result
+ * per proxy is 3 minus the number of occluded rays.
+ *
+ * Traversal stacks live in shared memory with a fixed depth; the walk is bounded by the node
+ * count and a stack overflow sets a status word instead of writing out of bounds.
+ */
+#include "sftg_types.h"
+#include "sftg_lane.cuh"
+#include "sftg_kernels.h"
+
+#define OCC_WARPS 4
+#define OCC_STACK 64
+
+struct frustum6 { float n[6][3], an[6][3], d[6]; };
+
+/* child mask of one BVH node against a frustum: lane c < 8 tests child c */
+SFTG_D uint32_t node_mask(const sftg_bvh_node* nd, const frustum6& fr, int lane) {
+    bool in = false;
+    if (lane < 8) {
+        const float mnx = nd->mn[0][lane], mny = nd->mn[1][lane], mnz = nd->mn[2][lane];
+        const float mxx = nd->mx[0][lane], mxy = nd->mx[1][lane], mxz = nd->mx[2][lane];
+        const float cx = (mxx + mnx) * 0.5f, cy = (mxy + mny) * 0.5f, cz = (mxz + mnz) * 0.5f;
+        const float ex = (mxx - mnx) * 0.5f, ey = (mxy - mny) * 0.5f, ez = (mxz - mnz) * 0.5f;
+        in = true;
+#pragma unroll
+        for (int p = 0; p < 6; p++) {
+            const float r = fma_(fr.an[p][0], ex, fma_(fr.an[p][1], ey, fr.an[p][2] * ez));
+            const float dc = fma_(fr.n[p][0], cx, fma_(fr.n[p][1], cy, fr.n[p][2] * cz));
+            const float dist = dc + fr.d[p];
+            in = in && (dist + r >= 0.f);
+        }
+    }
+    return __ballot_sync(0xFFFFFFFFu, in) & 0xFFu;
+}
+
+/* sft_m_view_look_at (1737-1770) */
+SFTG_D void view_look_at(v3 pos, v3 target, v3 up, float* m) {
+    const v3 fwd = snorm(sub3(target, pos));
+    if (fabsf(fwd.x) < 1e-6f && fabsf(fwd.z) < 1e-6f) up = mk3(0.f, 0.f, -1.f);
+    up = snorm(sub3(up, scl3(fwd, sdot(up, fwd))));
+    const v3 right = cross3(up, fwd);
+    m[0] = right.x; m[1] = up.x; m[2] = fwd.x; m[3] = 0.f;
+    m[4] = right.y; m[5] = up.y; m[6] = fwd.y; m[7] = 0.f;
+    m[8] = right.z; m[9] = up.z; m[10] = fwd.z; m[11] = 0.f;
+    m[12] = -sdot(pos, right); m[13] = -sdot(pos, up); m[14] = -sdot(pos, fwd); m[15] = 1.f;
+}
+
+/* sft__build_packet_frustum (3970-4084); returns false when the reference leaves the side
+ * planes undefined (a cluster corner at or behind the light); those planes then never cull. */
+SFTG_D bool packet_frustum(const float* ox, const float* oy, const float* oz, uint32_t active, v3 lpos, float lrad, frustum6& f) {
+    float mn[3] = { 1e9f, 1e9f, 1e9f }, mx[3] = { -1e9f, -1e9f, -1e9f };
+    v3 ctr = mk3(0.f, 0.f, 0.f); int nv = 0;
+    for (int i = 0; i < 8; i++) {
+        if (!((active >> i) & 1u)) continue;
+        if (ox[i] < mn[0]) mn[0] = ox[i];
+        if (ox[i] > mx[0]) mx[0] = ox[i];
+        if (oy[i] < mn[1]) mn[1] = oy[i];
+        if (oy[i] > mx[1]) mx[1] = oy[i];
+        if (oz[i] < mn[2]) mn[2] = oz[i];
+        if (oz[i] > mx[2]) mx[2] = oz[i];
+        ctr.x = ctr.x + ox[i]; ctr.y = ctr.y + oy[i]; ctr.z = ctr.z + oz[i]; nv++;
+    }
+    if (!nv) return true;
+    ctr.x = fdiv(ctr.x, (float)nv); ctr.y = fdiv(ctr.y, (float)nv); ctr.z = fdiv(ctr.z, (float)nv);
+    const v3 lf0 = snorm(sub3(ctr, lpos));
+    v3 up = mk3(0.f, 1.f, 0.f);
+    if (fabsf(lf0.y) > 0.99f) up = mk3(1.f, 0.f, 0.f);
+    float lv[16];
+    view_look_at(lpos, ctr, up, lv);
+    float mnxz = 1e9f, mxxz = -1e9f, mnyz = 1e9f, mxyz = -1e9f;
+    bool invalid = false;
+    for (int k = 0; k < 8; k++) {
+        const float x = (k & 1) ? mx[0] : mn[0], y = (k & 2) ? mx[1] : mn[1], z = (k & 4) ? mx[2] : mn[2];
+        const float cxv = x * lv[0] + y * lv[4] + z * lv[8] + 1.f * lv[12];
+        const float cyv = x * lv[1] + y * lv[5] + z * lv[9] + 1.f * lv[13];
+        const float czv = x * lv[2] + y * lv[6] + z * lv[10] + 1.f * lv[14];
+        if (czv < 1e-6f) { invalid = true; break; }
+        const float qx = fdiv(cxv, czv), qy = fdiv(cyv, czv);
+        if (qx < mnxz) mnxz = qx;
+        if (qx > mxxz) mxxz = qx;
+        if (qy < mnyz) mnyz = qy;
+        if (qy > mxyz) mxyz = qy;
+    }
+    const v3 lr = mk3(lv[0], lv[4], lv[8]), lu = mk3(lv[1], lv[5], lv[9]), lf = mk3(lv[2], lv[6], lv[10]);
+    if (invalid) {
+        for (int p = 0; p < 4; p++) { for (int a = 0; a < 3; a++) { f.n[p][a] = 0.f; f.an[p][a] = 0.f; } f.d[p] = 1e30f; }
+    } else {
+        const v3 nl[4] = { mk3(1.f, 0.f, -mnxz), mk3(-1.f, 0.f, mxxz), mk3(0.f, 1.f, -mnyz), mk3(0.f, -1.f, mxyz) };
+        for (int p = 0; p < 4; p++) {
+            const v3 q = snorm(nl[p]);
+            const v3 nw = add3(scl3(lr, q.x), add3(scl3(lu, q.y), scl3(lf, q.z)));
+            f.n[p][0] = nw.x; f.n[p][1] = nw.y; f.n[p][2] = nw.z;
+            f.d[p] = -sdot(nw, lpos) + 0.1f;
+            f.an[p][0] = fabsf(nw.x); f.an[p][1] = fabsf(nw.y); f.an[p][2] = fabsf(nw.z);
+        }
+    }
+    f.n[4][0] = lf.x; f.n[4][1] = lf.y; f.n[4][2] = lf.z; f.d[4] = -sdot(lf, lpos) + 0.1f;
+    f.an[4][0] = fabsf(lf.x); f.an[4][1] = fabsf(lf.y); f.an[4][2] = fabsf(lf.z);
+    const v3 nlf = mk3(-lf.x, -lf.y, -lf.z);
+    f.n[5][0] = nlf.x; f.n[5][1] = nlf.y; f.n[5][2] = nlf.z; f.d[5] = -sdot(nlf, lpos) + lrad;
+    f.an[5][0] = f.an[4][0]; f.an[5][1] = f.an[4][1]; f.an[5][2] = f.an[4][2];
+    return !invalid;
+}
+
+/* status bits */
+#define OCC_STACK_OVERFLOW 1u
+#define OCC_UNDEFINED_FRUSTUM 2u
+
+__global__ void __launch_bounds__(OCC_WARPS * 32)
+k_occlusion(const sftg_frame* __restrict__ F, uint8_t* __restrict__ light_vis, uint32_t* __restrict__ status)
+{
+    __shared__ uint32_t s_tstack[OCC_WARPS][OCC_STACK];
+    __shared__ uint32_t s_bstack[OCC_WARPS][OCC_STACK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t pc = F->n_proxies;
+    const uint32_t lc = min(F->n_point, 64u);
+    const uint32_t nbatch = (pc + 7) / 8;
+    const uint32_t item = blockIdx.x * OCC_WARPS + warp;
+    if (item >= lc * nbatch) return;
+    const uint32_t l = item / nbatch, pb = (item % nbatch) * 8;
+    const sftg_point_light L = F->point[l];
+    const v3 lpos = mk3(L.pos[0], L.pos[1], L.pos[2]);
+
+    /* batch centre and light-disk targets (8178-8210), computed identically on every lane */
+    v3 bc = mk3(0.f, 0.f, 0.f); int na = 0;
+    for (int k = 0; k < 8; k++) {
+        if (pb + k >= pc) continue;
+        const sftg_proxy px = F->proxies[pb + k];
+        bc.x = bc.x + (px.posa[0] + px.posb[0]) * 0.5f; bc.y = bc.y + (px.posa[1] + px.posb[1]) * 0.5f; bc.z = bc.z + (px.posa[2] + px.posb[2]) * 0.5f;
+        na++;
+    }
+    if (na > 0) bc = scl3(bc, fdiv(1.f, (float)na));
+    const v3 ldir = snorm(sub3(lpos, bc));
+    float mnv = fabsf(ldir.x); v3 card = mk3(1.f, 0.f, 0.f);
+    if (fabsf(ldir.y) < mnv) { mnv = fabsf(ldir.y); card = mk3(0.f, 1.f, 0.f); }
+    if (fabsf(ldir.z) < mnv) card = mk3(0.f, 0.f, 1.f);
+    const v3 perp = mk3(ldir.y * card.z - ldir.z * card.y, ldir.z * card.x - ldir.x * card.z, ldir.x * card.y - ldir.y * card.x);
+    const v3 lright = snorm(perp);
+    const v3 lup = cross3(lright, ldir);
+    const float r = 0.1f;
+    const v3 tg[3] = {
+        add3(lpos, scl3(lup, r)),
+        add3(lpos, add3(scl3(lright, r * 0.866025f), scl3(lup, -r * 0.5f))),
+        add3(lpos, add3(scl3(lright, -r * 0.866025f), scl3(lup, -r * 0.5f))),
+    };
+    int occluded = 0;   /* lane k < 8: rays of proxy pb + k found blocked */
+    for (int ray = 0; ray < 3; ray++) {
+        float ox[8], oy[8], oz[8], lx[8], ly[8], lz[8];
+        uint32_t am = 0;
+        for (int k = 0; k < 8; k++) {
+            if (pb + k < pc) {
+                const sftg_proxy px = F->proxies[pb + k];
+                float x, y, z;
+                if (ray == 0) { x = px.posa[0]; y = px.posa[1]; z = px.posa[2]; }
+                else if (ray == 1) { x = px.posb[0]; y = px.posb[1]; z = px.posb[2]; }
+                else { x = (px.posa[0] + px.posb[0]) * 0.5f; y = (px.posa[1] + px.posb[1]) * 0.5f; z = (px.posa[2] + px.posb[2]) * 0.5f; }
+                ox[k] = x; oy[k] = y; oz[k] = z;
+                lx[k] = tg[ray].x - x; ly[k] = tg[ray].y - y; lz[k] = tg[ray].z - z;
+                am |= 1u << k;
+            } else { ox[k] = oy[k] = oz[k] = lx[k] = ly[k] = lz[k] = 0.f; }
+        }
+        /* sft__trace_shadow_packet (4086-4243), static instances only */
+        frustum6 pf;
+        if (!packet_frustum(ox, oy, oz, am, lpos, L.radius, pf) && lane == 0) atomicOr(status, OCC_UNDEFINED_FRUSTUM);
+        /* this lane's ray (lanes 0-7) */
+        const int rl = lane & 7;
+        const v3 my_o = mk3(ox[rl], oy[rl], oz[rl]);
+        const v3 my_e = mk3(ox[rl] + lx[rl], oy[rl] + ly[rl], oz[rl] + lz[rl]);
+        uint32_t sat = 0;
+        const uint32_t full = am;
+        int ttop = 0;
+        if (lane == 0) s_tstack[warp][0] = F->tlas_root;
+        ttop = 1;
+        __syncwarp();
+        bool done = (am == 0) || (F->tlas_count == 0);
+        uint32_t guard = 0;
+        while (!done && ttop > 0) {
+            const uint32_t tni = s_tstack[warp][--ttop];
+            __syncwarp();
+            const sftg_bvh_node* tn = &F->tlas[tni];
+            uint32_t th = node_mask(tn, pf, lane);
+            while (th && !done) {
+                const int tl = __ffs(th) - 1; th &= th - 1;
+                const uint32_t ch = tn->child[tl];
+                if (ch == SFTG_INVALID) continue;
+                if (!tn->leaf) {
+                    if (ttop >= OCC_STACK || ch >= F->tlas_count) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); done = true; break; }
+                    if (lane == 0) s_tstack[warp][ttop] = ch;
+                    ttop++;
+                    __syncwarp();
+                    continue;
+                }
+                const uint32_t ii = ch & ~0x80000000u;
+                const sftg_inst* I = &F->inst[ii];
+                const sftg_model Md = F->models[I->model];
+                if (Md.bone_count > 0 || Md.blas_count == 0) continue;
+                const float* M = I->T;
+                frustum6 mf;
+                for (int p = 0; p < 6; p++) {
+                    const float nx = pf.n[p][0], ny = pf.n[p][1], nz = pf.n[p][2], d = pf.d[p];
+                    const float nmx = nx * M[0] + ny * M[1] + nz * M[2];
+                    const float nmy = nx * M[4] + ny * M[5] + nz * M[6];
+                    const float nmz = nx * M[8] + ny * M[9] + nz * M[10];
+                    const float dot_t = nx * M[12] + ny * M[13] + nz * M[14];
+                    const float dm = dot_t + d;
+                    const float il = fdiv(1.f, fsqrt(nmx * nmx + nmy * nmy + nmz * nmz));
+                    mf.n[p][0] = nmx * il; mf.n[p][1] = nmy * il; mf.n[p][2] = nmz * il;
+                    mf.d[p] = dm * il;
+                    mf.an[p][0] = fabsf(nmx * il); mf.an[p][1] = fabsf(nmy * il); mf.an[p][2] = fabsf(nmz * il);
+                }
+                /* sft_m_qinv (1693-1712) */
+                float im[16];
+                im[0] = M[0]; im[1] = M[4]; im[2] = M[8]; im[3] = 0.f;
+                im[4] = M[1]; im[5] = M[5]; im[6] = M[9]; im[7] = 0.f;
+                im[8] = M[2]; im[9] = M[6]; im[10] = M[10]; im[11] = 0.f;
+                for (int a = 0; a < 3; a++) im[12 + a] = -(M[12] * im[a] + M[13] * im[4 + a] + M[14] * im[8 + a]);
+                im[15] = 1.f;
+                const v3 lo = xform(my_o, im);
+                const v3 le = xform(my_e, im);
+                const v3 Lv = sub3(le, lo);
+                const float tmax = fsqrt(vdot(Lv, Lv));
+                const v3 ld = vnorm_fast(Lv);
+                int btop = 0;
+                if (lane == 0) s_bstack[warp][0] = Md.blas_root;
+                btop = 1;
+                __syncwarp();
+                const sftg_bvh_node* blas = F->blas + Md.blas_base;
+                while (!done && btop > 0) {
+                    const uint32_t bni = s_bstack[warp][--btop];
+                    __syncwarp();
+                    const sftg_bvh_node* bn = &blas[bni];
+                    uint32_t bh = node_mask(bn, mf, lane);
+                    while (bh) {
+                        const int bl = __ffs(bh) - 1; bh &= bh - 1;
+                        const uint32_t bc2 = bn->child[bl];
+                        if (bc2 == SFTG_INVALID) continue;
+                        if (!bn->leaf) {
+                            if (btop >= OCC_STACK || bc2 >= Md.blas_count || ++guard > (1u << 24)) {
+                                if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); done = true; break;
+                            }
+                            if (lane == 0) s_bstack[warp][btop] = bc2;
+                            btop++;
+                            __syncwarp();
+                            continue;
+                        }
+                        const uint32_t pay = bc2 & ~0x80000000u;
+                        const uint32_t g = I->meshlet_base + (pay >> 7), t = pay & 0x7F;
+                        const uint8_t* ind = F->ml_inds + (size_t)g * 512;
+                        const float* at = F->ml_attr + (size_t)g * 640;
+                        const uint32_t tb = t >> 3, tl2 = t & 7;
+                        const uint32_t i0 = ind[tb * 32 + tl2], i1 = ind[tb * 32 + 8 + tl2], i2 = ind[tb * 32 + 16 + tl2];
+                        const v3 v0 = mk3(at[i0], at[64 + i0], at[128 + i0]);
+                        const v3 v1 = mk3(at[i1], at[64 + i1], at[128 + i1]);
+                        const v3 v2 = mk3(at[i2], at[64 + i2], at[128 + i2]);
+                        /* sft__ray_packet_vs_triangle_any_hit, lane = ray */
+                        const uint32_t cur = am & ~sat;
+                        const v3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
+                        const v3 h = cross3(ld, e2);
+                        const float a = vdot(e1, h);
+                        bool hit = lane < 8 && ((cur >> rl) & 1u) && (fabsf(a) > 1e-6f);
+                        const float fr = rcpr(a);
+                        const v3 s = sub3(lo, v0);
+                        const float u = fr * vdot(s, h);
+                        hit = hit && u >= 0.f && u <= 1.f;
+                        const v3 q = cross3(s, e1);
+                        const float v = fr * vdot(ld, q);
+                        hit = hit && v >= 0.f && (u + v) <= 1.f;
+                        const float tt = fr * vdot(e2, q);
+                        hit = hit && tt > 1e-6f && tt < tmax;
+                        sat |= __ballot_sync(0xFFFFFFFFu, hit) & 0xFFu;
+                        if (sat == full) { done = true; break; }
+                    }
+                }
+            }
+        }
+        if (lane < 8) occluded += (sat >> lane) & 1u;
+    }
+    if (lane < 8 && pb + lane < pc) light_vis[(size_t)(pb + lane) * 64 + l] = (uint8_t)(3 - occluded);
+}

@@ -1,0 +1,709 @@
+/*
+ * k_tile: one CTA per 64x64 tile rasterises the tile's payload list into a shared-memory
+ * visibility buffer and resolves it to ARGB8888 (sft__worker_phase_rasterize, sofren2.c:6756-6813,
+ * sft__rast_simd_batch 5148-5499, sft__resolve_tile 5809-6753).
+ *
+ * Raster.  The reference walks the list in order and keeps a sample when z > stored z
+ * (strict), so a sample ends holding the largest z, and among equal z the earliest triangle.
+ * That final state does not depend on the order triangles are visited, so each sample is a
+ * 64-bit word (z bits << 32 | ~order) updated with a shared-memory atomicMax, where order =
+ * list position * 8 + lane.  Only z > 0 ever wins (the buffer starts at 0).  Coverage and z
+ * are replayed bit-exactly: a group of 8 threads takes one triangle, thread l owns pixel
+ * column l of every aligned 8-pixel chunk and performs exactly the reference's incremental
+ * adds (row start + B per row, + 8A per chunk) and its trivial-accept / AA guard-band choices;
+ * the AA chunk skip is a group ballot.
+ *
+ * Resolve.  A group of 8 threads is one 4x2 pixel block (the reference's AVX2 lanes).  For
+ * each distinct triangle in the block (peeled in the reference's order) all 8 lanes shade it,
+ * because the reference's LOD uses the first covered lane's screen derivatives (neighbour
+ * lanes via shuffles) and its proxy loop skips a proxy for the whole block when no lane is
+ * affected (a ballot), which changes the smooth-max shadow of every lane.
+ */
+#include "sftg_types.h"
+#include "sftg_lane.cuh"
+#include "sftg_kernels.h"
+
+#define TILE_THREADS 256
+#define SETUP_CAP 256
+
+struct tri_setup {
+    float A[3], B[3], se[3];
+    float sz, dzdx, dzdy;
+    float pad[3];
+    int ax0, ax1, miny, maxy;
+    uint32_t order;
+    int trivial;
+};
+
+struct proxy_cache {   /* sft_light_proxy_cache (sofren2.c:991-998) */
+    float pa[3], pb[3], ab[3], W[3];
+    float abdab, wdw, rb2, pr, pr2, vis_mult;
+};
+
+struct tri_verts {
+    float sx[3], sy[3], iw[3], u[3], v[3], lu[3], lv[3], px[3], py[3], pz[3], nx[3], ny[3], nz[3];
+    uint32_t inst, m;
+};
+
+__constant__ float c_ms_ox4[4] = { -0.125f, 0.375f, -0.375f, 0.125f };
+__constant__ float c_ms_oy4[4] = { -0.375f, -0.125f, 0.125f, 0.375f };
+__constant__ float c_ms_ox2[2] = { -0.25f, 0.25f };
+__constant__ float c_ms_oy2[2] = { -0.25f, 0.25f };
+
+template <int S> SFTG_D float ms_ox(int s) { return S == 4 ? c_ms_ox4[s] : (S == 2 ? c_ms_ox2[s] : 0.f); }
+template <int S> SFTG_D float ms_oy(int s) { return S == 4 ? c_ms_oy4[s] : (S == 2 ? c_ms_oy2[s] : 0.f); }
+
+SFTG_D uint64_t zkey(float z, uint32_t order) { return ((uint64_t)__float_as_uint(z) << 32) | (uint64_t)(0xFFFFFFFFu - order); }
+
+/* vertices of one vis id (sofren2.c:5163-5209, 6199-6278) */
+SFTG_D void fetch_tri(const sftg_frame* F, const float* ss, const sftg_clip_tri* clips, uint32_t vid, tri_verts& t) {
+    if (vid & 0x80000000u) {
+        const sftg_clip_tri* c = &clips[vid & 0x7FFFFFFFu];
+        const float* src = c->sx; float* dst = t.sx;
+#pragma unroll
+        for (int i = 0; i < 39; i++) dst[i] = src[i];
+        t.inst = c->inst; t.m = c->m;
+        return;
+    }
+    const uint32_t ii = (vid >> 25) & 63, m = (vid >> 7) & 0x3FFFF, tri = vid & 127;
+    const sftg_inst* I = &F->inst[ii];
+    const uint32_t g = I->meshlet_base + m;
+    const uint8_t* ind = F->ml_inds + (size_t)g * 512;
+    const float* at = F->ml_attr + (size_t)g * 640;
+    const float* Sc = ss + (size_t)(I->ss_offset + m) * 576;
+    const uint32_t b = tri >> 3, l = tri & 7;
+    const uint32_t q[3] = { ind[b * 32 + l], ind[b * 32 + 8 + l], ind[b * 32 + 16 + l] };
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint32_t v = q[k];
+        t.sx[k] = Sc[v]; t.sy[k] = Sc[64 + v]; t.iw[k] = Sc[128 + v];
+        t.u[k] = at[384 + v]; t.v[k] = at[448 + v]; t.lu[k] = at[512 + v]; t.lv[k] = at[576 + v];
+        t.px[k] = Sc[192 + v]; t.py[k] = Sc[256 + v]; t.pz[k] = Sc[320 + v];
+        t.nx[k] = Sc[384 + v]; t.ny[k] = Sc[448 + v]; t.nz[k] = Sc[512 + v];
+    }
+    t.inst = ii; t.m = m;
+}
+
+/* edge / depth setup of one triangle lane (5211-5311), false when culled or off-tile */
+template <int S>
+SFTG_D bool tri_setup_one(float sx0, float sy0, float iw0, float sx1, float sy1, float iw1, float sx2, float sy2, float iw2,
+                          int tmx, int tmy, uint32_t order, tri_setup& T) {
+    const float A0 = sy0 - sy1, B0 = sx1 - sx0, A1 = sy1 - sy2, B1 = sx2 - sx1, A2 = sy2 - sy0, B2 = sx0 - sx2;
+    const float m01 = sx0 * sy1, m10 = sy0 * sx1, m12 = sx1 * sy2, m21 = sy1 * sx2, m20 = sx2 * sy0, m02 = sy2 * sx0;
+    const float C0 = (fma_(sx0, sy1, -m10) - fma_(sy0, sx1, -m01)) * 0.5f;
+    const float C1 = (fma_(sx1, sy2, -m21) - fma_(sy1, sx2, -m12)) * 0.5f;
+    const float C2 = (fma_(sx2, sy0, -m02) - fma_(sy2, sx0, -m20)) * 0.5f;
+    const float dx1 = sx1 - sx0, dx2 = sx2 - sx0, dy1 = sy1 - sy0, dy2 = sy2 - sy0;
+    const float det = dx1 * dy2 - dx2 * dy1;
+    if (!(det > 1e-6f)) return false;
+    const float idet = rcpr(det);
+    const float dzdx = ((iw1 - iw0) * dy2 - (iw2 - iw0) * dy1) * idet;
+    const float dzdy = ((iw2 - iw0) * dx1 - (iw1 - iw0) * dx2) * idet;
+    const float c0 = fma_(B0, 0.5f, fma_(A0, 0.5f, C0)), c1 = fma_(B1, 0.5f, fma_(A1, 0.5f, C1)), c2 = fma_(B2, 0.5f, fma_(A2, 0.5f, C2));
+    const float zb = fma_(0.5f - sy0, dzdy, fma_(0.5f - sx0, dzdx, iw0));
+    const int minx = cvtt(vmax(vmin(sx0, vmin(sx1, sx2)), (float)tmx));
+    const int maxx = cvtt(vmin(vmax(sx0, vmax(sx1, sx2)), (float)(tmx + SFTG_TILE - 1)));
+    const int miny = cvtt(vmax(vmin(sy0, vmin(sy1, sy2)), (float)tmy));
+    const int maxy = cvtt(vmin(vmax(sy0, vmax(sy1, sy2)), (float)(tmy + SFTG_TILE - 1)));
+    if (minx > maxx || miny > maxy) return false;
+    const int ax0 = minx & ~7, ax1 = (maxx & ~7) + 8;
+    T.A[0] = A0; T.A[1] = A1; T.A[2] = A2; T.B[0] = B0; T.B[1] = B1; T.B[2] = B2;
+    T.se[0] = c0 + A0 * (float)ax0 + B0 * (float)miny;
+    T.se[1] = c1 + A1 * (float)ax0 + B1 * (float)miny;
+    T.se[2] = c2 + A2 * (float)ax0 + B2 * (float)miny;
+    T.sz = zb + dzdx * (float)ax0 + dzdy * (float)miny;
+    T.dzdx = dzdx; T.dzdy = dzdy;
+    const float bw = (float)(ax1 - 1 - ax0), bh = (float)(maxy - miny);
+    const float me0 = T.se[0] + (A0 < 0.f ? A0 * bw : 0.f) + (B0 < 0.f ? B0 * bh : 0.f);
+    const float me1 = T.se[1] + (A1 < 0.f ? A1 * bw : 0.f) + (B1 < 0.f ? B1 * bh : 0.f);
+    const float me2 = T.se[2] + (A2 < 0.f ? A2 * bw : 0.f) + (B2 < 0.f ? B2 * bh : 0.f);
+    if (S > 1) {
+        T.pad[0] = 0.375f * (fabsf(A0) + fabsf(B0));
+        T.pad[1] = 0.375f * (fabsf(A1) + fabsf(B1));
+        T.pad[2] = 0.375f * (fabsf(A2) + fabsf(B2));
+        T.trivial = (me0 >= T.pad[0] && me1 >= T.pad[1] && me2 >= T.pad[2]);
+    } else {
+        T.pad[0] = T.pad[1] = T.pad[2] = 0.f;
+        T.trivial = (me0 >= 0.f && me1 >= 0.f && me2 >= 0.f);
+    }
+    T.ax0 = ax0; T.ax1 = ax1; T.miny = miny; T.maxy = maxy; T.order = order;
+    return true;
+}
+
+/* the incremental edge walk for pixel column `l` of one triangle (5345-5497) */
+template <int S>
+SFTG_D void tri_raster(const tri_setup& T, int l, uint32_t gmask, int tmx, int tmy, unsigned long long* keys) {
+    float de0[S], de1[S], de2[S], dz[S];
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        const float ox = ms_ox<S>(s), oy = ms_oy<S>(s);
+        de0[s] = T.A[0] * ox + T.B[0] * oy; de1[s] = T.A[1] * ox + T.B[1] * oy; de2[s] = T.A[2] * ox + T.B[2] * oy;
+        dz[s] = T.dzdx * ox + T.dzdy * oy;
+    }
+    const float fl = (float)l;
+    float e0r = T.se[0] + T.A[0] * fl, e1r = T.se[1] + T.A[1] * fl, e2r = T.se[2] + T.A[2] * fl;
+    float zr = T.sz + T.dzdx * fl;
+    const float a0c = T.A[0] * 8.f, a1c = T.A[1] * 8.f, a2c = T.A[2] * 8.f, zc = T.dzdx * 8.f;
+    const float np0 = -T.pad[0], np1 = -T.pad[1], np2 = -T.pad[2];
+    const uint32_t order = T.order;
+    for (int y = T.miny; y <= T.maxy; y++) {
+        float e0 = e0r, e1 = e1r, e2 = e2r, z = zr;
+        int pi = (y - tmy) * SFTG_TILE + (T.ax0 - tmx) + l;
+        for (int x = T.ax0; x < T.ax1; x += 8, pi += 8) {
+            if (T.trivial) {
+#pragma unroll
+                for (int s = 0; s < S; s++) {
+                    const float zs = (S > 1) ? z + dz[s] : z;
+                    if (zs > 0.f) atomicMax(&keys[s * SFTG_TILE_PX + pi], zkey(zs, order));
+                }
+            } else if (S == 1) {
+                if (e0 >= 0.f && e1 >= 0.f && e2 >= 0.f && z > 0.f) atomicMax(&keys[pi], zkey(z, order));
+            } else {
+                const bool might = (e0 >= np0 && e1 >= np1 && e2 >= np2);
+                if (__ballot_sync(gmask, might) & gmask) {
+#pragma unroll
+                    for (int s = 0; s < S; s++) {
+                        const float a = e0 + de0[s], b = e1 + de1[s], c = e2 + de2[s];
+                        if (a >= 0.f && b >= 0.f && c >= 0.f) {
+                            const float zs = z + dz[s];
+                            if (zs > 0.f) atomicMax(&keys[s * SFTG_TILE_PX + pi], zkey(zs, order));
+                        }
+                    }
+                }
+            }
+            e0 = e0 + a0c; e1 = e1 + a1c; e2 = e2 + a2c; z = z + zc;
+        }
+        e0r = e0r + T.B[0]; e1r = e1r + T.B[1]; e2r = e2r + T.B[2]; zr = zr + T.dzdy;
+    }
+}
+
+/* ---------------------------------------------------------------- texture sampling */
+SFTG_D uint32_t tex_addr(const sftg_tex& t, int lod, int u, int v) {
+    const uint32_t uu = (uint32_t)u, vv = (uint32_t)v;
+    if (t.is_pot) return ((((vv >> 2) << t.shift[lod]) + (uu >> 2)) << 4) + ((vv & 3u) << 2) + (uu & 3u);
+    return ((((vv >> 2) * (uint32_t)t.bw[lod]) + (uu >> 2)) << 4) + ((vv & 3u) << 2) + (uu & 3u);
+}
+
+/* sft__sample_tex_bilinear (5543-5660) */
+SFTG_D void sample_bilinear(const sftg_frame* F, int ti, int lod, float cu, float cv, float& r, float& g, float& b) {
+    if (ti < 0) { r = g = b = 1.f; return; }
+    const sftg_tex& t = F->texs[ti];
+    const int w = max(t.w >> lod, 1), h = max(t.h >> lod, 1);
+    const float upx = cu * (float)w - 0.5f, vpx = cv * (float)h - 0.5f;
+    const float uf0 = floorf(upx), vf0 = floorf(vpx);
+    const float ufr = upx - uf0, vfr = vpx - vf0;
+    const int u0 = cvtt(uf0), v0 = cvtt(vf0);
+    const int wm = w - 1, hm = h - 1;
+    int u0w, v0w, u1, v1;
+    if (t.is_pot) { u1 = (u0 + 1) & wm; v1 = (v0 + 1) & hm; u0w = u0 & wm; v0w = v0 & hm; }
+    else { u1 = min(u0 + 1, wm); v1 = min(v0 + 1, hm); u0w = min(u0, wm); v0w = min(v0, hm); }
+    const uint32_t* base = F->texels + t.offs[lod];
+    const uint32_t c00 = __ldg(&base[tex_addr(t, lod, u0w, v0w)]), c10 = __ldg(&base[tex_addr(t, lod, u1, v0w)]);
+    const uint32_t c01 = __ldg(&base[tex_addr(t, lod, u0w, v1)]), c11 = __ldg(&base[tex_addr(t, lod, u1, v1)]);
+    const float i255 = 1.f / 255.f;
+    float out[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int sh = 16 - 8 * k;
+        const float f00 = (float)((c00 >> sh) & 255u) * i255, f10 = (float)((c10 >> sh) & 255u) * i255;
+        const float f01 = (float)((c01 >> sh) & 255u) * i255, f11 = (float)((c11 >> sh) & 255u) * i255;
+        const float top = f00 + (f10 - f00) * ufr, bot = f01 + (f11 - f01) * ufr;
+        out[k] = top + (bot - top) * vfr;
+    }
+    r = out[0]; g = out[1]; b = out[2];
+}
+
+/* sft__sample_tex_nearest (5662-5729) */
+SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float cv, float& r, float& g, float& b) {
+    if (ti < 0) { r = g = b = 1.f; return; }
+    const sftg_tex& t = F->texs[ti];
+    const int w = max(t.w >> lod, 1), h = max(t.h >> lod, 1);
+    const int u0 = cvtt(floorf(cu * (float)w)), v0 = cvtt(floorf(cv * (float)h));
+    const int wm = w - 1, hm = h - 1;
+    int uw, vw;
+    if (t.is_pot) { uw = u0 & wm; vw = v0 & hm; } else { uw = min(u0, wm); vw = min(v0, hm); }
+    const uint32_t c = __ldg(&F->texels[t.offs[lod] + tex_addr(t, lod, uw, vw)]);
+    const float i255 = 1.f / 255.f;
+    r = (float)((c >> 16) & 255u) * i255; g = (float)((c >> 8) & 255u) * i255; b = (float)(c & 255u) * i255;
+}
+
+/* ---------------------------------------------------------------- the tile kernel */
+template <int S>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sftg_clip_tri* __restrict__ clips,
+       const uint32_t* __restrict__ tile_start, const uint32_t* __restrict__ tile_count, const uint64_t* __restrict__ tile_pay,
+       const uint8_t* __restrict__ light_vis, uint32_t* __restrict__ color, float* __restrict__ vis_depth,
+       uint32_t* __restrict__ vis_id, float* __restrict__ shadow_out)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
+    unsigned char* aux = smem + (size_t)S * SFTG_TILE_PX * 8;
+    tri_setup* setups = (tri_setup*)aux;                                    /* raster phase */
+    proxy_cache* pcache = (proxy_cache*)aux;                                /* resolve phase [16][16] */
+    __shared__ uint32_t s_nsetup, s_next;
+    __shared__ float s_red[2][TILE_THREADS / 32];
+    __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
+    __shared__ int s_nlights;
+    __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
+
+    const int tile = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
+    uint32_t count = tile_count[tile];
+    if ((uint64_t)tile_start[tile] + count > F->tile_cap) count = 0;   /* overflowed frame, redone by the host */
+    const uint64_t* list = tile_pay + tile_start[tile];
+
+    for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) keys[i] = 0ull;
+
+    /* ---------------- raster ---------------- */
+    const int grp_lane = tid & 7;
+    const uint32_t gmask = 0xFFu << (lane & ~7);
+    for (uint32_t pbase = 0; pbase < count; pbase += SETUP_CAP / 8) {
+        if (tid == 0) { s_nsetup = 0; s_next = 0; }
+        __syncthreads();
+        {
+            const uint32_t p = pbase + (tid >> 3);
+            const int l = grp_lane;
+            if (p < count) {
+                const uint64_t pay = list[p];
+                const uint32_t raw = (uint32_t)(pay >> 56);
+                float sx[3], sy[3], iw[3];
+                bool active;
+                if (!raw) {
+                    active = (l == 0);
+                    if (active) {
+                        const sftg_clip_tri* c = &clips[(uint32_t)(pay & 0xFFFFFFFFu)];
+#pragma unroll
+                        for (int k = 0; k < 3; k++) { sx[k] = c->sx[k]; sy[k] = c->sy[k]; iw[k] = c->iw[k]; }
+                    }
+                } else {
+                    active = (raw >> l) & 1u;
+                    if (active) {
+                        const uint32_t ii = (uint32_t)(pay & 0xFFFFFF), m = (uint32_t)((pay >> 24) & 0xFFFFFF), b = (uint32_t)((pay >> 48) & 0xFF);
+                        const sftg_inst* I = &F->inst[ii];
+                        const uint32_t g = I->meshlet_base + m;
+                        const uint8_t* ind = F->ml_inds + (size_t)g * 512;
+                        const float* Sc = ss + (size_t)(I->ss_offset + m) * 576;
+                        const uint32_t q[3] = { ind[b * 32 + l], ind[b * 32 + 8 + l], ind[b * 32 + 16 + l] };
+#pragma unroll
+                        for (int k = 0; k < 3; k++) { sx[k] = Sc[q[k]]; sy[k] = Sc[64 + q[k]]; iw[k] = Sc[128 + q[k]]; }
+                    }
+                }
+                if (active) {
+                    tri_setup T;
+                    if (tri_setup_one<S>(sx[0], sy[0], iw[0], sx[1], sy[1], iw[1], sx[2], sy[2], iw[2], tmx, tmy, p * 8 + l, T)) {
+                        const uint32_t slot = atomicAdd(&s_nsetup, 1u);
+                        setups[slot] = T;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t nset = s_nsetup;
+        while (true) {
+            uint32_t idx = 0;
+            if (grp_lane == 0) idx = atomicAdd(&s_next, 1u);
+            idx = __shfl_sync(gmask, idx, lane & ~7);
+            if (idx >= nset) break;
+            const tri_setup T = setups[idx];
+            tri_raster<S>(T, grp_lane, gmask, tmx, tmy, keys);
+        }
+        __syncthreads();
+    }
+
+    /* ---------------- decode the visibility buffer ---------------- */
+    float zmin = 1e9f, zmax = -1e9f;
+    for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) {
+        const unsigned long long k = keys[i];
+        float d = 0.f; uint32_t vid = SFTG_INVALID;
+        if (k) {
+            d = __uint_as_float((uint32_t)(k >> 32));
+            const uint32_t order = 0xFFFFFFFFu - (uint32_t)k;
+            const uint64_t pay = list[order >> 3];
+            if ((pay >> 56) == 0) vid = (uint32_t)pay | 0x80000000u;
+            else vid = ((uint32_t)(pay & 0xFFFFFF) << 25) | ((uint32_t)((pay >> 24) & 0xFFFFFF) << 7) | ((uint32_t)((pay >> 48) & 0xFF) * 8 + (order & 7));
+        }
+        ((float2*)keys)[i] = make_float2(d, __uint_as_float(vid));
+        if (vis_id) {
+            vis_depth[(size_t)tile * S * SFTG_TILE_PX + i] = d;
+            vis_id[(size_t)tile * S * SFTG_TILE_PX + i] = vid;
+        }
+        if (d > 0.0001f) { zmin = fminf(zmin, d); zmax = fmaxf(zmax, d); }
+    }
+    /* D1: tile depth bounds (5820-5853) */
+#pragma unroll
+    for (int o = 16; o; o >>= 1) { zmin = fminf(zmin, __shfl_xor_sync(0xFFFFFFFFu, zmin, o)); zmax = fmaxf(zmax, __shfl_xor_sync(0xFFFFFFFFu, zmax, o)); }
+    if (lane == 0) { s_red[0][warp] = zmin; s_red[1][warp] = zmax; }
+    __syncthreads();
+    zmin = 1e9f; zmax = -1e9f;
+#pragma unroll
+    for (int w = 0; w < TILE_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
+
+    /* D2: tile light list, first 16 lights in index order that pass (5855-5934) */
+    if (warp == 0) {
+        int n = 0;
+        if (zmin <= zmax && F->n_point > 0) {
+            const float* vp = F->vp;
+            for (uint32_t base = 0; base < F->n_point && n < SFTG_MAX_TILE_LIGHTS; base += 32) {
+                const uint32_t l = base + lane;
+                bool pass = false;
+                if (l < F->n_point) {
+                    const sftg_point_light L = F->point[l];
+                    const float w = L.pos[0] * vp[3] + L.pos[1] * vp[7] + L.pos[2] * vp[11] + vp[15];
+                    const float lmin = w - L.radius, lmax = w + L.radius;
+                    pass = !(lmax <= 1e-6f);
+                    if (pass) {
+                        const float smin = (lmin > 1e-6f) ? lmin : 1e-6f;
+                        const float iwmin = fdiv(1.f, lmax), iwmax = fdiv(1.f, smin);
+                        if (iwmax < zmin || iwmin > zmax) pass = false;
+                    }
+                    if (pass && w > L.radius) {
+                        const float tx = L.pos[0] * vp[0] + L.pos[1] * vp[4] + L.pos[2] * vp[8] + vp[12];
+                        const float ty = L.pos[0] * vp[1] + L.pos[1] * vp[5] + L.pos[2] * vp[9] + vp[13];
+                        const float sx = (fdiv(tx, w) + 1.f) * F->hw + F->vpx;
+                        const float sy = (fdiv(-ty, w) + 1.f) * F->hh + F->vpy;
+                        const float psx = fsqrt(vp[0] * vp[0] + vp[4] * vp[4] + vp[8] * vp[8]);
+                        const float psy = fsqrt(vp[1] * vp[1] + vp[5] * vp[5] + vp[9] * vp[9]);
+                        const float safe_w = (w - L.radius) > 1e-6f ? (w - L.radius) : 1e-6f;
+                        const float rx = fdiv((L.radius * psx) + fabsf(tx) * fdiv(L.radius, w), safe_w) * F->hw;
+                        const float ry = fdiv((L.radius * psy) + fabsf(ty) * fdiv(L.radius, w), safe_w) * F->hh;
+                        if (sx + rx < (float)tmx || sx - rx > (float)(tmx + SFTG_TILE) || sy + ry < (float)tmy || sy - ry > (float)(tmy + SFTG_TILE)) pass = false;
+                    }
+                }
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
+                const int rank = __popc(bal & ((1u << lane) - 1u));
+                if (pass && n + rank < SFTG_MAX_TILE_LIGHTS) s_lights[n + rank] = (uint16_t)l;
+                n = min(SFTG_MAX_TILE_LIGHTS, n + __popc(bal));
+            }
+        }
+        if (lane == 0) s_nlights = n;
+    }
+    __syncthreads();
+    const int ntl = s_nlights;
+
+    /* D3: per light, the first 16 proxies that see it and can reach it (5936-5990) */
+    for (int i = warp; i < SFTG_MAX_TILE_LIGHTS; i += TILE_THREADS / 32) {
+        int n = 0;
+        if (i < ntl && F->shadows && F->n_proxies > 0) {
+            const sftg_point_light L = F->point[s_lights[i]];
+            for (uint32_t base = 0; base < F->n_proxies && n < SFTG_MAX_LIGHT_PROXIES; base += 32) {
+                const uint32_t p = base + lane;
+                bool take = false; uint8_t vs = 0;
+                v3 cc, ab, Wv; float br = 0.f, d2 = 0.f;
+                sftg_proxy px;
+                if (p < F->n_proxies) {
+                    px = F->proxies[p];
+                    vs = light_vis[(size_t)p * 64 + s_lights[i]];
+                    if (vs) {
+                        cc = mk3((px.posa[0] + px.posb[0]) * 0.5f, (px.posa[1] + px.posb[1]) * 0.5f, (px.posa[2] + px.posb[2]) * 0.5f);
+                        ab = mk3(px.posb[0] - px.posa[0], px.posb[1] - px.posa[1], px.posb[2] - px.posa[2]);
+                        const float cl = fsqrt(sdot(ab, ab));
+                        br = px.radius + (cl * 0.5f);
+                        const float cr = br + L.radius;
+                        Wv = sub3(cc, mk3(L.pos[0], L.pos[1], L.pos[2]));
+                        d2 = sdot(Wv, Wv);
+                        take = d2 <= cr * cr;
+                    }
+                }
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, take);
+                const int rank = __popc(bal & ((1u << lane) - 1u));
+                if (take && n + rank < SFTG_MAX_LIGHT_PROXIES) {
+                    proxy_cache* q = &pcache[i * SFTG_MAX_LIGHT_PROXIES + n + rank];
+                    q->pa[0] = px.posa[0]; q->pa[1] = px.posa[1]; q->pa[2] = px.posa[2];
+                    q->pb[0] = px.posb[0]; q->pb[1] = px.posb[1]; q->pb[2] = px.posb[2];
+                    q->ab[0] = ab.x; q->ab[1] = ab.y; q->ab[2] = ab.z;
+                    q->W[0] = Wv.x; q->W[1] = Wv.y; q->W[2] = Wv.z;
+                    q->abdab = sdot(ab, ab); q->wdw = d2; q->rb2 = br * br; q->pr = px.radius; q->pr2 = px.radius * px.radius;
+                    q->vis_mult = (float)vs * 0.3333333f;
+                }
+                n = min(SFTG_MAX_LIGHT_PROXIES, n + __popc(bal));
+            }
+        }
+        if (lane == 0) s_npc[i] = (uint8_t)n;
+    }
+    __syncthreads();
+
+    /* ---------------- resolve: one 8-thread group per 4x2 block ---------------- */
+    const int W = F->width, H = F->height;
+    const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
+    const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
+    const float2* vis = (const float2*)keys;
+    const int grp = tid >> 3, gl = tid & 7, gshift = lane & ~7;
+    const int ix = gl & 3, iy = gl >> 2;
+    const float inv_s = 1.f / (float)S;
+    const uint32_t cc = F->clear_color;
+    const float clr[3] = { (float)((cc >> 16) & 0xFF) * (1.f / 255.f), (float)((cc >> 8) & 0xFF) * (1.f / 255.f), (float)(cc & 0xFF) * (1.f / 255.f) };
+    const v3 cam = mk3(F->cam[0], F->cam[1], F->cam[2]);
+
+    for (int blk = grp; blk < 16 * 32; blk += TILE_THREADS / 8) {
+        const int x = tmx + (blk & 15) * 4, y = tmy + (blk >> 4) * 2;
+        if (x >= lim_x || y >= lim_y) continue;
+        const int gx = x + ix, gy = y + iy;
+        const bool inb = (sw > gx) && (sh > gy);
+        const int pind = (gy - tmy) * SFTG_TILE + (gx - tmx);
+        const float pxf = ((float)x + 0.5f) + (float)ix, pyf = ((float)y + 0.5f) + (float)iy;
+        uint32_t vids[S];
+        uint32_t asm_[S];
+        int ecount = 0;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            vids[s] = __float_as_uint(vis[s * SFTG_TILE_PX + pind].y);
+            const bool empty = vids[s] == SFTG_INVALID;
+            asm_[s] = (__ballot_sync(gmask, !empty && inb) >> gshift) & 0xFFu;
+            ecount += (empty && inb);
+        }
+        uint32_t act = 0;
+#pragma unroll
+        for (int s = 0; s < S; s++) act |= asm_[s];
+        float acc[3] = { 0.f, 0.f, 0.f };
+        if (S == 1) {
+            if (F->clear && inb && vids[0] == SFTG_INVALID) color[gy * W + gx] = cc;
+        } else {
+            if (!act) {
+                if (F->clear && inb) color[gy * W + gx] = cc;
+                continue;
+            }
+            const float ew = (float)ecount * inv_s;
+            const bool any_e = (__ballot_sync(gmask, ew > 0.f) & gmask) != 0;
+            if (F->clear) { acc[0] = clr[0] * ew; acc[1] = clr[1] * ew; acc[2] = clr[2] * ew; }
+            else if (any_e) {
+                float bg[3] = { 0.f, 0.f, 0.f };
+                if (gx < sw && gy < sh) {
+                    const uint32_t q = color[gy * W + gx];
+                    bg[0] = (float)((q >> 16) & 0xFF) * (1.f / 255.f); bg[1] = (float)((q >> 8) & 0xFF) * (1.f / 255.f); bg[2] = (float)(q & 0xFF) * (1.f / 255.f);
+                }
+                acc[0] = bg[0] * ew; acc[1] = bg[1] * ew; acc[2] = bg[2] * ew;
+            }
+        }
+        const uint32_t block_write = act;
+        while (act) {
+            uint32_t target, tri_mask = 0, tri_lanes = 0; int hits = 0;
+            if (S == 1) {
+                const int fl = __ffs(act) - 1;
+                target = __shfl_sync(gmask, vids[0], gshift + fl);
+                tri_mask = (__ballot_sync(gmask, vids[0] == target && inb) >> gshift) & 0xFFu;
+                tri_lanes = tri_mask & act;
+                act &= ~tri_lanes;
+            } else {
+                int fs = 0;
+                while (!asm_[fs]) fs++;
+                const int fl = __ffs(asm_[fs]) - 1;
+                uint32_t vsel = vids[0];
+#pragma unroll
+                for (int s = 1; s < S; s++) if (s == fs) vsel = vids[s];
+                target = __shfl_sync(gmask, vsel, gshift + fl);
+#pragma unroll
+                for (int s = 0; s < S; s++) {
+                    const bool match = vids[s] == target && inb;
+                    const uint32_t mb = (__ballot_sync(gmask, match) >> gshift) & 0xFFu;
+                    const uint32_t mm = mb & asm_[s];
+                    asm_[s] &= ~mm; tri_lanes |= mm; tri_mask |= mb;
+                    hits += match;
+                }
+                act = 0;
+#pragma unroll
+                for (int s = 0; s < S; s++) act |= asm_[s];
+            }
+            const bool in_tri = (tri_mask >> gl) & 1u;
+            tri_verts T;
+            fetch_tri(F, ss, clips, target, T);
+            const sftg_inst* I = &F->inst[T.inst];
+            const sftg_meshlet_info info = F->ml_info[I->meshlet_base + T.m];
+            /* D6 barycentrics and perspective-correct interpolation (6282-6347) */
+            const float dx1 = T.sx[1] - T.sx[0], dx2 = T.sx[2] - T.sx[0], dy1 = T.sy[1] - T.sy[0], dy2 = T.sy[2] - T.sy[0];
+            const float idet = rcpr(dx1 * dy2 - dx2 * dy1);
+            const float pxs = pxf - T.sx[0], pys = pyf - T.sy[0];
+            const float rbu = (pxs * dy2 - pys * dx2) * idet;
+            const float rbv = (pys * dx1 - pxs * dy1) * idet;
+            const float rbw = (1.f - rbu) - rbv;
+            float bu = rbu, bv = rbv, bw = rbw;
+            if (S > 1) {
+                bu = vmax(0.f, rbu); bv = vmax(0.f, rbv); bw = vmax(0.f, rbw);
+                const float bs = rcpr(bu + (bv + bw));
+                bu = bu * bs; bv = bv * bs; bw = bw * bs;
+            }
+            const float iz = fma_(bw, T.iw[0], fma_(bu, T.iw[1], bv * T.iw[2]));
+            const float z = rcpr(iz);
+            const float w0 = (bw * T.iw[0]) * z, w1 = (bu * T.iw[1]) * z, w2 = (bv * T.iw[2]) * z;
+#define INTERP(a) fma_(w0, (a)[0], fma_(w1, (a)[1], w2 * (a)[2]))
+            const float cu = INTERP(T.u), cv = INTERP(T.v), clu = INTERP(T.lu), clv = INTERP(T.lv);
+            const v3 P = mk3(INTERP(T.px), INTERP(T.py), INTERP(T.pz));
+            const v3 N = vnorm_fast(mk3(INTERP(T.nx), INTERP(T.ny), INTERP(T.nz)));
+#undef INTERP
+            const v3 V = vnorm_fast(sub3(cam, P));
+            /* material (6350-6382) */
+            uint32_t base = 0xFFFFFFFFu; int ti = -1; float shin = 4.f;
+            if (info.material >= 0) { const sftg_mat mt = F->mats[info.material]; base = mt.base_color; ti = mt.tex; shin = mt.shininess; }
+            const float i255 = 1.f / 255.f;
+            const float bcol[3] = { (float)((base >> 16) & 0xFF) * i255, (float)((base >> 8) & 0xFF) * i255, (float)(base & 0xFF) * i255 };
+            /* D7 LOD from the first covered lane's derivatives (5501-5541) */
+            int lod = 0;
+            {
+                const int fl = __ffs(tri_mask) - 1;
+                const float cu_f = __shfl_sync(gmask, cu, gshift + fl), cv_f = __shfl_sync(gmask, cv, gshift + fl);
+                const float cu_x = __shfl_sync(gmask, cu, gshift + (fl ^ 1)), cv_x = __shfl_sync(gmask, cv, gshift + (fl ^ 1));
+                const float cu_y = __shfl_sync(gmask, cu, gshift + (fl ^ 4)), cv_y = __shfl_sync(gmask, cv, gshift + (fl ^ 4));
+                if (ti >= 0) {
+                    const sftg_tex& tx = F->texs[ti];
+                    const float ux = (cu_f - cu_x) * (float)tx.w, vx = (cv_f - cv_x) * (float)tx.h;
+                    const float uy = (cu_f - cu_y) * (float)tx.w, vy = (cv_f - cv_y) * (float)tx.h;
+                    const float a1 = fabsf(ux) > fabsf(vx) ? fabsf(ux) : fabsf(vx);
+                    const float a2 = fabsf(uy) > fabsf(vy) ? fabsf(uy) : fabsf(vy);
+                    const float rho = a1 > a2 ? a1 : a2;
+                    if (rho > 1.f) {
+                        const float lf = (float)(31 - __clz((uint32_t)cvtt(rho)));
+                        lod = (int)((lf + 0.5f) + (-0.375f));
+                    }
+                    lod = lod < 0 ? 0 : (lod > tx.levels - 1 ? tx.levels - 1 : lod);
+                }
+            }
+            float out[3];
+            {
+                float tr, tg, tb;
+                if (lod > 1) sample_nearest(F, ti, lod, cu, cv, tr, tg, tb);
+                else sample_bilinear(F, ti, lod, cu, cv, tr, tg, tb);
+                out[0] = tr * bcol[0]; out[1] = tg * bcol[1]; out[2] = tb * bcol[2];
+            }
+            const bool lm = info.lightmap_tex >= 0;
+            if (shin < 0.f) {
+                out[0] = out[0] * (-shin); out[1] = out[1] * (-shin); out[2] = out[2] * (-shin);
+            } else {
+                const float sscale = ((shin + 8.f) / 8.f) * 0.04f;
+                float dif[3], spc[3] = { 0.f, 0.f, 0.f }, lms = 1.f;
+                if (lm) {
+                    sample_bilinear(F, info.lightmap_tex, 0, clu, clv, dif[0], dif[1], dif[2]);
+                    dif[0] = dif[0] * F->lightmap_brightness; dif[1] = dif[1] * F->lightmap_brightness; dif[2] = dif[2] * F->lightmap_brightness;
+                } else {
+                    dif[0] = F->ambient[0]; dif[1] = F->ambient[1]; dif[2] = F->ambient[2];
+                    for (uint32_t dl = 0; dl < F->n_dir; dl++) {
+                        const sftg_dir_light D = F->dir[dl];
+                        const v3 Ld = mk3(D.dir[0], D.dir[1], D.dir[2]);
+                        const float ndl = vmax(vdot(N, Ld), 0.f);
+                        dif[0] = fma_(ndl, D.color[0], dif[0]); dif[1] = fma_(ndl, D.color[1], dif[1]); dif[2] = fma_(ndl, D.color[2], dif[2]);
+                        if (ndl > 0.f) {
+                            const v3 Hh = vnorm_fast(add3(Ld, V));
+                            const float ndh = vmax(vdot(N, Hh), 0.f);
+                            const float den = (shin - shin * ndh) + ndh;
+                            const float sp = ndh * rcpr(den);
+                            const float term = (sp * sscale) * ndl;
+                            spc[0] = fma_(term, D.color[0], spc[0]); spc[1] = fma_(term, D.color[1], spc[1]); spc[2] = fma_(term, D.color[2], spc[2]);
+                        }
+                    }
+                }
+                /* D10 point lights and capsule shadows (6474-6607) */
+                for (int i = 0; i < ntl; i++) {
+                    const sftg_point_light L = F->point[s_lights[i]];
+                    const v3 Lr = sub3(mk3(L.pos[0], L.pos[1], L.pos[2]), P);
+                    const float d2 = vdot(Lr, Lr);
+                    float att = vmax(0.f, fma_(-d2, L.inv_radius_sqr, 1.f));
+                    att = att * att;
+                    const bool alive = att > 0.f;
+                    if (!(__ballot_sync(gmask, alive) & gmask)) continue;
+                    const v3 Ln = vnorm_fast(Lr);
+                    const float ndl = vmax(vdot(N, Ln), 0.f);
+                    const bool lit = (ndl > 0.f) && alive && in_tri;
+                    float msh = 0.f;
+                    const int np = s_npc[i];
+                    if (np > 0) {
+                        const float lrl = fsqrt(d2);
+                        const float bk = 0.2f, b4 = 0.25f / 0.2f;
+                        for (int pi = 0; pi < np; pi++) {
+                            const proxy_cache& q = pcache[i * SFTG_MAX_LIGHT_PROXIES + pi];
+                            const float wdv = 0.f - vdot(mk3(q.W[0], q.W[1], q.W[2]), Lr);
+                            const bool btw = wdv > 0.f && wdv < d2;
+                            const float tf = wdv * rcpr(d2);
+                            const float cd2 = fma_(-wdv, tf, q.wdw);
+                            const bool ray = btw && (cd2 < q.rb2) && (lm ? in_tri : lit);
+                            if (!(__ballot_sync(gmask, ray) & gmask)) continue;   /* block-level skip */
+                            const v3 pa = mk3(q.pa[0], q.pa[1], q.pa[2]), ab = mk3(q.ab[0], q.ab[1], q.ab[2]);
+                            const v3 ao = sub3(P, pa);
+                            const float abl = vdot(ab, Ln), abao = vdot(ab, ao), lao = vdot(Ln, ao);
+                            const float den = fma_(-abl, abl, q.abdab);
+                            const float sden = vmax(den, 1e-6f);
+                            float t2 = fma_(-abl, lao, abao) * rcpr(sden);
+                            t2 = vmax(0.f, vmin(t2, 1.f));
+                            const float t1 = fma_(t2, abl, -lao);
+                            const bool vc = t1 > 1e-6f && t1 < lrl;
+                            const v3 pr = add3(P, scl3(Ln, t1));
+                            const v3 pc = add3(pa, scl3(ab, t2));
+                            const v3 dd = sub3(pr, pc);
+                            const float dist2 = vdot(dd, dd);
+                            float sv = vmax(0.f, 1.f - fdiv(dist2, q.pr2));
+                            if (!ray || !vc) sv = 0.f;
+                            sv = sv * q.vis_mult;
+                            const float h = vmax(0.f, bk - fabsf(msh - sv));
+                            const float badd = (h * h) * b4;
+                            msh = vmax(msh, sv) + badd;
+                        }
+                    }
+                    const float si = vmax(0.f, 1.f - msh);
+                    if (shadow_out && S == 1 && ((tri_lanes >> gl) & 1u) && i < 16)
+                        shadow_out[((size_t)gy * W + gx) * 16 + i] = si;
+                    if (lm) {
+                        const float drop = (1.f - si) * att;
+                        lms = lms * (1.f - drop);
+                    } else {
+                        const float di = ndl * att;
+                        const float md = lit ? (di * si) : 0.f;
+                        dif[0] = fma_(md, L.color[0], dif[0]); dif[1] = fma_(md, L.color[1], dif[1]); dif[2] = fma_(md, L.color[2], dif[2]);
+                        if (lit) {
+                            const v3 Hh = vnorm_fast(add3(Ln, V));
+                            const float ndh = vmax(vdot(N, Hh), 0.f);
+                            const float den = (shin - shin * ndh) + ndh;
+                            const float sp = ndh * rcpr(den);
+                            const float term = ((sp * sscale) * di) * si;
+                            spc[0] = fma_(term, L.color[0], spc[0]); spc[1] = fma_(term, L.color[1], spc[1]); spc[2] = fma_(term, L.color[2], spc[2]);
+                        }
+                    }
+                }
+                if (lm) {
+                    const float mod = fma_(lms, 1.f - 0.4f, 0.4f);
+                    out[0] = out[0] * (dif[0] * mod); out[1] = out[1] * (dif[1] * mod); out[2] = out[2] * (dif[2] * mod);
+                } else {
+                    out[0] = fma_(out[0], dif[0], spc[0]); out[1] = fma_(out[1], dif[1], spc[1]); out[2] = fma_(out[2], dif[2], spc[2]);
+                }
+            }
+            if (S == 1) {
+                if ((tri_lanes >> gl) & 1u) {
+                    uint32_t px = 0xFF000000u;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) px |= ((uint32_t)cvtt(vmax(0.f, vmin(out[k], 1.f)) * 255.f)) << (16 - 8 * k);
+                    color[gy * W + gx] = px;
+                }
+            } else {
+                const float wgt = in_tri ? (float)hits * inv_s : 0.f;
+#pragma unroll
+                for (int k = 0; k < 3; k++) acc[k] = fma_(vmax(0.f, vmin(out[k], 1.f)), wgt, acc[k]);
+            }
+        }
+        if (S > 1) {
+            const bool store = F->clear ? inb : ((block_write >> gl) & 1u);
+            if (store) {
+                uint32_t px = 0xFF000000u;
+#pragma unroll
+                for (int k = 0; k < 3; k++) px |= ((uint32_t)cvtt(vmin(acc[k], 1.f) * 255.f)) << (16 - 8 * k);
+                color[gy * W + gx] = px;
+            }
+        }
+    }
+}
+
+template __global__ void k_tile<1>(const sftg_frame*, const float*, const sftg_clip_tri*, const uint32_t*, const uint32_t*, const uint64_t*, const uint8_t*, uint32_t*, float*, uint32_t*, float*);
+template __global__ void k_tile<2>(const sftg_frame*, const float*, const sftg_clip_tri*, const uint32_t*, const uint32_t*, const uint64_t*, const uint8_t*, uint32_t*, float*, uint32_t*, float*);
+template __global__ void k_tile<4>(const sftg_frame*, const float*, const sftg_clip_tri*, const uint32_t*, const uint32_t*, const uint64_t*, const uint8_t*, uint32_t*, float*, uint32_t*, float*);
+
+/* host-side launch helpers (template kernels are instantiated and launched from this unit) */
+cudaError_t sftg_tile_configure(int max_dynamic_smem) {
+    cudaError_t e = cudaFuncSetAttribute(k_tile<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tile<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    return e;
+}
+
+void sftg_launch_tile(int S, int tiles, size_t smem, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
+                      const uint32_t* tile_start, const uint32_t* tile_count, const uint64_t* tile_pay, const uint8_t* light_vis,
+                      uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out) {
+    if (S == 1) k_tile<1><<<tiles, TILE_THREADS, smem, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, light_vis, color, vis_depth, vis_id, shadow_out);
+    else if (S == 2) k_tile<2><<<tiles, TILE_THREADS, smem, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, light_vis, color, vis_depth, vis_id, shadow_out);
+    else k_tile<4><<<tiles, TILE_THREADS, smem, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, light_vis, color, vis_depth, vis_id, shadow_out);
+}

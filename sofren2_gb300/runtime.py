@@ -1,0 +1,152 @@
+"""ctypes front end of libsofren2_gb300.so: the sft_* API plus the scene player.
+
+The library is the only rendering path.  Loading fails loudly when it has not been built
+or when no CUDA device is present; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+
+
+class SftgDebugOut(C.Structure):
+    """struct sftg_debug_out (include/sftg.h)."""
+    _fields_ = [
+        ("vis_depth", C.c_void_p), ("vis_id", C.c_void_p), ("tile_counts", C.c_void_p),
+        ("tile_payloads", C.c_void_p), ("tile_payload_cap", C.c_uint64), ("tile_payload_total", C.c_void_p),
+        ("ss_cache", C.c_void_p), ("light_vis", C.c_void_p), ("clip_tris", C.c_void_p), ("clip_cap", C.c_uint64),
+        ("clip_total", C.c_void_p), ("shadow", C.c_void_p), ("status", C.c_void_p),
+    ]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = True) -> C.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run `python -m sofren2_gb300.build` first")
+        _build.build_library()
+    lib = C.CDLL(path)
+    v, i32, u32, u64, f32, p = None, C.c_int32, C.c_uint32, C.c_uint64, C.c_float, C.c_void_p
+    sig = {
+        "sft_init": (v, [i32, i32, i32]), "sft_release": (v, []), "sft_set_msaa_samples": (v, [i32]),
+        "sft_get_last_error": (C.c_char_p, []), "sft_set_debug_capture": (v, [p]),
+        "sft_get_frame_timings": (v, [p]), "sftx_scene_load": (p, [p, u64]), "sftx_scene_free": (v, [p]),
+        "sftx_scene_frame_count": (u32, [p]), "sftx_scene_render": (i32, [p, u32, p, i32]),
+        "sftx_scene_frame_size": (u32, [p, u32, p, p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype, fn.argtypes = res, args
+    _LIB = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Renderer:
+    """One GPU renderer (the reference's sft_state singleton)."""
+
+    _live = False
+
+    def __init__(self, width: int, height: int, samples: int = 1):
+        if Renderer._live:
+            raise RuntimeError("only one Renderer may exist at a time (the sft_* API keeps global state)")
+        self.lib = load_library()
+        self.lib.sft_init(width, height, 0)
+        self.lib.sft_set_msaa_samples(samples)
+        self.samples = samples
+        Renderer._live = True
+
+    def close(self):
+        if Renderer._live:
+            self.lib.sft_release()
+            Renderer._live = False
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_samples(self, samples: int):
+        self.lib.sft_set_msaa_samples(samples)
+        self.samples = samples
+
+    def load_scene(self, blob: bytes):
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        h = self.lib.sftx_scene_load(_ptr(buf), len(blob))
+        if not h:
+            raise RuntimeError("scene blob rejected: " + (self.lib.sft_get_last_error() or b"").decode())
+        return h
+
+    def free_scene(self, h):
+        self.lib.sftx_scene_free(h)
+
+    def frame_size(self, h, frame: int) -> tuple[int, int]:
+        w, hh = C.c_uint32(), C.c_uint32()
+        self.lib.sftx_scene_frame_size(h, frame, C.byref(w), C.byref(hh))
+        return w.value, hh.value
+
+    def render(self, h, frame: int = 0, color: np.ndarray | None = None) -> np.ndarray:
+        w, hh = self.frame_size(h, frame)
+        if color is None:
+            color = np.zeros((hh, w), dtype=np.uint32)
+        rc = self.lib.sftx_scene_render(h, frame, _ptr(color), color.strides[0])
+        err = self.lib.sft_get_last_error()
+        if rc != 0:
+            raise RuntimeError("render failed: " + (err or b"").decode())
+        return color
+
+    def render_debug(self, h, frame: int, total_ss: int, n_proxies: int, payload_cap: int = 1 << 22,
+                     clip_cap: int = 1 << 16) -> dict:
+        """Renders one frame and returns the parity buffers named like the oracle's dump sections."""
+        w, hh = self.frame_size(h, frame)
+        tiles = ((w + 63) // 64) * ((hh + 63) // 64)
+        S = self.samples
+        out = {
+            "depth": np.zeros(tiles * S * 4096, np.float32), "vid": np.zeros(tiles * S * 4096, np.uint32),
+            "tile_counts": np.zeros(tiles, np.int32), "tile_payloads_buf": np.zeros(payload_cap, np.uint64),
+            "ss_cache": np.zeros(max(1, total_ss) * 576, np.float32), "light_vis": np.zeros(max(1, n_proxies) * 64, np.uint8),
+            "clip_buf": np.zeros(clip_cap * 41, np.uint32), "shadow": np.zeros(w * hh * 16 if S == 1 else 1, np.float32),
+        }
+        pay_total, clip_total, status = np.zeros(1, np.uint64), np.zeros(1, np.uint64), np.zeros(1, np.uint32)
+        dbg = SftgDebugOut(_ptr(out["depth"]), _ptr(out["vid"]), _ptr(out["tile_counts"]), _ptr(out["tile_payloads_buf"]),
+                           payload_cap, _ptr(pay_total), _ptr(out["ss_cache"]), _ptr(out["light_vis"]), _ptr(out["clip_buf"]),
+                           clip_cap, _ptr(clip_total), _ptr(out["shadow"]) if S == 1 else None, _ptr(status))
+        self.lib.sft_set_debug_capture(C.byref(dbg))
+        try:
+            out["color"] = self.render(h, frame).reshape(-1)
+        finally:
+            self.lib.sft_set_debug_capture(None)
+        out["tile_payloads"] = out.pop("tile_payloads_buf")[: int(pay_total[0])].copy()
+        out["clip"] = out.pop("clip_buf")[: int(clip_total[0]) * 41].view(np.float32).copy()
+        out["ss_cache"] = out["ss_cache"][: total_ss * 576]
+        out["light_vis"] = out["light_vis"][: n_proxies * 64]
+        out["status"] = int(status[0])
+        timings = np.zeros(4, np.float32)
+        self.lib.sft_get_frame_timings(_ptr(timings))
+        out["timings_ms"] = timings
+        return out
+
+
+def scene_counts(scene, frame: int = 0) -> tuple[int, int]:
+    """(screen-space meshlets, world shadow proxies) of a frame of a scenes.Scene."""
+    f = scene.frames[frame]
+    total_ss = sum(sum(ms.n for ms in scene.models[mi].meshes) for mi, _, _ in f.instances)
+    n_prox = sum(len(scene.models[mi].proxies) for mi, _, _ in f.instances) if f.shadows else 0
+    return total_ss, n_prox

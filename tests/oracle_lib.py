@@ -1,0 +1,94 @@
+"""ctypes access to the CPU oracle (oracle/sft_oracle.c) for tests and the CPU baseline.
+
+Test infrastructure only: the shipped library never loads this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from oracle_io import read_dump
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libsft_oracle.so")
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
+
+
+def build_oracle() -> str:
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
+    return ORACLE_SO
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build_oracle()
+        L = C.CDLL(ORACLE_SO)
+        L.sfto_open.restype, L.sfto_open.argtypes = C.c_void_p, [C.c_void_p, C.c_uint64]
+        L.sfto_render.restype = C.c_int
+        L.sfto_render.argtypes = [C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_char_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p]
+        L.sfto_close.restype, L.sfto_close.argtypes = None, [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    def __init__(self, blob: bytes):
+        self._buf = np.frombuffer(blob, dtype=np.uint8)
+        self.h = lib().sfto_open(self._buf.ctypes.data_as(C.c_void_p), len(blob))
+        if not self.h:
+            raise RuntimeError("oracle rejected the scene blob")
+
+    def close(self):
+        if self.h:
+            lib().sfto_close(self.h)
+            self.h = None
+
+    def render_dump(self, frame: int, samples: int, threads: int = 1, shadow: bool = False) -> dict:
+        """Renders one frame and returns its dump sections (plus 'ns', 'invalid_packets', 'shadow')."""
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "o.dump")
+            ns, inv = np.zeros(1, np.uint64), np.zeros(1, np.uint32)
+            rc = lib().sfto_render(self.h, frame, samples, threads, path.encode(), None, None,
+                                   ns.ctypes.data_as(C.c_void_p), inv.ctypes.data_as(C.c_void_p))
+            if rc != 0:
+                raise RuntimeError(f"oracle render failed ({rc})")
+            frames = read_dump(path)
+        out = frames[-1]
+        out["blas"] = frames[0].get("blas", [])
+        out["ns"] = int(ns[0])
+        out["invalid_packets"] = int(inv[0])
+        return out
+
+    def render_color(self, frame: int, samples: int, width: int, height: int, threads: int = 1,
+                     shadow: bool = False) -> tuple[np.ndarray, int, np.ndarray | None]:
+        color = np.zeros(width * height, np.uint32)
+        ns = np.zeros(1, np.uint64)
+        sh = np.zeros(width * height * 16, np.float32) if shadow else None
+        rc = lib().sfto_render(self.h, frame, samples, threads, None, color.ctypes.data_as(C.c_void_p),
+                               None if sh is None else sh.ctypes.data_as(C.c_void_p), ns.ctypes.data_as(C.c_void_p), None)
+        if rc != 0:
+            raise RuntimeError(f"oracle render failed ({rc})")
+        return color, int(ns[0]), sh
+
+
+def reference_available(samples: int) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"ref_harness_{samples}x"))
+
+
+def reference_dump(blob: bytes, samples: int, frame: int = -1) -> list[dict]:
+    with tempfile.TemporaryDirectory() as td:
+        sp, dp = os.path.join(td, "s.sfts"), os.path.join(td, "r.dump")
+        open(sp, "wb").write(blob)
+        subprocess.run([os.path.join(REF_DIR, f"ref_harness_{samples}x"), sp, dp, str(frame)], check=True,
+                       stdout=subprocess.DEVNULL)
+        return read_dump(dp)
