@@ -130,6 +130,8 @@ int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* frame, const 
 int sftg_last_timings(const sftg_ctx* ctx, float* out4);
 /* Number of kernels launched by the last frame. */
 int sftg_last_launch_count(const sftg_ctx* ctx);
+/* The cudaStream_t the context renders on (for callers that time or order work around frames). */
+void* sftg_stream(const sftg_ctx* ctx);
 
 #ifdef __cplusplus
 }

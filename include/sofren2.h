@@ -197,6 +197,9 @@ SFT_FUNC void sft_set_debug_capture(void* sftg_debug_out_or_null);
 SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, u32* out_root);
 /* extension: device time of the last present, ms: [occlusion, geometry, binning, tile] */
 SFT_FUNC void sft_get_frame_timings(f32* out4);
+/* extension: kernels launched by the last present, and the CUDA stream the runtime renders on */
+SFT_FUNC i32 sft_get_launch_count(void);
+SFT_FUNC void* sft_get_cuda_stream(void);
 
 #ifdef __cplusplus
 }
@@ -449,7 +452,9 @@ SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads) {
     (void)requested_threads;   /* host work is a single thread; the GPU replaces the worker pool */
     sft__s = (struct sft__state*)calloc(1, sizeof(*sft__s));
     if (!sft__s) SFT__FATAL("out of memory\n");
-    const int rc = sftg_create(0, &sft__s->gpu);
+    /* extension: SFT_CUDA_DEVICE selects the GPU (one process per GPU in multi-GPU jobs) */
+    const char* dev_env = getenv("SFT_CUDA_DEVICE");
+    const int rc = sftg_create(dev_env ? atoi(dev_env) : 0, &sft__s->gpu);
     if (rc) SFT__FATAL("no usable CUDA device (sftg_create returned %d)\n", rc);
     sft__s->width = width; sft__s->height = height; sft__s->samples = SFT_AA_SAMPLES;
     sft__s->lightmap_brightness = 1.5f;
@@ -479,6 +484,8 @@ SFT_FUNC void sft_set_msaa_samples(i32 samples) { if (sft__s && (samples == 1 ||
 SFT_FUNC const char* sft_get_last_error(void) { return sft__s && sft__s->gpu ? sftg_last_error(sft__s->gpu) : ""; }
 SFT_FUNC void sft_set_debug_capture(void* d) { if (sft__s) sft__s->debug = (sftg_debug_out*)d; }
 SFT_FUNC void sft_get_frame_timings(f32* out4) { if (sft__s) sftg_last_timings(sft__s->gpu, out4); }
+SFT_FUNC i32 sft_get_launch_count(void) { return sft__s ? sftg_last_launch_count(sft__s->gpu) : 0; }
+SFT_FUNC void* sft_get_cuda_stream(void) { return sft__s ? sftg_stream(sft__s->gpu) : NULL; }
 
 SFT_FUNC void sft_frame_begin(void) { }
 SFT_FUNC void sft_frame_end(void) {

@@ -199,7 +199,10 @@ static void sample_bilinear(const otex* t, i32 lod, f32 cu, f32 cv, f32* r, f32*
     const i32 wm = w - 1, hm = h - 1;
     i32 u0w, v0w, u1, v1;
     if (t->is_pot) { u1 = (u0 + 1) & wm; v1 = (v0 + 1) & hm; u0w = u0 & wm; v0w = v0 & hm; }
-    else { u1 = (u0 + 1) < wm ? u0 + 1 : wm; v1 = (v0 + 1) < hm ? v0 + 1 : hm; u0w = u0 < wm ? u0 : wm; v0w = v0 < hm ? v0 : hm; }
+    else {   /* the reference has no lower clamp here (reads outside the texture); clamp at 0 */
+        u1 = (u0 + 1) < wm ? u0 + 1 : wm; v1 = (v0 + 1) < hm ? v0 + 1 : hm; u0w = u0 < wm ? u0 : wm; v0w = v0 < hm ? v0 : hm;
+        u1 = u1 < 0 ? 0 : u1; v1 = v1 < 0 ? 0 : v1; u0w = u0w < 0 ? 0 : u0w; v0w = v0w < 0 ? 0 : v0w;
+    }
     const u32* base = t->texels + t->offs[lod];
 #define ADDR(ux, vy) (t->is_pot ? ((((((u32)(vy) >> 2) << t->shift[lod]) + ((u32)(ux) >> 2)) << 4) + (((u32)(vy) & 3) << 2) + ((u32)(ux) & 3)) \
                                : ((((((u32)(vy) >> 2) * (u32)t->bw[lod]) + ((u32)(ux) >> 2)) << 4) + (((u32)(vy) & 3) << 2) + ((u32)(ux) & 3)))
@@ -224,7 +227,7 @@ static void sample_nearest(const otex* t, i32 lod, f32 cu, f32 cv, f32* r, f32* 
     const i32 u0 = cvtt(floorf(cu * (f32)w)), v0 = cvtt(floorf(cv * (f32)h));
     const i32 wm = w - 1, hm = h - 1;
     i32 uw, vw;
-    if (t->is_pot) { uw = u0 & wm; vw = v0 & hm; } else { uw = u0 < wm ? u0 : wm; vw = v0 < hm ? v0 : hm; }
+    if (t->is_pot) { uw = u0 & wm; vw = v0 & hm; } else { uw = u0 < wm ? u0 : wm; vw = v0 < hm ? v0 : hm; uw = uw < 0 ? 0 : uw; vw = vw < 0 ? 0 : vw; }
     u32 a;
     if (t->is_pot) a = (((((u32)vw >> 2) << t->shift[lod]) + ((u32)uw >> 2)) << 4) + (((u32)vw & 3) << 2) + ((u32)uw & 3);
     else a = (((((u32)vw >> 2) * (u32)t->bw[lod]) + ((u32)uw >> 2)) << 4) + (((u32)vw & 3) << 2) + ((u32)uw & 3);

@@ -9,7 +9,7 @@
  *
  * Frame sequence on one stream (sft_present, sofren2.c:8139-8289):
  *   1. one H2D copy of the frame block: constants, instances, bones, jobs, lights, proxies, TLAS
- *   2. k_occlusion        light visibility of every shadow proxy (8163-8280)
+ *   2. k_occl_*           light visibility of every shadow proxy (8163-8280)
  *   3. k_geometry         cull, skin, transform, project, batch setup (4901-5145)
  *   4. scan + k_clip      near-plane clipping in emission order (4691-4772)
  *   5. k_bin (count), scan, k_bin (write)   per-tile payload lists (4619-4688)
@@ -282,6 +282,7 @@ struct frame_bufs {
     uint32_t* tile_count; uint32_t* tile_start;
     uint64_t* tile_pay;
     uint8_t* light_vis;
+    void* packets; uint2* pairs; uint32_t* n_pairs; uint32_t max_pairs;
     uint32_t* scan_tmp;
     uint32_t* status;
     uint32_t* totals;    /* [0] clip total, [1] tile payload total */
@@ -358,7 +359,9 @@ static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug
     acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
     acc((size_t)tiles * 4); acc((size_t)tiles * 4); acc(ctx->tile_cap * 8);
-    acc((size_t)fd->n_proxies * 64 + 64); acc(((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
+    const size_t n_packets = (size_t)(fd->n_point < 64 ? fd->n_point : 64) * ((fd->n_proxies + 7) / 8) * 3;
+    acc((size_t)fd->n_proxies * 64 + 64); acc(n_packets * sftg_packet_bytes() + 64);
+    acc((n_packets * (fd->n_instances ? fd->n_instances : 1) + 1) * 8); acc(64); acc(((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
     if (want_debug) { acc((size_t)tiles * S * 4096 * 4); acc((size_t)tiles * S * 4096 * 4); acc((size_t)W * H * 16 * 4); }
     if (need > ctx->arena_cap) {
         if (ctx->arena) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->arena); ctx->arena = nullptr; }
@@ -386,6 +389,10 @@ static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug
     B.tile_start = bp.take<uint32_t>(tiles);
     B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
     B.light_vis = bp.take<uint8_t>((size_t)fd->n_proxies * 64 + 64);
+    B.packets = bp.take<char>(n_packets * sftg_packet_bytes() + 64);
+    B.max_pairs = (uint32_t)(n_packets * (fd->n_instances ? fd->n_instances : 1));
+    B.pairs = bp.take<uint2>((size_t)B.max_pairs + 1);
+    B.n_pairs = bp.take<uint32_t>(16);
     B.scan_tmp = bp.take<uint32_t>((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
     B.status = bp.take<uint32_t>(16);
     B.totals = bp.take<uint32_t>(16);
@@ -453,9 +460,9 @@ static int launch_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, const frame_bu
     CK(cudaMemsetAsync(B.status, 0, 64, st));
     CK(cudaEventRecord(ctx->ev[0], st));
     if (fd->shadows && fd->n_point && fd->n_proxies) {
-        const uint32_t items = (fd->n_point < 64 ? fd->n_point : 64) * ((fd->n_proxies + 7) / 8);
-        k_occlusion<<<(items + 3) / 4, 128, 0, st>>>(B.F, B.light_vis, B.status);
-        ctx->launches++;
+        sftg_launch_occlusion(B.F, fd->n_point, fd->n_proxies, fd->n_instances, B.packets, B.pairs, B.n_pairs, B.max_pairs,
+                              B.light_vis, B.status, st);
+        ctx->launches += 3;
     }
     CK(cudaEventRecord(ctx->ev[1], st));
     if (n_jobs) {
@@ -475,6 +482,7 @@ static int launch_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, const frame_bu
     k_bin<<<tiles, 256, 0, st>>>(B.F, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
     ctx->launches += 2;
     CK(cudaEventRecord(ctx->ev[3], st));
+    if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, (size_t)fd->width * fd->height * 16 * 4, st));
     const size_t sm = tile_smem(S);
     sftg_launch_tile(S, tiles, sm, st, B.F, B.ss, B.clips, B.tile_start, B.tile_count, B.tile_pay, B.light_vis, d_color, B.vis_depth, B.vis_id, B.shadow);
     ctx->launches++;
@@ -554,3 +562,5 @@ extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out4) {
 }
 
 extern "C" int sftg_last_launch_count(const sftg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" void* sftg_stream(const sftg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }

@@ -23,7 +23,9 @@ __global__ void k_bin(const sftg_frame* F, const sftg_batch_rec* recs, const uin
 __global__ void k_scan_reduce(const uint32_t* in, uint32_t n, uint32_t* sums);
 __global__ void k_scan_top(uint32_t* sums, uint32_t nb, uint32_t* total_out);
 __global__ void k_scan_down(const uint32_t* in, uint32_t n, const uint32_t* sums, uint32_t* out);
-__global__ void k_occlusion(const sftg_frame* F, uint8_t* light_vis, uint32_t* status);
+size_t sftg_packet_bytes();
+void sftg_launch_occlusion(const sftg_frame* F, uint32_t n_point, uint32_t n_proxies, uint32_t n_inst, void* packets, uint2* pairs,
+                           uint32_t* n_pairs, uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
 void sftg_launch_tile(int S, int tiles, size_t smem, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
                       const uint32_t* tile_start, const uint32_t* tile_count, const uint64_t* tile_pay, const uint8_t* light_vis,

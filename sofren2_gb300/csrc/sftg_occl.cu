@@ -1,14 +1,16 @@
 /*
- * k_occlusion: the per-frame proxy occlusion pass (inside sft_present, sofren2.c:8163-8280).
- * One warp per (light, batch of 8 proxies).  For each of the three rays toward the light disk
- * the warp traces the 8-ray packet through the instance TLAS and each static model's BLAS:
- * lanes 0-7 test the node's eight child AABBs against the packet frustum (one child per lane,
- * sft__frustum_vs_bvh_node 3906-3968) and a ballot gives the hit mask, visited in child order;
- * at a leaf triangle lanes 0-7 run the any-hit test of their own ray (3840-3904).  The result
- * per proxy is 3 minus the number of occluded rays.
- *
- * Traversal stacks live in shared memory with a fixed depth; the walk is bounded by the node
- * count and a stack overflow sets a status word instead of writing out of bounds.
+ * The per-frame proxy occlusion pass (inside sft_present, sofren2.c:8163-8280), in three phases:
+ *   k_occl_tlas      one warp per packet (light, batch of 8 proxies, one of 3 disk rays): ray
+ *                    set-up, packet frustum, TLAS walk; each reached static instance becomes a
+ *                    (packet, instance) pair
+ *   k_occl_blas      one warp per pair: BLAS walk with one child AABB per lane
+ *                    (sft__frustum_vs_bvh_node 3906-3968) and the any-hit test on lanes
+ *                    (triangle, ray) (3840-3904); blocked rays are OR-ed into the packet
+ *   k_occl_finalize  light_vis = 3 - blocked rays per (proxy, light)
+ * The reference traces each packet serially and stops once every ray is blocked; the OR of
+ * hits it accumulates does not depend on the visiting order, so splitting the walk across
+ * warps gives the same light_vis.  Stacks are fixed-size in shared memory; an overflow sets a
+ * status bit instead of writing out of bounds.
  */
 #include "sftg_types.h"
 #include "sftg_lane.cuh"
@@ -111,23 +113,32 @@ SFTG_D bool packet_frustum(const float* ox, const float* oy, const float* oz, ui
 /* status bits */
 #define OCC_STACK_OVERFLOW 1u
 #define OCC_UNDEFINED_FRUSTUM 2u
+#define OCC_PAIR_OVERFLOW 4u
 
+/* one traced packet: 8 rays from proxy points toward one point of the light disk */
+struct sftg_packet {
+    frustum6 f;                 /* world-space packet frustum */
+    float o[3][8], e[3][8];     /* ray origins and ends (origin + L) */
+    uint32_t active;
+    uint32_t hits;              /* OR of the rays found blocked */
+};
+
+/* Phase A: one warp per packet (light, proxy batch, ray): ray set-up, packet frustum and the
+ * TLAS walk (sofren2.c:8178-8269, 4086-4135); every static instance the frustum reaches becomes
+ * a (packet, instance) pair for phase B. */
 __global__ void __launch_bounds__(OCC_WARPS * 32)
-k_occlusion(const sftg_frame* __restrict__ F, uint8_t* __restrict__ light_vis, uint32_t* __restrict__ status)
+k_occl_tlas(const sftg_frame* __restrict__ F, sftg_packet* __restrict__ packets, uint2* __restrict__ pairs,
+            uint32_t* __restrict__ n_pairs, uint32_t max_pairs, uint32_t* __restrict__ status)
 {
-    __shared__ uint32_t s_tstack[OCC_WARPS][OCC_STACK];
-    __shared__ uint32_t s_bstack[OCC_WARPS][OCC_STACK];
+    __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t pc = F->n_proxies;
-    const uint32_t lc = min(F->n_point, 64u);
-    const uint32_t nbatch = (pc + 7) / 8;
-    const uint32_t item = blockIdx.x * OCC_WARPS + warp;
-    if (item >= lc * nbatch) return;
-    const uint32_t l = item / nbatch, pb = (item % nbatch) * 8;
+    const uint32_t pc = F->n_proxies, lc = min(F->n_point, 64u), nbatch = (pc + 7) / 8;
+    const uint32_t pk = blockIdx.x * OCC_WARPS + warp;
+    if (pk >= lc * nbatch * 3) return;
+    const uint32_t ray = pk % 3, b = (pk / 3) % nbatch, l = pk / (3 * nbatch), pb = b * 8;
     const sftg_point_light L = F->point[l];
     const v3 lpos = mk3(L.pos[0], L.pos[1], L.pos[2]);
-
-    /* batch centre and light-disk targets (8178-8210), computed identically on every lane */
+    /* batch centre and light-disk targets, identical on every lane */
     v3 bc = mk3(0.f, 0.f, 0.f); int na = 0;
     for (int k = 0; k < 8; k++) {
         if (pb + k >= pc) continue;
@@ -144,142 +155,192 @@ k_occlusion(const sftg_frame* __restrict__ F, uint8_t* __restrict__ light_vis, u
     const v3 lright = snorm(perp);
     const v3 lup = cross3(lright, ldir);
     const float r = 0.1f;
-    const v3 tg[3] = {
-        add3(lpos, scl3(lup, r)),
-        add3(lpos, add3(scl3(lright, r * 0.866025f), scl3(lup, -r * 0.5f))),
-        add3(lpos, add3(scl3(lright, -r * 0.866025f), scl3(lup, -r * 0.5f))),
-    };
-    int occluded = 0;   /* lane k < 8: rays of proxy pb + k found blocked */
-    for (int ray = 0; ray < 3; ray++) {
-        float ox[8], oy[8], oz[8], lx[8], ly[8], lz[8];
-        uint32_t am = 0;
-        for (int k = 0; k < 8; k++) {
-            if (pb + k < pc) {
-                const sftg_proxy px = F->proxies[pb + k];
-                float x, y, z;
-                if (ray == 0) { x = px.posa[0]; y = px.posa[1]; z = px.posa[2]; }
-                else if (ray == 1) { x = px.posb[0]; y = px.posb[1]; z = px.posb[2]; }
-                else { x = (px.posa[0] + px.posb[0]) * 0.5f; y = (px.posa[1] + px.posb[1]) * 0.5f; z = (px.posa[2] + px.posb[2]) * 0.5f; }
-                ox[k] = x; oy[k] = y; oz[k] = z;
-                lx[k] = tg[ray].x - x; ly[k] = tg[ray].y - y; lz[k] = tg[ray].z - z;
-                am |= 1u << k;
-            } else { ox[k] = oy[k] = oz[k] = lx[k] = ly[k] = lz[k] = 0.f; }
+    v3 tg;
+    if (ray == 0) tg = add3(lpos, scl3(lup, r));
+    else if (ray == 1) tg = add3(lpos, add3(scl3(lright, r * 0.866025f), scl3(lup, -r * 0.5f)));
+    else tg = add3(lpos, add3(scl3(lright, -r * 0.866025f), scl3(lup, -r * 0.5f)));
+    float ox[8], oy[8], oz[8];
+    uint32_t am = 0;
+    sftg_packet* P = &packets[pk];
+    for (int k = 0; k < 8; k++) {
+        float x = 0.f, y = 0.f, z = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+        if (pb + k < pc) {
+            const sftg_proxy px = F->proxies[pb + k];
+            if (ray == 0) { x = px.posa[0]; y = px.posa[1]; z = px.posa[2]; }
+            else if (ray == 1) { x = px.posb[0]; y = px.posb[1]; z = px.posb[2]; }
+            else { x = (px.posa[0] + px.posb[0]) * 0.5f; y = (px.posa[1] + px.posb[1]) * 0.5f; z = (px.posa[2] + px.posb[2]) * 0.5f; }
+            lx = tg.x - x; ly = tg.y - y; lz = tg.z - z;
+            am |= 1u << k;
         }
-        /* sft__trace_shadow_packet (4086-4243), static instances only */
-        frustum6 pf;
-        if (!packet_frustum(ox, oy, oz, am, lpos, L.radius, pf) && lane == 0) atomicOr(status, OCC_UNDEFINED_FRUSTUM);
-        /* this lane's ray (lanes 0-7) */
-        const int rl = lane & 7;
-        const v3 my_o = mk3(ox[rl], oy[rl], oz[rl]);
-        const v3 my_e = mk3(ox[rl] + lx[rl], oy[rl] + ly[rl], oz[rl] + lz[rl]);
-        uint32_t sat = 0;
-        const uint32_t full = am;
-        int ttop = 0;
-        if (lane == 0) s_tstack[warp][0] = F->tlas_root;
-        ttop = 1;
+        ox[k] = x; oy[k] = y; oz[k] = z;
+        if (lane == k) {
+            P->o[0][k] = x; P->o[1][k] = y; P->o[2][k] = z;
+            P->e[0][k] = x + lx; P->e[1][k] = y + ly; P->e[2][k] = z + lz;
+        }
+    }
+    frustum6 pf;
+    if (!packet_frustum(ox, oy, oz, am, lpos, L.radius, pf) && lane == 0) atomicOr(status, OCC_UNDEFINED_FRUSTUM);
+    if (lane == 0) { P->f = pf; P->active = am; P->hits = 0; }
+    if (am == 0 || F->tlas_count == 0) return;
+    int top = 1;
+    if (lane == 0) s_stack[warp][0] = F->tlas_root;
+    __syncwarp();
+    while (top > 0) {
+        const uint32_t ni = s_stack[warp][--top];
         __syncwarp();
-        bool done = (am == 0) || (F->tlas_count == 0);
-        uint32_t guard = 0;
-        while (!done && ttop > 0) {
-            const uint32_t tni = s_tstack[warp][--ttop];
-            __syncwarp();
-            const sftg_bvh_node* tn = &F->tlas[tni];
-            uint32_t th = node_mask(tn, pf, lane);
-            while (th && !done) {
-                const int tl = __ffs(th) - 1; th &= th - 1;
-                const uint32_t ch = tn->child[tl];
-                if (ch == SFTG_INVALID) continue;
-                if (!tn->leaf) {
-                    if (ttop >= OCC_STACK || ch >= F->tlas_count) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); done = true; break; }
-                    if (lane == 0) s_tstack[warp][ttop] = ch;
-                    ttop++;
-                    __syncwarp();
-                    continue;
-                }
-                const uint32_t ii = ch & ~0x80000000u;
-                const sftg_inst* I = &F->inst[ii];
-                const sftg_model Md = F->models[I->model];
-                if (Md.bone_count > 0 || Md.blas_count == 0) continue;
-                const float* M = I->T;
-                frustum6 mf;
-                for (int p = 0; p < 6; p++) {
-                    const float nx = pf.n[p][0], ny = pf.n[p][1], nz = pf.n[p][2], d = pf.d[p];
-                    const float nmx = nx * M[0] + ny * M[1] + nz * M[2];
-                    const float nmy = nx * M[4] + ny * M[5] + nz * M[6];
-                    const float nmz = nx * M[8] + ny * M[9] + nz * M[10];
-                    const float dot_t = nx * M[12] + ny * M[13] + nz * M[14];
-                    const float dm = dot_t + d;
-                    const float il = fdiv(1.f, fsqrt(nmx * nmx + nmy * nmy + nmz * nmz));
-                    mf.n[p][0] = nmx * il; mf.n[p][1] = nmy * il; mf.n[p][2] = nmz * il;
-                    mf.d[p] = dm * il;
-                    mf.an[p][0] = fabsf(nmx * il); mf.an[p][1] = fabsf(nmy * il); mf.an[p][2] = fabsf(nmz * il);
-                }
-                /* sft_m_qinv (1693-1712) */
-                float im[16];
-                im[0] = M[0]; im[1] = M[4]; im[2] = M[8]; im[3] = 0.f;
-                im[4] = M[1]; im[5] = M[5]; im[6] = M[9]; im[7] = 0.f;
-                im[8] = M[2]; im[9] = M[6]; im[10] = M[10]; im[11] = 0.f;
-                for (int a = 0; a < 3; a++) im[12 + a] = -(M[12] * im[a] + M[13] * im[4 + a] + M[14] * im[8 + a]);
-                im[15] = 1.f;
-                const v3 lo = xform(my_o, im);
-                const v3 le = xform(my_e, im);
-                const v3 Lv = sub3(le, lo);
-                const float tmax = fsqrt(vdot(Lv, Lv));
-                const v3 ld = vnorm_fast(Lv);
-                int btop = 0;
-                if (lane == 0) s_bstack[warp][0] = Md.blas_root;
-                btop = 1;
+        const sftg_bvh_node* nd = &F->tlas[ni];
+        uint32_t m = node_mask(nd, pf, lane);
+        while (m) {
+            const int c = __ffs(m) - 1; m &= m - 1;
+            const uint32_t ch = nd->child[c];
+            if (ch == SFTG_INVALID) continue;
+            if (!nd->leaf) {
+                if (top >= OCC_STACK || ch >= F->tlas_count) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); return; }
+                if (lane == 0) s_stack[warp][top] = ch;
+                top++;
                 __syncwarp();
-                const sftg_bvh_node* blas = F->blas + Md.blas_base;
-                while (!done && btop > 0) {
-                    const uint32_t bni = s_bstack[warp][--btop];
-                    __syncwarp();
-                    const sftg_bvh_node* bn = &blas[bni];
-                    uint32_t bh = node_mask(bn, mf, lane);
-                    while (bh) {
-                        const int bl = __ffs(bh) - 1; bh &= bh - 1;
-                        const uint32_t bc2 = bn->child[bl];
-                        if (bc2 == SFTG_INVALID) continue;
-                        if (!bn->leaf) {
-                            if (btop >= OCC_STACK || bc2 >= Md.blas_count || ++guard > (1u << 24)) {
-                                if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); done = true; break;
-                            }
-                            if (lane == 0) s_bstack[warp][btop] = bc2;
-                            btop++;
-                            __syncwarp();
-                            continue;
-                        }
-                        const uint32_t pay = bc2 & ~0x80000000u;
-                        const uint32_t g = I->meshlet_base + (pay >> 7), t = pay & 0x7F;
-                        const uint8_t* ind = F->ml_inds + (size_t)g * 512;
-                        const float* at = F->ml_attr + (size_t)g * 640;
-                        const uint32_t tb = t >> 3, tl2 = t & 7;
-                        const uint32_t i0 = ind[tb * 32 + tl2], i1 = ind[tb * 32 + 8 + tl2], i2 = ind[tb * 32 + 16 + tl2];
-                        const v3 v0 = mk3(at[i0], at[64 + i0], at[128 + i0]);
-                        const v3 v1 = mk3(at[i1], at[64 + i1], at[128 + i1]);
-                        const v3 v2 = mk3(at[i2], at[64 + i2], at[128 + i2]);
-                        /* sft__ray_packet_vs_triangle_any_hit, lane = ray */
-                        const uint32_t cur = am & ~sat;
-                        const v3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
-                        const v3 h = cross3(ld, e2);
-                        const float a = vdot(e1, h);
-                        bool hit = lane < 8 && ((cur >> rl) & 1u) && (fabsf(a) > 1e-6f);
-                        const float fr = rcpr(a);
-                        const v3 s = sub3(lo, v0);
-                        const float u = fr * vdot(s, h);
-                        hit = hit && u >= 0.f && u <= 1.f;
-                        const v3 q = cross3(s, e1);
-                        const float v = fr * vdot(ld, q);
-                        hit = hit && v >= 0.f && (u + v) <= 1.f;
-                        const float tt = fr * vdot(e2, q);
-                        hit = hit && tt > 1e-6f && tt < tmax;
-                        sat |= __ballot_sync(0xFFFFFFFFu, hit) & 0xFFu;
-                        if (sat == full) { done = true; break; }
-                    }
-                }
+                continue;
+            }
+            const uint32_t ii = ch & ~0x80000000u;
+            if (ii >= F->n_inst) continue;
+            const sftg_model Md = F->models[F->inst[ii].model];
+            if (Md.bone_count > 0 || Md.blas_count == 0) continue;   /* static instances only */
+            if (lane == 0) {
+                const uint32_t slot = atomicAdd(n_pairs, 1u);
+                if (slot < max_pairs) pairs[slot] = make_uint2(pk, ii);
+                else atomicOr(status, OCC_PAIR_OVERFLOW);
             }
         }
-        if (lane < 8) occluded += (sat >> lane) & 1u;
     }
-    if (lane < 8 && pb + lane < pc) light_vis[(size_t)(pb + lane) * 64 + l] = (uint8_t)(3 - occluded);
+}
+
+/* Phase B: one warp per (packet, instance): the packet frustum and rays in model space and the
+ * BLAS walk (4137-4238).  Child AABBs are tested one per lane; at a leaf, lanes are
+ * (triangle k of 4, ray r of 8) and run the any-hit test (3840-3904).  Hits are OR-ed into the
+ * packet, which is what the reference accumulates in any visiting order. */
+__global__ void __launch_bounds__(OCC_WARPS * 32)
+k_occl_blas(const sftg_frame* __restrict__ F, sftg_packet* __restrict__ packets, const uint2* __restrict__ pairs,
+            const uint32_t* __restrict__ n_pairs, uint32_t max_pairs, uint32_t* __restrict__ status)
+{
+    __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t item = blockIdx.x * OCC_WARPS + warp;
+    if (item >= min(*n_pairs, max_pairs)) return;
+    const uint2 pr = pairs[item];
+    sftg_packet* P = &packets[pr.x];
+    const uint32_t full = P->active;
+    const frustum6 pf = P->f;
+    const sftg_inst* I = &F->inst[pr.y];
+    const sftg_model Md = F->models[I->model];
+    const float* M = I->T;
+    frustum6 mf;
+    for (int p = 0; p < 6; p++) {
+        const float nx = pf.n[p][0], ny = pf.n[p][1], nz = pf.n[p][2], d = pf.d[p];
+        const float nmx = nx * M[0] + ny * M[1] + nz * M[2];
+        const float nmy = nx * M[4] + ny * M[5] + nz * M[6];
+        const float nmz = nx * M[8] + ny * M[9] + nz * M[10];
+        const float dot_t = nx * M[12] + ny * M[13] + nz * M[14];
+        const float dm = dot_t + d;
+        const float il = fdiv(1.f, fsqrt(nmx * nmx + nmy * nmy + nmz * nmz));
+        mf.n[p][0] = nmx * il; mf.n[p][1] = nmy * il; mf.n[p][2] = nmz * il;
+        mf.d[p] = dm * il;
+        mf.an[p][0] = fabsf(nmx * il); mf.an[p][1] = fabsf(nmy * il); mf.an[p][2] = fabsf(nmz * il);
+    }
+    /* sft_m_qinv (1693-1712) */
+    float im[16];
+    im[0] = M[0]; im[1] = M[4]; im[2] = M[8]; im[3] = 0.f;
+    im[4] = M[1]; im[5] = M[5]; im[6] = M[9]; im[7] = 0.f;
+    im[8] = M[2]; im[9] = M[6]; im[10] = M[10]; im[11] = 0.f;
+    for (int a = 0; a < 3; a++) im[12 + a] = -(M[12] * im[a] + M[13] * im[4 + a] + M[14] * im[8 + a]);
+    im[15] = 1.f;
+    const int r = lane & 7, kq = lane >> 3;
+    const v3 lo = xform(mk3(P->o[0][r], P->o[1][r], P->o[2][r]), im);
+    const v3 le = xform(mk3(P->e[0][r], P->e[1][r], P->e[2][r]), im);
+    const v3 Lv = sub3(le, lo);
+    const float tmax = fsqrt(vdot(Lv, Lv));
+    const v3 ld = vnorm_fast(Lv);
+    uint32_t sat = 0;
+    int top = 1;
+    if (lane == 0) s_stack[warp][0] = Md.blas_root;
+    __syncwarp();
+    const sftg_bvh_node* blas = F->blas + Md.blas_base;
+    uint32_t guard = 0;
+    while (top > 0 && sat != full) {
+        const uint32_t ni = s_stack[warp][--top];
+        __syncwarp();
+        const sftg_bvh_node* nd = &blas[ni];
+        uint32_t m = node_mask(nd, mf, lane);
+        if (!nd->leaf) {
+            while (m) {
+                const int c = __ffs(m) - 1; m &= m - 1;
+                const uint32_t ch = nd->child[c];
+                if (ch == SFTG_INVALID) continue;
+                if (top >= OCC_STACK || ch >= Md.blas_count || ++guard > (1u << 24)) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); top = 0; break; }
+                if (lane == 0) s_stack[warp][top] = ch;
+                top++;
+                __syncwarp();
+            }
+            continue;
+        }
+        while (m && sat != full) {
+            /* the next up to 4 triangles of this leaf, lane = (triangle kq, ray r) */
+            int c = -1;
+            uint32_t mm = m;
+            for (int q = 0; q <= kq && mm; q++) { c = __ffs(mm) - 1; mm &= mm - 1; }
+            const bool have = (__popc(m) > kq) && c >= 0;
+            for (int q = 0; q < 4 && m; q++) m &= m - 1;
+            bool hit = false;
+            if (have && nd->child[c] != SFTG_INVALID && ((full & ~sat) >> r & 1u)) {
+                const uint32_t pay = nd->child[c] & ~0x80000000u;
+                const uint32_t g = I->meshlet_base + (pay >> 7), t = pay & 0x7F;
+                const uint8_t* ind = F->ml_inds + (size_t)g * 512;
+                const float* at = F->ml_attr + (size_t)g * 640;
+                const uint32_t tb = t >> 3, tl = t & 7;
+                const uint32_t i0 = ind[tb * 32 + tl], i1 = ind[tb * 32 + 8 + tl], i2 = ind[tb * 32 + 16 + tl];
+                const v3 v0 = mk3(at[i0], at[64 + i0], at[128 + i0]);
+                const v3 v1 = mk3(at[i1], at[64 + i1], at[128 + i1]);
+                const v3 v2 = mk3(at[i2], at[64 + i2], at[128 + i2]);
+                const v3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
+                const v3 h = cross3(ld, e2);
+                const float a = vdot(e1, h);
+                hit = fabsf(a) > 1e-6f;
+                const float fr = rcpr(a);
+                const v3 s = sub3(lo, v0);
+                const float u = fr * vdot(s, h);
+                hit = hit && u >= 0.f && u <= 1.f;
+                const v3 q = cross3(s, e1);
+                const float v = fr * vdot(ld, q);
+                hit = hit && v >= 0.f && (u + v) <= 1.f;
+                const float tt = fr * vdot(e2, q);
+                hit = hit && tt > 1e-6f && tt < tmax;
+            }
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
+            sat |= (bal | (bal >> 8) | (bal >> 16) | (bal >> 24)) & 0xFFu;
+        }
+    }
+    if (lane == 0 && sat) atomicOr(&P->hits, sat);
+}
+
+/* Phase C: light_vis[p][l] = 3 - rays blocked (8169-8276) */
+__global__ void k_occl_finalize(const sftg_frame* __restrict__ F, const sftg_packet* __restrict__ packets, uint8_t* __restrict__ light_vis)
+{
+    const uint32_t pc = F->n_proxies, lc = min(F->n_point, 64u), nbatch = (pc + 7) / 8;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc * lc) return;
+    const uint32_t p = i / lc, l = i % lc, b = p / 8, k = p % 8;
+    int blocked = 0;
+    for (int ray = 0; ray < 3; ray++) blocked += (packets[(l * nbatch + b) * 3 + ray].hits >> k) & 1u;
+    light_vis[(size_t)p * 64 + l] = (uint8_t)(3 - blocked);
+}
+
+size_t sftg_packet_bytes() { return sizeof(sftg_packet); }
+
+void sftg_launch_occlusion(const sftg_frame* F, uint32_t n_point, uint32_t n_proxies, uint32_t n_inst, void* packets, uint2* pairs,
+                           uint32_t* n_pairs, uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st) {
+    const uint32_t lc = n_point < 64 ? n_point : 64, nbatch = (n_proxies + 7) / 8, npk = lc * nbatch * 3;
+    cudaMemsetAsync(n_pairs, 0, 4, st);
+    k_occl_tlas<<<(npk + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(F, (sftg_packet*)packets, pairs, n_pairs, max_pairs, status);
+    const uint32_t mp = npk * (n_inst ? n_inst : 1) < max_pairs ? npk * (n_inst ? n_inst : 1) : max_pairs;
+    k_occl_blas<<<(mp + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(F, (sftg_packet*)packets, pairs, n_pairs, max_pairs, status);
+    k_occl_finalize<<<(n_proxies * lc + 255) / 256, 256, 0, st>>>(F, (const sftg_packet*)packets, light_vis);
 }

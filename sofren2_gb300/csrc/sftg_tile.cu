@@ -196,7 +196,9 @@ SFTG_D void sample_bilinear(const sftg_frame* F, int ti, int lod, float cu, floa
     const int wm = w - 1, hm = h - 1;
     int u0w, v0w, u1, v1;
     if (t.is_pot) { u1 = (u0 + 1) & wm; v1 = (v0 + 1) & hm; u0w = u0 & wm; v0w = v0 & hm; }
-    else { u1 = min(u0 + 1, wm); v1 = min(v0 + 1, hm); u0w = min(u0, wm); v0w = min(v0, hm); }
+    else {   /* the reference has no lower clamp here (it reads outside the texture); clamp at 0 */
+        u1 = max(0, min(u0 + 1, wm)); v1 = max(0, min(v0 + 1, hm)); u0w = max(0, min(u0, wm)); v0w = max(0, min(v0, hm));
+    }
     const uint32_t* base = F->texels + t.offs[lod];
     const uint32_t c00 = __ldg(&base[tex_addr(t, lod, u0w, v0w)]), c10 = __ldg(&base[tex_addr(t, lod, u1, v0w)]);
     const uint32_t c01 = __ldg(&base[tex_addr(t, lod, u0w, v1)]), c11 = __ldg(&base[tex_addr(t, lod, u1, v1)]);
@@ -221,7 +223,7 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
     const int u0 = cvtt(floorf(cu * (float)w)), v0 = cvtt(floorf(cv * (float)h));
     const int wm = w - 1, hm = h - 1;
     int uw, vw;
-    if (t.is_pot) { uw = u0 & wm; vw = v0 & hm; } else { uw = min(u0, wm); vw = min(v0, hm); }
+    if (t.is_pot) { uw = u0 & wm; vw = v0 & hm; } else { uw = max(0, min(u0, wm)); vw = max(0, min(v0, hm)); }
     const uint32_t c = __ldg(&F->texels[t.offs[lod] + tex_addr(t, lod, uw, vw)]);
     const float i255 = 1.f / 255.f;
     r = (float)((c >> 16) & 255u) * i255; g = (float)((c >> 8) & 255u) * i255; b = (float)(c & 255u) * i255;

@@ -45,7 +45,8 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sft_get_last_error": (C.c_char_p, []), "sft_set_debug_capture": (v, [p]),
         "sft_get_frame_timings": (v, [p]), "sftx_scene_load": (p, [p, u64]), "sftx_scene_free": (v, [p]),
         "sftx_scene_frame_count": (u32, [p]), "sftx_scene_render": (i32, [p, u32, p, i32]),
-        "sftx_scene_frame_size": (u32, [p, u32, p, p]),
+        "sftx_scene_frame_size": (u32, [p, u32, p, p]), "sft_get_launch_count": (i32, []),
+        "sft_get_cuda_stream": (p, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -101,6 +102,23 @@ class Renderer:
         w, hh = C.c_uint32(), C.c_uint32()
         self.lib.sftx_scene_frame_size(h, frame, C.byref(w), C.byref(hh))
         return w.value, hh.value
+
+    def render_device(self, h, frame: int = 0) -> None:
+        """Renders with the colour left in device memory (no pixel copy to the host)."""
+        rc = self.lib.sftx_scene_render(h, frame, None, 0)
+        if rc != 0:
+            raise RuntimeError("render failed: " + (self.lib.sft_get_last_error() or b"").decode())
+
+    def stream(self) -> int:
+        return self.lib.sft_get_cuda_stream() or 0
+
+    def launch_count(self) -> int:
+        return int(self.lib.sft_get_launch_count())
+
+    def timings(self) -> np.ndarray:
+        t = np.zeros(4, np.float32)
+        self.lib.sft_get_frame_timings(_ptr(t))
+        return t
 
     def render(self, h, frame: int = 0, color: np.ndarray | None = None) -> np.ndarray:
         w, hh = self.frame_size(h, frame)

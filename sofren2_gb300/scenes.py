@@ -565,3 +565,450 @@ def config1(width=640, height=360, seed=1001) -> Scene:
     """Plain static frame: 16 UV-spheres (32x16) + 16 unit cubes, 256x256 textures, one point light,
     camera at the origin looking +Z, 60 degree fov, near 0.1, far 100."""
     return static_shapes_scene(width, height, seed)
+
+
+# ------------------------------------------------------------------ capsules and skinning
+def _frame_for(axis: np.ndarray):
+    """Orthonormal (u, v) perpendicular to a unit axis, built from the least-aligned cardinal axis."""
+    ax = np.abs(axis)
+    card = np.zeros(3, dtype=F32)
+    card[int(np.argmin(ax))] = F32(1.0)
+    u = _norm3(_cross3(axis, card))
+    v = _cross3(axis, u)
+    return u, v
+
+
+def capsule(a, b, radius, slices=16, rings=5, body=4, caps=True) -> RawMesh:
+    """Capsule (or open cylinder when caps=False) from a to b; rows of vertices joined by quads,
+    pole triangles skipped."""
+    a, b = np.asarray(a, dtype=F32), np.asarray(b, dtype=F32)
+    d = (b - a).astype(F32)
+    axis = _norm3(d)
+    u, v = _frame_for(axis)
+    rows = []   # (centre, phi)
+    if caps:
+        for i in range(rings + 1):
+            rows.append((a, F32(-_HALF_PI + _HALF_PI * F32(i) / F32(rings))))
+    else:
+        rows.append((a, F32(0.0)))
+    for j in range(1, body):
+        t = F32(F32(j) / F32(body))
+        rows.append(((a + d * t).astype(F32), F32(0.0)))
+    if caps:
+        for i in range(rings + 1):
+            rows.append((b, F32(_HALF_PI * F32(i) / F32(rings))))
+    else:
+        rows.append((b, F32(0.0)))
+    pos, nrm, uv = [], [], []
+    th = (np.arange(slices + 1, dtype=F32) / F32(slices) * _TWO_PI).astype(F32)
+    ct, st = dcos(th), dsin(th)
+    for ri, (c, phi) in enumerate(rows):
+        cp, sp = dcos(phi), dsin(phi)
+        ring = ((ct[:, None] * u[None, :] + st[:, None] * v[None, :]).astype(F32) * cp + axis[None, :] * sp).astype(F32)
+        nrm.append(ring)
+        pos.append((c[None, :] + ring * F32(radius)).astype(F32))
+        uv.append(np.stack([th / _TWO_PI, np.full(slices + 1, F32(ri) / F32(len(rows) - 1), dtype=F32)], axis=1))
+    pos, nrm, uv = np.concatenate(pos), np.concatenate(nrm), np.concatenate(uv).astype(F32)
+    w = slices + 1
+    tris = []
+    nr = len(rows)
+    for r in range(nr - 1):
+        pole_lo = caps and r == 0
+        pole_hi = caps and r == nr - 2
+        for s in range(slices):
+            p0, p1, p2, p3 = r * w + s, r * w + s + 1, (r + 1) * w + s + 1, (r + 1) * w + s
+            if not pole_lo:
+                tris.append([p0, p1, p2])
+            if not pole_hi:
+                tris.append([p0, p2, p3])
+    tris = _orient(pos, nrm, np.array(tris))
+    return RawMesh(pos, nrm, uv, tris)
+
+
+HUMANOID_JOINTS = [   # (name, parent, bind position)
+    ("pelvis", -1, (0.0, 1.0, 0.0)), ("spine1", 0, (0.0, 1.15, 0.0)), ("spine2", 1, (0.0, 1.3, 0.0)),
+    ("chest", 2, (0.0, 1.45, 0.0)), ("neck", 3, (0.0, 1.58, 0.0)), ("head", 4, (0.0, 1.7, 0.0)),
+    ("l_clav", 3, (0.08, 1.5, 0.0)), ("l_upperarm", 6, (0.2, 1.48, 0.0)), ("l_forearm", 7, (0.45, 1.48, 0.0)),
+    ("l_hand", 8, (0.68, 1.48, 0.0)), ("r_clav", 3, (-0.08, 1.5, 0.0)), ("r_upperarm", 10, (-0.2, 1.48, 0.0)),
+    ("r_forearm", 11, (-0.45, 1.48, 0.0)), ("r_hand", 12, (-0.68, 1.48, 0.0)), ("l_thigh", 0, (0.1, 0.95, 0.0)),
+    ("l_shin", 14, (0.1, 0.52, 0.0)), ("l_foot", 15, (0.1, 0.08, 0.0)), ("l_toe", 16, (0.1, 0.03, -0.15)),
+    ("r_thigh", 0, (-0.1, 0.95, 0.0)), ("r_shin", 18, (-0.1, 0.52, 0.0)), ("r_foot", 19, (-0.1, 0.08, 0.0)),
+    ("r_toe", 20, (-0.1, 0.03, -0.15)),
+]
+
+# body parts: (a, b, radius, caps); shadow proxies are the head, torso, arm and leg capsules
+HUMANOID_PARTS = [
+    ((0.0, 0.95, 0.0), (0.0, 1.5, 0.0), 0.16, True), ((0.0, 1.62, 0.0), (0.0, 1.8, 0.0), 0.11, True),
+    ((0.0, 1.52, 0.0), (0.0, 1.64, 0.0), 0.05, False),
+    ((0.2, 1.48, 0.0), (0.45, 1.48, 0.0), 0.055, True), ((0.45, 1.48, 0.0), (0.68, 1.48, 0.0), 0.045, True),
+    ((0.68, 1.48, 0.0), (0.78, 1.48, 0.0), 0.04, True),
+    ((-0.2, 1.48, 0.0), (-0.45, 1.48, 0.0), 0.055, True), ((-0.45, 1.48, 0.0), (-0.68, 1.48, 0.0), 0.045, True),
+    ((-0.68, 1.48, 0.0), (-0.78, 1.48, 0.0), 0.04, True),
+    ((0.1, 0.95, 0.0), (0.1, 0.52, 0.0), 0.08, True), ((0.1, 0.52, 0.0), (0.1, 0.1, 0.0), 0.06, True),
+    ((0.1, 0.06, 0.0), (0.1, 0.05, -0.18), 0.045, True),
+    ((-0.1, 0.95, 0.0), (-0.1, 0.52, 0.0), 0.08, True), ((-0.1, 0.52, 0.0), (-0.1, 0.1, 0.0), 0.06, True),
+    ((-0.1, 0.06, 0.0), (-0.1, 0.05, -0.18), 0.045, True),
+]
+HUMANOID_PROXIES = [   # (part index, bone)
+    (1, 5), (0, 2), (3, 7), (4, 8), (6, 11), (7, 12), (9, 14), (10, 15), (12, 18), (13, 19),
+]
+
+
+def humanoid_mesh(seed: int) -> RawMesh:
+    """About 6k triangles of capsules and cylinders, skinned to the 4 nearest of 22 joints with
+    Dirichlet(1) weights quantised to u8."""
+    parts = [capsule(a, b, r, slices=16, rings=5, body=4, caps=c) for a, b, r, c in HUMANOID_PARTS]
+    m = merge(parts)
+    rng = Pcg32(seed, 7)
+    jp = np.array([p for _, _, p in HUMANOID_JOINTS], dtype=F32)
+    n = len(m.pos)
+    joints = np.zeros((n, 4), dtype=np.uint16)
+    weights = np.zeros((n, 4), dtype=np.uint8)
+    for i in range(n):
+        d = (m.pos[i][None, :] - jp).astype(F32)
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2]).astype(F32)
+        near = np.argsort(d2, kind="stable")[:4]
+        u = np.array([F32(((rng.next_u32() >> 8) + 1)) * F32(1.0 / 16777216.0) for _ in range(4)], dtype=F32)
+        e = (-dlog(u)).astype(F32)
+        s = F32(F32(F32(e[0] + e[1]) + e[2]) + e[3])
+        w = (e / s).astype(F32)
+        joints[i] = near
+        weights[i] = np.floor((w * F32(255.0) + F32(0.5)).astype(F32)).astype(np.uint8)
+    m.joints, m.weights = joints, weights
+    return m
+
+
+def _quat_axis_angle(axis, ang):
+    h = F32(F32(ang) * F32(0.5))
+    s, c = dsin(h), dcos(h)
+    return np.array([axis[0] * s, axis[1] * s, axis[2] * s, c], dtype=F32)
+
+
+def _quat_to_mat(q):
+    """sft_m_from_quat layout (sofren2.c:1822)."""
+    x, y, z, w = (F32(v) for v in q)
+    x2, y2, z2 = F32(x + x), F32(y + y), F32(z + z)
+    xx, xy, xz = F32(x * x2), F32(x * y2), F32(x * z2)
+    yy, yz, zz = F32(y * y2), F32(y * z2), F32(z * z2)
+    wx, wy, wz = F32(w * x2), F32(w * y2), F32(w * z2)
+    m = mat_identity()
+    m[0, 0], m[0, 1], m[0, 2] = F32(1.0) - F32(yy + zz), F32(xy + wz), F32(xz - wy)
+    m[1, 0], m[1, 1], m[1, 2] = F32(xy - wz), F32(1.0) - F32(xx + zz), F32(yz + wx)
+    m[2, 0], m[2, 1], m[2, 2] = F32(xz + wy), F32(yz - wx), F32(1.0) - F32(xx + yy)
+    return m
+
+
+class HumanoidAnim:
+    """30 keyframes per joint of a sinusoidal local rotation (amplitude U[0, 0.6] rad, seeded
+    axis and phase), normalised-linear interpolation between keys."""
+
+    def __init__(self, seed: int, keys: int = 30):
+        rng = Pcg32(seed, 11)
+        self.keys = keys
+        self.q = np.zeros((len(HUMANOID_JOINTS), keys, 4), dtype=F32)
+        for j in range(len(HUMANOID_JOINTS)):
+            ax = _norm3(np.array([rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(-1, 1)], dtype=F32) + F32(1e-3))
+            amp, ph = rng.uniform(0.0, 0.6), rng.uniform(0.0, 1.0)
+            for k in range(keys):
+                t = F32(F32(k) / F32(keys - 1))
+                ang = F32(amp * dsin(F32(_TWO_PI * F32(t + ph))))
+                self.q[j, k] = _quat_axis_angle(ax, ang)
+
+    def pose(self, t: float) -> np.ndarray:
+        """Posed bone matrices (inverse bind x global), [22, 4, 4] float32, at clip time t in [0, 1)."""
+        ft = F32(F32(t) * F32(self.keys - 1))
+        k0 = int(np.floor(ft)) % (self.keys - 1)
+        a = F32(ft - F32(k0))
+        glob = []
+        out = np.zeros((len(HUMANOID_JOINTS), 4, 4), dtype=F32)
+        for j, (_, parent, bp) in enumerate(HUMANOID_JOINTS):
+            q0, q1 = self.q[j, k0], self.q[j, k0 + 1]
+            q = (q0 + (q1 - q0) * a).astype(F32)
+            q = (q / F32(np.sqrt(F32(F32(F32(q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3])))).astype(F32)
+            if parent < 0:
+                off = np.asarray(bp, dtype=F32)
+            else:
+                off = (np.asarray(bp, dtype=F32) - np.asarray(HUMANOID_JOINTS[parent][2], dtype=F32)).astype(F32)
+            local = mat_mul(_quat_to_mat(q), mat_translate(*off))
+            g = local if parent < 0 else mat_mul(local, glob[parent])
+            glob.append(g)
+            inv_bind = mat_translate(*(-np.asarray(bp, dtype=F32)))
+            out[j] = mat_mul(inv_bind, g)
+        return out
+
+
+def humanoid_model(sc: Scene, seed: int, tex_size: int = 512) -> int:
+    mesh = humanoid_mesh(seed)
+    ml = build_meshlets(mesh)
+    # skinned bounds must hold the deformed meshlet around the culling bone
+    ml.cull[:, 3] = (ml.cull[:, 3] * F32(1.5) + F32(0.25)).astype(F32)
+    tex = sc.add_texture(value_noise_texture(tex_size, tex_size, seed * 17 + 3))
+    mat = sc.add_material(tex, 0xFFFFFFFF, 16.0)
+    proxies = []
+    for part, bone in HUMANOID_PROXIES:
+        a, b, r, _ = HUMANOID_PARTS[part]
+        proxies.append((a, b, r, bone))
+    return sc.add_model(Model([ml], [mat], bone_count=len(HUMANOID_JOINTS), proxies=proxies))
+
+
+def ground_model(sc: Scene, seed: int, n: int = 64, half: float = 16.0, center=(0.0, 0.0, 8.0), tex_size: int = 512,
+                 lightmap: int | None = None) -> int:
+    cx, cy, cz = (F32(c) for c in center)
+    xs = (np.arange(n + 1, dtype=F32) / F32(n) * F32(2 * half) - F32(half)).astype(F32)
+    pos, nrm, uv, tris = [], [], [], []
+    for j in range(n + 1):
+        for i in range(n + 1):
+            pos.append([F32(cx + xs[i]), cy, F32(cz + xs[j])])
+            nrm.append([0.0, 1.0, 0.0])
+            uv.append([F32(i) / F32(8), F32(j) / F32(8)])
+    for j in range(n):
+        for i in range(n):
+            a, b, c, d = j * (n + 1) + i, j * (n + 1) + i + 1, (j + 1) * (n + 1) + i + 1, (j + 1) * (n + 1) + i
+            tris += [[a, b, c], [a, c, d]]
+    pos, nrm = np.array(pos, dtype=F32), np.array(nrm, dtype=F32)
+    mesh = RawMesh(pos, nrm, np.array(uv, dtype=F32), _orient(pos, nrm, np.array(tris)))
+    tex = sc.add_texture(value_noise_texture(tex_size, tex_size, seed * 19 + 5))
+    mat = sc.add_material(tex, 0xFFFFFFFF, 32.0)
+    return sc.add_model(Model([build_meshlets(mesh)], [mat]))
+
+
+def skinned_characters_scene(width=1920, height=1080, seed=2001, n_chars=8, n_lights=4, tex_size=512, frames=1,
+                             ground_quads=64, time0=0.0) -> Scene:
+    """Skinned humanoids on a ground plane, lit by point lights above them; one capsule proxy per
+    head, torso, upper/lower arm and thigh/shin."""
+    rng = Pcg32(seed)
+    sc = Scene()
+    ground = ground_model(sc, seed, n=ground_quads)
+    chars, anims = [], []
+    for c in range(n_chars):
+        chars.append(humanoid_model(sc, seed * 97 + c, tex_size))
+        anims.append(HumanoidAnim(seed * 89 + c))
+    place = []
+    for c in range(n_chars):
+        col, row = c % 4, c // 4
+        x = F32(F32(-3.0 + 2.0 * col) + rng.uniform(-0.3, 0.3))
+        z = F32(F32(5.0 + 3.0 * row) + rng.uniform(-0.3, 0.3))
+        yaw = rng.uniform(0.0, 6.28318530717959)
+        place.append(mat_mul(mat_rot_y(yaw), mat_translate(x, F32(0.0), z)))
+    lights = []
+    for l in range(n_lights):
+        lp = (rng.uniform(-6.0, 6.0), rng.uniform(5.0, 7.0), rng.uniform(3.0, 11.0))
+        col = (rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0))
+        lights.append((lp, col[0], col[1], col[2], F32(1.0), F32(14.0)))
+    for fi in range(frames):
+        fr = _camera_frame(width, height, cam_pos=(0.0, 1.7, 0.0), target=(0.0, 1.0, 8.0))
+        fr.ambient = np.array([0.15, 0.15, 0.17], dtype=F32)
+        fr.point_lights = list(lights)
+        t = F32(time0 + fi / max(frames, 1)) % F32(1.0)
+        insts = [(ground, mat_identity(), None)]
+        for c in range(n_chars):
+            insts.append((chars[c], place[c], anims[c].pose(t)))
+        fr.instances = insts
+        sc.frames.append(fr)
+    return sc
+
+
+def config2(width=1920, height=1080, seed=2001) -> Scene:
+    """Skinned characters at 1920x1080 (rendered with 2x MSAA): eight ~6k-triangle humanoids on
+    a 22-joint skeleton, ground of 64x64 quads, four point lights, 512x512 textures."""
+    return skinned_characters_scene(width, height, seed)
+
+
+# ------------------------------------------------------------------ edge-case variety scene
+def variety_scene(width=320, height=200, seed=4001, n_objects=20, n_lights=18, n_dir=2, near_camera=True,
+                  clear=1) -> Scene:
+    """Parity scene for the less common branches: camera inside the object field (near-plane
+    clipping), untextured and emissive materials, NPOT textures with non-negative UVs,
+    directional lights, more point lights than the per-tile cap of 16, optional no-clear."""
+    rng = Pcg32(seed)
+    sc = Scene()
+    sphere_ml = build_meshlets(uv_sphere(16, 8, 0.5))
+    cube_ml = build_meshlets(box((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    # NPOT bilinear reads are only defined for texel coordinates >= 0 in the reference
+    # (sofren2.c:5594-5600), so the NPOT material's UVs stay inside [0.1, 0.9]
+    inner = uv_sphere(16, 8, 0.5)
+    inner.uv = (inner.uv * F32(0.8) + F32(0.1)).astype(F32)
+    sphere_npot_ml = build_meshlets(inner)
+    tex_pot = sc.add_texture(value_noise_texture(64, 64, seed + 1, lattice=8))
+    tex_npot = sc.add_texture(value_noise_texture(48, 40, seed + 2, lattice=8))
+    mats = [sc.add_material(tex_pot, 0xFFFFFFFF, 16.0), sc.add_material(tex_npot, 0xFFC08040, 8.0),
+            sc.add_material(-1, 0xFF80C0FF, 4.0), sc.add_material(tex_pot, 0xFFFFFFFF, -1.5),
+            sc.add_material(-1, 0xFFFFFFFF, 64.0)]
+    models = []
+    for k, mat in enumerate(mats):
+        models.append(sc.add_model(Model([sphere_npot_ml if k == 1 else sphere_ml], [mat], proxies=[((0, 0, 0), (0, 0, 0), 0.45, 0xFFFFFFFF)])))
+        if k != 1:
+            models.append(sc.add_model(Model([cube_ml], [mat], proxies=[((0, -0.2, 0), (0, 0.2, 0), 0.4, 0xFFFFFFFF)])))
+    insts = []
+    zc = 2.0 if near_camera else 8.0
+    for i in range(n_objects):
+        mi = models[i % len(models)]
+        p = (rng.uniform(-3, 3), rng.uniform(-2, 2), F32(zc + rng.uniform(-2.0, 4.0)))
+        s = rng.uniform(0.5, 1.8)
+        tr = mat_mul(mat_mul(mat_scale(s), mat_rot_y(rng.uniform(0, 6.28318530717959))), mat_translate(*p))
+        insts.append((mi, tr, None))
+    lights = []
+    for l in range(n_lights):
+        lp = (rng.uniform(-4, 4), F32(rng.uniform(9.0, 11.0)), rng.uniform(3.0, 9.0))
+        lights.append((lp, rng.uniform(0.3, 1.0), rng.uniform(0.3, 1.0), rng.uniform(0.3, 1.0), F32(0.8), rng.uniform(12.0, 20.0)))
+    fr = _camera_frame(width, height)
+    fr.ambient = np.array([0.12, 0.1, 0.1], dtype=F32)
+    fr.point_lights = lights
+    fr.dir_lights = [((rng.uniform(-1, 1), F32(-1.0), rng.uniform(-1, 1)), F32(0.8), F32(0.8), F32(0.7), F32(0.6))
+                     for _ in range(n_dir)]
+    fr.clear = clear
+    fr.instances = insts
+    sc.frames.append(fr)
+    return sc
+
+
+# ------------------------------------------------------------------ lightmapped atrium
+class _QuadMesh:
+    """Accumulates quads (4 verts, 2 tris) with flat normals, UVs and a lightmap chart each."""
+
+    def __init__(self, lm_size: int, chart_base: list):
+        self.pos, self.nrm, self.uv, self.luv, self.tris = [], [], [], [], []
+        self.lm_size, self.chart = lm_size, chart_base   # shared [next chart index]
+
+    def quad(self, p0, p1, p2, p3, n, uv_scale=1.0):
+        base = len(self.pos)
+        c = self.chart[0]
+        self.chart[0] += 1
+        cols = self.lm_size // 2
+        cx, cy = (c % cols) * 2, (c // cols) * 2
+        inv = F32(1.0 / self.lm_size)
+        corners = ((0, 0), (0, 1), (1, 1), (1, 0))
+        for (p, (i, j)) in zip((p0, p1, p2, p3), corners):
+            self.pos.append(p)
+            self.nrm.append(n)
+            self.uv.append([F32(i) * F32(uv_scale), F32(j) * F32(uv_scale)])
+            self.luv.append([F32(F32(cx + i) + F32(0.5)) * inv, F32(F32(cy + j) + F32(0.5)) * inv])
+        self.tris += [[base, base + 1, base + 2], [base, base + 2, base + 3]]
+
+    def box(self, lo, hi, uv_scale=1.0):
+        lo, hi = np.asarray(lo, dtype=F32), np.asarray(hi, dtype=F32)
+        for ax in range(3):
+            for sgn in (-1, 1):
+                ua, va = [a for a in range(3) if a != ax]
+                n = np.zeros(3, dtype=F32); n[ax] = F32(sgn)
+                pts = []
+                for (cu, cv) in ((0, 0), (0, 1), (1, 1), (1, 0)):
+                    p = np.zeros(3, dtype=F32)
+                    p[ax] = hi[ax] if sgn > 0 else lo[ax]
+                    p[ua] = hi[ua] if cu else lo[ua]
+                    p[va] = hi[va] if cv else lo[va]
+                    pts.append(p)
+                e1, e2 = (pts[1] - pts[0]).astype(F32), (pts[2] - pts[0]).astype(F32)
+                if _dot3(_cross3(e1, e2), n) < 0:
+                    pts = [pts[0], pts[3], pts[2], pts[1]]
+                self.quad(*pts, n, uv_scale)
+
+    def raw(self) -> RawMesh:
+        pos = np.array(self.pos, dtype=F32).reshape(-1, 3)
+        return RawMesh(pos, np.array(self.nrm, dtype=F32), np.array(self.uv, dtype=F32), np.array(self.tris).reshape(-1, 3),
+                       luv=np.array(self.luv, dtype=F32))
+
+
+def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arch_segments=16, n_tex=25,
+                 tex_size=1024, lm_size=1024, n_lights=16, n_chars=4, char_tex=512, floor_quads=(120, 60), frames=1) -> Scene:
+    """An atrium of pillars and semicircular arches (boxes, arch_segments per arch) on `levels`
+    floors of an nx x nz grid, floor and walls as quad grids; every static quad owns a 2x2 texel
+    chart in one lightmap page holding per-vertex baked colours uniform in [0,1]^3.  Point
+    lights sit under the roof with a radius that covers the whole atrium, and skinned humanoids
+    stand on the floor."""
+    rng = Pcg32(seed)
+    sc = Scene()
+    chart = [0]
+    groups = [_QuadMesh(lm_size, chart) for _ in range(n_tex)]
+    x0, x1, z0, z1, height_m = -15.0, 15.0, 4.0, 19.0, 15.0
+    fq = _QuadMesh(lm_size, chart)
+    fx, fz = floor_quads
+    for j in range(fz):
+        for i in range(fx):
+            ax, bx = F32(x0 + (x1 - x0) * i / fx), F32(x0 + (x1 - x0) * (i + 1) / fx)
+            az, bz = F32(z0 + (z1 - z0) * j / fz), F32(z0 + (z1 - z0) * (j + 1) / fz)
+            fq.quad(np.array([ax, 0, az], F32), np.array([ax, 0, bz], F32), np.array([bx, 0, bz], F32),
+                    np.array([bx, 0, az], F32), np.array([0, 1, 0], F32), 0.25)
+    wq = _QuadMesh(lm_size, chart)
+    wy = max(1, fz)
+    for j in range(wy):
+        for i in range(fx):
+            ax, bx = F32(x0 + (x1 - x0) * i / fx), F32(x0 + (x1 - x0) * (i + 1) / fx)
+            ay, by = F32(height_m * j / wy), F32(height_m * (j + 1) / wy)
+            wq.quad(np.array([ax, ay, z1], F32), np.array([ax, by, z1], F32), np.array([bx, by, z1], F32),
+                    np.array([bx, ay, z1], F32), np.array([0, 0, -1], F32), 0.25)
+    dx, dz = (x1 - x0) / nx, (z1 - z0) / nz
+    lvl_h = height_m / levels
+    pw = 0.18
+    for lv in range(levels):
+        yb = lv * lvl_h
+        ph = lvl_h * 0.55
+        for iz in range(nz):
+            for ix in range(nx):
+                g = groups[(ix + iz * nx + lv * 7) % n_tex]
+                cxp, czp = x0 + dx * (ix + 0.5), z0 + dz * (iz + 0.5)
+                g.box((cxp - pw, yb, czp - pw), (cxp + pw, yb + ph, czp + pw))
+                for (ddx, ddz) in ((1, 0), (0, 1)):
+                    if (ddx and ix == nx - 1) or (ddz and iz == nz - 1):
+                        continue
+                    span = dx if ddx else dz
+                    rad = span * 0.5
+                    for sgi in range(arch_segments):
+                        a0 = F32(_PI * sgi / arch_segments)
+                        a1 = F32(_PI * (sgi + 1) / arch_segments)
+                        am = F32((a0 + a1) * F32(0.5))
+                        ca, sa = float(dcos(am)), float(dsin(am))
+                        cx_ = cxp + ddx * (rad - rad * ca)
+                        cz_ = czp + ddz * (rad - rad * ca)
+                        cy_ = yb + ph + rad * sa
+                        hl = rad * np.pi / arch_segments * 0.5 + 0.01
+                        ext = (hl if ddx else 0.08, 0.06, hl if ddz else 0.08)
+                        g.box((cx_ - ext[0], cy_ - ext[1], cz_ - ext[2]), (cx_ + ext[0], cy_ + ext[1], cz_ + ext[2]))
+    assert chart[0] * 4 <= lm_size * lm_size, "lightmap page too small for the quad charts"
+    lm = np.full((lm_size, lm_size), 0xFF000000, dtype=np.uint32)
+    cols_rgb = np.zeros((chart[0] * 4, 3), dtype=np.uint32)
+    for k in range(chart[0] * 4):
+        cols_rgb[k] = [rng.next_u32() >> 24, rng.next_u32() >> 24, rng.next_u32() >> 24]
+    cols = lm_size // 2
+    ci = np.arange(chart[0])
+    cx, cy = (ci % cols) * 2, (ci // cols) * 2
+    for q, (i, j) in enumerate(((0, 0), (0, 1), (1, 1), (1, 0))):
+        c = cols_rgb[q::4]
+        lm[cy + j, cx + i] = 0xFF000000 | (c[:, 0] << 16) | (c[:, 1] << 8) | c[:, 2]
+    lm_tex = sc.add_texture(lm)
+    tex_ids = [sc.add_texture(value_noise_texture(tex_size, tex_size, seed * 31 + t)) for t in range(n_tex)]
+    meshes, mats = [], []
+    for t, g in enumerate(groups + [fq, wq]):
+        if not g.tris:
+            continue
+        meshes.append(build_meshlets(g.raw()))
+        mats.append(sc.add_material(tex_ids[t % n_tex], 0xFFFFFFFF, 16.0))
+    atrium = sc.add_model(Model(meshes, mats, lightmaps=[lm_tex], lightmap_pages=[0] * len(meshes)))
+    chars, anims = [], []
+    for c in range(n_chars):
+        chars.append(humanoid_model(sc, seed * 97 + c, char_tex))
+        anims.append(HumanoidAnim(seed * 89 + c))
+    place = []
+    for c in range(n_chars):
+        x = F32(F32(-1.5 + 1.0 * c) + rng.uniform(-0.2, 0.2))
+        z = F32(rng.uniform(5.5, 7.0))
+        place.append(mat_mul(mat_rot_y(rng.uniform(0.0, 6.28318530717959)), mat_translate(x, F32(0.0), z)))
+    lights = []
+    for l in range(n_lights):
+        lp = (rng.uniform(-12.0, 12.0), rng.uniform(13.0, 14.5), rng.uniform(6.0, 17.0))
+        lights.append((lp, rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0), F32(0.5), F32(60.0)))
+    for fi in range(frames):
+        fr = _camera_frame(width, height, cam_pos=(0.0, 1.7, 0.5), target=(0.0, 3.0, 12.0))
+        fr.ambient = np.array([0.1, 0.1, 0.1], dtype=F32)
+        fr.point_lights = list(lights)
+        t = F32(fi / max(frames, 1))
+        fr.instances = [(atrium, mat_identity(), None)] + [(chars[c], place[c], anims[c].pose(t)) for c in range(n_chars)]
+        sc.frames.append(fr)
+    return sc
+
+
+def config3(width=1920, height=1080, seed=3001) -> Scene:
+    """Large static scene (rendered with 4x MSAA): about 262k triangles of boxes and
+    semicircular arches forming a 30x15x15 m atrium, 25 textures of 1024x1024, a baked
+    lightmap page, four skinned characters, sixteen point lights covering the floor."""
+    return atrium_scene(width, height, seed)

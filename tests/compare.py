@@ -35,8 +35,10 @@ def compare_frames(ref: dict, other: dict, samples: int) -> dict:
         out["ss_cache"] = int(np.count_nonzero(live[mask] != os_.reshape(-1, 9 * 64)[mask]))
     else:
         out["ss_cache"] = -1
+    # the reference reserves clip slots 64 at a time (sofren2.c:4356-4361): only its used prefix compares
     rc, oc = ref["clip"].view(np.uint32), other["clip"].view(np.uint32)
-    out["clip"] = int(np.count_nonzero(rc != oc)) if rc.size == oc.size else -1
+    n = min(rc.size, oc.size)
+    out["clip"] = int(np.count_nonzero(rc[:n] != oc[:n])) if (rc.size == oc.size or rc.size % (64 * 41) == 0) else -1
     out["light_vis"] = int(np.count_nonzero(ref["light_vis"].reshape(-1, 64) != other["light_vis"].reshape(-1, 64))) \
         if ref["light_vis"].size == other["light_vis"].size else -1
     if "tlas" in ref and "tlas" in other:

@@ -1,0 +1,49 @@
+"""Regenerates tests/golden/golden.json from the reference itself.
+
+Requires the reference sources at /root/reference (or SFT_REFERENCE_DIR) on an x86-64 host
+with AVX2: `make -C oracle ref` compiles them unmodified into oracle/_ref, and each golden case
+(tests/golden_cases.py) is rendered by that binary with one worker thread.  Stored per case and
+sample count: the SHA-256 of the scene blob and of every dump section, the live meshlet list
+and the number of used clip slots, plus the reference's sft_present time.
+
+    python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TESTS = os.path.dirname(HERE)
+ROOT = os.path.dirname(TESTS)
+sys.path.insert(0, TESTS)
+sys.path.insert(0, ROOT)
+
+import golden_cases as gc  # noqa: E402
+from oracle_lib import reference_dump  # noqa: E402
+
+
+def main(names: list[str]) -> None:
+    ref_dir = os.environ.get("SFT_REFERENCE_DIR", "/root/reference")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={ref_dir}"], check=True)
+    path = os.path.join(HERE, "golden.json")
+    golden = json.load(open(path)) if os.path.exists(path) else {}
+    for name in names or list(gc.CASES):
+        blob = gc.blob(name)
+        entry = {"generator": gc.CASES[name][0], "kwargs": gc.CASES[name][1], "scene_sha256": gc.sha(memoryview(blob)),
+                 "samples": {}}
+        for S in gc.SAMPLES[name]:
+            frame = reference_dump(blob, S)[0]
+            d, live = gc.digests(frame)
+            d["live_meshlets"] = live
+            d["reference_present_ms"] = float(frame["present_ns"][0]) / 1e6
+            entry["samples"][str(S)] = d
+            print(name, S, "payloads", int(frame["tile_counts"].sum()), "clips", d["clip_used"], flush=True)
+        golden[name] = entry
+    json.dump(golden, open(path, "w"), indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,67 @@
+"""The golden parity cases: seeded scenes rendered by the reference (tests/golden/make_golden.py)
+and re-checked against the CPU oracle and the GPU library.  Each case names a scene generator
+and its arguments; the scene bytes themselves are regenerated deterministically (their SHA-256
+is pinned too, so a platform that generated different bytes fails loudly)."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+
+from sofren2_gb300 import scenes
+
+CASES = {
+    "small": ("static_shapes_scene", dict(width=200, height=136, seed=7, n_spheres=3, n_cubes=3, tex_size=64)),
+    "config1": ("config1", dict()),
+    "skinned_small": ("skinned_characters_scene", dict(width=640, height=360, seed=3, n_chars=4, tex_size=64, ground_quads=16)),
+    "atrium_small": ("atrium_scene", dict(width=320, height=200, seed=5, nx=4, nz=3, levels=2, arch_segments=8, n_tex=3,
+                                          tex_size=64, lm_size=256, n_lights=5, n_chars=2, char_tex=64, floor_quads=(12, 6))),
+    "variety": ("variety_scene", dict()),
+    "variety_noclear": ("variety_scene", dict(seed=4002, clear=0)),
+    "config2": ("config2", dict()),
+    "config3": ("config3", dict()),
+}
+
+# cases the CPU oracle re-checks in the default (not-gpu) test run; the big configurations are
+# checked on the GPU against their digests, and against the oracle in the slow tier
+FAST = ["small", "config1", "skinned_small", "atrium_small", "variety", "variety_noclear"]
+SAMPLES = {name: (1, 2, 4) for name in CASES}
+SAMPLES["config2"] = (2,)
+SAMPLES["config3"] = (4,)
+
+_cache: dict = {}
+
+
+def scene(name: str):
+    if name not in _cache:
+        fn, kw = CASES[name]
+        _cache[name] = getattr(scenes, fn)(**kw)
+    return _cache[name]
+
+
+def blob(name: str) -> bytes:
+    key = ("blob", name)
+    if key not in _cache:
+        _cache[key] = scene(name).to_bytes()
+    return _cache[key]
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def digests(frame: dict, live_meshlets: list[int] | None = None, clip_used: int | None = None) -> dict:
+    """Digest of every parity section of a render dump.  ss_cache is digested over the live
+    (drawn) meshlets only: culled slots are never written.  The clip pool over its used prefix."""
+    out = {k: sha(frame[k]) for k in ("color", "tile_counts", "tile_payloads", "vid", "light_vis")}
+    out["depth"] = sha(frame["depth"].view(np.uint32))
+    ss = frame["ss_cache"].view(np.uint32).reshape(-1, 576)
+    if live_meshlets is None:
+        live_meshlets = np.nonzero(~np.all(ss == 0xFFFFFFFF, axis=1))[0].tolist()
+    out["ss_cache_live"] = sha(ss[np.asarray(live_meshlets, dtype=np.int64)]) if len(live_meshlets) else sha(np.zeros(0))
+    clip = frame["clip"].view(np.uint32).reshape(-1, 41)
+    if clip_used is None:
+        clip_used = int(np.count_nonzero(clip[:, 6] != 0))   # inv_w of a used slot is never 0
+    out["clip_used"] = clip_used
+    out["clip"] = sha(clip[:clip_used])
+    return out, live_meshlets

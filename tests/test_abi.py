@@ -1,0 +1,91 @@
+"""The C ABI and host pieces that need no GPU: every function declared in include/*.h is
+exported by libsofren2_gb300.so, and the measured RCPPS/RSQRTPS tables reproduce the x86
+instructions (checked against the instructions themselves where the host is x86-64)."""
+import ctypes as C
+import os
+import platform
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from sofren2_gb300 import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared(header: str) -> set[str]:
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = src.split("#ifdef SFT_IMPL")[0]
+    return set(re.findall(r"^(?:SFT_FUNC|int|void|const char\*)\s+[\w\s\*]*?\b((?:sft|sftg)_\w+)\s*\(", src, re.M))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    return build.build_library()
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    lib = C.CDLL(lib_path)
+    declared = _declared("sofren2.h") | _declared("sftg.h")
+    assert len(declared) > 60
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_scene_player_symbols(lib_path):
+    lib = C.CDLL(lib_path)
+    for s in ("sftx_scene_load", "sftx_scene_render", "sftx_scene_free", "sftx_scene_frame_count"):
+        assert hasattr(lib, s)
+
+
+def test_build_targets_sm103a_only():
+    assert build.ARCH == "-gencode=arch=compute_103a,code=sm_103a"
+
+
+@pytest.mark.skipif(platform.machine() != "x86_64", reason="needs the x86 RCPPS/RSQRTPS instructions")
+def test_approx_tables_match_instructions():
+    src = r'''
+#include <immintrin.h>
+#include <stdio.h>
+#include <stdint.h>
+#include <string.h>
+#include "x86_approx_tables.h"
+static const uint32_t R[2048] = SFT_X86_RCP_TABLE_INIT, Q[2048] = SFT_X86_RSQRT_TABLE_INIT;
+static uint32_t rcp_t(uint32_t x){uint32_t s=x&0x80000000u,e=(x>>23)&255,m=x&0x7FFFFF;
+ if(e==255)return m?(x|0x400000u):s; if(e==0)return s|0x7F800000u; if(e>=253)return s; return s|((253u-e)<<23)|R[m>>12];}
+static uint32_t rsq_t(uint32_t x){uint32_t s=x&0x80000000u,e=(x>>23)&255,m=x&0x7FFFFF;
+ if(e==255){if(m)return x|0x400000u;return s?0xFFC00000u:0u;} if(e==0)return s|0x7F800000u; if(s)return 0xFFC00000u;
+ uint32_t t=Q[(e&1)*1024+(m>>13)]; int oe=((380-(int)e)>>1)+(int)(t>>23)-1; return ((uint32_t)oe<<23)|(t&0x7FFFFF);}
+int main(void){uint64_t st=0x9E3779B97F4A7C15ull; unsigned bad=0;
+ for(int i=0;i<(1<<22);i++){st^=st<<13;st^=st>>7;st^=st<<17; uint32_t x=(uint32_t)st; float f; memcpy(&f,&x,4);
+  float r=_mm_cvtss_f32(_mm_rcp_ss(_mm_set_ss(f))), q=_mm_cvtss_f32(_mm_rsqrt_ss(_mm_set_ss(f))); uint32_t a,b; memcpy(&a,&r,4); memcpy(&b,&q,4);
+  if(a!=rcp_t(x)||b!=rsq_t(x))bad++;} printf("%u\n",bad); return bad!=0;}
+'''
+    with tempfile.TemporaryDirectory() as td:
+        c, exe = os.path.join(td, "t.c"), os.path.join(td, "t")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-O1", "-msse", "-I", os.path.join(ROOT, "sofren2_gb300", "csrc"), c, "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, f"{r.stdout.strip()} mismatching inputs"
+
+
+def test_product_and_oracle_tables_identical():
+    a = open(os.path.join(ROOT, "sofren2_gb300", "csrc", "x86_approx_tables.h")).read()
+    b = open(os.path.join(ROOT, "oracle", "x86_approx_tables.h")).read()
+    assert a == b
+
+
+def test_scene_generation_is_platform_independent():
+    """Only IEEE add/sub/mul/div/sqrt feed the scenes: the deterministic sin/log stay within
+    their polynomial error, and two generations give identical bytes."""
+    from sofren2_gb300 import scenes
+    x = np.linspace(-20, 20, 2001, dtype=np.float32)
+    assert np.max(np.abs(scenes.dsin(x) - np.sin(x.astype(np.float64)))) < 2e-6
+    y = np.linspace(0.01, 50, 999, dtype=np.float32)
+    assert np.max(np.abs(scenes.dlog(y) - np.log(y.astype(np.float64)))) < 5e-6
+    a = scenes.static_shapes_scene(64, 64, seed=3, n_spheres=2, n_cubes=1, tex_size=16).to_bytes()
+    b = scenes.static_shapes_scene(64, 64, seed=3, n_spheres=2, n_cubes=1, tex_size=16).to_bytes()
+    assert a == b

@@ -1,0 +1,77 @@
+"""The CPU oracle against the reference's golden digests, and against the reference itself on
+fresh seeds where the reference is compiled here (oracle/_ref, x86-64 only)."""
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from compare import compare_frames
+from oracle_lib import Oracle, reference_available, reference_dump
+
+
+@pytest.mark.parametrize("name", gc.FAST)
+def test_scene_bytes_pinned(golden, name):
+    assert gc.sha(memoryview(gc.blob(name))) == golden[name]["scene_sha256"]
+
+
+@pytest.mark.parametrize("name", gc.FAST)
+def test_oracle_matches_reference_digests(golden, name):
+    o = Oracle(gc.blob(name))
+    try:
+        for S in gc.SAMPLES[name]:
+            g = golden[name]["samples"][str(S)]
+            frame = o.render_dump(0, S)
+            d, _ = gc.digests(frame, g["live_meshlets"], g["clip_used"])
+            mism = [k for k in d if k in g and d[k] != g[k]]
+            assert not mism, f"{name} {S}x: sections differ from the reference: {mism}"
+            assert frame["invalid_packets"] == 0
+    finally:
+        o.close()
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("name", ["config2", "config3"])
+def test_oracle_matches_reference_digests_full(golden, name):
+    o = Oracle(gc.blob(name))
+    try:
+        for S in gc.SAMPLES[name]:
+            g = golden[name]["samples"][str(S)]
+            d, _ = gc.digests(o.render_dump(0, S, threads=8), g["live_meshlets"], g["clip_used"])
+            assert [k for k in d if k in g and d[k] != g[k]] == []
+    finally:
+        o.close()
+
+
+SEEDS = [11, 12, 13]
+
+
+@pytest.mark.skipif(not reference_available(1), reason="reference not compiled here (oracle/_ref, x86-64 with AVX2)")
+@pytest.mark.parametrize("seed", SEEDS)
+@pytest.mark.parametrize("samples", [1, 2, 4])
+def test_oracle_equals_reference_random(seed, samples):
+    from sofren2_gb300 import scenes
+    sc = scenes.variety_scene(width=192, height=128, seed=seed, n_objects=14, n_lights=6 + seed % 12)
+    blob = sc.to_bytes()
+    r = reference_dump(blob, samples)[0]
+    o = Oracle(blob)
+    try:
+        g = o.render_dump(0, samples)
+    finally:
+        o.close()
+    res = compare_frames(r, g, samples)
+    bad = {k: v for k, v in res.items() if k != "color_max_lsb" and v != 0}
+    assert not bad, res
+
+
+def test_oracle_detects_undefined_packet_frustum():
+    """A light inside a proxy batch's bounding box leaves the reference's packet frustum
+    uninitialised (sofren2.c:4044-4048); the oracle counts those packets so parity scenes can
+    exclude them."""
+    from sofren2_gb300 import scenes
+    sc = scenes.static_shapes_scene(160, 96, seed=9, n_spheres=4, n_cubes=4, tex_size=32)
+    lp, *rest = sc.frames[0].point_lights[0]
+    sc.frames[0].point_lights = [((np.float32(0.0), np.float32(0.0), np.float32(25.0)), *rest)]
+    o = Oracle(sc.to_bytes())
+    try:
+        assert o.render_dump(0, 1)["invalid_packets"] > 0
+    finally:
+        o.close()
