@@ -460,6 +460,7 @@ static int launch_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, const frame_bu
     CK(cudaMemsetAsync(B.status, 0, 64, st));
     CK(cudaEventRecord(ctx->ev[0], st));
     if (fd->shadows && fd->n_point && fd->n_proxies) {
+        CK(cudaMemsetAsync(B.light_vis, 0, (size_t)fd->n_proxies * 64, st));   /* columns past the lights stay 0 */
         sftg_launch_occlusion(B.F, fd->n_point, fd->n_proxies, fd->n_instances, B.packets, B.pairs, B.n_pairs, B.max_pairs,
                               B.light_vis, B.status, st);
         ctx->launches += 3;

@@ -14,8 +14,10 @@ def _nodes_meaningful(raw: np.ndarray) -> np.ndarray:
     return raw[: n * 256].reshape(n, 256)[:, :NODE_FIELDS]
 
 
-def compare_frames(ref: dict, other: dict, samples: int) -> dict:
-    """Returns {section: mismatch count} (0 everywhere means bit-exact)."""
+def compare_frames(ref: dict, other: dict, samples: int, n_lights: int = 64) -> dict:
+    """Returns {section: mismatch count} (0 everywhere means bit-exact).  light_vis is compared
+    for the frame's first min(n_lights, 64) lights: the reference writes no other column
+    (sofren2.c:8166-8173)."""
     out = {}
     out["color"] = int(np.count_nonzero(ref["color"] != other["color"]))
     out["color_max_lsb"] = int(np.max(np.abs(
@@ -39,7 +41,8 @@ def compare_frames(ref: dict, other: dict, samples: int) -> dict:
     rc, oc = ref["clip"].view(np.uint32), other["clip"].view(np.uint32)
     n = min(rc.size, oc.size)
     out["clip"] = int(np.count_nonzero(rc[:n] != oc[:n])) if (rc.size == oc.size or rc.size % (64 * 41) == 0) else -1
-    out["light_vis"] = int(np.count_nonzero(ref["light_vis"].reshape(-1, 64) != other["light_vis"].reshape(-1, 64))) \
+    nl = min(n_lights, 64)
+    out["light_vis"] = int(np.count_nonzero(ref["light_vis"].reshape(-1, 64)[:, :nl] != other["light_vis"].reshape(-1, 64)[:, :nl])) \
         if ref["light_vis"].size == other["light_vis"].size else -1
     if "tlas" in ref and "tlas" in other:
         a, b = _nodes_meaningful(ref["tlas"]), _nodes_meaningful(other["tlas"])

@@ -36,7 +36,7 @@ def main(names: list[str]) -> None:
                  "samples": {}}
         for S in gc.SAMPLES[name]:
             frame = reference_dump(blob, S)[0]
-            d, live = gc.digests(frame)
+            d, live = gc.digests(frame, lights=gc.n_lights(name))
             d["live_meshlets"] = live
             d["reference_present_ms"] = float(frame["present_ns"][0]) / 1e6
             entry["samples"][str(S)] = d

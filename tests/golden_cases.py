@@ -50,10 +50,17 @@ def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def digests(frame: dict, live_meshlets: list[int] | None = None, clip_used: int | None = None) -> dict:
+def n_lights(name: str) -> int:
+    return min(64, len(scene(name).frames[0].point_lights))
+
+
+def digests(frame: dict, live_meshlets: list[int] | None = None, clip_used: int | None = None,
+            lights: int = 64) -> dict:
     """Digest of every parity section of a render dump.  ss_cache is digested over the live
-    (drawn) meshlets only: culled slots are never written.  The clip pool over its used prefix."""
-    out = {k: sha(frame[k]) for k in ("color", "tile_counts", "tile_payloads", "vid", "light_vis")}
+    (drawn) meshlets only: culled slots are never written.  The clip pool over its used prefix,
+    light visibility over the frame's lights (the reference writes no other column)."""
+    out = {k: sha(frame[k]) for k in ("color", "tile_counts", "tile_payloads", "vid")}
+    out["light_vis"] = sha(frame["light_vis"].reshape(-1, 64)[:, :lights])
     out["depth"] = sha(frame["depth"].view(np.uint32))
     ss = frame["ss_cache"].view(np.uint32).reshape(-1, 576)
     if live_meshlets is None:

@@ -30,7 +30,7 @@ def test_gpu_matches_reference_digests(renderer, golden, name):
         g = golden[name]["samples"][str(S)]
         out = _render_case(renderer, name, S)
         assert out["status"] == 0
-        d, _ = gc.digests(out, g["live_meshlets"], g["clip_used"])
+        d, _ = gc.digests(out, g["live_meshlets"], g["clip_used"], gc.n_lights(name))
         mism = [k for k in d if k in g and d[k] != g[k]]
         assert not mism, f"{name} {S}x differs from the reference in {mism}"
 
@@ -59,7 +59,7 @@ def test_gpu_equals_oracle_random(renderer, seed, samples):
         out = renderer.render_debug(h, 0, tss, npx)
     finally:
         renderer.free_scene(h)
-    res = compare_frames(ref, out, samples)
+    res = compare_frames(ref, out, samples, len(sc.frames[0].point_lights))
     bad = {k: v for k, v in res.items() if k not in ("color_max_lsb", "tlas") and v != 0}
     cols = (sc.frames[0].width + 63) // 64
     assert not bad, (res, first_vid_mismatch(ref, out, cols, samples))

@@ -20,7 +20,7 @@ def test_oracle_matches_reference_digests(golden, name):
         for S in gc.SAMPLES[name]:
             g = golden[name]["samples"][str(S)]
             frame = o.render_dump(0, S)
-            d, _ = gc.digests(frame, g["live_meshlets"], g["clip_used"])
+            d, _ = gc.digests(frame, g["live_meshlets"], g["clip_used"], gc.n_lights(name))
             mism = [k for k in d if k in g and d[k] != g[k]]
             assert not mism, f"{name} {S}x: sections differ from the reference: {mism}"
             assert frame["invalid_packets"] == 0
@@ -35,7 +35,7 @@ def test_oracle_matches_reference_digests_full(golden, name):
     try:
         for S in gc.SAMPLES[name]:
             g = golden[name]["samples"][str(S)]
-            d, _ = gc.digests(o.render_dump(0, S, threads=8), g["live_meshlets"], g["clip_used"])
+            d, _ = gc.digests(o.render_dump(0, S, threads=8), g["live_meshlets"], g["clip_used"], gc.n_lights(name))
             assert [k for k in d if k in g and d[k] != g[k]] == []
     finally:
         o.close()
@@ -57,7 +57,7 @@ def test_oracle_equals_reference_random(seed, samples):
         g = o.render_dump(0, samples)
     finally:
         o.close()
-    res = compare_frames(r, g, samples)
+    res = compare_frames(r, g, samples, len(sc.frames[0].point_lights))
     bad = {k: v for k, v in res.items() if k != "color_max_lsb" and v != 0}
     assert not bad, res
 
