@@ -100,14 +100,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _algorithmic_tile_bytes(width: int, height: int, samples: int, payloads: int) -> float:
-    """Bytes the tile kernel must move per frame at minimum: its payload list (8 B each), per
-    pixel one 2304 B screen-space record share (vertex data, amortised over a 4x2 block: 156 B
-    per distinct block triangle, about one per block), 4 bilinear texels (16 B), the colour
-    write (4 B); the visibility buffer (4 B per sample) stays on chip in this design but is
-    counted as the reference's tile buffer traffic."""
+def _algorithmic_resolve_bytes(width: int, height: int, samples: int) -> float:
+    """Bytes the resolve kernel must move per frame at minimum: per pixel the visibility
+    buffer (8 B per sample: depth and id), the vertex data of its triangle (156 B per distinct
+    triangle of a 4x2 block, about one per block, so 156/8 B per pixel), 4 bilinear texels
+    (16 B) and the colour write (4 B)."""
     pixels = width * height
-    return payloads * 8 + pixels * (156.0 / 8 + 16 + 4 + 4 * samples)
+    return pixels * (8.0 * samples + 156.0 / 8 + 16 + 4)
 
 
 def run_ours(args, cfg) -> dict:
@@ -167,7 +166,7 @@ def run_ours(args, cfg) -> dict:
     t0 = time.perf_counter()
     dev_times = timed(device_step, args.steps)
     launches = R.launch_count() * args.steps
-    kern = np.zeros(4)
+    kern = np.zeros(5)
     for _ in range(3):
         device_step()
         kern += R.timings()
@@ -183,8 +182,8 @@ def run_ours(args, cfg) -> dict:
         ms_dev, ms_e2e = float(t[0]), float(t[1])
     frames = args.steps * world
     peaks = _peaks()
-    tile_ms = float(kern[3])
-    alg = _algorithmic_tile_bytes(W, H, S, payloads)
+    tile_ms = float(kern[4])
+    alg = _algorithmic_resolve_bytes(W, H, S)
     achieved = alg / (tile_ms * 1e-3) / 1e9 if tile_ms > 0 else 0.0
     h2d = 4096 + sum(16 * 4 * (len(b) if b is not None else 0) for _, _, b in sc.frames[0].instances)
     line = {
@@ -200,15 +199,17 @@ def run_ours(args, cfg) -> dict:
         "e2e": {"value": frames / (ms_e2e * 1e-3), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(W * H * 4)},
         "gpu_launches": int(launches),
-        "kernel_ms": {"occlusion": float(kern[0]), "geometry": float(kern[1]), "binning": float(kern[2]), "tile": tile_ms},
-        "roofline": {"kernel": "k_tile (raster + resolve)", "bound": "hbm", "achieved": achieved,
+        "kernel_ms": {"occlusion": float(kern[0]), "geometry": float(kern[1]), "binning": float(kern[2]),
+                      "raster": float(kern[3]), "resolve": tile_ms},
+        "roofline": {"kernel": "k_resolve", "bound": "hbm", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                      "traffic": None, "peak_source": peaks["src"],
-                     "note": "the tile kernel is FP32/issue bound; HBM fraction shown per contract"},
+                     "note": "the resolve is FP32/issue bound (lights x capsule proxies per pixel); "
+                             "HBM fraction of its algorithmic bytes shown per contract"},
         "clocks": clk,
         "wall_s": wall,
     }
-    if rank == 0:
+    if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(blob, S, W, H, seconds=args.cpu_seconds)
     R.free_scene(h)
     R.close()
@@ -282,6 +283,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=2, choices=sorted(CONFIGS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     cfg = CONFIGS[args.config]

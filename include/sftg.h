@@ -126,8 +126,8 @@ int sftg_frame_render(sftg_ctx* ctx, const sftg_frame_desc* frame, uint32_t* col
  * width*height u32 owned by the context (valid until the next frame). No host copies of pixels. */
 int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* frame, const uint32_t** out_device_color);
 
-/* Device time in ms of the last frame's kernels, split as [occlusion, geometry+clip, binning, tile]. */
-int sftg_last_timings(const sftg_ctx* ctx, float* out4);
+/* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
+int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */
 int sftg_last_launch_count(const sftg_ctx* ctx);
 /* The cudaStream_t the context renders on (for callers that time or order work around frames). */

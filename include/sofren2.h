@@ -195,8 +195,8 @@ SFT_FUNC const char* sft_get_last_error(void);
 SFT_FUNC void sft_set_debug_capture(void* sftg_debug_out_or_null);
 /* extension: BLAS of a model as sft_bvh_node images (256 B each) */
 SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, u32* out_root);
-/* extension: device time of the last present, ms: [occlusion, geometry, binning, tile] */
-SFT_FUNC void sft_get_frame_timings(f32* out4);
+/* extension: device time of the last present, ms: [occlusion, geometry, binning, raster, resolve] */
+SFT_FUNC void sft_get_frame_timings(f32* out5);
 /* extension: kernels launched by the last present, and the CUDA stream the runtime renders on */
 SFT_FUNC i32 sft_get_launch_count(void);
 SFT_FUNC void* sft_get_cuda_stream(void);
@@ -483,7 +483,7 @@ SFT_FUNC void sft_resize(i32 width, i32 height) { if (sft__s) { sft__s->width = 
 SFT_FUNC void sft_set_msaa_samples(i32 samples) { if (sft__s && (samples == 1 || samples == 2 || samples == 4)) sft__s->samples = samples; }
 SFT_FUNC const char* sft_get_last_error(void) { return sft__s && sft__s->gpu ? sftg_last_error(sft__s->gpu) : ""; }
 SFT_FUNC void sft_set_debug_capture(void* d) { if (sft__s) sft__s->debug = (sftg_debug_out*)d; }
-SFT_FUNC void sft_get_frame_timings(f32* out4) { if (sft__s) sftg_last_timings(sft__s->gpu, out4); }
+SFT_FUNC void sft_get_frame_timings(f32* out5) { if (sft__s) sftg_last_timings(sft__s->gpu, out5); }
 SFT_FUNC i32 sft_get_launch_count(void) { return sft__s ? sftg_last_launch_count(sft__s->gpu) : 0; }
 SFT_FUNC void* sft_get_cuda_stream(void) { return sft__s ? sftg_stream(sft__s->gpu) : NULL; }
 

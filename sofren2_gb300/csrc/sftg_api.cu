@@ -13,7 +13,8 @@
  *   3. k_geometry         cull, skin, transform, project, batch setup (4901-5145)
  *   4. scan + k_clip      near-plane clipping in emission order (4691-4772)
  *   5. k_bin (count), scan, k_bin (write)   per-tile payload lists (4619-4688)
- *   6. k_tile             raster + resolve per tile (6756-6813)
+ *   6. k_raster, k_resolve  per-tile raster into a shared-memory visibility buffer, then
+ *                         the resolve, four CTAs per tile (6756-6813)
  *   7. D2H of the colour buffer into the caller's pitch
  */
 #include <cuda_runtime.h>
@@ -57,8 +58,8 @@ struct sftg_ctx {
     size_t h_stage_cap = 0;
     uint32_t* h_status = nullptr;
     uint64_t tile_cap = 1u << 20, clip_cap = 1u << 16;
-    cudaEvent_t ev[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
-    float timings[4] = { 0, 0, 0, 0 };
+    cudaEvent_t ev[6] = { nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
+    float timings[5] = { 0, 0, 0, 0, 0 };
     int launches = 0;
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
@@ -110,7 +111,7 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) { delete ctx; return SFTG_E_CUDA; }
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
-    for (int i = 0; i < 5; i++) cudaEventCreate(&ctx->ev[i]);
+    for (int i = 0; i < 6; i++) cudaEventCreate(&ctx->ev[i]);
     if (cudaMallocHost((void**)&ctx->h_status, 64) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     sftg_tile_configure(200 * 1024);
     *out = ctx;
@@ -128,7 +129,7 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
     if (ctx->d_color) cudaFree(ctx->d_color);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
-    for (int i = 0; i < 5; i++) if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    for (int i = 0; i < 6; i++) if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -287,6 +288,7 @@ struct frame_bufs {
     uint32_t* status;
     uint32_t* totals;    /* [0] clip total, [1] tile payload total */
     float* vis_depth; uint32_t* vis_id; float* shadow;
+    float2* vis; float2* zrange;
     size_t used;
 };
 
@@ -297,11 +299,6 @@ static void scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tm
     k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, total);
     k_scan_down<<<nb, 1024, 0, st>>>(in, n, tmp, out);
     *launches += 3;
-}
-
-static size_t tile_smem(int S) {
-    const size_t aux = 256 * 84 > 256 * 72 ? (size_t)SETUP_CAP * 84 : (size_t)256 * 72;
-    return (size_t)S * SFTG_TILE_PX * 8 + aux;
 }
 
 /* lays out and uploads the frame block; returns 0 or an error */
@@ -359,6 +356,7 @@ static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug
     acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
     acc((size_t)tiles * 4); acc((size_t)tiles * 4); acc(ctx->tile_cap * 8);
+    acc((size_t)tiles * S * 4096 * 8); acc((size_t)tiles * 8 + 8);
     const size_t n_packets = (size_t)(fd->n_point < 64 ? fd->n_point : 64) * ((fd->n_proxies + 7) / 8) * 3;
     acc((size_t)fd->n_proxies * 64 + 64); acc(n_packets * sftg_packet_bytes() + 64);
     acc((n_packets * (fd->n_instances ? fd->n_instances : 1) + 1) * 8); acc(64); acc(((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
@@ -396,6 +394,8 @@ static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug
     B.scan_tmp = bp.take<uint32_t>((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
     B.status = bp.take<uint32_t>(16);
     B.totals = bp.take<uint32_t>(16);
+    B.vis = bp.take<float2>((size_t)tiles * S * 4096);
+    B.zrange = bp.take<float2>((size_t)tiles + 1);
     B.vis_depth = nullptr; B.vis_id = nullptr; B.shadow = nullptr;
     if (want_debug) {
         B.vis_depth = bp.take<float>((size_t)tiles * S * 4096);
@@ -484,11 +484,10 @@ static int launch_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, const frame_bu
     ctx->launches += 2;
     CK(cudaEventRecord(ctx->ev[3], st));
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, (size_t)fd->width * fd->height * 16 * 4, st));
-    const size_t sm = tile_smem(S);
-    sftg_launch_tile(S, tiles, sm, st, B.F, B.ss, B.clips, B.tile_start, B.tile_count, B.tile_pay, B.light_vis, d_color, B.vis_depth, B.vis_id, B.shadow);
-    ctx->launches++;
+    sftg_launch_tile(S, tiles, st, B.F, B.ss, B.clips, B.tile_start, B.tile_count, B.tile_pay, B.light_vis, B.vis, B.zrange, d_color, B.vis_depth, B.vis_id, B.shadow, ctx->ev[4]);
+    ctx->launches += 2;
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev[4], st));
+    CK(cudaEventRecord(ctx->ev[5], st));
     return 0;
 }
 
@@ -522,8 +521,8 @@ static int frame_common(sftg_ctx* ctx, const sftg_frame_desc* fd, uint32_t* host
             while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
             continue;
         }
-        float t[4];
-        for (int k = 0; k < 4; k++) { t[k] = 0.f; cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]); ctx->timings[k] = t[k]; }
+        float t[5];
+        for (int k = 0; k < 5; k++) { t[k] = 0.f; cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]); ctx->timings[k] = t[k]; }
         if (dbg) {
             const int S = fd->samples, tiles = ((W + 63) / 64) * ((H + 63) / 64);
             if (dbg->vis_depth) CK(cudaMemcpy(dbg->vis_depth, B.vis_depth, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
@@ -556,9 +555,9 @@ extern "C" int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* fd
     return frame_common(ctx, fd, nullptr, 0, nullptr, out_device_color);
 }
 
-extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out4) {
-    if (!ctx || !out4) return SFTG_E_ARG;
-    for (int k = 0; k < 4; k++) out4[k] = ctx->timings[k];
+extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {
+    if (!ctx || !out5) return SFTG_E_ARG;
+    for (int k = 0; k < 5; k++) out5[k] = ctx->timings[k];
     return SFTG_OK;
 }
 

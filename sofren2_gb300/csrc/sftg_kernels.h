@@ -27,8 +27,9 @@ size_t sftg_packet_bytes();
 void sftg_launch_occlusion(const sftg_frame* F, uint32_t n_point, uint32_t n_proxies, uint32_t n_inst, void* packets, uint2* pairs,
                            uint32_t* n_pairs, uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
-void sftg_launch_tile(int S, int tiles, size_t smem, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
+void sftg_launch_tile(int S, int tiles, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
                       const uint32_t* tile_start, const uint32_t* tile_count, const uint64_t* tile_pay, const uint8_t* light_vis,
-                      uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out);
+                      float2* vis, float2* zrange, uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out,
+                      cudaEvent_t between);
 
 #define SFTG_SCAN_ELEMS_PER_BLOCK 4096

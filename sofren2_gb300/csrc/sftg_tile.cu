@@ -1,19 +1,20 @@
 /*
- * k_tile: one CTA per 64x64 tile rasterises the tile's payload list into a shared-memory
- * visibility buffer and resolves it to ARGB8888 (sft__worker_phase_rasterize, sofren2.c:6756-6813,
+ * Per-tile raster and resolve (sft__worker_phase_rasterize, sofren2.c:6756-6813,
  * sft__rast_simd_batch 5148-5499, sft__resolve_tile 5809-6753).
  *
- * Raster.  The reference walks the list in order and keeps a sample when z > stored z
- * (strict), so a sample ends holding the largest z, and among equal z the earliest triangle.
- * That final state does not depend on the order triangles are visited, so each sample is a
- * 64-bit word (z bits << 32 | ~order) updated with a shared-memory atomicMax, where order =
- * list position * 8 + lane.  Only z > 0 ever wins (the buffer starts at 0).  Coverage and z
- * are replayed bit-exactly: a group of 8 threads takes one triangle, thread l owns pixel
- * column l of every aligned 8-pixel chunk and performs exactly the reference's incremental
- * adds (row start + B per row, + 8A per chunk) and its trivial-accept / AA guard-band choices;
- * the AA chunk skip is a group ballot.
+ * k_raster: one CTA per 64x64 tile.  The reference walks the tile's list in order and keeps a
+ * sample when z > stored z (strict), so a sample ends holding the largest z, and among equal z
+ * the earliest triangle.  That final state does not depend on the order triangles are visited,
+ * so each sample is a 64-bit shared-memory word (z bits << 32 | ~order) updated with atomicMax,
+ * where order = list position * 8 + lane; only z > 0 ever wins (the buffer starts at 0).
+ * Coverage and z are replayed bit-exactly: a group of 8 threads takes one triangle, thread l
+ * owns pixel column l of every aligned 8-pixel chunk and performs exactly the reference's
+ * incremental adds (row start + B per row, + 8A per chunk) and its trivial-accept / AA
+ * guard-band choices; the AA chunk skip is a group ballot.  The decoded visibility buffer
+ * (depth, vid) goes to global memory, where it stays L2-resident, with the tile's depth range.
  *
- * Resolve.  A group of 8 threads is one 4x2 pixel block (the reference's AVX2 lanes).  For
+ * k_resolve: four CTAs per tile, each a quarter of its 4x2 blocks, small shared memory for
+ * high occupancy.  A group of 8 threads is one 4x2 block (the reference's AVX2 lanes).  For
  * each distinct triangle in the block (peeled in the reference's order) all 8 lanes shade it,
  * because the reference's LOD uses the first covered lane's screen derivatives (neighbour
  * lanes via shuffles) and its proxy loop skips a proxy for the whole block when no lane is
@@ -229,25 +230,22 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
     r = (float)((c >> 16) & 255u) * i255; g = (float)((c >> 8) & 255u) * i255; b = (float)(c & 255u) * i255;
 }
 
-/* ---------------------------------------------------------------- the tile kernel */
+/* ---------------------------------------------------------------- raster */
+/* One CTA per tile: the tile's payload list into a shared-memory visibility buffer (64-bit
+ * z/order words), decoded into the global visibility buffer (float2: depth, vid bits) plus the
+ * tile's depth range over valid samples (sofren2.c:5820-5853), which the resolve needs for its
+ * light culling. */
 template <int S>
 __global__ void __launch_bounds__(TILE_THREADS)
-k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sftg_clip_tri* __restrict__ clips,
-       const uint32_t* __restrict__ tile_start, const uint32_t* __restrict__ tile_count, const uint64_t* __restrict__ tile_pay,
-       const uint8_t* __restrict__ light_vis, uint32_t* __restrict__ color, float* __restrict__ vis_depth,
-       uint32_t* __restrict__ vis_id, float* __restrict__ shadow_out)
+k_raster(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sftg_clip_tri* __restrict__ clips,
+         const uint32_t* __restrict__ tile_start, const uint32_t* __restrict__ tile_count, const uint64_t* __restrict__ tile_pay,
+         float2* __restrict__ vis, float2* __restrict__ zrange, float* __restrict__ vis_depth, uint32_t* __restrict__ vis_id)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
-    unsigned char* aux = smem + (size_t)S * SFTG_TILE_PX * 8;
-    tri_setup* setups = (tri_setup*)aux;                                    /* raster phase */
-    proxy_cache* pcache = (proxy_cache*)aux;                                /* resolve phase [16][16] */
+    tri_setup* setups = (tri_setup*)(smem + (size_t)S * SFTG_TILE_PX * 8);
     __shared__ uint32_t s_nsetup, s_next;
     __shared__ float s_red[2][TILE_THREADS / 32];
-    __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
-    __shared__ int s_nlights;
-    __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
-
     const int tile = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
@@ -256,8 +254,6 @@ k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sft
     const uint64_t* list = tile_pay + tile_start[tile];
 
     for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) keys[i] = 0ull;
-
-    /* ---------------- raster ---------------- */
     const int grp_lane = tid & 7;
     const uint32_t gmask = 0xFFu << (lane & ~7);
     for (uint32_t pbase = 0; pbase < count; pbase += SETUP_CAP / 8) {
@@ -312,9 +308,10 @@ k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sft
         }
         __syncthreads();
     }
-
-    /* ---------------- decode the visibility buffer ---------------- */
+    __syncthreads();
+    /* decode, store, depth range */
     float zmin = 1e9f, zmax = -1e9f;
+    float2* tv = vis + (size_t)tile * S * SFTG_TILE_PX;
     for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) {
         const unsigned long long k = keys[i];
         float d = 0.f; uint32_t vid = SFTG_INVALID;
@@ -325,21 +322,47 @@ k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sft
             if ((pay >> 56) == 0) vid = (uint32_t)pay | 0x80000000u;
             else vid = ((uint32_t)(pay & 0xFFFFFF) << 25) | ((uint32_t)((pay >> 24) & 0xFFFFFF) << 7) | ((uint32_t)((pay >> 48) & 0xFF) * 8 + (order & 7));
         }
-        ((float2*)keys)[i] = make_float2(d, __uint_as_float(vid));
+        tv[i] = make_float2(d, __uint_as_float(vid));
         if (vis_id) {
             vis_depth[(size_t)tile * S * SFTG_TILE_PX + i] = d;
             vis_id[(size_t)tile * S * SFTG_TILE_PX + i] = vid;
         }
         if (d > 0.0001f) { zmin = fminf(zmin, d); zmax = fmaxf(zmax, d); }
     }
-    /* D1: tile depth bounds (5820-5853) */
 #pragma unroll
     for (int o = 16; o; o >>= 1) { zmin = fminf(zmin, __shfl_xor_sync(0xFFFFFFFFu, zmin, o)); zmax = fmaxf(zmax, __shfl_xor_sync(0xFFFFFFFFu, zmax, o)); }
     if (lane == 0) { s_red[0][warp] = zmin; s_red[1][warp] = zmax; }
     __syncthreads();
-    zmin = 1e9f; zmax = -1e9f;
-#pragma unroll
-    for (int w = 0; w < TILE_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
+    if (tid == 0) {
+        zmin = 1e9f; zmax = -1e9f;
+        for (int w = 0; w < TILE_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
+        zrange[tile] = make_float2(zmin, zmax);
+    }
+}
+
+/* ---------------------------------------------------------------- resolve */
+#define RESOLVE_SPLIT 4                       /* CTAs per tile, each 1/4 of the tile's 4x2 blocks */
+#define RESOLVE_BLOCKS (16 * 32 / RESOLVE_SPLIT)
+
+/* One CTA per quarter tile: tile light list (5855-5934) and proxy cache (5936-5990), then one
+ * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
+template <int S>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_resolve(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sftg_clip_tri* __restrict__ clips,
+          const float2* __restrict__ vis_all, const float2* __restrict__ zrange, const uint8_t* __restrict__ light_vis,
+          uint32_t* __restrict__ color, float* __restrict__ shadow_out)
+{
+    __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
+    __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
+    __shared__ int s_nlights;
+    __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
+
+    const int tile = blockIdx.x / RESOLVE_SPLIT, part = blockIdx.x % RESOLVE_SPLIT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
+    const float2 zr = zrange[tile];
+    const float zmin = zr.x, zmax = zr.y;
+    const float2* vis = vis_all + (size_t)tile * S * SFTG_TILE_PX;
 
     /* D2: tile light list, first 16 lights in index order that pass (5855-5934) */
     if (warp == 0) {
@@ -426,18 +449,19 @@ k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sft
     __syncthreads();
 
     /* ---------------- resolve: one 8-thread group per 4x2 block ---------------- */
-    const int W = F->width, H = F->height;
+    const int W = F->width;
     const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
     const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
-    const float2* vis = (const float2*)keys;
     const int grp = tid >> 3, gl = tid & 7, gshift = lane & ~7;
+    const uint32_t gmask = 0xFFu << gshift;
     const int ix = gl & 3, iy = gl >> 2;
     const float inv_s = 1.f / (float)S;
     const uint32_t cc = F->clear_color;
     const float clr[3] = { (float)((cc >> 16) & 0xFF) * (1.f / 255.f), (float)((cc >> 8) & 0xFF) * (1.f / 255.f), (float)(cc & 0xFF) * (1.f / 255.f) };
     const v3 cam = mk3(F->cam[0], F->cam[1], F->cam[2]);
 
-    for (int blk = grp; blk < 16 * 32; blk += TILE_THREADS / 8) {
+    for (int b = grp; b < RESOLVE_BLOCKS; b += TILE_THREADS / 8) {
+        const int blk = part * RESOLVE_BLOCKS + b;
         const int x = tmx + (blk & 15) * 4, y = tmy + (blk >> 4) * 2;
         if (x >= lim_x || y >= lim_y) continue;
         const int gx = x + ix, gy = y + iy;
@@ -608,12 +632,13 @@ k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sft
                     const int np = s_npc[i];
                     if (np > 0) {
                         const float lrl = fsqrt(d2);
+                        const float rd2 = rcpr(d2);   /* loop-invariant: the reference recomputes the same value per proxy */
                         const float bk = 0.2f, b4 = 0.25f / 0.2f;
                         for (int pi = 0; pi < np; pi++) {
                             const proxy_cache& q = pcache[i * SFTG_MAX_LIGHT_PROXIES + pi];
                             const float wdv = 0.f - vdot(mk3(q.W[0], q.W[1], q.W[2]), Lr);
                             const bool btw = wdv > 0.f && wdv < d2;
-                            const float tf = wdv * rcpr(d2);
+                            const float tf = wdv * rd2;
                             const float cd2 = fma_(-wdv, tf, q.wdw);
                             const bool ray = btw && (cd2 < q.rb2) && (lm ? in_tri : lit);
                             if (!(__ballot_sync(gmask, ray) & gmask)) continue;   /* block-level skip */
@@ -690,22 +715,33 @@ k_tile(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sft
     }
 }
 
-template __global__ void k_tile<1>(const sftg_frame*, const float*, const sftg_clip_tri*, const uint32_t*, const uint32_t*, const uint64_t*, const uint8_t*, uint32_t*, float*, uint32_t*, float*);
-template __global__ void k_tile<2>(const sftg_frame*, const float*, const sftg_clip_tri*, const uint32_t*, const uint32_t*, const uint64_t*, const uint8_t*, uint32_t*, float*, uint32_t*, float*);
-template __global__ void k_tile<4>(const sftg_frame*, const float*, const sftg_clip_tri*, const uint32_t*, const uint32_t*, const uint64_t*, const uint8_t*, uint32_t*, float*, uint32_t*, float*);
+/* ---------------------------------------------------------------- host-side launch helpers */
+static size_t raster_smem(int S) { return (size_t)S * SFTG_TILE_PX * 8 + (size_t)SETUP_CAP * sizeof(tri_setup); }
 
-/* host-side launch helpers (template kernels are instantiated and launched from this unit) */
 cudaError_t sftg_tile_configure(int max_dynamic_smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_tile<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tile<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    cudaError_t e = cudaSuccess;
+    const int S_[3] = { 1, 2, 4 };
+    for (int k = 0; k < 3 && e == cudaSuccess; k++) {
+        const int need = (int)raster_smem(S_[k]);
+        const int v = need < max_dynamic_smem ? need : max_dynamic_smem;
+        if (S_[k] == 1) e = cudaFuncSetAttribute(k_raster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        if (S_[k] == 2) e = cudaFuncSetAttribute(k_raster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        if (S_[k] == 4) e = cudaFuncSetAttribute(k_raster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    }
     return e;
 }
 
-void sftg_launch_tile(int S, int tiles, size_t smem, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
+void sftg_launch_tile(int S, int tiles, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
                       const uint32_t* tile_start, const uint32_t* tile_count, const uint64_t* tile_pay, const uint8_t* light_vis,
-                      uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out) {
-    if (S == 1) k_tile<1><<<tiles, TILE_THREADS, smem, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, light_vis, color, vis_depth, vis_id, shadow_out);
-    else if (S == 2) k_tile<2><<<tiles, TILE_THREADS, smem, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, light_vis, color, vis_depth, vis_id, shadow_out);
-    else k_tile<4><<<tiles, TILE_THREADS, smem, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, light_vis, color, vis_depth, vis_id, shadow_out);
+                      float2* vis, float2* zrange, uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out,
+                      cudaEvent_t between) {
+    const size_t sm = raster_smem(S);
+    if (S == 1) k_raster<1><<<tiles, TILE_THREADS, sm, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, vis, zrange, vis_depth, vis_id);
+    else if (S == 2) k_raster<2><<<tiles, TILE_THREADS, sm, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, vis, zrange, vis_depth, vis_id);
+    else k_raster<4><<<tiles, TILE_THREADS, sm, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, vis, zrange, vis_depth, vis_id);
+    if (between) cudaEventRecord(between, st);
+    const int grid = tiles * RESOLVE_SPLIT;
+    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(F, ss, clips, vis, zrange, light_vis, color, shadow_out);
+    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(F, ss, clips, vis, zrange, light_vis, color, shadow_out);
+    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(F, ss, clips, vis, zrange, light_vis, color, shadow_out);
 }

@@ -116,7 +116,7 @@ class Renderer:
         return int(self.lib.sft_get_launch_count())
 
     def timings(self) -> np.ndarray:
-        t = np.zeros(4, np.float32)
+        t = np.zeros(5, np.float32)
         self.lib.sft_get_frame_timings(_ptr(t))
         return t
 
@@ -156,7 +156,7 @@ class Renderer:
         out["ss_cache"] = out["ss_cache"][: total_ss * 576]
         out["light_vis"] = out["light_vis"][: n_proxies * 64]
         out["status"] = int(status[0])
-        timings = np.zeros(4, np.float32)
+        timings = np.zeros(5, np.float32)
         self.lib.sft_get_frame_timings(_ptr(timings))
         out["timings_ms"] = timings
         return out
