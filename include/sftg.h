@@ -126,6 +126,17 @@ int sftg_frame_render(sftg_ctx* ctx, const sftg_frame_desc* frame, uint32_t* col
  * width*height u32 owned by the context (valid until the next frame). No host copies of pixels. */
 int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* frame, const uint32_t** out_device_color);
 
+/* Renders n_views independent frames (each with its own camera, size, sample count, instances,
+ * lights and proxies; all drawing from the context's resident models) in one submission: every
+ * pipeline stage is one launch over all views' work, so small views fill the GPU together.
+ * Each view's result is identical to rendering it alone with sftg_frame_render.
+ * colors (optional) holds one host pointer per view (entries may be null), pitch_bytes
+ * (optional) one pitch per view (0 = width*4); out_device_colors (optional) receives one device
+ * pointer per view, valid until the next render call.  No counterpart in the reference, which
+ * renders one view per sft_present. */
+int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, uint32_t* const* colors,
+                       const int32_t* pitch_bytes, const uint32_t** out_device_colors);
+
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */

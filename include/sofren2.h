@@ -200,6 +200,14 @@ SFT_FUNC void sft_get_frame_timings(f32* out5);
 /* extension: kernels launched by the last present, and the CUDA stream the runtime renders on */
 SFT_FUNC i32 sft_get_launch_count(void);
 SFT_FUNC void* sft_get_cuda_stream(void);
+/* extension: batched submission.  Between sft_batch_begin and sft_batch_submit, sft_present
+ * records the frame (camera, size, instances, poses, lights, proxies, colour buffer) instead of
+ * rendering it; sft_batch_submit renders every recorded frame in one GPU submission
+ * (sftg_frames_render) and writes each into the colour buffer that was set for it, leaving the
+ * colour in device memory for frames recorded without one.  Each frame's pixels are those
+ * sft_present would have produced alone.  Returns 0 or a negative sftg error code. */
+SFT_FUNC void sft_batch_begin(void);
+SFT_FUNC i32 sft_batch_submit(void);
 
 #ifdef __cplusplus
 }
@@ -269,6 +277,9 @@ static struct sft__state {
     sft_mat_handle base_mat;
     sftg_debug_out* debug;
     char err[512];
+    /* batched submission: frames recorded by sft_present between sft_batch_begin / _submit */
+    u8 batching; u32 n_batch, cap_batch;
+    sftg_frame_desc* batch_fd; u32** batch_color; i32* batch_pitch; void** batch_mem;
 } *sft__s;
 
 /* ---------------------------------------------------------------- math (sofren2.c:1503-1918) */
@@ -475,6 +486,8 @@ SFT_FUNC void sft_release(void) {
     for (i32 i = 0; i < sft__s->tex_cap; i++) free(sft__s->tex[i].level0);
     free(sft__s->tex); free(sft__s->mat_gen); free(sft__s->mat_next);
     free(sft__s->point); free(sft__s->dir); free(sft__s->bones); free(sft__s->proxies);
+    for (u32 i = 0; i < sft__s->n_batch; i++) free(sft__s->batch_mem[i]);
+    free(sft__s->batch_fd); free(sft__s->batch_color); free(sft__s->batch_pitch); free(sft__s->batch_mem);
     free(sft__s);
     sft__s = NULL;
 }
@@ -791,6 +804,46 @@ SFT_FUNC void sft_draw_instance(const sft_instance* in) {
     }
 }
 
+/* copies one frame description and everything it points at into one allocation */
+static void sft__batch_record(const sftg_frame_desc* fd, u32* color, i32 pitch) {
+    struct sft__state* s = sft__s;
+    if (s->n_batch == s->cap_batch) {
+        s->cap_batch = s->cap_batch ? s->cap_batch * 2 : 16;
+        s->batch_fd = (sftg_frame_desc*)realloc(s->batch_fd, s->cap_batch * sizeof(sftg_frame_desc));
+        s->batch_color = (u32**)realloc(s->batch_color, s->cap_batch * sizeof(u32*));
+        s->batch_pitch = (i32*)realloc(s->batch_pitch, s->cap_batch * sizeof(i32));
+        s->batch_mem = (void**)realloc(s->batch_mem, s->cap_batch * sizeof(void*));
+    }
+    size_t nbones = 0;
+    for (u32 i = 0; i < fd->n_instances; i++) nbones += fd->instances[i].bone_count;
+    const size_t b_inst = (size_t)fd->n_instances * sizeof(sftg_instance_desc), b_bones = nbones * 64;
+    const size_t b_pl = (size_t)fd->n_point * 32, b_dl = (size_t)fd->n_dir * 24, b_px = (size_t)fd->n_proxies * 32;
+    const size_t b_tl = (size_t)fd->tlas_count * sizeof(sft__node);
+    char* m = (char*)malloc(b_inst + b_bones + b_pl + b_dl + b_px + b_tl + 64);
+    char* q = m;
+    sftg_frame_desc c = *fd;
+    sftg_instance_desc* inst = (sftg_instance_desc*)q; q += b_inst;
+    f32* bones = (f32*)q; q += b_bones;
+    for (u32 i = 0; i < fd->n_instances; i++) {
+        inst[i] = fd->instances[i];
+        if (fd->instances[i].bone_count) {
+            memcpy(bones, fd->instances[i].bones, (size_t)fd->instances[i].bone_count * 64);
+            inst[i].bones = bones;
+            bones += 16 * (size_t)fd->instances[i].bone_count;
+        }
+    }
+    c.instances = inst;
+    if (b_pl) { memcpy(q, fd->point_lights, b_pl); c.point_lights = (const f32*)q; q += b_pl; }
+    if (b_dl) { memcpy(q, fd->dir_lights, b_dl); c.dir_lights = (const f32*)q; q += b_dl; }
+    if (b_px) { memcpy(q, fd->proxies, b_px); c.proxies = (const f32*)q; q += b_px; }
+    if (b_tl) { memcpy(q, fd->tlas_nodes, b_tl); c.tlas_nodes = q; q += b_tl; }
+    s->batch_fd[s->n_batch] = c;
+    s->batch_color[s->n_batch] = color;
+    s->batch_pitch[s->n_batch] = pitch;
+    s->batch_mem[s->n_batch] = m;
+    s->n_batch++;
+}
+
 SFT_FUNC void sft_present(void) {
     struct sft__state* s = sft__s;
     /* TLAS over instance bounds, rebuilt per frame (sofren2.c:3619-3703) */
@@ -836,9 +889,34 @@ SFT_FUNC void sft_present(void) {
     fd.n_instances = s->n_inst; fd.instances = s->inst;
     fd.n_proxies = s->n_prox; fd.proxies = s->proxies;
     fd.tlas_nodes = tlas; fd.tlas_count = tlas_count; fd.tlas_root = tlas_root;
+    if (s->batching) {   /* record a self-contained copy; sft_frame_end may reuse every array */
+        sft__batch_record(&fd, s->color, s->pitch);
+        free(tlas);
+        return;
+    }
     const int rc = sftg_frame_render(s->gpu, &fd, s->color, s->pitch, s->debug);
     free(tlas);
     if (rc) fprintf(stderr, "sofren2-gb300: sft_present failed (%d): %s\n", rc, sftg_last_error(s->gpu));
+}
+
+SFT_FUNC void sft_batch_begin(void) {
+    struct sft__state* s = sft__s;
+    for (u32 i = 0; i < s->n_batch; i++) free(s->batch_mem[i]);
+    s->n_batch = 0;
+    s->batching = 1;
+}
+
+SFT_FUNC i32 sft_batch_submit(void) {
+    struct sft__state* s = sft__s;
+    s->batching = 0;
+    if (!s->n_batch) return 0;
+    u8 any_host = 0;
+    for (u32 i = 0; i < s->n_batch; i++) any_host |= s->batch_color[i] != NULL;
+    const int rc = sftg_frames_render(s->gpu, s->batch_fd, s->n_batch, any_host ? s->batch_color : NULL, s->batch_pitch, NULL);
+    for (u32 i = 0; i < s->n_batch; i++) free(s->batch_mem[i]);
+    s->n_batch = 0;
+    if (rc) fprintf(stderr, "sofren2-gb300: sft_batch_submit failed (%d): %s\n", rc, sftg_last_error(s->gpu));
+    return rc;
 }
 
 SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena) {

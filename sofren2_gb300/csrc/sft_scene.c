@@ -186,6 +186,21 @@ SFTX_EXPORT int sftx_scene_render(void* p, uint32_t frame, uint32_t* color, int3
     return 0;
 }
 
+/* Renders n (scene, frame, samples) views in one batched submission; colors (optional) holds a
+ * host buffer per view (entries may be null: that view's colour stays on the device). */
+SFTX_EXPORT int sftx_scene_render_batch(void* const* scenes, const uint32_t* frames, const int32_t* samples, uint32_t n,
+                                        uint32_t* const* colors, const int32_t* pitch_bytes) {
+    sft_batch_begin();
+    for (uint32_t i = 0; i < n; i++) {
+        sft_set_msaa_samples(samples[i]);
+        if (sftx_scene_render(scenes[i], frames[i], colors ? colors[i] : NULL, pitch_bytes ? pitch_bytes[i] : 0)) {
+            sft_batch_submit();
+            return -1;
+        }
+    }
+    return sft_batch_submit();
+}
+
 SFTX_EXPORT void sftx_scene_free(void* p) {
     sftx_scene* s = (sftx_scene*)p;
     if (!s) return;

@@ -273,8 +273,17 @@ struct bump {
     }
 };
 
-struct frame_bufs {
-    sftg_frame* F;
+/* Placement of one view inside a batch: where its rows start in the batch-wide arrays. */
+struct view_plan {
+    uint32_t ss_base, total_ss, tile_base, tiles, prox_base, packet_base, n_packets;
+    uint32_t inst_off, bone_off, pl_off, dl_off, tl_off;
+    uint64_t vis_base, color_off;
+};
+
+struct batch_bufs {
+    sftg_frame* frames;  /* device copies of the views' frame blocks */
+    const sftg_job* jobs;
+    const uint16_t* tile_view; const uint16_t* packet_view; const uint16_t* prox_view;
     float* ss;
     sftg_batch_rec* recs;
     uint32_t* clip_cnt; uint32_t* clip_base;
@@ -289,7 +298,10 @@ struct frame_bufs {
     uint32_t* totals;    /* [0] clip total, [1] tile payload total */
     float* vis_depth; uint32_t* vis_id; float* shadow;
     float2* vis; float2* zrange;
-    size_t used;
+    uint32_t n_views, total_ss, n_jobs, total_tiles, total_prox, total_packets, max_inst;
+    uint32_t s_tile0[3], s_tiles[3];   /* batch-wide tile range of the views with 1, 2 and 4 samples */
+    uint64_t color_total;              /* pixels over all views */
+    std::vector<view_plan> plan;
 };
 
 static void scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, uint32_t* total, cudaStream_t st, int* launches) {
@@ -301,74 +313,126 @@ static void scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tm
     *launches += 3;
 }
 
-/* lays out and uploads the frame block; returns 0 or an error */
-static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug, frame_bufs& B, uint32_t& total_ss, uint32_t& n_jobs) {
-    const int W = fd->width, H = fd->height, S = fd->samples;
-    if (W <= 0 || H <= 0 || !(S == 1 || S == 2 || S == 4)) return set_err(ctx, SFTG_E_ARG, "bad frame size or samples");
-    if (fd->n_instances > SFTG_MAX_INSTANCES) return set_err(ctx, SFTG_E_LIMIT, "more than %d instances in one frame", SFTG_MAX_INSTANCES);
-    const int cols = (W + 63) / 64, rows = (H + 63) / 64, tiles = cols * rows;
-    /* host-side frame block */
-    std::vector<sftg_inst> inst(fd->n_instances + 1);
+static int sample_slot(int S) { return S == 1 ? 0 : (S == 2 ? 1 : 2); }
+
+/* Plans the views, sizes the arena and colour pool, and uploads every view's frame block with
+ * one H2D copy.  Views keep their own instance, light, proxy and TLAS arrays; the shared arrays
+ * (screen-space cache, batch records, clip pool, tile lists, light_vis, visibility buffers) are
+ * laid out view after view, with tiles numbered by sample count first (1, 2, 4) so that each
+ * raster/resolve specialisation covers one contiguous tile range. */
+static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, bool want_debug, batch_bufs& B) {
+    if (!nv || nv > 65535) return set_err(ctx, SFTG_E_ARG, "a batch holds 1 to 65535 views, not %u", nv);
+    if (want_debug && nv != 1) return set_err(ctx, SFTG_E_ARG, "debug capture covers single-view submissions only");
+    B.plan.assign(nv, view_plan{});
+    B.n_views = nv;
+    std::vector<sftg_inst> inst;
     std::vector<sftg_job> jobs;
     std::vector<float> bones;
-    total_ss = 0;
-    for (uint32_t i = 0; i < fd->n_instances; i++) {
-        const sftg_instance_desc& id = fd->instances[i];
-        if (id.model < 0 || (size_t)id.model >= ctx->h_models.size()) return set_err(ctx, SFTG_E_ARG, "instance %u: bad model", i);
-        const sftg_model& md = ctx->h_models[id.model];
-        sftg_inst& I = inst[i];
-        memcpy(I.T, id.transform, 64);
-        I.model = (uint32_t)id.model;
-        I.ss_offset = total_ss;
-        I.meshlet_base = md.meshlet_base;
-        I.bones = -1;
-        if (id.bones && id.bone_count) {
-            I.bones = (int32_t)(bones.size() / 16);
-            bones.insert(bones.end(), id.bones, id.bones + (size_t)id.bone_count * 16);
-        }
-        for (uint32_t k = 0; k < md.mesh_count; k++) {
-            const uint32_t first = ctx->h_mesh_first[id.model][k], cnt = ctx->h_mesh_count[id.model][k];
-            const uint32_t sk = ctx->h_mesh_skinned[id.model][k] && I.bones >= 0;
-            for (uint32_t s = 0; s < cnt; s += 8) {
-                sftg_job j; j.inst = i; j.first = first + s; j.count = (cnt - s) < 8 ? (cnt - s) : 8; j.skinned = sk;
-                jobs.push_back(j);
+    uint32_t total_ss = 0, total_prox = 0, total_packets = 0, max_inst = 0, n_pl = 0, n_dl = 0, n_tl = 0;
+    uint64_t max_pairs = 0, color_total = 0;
+    for (uint32_t v = 0; v < nv; v++) {
+        const sftg_frame_desc* fd = &fds[v];
+        view_plan& P = B.plan[v];
+        const int W = fd->width, H = fd->height, S = fd->samples;
+        if (W <= 0 || H <= 0 || !(S == 1 || S == 2 || S == 4)) return set_err(ctx, SFTG_E_ARG, "view %u: bad frame size or samples", v);
+        if (fd->n_instances > SFTG_MAX_INSTANCES) return set_err(ctx, SFTG_E_LIMIT, "view %u: more than %d instances in one frame", v, SFTG_MAX_INSTANCES);
+        P.ss_base = total_ss; P.inst_off = (uint32_t)inst.size(); P.bone_off = (uint32_t)bones.size();
+        P.pl_off = n_pl; P.dl_off = n_dl; P.tl_off = n_tl;
+        uint32_t lss = 0;
+        for (uint32_t i = 0; i < fd->n_instances; i++) {
+            const sftg_instance_desc& id = fd->instances[i];
+            if (id.model < 0 || (size_t)id.model >= ctx->h_models.size()) return set_err(ctx, SFTG_E_ARG, "view %u instance %u: bad model", v, i);
+            const sftg_model& md = ctx->h_models[id.model];
+            sftg_inst I;
+            memset(&I, 0, sizeof(I));
+            memcpy(I.T, id.transform, 64);
+            I.model = (uint32_t)id.model;
+            I.ss_offset = lss;
+            I.meshlet_base = md.meshlet_base;
+            I.bones = -1;
+            if (id.bones && id.bone_count) {
+                I.bones = (int32_t)((bones.size() - P.bone_off) / 16);
+                bones.insert(bones.end(), id.bones, id.bones + (size_t)id.bone_count * 16);
             }
+            for (uint32_t k = 0; k < md.mesh_count; k++) {
+                const uint32_t first = ctx->h_mesh_first[id.model][k], cnt = ctx->h_mesh_count[id.model][k];
+                const uint32_t sk = ctx->h_mesh_skinned[id.model][k] && I.bones >= 0;
+                for (uint32_t s = 0; s < cnt; s += 8) {
+                    sftg_job j; j.inst = i; j.first = first + s; j.count = (uint16_t)((cnt - s) < 8 ? (cnt - s) : 8); j.skinned = (uint16_t)sk; j.view = v;
+                    jobs.push_back(j);
+                }
+            }
+            lss += md.total_meshlets;
+            inst.push_back(I);
         }
-        total_ss += md.total_meshlets;
+        inst.push_back(sftg_inst{});   /* keeps every view's instance array non-empty */
+        P.total_ss = lss; total_ss += lss;
+        P.prox_base = total_prox; total_prox += fd->n_proxies;
+        const uint32_t lc = fd->n_point < 64 ? fd->n_point : 64;
+        P.n_packets = (fd->shadows && fd->n_point && fd->n_proxies) ? lc * ((fd->n_proxies + 7) / 8) * 3 : 0;
+        P.packet_base = total_packets; total_packets += P.n_packets;
+        max_pairs += (uint64_t)P.n_packets * (fd->n_instances ? fd->n_instances : 1);
+        if (fd->n_instances > max_inst) max_inst = fd->n_instances;
+        n_pl += fd->n_point; n_dl += fd->n_dir; n_tl += fd->tlas_count;
+        P.color_off = color_total; color_total += (uint64_t)W * H;
     }
-    n_jobs = (uint32_t)jobs.size();
+    if (max_pairs > 0xFFFFFFF0ull || total_ss > (1u << 26)) return set_err(ctx, SFTG_E_LIMIT, "batch too large for one submission");
+    uint32_t total_tiles = 0;
+    uint64_t vis_total = 0;
+    for (int si = 0; si < 3; si++) {
+        const int Sv = 1 << si;
+        B.s_tile0[si] = total_tiles;
+        for (uint32_t v = 0; v < nv; v++) {
+            if (fds[v].samples != Sv) continue;
+            view_plan& P = B.plan[v];
+            P.tiles = (uint32_t)(((fds[v].width + 63) / 64) * ((fds[v].height + 63) / 64));
+            P.tile_base = total_tiles; total_tiles += P.tiles;
+            P.vis_base = vis_total; vis_total += (uint64_t)P.tiles * Sv * 4096;
+        }
+        B.s_tiles[si] = total_tiles - B.s_tile0[si];
+    }
+    B.total_ss = total_ss; B.n_jobs = (uint32_t)jobs.size(); B.total_tiles = total_tiles; B.total_prox = total_prox;
+    B.total_packets = total_packets; B.max_inst = max_inst; B.max_pairs = (uint32_t)max_pairs; B.color_total = color_total;
     const size_t n_rec = (size_t)total_ss * 16;
     /* staging layout */
     size_t so = 0;
     auto stage_take = [&](size_t bytes) { so = (so + 255) & ~(size_t)255; const size_t r = so; so += bytes; return r; };
-    const size_t o_F = stage_take(sizeof(sftg_frame));
+    const size_t o_F = stage_take((size_t)nv * sizeof(sftg_frame));
     const size_t o_inst = stage_take(inst.size() * sizeof(sftg_inst));
     const size_t o_bones = stage_take(bones.size() * 4 + 64);
     const size_t o_jobs = stage_take(jobs.size() * sizeof(sftg_job) + 16);
-    const size_t o_pl = stage_take((size_t)fd->n_point * sizeof(sftg_point_light) + 16);
-    const size_t o_dl = stage_take((size_t)fd->n_dir * sizeof(sftg_dir_light) + 16);
-    const size_t o_px = stage_take((size_t)fd->n_proxies * sizeof(sftg_proxy) + 16);
-    const size_t o_tl = stage_take((size_t)fd->tlas_count * 256 + 16);
+    const size_t o_pl = stage_take((size_t)n_pl * sizeof(sftg_point_light) + 16);
+    const size_t o_dl = stage_take((size_t)n_dl * sizeof(sftg_dir_light) + 16);
+    const size_t o_px = stage_take((size_t)total_prox * sizeof(sftg_proxy) + 16);
+    const size_t o_tl = stage_take((size_t)n_tl * 256 + 16);
+    const size_t o_tv = stage_take((size_t)total_tiles * 2 + 16);
+    const size_t o_pv = stage_take((size_t)total_packets * 2 + 16);
+    const size_t o_xv = stage_take((size_t)total_prox * 2 + 16);
     const size_t stage_bytes = so;
     /* device arena layout */
     size_t need = stage_bytes + 4096;
     auto acc = [&](size_t bytes) { need = ((need + 255) & ~(size_t)255) + bytes; };
     acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
-    acc((size_t)tiles * 4); acc((size_t)tiles * 4); acc(ctx->tile_cap * 8);
-    acc((size_t)tiles * S * 4096 * 8); acc((size_t)tiles * 8 + 8);
-    const size_t n_packets = (size_t)(fd->n_point < 64 ? fd->n_point : 64) * ((fd->n_proxies + 7) / 8) * 3;
-    acc((size_t)fd->n_proxies * 64 + 64); acc(n_packets * sftg_packet_bytes() + 64);
-    acc((n_packets * (fd->n_instances ? fd->n_instances : 1) + 1) * 8); acc(64); acc(((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
-    if (want_debug) { acc((size_t)tiles * S * 4096 * 4); acc((size_t)tiles * S * 4096 * 4); acc((size_t)W * H * 16 * 4); }
+    acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(ctx->tile_cap * 8);
+    acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
+    acc((max_pairs + 1) * 8); acc(64); acc(((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
+    acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
+    const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
+    if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
     if (need > ctx->arena_cap) {
         if (ctx->arena) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->arena); ctx->arena = nullptr; }
         size_t nc = need + need / 4;
         if (cudaMalloc(&ctx->arena, nc) != cudaSuccess) { ctx->arena_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "frame arena of %zu bytes", nc); }
         ctx->arena_cap = nc;
     }
+    if (color_total * 4 > ctx->d_color_cap) {
+        if (ctx->d_color) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->d_color); }
+        if (cudaMalloc((void**)&ctx->d_color, color_total * 4) != cudaSuccess) { ctx->d_color = nullptr; ctx->d_color_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "colour buffers"); }
+        ctx->d_color_cap = color_total * 4;
+    }
     if (stage_bytes > ctx->h_stage_cap) {
-        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        if (ctx->h_stage) { cudaStreamSynchronize(ctx->stream); cudaFreeHost(ctx->h_stage); }
         size_t nc = stage_bytes + stage_bytes / 4 + 4096;
         if (cudaMallocHost(&ctx->h_stage, nc) != cudaSuccess) { ctx->h_stage = nullptr; ctx->h_stage_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "pinned staging"); }
         ctx->h_stage_cap = nc;
@@ -383,161 +447,182 @@ static int build_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, bool want_debug
     B.mrect = bp.take<int4>((size_t)total_ss + 1);
     B.clips = bp.take<sftg_clip_tri>(ctx->clip_cap);
     B.clip_rect = bp.take<int4>(ctx->clip_cap);
-    B.tile_count = bp.take<uint32_t>(tiles);
-    B.tile_start = bp.take<uint32_t>(tiles);
+    B.tile_count = bp.take<uint32_t>(total_tiles);
+    B.tile_start = bp.take<uint32_t>(total_tiles);
     B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
-    B.light_vis = bp.take<uint8_t>((size_t)fd->n_proxies * 64 + 64);
-    B.packets = bp.take<char>(n_packets * sftg_packet_bytes() + 64);
-    B.max_pairs = (uint32_t)(n_packets * (fd->n_instances ? fd->n_instances : 1));
-    B.pairs = bp.take<uint2>((size_t)B.max_pairs + 1);
+    B.light_vis = bp.take<uint8_t>((size_t)total_prox * 64 + 64);
+    B.packets = bp.take<char>((size_t)total_packets * sftg_packet_bytes() + 64);
+    B.pairs = bp.take<uint2>((size_t)max_pairs + 1);
     B.n_pairs = bp.take<uint32_t>(16);
-    B.scan_tmp = bp.take<uint32_t>((n_rec + tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
+    B.scan_tmp = bp.take<uint32_t>((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
     B.status = bp.take<uint32_t>(16);
     B.totals = bp.take<uint32_t>(16);
-    B.vis = bp.take<float2>((size_t)tiles * S * 4096);
-    B.zrange = bp.take<float2>((size_t)tiles + 1);
+    B.vis = bp.take<float2>(vis_total);
+    B.zrange = bp.take<float2>((size_t)total_tiles + 1);
     B.vis_depth = nullptr; B.vis_id = nullptr; B.shadow = nullptr;
     if (want_debug) {
-        B.vis_depth = bp.take<float>((size_t)tiles * S * 4096);
-        B.vis_id = bp.take<uint32_t>((size_t)tiles * S * 4096);
-        B.shadow = bp.take<float>((size_t)W * H * 16);
+        B.vis_depth = bp.take<float>((size_t)total_tiles * S0 * 4096);
+        B.vis_id = bp.take<uint32_t>((size_t)total_tiles * S0 * 4096);
+        B.shadow = bp.take<float>((size_t)W0 * H0 * 16);
     }
-    B.used = bp.off;
     /* fill the staging block */
-    sftg_frame* F = (sftg_frame*)(hs + o_F);
-    memset(F, 0, sizeof(*F));
-    F->width = W; F->height = H; F->samples = S; F->pitch = W;
-    F->hw = (float)W * 0.5f; F->hh = (float)H * 0.5f; F->vpx = 0.f; F->vpy = 0.f;
-    F->cols = cols; F->rows = rows; F->tiles = tiles; F->debug_mode = (int32_t)fd->debug_mode;
-    F->clear = fd->clear; F->clear_color = fd->clear_color; F->shadows = fd->shadows;
-    memcpy(F->cam, fd->cam_pos, 12);
-    memcpy(F->vp, fd->view_proj, 64);
-    for (int p = 0; p < 6; p++) {
-        for (int a = 0; a < 3; a++) { F->fn[p][a] = fd->frustum_n[p][a]; F->fan[p][a] = fabsf(fd->frustum_n[p][a]); }
-        F->fd[p] = fd->frustum_d[p];
+    uint16_t* tv = (uint16_t*)(hs + o_tv);
+    uint16_t* pv = (uint16_t*)(hs + o_pv);
+    uint16_t* xv = (uint16_t*)(hs + o_xv);
+    for (uint32_t v = 0; v < nv; v++) {
+        const sftg_frame_desc* fd = &fds[v];
+        const view_plan& P = B.plan[v];
+        const int W = fd->width, H = fd->height;
+        sftg_frame* F = (sftg_frame*)(hs + o_F) + v;
+        memset(F, 0, sizeof(*F));
+        F->width = W; F->height = H; F->samples = fd->samples; F->pitch = W;
+        F->hw = (float)W * 0.5f; F->hh = (float)H * 0.5f; F->vpx = 0.f; F->vpy = 0.f;
+        F->cols = (W + 63) / 64; F->rows = (H + 63) / 64; F->tiles = (int32_t)P.tiles; F->debug_mode = (int32_t)fd->debug_mode;
+        F->clear = fd->clear; F->clear_color = fd->clear_color; F->shadows = fd->shadows;
+        memcpy(F->cam, fd->cam_pos, 12);
+        memcpy(F->vp, fd->view_proj, 64);
+        for (int p = 0; p < 6; p++) {
+            for (int a = 0; a < 3; a++) { F->fn[p][a] = fd->frustum_n[p][a]; F->fan[p][a] = fabsf(fd->frustum_n[p][a]); }
+            F->fd[p] = fd->frustum_d[p];
+        }
+        memcpy(F->ambient, fd->ambient, 12);
+        F->lightmap_brightness = fd->lightmap_brightness;
+        F->n_point = fd->n_point; F->n_dir = fd->n_dir; F->n_proxies = fd->n_proxies; F->n_inst = fd->n_instances;
+        F->total_ss = P.total_ss; F->n_jobs = B.n_jobs; F->tlas_root = fd->tlas_root; F->tlas_count = fd->tlas_count;
+        F->clip_cap = (uint32_t)ctx->clip_cap; F->tile_cap = (uint32_t)ctx->tile_cap;
+        F->view = v; F->ss_base = P.ss_base; F->tile_base = P.tile_base; F->prox_base = P.prox_base;
+        F->packet_base = P.packet_base; F->n_packets = P.n_packets; F->vis_base = P.vis_base;
+        F->color_dev = ctx->d_color + P.color_off;
+        F->inst = (const sftg_inst*)(ds + o_inst) + P.inst_off;
+        F->bones = (const float*)(ds + o_bones) + P.bone_off;
+        F->jobs = (const sftg_job*)(ds + o_jobs);
+        F->point = (const sftg_point_light*)(ds + o_pl) + P.pl_off;
+        F->dir = (const sftg_dir_light*)(ds + o_dl) + P.dl_off;
+        F->proxies = (const sftg_proxy*)(ds + o_px) + P.prox_base;
+        F->tlas = (const sftg_bvh_node*)(ds + o_tl) + P.tl_off;
+        F->models = (const sftg_model*)ctx->models.ptr;
+        F->texs = (const sftg_tex*)ctx->texs.ptr;
+        F->texels = (const uint32_t*)ctx->texels.ptr;
+        F->mats = (const sftg_mat*)ctx->mats.ptr;
+        F->ml_attr = (const float*)ctx->ml_attr.ptr;
+        F->ml_inds = (const uint8_t*)ctx->ml_inds.ptr;
+        F->ml_cull = (const float*)ctx->ml_cull.ptr;
+        F->ml_info = (const sftg_meshlet_info*)ctx->ml_info.ptr;
+        F->skin_j = (const uint16_t*)ctx->skin_j.ptr;
+        F->skin_w = (const uint8_t*)ctx->skin_w.ptr;
+        F->blas = (const sftg_bvh_node*)ctx->blas.ptr;
+        for (uint32_t l = 0; l < fd->n_point; l++) memcpy(hs + o_pl + (P.pl_off + l) * sizeof(sftg_point_light), fd->point_lights + 8 * l, 32);
+        for (uint32_t l = 0; l < fd->n_dir; l++) memcpy(hs + o_dl + (P.dl_off + l) * sizeof(sftg_dir_light), fd->dir_lights + 6 * l, 24);
+        for (uint32_t p = 0; p < fd->n_proxies; p++) memcpy(hs + o_px + (P.prox_base + p) * sizeof(sftg_proxy), fd->proxies + 8 * p, 32);
+        if (fd->tlas_count) memcpy(hs + o_tl + (size_t)P.tl_off * 256, fd->tlas_nodes, (size_t)fd->tlas_count * 256);
+        for (uint32_t t = 0; t < P.tiles; t++) tv[P.tile_base + t] = (uint16_t)v;
+        for (uint32_t k = 0; k < P.n_packets; k++) pv[P.packet_base + k] = (uint16_t)v;
+        for (uint32_t p = 0; p < fd->n_proxies; p++) xv[P.prox_base + p] = (uint16_t)v;
     }
-    memcpy(F->ambient, fd->ambient, 12);
-    F->lightmap_brightness = fd->lightmap_brightness;
-    F->n_point = fd->n_point; F->n_dir = fd->n_dir; F->n_proxies = fd->n_proxies; F->n_inst = fd->n_instances;
-    F->total_ss = total_ss; F->n_jobs = n_jobs; F->tlas_root = fd->tlas_root; F->tlas_count = fd->tlas_count;
-    F->clip_cap = (uint32_t)ctx->clip_cap; F->tile_cap = (uint32_t)ctx->tile_cap;
-    F->inst = (const sftg_inst*)(ds + o_inst);
-    F->bones = (const float*)(ds + o_bones);
-    F->jobs = (const sftg_job*)(ds + o_jobs);
-    F->point = (const sftg_point_light*)(ds + o_pl);
-    F->dir = (const sftg_dir_light*)(ds + o_dl);
-    F->proxies = (const sftg_proxy*)(ds + o_px);
-    F->tlas = (const sftg_bvh_node*)(ds + o_tl);
-    F->models = (const sftg_model*)ctx->models.ptr;
-    F->texs = (const sftg_tex*)ctx->texs.ptr;
-    F->texels = (const uint32_t*)ctx->texels.ptr;
-    F->mats = (const sftg_mat*)ctx->mats.ptr;
-    F->ml_attr = (const float*)ctx->ml_attr.ptr;
-    F->ml_inds = (const uint8_t*)ctx->ml_inds.ptr;
-    F->ml_cull = (const float*)ctx->ml_cull.ptr;
-    F->ml_info = (const sftg_meshlet_info*)ctx->ml_info.ptr;
-    F->skin_j = (const uint16_t*)ctx->skin_j.ptr;
-    F->skin_w = (const uint8_t*)ctx->skin_w.ptr;
-    F->blas = (const sftg_bvh_node*)ctx->blas.ptr;
     memcpy(hs + o_inst, inst.data(), inst.size() * sizeof(sftg_inst));
     if (!bones.empty()) memcpy(hs + o_bones, bones.data(), bones.size() * 4);
     if (!jobs.empty()) memcpy(hs + o_jobs, jobs.data(), jobs.size() * sizeof(sftg_job));
-    for (uint32_t l = 0; l < fd->n_point; l++) memcpy(hs + o_pl + l * sizeof(sftg_point_light), fd->point_lights + 8 * l, 32);
-    for (uint32_t l = 0; l < fd->n_dir; l++) memcpy(hs + o_dl + l * sizeof(sftg_dir_light), fd->dir_lights + 6 * l, 24);
-    for (uint32_t p = 0; p < fd->n_proxies; p++) memcpy(hs + o_px + p * sizeof(sftg_proxy), fd->proxies + 8 * p, 32);
-    if (fd->tlas_count) memcpy(hs + o_tl, fd->tlas_nodes, (size_t)fd->tlas_count * 256);
-    B.F = (sftg_frame*)(ds + o_F);
+    B.frames = (sftg_frame*)(ds + o_F);
+    B.jobs = (const sftg_job*)(ds + o_jobs);
+    B.tile_view = (const uint16_t*)(ds + o_tv);
+    B.packet_view = (const uint16_t*)(ds + o_pv);
+    B.prox_view = (const uint16_t*)(ds + o_xv);
     CK(cudaMemcpyAsync(ds, hs, stage_bytes, cudaMemcpyHostToDevice, ctx->stream));
     return 0;
 }
 
-static int launch_frame(sftg_ctx* ctx, const sftg_frame_desc* fd, const frame_bufs& B, uint32_t total_ss, uint32_t n_jobs, uint32_t* d_color) {
-    const int S = fd->samples;
-    const int tiles = ((fd->width + 63) / 64) * ((fd->height + 63) / 64);
-    const uint32_t n_rec = total_ss * 16;
+static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
+    const uint32_t n_rec = B.total_ss * 16;
     cudaStream_t st = ctx->stream;
     ctx->launches = 0;
     CK(cudaMemsetAsync(B.status, 0, 64, st));
     CK(cudaEventRecord(ctx->ev[0], st));
-    if (fd->shadows && fd->n_point && fd->n_proxies) {
-        CK(cudaMemsetAsync(B.light_vis, 0, (size_t)fd->n_proxies * 64, st));   /* columns past the lights stay 0 */
-        sftg_launch_occlusion(B.F, fd->n_point, fd->n_proxies, fd->n_instances, B.packets, B.pairs, B.n_pairs, B.max_pairs,
-                              B.light_vis, B.status, st);
+    if (B.total_prox) CK(cudaMemsetAsync(B.light_vis, 0, (size_t)B.total_prox * 64, st));   /* columns past the lights stay 0 */
+    if (B.total_packets) {
+        sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
+                              B.pairs, B.n_pairs, B.max_pairs, B.light_vis, B.status, st);
         ctx->launches += 3;
     }
     CK(cudaEventRecord(ctx->ev[1], st));
-    if (n_jobs) {
-        k_geometry<<<(n_jobs + 3) / 4, 128, 0, st>>>(B.F, B.ss, B.recs, B.clip_cnt, B.mrect);
+    if (B.n_jobs) {
+        k_geometry<<<(B.n_jobs + 3) / 4, 128, 0, st>>>(B.frames, B.jobs, B.n_jobs, B.ss, B.recs, B.clip_cnt, B.mrect);
         ctx->launches++;
     }
     if (n_rec) {
         scan_u32(B.clip_cnt, B.clip_base, n_rec, B.scan_tmp, B.totals + 0, st, &ctx->launches);
-        k_clip<<<(n_rec + 255) / 256, 256, 0, st>>>(B.F, B.ss, B.clip_cnt, B.clip_base, B.clips, B.clip_rect, B.mrect, n_rec);
+        k_clip<<<(n_rec + 255) / 256, 256, 0, st>>>(B.frames, B.n_views, B.ss, B.clip_cnt, B.clip_base, B.clips, B.clip_rect, B.mrect, n_rec);
         ctx->launches++;
     } else {
         CK(cudaMemsetAsync(B.totals, 0, 8, st));
     }
     CK(cudaEventRecord(ctx->ev[2], st));
-    k_bin<<<tiles, 256, 0, st>>>(B.F, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
-    scan_u32(B.tile_count, B.tile_start, tiles, B.scan_tmp, B.totals + 1, st, &ctx->launches);
-    k_bin<<<tiles, 256, 0, st>>>(B.F, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
+    k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
+    scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ctx->launches);
+    k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
     ctx->launches += 2;
     CK(cudaEventRecord(ctx->ev[3], st));
-    if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, (size_t)fd->width * fd->height * 16 * 4, st));
-    sftg_launch_tile(S, tiles, st, B.F, B.ss, B.clips, B.tile_start, B.tile_count, B.tile_pay, B.light_vis, B.vis, B.zrange, d_color, B.vis_depth, B.vis_id, B.shadow, ctx->ev[4]);
-    ctx->launches += 2;
+    if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));
+    sftg_tile_args A;
+    A.frames = B.frames; A.tile_view = B.tile_view; A.ss = B.ss; A.clips = B.clips; A.clip_base = B.clip_base;
+    A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
+    A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
+    for (int si = 0; si < 3; si++)
+        if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], st, A); ctx->launches++; }
+    CK(cudaEventRecord(ctx->ev[4], st));
+    for (int si = 0; si < 3; si++)
+        if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], st, A); ctx->launches++; }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[5], st));
     return 0;
 }
 
-static int frame_common(sftg_ctx* ctx, const sftg_frame_desc* fd, uint32_t* host_color, int32_t pitch_bytes, sftg_debug_out* dbg, const uint32_t** out_dev) {
-    if (!ctx || !fd) return SFTG_E_ARG;
+/* Renders a batch of views.  host_color[v] (optional) receives view v's colour with pitch
+ * pitch_bytes[v]; out_dev[v] (optional) its device colour buffer, valid until the next call. */
+static int batch_common(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, uint32_t* const* host_color, const int32_t* pitch_bytes,
+                        sftg_debug_out* dbg, const uint32_t** out_dev) {
+    if (!ctx || !fds) return SFTG_E_ARG;
     CK(cudaSetDevice(ctx->device));
     int rc = sync_tables(ctx);
     if (rc) return rc;
-    const int W = fd->width, H = fd->height;
-    const size_t cbytes = (size_t)W * H * 4;
-    if (cbytes > ctx->d_color_cap) {
-        if (ctx->d_color) cudaFree(ctx->d_color);
-        if (cudaMalloc((void**)&ctx->d_color, cbytes) != cudaSuccess) { ctx->d_color = nullptr; ctx->d_color_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "colour buffer"); }
-        ctx->d_color_cap = cbytes;
-    }
-    const int pitch = pitch_bytes > 0 ? pitch_bytes : W * 4;
+    auto pitch_of = [&](uint32_t v) { return (pitch_bytes && pitch_bytes[v] > 0) ? (size_t)pitch_bytes[v] : (size_t)fds[v].width * 4; };
     for (int attempt = 0; attempt < 4; attempt++) {
-        frame_bufs B; uint32_t total_ss = 0, n_jobs = 0;
-        if ((rc = build_frame(ctx, fd, dbg != nullptr, B, total_ss, n_jobs))) return rc;
-        if (!fd->clear && host_color)   /* the reference blends over / keeps the caller's pixels */
-            CK(cudaMemcpy2DAsync(ctx->d_color, (size_t)W * 4, host_color, (size_t)pitch, (size_t)W * 4, H, cudaMemcpyHostToDevice, ctx->stream));
-        if ((rc = launch_frame(ctx, fd, B, total_ss, n_jobs, ctx->d_color))) return rc;
+        batch_bufs B;
+        if ((rc = build_batch(ctx, fds, nv, dbg != nullptr, B))) return rc;
+        for (uint32_t v = 0; v < nv; v++)   /* the reference blends over / keeps the caller's pixels */
+            if (!fds[v].clear && host_color && host_color[v])
+                CK(cudaMemcpy2DAsync(ctx->d_color + B.plan[v].color_off, (size_t)fds[v].width * 4, host_color[v], pitch_of(v),
+                                     (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyHostToDevice, ctx->stream));
+        if ((rc = launch_batch(ctx, B))) return rc;
         CK(cudaMemcpyAsync(ctx->h_status, B.status, 4, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaMemcpyAsync(ctx->h_status + 2, B.totals, 8, cudaMemcpyDeviceToHost, ctx->stream));
-        if (host_color)
-            CK(cudaMemcpy2DAsync(host_color, (size_t)pitch, ctx->d_color, (size_t)W * 4, (size_t)W * 4, H, cudaMemcpyDeviceToHost, ctx->stream));
+        for (uint32_t v = 0; v < nv; v++)
+            if (host_color && host_color[v])
+                CK(cudaMemcpy2DAsync(host_color[v], pitch_of(v), ctx->d_color + B.plan[v].color_off, (size_t)fds[v].width * 4,
+                                     (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         const uint32_t clip_total = ctx->h_status[2], pay_total = ctx->h_status[3];
-        if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap) {   /* capacity exceeded: grow and redo the frame */
+        if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap) {   /* capacity exceeded: grow and redo the batch */
             while (ctx->clip_cap < clip_total) ctx->clip_cap *= 2;
             while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
             continue;
         }
-        float t[5];
-        for (int k = 0; k < 5; k++) { t[k] = 0.f; cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]); ctx->timings[k] = t[k]; }
+        for (int k = 0; k < 5; k++) { float t = 0.f; cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]); ctx->timings[k] = t; }
         if (dbg) {
-            const int S = fd->samples, tiles = ((W + 63) / 64) * ((H + 63) / 64);
+            const sftg_frame_desc* fd = &fds[0];
+            const int W = fd->width, H = fd->height, S = fd->samples, tiles = (int)B.total_tiles;
             if (dbg->vis_depth) CK(cudaMemcpy(dbg->vis_depth, B.vis_depth, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
             if (dbg->vis_id) CK(cudaMemcpy(dbg->vis_id, B.vis_id, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
             if (dbg->tile_counts) CK(cudaMemcpy(dbg->tile_counts, B.tile_count, (size_t)tiles * 4, cudaMemcpyDeviceToHost));
             if (dbg->tile_payload_total) *dbg->tile_payload_total = pay_total;
             if (dbg->tile_payloads && pay_total <= dbg->tile_payload_cap) CK(cudaMemcpy(dbg->tile_payloads, B.tile_pay, (size_t)pay_total * 8, cudaMemcpyDeviceToHost));
-            if (dbg->ss_cache) CK(cudaMemcpy(dbg->ss_cache, B.ss, (size_t)total_ss * 2304, cudaMemcpyDeviceToHost));
+            if (dbg->ss_cache) CK(cudaMemcpy(dbg->ss_cache, B.ss, (size_t)B.total_ss * 2304, cudaMemcpyDeviceToHost));
             if (dbg->light_vis && fd->n_proxies) CK(cudaMemcpy(dbg->light_vis, B.light_vis, (size_t)fd->n_proxies * 64, cudaMemcpyDeviceToHost));
             if (dbg->clip_total) *dbg->clip_total = clip_total;
             if (dbg->clip_tris && clip_total <= dbg->clip_cap) CK(cudaMemcpy(dbg->clip_tris, B.clips, (size_t)clip_total * sizeof(sftg_clip_tri), cudaMemcpyDeviceToHost));
-            if (dbg->shadow && fd->samples == 1) CK(cudaMemcpy(dbg->shadow, B.shadow, (size_t)W * H * 16 * 4, cudaMemcpyDeviceToHost));
+            if (dbg->shadow && S == 1) CK(cudaMemcpy(dbg->shadow, B.shadow, (size_t)W * H * 16 * 4, cudaMemcpyDeviceToHost));
             if (dbg->status) *dbg->status = ctx->h_status[0];
         }
-        if (out_dev) *out_dev = ctx->d_color;
+        if (out_dev) for (uint32_t v = 0; v < nv; v++) out_dev[v] = ctx->d_color + B.plan[v].color_off;
         if (ctx->h_status[0] & 1u) return set_err(ctx, SFTG_E_DEVICE_STATUS, "occlusion traversal exceeded its stack bound");
         return SFTG_OK;
     }
@@ -545,14 +630,18 @@ static int frame_common(sftg_ctx* ctx, const sftg_frame_desc* fd, uint32_t* host
 }
 
 extern "C" int sftg_frame_render(sftg_ctx* ctx, const sftg_frame_desc* fd, uint32_t* color, int32_t pitch_bytes, sftg_debug_out* dbg) {
-    if (dbg) {   /* debug capture renders into scratch state first so vis buffers are available */
-        if (dbg->shadow && fd->samples == 1) {}
-    }
-    return frame_common(ctx, fd, color, pitch_bytes, dbg, nullptr);
+    uint32_t* hc[1] = { color };
+    const int32_t pb[1] = { pitch_bytes };
+    return batch_common(ctx, fd, 1, color ? hc : nullptr, pb, dbg, nullptr);
 }
 
 extern "C" int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* fd, const uint32_t** out_device_color) {
-    return frame_common(ctx, fd, nullptr, 0, nullptr, out_device_color);
+    return batch_common(ctx, fd, 1, nullptr, nullptr, nullptr, out_device_color);
+}
+
+extern "C" int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, uint32_t* const* colors,
+                                  const int32_t* pitch_bytes, const uint32_t** out_device_colors) {
+    return batch_common(ctx, fds, n_views, colors, pitch_bytes, nullptr, out_device_colors);
 }
 
 extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {

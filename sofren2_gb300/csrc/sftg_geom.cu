@@ -25,15 +25,16 @@
 
 /* ----------------------------------------------------------------------------------------- */
 __global__ void __launch_bounds__(GEOM_WARPS * 32)
-k_geometry(const sftg_frame* __restrict__ F, float* __restrict__ ss, sftg_batch_rec* __restrict__ recs,
-           uint32_t* __restrict__ clip_cnt, int4* __restrict__ mrect)
+k_geometry(const sftg_frame* __restrict__ frames, const sftg_job* __restrict__ jobs, uint32_t n_jobs, float* __restrict__ ss,
+           sftg_batch_rec* __restrict__ recs, uint32_t* __restrict__ clip_cnt, int4* __restrict__ mrect)
 {
     __shared__ float s_bones[GEOM_WARPS][GEOM_BONES * 16];
     __shared__ float s_v[GEOM_WARPS][6][64];   /* tx ty tz w sx sy */
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t job_i = blockIdx.x * GEOM_WARPS + warp;
-    if (job_i >= F->n_jobs) return;
-    const sftg_job J = F->jobs[job_i];
+    if (job_i >= n_jobs) return;
+    const sftg_job J = jobs[job_i];
+    const sftg_frame* F = frames + J.view;
     const sftg_inst* I = &F->inst[J.inst];
     float T[16];
 #pragma unroll
@@ -85,7 +86,7 @@ k_geometry(const sftg_frame* __restrict__ F, float* __restrict__ ss, sftg_batch_
     for (uint32_t ln = 0; ln < J.count; ln++) {
         const uint32_t m = J.first + ln;             /* model-relative meshlet index */
         const uint32_t g = I->meshlet_base + m;      /* pool index */
-        const uint32_t ssi = I->ss_offset + m;
+        const uint32_t ssi = F->ss_base + I->ss_offset + m;
         if (!((alive >> ln) & 1u)) {
             if (lane < 16) {
                 sftg_batch_rec r; r.payload = 0; r.x0 = 1; r.x1 = 0; r.y0 = 1; r.y1 = 0;
@@ -209,7 +210,7 @@ SFTG_D cvert lerp_cv(const cvert& a, const cvert& b, float t) {
 }
 
 /* one thread per batch record with clip outputs (clipping is rare) */
-__global__ void k_clip(const sftg_frame* __restrict__ F, const float* __restrict__ ss,
+__global__ void k_clip(const sftg_frame* __restrict__ frames, uint32_t n_views, const float* __restrict__ ss,
                        const uint32_t* __restrict__ clip_cnt, const uint32_t* __restrict__ clip_base,
                        sftg_clip_tri* __restrict__ clips, int4* __restrict__ clip_rect, int4* __restrict__ mrect,
                        uint32_t n_records)
@@ -217,11 +218,15 @@ __global__ void k_clip(const sftg_frame* __restrict__ F, const float* __restrict
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_records || clip_cnt[r] == 0) return;
     const uint32_t ssi = r / 16, b = r % 16;
-    /* find the instance owning this screen-space slot */
+    /* the view, then the instance, owning this screen-space slot (both laid out in order) */
+    uint32_t v = 0;
+    for (uint32_t k = 0; k < n_views; k++) if (frames[k].ss_base <= ssi && frames[k].total_ss) v = k;
+    const sftg_frame* F = frames + v;
+    const uint32_t lss = ssi - F->ss_base;
     uint32_t ii = 0;
-    for (uint32_t k = 0; k < F->n_inst; k++) if (F->inst[k].ss_offset <= ssi) ii = k;
+    for (uint32_t k = 0; k < F->n_inst; k++) if (F->inst[k].ss_offset <= lss) ii = k;
     const sftg_inst* I = &F->inst[ii];
-    const uint32_t m = ssi - I->ss_offset, g = I->meshlet_base + m;
+    const uint32_t m = lss - I->ss_offset, g = I->meshlet_base + m;
     const float* at = F->ml_attr + (size_t)g * 640;
     const float* S = ss + (size_t)ssi * 576;
     const uint8_t* ind = F->ml_inds + (size_t)g * 512;
@@ -311,7 +316,7 @@ SFTG_D bool rect_has(int x0, int x1, int y0, int y1, int tx, int ty) { return x0
  * for each batch, its clipped triangles (slot order) then its batch payload.  Lanes 0..15 =
  * batches; returns the meshlet total (same on all lanes). */
 SFTG_D uint32_t bin_meshlet(const sftg_batch_rec* recs, const uint32_t* clip_cnt, const uint32_t* clip_base,
-                            const int4* clip_rect, uint32_t clip_cap, uint32_t ssi, int tx, int ty, int lane, uint64_t* out)
+                            const int4* clip_rect, uint32_t clip_cap, uint32_t vclip, uint32_t ssi, int tx, int ty, int lane, uint64_t* out)
 {
     uint32_t cnt = 0, nclip = 0, cb = 0;
     sftg_batch_rec r; r.payload = 0;
@@ -338,7 +343,7 @@ SFTG_D uint32_t bin_meshlet(const sftg_batch_rec* recs, const uint32_t* clip_cnt
         uint64_t* o = out + (incl - cnt);
         for (uint32_t k = 0; k < nclip && cb + k < clip_cap; k++) {
             const int4 q = clip_rect[cb + k];
-            if (rect_has(q.x, q.y, q.z, q.w, tx, ty)) *o++ = (uint64_t)(cb + k);
+            if (rect_has(q.x, q.y, q.z, q.w, tx, ty)) *o++ = (uint64_t)(cb + k - vclip);
         }
         if (r.payload != 0 && rect_has(r.x0, r.x1, r.y0, r.y1, tx, ty)) *o = r.payload;
     }
@@ -346,29 +351,34 @@ SFTG_D uint32_t bin_meshlet(const sftg_batch_rec* recs, const uint32_t* clip_cnt
 }
 
 __global__ void __launch_bounds__(BIN_THREADS)
-k_bin(const sftg_frame* __restrict__ F, const sftg_batch_rec* __restrict__ recs, const uint32_t* __restrict__ clip_cnt,
-      const uint32_t* __restrict__ clip_base, const int4* __restrict__ clip_rect, const int4* __restrict__ mrect,
-      uint32_t* __restrict__ tile_count, const uint32_t* __restrict__ tile_start, uint64_t* __restrict__ tile_pay)
+k_bin(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_view, const sftg_batch_rec* __restrict__ recs,
+      const uint32_t* __restrict__ clip_cnt, const uint32_t* __restrict__ clip_base, const int4* __restrict__ clip_rect,
+      const int4* __restrict__ mrect, uint32_t* __restrict__ tile_count, const uint32_t* __restrict__ tile_start,
+      uint64_t* __restrict__ tile_pay)
 {
     __shared__ uint32_t s_hits[BIN_THREADS];
     __shared__ uint32_t s_cnt[BIN_THREADS];
     __shared__ uint32_t s_wsum[BIN_THREADS / 32];
     __shared__ uint32_t s_nhits;
-    const int tile = blockIdx.x;
+    const int gtile = blockIdx.x;                       /* batch-wide tile index */
+    const sftg_frame* F = frames + tile_view[gtile];
+    const int tile = gtile - (int)F->tile_base;
     const int tx = tile % F->cols, ty = tile / F->cols;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t n_ss = F->total_ss;
+    /* clipped payloads carry the view's own slot numbers (slots restart at 0 per frame) */
+    const uint32_t vclip = n_ss ? clip_base[(size_t)F->ss_base * 16] : 0u;
     uint64_t* out = nullptr;
     if (tile_pay) {
         /* over capacity: the host grows the buffer and re-renders; write nothing */
-        if ((uint64_t)tile_start[tile] + tile_count[tile] > F->tile_cap) return;
-        out = tile_pay + tile_start[tile];
+        if ((uint64_t)tile_start[gtile] + tile_count[gtile] > F->tile_cap) return;
+        out = tile_pay + tile_start[gtile];
     }
     uint32_t running = 0;
     for (uint32_t base = 0; base < n_ss; base += BIN_THREADS) {
-        const uint32_t s = base + tid;
+        const uint32_t s = F->ss_base + base + tid;
         bool hit = false;
-        if (s < n_ss) { const int4 q = mrect[s]; hit = rect_has(q.x, q.y, q.z, q.w, tx, ty); }
+        if (base + tid < n_ss) { const int4 q = mrect[s]; hit = rect_has(q.x, q.y, q.z, q.w, tx, ty); }
         /* ordered compaction of hit meshlets */
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
         if (lane == 0) s_wsum[warp] = __popc(bal);
@@ -381,7 +391,7 @@ k_bin(const sftg_frame* __restrict__ F, const sftg_batch_rec* __restrict__ recs,
         const uint32_t nh = s_nhits;
         /* per-hit payload counts */
         for (uint32_t h = warp; h < nh; h += BIN_THREADS / 32) {
-            const uint32_t c = bin_meshlet(recs, clip_cnt, clip_base, clip_rect, F->clip_cap, s_hits[h], tx, ty, lane, nullptr);
+            const uint32_t c = bin_meshlet(recs, clip_cnt, clip_base, clip_rect, F->clip_cap, vclip, s_hits[h], tx, ty, lane, nullptr);
             if (lane == 0) s_cnt[h] = c;
         }
         __syncthreads();
@@ -394,7 +404,7 @@ k_bin(const sftg_frame* __restrict__ F, const sftg_batch_rec* __restrict__ recs,
             }
             __syncthreads();
             for (uint32_t h = warp; h < nh; h += BIN_THREADS / 32)
-                bin_meshlet(recs, clip_cnt, clip_base, clip_rect, F->clip_cap, s_hits[h], tx, ty, lane, out + running + s_cnt[h]);
+                bin_meshlet(recs, clip_cnt, clip_base, clip_rect, F->clip_cap, vclip, s_hits[h], tx, ty, lane, out + running + s_cnt[h]);
             running += s_wsum[0];
         } else {
             if (tid == 0) { uint32_t acc = 0; for (uint32_t h = 0; h < nh; h++) acc += s_cnt[h]; s_wsum[0] = acc; }
@@ -403,7 +413,7 @@ k_bin(const sftg_frame* __restrict__ F, const sftg_batch_rec* __restrict__ recs,
         }
         __syncthreads();
     }
-    if (!out && tid == 0) tile_count[tile] = running;
+    if (!out && tid == 0) tile_count[gtile] = running;
 }
 
 /* ----------------------------------------------------------------------------------------- */

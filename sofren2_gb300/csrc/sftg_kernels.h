@@ -15,21 +15,43 @@ struct sftg_clip_tri {
     uint32_t inst, m;
 };
 
-__global__ void k_geometry(const sftg_frame* F, float* ss, sftg_batch_rec* recs, uint32_t* clip_cnt, int4* mrect);
-__global__ void k_clip(const sftg_frame* F, const float* ss, const uint32_t* clip_cnt, const uint32_t* clip_base,
-                       sftg_clip_tri* clips, int4* clip_rect, int4* mrect, uint32_t n_records);
-__global__ void k_bin(const sftg_frame* F, const sftg_batch_rec* recs, const uint32_t* clip_cnt, const uint32_t* clip_base,
-                      const int4* clip_rect, const int4* mrect, uint32_t* tile_count, const uint32_t* tile_start, uint64_t* tile_pay);
+/* Arguments of the tile kernels.  Tiles are numbered batch-wide: tile_view maps a tile to its
+ * view's frame block, whose tile_base, ss_base, prox_base and vis_base locate the view's rows in
+ * the shared arrays. */
+struct sftg_tile_args {
+    const sftg_frame* frames;
+    const uint16_t* tile_view;
+    const float* ss;
+    const sftg_clip_tri* clips;
+    const uint32_t* clip_base;     /* exclusive scan of clip counts: a view's first slot is clip_base[ss_base * 16] */
+    const uint32_t* tile_start;
+    const uint32_t* tile_count;
+    const uint64_t* tile_pay;
+    const uint8_t* light_vis;      /* [proxy][64] */
+    float2* vis;                   /* (depth, vis id) per sample */
+    float2* zrange;                /* per tile */
+    float* vis_depth;              /* debug capture of a single view, or null */
+    uint32_t* vis_id;
+    float* shadow_out;
+};
+
+__global__ void k_geometry(const sftg_frame* frames, const sftg_job* jobs, uint32_t n_jobs, float* ss, sftg_batch_rec* recs,
+                           uint32_t* clip_cnt, int4* mrect);
+__global__ void k_clip(const sftg_frame* frames, uint32_t n_views, const float* ss, const uint32_t* clip_cnt,
+                       const uint32_t* clip_base, sftg_clip_tri* clips, int4* clip_rect, int4* mrect, uint32_t n_records);
+__global__ void k_bin(const sftg_frame* frames, const uint16_t* tile_view, const sftg_batch_rec* recs, const uint32_t* clip_cnt,
+                      const uint32_t* clip_base, const int4* clip_rect, const int4* mrect, uint32_t* tile_count,
+                      const uint32_t* tile_start, uint64_t* tile_pay);
 __global__ void k_scan_reduce(const uint32_t* in, uint32_t n, uint32_t* sums);
 __global__ void k_scan_top(uint32_t* sums, uint32_t nb, uint32_t* total_out);
 __global__ void k_scan_down(const uint32_t* in, uint32_t n, const uint32_t* sums, uint32_t* out);
 size_t sftg_packet_bytes();
-void sftg_launch_occlusion(const sftg_frame* F, uint32_t n_point, uint32_t n_proxies, uint32_t n_inst, void* packets, uint2* pairs,
-                           uint32_t* n_pairs, uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
+/* packet_view maps a batch-wide shadow packet to its view, prox_view a batch-wide proxy */
+void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view, uint32_t n_packets, const uint16_t* prox_view,
+                           uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
+                           uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
-void sftg_launch_tile(int S, int tiles, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
-                      const uint32_t* tile_start, const uint32_t* tile_count, const uint64_t* tile_pay, const uint8_t* light_vis,
-                      float2* vis, float2* zrange, uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out,
-                      cudaEvent_t between);
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
 
 #define SFTG_SCAN_ELEMS_PER_BLOCK 4096

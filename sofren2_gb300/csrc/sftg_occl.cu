@@ -127,15 +127,18 @@ struct sftg_packet {
  * TLAS walk (sofren2.c:8178-8269, 4086-4135); every static instance the frustum reaches becomes
  * a (packet, instance) pair for phase B. */
 __global__ void __launch_bounds__(OCC_WARPS * 32)
-k_occl_tlas(const sftg_frame* __restrict__ F, sftg_packet* __restrict__ packets, uint2* __restrict__ pairs,
-            uint32_t* __restrict__ n_pairs, uint32_t max_pairs, uint32_t* __restrict__ status)
+k_occl_tlas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, uint32_t n_packets,
+            sftg_packet* __restrict__ packets, uint2* __restrict__ pairs, uint32_t* __restrict__ n_pairs, uint32_t max_pairs,
+            uint32_t* __restrict__ status)
 {
     __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t pc = F->n_proxies, lc = min(F->n_point, 64u), nbatch = (pc + 7) / 8;
-    const uint32_t pk = blockIdx.x * OCC_WARPS + warp;
-    if (pk >= lc * nbatch * 3) return;
-    const uint32_t ray = pk % 3, b = (pk / 3) % nbatch, l = pk / (3 * nbatch), pb = b * 8;
+    const uint32_t pk = blockIdx.x * OCC_WARPS + warp;   /* batch-wide packet index */
+    if (pk >= n_packets) return;
+    const sftg_frame* F = frames + packet_view[pk];
+    const uint32_t lpk = pk - F->packet_base;            /* packet index within the view */
+    const uint32_t pc = F->n_proxies, nbatch = (pc + 7) / 8;
+    const uint32_t ray = lpk % 3, b = (lpk / 3) % nbatch, l = lpk / (3 * nbatch), pb = b * 8;
     const sftg_point_light L = F->point[l];
     const v3 lpos = mk3(L.pos[0], L.pos[1], L.pos[2]);
     /* batch centre and light-disk targets, identical on every lane */
@@ -219,14 +222,15 @@ k_occl_tlas(const sftg_frame* __restrict__ F, sftg_packet* __restrict__ packets,
  * (triangle k of 4, ray r of 8) and run the any-hit test (3840-3904).  Hits are OR-ed into the
  * packet, which is what the reference accumulates in any visiting order. */
 __global__ void __launch_bounds__(OCC_WARPS * 32)
-k_occl_blas(const sftg_frame* __restrict__ F, sftg_packet* __restrict__ packets, const uint2* __restrict__ pairs,
-            const uint32_t* __restrict__ n_pairs, uint32_t max_pairs, uint32_t* __restrict__ status)
+k_occl_blas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, sftg_packet* __restrict__ packets,
+            const uint2* __restrict__ pairs, const uint32_t* __restrict__ n_pairs, uint32_t max_pairs, uint32_t* __restrict__ status)
 {
     __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t item = blockIdx.x * OCC_WARPS + warp;
     if (item >= min(*n_pairs, max_pairs)) return;
     const uint2 pr = pairs[item];
+    const sftg_frame* F = frames + packet_view[pr.x];
     sftg_packet* P = &packets[pr.x];
     const uint32_t full = P->active;
     const frustum6 pf = P->f;
@@ -321,26 +325,36 @@ k_occl_blas(const sftg_frame* __restrict__ F, sftg_packet* __restrict__ packets,
     if (lane == 0 && sat) atomicOr(&P->hits, sat);
 }
 
-/* Phase C: light_vis[p][l] = 3 - rays blocked (8169-8276) */
-__global__ void k_occl_finalize(const sftg_frame* __restrict__ F, const sftg_packet* __restrict__ packets, uint8_t* __restrict__ light_vis)
+/* Phase C: light_vis[p][l] = 3 - rays blocked (8169-8276); one thread per (batch-wide proxy,
+ * light column); columns at or beyond the view's light count keep the zero they were cleared to. */
+__global__ void k_occl_finalize(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ prox_view, uint32_t n_proxies,
+                                const sftg_packet* __restrict__ packets, uint8_t* __restrict__ light_vis)
 {
-    const uint32_t pc = F->n_proxies, lc = min(F->n_point, 64u), nbatch = (pc + 7) / 8;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= pc * lc) return;
-    const uint32_t p = i / lc, l = i % lc, b = p / 8, k = p % 8;
+    if (i >= n_proxies * 64) return;
+    const uint32_t gp = i >> 6, l = i & 63;
+    const sftg_frame* F = frames + prox_view[gp];
+    const uint32_t pc = F->n_proxies, lc = min(F->n_point, 64u), nbatch = (pc + 7) / 8;
+    if (l >= lc) return;
+    const uint32_t p = gp - F->prox_base, b = p / 8, k = p % 8;
+    const sftg_packet* P = packets + F->packet_base;
     int blocked = 0;
-    for (int ray = 0; ray < 3; ray++) blocked += (packets[(l * nbatch + b) * 3 + ray].hits >> k) & 1u;
-    light_vis[(size_t)p * 64 + l] = (uint8_t)(3 - blocked);
+    for (int ray = 0; ray < 3; ray++) blocked += (P[(l * nbatch + b) * 3 + ray].hits >> k) & 1u;
+    light_vis[(size_t)gp * 64 + l] = (uint8_t)(3 - blocked);
 }
 
 size_t sftg_packet_bytes() { return sizeof(sftg_packet); }
 
-void sftg_launch_occlusion(const sftg_frame* F, uint32_t n_point, uint32_t n_proxies, uint32_t n_inst, void* packets, uint2* pairs,
-                           uint32_t* n_pairs, uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st) {
-    const uint32_t lc = n_point < 64 ? n_point : 64, nbatch = (n_proxies + 7) / 8, npk = lc * nbatch * 3;
+void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view, uint32_t n_packets, const uint16_t* prox_view,
+                           uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
+                           uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st) {
     cudaMemsetAsync(n_pairs, 0, 4, st);
-    k_occl_tlas<<<(npk + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(F, (sftg_packet*)packets, pairs, n_pairs, max_pairs, status);
-    const uint32_t mp = npk * (n_inst ? n_inst : 1) < max_pairs ? npk * (n_inst ? n_inst : 1) : max_pairs;
-    k_occl_blas<<<(mp + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(F, (sftg_packet*)packets, pairs, n_pairs, max_pairs, status);
-    k_occl_finalize<<<(n_proxies * lc + 255) / 256, 256, 0, st>>>(F, (const sftg_packet*)packets, light_vis);
+    if (!n_packets) return;
+    k_occl_tlas<<<(n_packets + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, n_packets,
+                                                                                   (sftg_packet*)packets, pairs, n_pairs, max_pairs, status);
+    const uint64_t want = (uint64_t)n_packets * (max_inst ? max_inst : 1);
+    const uint32_t mp = want < max_pairs ? (uint32_t)want : max_pairs;
+    k_occl_blas<<<(mp + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, (sftg_packet*)packets, pairs,
+                                                                             n_pairs, max_pairs, status);
+    k_occl_finalize<<<(n_proxies * 64 + 255) / 256, 256, 0, st>>>(frames, prox_view, n_proxies, (const sftg_packet*)packets, light_vis);
 }

@@ -237,21 +237,25 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
  * light culling. */
 template <int S>
 __global__ void __launch_bounds__(TILE_THREADS)
-k_raster(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sftg_clip_tri* __restrict__ clips,
-         const uint32_t* __restrict__ tile_start, const uint32_t* __restrict__ tile_count, const uint64_t* __restrict__ tile_pay,
-         float2* __restrict__ vis, float2* __restrict__ zrange, float* __restrict__ vis_depth, uint32_t* __restrict__ vis_id)
+k_raster(const sftg_tile_args A, uint32_t tile0)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
     tri_setup* setups = (tri_setup*)(smem + (size_t)S * SFTG_TILE_PX * 8);
     __shared__ uint32_t s_nsetup, s_next;
     __shared__ float s_red[2][TILE_THREADS / 32];
-    const int tile = blockIdx.x;
+    const uint32_t gtile = tile0 + blockIdx.x;                             /* batch-wide tile index */
+    const sftg_frame* F = A.frames + A.tile_view[gtile];
+    const int tile = (int)(gtile - F->tile_base);
+    const float* ss = A.ss + (size_t)F->ss_base * 576;
+    const sftg_clip_tri* clips = A.clips + (F->total_ss ? A.clip_base[(size_t)F->ss_base * 16] : 0u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
-    uint32_t count = tile_count[tile];
-    if ((uint64_t)tile_start[tile] + count > F->tile_cap) count = 0;   /* overflowed frame, redone by the host */
-    const uint64_t* list = tile_pay + tile_start[tile];
+    uint32_t count = A.tile_count[gtile];
+    if ((uint64_t)A.tile_start[gtile] + count > F->tile_cap) count = 0;   /* overflowed frame, redone by the host */
+    const uint64_t* list = A.tile_pay + A.tile_start[gtile];
+    float* vis_depth = A.vis_depth;
+    uint32_t* vis_id = A.vis_id;
 
     for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) keys[i] = 0ull;
     const int grp_lane = tid & 7;
@@ -311,7 +315,7 @@ k_raster(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const s
     __syncthreads();
     /* decode, store, depth range */
     float zmin = 1e9f, zmax = -1e9f;
-    float2* tv = vis + (size_t)tile * S * SFTG_TILE_PX;
+    float2* tv = A.vis + F->vis_base + (size_t)tile * S * SFTG_TILE_PX;
     for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) {
         const unsigned long long k = keys[i];
         float d = 0.f; uint32_t vid = SFTG_INVALID;
@@ -336,7 +340,7 @@ k_raster(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const s
     if (tid == 0) {
         zmin = 1e9f; zmax = -1e9f;
         for (int w = 0; w < TILE_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
-        zrange[tile] = make_float2(zmin, zmax);
+        A.zrange[gtile] = make_float2(zmin, zmax);
     }
 }
 
@@ -348,21 +352,27 @@ k_raster(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const s
  * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
 template <int S>
 __global__ void __launch_bounds__(TILE_THREADS)
-k_resolve(const sftg_frame* __restrict__ F, const float* __restrict__ ss, const sftg_clip_tri* __restrict__ clips,
-          const float2* __restrict__ vis_all, const float2* __restrict__ zrange, const uint8_t* __restrict__ light_vis,
-          uint32_t* __restrict__ color, float* __restrict__ shadow_out)
+k_resolve(const sftg_tile_args A, uint32_t tile0)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
     __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
     __shared__ int s_nlights;
     __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
 
-    const int tile = blockIdx.x / RESOLVE_SPLIT, part = blockIdx.x % RESOLVE_SPLIT;
+    const uint32_t gtile = tile0 + blockIdx.x / RESOLVE_SPLIT;              /* batch-wide tile index */
+    const int part = blockIdx.x % RESOLVE_SPLIT;
+    const sftg_frame* F = A.frames + A.tile_view[gtile];
+    const int tile = (int)(gtile - F->tile_base);
+    const float* ss = A.ss + (size_t)F->ss_base * 576;
+    const sftg_clip_tri* clips = A.clips + (F->total_ss ? A.clip_base[(size_t)F->ss_base * 16] : 0u);
+    const uint8_t* light_vis = A.light_vis + (size_t)F->prox_base * 64;
+    uint32_t* color = F->color_dev;
+    float* shadow_out = A.shadow_out;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
-    const float2 zr = zrange[tile];
+    const float2 zr = A.zrange[gtile];
     const float zmin = zr.x, zmax = zr.y;
-    const float2* vis = vis_all + (size_t)tile * S * SFTG_TILE_PX;
+    const float2* vis = A.vis + F->vis_base + (size_t)tile * S * SFTG_TILE_PX;
 
     /* D2: tile light list, first 16 lights in index order that pass (5855-5934) */
     if (warp == 0) {
@@ -731,17 +741,18 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
     return e;
 }
 
-void sftg_launch_tile(int S, int tiles, cudaStream_t st, const sftg_frame* F, const float* ss, const sftg_clip_tri* clips,
-                      const uint32_t* tile_start, const uint32_t* tile_count, const uint64_t* tile_pay, const uint8_t* light_vis,
-                      float2* vis, float2* zrange, uint32_t* color, float* vis_depth, uint32_t* vis_id, float* shadow_out,
-                      cudaEvent_t between) {
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
+    if (!tiles) return;
     const size_t sm = raster_smem(S);
-    if (S == 1) k_raster<1><<<tiles, TILE_THREADS, sm, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, vis, zrange, vis_depth, vis_id);
-    else if (S == 2) k_raster<2><<<tiles, TILE_THREADS, sm, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, vis, zrange, vis_depth, vis_id);
-    else k_raster<4><<<tiles, TILE_THREADS, sm, st>>>(F, ss, clips, tile_start, tile_count, tile_pay, vis, zrange, vis_depth, vis_id);
-    if (between) cudaEventRecord(between, st);
-    const int grid = tiles * RESOLVE_SPLIT;
-    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(F, ss, clips, vis, zrange, light_vis, color, shadow_out);
-    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(F, ss, clips, vis, zrange, light_vis, color, shadow_out);
-    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(F, ss, clips, vis, zrange, light_vis, color, shadow_out);
+    if (S == 1) k_raster<1><<<tiles, TILE_THREADS, sm, st>>>(A, tile0);
+    else if (S == 2) k_raster<2><<<tiles, TILE_THREADS, sm, st>>>(A, tile0);
+    else k_raster<4><<<tiles, TILE_THREADS, sm, st>>>(A, tile0);
+}
+
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
+    if (!tiles) return;
+    const uint32_t grid = tiles * RESOLVE_SPLIT;
+    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(A, tile0);
+    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(A, tile0);
+    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(A, tile0);
 }

@@ -83,8 +83,9 @@ typedef struct sftg_inst {
 typedef struct sftg_job {   /* up to 8 consecutive meshlets of one mesh, sft_geom_job (sofren2.c:1264) */
     uint32_t inst;
     uint32_t first;        /* model-relative meshlet index */
-    uint32_t count;        /* 1..8 */
-    uint32_t skinned;      /* mesh has skin and the instance has bones */
+    uint16_t count;        /* 1..8 */
+    uint16_t skinned;      /* mesh has skin and the instance has bones */
+    uint32_t view;         /* view of the batch this job belongs to */
 } sftg_job;
 
 typedef struct sftg_point_light {
@@ -120,6 +121,12 @@ typedef struct sftg_frame {
     uint32_t n_point, n_dir, n_proxies, n_inst;
     uint32_t total_ss, n_jobs, tlas_root, tlas_count;
     uint32_t clip_cap, tile_cap, pad3[2];        /* capacities of the clip pool and tile payload buffer */
+    /* where this view's rows start in the batch-wide arrays (all 0 for a single frame) */
+    uint32_t view, ss_base;        /* screen-space cache slot; batch records start at ss_base * 16 */
+    uint32_t tile_base, prox_base; /* global tile index; global proxy index (light_vis rows) */
+    uint32_t packet_base, n_packets;
+    uint64_t vis_base;             /* float2 offset of this view's visibility buffer */
+    uint32_t* color_dev;           /* this view's colour buffer, width * height */
     /* per-frame arrays */
     const sftg_inst* inst;
     const float* bones;            /* 16 floats per matrix */

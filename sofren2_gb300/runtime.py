@@ -47,6 +47,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftx_scene_frame_count": (u32, [p]), "sftx_scene_render": (i32, [p, u32, p, i32]),
         "sftx_scene_frame_size": (u32, [p, u32, p, p]), "sft_get_launch_count": (i32, []),
         "sft_get_cuda_stream": (p, []),
+        "sftx_scene_render_batch": (i32, [p, p, p, u32, p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -129,6 +130,36 @@ class Renderer:
         if rc != 0:
             raise RuntimeError("render failed: " + (err or b"").decode())
         return color
+
+    def render_batch(self, views: list[tuple], colors: list[np.ndarray | None] | None = None) -> list[np.ndarray | None]:
+        """Renders views [(scene handle, frame, samples), ...] in one batched submission.
+
+        colors: None (every colour stays on the device) or one array (or None) per view; a
+        missing array is allocated.  Returns the per-view colour arrays (None for device-only)."""
+        n = len(views)
+        hs = (C.c_void_p * n)(*[h for h, _, _ in views])
+        fr = np.array([f for _, f, _ in views], np.uint32)
+        sm = np.array([s for _, _, s in views], np.int32)
+        out: list[np.ndarray | None] = [None] * n
+        cp = None
+        pitch = None
+        if colors is not None:
+            ptrs = (C.c_void_p * n)()
+            pitch = np.zeros(n, np.int32)
+            for i, (h, f, _) in enumerate(views):
+                c = colors[i]
+                if c is None:
+                    w, hh = self.frame_size(h, f)
+                    c = np.zeros((hh, w), np.uint32)
+                out[i] = c
+                ptrs[i] = c.ctypes.data
+                pitch[i] = c.strides[0]
+            cp = ptrs
+        rc = self.lib.sftx_scene_render_batch(hs, _ptr(fr), _ptr(sm), n, cp, _ptr(pitch))
+        self.lib.sft_set_msaa_samples(self.samples)
+        if rc != 0:
+            raise RuntimeError("batch render failed: " + (self.lib.sft_get_last_error() or b"").decode())
+        return out
 
     def render_debug(self, h, frame: int, total_ss: int, n_proxies: int, payload_cap: int = 1 << 22,
                      clip_cap: int = 1 << 16) -> dict:
