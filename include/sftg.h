@@ -137,6 +137,22 @@ int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* frame, const 
 int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, uint32_t* const* colors,
                        const int32_t* pitch_bytes, const uint32_t** out_device_colors);
 
+/* Light visibility of a frame's shadow proxies (the occlusion pass of sft_present,
+ * sofren2.c:8163-8280) computed without allocating anything: no cudaMalloc / cudaFree, no
+ * growth of the context's arena or pinned staging, no host heap.  For callers that must not
+ * allocate while they run (a serving loop whose device-memory budget is already committed,
+ * per-frame code on a latency deadline).  Scratch is a static device array of
+ * SFTG_NOALLOC_SCRATCH_BYTES; a frame needing more (many proxies x lights x instances) is
+ * rejected with SFTG_E_LIMIT before any device work.  light_vis (host, n_proxies * 64 bytes)
+ * receives 3 - rays blocked per (proxy, light), 0 in columns past the light count: the rows
+ * sftg_frame_render computes for the same frame.  The models must be on the device already
+ * (a render since the last model upload).  The first call per device looks up the scratch
+ * address: make it outside any stream capture.  The scratch is shared by all contexts on a
+ * device, so overlapping calls race: serialise them.  No counterpart in the reference, whose
+ * CPU frame always has its arenas. */
+#define SFTG_NOALLOC_SCRATCH_BYTES (4u << 20)
+int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* frame, uint8_t* light_vis);
+
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */

@@ -208,6 +208,10 @@ SFT_FUNC void* sft_get_cuda_stream(void);
  * sft_present would have produced alone.  Returns 0 or a negative sftg error code. */
 SFT_FUNC void sft_batch_begin(void);
 SFT_FUNC i32 sft_batch_submit(void);
+/* extension: the i-th frame recorded since sft_batch_begin (a struct sftg_frame_desc, valid until
+ * sft_batch_submit), and the sftg context the runtime renders with, for direct sftg_* calls */
+SFT_FUNC const void* sft_batch_peek(u32 i);
+SFT_FUNC void* sft_get_gpu_context(void);
 
 #ifdef __cplusplus
 }
@@ -905,6 +909,9 @@ SFT_FUNC void sft_batch_begin(void) {
     s->n_batch = 0;
     s->batching = 1;
 }
+
+SFT_FUNC const void* sft_batch_peek(u32 i) { return sft__s && i < sft__s->n_batch ? (const void*)&sft__s->batch_fd[i] : NULL; }
+SFT_FUNC void* sft_get_gpu_context(void) { return sft__s ? (void*)sft__s->gpu : NULL; }
 
 SFT_FUNC i32 sft_batch_submit(void) {
     struct sft__state* s = sft__s;

@@ -653,3 +653,106 @@ extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {
 extern "C" int sftg_last_launch_count(const sftg_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 extern "C" void* sftg_stream(const sftg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+/* ------------------------------------------------------------------ allocation-free light visibility
+ *
+ * sftg_light_vis_noalloc runs the proxy-occlusion pass (sft_present's light visibility,
+ * sofren2.c:8163-8280) without touching any allocator.  It is for callers that must not
+ * allocate while they run: a serving loop whose admission control has already committed the
+ * device-memory budget (a cudaMalloc there can fail, or take memory promised to a resident
+ * scene), and per-frame code on a latency deadline (cudaMalloc / cudaFree can synchronise the
+ * whole device).  The context's frame arena and pinned staging may need to grow and so are
+ * not used; all scratch lives in one file-scope device array of SFTG_NOALLOC_SCRATCH_BYTES
+ * whose address is looked up once per device.
+ *
+ * Scratch layout (each part 256-byte aligned): frame block, instances, point lights (first 64),
+ * proxies, TLAS nodes, shadow packets, (packet, instance) pairs, pair counter, status word,
+ * light_vis rows, packet -> view and proxy -> view maps.  What must start at zero, and is
+ * cleared by this call with cudaMemsetAsync: the pair counter, the status word, the light_vis
+ * rows (columns at or beyond the light count are never written) and both maps (one view).
+ *
+ * The scratch is shared by every context on the device: two calls that overlap in time, from
+ * any threads or contexts, race on it.  Callers serialise them. */
+#define SFTG_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SFTG_NOALLOC_SCRATCH_BYTES];
+static void* g_noalloc_addr[SFTG_NOALLOC_MAX_DEVICES];
+
+extern "C" int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* fd, uint8_t* light_vis) {
+    if (!ctx || !fd) return SFTG_E_ARG;
+    if (ctx->device < 0 || ctx->device >= SFTG_NOALLOC_MAX_DEVICES) return set_err(ctx, SFTG_E_ARG, "device %d out of range", ctx->device);
+    if (fd->n_proxies && !light_vis) return set_err(ctx, SFTG_E_ARG, "light_vis output is NULL");
+    if (fd->n_instances > SFTG_MAX_INSTANCES) return set_err(ctx, SFTG_E_LIMIT, "more than %d instances in one frame", SFTG_MAX_INSTANCES);
+    if (ctx->tables_dirty)   /* copying the model table may have to grow its device pool */
+        return set_err(ctx, SFTG_E_ARG, "models changed since the last render: render one frame first");
+    for (uint32_t i = 0; i < fd->n_instances; i++)
+        if (fd->instances[i].model < 0 || (size_t)fd->instances[i].model >= ctx->h_models.size())
+            return set_err(ctx, SFTG_E_ARG, "instance %u: bad model", i);
+    const uint32_t np = fd->n_proxies, lc = fd->n_point < 64 ? fd->n_point : 64, nbatch = (np + 7) / 8;
+    const uint32_t n_packets = (fd->shadows && lc && np) ? lc * nbatch * 3 : 0;
+    const uint64_t max_pairs = (uint64_t)n_packets * (fd->n_instances ? fd->n_instances : 1);
+    size_t off = 0;
+    auto take = [&](uint64_t bytes) { off = (off + 255) & ~(size_t)255; const size_t r = off; off += (size_t)bytes; return r; };
+    const size_t o_F = take(sizeof(sftg_frame)), o_inst = take((uint64_t)(fd->n_instances + 1) * sizeof(sftg_inst));
+    const size_t o_pl = take((uint64_t)lc * sizeof(sftg_point_light)), o_px = take((uint64_t)np * sizeof(sftg_proxy));
+    const size_t o_tl = take((uint64_t)fd->tlas_count * 256), o_pk = take((uint64_t)n_packets * sftg_packet_bytes());
+    const size_t o_pr = take(max_pairs * 8 + 8), o_np = take(16), o_st = take(16), o_lv = take((uint64_t)np * 64);
+    const size_t o_pv = take((uint64_t)n_packets * 2), o_xv = take((uint64_t)np * 2);
+    if (off > SFTG_NOALLOC_SCRATCH_BYTES)
+        return set_err(ctx, SFTG_E_LIMIT, "frame needs %zu bytes of occlusion scratch; the static scratch holds %u (%u proxies, %u lights, %u instances)",
+                       off, (unsigned)SFTG_NOALLOC_SCRATCH_BYTES, np, fd->n_point, fd->n_instances);
+    if (!np) return SFTG_OK;
+    CK(cudaSetDevice(ctx->device));
+    if (!g_noalloc_addr[ctx->device]) {   /* once per device; make this first call outside any stream capture */
+        void* a = nullptr;
+        CK(cudaGetSymbolAddress(&a, g_noalloc_scratch));
+        g_noalloc_addr[ctx->device] = a;
+    }
+    char* d = (char*)g_noalloc_addr[ctx->device];
+    cudaStream_t st = ctx->stream;
+    sftg_frame F;
+    memset(&F, 0, sizeof(F));
+    F.width = fd->width; F.height = fd->height; F.samples = fd->samples; F.shadows = fd->shadows;
+    F.n_point = lc; F.n_proxies = np; F.n_inst = fd->n_instances;
+    F.tlas_root = fd->tlas_root; F.tlas_count = fd->tlas_count;
+    F.n_packets = n_packets;
+    F.inst = (const sftg_inst*)(d + o_inst);
+    F.point = (const sftg_point_light*)(d + o_pl);
+    F.proxies = (const sftg_proxy*)(d + o_px);
+    F.tlas = (const sftg_bvh_node*)(d + o_tl);
+    F.models = (const sftg_model*)ctx->models.ptr;
+    F.ml_attr = (const float*)ctx->ml_attr.ptr;
+    F.ml_inds = (const uint8_t*)ctx->ml_inds.ptr;
+    F.ml_info = (const sftg_meshlet_info*)ctx->ml_info.ptr;
+    F.blas = (const sftg_bvh_node*)ctx->blas.ptr;
+    sftg_inst inst[SFTG_MAX_INSTANCES + 1];
+    memset(inst, 0, sizeof(inst));
+    for (uint32_t i = 0; i < fd->n_instances; i++) {
+        const sftg_instance_desc& id = fd->instances[i];
+        memcpy(inst[i].T, id.transform, 64);
+        inst[i].model = (uint32_t)id.model;
+        inst[i].bones = -1;
+        inst[i].meshlet_base = ctx->h_models[id.model].meshlet_base;
+    }
+    /* pageable sources: each copy returns once its source has been read */
+    CK(cudaMemcpyAsync(d + o_F, &F, sizeof(F), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d + o_inst, inst, (size_t)(fd->n_instances + 1) * sizeof(sftg_inst), cudaMemcpyHostToDevice, st));
+    if (lc) CK(cudaMemcpyAsync(d + o_pl, fd->point_lights, (size_t)lc * 32, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d + o_px, fd->proxies, (size_t)np * 32, cudaMemcpyHostToDevice, st));
+    if (fd->tlas_count) CK(cudaMemcpyAsync(d + o_tl, fd->tlas_nodes, (size_t)fd->tlas_count * 256, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(d + o_st, 0, 16, st));
+    CK(cudaMemsetAsync(d + o_lv, 0, (size_t)np * 64, st));
+    if (n_packets) {
+        CK(cudaMemsetAsync(d + o_pv, 0, (size_t)n_packets * 2, st));
+        CK(cudaMemsetAsync(d + o_xv, 0, (size_t)np * 2, st));
+        sftg_launch_occlusion((const sftg_frame*)(d + o_F), (const uint16_t*)(d + o_pv), n_packets, (const uint16_t*)(d + o_xv), np,
+                              fd->n_instances, d + o_pk, (uint2*)(d + o_pr), (uint32_t*)(d + o_np), (uint32_t)max_pairs,
+                              (uint8_t*)(d + o_lv), (uint32_t*)(d + o_st), st);
+        CK(cudaGetLastError());
+    }
+    uint32_t status = 0;
+    CK(cudaMemcpyAsync(light_vis, d + o_lv, (size_t)np * 64, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&status, d + o_st, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (status & 1u) return set_err(ctx, SFTG_E_DEVICE_STATUS, "occlusion traversal exceeded its stack bound");
+    return SFTG_OK;
+}
