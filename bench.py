@@ -139,7 +139,9 @@ def run_ours(args, cfg) -> dict:
     def e2e_step():
         R.render(h, 0, color)
 
-    def timed(step, n):
+    def timed(step, n, kern=None):
+        """n steps, each bracketed by CUDA events on the renderer's stream; kern (optional)
+        accumulates the library's per-phase event timings of every timed step."""
         times = []
         for _ in range(n):
             flush.fill_(1.0)
@@ -150,6 +152,8 @@ def run_ours(args, cfg) -> dict:
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
+            if kern is not None:
+                kern += R.timings()
         return times
 
     for _ in range(args.warmup):
@@ -164,13 +168,10 @@ def run_ours(args, cfg) -> dict:
     clocks = ClockSampler(local)
     clocks.start()
     t0 = time.perf_counter()
-    dev_times = timed(device_step, args.steps)
-    launches = R.launch_count() * args.steps
     kern = np.zeros(5)
-    for _ in range(3):
-        device_step()
-        kern += R.timings()
-    kern /= 3
+    dev_times = timed(device_step, args.steps, kern)
+    launches = R.launch_count() * args.steps
+    kern /= args.steps
     e2e_times = timed(e2e_step, args.steps)
     wall = time.perf_counter() - t0
     clk = clocks.stop()

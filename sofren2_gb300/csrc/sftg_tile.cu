@@ -24,8 +24,11 @@
 #include "sftg_lane.cuh"
 #include "sftg_kernels.h"
 
-#define TILE_THREADS 256
-#define SETUP_CAP 256
+#define TILE_THREADS 256          /* resolve CTA */
+#define RASTER_THREADS 512        /* raster CTA: 64 groups of 8 */
+#define SETUP_CAP RASTER_THREADS  /* triangle set-ups per round: 64 payloads x 8 lanes */
+#define SLAB_ROWS 8               /* rows of one raster work item */
+#define ITEM_CAP (SETUP_CAP * (SFTG_TILE / SLAB_ROWS))
 
 struct tri_setup {
     float A[3], B[3], se[3];
@@ -85,6 +88,42 @@ SFTG_D void fetch_tri(const sftg_frame* F, const float* ss, const sftg_clip_tri*
     t.inst = ii; t.m = m;
 }
 
+/* Grows [mn, mx] by the world positions the resolve can interpolate on triangle `vid`.
+ * Interpolated positions are convex combinations of the three world vertices, up to the
+ * rounding of the barycentrics: at 1x they are not clamped, and a pixel centre inside a sliver
+ * can get a weight of about -eps * extent^2 / det.  The box is widened by twice that bound
+ * times the triangle's extent, plus a relative margin for the interpolation's own rounding. */
+SFTG_D void tri_bounds_acc(const sftg_frame* F, const float* ss, const sftg_clip_tri* clips, uint32_t vid, float* mn, float* mx) {
+    float X[3][3], sx[3], sy[3];
+    if (vid & 0x80000000u) {
+        const sftg_clip_tri* c = &clips[vid & 0x7FFFFFFFu];
+#pragma unroll
+        for (int k = 0; k < 3; k++) { X[0][k] = c->px[k]; X[1][k] = c->py[k]; X[2][k] = c->pz[k]; sx[k] = c->sx[k]; sy[k] = c->sy[k]; }
+    } else {
+        const uint32_t ii = (vid >> 25) & 63, m = (vid >> 7) & 0x3FFFF, tri = vid & 127;
+        const sftg_inst* I = &F->inst[ii];
+        const uint32_t g = I->meshlet_base + m;
+        const uint8_t* ind = F->ml_inds + (size_t)g * 512;
+        const float* Sc = ss + (size_t)(I->ss_offset + m) * 576;
+        const uint32_t b = tri >> 3, l = tri & 7;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint32_t v = ind[b * 32 + 8 * k + l];
+            X[0][k] = Sc[192 + v]; X[1][k] = Sc[256 + v]; X[2][k] = Sc[320 + v]; sx[k] = Sc[v]; sy[k] = Sc[64 + v];
+        }
+    }
+    const float dx1 = sx[1] - sx[0], dx2 = sx[2] - sx[0], dy1 = sy[1] - sy[0], dy2 = sy[2] - sy[0];
+    const float det = fabsf(dx1 * dy2 - dx2 * dy1);
+    const float ext = fmaxf(fmaxf(fabsf(dx1), fabsf(dx2)), fmaxf(fabsf(dy1), fabsf(dy2))) + 2.f;
+    const float delta = fminf(1e-5f + 4e-6f * (ext * ext) / fmaxf(det, 1e-30f), 1e6f);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float lo = fminf(X[a][0], fminf(X[a][1], X[a][2])), hi = fmaxf(X[a][0], fmaxf(X[a][1], X[a][2]));
+        const float e = (hi - lo) * (2.f * delta) + 1e-4f * (fabsf(lo) + fabsf(hi)) + 1e-5f;
+        mn[a] = fminf(mn[a], lo - e); mx[a] = fmaxf(mx[a], hi + e);
+    }
+}
+
 /* edge / depth setup of one triangle lane (5211-5311), false when culled or off-tile */
 template <int S>
 SFTG_D bool tri_setup_one(float sx0, float sy0, float iw0, float sx1, float sy1, float iw1, float sx2, float sy2, float iw2,
@@ -133,7 +172,7 @@ SFTG_D bool tri_setup_one(float sx0, float sy0, float iw0, float sx1, float sy1,
 
 /* the incremental edge walk for pixel column `l` of one triangle (5345-5497) */
 template <int S>
-SFTG_D void tri_raster(const tri_setup& T, int l, uint32_t gmask, int tmx, int tmy, unsigned long long* keys) {
+SFTG_D void tri_raster(const tri_setup& T, int y0, int y1, int l, uint32_t gmask, int tmx, int tmy, unsigned long long* keys) {
     float de0[S], de1[S], de2[S], dz[S];
 #pragma unroll
     for (int s = 0; s < S; s++) {
@@ -144,10 +183,13 @@ SFTG_D void tri_raster(const tri_setup& T, int l, uint32_t gmask, int tmx, int t
     const float fl = (float)l;
     float e0r = T.se[0] + T.A[0] * fl, e1r = T.se[1] + T.A[1] * fl, e2r = T.se[2] + T.A[2] * fl;
     float zr = T.sz + T.dzdx * fl;
+    /* a slab starting below miny replays the per-row adds it skips, so every row start is the
+     * same float the reference's sequential walk reaches */
+    for (int y = T.miny; y < y0; y++) { e0r = e0r + T.B[0]; e1r = e1r + T.B[1]; e2r = e2r + T.B[2]; zr = zr + T.dzdy; }
     const float a0c = T.A[0] * 8.f, a1c = T.A[1] * 8.f, a2c = T.A[2] * 8.f, zc = T.dzdx * 8.f;
     const float np0 = -T.pad[0], np1 = -T.pad[1], np2 = -T.pad[2];
     const uint32_t order = T.order;
-    for (int y = T.miny; y <= T.maxy; y++) {
+    for (int y = y0; y <= y1; y++) {
         float e0 = e0r, e1 = e1r, e2 = e2r, z = zr;
         int pi = (y - tmy) * SFTG_TILE + (T.ax0 - tmx) + l;
         for (int x = T.ax0; x < T.ax1; x += 8, pi += 8) {
@@ -236,14 +278,15 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
  * tile's depth range over valid samples (sofren2.c:5820-5853), which the resolve needs for its
  * light culling. */
 template <int S>
-__global__ void __launch_bounds__(TILE_THREADS)
+__global__ void __launch_bounds__(RASTER_THREADS)
 k_raster(const sftg_tile_args A, uint32_t tile0)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
     tri_setup* setups = (tri_setup*)(smem + (size_t)S * SFTG_TILE_PX * 8);
-    __shared__ uint32_t s_nsetup, s_next;
-    __shared__ float s_red[2][TILE_THREADS / 32];
+    uint32_t* items = (uint32_t*)(setups + SETUP_CAP);                     /* set-up index << 8 | slab */
+    __shared__ uint32_t s_nsetup, s_nitems, s_next;
+    __shared__ float s_red[2][RASTER_THREADS / 32];
     const uint32_t gtile = tile0 + blockIdx.x;                             /* batch-wide tile index */
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
@@ -257,11 +300,11 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
     float* vis_depth = A.vis_depth;
     uint32_t* vis_id = A.vis_id;
 
-    for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) keys[i] = 0ull;
+    for (int i = tid; i < S * SFTG_TILE_PX; i += RASTER_THREADS) keys[i] = 0ull;
     const int grp_lane = tid & 7;
     const uint32_t gmask = 0xFFu << (lane & ~7);
     for (uint32_t pbase = 0; pbase < count; pbase += SETUP_CAP / 8) {
-        if (tid == 0) { s_nsetup = 0; s_next = 0; }
+        if (tid == 0) { s_nsetup = 0; s_nitems = 0; s_next = 0; }
         __syncthreads();
         {
             const uint32_t p = pbase + (tid >> 3);
@@ -296,19 +339,25 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
                     if (tri_setup_one<S>(sx[0], sy[0], iw[0], sx[1], sy[1], iw[1], sx[2], sy[2], iw[2], tmx, tmy, p * 8 + l, T)) {
                         const uint32_t slot = atomicAdd(&s_nsetup, 1u);
                         setups[slot] = T;
+                        const uint32_t nslab = (uint32_t)(T.maxy - T.miny) / SLAB_ROWS + 1u;
+                        const uint32_t ib = atomicAdd(&s_nitems, nslab);
+                        for (uint32_t k = 0; k < nslab; k++) items[ib + k] = (slot << 8) | k;
                     }
                 }
             }
         }
         __syncthreads();
-        const uint32_t nset = s_nsetup;
+        const uint32_t nitem = s_nitems;
         while (true) {
             uint32_t idx = 0;
             if (grp_lane == 0) idx = atomicAdd(&s_next, 1u);
             idx = __shfl_sync(gmask, idx, lane & ~7);
-            if (idx >= nset) break;
-            const tri_setup T = setups[idx];
-            tri_raster<S>(T, grp_lane, gmask, tmx, tmy, keys);
+            if (idx >= nitem) break;
+            const uint32_t it = items[idx];
+            const tri_setup T = setups[it >> 8];
+            const int y0 = T.miny + (int)(it & 0xFFu) * SLAB_ROWS;
+            const int y1 = min(y0 + SLAB_ROWS - 1, T.maxy);
+            tri_raster<S>(T, y0, y1, grp_lane, gmask, tmx, tmy, keys);
         }
         __syncthreads();
     }
@@ -316,7 +365,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
     /* decode, store, depth range */
     float zmin = 1e9f, zmax = -1e9f;
     float2* tv = A.vis + F->vis_base + (size_t)tile * S * SFTG_TILE_PX;
-    for (int i = tid; i < S * SFTG_TILE_PX; i += TILE_THREADS) {
+    for (int i = tid; i < S * SFTG_TILE_PX; i += RASTER_THREADS) {
         const unsigned long long k = keys[i];
         float d = 0.f; uint32_t vid = SFTG_INVALID;
         if (k) {
@@ -339,7 +388,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
     __syncthreads();
     if (tid == 0) {
         zmin = 1e9f; zmax = -1e9f;
-        for (int w = 0; w < TILE_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
+        for (int w = 0; w < RASTER_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
         A.zrange[gtile] = make_float2(zmin, zmax);
     }
 }
@@ -416,6 +465,36 @@ k_resolve(const sftg_tile_args A, uint32_t tile0)
     __syncthreads();
     const int ntl = s_nlights;
 
+    /* World bounds of every triangle visible in this quarter tile, for the proxy filter below. */
+    __shared__ float s_bnd[TILE_THREADS / 32][6];
+    const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
+    const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
+    const bool cull_proxies = F->shadows && F->n_proxies > 0 && ntl > 0;
+    if (cull_proxies) {
+        float mn[3] = { 1e30f, 1e30f, 1e30f }, mx[3] = { -1e30f, -1e30f, -1e30f };
+        uint32_t last = SFTG_INVALID;
+        const int ix0 = tid & 3, iy0 = (tid >> 2) & 1;
+        for (int b = tid >> 3; b < RESOLVE_BLOCKS; b += TILE_THREADS / 8) {
+            const int blk = part * RESOLVE_BLOCKS + b;
+            const int gx = tmx + (blk & 15) * 4 + ix0, gy = tmy + (blk >> 4) * 2 + iy0;
+            if (gx >= lim_x || gy >= lim_y) continue;
+            const int pind = (gy - tmy) * SFTG_TILE + (gx - tmx);
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                const uint32_t vid = __float_as_uint(vis[s * SFTG_TILE_PX + pind].y);
+                if (vid != SFTG_INVALID && vid != last) { last = vid; tri_bounds_acc(F, ss, clips, vid, mn, mx); }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                mn[a] = fminf(mn[a], __shfl_xor_sync(0xFFFFFFFFu, mn[a], o));
+                mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], o));
+            }
+        if (lane == 0) { s_bnd[warp][0] = mn[0]; s_bnd[warp][1] = mn[1]; s_bnd[warp][2] = mn[2]; s_bnd[warp][3] = mx[0]; s_bnd[warp][4] = mx[1]; s_bnd[warp][5] = mx[2]; }
+    }
+
     /* D3: per light, the first 16 proxies that see it and can reach it (5936-5990) */
     for (int i = warp; i < SFTG_MAX_TILE_LIGHTS; i += TILE_THREADS / 32) {
         int n = 0;
@@ -458,10 +537,53 @@ k_resolve(const sftg_tile_args A, uint32_t tile0)
     }
     __syncthreads();
 
+    /* Conservative filter of the cached proxies (order kept).  Every pixel this CTA shades lies
+     * in the ball (Bc, Br) around the bounds above.  The per-block skip (6520-6540) drops a
+     * proxy unless some lane's segment pixel -> light passes within the proxy's bounding radius
+     * of its centre; for pixels in the ball that segment stays within Br of the segment
+     * Bc -> light.  So a proxy farther than rb + Br (+ a rounding margin) from that segment is
+     * skipped by every block, and removing it here leaves every pixel unchanged. */
+    if (cull_proxies) {
+        float mn[3], mx[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) { mn[a] = s_bnd[0][a]; mx[a] = s_bnd[0][3 + a]; }
+        for (int w = 1; w < TILE_THREADS / 32; w++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) { mn[a] = fminf(mn[a], s_bnd[w][a]); mx[a] = fmaxf(mx[a], s_bnd[w][3 + a]); }
+        const bool empty = !(mn[0] <= mx[0] && mn[1] <= mx[1] && mn[2] <= mx[2]);
+        const v3 bc = mk3((mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f);
+        const v3 he = mk3((mx[0] - mn[0]) * 0.5f, (mx[1] - mn[1]) * 0.5f, (mx[2] - mn[2]) * 0.5f);
+        const float br = sqrtf(he.x * he.x + he.y * he.y + he.z * he.z);
+        const bool usable = isfinite(br) && isfinite(bc.x) && isfinite(bc.y) && isfinite(bc.z);
+        for (int i = warp; i < ntl; i += TILE_THREADS / 32) {
+            const int n = s_npc[i];
+            if (n == 0 || (usable == false && !empty)) continue;
+            const sftg_point_light L = F->point[s_lights[i]];
+            bool keep = false;
+            proxy_cache q;
+            if (lane < n) {
+                q = pcache[i * SFTG_MAX_LIGHT_PROXIES + lane];
+                if (!empty) {
+                    const v3 Wv = mk3(q.W[0], q.W[1], q.W[2]);
+                    const v3 D = mk3(bc.x - L.pos[0], bc.y - L.pos[1], bc.z - L.pos[2]);
+                    const float dd = D.x * D.x + D.y * D.y + D.z * D.z;
+                    const float t = dd > 0.f ? fminf(fmaxf((Wv.x * D.x + Wv.y * D.y + Wv.z * D.z) / dd, 0.f), 1.f) : 0.f;
+                    const v3 E = mk3(Wv.x - t * D.x, Wv.y - t * D.y, Wv.z - t * D.z);
+                    const float dist = sqrtf(E.x * E.x + E.y * E.y + E.z * E.z);
+                    const float m = 2e-3f * (sqrtf(q.wdw) + sqrtf(dd) + br) + 1e-3f;
+                    keep = !(dist > sqrtf(q.rb2) + br + m);
+                }
+            }
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
+            __syncwarp();
+            if (keep) pcache[i * SFTG_MAX_LIGHT_PROXIES + __popc(bal & ((1u << lane) - 1u))] = q;
+            if (lane == 0) s_npc[i] = (uint8_t)__popc(bal);
+        }
+        __syncthreads();
+    }
+
     /* ---------------- resolve: one 8-thread group per 4x2 block ---------------- */
     const int W = F->width;
-    const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
-    const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
     const int grp = tid >> 3, gl = tid & 7, gshift = lane & ~7;
     const uint32_t gmask = 0xFFu << gshift;
     const int ix = gl & 3, iy = gl >> 2;
@@ -726,7 +848,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0)
 }
 
 /* ---------------------------------------------------------------- host-side launch helpers */
-static size_t raster_smem(int S) { return (size_t)S * SFTG_TILE_PX * 8 + (size_t)SETUP_CAP * sizeof(tri_setup); }
+static size_t raster_smem(int S) { return (size_t)S * SFTG_TILE_PX * 8 + (size_t)SETUP_CAP * sizeof(tri_setup) + (size_t)ITEM_CAP * 4; }
 
 cudaError_t sftg_tile_configure(int max_dynamic_smem) {
     cudaError_t e = cudaSuccess;
@@ -744,9 +866,9 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
     const size_t sm = raster_smem(S);
-    if (S == 1) k_raster<1><<<tiles, TILE_THREADS, sm, st>>>(A, tile0);
-    else if (S == 2) k_raster<2><<<tiles, TILE_THREADS, sm, st>>>(A, tile0);
-    else k_raster<4><<<tiles, TILE_THREADS, sm, st>>>(A, tile0);
+    if (S == 1) k_raster<1><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0);
+    else if (S == 2) k_raster<2><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0);
+    else k_raster<4><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0);
 }
 
 void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
