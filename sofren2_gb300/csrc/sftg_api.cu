@@ -376,7 +376,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
         n_pl += fd->n_point; n_dl += fd->n_dir; n_tl += fd->tlas_count;
         P.color_off = color_total; color_total += (uint64_t)W * H;
     }
-    if (max_pairs > 0xFFFFFFF0ull || total_ss > (1u << 26)) return set_err(ctx, SFTG_E_LIMIT, "batch too large for one submission");
+    if (max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) > 0xFFFFFFF0ull || total_ss > (1u << 26)) return set_err(ctx, SFTG_E_LIMIT, "batch too large for one submission");
     uint32_t total_tiles = 0;
     uint64_t vis_total = 0;
     for (int si = 0; si < 3; si++) {
@@ -416,7 +416,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
     acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(ctx->tile_cap * 8);
     acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
-    acc((max_pairs + 1) * 8); acc(64); acc(((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
+    acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
     acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
     const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
     if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
@@ -452,7 +452,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
     B.light_vis = bp.take<uint8_t>((size_t)total_prox * 64 + 64);
     B.packets = bp.take<char>((size_t)total_packets * sftg_packet_bytes() + 64);
-    B.pairs = bp.take<uint2>((size_t)max_pairs + 1);
+    B.pairs = bp.take<uint2>((size_t)max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1);   /* pairs, then BLAS sub-walk items */
     B.n_pairs = bp.take<uint32_t>(16);
     B.scan_tmp = bp.take<uint32_t>((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
     B.status = bp.take<uint32_t>(16);
@@ -541,7 +541,7 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     if (B.total_packets) {
         sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
                               B.pairs, B.n_pairs, B.max_pairs, B.light_vis, B.status, st);
-        ctx->launches += 3;
+        ctx->launches += 4;
     }
     CK(cudaEventRecord(ctx->ev[1], st));
     if (B.n_jobs) {
@@ -695,7 +695,7 @@ extern "C" int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* fd, 
     const size_t o_F = take(sizeof(sftg_frame)), o_inst = take((uint64_t)(fd->n_instances + 1) * sizeof(sftg_inst));
     const size_t o_pl = take((uint64_t)lc * sizeof(sftg_point_light)), o_px = take((uint64_t)np * sizeof(sftg_proxy));
     const size_t o_tl = take((uint64_t)fd->tlas_count * 256), o_pk = take((uint64_t)n_packets * sftg_packet_bytes());
-    const size_t o_pr = take(max_pairs * 8 + 8), o_np = take(16), o_st = take(16), o_lv = take((uint64_t)np * 64);
+    const size_t o_pr = take(max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) * 8 + 8), o_np = take(16), o_st = take(16), o_lv = take((uint64_t)np * 64);
     const size_t o_pv = take((uint64_t)n_packets * 2), o_xv = take((uint64_t)np * 2);
     if (off > SFTG_NOALLOC_SCRATCH_BYTES)
         return set_err(ctx, SFTG_E_LIMIT, "frame needs %zu bytes of occlusion scratch; the static scratch holds %u (%u proxies, %u lights, %u instances)",

@@ -46,6 +46,9 @@ __global__ void k_scan_reduce(const uint32_t* in, uint32_t n, uint32_t* sums);
 __global__ void k_scan_top(uint32_t* sums, uint32_t nb, uint32_t* total_out);
 __global__ void k_scan_down(const uint32_t* in, uint32_t n, const uint32_t* sums, uint32_t* out);
 size_t sftg_packet_bytes();
+/* BLAS sub-walk items per (packet, instance) pair: the pair buffer holds max_pairs pairs, then
+ * max_pairs * SFTG_OCC_ITEMS_PER_PAIR items; the counter word after n_pairs counts the items */
+#define SFTG_OCC_ITEMS_PER_PAIR 64
 /* packet_view maps a batch-wide shadow packet to its view, prox_view a batch-wide proxy */
 void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view, uint32_t n_packets, const uint16_t* prox_view,
                            uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,

@@ -217,27 +217,28 @@ k_occl_tlas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ 
     }
 }
 
-/* Phase B: one warp per (packet, instance): the packet frustum and rays in model space and the
- * BLAS walk (4137-4238).  Child AABBs are tested one per lane; at a leaf, lanes are
- * (triangle k of 4, ray r of 8) and run the any-hit test (3840-3904).  Hits are OR-ed into the
- * packet, which is what the reference accumulates in any visiting order. */
-__global__ void __launch_bounds__(OCC_WARPS * 32)
-k_occl_blas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, sftg_packet* __restrict__ packets,
-            const uint2* __restrict__ pairs, const uint32_t* __restrict__ n_pairs, uint32_t max_pairs, uint32_t* __restrict__ status)
-{
-    __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t item = blockIdx.x * OCC_WARPS + warp;
-    if (item >= min(*n_pairs, max_pairs)) return;
-    const uint2 pr = pairs[item];
-    const sftg_frame* F = frames + packet_view[pr.x];
-    sftg_packet* P = &packets[pr.x];
-    const uint32_t full = P->active;
-    const frustum6 pf = P->f;
-    const sftg_inst* I = &F->inst[pr.y];
-    const sftg_model Md = F->models[I->model];
-    const float* M = I->T;
+/* Phase B: a warp per (packet, static instance) pair, in two launches.  The packet frustum and
+ * rays are taken into model space, then the BLAS is walked with one child AABB per lane
+ * (4137-4238); at a leaf, lanes are (triangle k of 4, ray r of 8) and run the any-hit test
+ * (3840-3904).  Hits are OR-ed into the packet, which is what the reference accumulates in any
+ * visiting order, so a walk can be split into independent sub-walks: the expand launch walks
+ * the top OCC_EXPAND_DEPTH levels of every pair and turns each deeper node that passes the
+ * frustum test into an item (pair, node); the walk launch runs every item to the bottom.  Both
+ * start from the rays the packet already has blocked, which only skips tests whose outcome is
+ * already recorded. */
+#define OCC_EXPAND_DEPTH 2
+#define OCC_GRID_CTAS (152 * 8)
+
+struct occ_walk {
     frustum6 mf;
+    v3 lo, ld;
+    float tmax;
+    uint32_t full;
+};
+
+SFTG_D void occ_pair_setup(const sftg_inst* I, const sftg_packet* P, int lane, occ_walk& w) {
+    const frustum6 pf = P->f;
+    const float* M = I->T;
     for (int p = 0; p < 6; p++) {
         const float nx = pf.n[p][0], ny = pf.n[p][1], nz = pf.n[p][2], d = pf.d[p];
         const float nmx = nx * M[0] + ny * M[1] + nz * M[2];
@@ -246,9 +247,9 @@ k_occl_blas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ 
         const float dot_t = nx * M[12] + ny * M[13] + nz * M[14];
         const float dm = dot_t + d;
         const float il = fdiv(1.f, fsqrt(nmx * nmx + nmy * nmy + nmz * nmz));
-        mf.n[p][0] = nmx * il; mf.n[p][1] = nmy * il; mf.n[p][2] = nmz * il;
-        mf.d[p] = dm * il;
-        mf.an[p][0] = fabsf(nmx * il); mf.an[p][1] = fabsf(nmy * il); mf.an[p][2] = fabsf(nmz * il);
+        w.mf.n[p][0] = nmx * il; w.mf.n[p][1] = nmy * il; w.mf.n[p][2] = nmz * il;
+        w.mf.d[p] = dm * il;
+        w.mf.an[p][0] = fabsf(nmx * il); w.mf.an[p][1] = fabsf(nmy * il); w.mf.an[p][2] = fabsf(nmz * il);
     }
     /* sft_m_qinv (1693-1712) */
     float im[16];
@@ -257,30 +258,54 @@ k_occl_blas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ 
     im[8] = M[2]; im[9] = M[6]; im[10] = M[10]; im[11] = 0.f;
     for (int a = 0; a < 3; a++) im[12 + a] = -(M[12] * im[a] + M[13] * im[4 + a] + M[14] * im[8 + a]);
     im[15] = 1.f;
-    const int r = lane & 7, kq = lane >> 3;
-    const v3 lo = xform(mk3(P->o[0][r], P->o[1][r], P->o[2][r]), im);
+    const int r = lane & 7;
+    w.lo = xform(mk3(P->o[0][r], P->o[1][r], P->o[2][r]), im);
     const v3 le = xform(mk3(P->e[0][r], P->e[1][r], P->e[2][r]), im);
-    const v3 Lv = sub3(le, lo);
-    const float tmax = fsqrt(vdot(Lv, Lv));
-    const v3 ld = vnorm_fast(Lv);
-    uint32_t sat = 0;
+    const v3 Lv = sub3(le, w.lo);
+    w.tmax = fsqrt(vdot(Lv, Lv));
+    w.ld = vnorm_fast(Lv);
+    w.full = P->active;
+}
+
+/* Walks the BLAS of instance I from `start` (depth `start_depth`).  With EXPAND, a child that
+ * would sit at depth OCC_EXPAND_DEPTH is handed out as an item instead of being pushed (or
+ * pushed after all when the item list is full).  Returns the rays found blocked. */
+template <bool EXPAND>
+SFTG_D uint32_t occ_walk_from(const sftg_frame* F, const sftg_inst* I, const sftg_model& Md, const occ_walk& w, uint32_t sat,
+                              uint32_t start, uint32_t pair, uint32_t* stack, uint2* items, uint32_t* n_items, uint32_t max_items,
+                              uint32_t* status, int lane) {
+    const int r = lane & 7, kq = lane >> 3;
+    const uint32_t full = w.full;
     int top = 1;
-    if (lane == 0) s_stack[warp][0] = Md.blas_root;
+    if (lane == 0) stack[0] = start;      /* entry: node | depth << 29 (depth only tracked when expanding) */
     __syncwarp();
     const sftg_bvh_node* blas = F->blas + Md.blas_base;
     uint32_t guard = 0;
     while (top > 0 && sat != full) {
-        const uint32_t ni = s_stack[warp][--top];
+        const uint32_t ent = stack[--top];
         __syncwarp();
+        const uint32_t ni = ent & 0x1FFFFFFFu, depth = ent >> 29;
         const sftg_bvh_node* nd = &blas[ni];
-        uint32_t m = node_mask(nd, mf, lane);
+        uint32_t m = node_mask(nd, w.mf, lane);
         if (!nd->leaf) {
             while (m) {
                 const int c = __ffs(m) - 1; m &= m - 1;
                 const uint32_t ch = nd->child[c];
                 if (ch == SFTG_INVALID) continue;
-                if (top >= OCC_STACK || ch >= Md.blas_count || ++guard > (1u << 24)) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); top = 0; break; }
-                if (lane == 0) s_stack[warp][top] = ch;
+                if (top >= OCC_STACK || ch >= Md.blas_count || ch >= (1u << 29) || ++guard > (1u << 24)) {
+                    if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW);
+                    return sat;
+                }
+                if (EXPAND && depth + 1 >= OCC_EXPAND_DEPTH) {
+                    uint32_t slot = 0;
+                    if (lane == 0) slot = atomicAdd(n_items, 1u);
+                    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+                    if (slot < max_items) {
+                        if (lane == 0) items[slot] = make_uint2(pair, ch);
+                        continue;
+                    }
+                }
+                if (lane == 0) stack[top] = ch | (EXPAND ? (depth + 1) << 29 : 0u);
                 top++;
                 __syncwarp();
             }
@@ -305,24 +330,74 @@ k_occl_blas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ 
                 const v3 v1 = mk3(at[i1], at[64 + i1], at[128 + i1]);
                 const v3 v2 = mk3(at[i2], at[64 + i2], at[128 + i2]);
                 const v3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
-                const v3 h = cross3(ld, e2);
+                const v3 h = cross3(w.ld, e2);
                 const float a = vdot(e1, h);
                 hit = fabsf(a) > 1e-6f;
                 const float fr = rcpr(a);
-                const v3 s = sub3(lo, v0);
-                const float u = fr * vdot(s, h);
+                const v3 sv = sub3(w.lo, v0);
+                const float u = fr * vdot(sv, h);
                 hit = hit && u >= 0.f && u <= 1.f;
-                const v3 q = cross3(s, e1);
-                const float v = fr * vdot(ld, q);
+                const v3 q = cross3(sv, e1);
+                const float v = fr * vdot(w.ld, q);
                 hit = hit && v >= 0.f && (u + v) <= 1.f;
                 const float tt = fr * vdot(e2, q);
-                hit = hit && tt > 1e-6f && tt < tmax;
+                hit = hit && tt > 1e-6f && tt < w.tmax;
             }
             const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
             sat |= (bal | (bal >> 8) | (bal >> 16) | (bal >> 24)) & 0xFFu;
         }
     }
-    if (lane == 0 && sat) atomicOr(&P->hits, sat);
+    return sat;
+}
+
+SFTG_D uint32_t occ_hits_now(const sftg_packet* P) { return *(volatile const uint32_t*)&P->hits; }
+
+__global__ void __launch_bounds__(OCC_WARPS * 32)
+k_occl_blas_expand(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, sftg_packet* __restrict__ packets,
+                   const uint2* __restrict__ pairs, const uint32_t* __restrict__ n_pairs, uint32_t max_pairs,
+                   uint2* __restrict__ items, uint32_t* __restrict__ n_items, uint32_t max_items, uint32_t* __restrict__ status)
+{
+    __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t np = min(*n_pairs, max_pairs);
+    for (uint32_t item = blockIdx.x * OCC_WARPS + warp; item < np; item += gridDim.x * OCC_WARPS) {
+        const uint2 pr = pairs[item];
+        const sftg_frame* F = frames + packet_view[pr.x];
+        sftg_packet* P = &packets[pr.x];
+        const sftg_inst* I = &F->inst[pr.y];
+        const sftg_model Md = F->models[I->model];
+        occ_walk w;
+        occ_pair_setup(I, P, lane, w);
+        const uint32_t sat = occ_walk_from<true>(F, I, Md, w, occ_hits_now(P) & w.full, Md.blas_root, item, s_stack[warp], items,
+                                                 n_items, max_items, status, lane);
+        if (lane == 0 && sat) atomicOr(&P->hits, sat);
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(OCC_WARPS * 32)
+k_occl_blas_walk(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, sftg_packet* __restrict__ packets,
+                 const uint2* __restrict__ pairs, const uint2* __restrict__ items, const uint32_t* __restrict__ n_items,
+                 uint32_t max_items, uint32_t* __restrict__ status)
+{
+    __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ni = min(*n_items, max_items);
+    for (uint32_t it = blockIdx.x * OCC_WARPS + warp; it < ni; it += gridDim.x * OCC_WARPS) {
+        const uint2 itm = items[it];
+        const uint2 pr = pairs[itm.x];
+        const sftg_frame* F = frames + packet_view[pr.x];
+        sftg_packet* P = &packets[pr.x];
+        const uint32_t known = occ_hits_now(P) & P->active;
+        if (known == P->active) continue;            /* every ray already blocked */
+        const sftg_inst* I = &F->inst[pr.y];
+        const sftg_model Md = F->models[I->model];
+        occ_walk w;
+        occ_pair_setup(I, P, lane, w);
+        const uint32_t sat = occ_walk_from<false>(F, I, Md, w, known, itm.y, 0, s_stack[warp], nullptr, nullptr, 0, status, lane);
+        if (lane == 0 && (sat & ~known)) atomicOr(&P->hits, sat);
+        __syncwarp();
+    }
 }
 
 /* Phase C: light_vis[p][l] = 3 - rays blocked (8169-8276); one thread per (batch-wide proxy,
@@ -348,13 +423,21 @@ size_t sftg_packet_bytes() { return sizeof(sftg_packet); }
 void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view, uint32_t n_packets, const uint16_t* prox_view,
                            uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
                            uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st) {
-    cudaMemsetAsync(n_pairs, 0, 4, st);
+    cudaMemsetAsync(n_pairs, 0, 8, st);   /* pair and item counters */
     if (!n_packets) return;
     k_occl_tlas<<<(n_packets + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, n_packets,
                                                                                    (sftg_packet*)packets, pairs, n_pairs, max_pairs, status);
+    /* the item list shares the pair buffer's tail: pairs take [0, max_pairs), items the rest */
+    uint2* items = pairs + max_pairs;
+    uint32_t* n_items = n_pairs + 1;
+    const uint32_t max_items = max_pairs * SFTG_OCC_ITEMS_PER_PAIR;
     const uint64_t want = (uint64_t)n_packets * (max_inst ? max_inst : 1);
     const uint32_t mp = want < max_pairs ? (uint32_t)want : max_pairs;
-    k_occl_blas<<<(mp + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, (sftg_packet*)packets, pairs,
-                                                                             n_pairs, max_pairs, status);
+    const uint32_t g1 = (mp + OCC_WARPS - 1) / OCC_WARPS;
+    k_occl_blas_expand<<<g1 < OCC_GRID_CTAS ? g1 : OCC_GRID_CTAS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, (sftg_packet*)packets,
+                                                                                         pairs, n_pairs, max_pairs, items, n_items,
+                                                                                         max_items, status);
+    k_occl_blas_walk<<<OCC_GRID_CTAS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, (sftg_packet*)packets, pairs, items, n_items,
+                                                               max_items, status);
     k_occl_finalize<<<(n_proxies * 64 + 255) / 256, 256, 0, st>>>(frames, prox_view, n_proxies, (const sftg_packet*)packets, light_vis);
 }
