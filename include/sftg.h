@@ -153,6 +153,22 @@ int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_
 #define SFTG_NOALLOC_SCRATCH_BYTES (4u << 20)
 int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* frame, uint8_t* light_vis);
 
+/* Scheduling knobs.  None of them changes a result: they set how the same work is cut into
+ * CTAs and warps.  No counterpart in the reference (its SIMD width and tile size are fixed;
+ * the 64x64 tile stays fixed here too, because the per-tile payload lists are part of the
+ * render path's observable output). */
+typedef struct sftg_tuning {
+    int32_t resolve_split[3];     /* resolve CTAs per 64x64 tile at 1x, 2x, 4x: 1, 2, 4 or 8 (default 4) */
+    int32_t raster_slab_rows[3];  /* tile rows per raster work item at 1x, 2x, 4x: 4..64 (default 8) */
+    int32_t geom_job_width;       /* meshlets per geometry warp: 1..8 (default 8, the reference's job) */
+} sftg_tuning;
+int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out);
+int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* tuning);
+/* Times the given views with each candidate setting (median of reps renders per candidate,
+ * coordinate search: job width, then per sample count slab rows and resolve split), keeps the
+ * fastest in the context and copies it to *out (optional). */
+int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, int32_t reps, sftg_tuning* out);
+
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */

@@ -211,6 +211,9 @@ SFT_FUNC i32 sft_batch_submit(void);
 /* extension: the i-th frame recorded since sft_batch_begin (a struct sftg_frame_desc, valid until
  * sft_batch_submit), and the sftg context the runtime renders with, for direct sftg_* calls */
 SFT_FUNC const void* sft_batch_peek(u32 i);
+/* extension: instead of rendering the recorded frames, tune the scheduling knobs on them
+ * (sftg_autotune, reps renders per candidate) and drop them; ends the batch */
+SFT_FUNC i32 sft_batch_autotune(i32 reps);
 SFT_FUNC void* sft_get_gpu_context(void);
 
 #ifdef __cplusplus
@@ -912,6 +915,16 @@ SFT_FUNC void sft_batch_begin(void) {
 
 SFT_FUNC const void* sft_batch_peek(u32 i) { return sft__s && i < sft__s->n_batch ? (const void*)&sft__s->batch_fd[i] : NULL; }
 SFT_FUNC void* sft_get_gpu_context(void) { return sft__s ? (void*)sft__s->gpu : NULL; }
+
+SFT_FUNC i32 sft_batch_autotune(i32 reps) {
+    struct sft__state* s = sft__s;
+    s->batching = 0;
+    const int rc = s->n_batch ? sftg_autotune(s->gpu, s->batch_fd, s->n_batch, reps, NULL) : 0;
+    for (u32 i = 0; i < s->n_batch; i++) free(s->batch_mem[i]);
+    s->n_batch = 0;
+    if (rc) fprintf(stderr, "sofren2-gb300: sft_batch_autotune failed (%d): %s\n", rc, sftg_last_error(s->gpu));
+    return rc;
+}
 
 SFT_FUNC i32 sft_batch_submit(void) {
     struct sft__state* s = sft__s;

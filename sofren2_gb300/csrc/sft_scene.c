@@ -201,6 +201,20 @@ SFTX_EXPORT int sftx_scene_render_batch(void* const* scenes, const uint32_t* fra
     return sft_batch_submit();
 }
 
+/* Tunes the scheduling knobs on n (scene, frame, samples) views rendered as one batch. */
+SFTX_EXPORT int sftx_scene_autotune_batch(void* const* scenes, const uint32_t* frames, const int32_t* samples, uint32_t n,
+                                          int32_t reps) {
+    sft_batch_begin();
+    for (uint32_t i = 0; i < n; i++) {
+        sft_set_msaa_samples(samples[i]);
+        if (sftx_scene_render(scenes[i], frames[i], NULL, 0)) {
+            sft_batch_submit();
+            return -1;
+        }
+    }
+    return sft_batch_autotune(reps);
+}
+
 SFTX_EXPORT void sftx_scene_free(void* p) {
     sftx_scene* s = (sftx_scene*)p;
     if (!s) return;

@@ -22,6 +22,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/sftg.h"
@@ -63,6 +64,7 @@ struct sftg_ctx {
     int launches = 0;
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
+    sftg_tuning tuning = { { 4, 4, 4 }, { 8, 8, 8 }, 8 };
 };
 
 static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
@@ -113,7 +115,7 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     for (int i = 0; i < 6; i++) cudaEventCreate(&ctx->ev[i]);
     if (cudaMallocHost((void**)&ctx->h_status, 64) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
-    sftg_tile_configure(200 * 1024);
+    sftg_tile_configure(227 * 1024);
     *out = ctx;
     return SFTG_OK;
 }
@@ -357,9 +359,14 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
             for (uint32_t k = 0; k < md.mesh_count; k++) {
                 const uint32_t first = ctx->h_mesh_first[id.model][k], cnt = ctx->h_mesh_count[id.model][k];
                 const uint32_t sk = ctx->h_mesh_skinned[id.model][k] && I.bones >= 0;
-                for (uint32_t s = 0; s < cnt; s += 8) {
-                    sftg_job j; j.inst = i; j.first = first + s; j.count = (uint16_t)((cnt - s) < 8 ? (cnt - s) : 8); j.skinned = (uint16_t)sk; j.view = v;
-                    jobs.push_back(j);
+                const uint32_t jw = (uint32_t)ctx->tuning.geom_job_width;
+                for (uint32_t s = 0; s < cnt; s += 8) {   /* the reference's groups of 8, cut into jobs of jw */
+                    const uint32_t gc = (cnt - s) < 8 ? (cnt - s) : 8;
+                    for (uint32_t k = 0; k < gc; k += jw) {
+                        sftg_job j; j.inst = i; j.first = first + s + k; j.count = (uint16_t)((gc - k) < jw ? (gc - k) : jw);
+                        j.skinned = (uint16_t)sk; j.view = v; j.group_first = first + s;
+                        jobs.push_back(j);
+                    }
                 }
             }
             lss += md.total_meshlets;
@@ -567,10 +574,10 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
     for (int si = 0; si < 3; si++)
-        if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], st, A); ctx->launches++; }
+        if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], st, A); ctx->launches++; }
     CK(cudaEventRecord(ctx->ev[4], st));
     for (int si = 0; si < 3; si++)
-        if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], st, A); ctx->launches++; }
+        if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ctx->launches++; }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[5], st));
     return 0;
@@ -642,6 +649,88 @@ extern "C" int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* fd
 extern "C" int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, uint32_t* const* colors,
                                   const int32_t* pitch_bytes, const uint32_t** out_device_colors) {
     return batch_common(ctx, fds, n_views, colors, pitch_bytes, nullptr, out_device_colors);
+}
+
+/* ------------------------------------------------------------------ tuning */
+static bool tuning_valid(const sftg_tuning* t) {
+    for (int k = 0; k < 3; k++) {
+        const int sp = t->resolve_split[k], sl = t->raster_slab_rows[k];
+        if (!(sp == 1 || sp == 2 || sp == 4 || sp == 8)) return false;
+        if (sl < 4 || sl > 64) return false;
+    }
+    return t->geom_job_width >= 1 && t->geom_job_width <= 8;
+}
+
+extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
+    if (!ctx || !out) return SFTG_E_ARG;
+    *out = ctx->tuning;
+    return SFTG_OK;
+}
+
+extern "C" int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* t) {
+    if (!ctx || !t) return SFTG_E_ARG;
+    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8, slab rows 4..64, job width 1..8)");
+    ctx->tuning = *t;
+    return SFTG_OK;
+}
+
+/* median over reps renders of one phase's device time (ms) */
+static int time_phase(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n, int reps, int phase, float* out) {
+    std::vector<float> t;
+    for (int r = 0; r < reps; r++) {
+        const int rc = batch_common(ctx, fds, n, nullptr, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+        t.push_back(ctx->timings[phase]);
+    }
+    std::sort(t.begin(), t.end());
+    *out = t[t.size() / 2];
+    return 0;
+}
+
+/* Coordinate search over the knobs that change only scheduling, never results: the geometry
+ * job width against the geometry phase, then per sample count the raster slab height against
+ * the raster phase and the resolve split against the resolve phase, each measured on the views
+ * with that sample count.  Leaves the best setting in the context. */
+extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, int32_t reps, sftg_tuning* out) {
+    if (!ctx || !fds || !n_views) return SFTG_E_ARG;
+    if (reps < 1) reps = 5;
+    sftg_tuning best = ctx->tuning;
+    int rc;
+    if ((rc = batch_common(ctx, fds, n_views, nullptr, nullptr, nullptr, nullptr))) return rc;   /* warm: arena, tables */
+    {
+        const int widths[4] = { 2, 4, 8, 1 };
+        float bt = 1e30f;
+        for (int k = 0; k < 3; k++) {
+            ctx->tuning = best; ctx->tuning.geom_job_width = widths[k];
+            float t;
+            if ((rc = time_phase(ctx, fds, n_views, reps, 1, &t))) { ctx->tuning = best; return rc; }
+            if (t < bt) { bt = t; best.geom_job_width = widths[k]; }
+        }
+    }
+    for (int si = 0; si < 3; si++) {
+        std::vector<sftg_frame_desc> sub;
+        for (uint32_t v = 0; v < n_views; v++) if (fds[v].samples == (1 << si)) sub.push_back(fds[v]);
+        if (sub.empty()) continue;
+        const int slabs[4] = { 4, 8, 16, 64 };
+        float bt = 1e30f;
+        for (int k = 0; k < 4; k++) {
+            ctx->tuning = best; ctx->tuning.raster_slab_rows[si] = slabs[k];
+            float t;
+            if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 3, &t))) { ctx->tuning = best; return rc; }
+            if (t < bt) { bt = t; best.raster_slab_rows[si] = slabs[k]; }
+        }
+        const int splits[4] = { 2, 4, 8, 1 };
+        bt = 1e30f;
+        for (int k = 0; k < 3; k++) {
+            ctx->tuning = best; ctx->tuning.resolve_split[si] = splits[k];
+            float t;
+            if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
+            if (t < bt) { bt = t; best.resolve_split[si] = splits[k]; }
+        }
+    }
+    ctx->tuning = best;
+    if (out) *out = best;
+    return SFTG_OK;
 }
 
 extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {

@@ -56,7 +56,7 @@ k_geometry(const sftg_frame* __restrict__ frames, const sftg_job* __restrict__ j
         const float* cl = F->ml_cull + (size_t)(g0 + lane) * 8;
         v3 ctr = mk3(cl[0], cl[1], cl[2]), ax = mk3(cl[4], cl[5], cl[6]);
         if (J.skinned) {
-            const int cb = F->ml_info[g0].culling_bone;     /* lane 0's bone for the whole group */
+            const int cb = F->ml_info[I->meshlet_base + J.group_first].culling_bone;   /* the group's first bone */
             const float* B = bones + (size_t)cb * 16;
             ctr = xform(ctr, B); ax = xform_dir(ax, B);
         }

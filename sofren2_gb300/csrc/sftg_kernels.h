@@ -54,7 +54,8 @@ void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view
                            uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
                            uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
-void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
-void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
+/* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4 or 8) */
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A);
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A);
 
 #define SFTG_SCAN_ELEMS_PER_BLOCK 4096

@@ -27,8 +27,8 @@
 #define TILE_THREADS 256          /* resolve CTA */
 #define RASTER_THREADS 512        /* raster CTA: 64 groups of 8 */
 #define SETUP_CAP RASTER_THREADS  /* triangle set-ups per round: 64 payloads x 8 lanes */
-#define SLAB_ROWS 8               /* rows of one raster work item */
-#define ITEM_CAP (SETUP_CAP * (SFTG_TILE / SLAB_ROWS))
+#define MIN_SLAB_ROWS 4           /* smallest raster work item (rows); the slab height is a tuning knob */
+#define ITEM_CAP (SETUP_CAP * (SFTG_TILE / MIN_SLAB_ROWS))
 
 struct tri_setup {
     float A[3], B[3], se[3];
@@ -279,7 +279,7 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
  * light culling. */
 template <int S>
 __global__ void __launch_bounds__(RASTER_THREADS)
-k_raster(const sftg_tile_args A, uint32_t tile0)
+k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
@@ -339,7 +339,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
                     if (tri_setup_one<S>(sx[0], sy[0], iw[0], sx[1], sy[1], iw[1], sx[2], sy[2], iw[2], tmx, tmy, p * 8 + l, T)) {
                         const uint32_t slot = atomicAdd(&s_nsetup, 1u);
                         setups[slot] = T;
-                        const uint32_t nslab = (uint32_t)(T.maxy - T.miny) / SLAB_ROWS + 1u;
+                        const uint32_t nslab = (uint32_t)(T.maxy - T.miny) / (uint32_t)slab_rows + 1u;
                         const uint32_t ib = atomicAdd(&s_nitems, nslab);
                         for (uint32_t k = 0; k < nslab; k++) items[ib + k] = (slot << 8) | k;
                     }
@@ -355,8 +355,8 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
             if (idx >= nitem) break;
             const uint32_t it = items[idx];
             const tri_setup T = setups[it >> 8];
-            const int y0 = T.miny + (int)(it & 0xFFu) * SLAB_ROWS;
-            const int y1 = min(y0 + SLAB_ROWS - 1, T.maxy);
+            const int y0 = T.miny + (int)(it & 0xFFu) * slab_rows;
+            const int y1 = min(y0 + slab_rows - 1, T.maxy);
             tri_raster<S>(T, y0, y1, grp_lane, gmask, tmx, tmy, keys);
         }
         __syncthreads();
@@ -394,22 +394,22 @@ k_raster(const sftg_tile_args A, uint32_t tile0)
 }
 
 /* ---------------------------------------------------------------- resolve */
-#define RESOLVE_SPLIT 4                       /* CTAs per tile, each 1/4 of the tile's 4x2 blocks */
-#define RESOLVE_BLOCKS (16 * 32 / RESOLVE_SPLIT)
+#define TILE_BLOCKS (16 * 32)                 /* 4x2 blocks per 64x64 tile; a CTA resolves 1/split of them */
 
 /* One CTA per quarter tile: tile light list (5855-5934) and proxy cache (5936-5990), then one
  * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
 template <int S>
 __global__ void __launch_bounds__(TILE_THREADS)
-k_resolve(const sftg_tile_args A, uint32_t tile0)
+k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
     __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
     __shared__ int s_nlights;
     __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
 
-    const uint32_t gtile = tile0 + blockIdx.x / RESOLVE_SPLIT;              /* batch-wide tile index */
-    const int part = blockIdx.x % RESOLVE_SPLIT;
+    const uint32_t gtile = tile0 + blockIdx.x / (uint32_t)split;            /* batch-wide tile index */
+    const int part = (int)(blockIdx.x % (uint32_t)split);
+    const int nblk = TILE_BLOCKS / split;
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
     const float* ss = A.ss + (size_t)F->ss_base * 576;
@@ -474,8 +474,8 @@ k_resolve(const sftg_tile_args A, uint32_t tile0)
         float mn[3] = { 1e30f, 1e30f, 1e30f }, mx[3] = { -1e30f, -1e30f, -1e30f };
         uint32_t last = SFTG_INVALID;
         const int ix0 = tid & 3, iy0 = (tid >> 2) & 1;
-        for (int b = tid >> 3; b < RESOLVE_BLOCKS; b += TILE_THREADS / 8) {
-            const int blk = part * RESOLVE_BLOCKS + b;
+        for (int b = tid >> 3; b < nblk; b += TILE_THREADS / 8) {
+            const int blk = part * nblk + b;
             const int gx = tmx + (blk & 15) * 4 + ix0, gy = tmy + (blk >> 4) * 2 + iy0;
             if (gx >= lim_x || gy >= lim_y) continue;
             const int pind = (gy - tmy) * SFTG_TILE + (gx - tmx);
@@ -592,8 +592,8 @@ k_resolve(const sftg_tile_args A, uint32_t tile0)
     const float clr[3] = { (float)((cc >> 16) & 0xFF) * (1.f / 255.f), (float)((cc >> 8) & 0xFF) * (1.f / 255.f), (float)(cc & 0xFF) * (1.f / 255.f) };
     const v3 cam = mk3(F->cam[0], F->cam[1], F->cam[2]);
 
-    for (int b = grp; b < RESOLVE_BLOCKS; b += TILE_THREADS / 8) {
-        const int blk = part * RESOLVE_BLOCKS + b;
+    for (int b = grp; b < nblk; b += TILE_THREADS / 8) {
+        const int blk = part * nblk + b;
         const int x = tmx + (blk & 15) * 4, y = tmy + (blk >> 4) * 2;
         if (x >= lim_x || y >= lim_y) continue;
         const int gx = x + ix, gy = y + iy;
@@ -863,18 +863,18 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
     return e;
 }
 
-void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
     const size_t sm = raster_smem(S);
-    if (S == 1) k_raster<1><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0);
-    else if (S == 2) k_raster<2><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0);
-    else k_raster<4><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0);
+    if (S == 1) k_raster<1><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
+    else if (S == 2) k_raster<2><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
+    else k_raster<4><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
 }
 
-void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
-    const uint32_t grid = tiles * RESOLVE_SPLIT;
-    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(A, tile0);
-    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(A, tile0);
-    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(A, tile0);
+    const uint32_t grid = tiles * (uint32_t)split;
+    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split);
+    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split);
+    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split);
 }

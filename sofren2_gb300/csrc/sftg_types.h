@@ -86,6 +86,8 @@ typedef struct sftg_job {   /* up to 8 consecutive meshlets of one mesh, sft_geo
     uint16_t count;        /* 1..8 */
     uint16_t skinned;      /* mesh has skin and the instance has bones */
     uint32_t view;         /* view of the batch this job belongs to */
+    uint32_t group_first;  /* first meshlet of the reference's 8-meshlet group: its culling bone is
+                              the whole group's (sofren2.c:4939-4960), also when a job covers part of it */
 } sftg_job;
 
 typedef struct sftg_point_light {

@@ -48,6 +48,8 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftx_scene_frame_size": (u32, [p, u32, p, p]), "sft_get_launch_count": (i32, []),
         "sft_get_cuda_stream": (p, []),
         "sftx_scene_render_batch": (i32, [p, p, p, u32, p, p]),
+        "sftx_scene_autotune_batch": (i32, [p, p, p, u32, i32]),
+        "sft_get_gpu_context": (p, []), "sftg_get_tuning": (i32, [p, p]), "sftg_set_tuning": (i32, [p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -160,6 +162,29 @@ class Renderer:
         if rc != 0:
             raise RuntimeError("batch render failed: " + (self.lib.sft_get_last_error() or b"").decode())
         return out
+
+    def autotune_batch(self, views: list[tuple], reps: int = 5) -> dict:
+        """Tunes the scheduling knobs (sftg_autotune) on views [(scene handle, frame, samples)]
+        rendered as one batch; returns the chosen setting."""
+        n = len(views)
+        hs = (C.c_void_p * n)(*[h for h, _, _ in views])
+        fr = np.array([f for _, f, _ in views], np.uint32)
+        sm = np.array([s for _, _, s in views], np.int32)
+        rc = self.lib.sftx_scene_autotune_batch(hs, _ptr(fr), _ptr(sm), n, reps)
+        self.lib.sft_set_msaa_samples(self.samples)
+        if rc != 0:
+            raise RuntimeError("autotune failed: " + (self.lib.sft_get_last_error() or b"").decode())
+        return self.tuning()
+
+    def tuning(self) -> dict:
+        t = np.zeros(7, np.int32)
+        self.lib.sftg_get_tuning(self.lib.sft_get_gpu_context(), _ptr(t))
+        return {"resolve_split": t[0:3].tolist(), "raster_slab_rows": t[3:6].tolist(), "geom_job_width": int(t[6])}
+
+    def set_tuning(self, resolve_split=(4, 4, 4), raster_slab_rows=(8, 8, 8), geom_job_width=8) -> None:
+        t = np.array([*resolve_split, *raster_slab_rows, geom_job_width], np.int32)
+        if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
+            raise ValueError("tuning out of range")
 
     def render_debug(self, h, frame: int, total_ss: int, n_proxies: int, payload_cap: int = 1 << 22,
                      clip_cap: int = 1 << 16) -> dict:

@@ -773,7 +773,7 @@ def ground_model(sc: Scene, seed: int, n: int = 64, half: float = 16.0, center=(
 
 
 def skinned_characters_scene(width=1920, height=1080, seed=2001, n_chars=8, n_lights=4, tex_size=512, frames=1,
-                             ground_quads=64, time0=0.0) -> Scene:
+                             ground_quads=64, time0=0.0, views=None) -> Scene:
     """Skinned humanoids on a ground plane, lit by point lights above them; one capsule proxy per
     head, torso, upper/lower arm and thigh/shin."""
     rng = Pcg32(seed)
@@ -795,11 +795,13 @@ def skinned_characters_scene(width=1920, height=1080, seed=2001, n_chars=8, n_li
         lp = (rng.uniform(-6.0, 6.0), rng.uniform(5.0, 7.0), rng.uniform(3.0, 11.0))
         col = (rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0))
         lights.append((lp, col[0], col[1], col[2], F32(1.0), F32(14.0)))
-    for fi in range(frames):
-        fr = _camera_frame(width, height, cam_pos=(0.0, 1.7, 0.0), target=(0.0, 1.0, 8.0))
+    if views is None:
+        views = [(width, height, (0.0, 1.7, 0.0), (0.0, 1.0, 8.0), F32(time0 + fi / max(frames, 1)) % F32(1.0))
+                 for fi in range(frames)]
+    for vw, vh, cpos, tgt, t in views:
+        fr = _camera_frame(vw, vh, cam_pos=cpos, target=tgt)
         fr.ambient = np.array([0.15, 0.15, 0.17], dtype=F32)
         fr.point_lights = list(lights)
-        t = F32(time0 + fi / max(frames, 1)) % F32(1.0)
         insts = [(ground, mat_identity(), None)]
         for c in range(n_chars):
             insts.append((chars[c], place[c], anims[c].pose(t)))
@@ -910,7 +912,8 @@ class _QuadMesh:
 
 
 def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arch_segments=16, n_tex=25,
-                 tex_size=1024, lm_size=1024, n_lights=16, n_chars=4, char_tex=512, floor_quads=(120, 60), frames=1) -> Scene:
+                 tex_size=1024, lm_size=1024, n_lights=16, n_chars=4, char_tex=512, floor_quads=(120, 60), frames=1,
+                 views=None) -> Scene:
     """An atrium of pillars and semicircular arches (boxes, arch_segments per arch) on `levels`
     floors of an nx x nz grid, floor and walls as quad grids; every static quad owns a 2x2 texel
     chart in one lightmap page holding per-vertex baked colours uniform in [0,1]^3.  Point
@@ -997,14 +1000,53 @@ def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arc
     for l in range(n_lights):
         lp = (rng.uniform(-12.0, 12.0), rng.uniform(13.0, 14.5), rng.uniform(6.0, 17.0))
         lights.append((lp, rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0), rng.uniform(0.6, 1.0), F32(0.5), F32(60.0)))
-    for fi in range(frames):
-        fr = _camera_frame(width, height, cam_pos=(0.0, 1.7, 0.5), target=(0.0, 3.0, 12.0))
+    if views is None:
+        views = [(width, height, (0.0, 1.7, 0.5), (0.0, 3.0, 12.0), F32(fi / max(frames, 1))) for fi in range(frames)]
+    for vw, vh, cpos, tgt, t in views:
+        fr = _camera_frame(vw, vh, cam_pos=cpos, target=tgt)
         fr.ambient = np.array([0.1, 0.1, 0.1], dtype=F32)
         fr.point_lights = list(lights)
-        t = F32(fi / max(frames, 1))
         fr.instances = [(atrium, mat_identity(), None)] + [(chars[c], place[c], anims[c].pose(t)) for c in range(n_chars)]
         sc.frames.append(fr)
     return sc
+
+
+MULTIVIEW_SIZES = ((320, 180), (640, 360), (1280, 720), (1920, 1080), (2560, 1440))
+
+
+def config4(seed=4001, n_views=96, n_scenes=6, quick=False) -> tuple[list[Scene], list[tuple[int, int, int]]]:
+    """Batched multi-view workload: n_views views over n_scenes resident scenes (half of the
+    skinned-characters type, half of the atrium type, each with its own seed).  Each view draws
+    its resolution from MULTIVIEW_SIZES, its MSAA from (1, 2, 4), a seeded camera looking into the
+    scene and an animation time in [0, 1).  Returns (scenes, [(scene index, frame index, samples)]),
+    view k being frame k // n_scenes of scene k % n_scenes.  quick=True shrinks the atrium type
+    (fewer textures and floor quads) for CPU-side tests."""
+    rng = Pcg32(seed)
+    per_scene: list[list] = [[] for _ in range(n_scenes)]
+    out_views = []
+    for k in range(n_views):
+        si = k % n_scenes
+        w, h = MULTIVIEW_SIZES[rng.next_u32() % len(MULTIVIEW_SIZES)]
+        S = (1, 2, 4)[rng.next_u32() % 3]
+        t = F32(rng.uniform(0.0, 1.0))
+        if si < n_scenes // 2:   # skinned characters: characters at z 5..8, x -3..3
+            cpos = (rng.uniform(-4.0, 4.0), rng.uniform(1.2, 2.6), rng.uniform(-1.0, 1.5))
+            tgt = (rng.uniform(-2.0, 2.0), rng.uniform(0.6, 1.4), rng.uniform(6.0, 9.0))
+        else:                    # atrium: floor 30 x 15 m from z ~1, characters near z 6
+            cpos = (rng.uniform(-5.0, 5.0), rng.uniform(1.5, 4.0), rng.uniform(0.2, 2.5))
+            tgt = (rng.uniform(-4.0, 4.0), rng.uniform(1.0, 5.0), rng.uniform(9.0, 15.0))
+        out_views.append((si, len(per_scene[si]), S))
+        per_scene[si].append((w, h, cpos, tgt, t))
+    scenes = []
+    for si in range(n_scenes):
+        if si < n_scenes // 2:
+            scenes.append(skinned_characters_scene(seed=2001 + 10 * si, views=per_scene[si]))
+        elif quick:
+            scenes.append(atrium_scene(seed=3001 + 10 * si, n_tex=4, tex_size=128, lm_size=512, char_tex=64,
+                                       floor_quads=(30, 15), views=per_scene[si]))
+        else:
+            scenes.append(atrium_scene(seed=3001 + 10 * si, views=per_scene[si]))
+    return scenes, out_views
 
 
 def config3(width=1920, height=1080, seed=3001) -> Scene:

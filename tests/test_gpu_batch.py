@@ -83,3 +83,48 @@ def test_golden_cases_in_one_batch(renderer, golden):
     finally:
         for h in hs:
             renderer.free_scene(h)
+
+
+TUNINGS = [
+    dict(resolve_split=(1, 2, 8), raster_slab_rows=(4, 16, 64), geom_job_width=1),
+    dict(resolve_split=(8, 1, 2), raster_slab_rows=(64, 4, 16), geom_job_width=3),
+    dict(resolve_split=(2, 8, 1), raster_slab_rows=(16, 64, 4), geom_job_width=5),
+]
+
+
+@pytest.mark.parametrize("tuning", TUNINGS)
+def test_tuning_knobs_do_not_change_results(renderer, golden, tuning):
+    """Every scheduling knob of sftg_tuning leaves every pixel of every golden case unchanged."""
+    names = [n for n in gc.CASES if n != "variety_noclear"]
+    hs = [renderer.load_scene(gc.blob(n)) for n in names]
+    saved = renderer.tuning()
+    try:
+        renderer.set_tuning(**tuning)
+        views, keys = [], []
+        for n, h in zip(names, hs):
+            for S in gc.SAMPLES[n]:
+                views.append((h, 0, S))
+                keys.append((n, S))
+        got = renderer.render_batch(views, [None] * len(views))
+        for (n, S), c in zip(keys, got):
+            assert gc.sha(c.reshape(-1)) == golden[n]["samples"][str(S)]["color"], f"{n} {S}x differs with {tuning}"
+    finally:
+        renderer.set_tuning(**saved)
+        for h in hs:
+            renderer.free_scene(h)
+
+
+def test_autotune_keeps_results(renderer, golden, handles):
+    views = [(handles[n], 0, S) for n, S in zip(MIXED, (1, 2, 4, 2, 1, 4)) if n != "variety_noclear"]
+    saved = renderer.tuning()
+    try:
+        t = renderer.autotune_batch(views, reps=1)
+        assert t["geom_job_width"] in (2, 4, 8)
+        h = renderer.load_scene(gc.blob("config1"))
+        try:
+            got = renderer.render_batch([(h, 0, 2)], [None])
+            assert gc.sha(got[0].reshape(-1)) == golden["config1"]["samples"]["2"]["color"]
+        finally:
+            renderer.free_scene(h)
+    finally:
+        renderer.set_tuning(**saved)
