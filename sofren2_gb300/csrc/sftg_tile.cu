@@ -399,7 +399,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
 /* One CTA per quarter tile: tile light list (5855-5934) and proxy cache (5936-5990), then one
  * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
 template <int S>
-__global__ void __launch_bounds__(TILE_THREADS)
+__global__ void __launch_bounds__(TILE_THREADS, S == 4 ? 4 : 3)   /* 64 / 85 registers: occupancy measured best */
 k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
@@ -766,14 +766,29 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                         const float lrl = fsqrt(d2);
                         const float rd2 = rcpr(d2);   /* loop-invariant: the reference recomputes the same value per proxy */
                         const float bk = 0.2f, b4 = 0.25f / 0.2f;
+                        /* every proxy's "between" test first (independent, so they overlap), then
+                         * the block-level skip as the OR over the block's lanes, then the smooth-max
+                         * blend over the surviving proxies in index order */
+                        const bool want = lm ? in_tri : lit;
+                        uint32_t rmask = 0;
+#pragma unroll 4
                         for (int pi = 0; pi < np; pi++) {
                             const proxy_cache& q = pcache[i * SFTG_MAX_LIGHT_PROXIES + pi];
                             const float wdv = 0.f - vdot(mk3(q.W[0], q.W[1], q.W[2]), Lr);
                             const bool btw = wdv > 0.f && wdv < d2;
                             const float tf = wdv * rd2;
                             const float cd2 = fma_(-wdv, tf, q.wdw);
-                            const bool ray = btw && (cd2 < q.rb2) && (lm ? in_tri : lit);
-                            if (!(__ballot_sync(gmask, ray) & gmask)) continue;   /* block-level skip */
+                            rmask |= (uint32_t)(btw && (cd2 < q.rb2) && want) << pi;
+                        }
+                        uint32_t bmask = rmask;
+                        bmask |= __shfl_xor_sync(gmask, bmask, 1);
+                        bmask |= __shfl_xor_sync(gmask, bmask, 2);
+                        bmask |= __shfl_xor_sync(gmask, bmask, 4);
+                        while (bmask) {
+                            const int pi = __ffs(bmask) - 1;
+                            bmask &= bmask - 1;
+                            const proxy_cache& q = pcache[i * SFTG_MAX_LIGHT_PROXIES + pi];
+                            const bool ray = (rmask >> pi) & 1u;
                             const v3 pa = mk3(q.pa[0], q.pa[1], q.pa[2]), ab = mk3(q.ab[0], q.ab[1], q.ab[2]);
                             const v3 ao = sub3(P, pa);
                             const float abl = vdot(ab, Ln), abao = vdot(ab, ao), lao = vdot(Ln, ao);
