@@ -101,6 +101,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_resolve launch of the
+# workload, from one full ncu capture of that launch on a GB300 (the 6th launch of
+# `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`)
+RESOLVE_TRAFFIC = {"skinned_1080p_2xmsaa": 38515968 + 15360, "atrium_1080p_4xmsaa": 76697856 + 3112704}
+
+
 def _algorithmic_resolve_bytes(width: int, height: int, samples: int) -> float:
     """Bytes the resolve kernel must move per frame at minimum: per pixel the visibility
     buffer (8 B per sample: depth and id), the vertex data of its triangle (156 B per distinct
@@ -205,7 +211,7 @@ def run_ours(args, cfg) -> dict:
                       "raster": float(kern[3]), "resolve": tile_ms},
         "roofline": {"kernel": "k_resolve", "bound": "hbm", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": None, "peak_source": peaks["src"],
+                     "traffic": RESOLVE_TRAFFIC.get(cfg["name"]), "algorithmic_bytes": alg, "peak_source": peaks["src"],
                      "note": "the resolve is FP32/issue bound (lights x capsule proxies per pixel); "
                              "HBM fraction of its algorithmic bytes shown per contract"},
         "clocks": clk,
