@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libsofren2_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["sftg_geom.cu", "sftg_tile.cu", "sftg_occl.cu", "sftg_api.cu"]
-C_SOURCES = ["sft_lib.c", "sft_scene.c"]
+C_SOURCES = ["sft_lib.c", "sft_scene.c", "sft_serve.c"]
 
 
 def _nvcc() -> str:

@@ -141,18 +141,22 @@ SFTX_EXPORT uint32_t sftx_scene_frame_size(const void* p, uint32_t frame, uint32
 
 static float sftx_ld(const float* p, int i) { float v; memcpy(&v, p + i, 4); return v; }
 
-/* Issues one frame's API calls and sft_present into `color` (pitch in bytes). */
-SFTX_EXPORT int sftx_scene_render(void* p, uint32_t frame, uint32_t* color, int32_t pitch_bytes) {
+SFTX_EXPORT int sftx_scene_render(void* p, uint32_t frame, uint32_t* color, int32_t pitch_bytes);
+
+/* Issues one frame's API calls and sft_present into `color` (pitch in bytes), drawing at most
+ * max_point_lights of the frame's point lights (the first ones). */
+SFTX_EXPORT int sftx_scene_render_ex(void* p, uint32_t frame, uint32_t* color, int32_t pitch_bytes, uint32_t max_point_lights) {
     sftx_scene* s = (sftx_scene*)p;
     if (!s || frame >= s->n_frame) return -1;
     const sftx_frame* f = &s->frames[frame];
+    const uint32_t n_point = f->n_point < max_point_lights ? f->n_point : max_point_lights;
     sft_resize((i32)f->width, (i32)f->height);
     sft_set_ambient_light(sftx_ld(f->ambient, 0), sftx_ld(f->ambient, 1), sftx_ld(f->ambient, 2));
     for (uint32_t l = 0; l < f->n_dir; l++) {
         const float* d = f->dir + 7 * l;
         sft_draw_directional_light(SFT_V(sftx_ld(d, 0), sftx_ld(d, 1), sftx_ld(d, 2)), sftx_ld(d, 3), sftx_ld(d, 4), sftx_ld(d, 5), sftx_ld(d, 6));
     }
-    for (uint32_t l = 0; l < f->n_point; l++) {
+    for (uint32_t l = 0; l < n_point; l++) {
         const float* q = f->point + 8 * l;
         sft_draw_point_light(SFT_V(sftx_ld(q, 0), sftx_ld(q, 1), sftx_ld(q, 2)), sftx_ld(q, 3), sftx_ld(q, 4), sftx_ld(q, 5), sftx_ld(q, 6), sftx_ld(q, 7), l);
     }
@@ -213,6 +217,10 @@ SFTX_EXPORT int sftx_scene_autotune_batch(void* const* scenes, const uint32_t* f
         }
     }
     return sft_batch_autotune(reps);
+}
+
+SFTX_EXPORT int sftx_scene_render(void* p, uint32_t frame, uint32_t* color, int32_t pitch_bytes) {
+    return sftx_scene_render_ex(p, frame, color, pitch_bytes, 0xFFFFFFFFu);
 }
 
 SFTX_EXPORT void sftx_scene_free(void* p) {

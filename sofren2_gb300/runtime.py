@@ -49,6 +49,8 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sft_get_cuda_stream": (p, []),
         "sftx_scene_render_batch": (i32, [p, p, p, u32, p, p]),
         "sftx_scene_autotune_batch": (i32, [p, p, p, u32, i32]),
+        "sftx_scene_render_ex": (i32, [p, u32, p, i32, u32]),
+        "sftx_serve": (i32, [p, p, u32, u32, u64, i32, p, u32, p, p, p]),
         "sft_get_gpu_context": (p, []), "sftg_get_tuning": (i32, [p, p]), "sftg_set_tuning": (i32, [p, p]),
     }
     for name, (res, args) in sig.items():
@@ -60,6 +62,24 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
 
 def _ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class SftxRequest(C.Structure):
+    """struct sftx_request (sofren2_gb300/csrc/sft_serve.c)."""
+    _fields_ = [("arrival_ns", C.c_uint64), ("device_bytes", C.c_uint64), ("scene", C.c_uint32), ("frame", C.c_uint32),
+                ("samples", C.c_int32), ("max_point_lights", C.c_uint32)]
+
+
+class SftxServeStats(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("max_batch", C.c_uint64), ("peak_bytes", C.c_uint64), ("errors", C.c_uint64)]
+
+
+def request_device_bytes(width: int, height: int, samples: int, meshlets: int) -> int:
+    """Device memory a request holds while in flight: visibility buffer (8 B per sample), colour,
+    screen-space cache and batch records per meshlet, tile lists and clip pool at a generous
+    estimate."""
+    tiles = ((width + 63) // 64) * ((height + 63) // 64)
+    return tiles * samples * 4096 * 8 + width * height * 4 + meshlets * (2304 + 16 * 16 + 16 * 8 + 16) + tiles * 64 * 1024
 
 
 class Renderer:
@@ -185,6 +205,29 @@ class Renderer:
         t = np.array([*resolve_split, *raster_slab_rows, geom_job_width], np.int32)
         if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
             raise ValueError("tuning out of range")
+
+    def serve(self, handles: list, requests: list[tuple], max_batch: int, budget_bytes: int, plain: bool,
+              colors: list[np.ndarray]) -> tuple[np.ndarray, np.ndarray, dict]:
+        """Runs the native serving loop (sftx_serve) over requests
+        [(arrival_s, scene index, frame, samples, max point lights, device bytes)], sorted by
+        arrival.  colors is the ring of host colour buffers (at least max_batch, each as large as
+        the largest request).  Returns (completion times in s, batch index per request, stats)."""
+        n = len(requests)
+        reqs = (SftxRequest * max(1, n))()
+        for k, (t, si, f, S, nl, nb) in enumerate(requests):
+            reqs[k] = SftxRequest(int(t * 1e9), int(nb), si, f, S, nl)
+        hs = (C.c_void_p * len(handles))(*handles)
+        cp = (C.c_void_p * len(colors))(*[c.ctypes.data for c in colors])
+        done = np.zeros(max(1, n), np.uint64)
+        batch = np.zeros(max(1, n), np.uint32)
+        st = SftxServeStats()
+        rc = self.lib.sftx_serve(hs, reqs, n, max_batch, budget_bytes, 1 if plain else 0, cp, len(colors), _ptr(done),
+                                 _ptr(batch), C.byref(st))
+        self.lib.sft_set_msaa_samples(self.samples)
+        if rc != 0:
+            raise RuntimeError(f"serving loop failed ({rc}): " + (self.lib.sft_get_last_error() or b"").decode())
+        stats = {"batches": st.batches, "max_batch": st.max_batch, "peak_bytes": st.peak_bytes}
+        return done[:n].astype(np.float64) * 1e-9, batch[:n].copy(), stats
 
     def render_debug(self, h, frame: int, total_ss: int, n_proxies: int, payload_cap: int = 1 << 22,
                      clip_cap: int = 1 << 16) -> dict:

@@ -911,16 +911,15 @@ class _QuadMesh:
                        luv=np.array(self.luv, dtype=F32))
 
 
-def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arch_segments=16, n_tex=25,
-                 tex_size=1024, lm_size=1024, n_lights=16, n_chars=4, char_tex=512, floor_quads=(120, 60), frames=1,
-                 views=None) -> Scene:
-    """An atrium of pillars and semicircular arches (boxes, arch_segments per arch) on `levels`
-    floors of an nx x nz grid, floor and walls as quad grids; every static quad owns a 2x2 texel
-    chart in one lightmap page holding per-vertex baked colours uniform in [0,1]^3.  Point
-    lights sit under the roof with a radius that covers the whole atrium, and skinned humanoids
-    stand on the floor."""
-    rng = Pcg32(seed)
-    sc = Scene()
+_ATRIUM_GEOMETRY: dict = {}
+
+
+def _atrium_geometry(lm_size, nx, nz, levels, arch_segments, n_tex, floor_quads):
+    """The atrium's static meshes, [(texture group, Meshlets)], and its lightmap chart count.
+    Depends on the layout parameters only, so scenes of one layout share it (memoised)."""
+    key = (lm_size, nx, nz, levels, arch_segments, n_tex, tuple(floor_quads))
+    if key in _ATRIUM_GEOMETRY:
+        return _ATRIUM_GEOMETRY[key]
     chart = [0]
     groups = [_QuadMesh(lm_size, chart) for _ in range(n_tex)]
     x0, x1, z0, z1, height_m = -15.0, 15.0, 4.0, 19.0, 15.0
@@ -967,6 +966,23 @@ def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arc
                         hl = rad * np.pi / arch_segments * 0.5 + 0.01
                         ext = (hl if ddx else 0.08, 0.06, hl if ddz else 0.08)
                         g.box((cx_ - ext[0], cy_ - ext[1], cz_ - ext[2]), (cx_ + ext[0], cy_ + ext[1], cz_ + ext[2]))
+    built = [(t, build_meshlets(g.raw())) for t, g in enumerate(groups + [fq, wq]) if g.tris]
+    _ATRIUM_GEOMETRY[key] = (built, chart[0])
+    return _ATRIUM_GEOMETRY[key]
+
+
+def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arch_segments=16, n_tex=25,
+                 tex_size=1024, lm_size=1024, n_lights=16, n_chars=4, char_tex=512, floor_quads=(120, 60), frames=1,
+                 views=None) -> Scene:
+    """An atrium of pillars and semicircular arches (boxes, arch_segments per arch) on `levels`
+    floors of an nx x nz grid, floor and walls as quad grids; every static quad owns a 2x2 texel
+    chart in one lightmap page holding per-vertex baked colours uniform in [0,1]^3.  Point
+    lights sit under the roof with a radius that covers the whole atrium, and skinned humanoids
+    stand on the floor."""
+    rng = Pcg32(seed)
+    sc = Scene()
+    built, n_chart = _atrium_geometry(lm_size, nx, nz, levels, arch_segments, n_tex, floor_quads)
+    chart = [n_chart]
     assert chart[0] * 4 <= lm_size * lm_size, "lightmap page too small for the quad charts"
     lm = np.full((lm_size, lm_size), 0xFF000000, dtype=np.uint32)
     cols_rgb = np.zeros((chart[0] * 4, 3), dtype=np.uint32)
@@ -981,10 +997,8 @@ def atrium_scene(width=1920, height=1080, seed=3001, nx=20, nz=10, levels=3, arc
     lm_tex = sc.add_texture(lm)
     tex_ids = [sc.add_texture(value_noise_texture(tex_size, tex_size, seed * 31 + t)) for t in range(n_tex)]
     meshes, mats = [], []
-    for t, g in enumerate(groups + [fq, wq]):
-        if not g.tris:
-            continue
-        meshes.append(build_meshlets(g.raw()))
+    for t, ms in built:
+        meshes.append(ms)
         mats.append(sc.add_material(tex_ids[t % n_tex], 0xFFFFFFFF, 16.0))
     atrium = sc.add_model(Model(meshes, mats, lightmaps=[lm_tex], lightmap_pages=[0] * len(meshes)))
     chars, anims = [], []
@@ -1042,11 +1056,46 @@ def config4(seed=4001, n_views=96, n_scenes=6, quick=False) -> tuple[list[Scene]
         if si < n_scenes // 2:
             scenes.append(skinned_characters_scene(seed=2001 + 10 * si, views=per_scene[si]))
         elif quick:
-            scenes.append(atrium_scene(seed=3001 + 10 * si, n_tex=4, tex_size=128, lm_size=512, char_tex=64,
-                                       floor_quads=(30, 15), views=per_scene[si]))
+            scenes.append(atrium_scene(seed=3001 + 10 * si, nx=10, nz=5, levels=2, n_tex=4, tex_size=128, lm_size=512,
+                                       char_tex=64, floor_quads=(30, 15), views=per_scene[si]))
         else:
             scenes.append(atrium_scene(seed=3001 + 10 * si, views=per_scene[si]))
     return scenes, out_views
+
+
+def config5(seed=5001, n_scenes=16, frames_per_scene=24, quick=False) -> tuple[list[Scene], list[int]]:
+    """Served-rendering scenes: n_scenes resident scenes, half of the skinned-characters type
+    (eight humanoids, sixteen point lights, rendered at 2x MSAA) and half of the atrium type (the
+    config-3 layout with per-scene textures, lightmap colours, lights and characters, rendered at
+    4x MSAA).  Each scene holds a pool of frames_per_scene request frames: a seeded camera, a
+    resolution from MULTIVIEW_SIZES and an animation time in [0, 1).  Returns (scenes, MSAA per
+    scene).  quick=True shrinks the atrium type for CPU-side tests."""
+    rng = Pcg32(seed)
+    scenes_out, samples = [], []
+    for si in range(n_scenes):
+        views = []
+        skinned = si < n_scenes // 2
+        for _ in range(frames_per_scene):
+            w, h = MULTIVIEW_SIZES[rng.next_u32() % len(MULTIVIEW_SIZES)]
+            t = F32(rng.uniform(0.0, 1.0))
+            if skinned:
+                cpos = (rng.uniform(-4.0, 4.0), rng.uniform(1.2, 2.6), rng.uniform(-1.0, 1.5))
+                tgt = (rng.uniform(-2.0, 2.0), rng.uniform(0.6, 1.4), rng.uniform(6.0, 9.0))
+            else:
+                cpos = (rng.uniform(-5.0, 5.0), rng.uniform(1.5, 4.0), rng.uniform(0.2, 2.5))
+                tgt = (rng.uniform(-4.0, 4.0), rng.uniform(1.0, 5.0), rng.uniform(9.0, 15.0))
+            views.append((w, h, cpos, tgt, t))
+        if skinned:
+            scenes_out.append(skinned_characters_scene(seed=seed + 10 * si, n_lights=16, views=views))
+            samples.append(2)
+        elif quick:
+            scenes_out.append(atrium_scene(seed=seed + 10 * si, nx=10, nz=5, levels=2, n_tex=4, tex_size=128, lm_size=512,
+                                           char_tex=64, floor_quads=(30, 15), views=views))
+            samples.append(4)
+        else:
+            scenes_out.append(atrium_scene(seed=seed + 10 * si, views=views))
+            samples.append(4)
+    return scenes_out, samples
 
 
 def config3(width=1920, height=1080, seed=3001) -> Scene:

@@ -1,0 +1,68 @@
+"""Served rendering (sftx_serve, the native continuous-batching loop): every request's pixels
+are the ones a lone render of it produces, whether it was served in a batch, alone (plain) or
+under a memory budget that forces one request per batch."""
+import numpy as np
+import pytest
+
+from sofren2_gb300 import runtime, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def served(renderer):
+    scs, samples = scenes.config5(n_scenes=4, frames_per_scene=3, quick=True)
+    hs = [renderer.load_scene(sc.to_bytes()) for sc in scs]
+    rng = np.random.default_rng(5)
+    reqs = []
+    for k in range(24):
+        si = int(rng.integers(len(scs)))
+        f = int(rng.integers(3))
+        fr = scs[si].frames[f]
+        meshlets = sum(sum(ms.n for ms in scs[si].models[mi].meshes) for mi, _, _ in fr.instances)
+        nb = runtime.request_device_bytes(fr.width, fr.height, samples[si], meshlets)
+        reqs.append((0.0005 * (k // 6), si, f, samples[si], int(rng.integers(1, 17)), nb))
+    sizes = [(scs[si].frames[f].width, scs[si].frames[f].height) for _, si, f, _, _, _ in reqs]
+    alone = []
+    for (_, si, f, S, nl, _), (w, h) in zip(reqs, sizes):
+        renderer.set_samples(S)
+        c = np.zeros((h, w), np.uint32)
+        assert renderer.lib.sftx_scene_render_ex(hs[si], f, c.ctypes.data, c.strides[0], nl) == 0
+        alone.append(c)
+    renderer.set_samples(1)
+    yield hs, reqs, sizes, alone
+    for h in hs:
+        renderer.free_scene(h)
+
+
+def _ring(sizes, n):
+    big = max(w * h for w, h in sizes)
+    return [np.zeros(big, np.uint32) for _ in range(n)]
+
+
+def _check(colors, sizes, alone):
+    for k, ((w, h), a) in enumerate(zip(sizes, alone)):
+        got = colors[k][: w * h].reshape(h, w)
+        assert np.array_equal(got, a), f"request {k} differs from its lone render"
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_served_equals_alone(renderer, served, plain):
+    hs, reqs, sizes, alone = served
+    colors = _ring(sizes, len(reqs))
+    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=1 << 40, plain=plain, colors=colors)
+    _check(colors, sizes, alone)
+    assert np.all(done >= np.array([r[0] for r in reqs]))
+    if plain:
+        assert st["max_batch"] == 1 and st["batches"] == len(reqs)
+    else:
+        assert 1 < st["max_batch"] <= 8 and st["batches"] < len(reqs)
+
+
+def test_memory_budget_limits_batches(renderer, served):
+    hs, reqs, sizes, alone = served
+    colors = _ring(sizes, len(reqs))
+    budget = min(r[5] for r in reqs)   # any two requests exceed it: one request per batch
+    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=budget, plain=False, colors=colors)
+    _check(colors, sizes, alone)
+    assert st["max_batch"] == 1
