@@ -158,8 +158,8 @@ int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* frame, uint8_t*
  * the 64x64 tile stays fixed here too, because the per-tile payload lists are part of the
  * render path's observable output). */
 typedef struct sftg_tuning {
-    int32_t resolve_split[3];     /* resolve CTAs per 64x64 tile at 1x, 2x, 4x: 1, 2, 4 or 8 (default 4) */
-    int32_t raster_slab_rows[3];  /* tile rows per raster work item at 1x, 2x, 4x: 4..64 (default 8) */
+    int32_t resolve_split[3];     /* resolve CTAs per 64x64 tile at 1x, 2x, 4x: 1, 2, 4, 8 or 16 (default 16, 8, 16) */
+    int32_t raster_slab_rows[3];  /* tile rows per raster work item at 1x, 2x, 4x: 4..64 (default 8, 8, 4) */
     int32_t geom_job_width;       /* meshlets per geometry warp: 1..8 (default 8, the reference's job) */
 } sftg_tuning;
 int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out);

@@ -64,7 +64,7 @@ struct sftg_ctx {
     int launches = 0;
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
-    sftg_tuning tuning = { { 4, 4, 4 }, { 8, 8, 8 }, 8 };
+    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 8 };   /* measured best on the single-view workloads */
 };
 
 static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
@@ -292,6 +292,7 @@ struct batch_bufs {
     int4* mrect;
     sftg_clip_tri* clips; int4* clip_rect;
     uint32_t* tile_count; uint32_t* tile_start;
+    uint32_t* tile_order; uint32_t* order_scratch;
     uint64_t* tile_pay;
     uint8_t* light_vis;
     void* packets; uint2* pairs; uint32_t* n_pairs; uint32_t max_pairs;
@@ -421,7 +422,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     auto acc = [&](size_t bytes) { need = ((need + 255) & ~(size_t)255) + bytes; };
     acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
-    acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(ctx->tile_cap * 8);
+    acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(1024); acc(ctx->tile_cap * 8);
     acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
     acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
     acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
@@ -456,6 +457,8 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     B.clip_rect = bp.take<int4>(ctx->clip_cap);
     B.tile_count = bp.take<uint32_t>(total_tiles);
     B.tile_start = bp.take<uint32_t>(total_tiles);
+    B.tile_order = bp.take<uint32_t>(total_tiles);
+    B.order_scratch = bp.take<uint32_t>(256);
     B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
     B.light_vis = bp.take<uint8_t>((size_t)total_prox * 64 + 64);
     B.packets = bp.take<char>((size_t)total_packets * sftg_packet_bytes() + 64);
@@ -566,11 +569,13 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
     scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ctx->launches);
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
-    ctx->launches += 2;
+    sftg_launch_tile_order(B.frames, B.tile_view, B.tile_count, B.total_tiles, B.order_scratch, B.tile_order, st);
+    ctx->launches += 4;
     CK(cudaEventRecord(ctx->ev[3], st));
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));
     sftg_tile_args A;
     A.frames = B.frames; A.tile_view = B.tile_view; A.ss = B.ss; A.clips = B.clips; A.clip_base = B.clip_base;
+    A.tile_order = B.tile_order;
     A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
     for (int si = 0; si < 3; si++)
@@ -655,7 +660,7 @@ extern "C" int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* fds, uin
 static bool tuning_valid(const sftg_tuning* t) {
     for (int k = 0; k < 3; k++) {
         const int sp = t->resolve_split[k], sl = t->raster_slab_rows[k];
-        if (!(sp == 1 || sp == 2 || sp == 4 || sp == 8)) return false;
+        if (!(sp == 1 || sp == 2 || sp == 4 || sp == 8 || sp == 16)) return false;
         if (sl < 4 || sl > 64) return false;
     }
     return t->geom_job_width >= 1 && t->geom_job_width <= 8;
@@ -669,7 +674,7 @@ extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
 
 extern "C" int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* t) {
     if (!ctx || !t) return SFTG_E_ARG;
-    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8, slab rows 4..64, job width 1..8)");
+    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8)");
     ctx->tuning = *t;
     return SFTG_OK;
 }
@@ -719,7 +724,7 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
             if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 3, &t))) { ctx->tuning = best; return rc; }
             if (t < bt) { bt = t; best.raster_slab_rows[si] = slabs[k]; }
         }
-        const int splits[4] = { 2, 4, 8, 1 };
+        const int splits[4] = { 4, 8, 16, 2 };
         bt = 1e30f;
         for (int k = 0; k < 3; k++) {
             ctx->tuning = best; ctx->tuning.resolve_split[si] = splits[k];

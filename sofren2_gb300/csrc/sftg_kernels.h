@@ -24,6 +24,7 @@ struct sftg_tile_args {
     const float* ss;
     const sftg_clip_tri* clips;
     const uint32_t* clip_base;     /* exclusive scan of clip counts: a view's first slot is clip_base[ss_base * 16] */
+    const uint32_t* tile_order;    /* launch order of the tiles (heaviest first within each sample count) */
     const uint32_t* tile_start;
     const uint32_t* tile_count;
     const uint64_t* tile_pay;
@@ -54,7 +55,10 @@ void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view
                            uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
                            uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
-/* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4 or 8) */
+/* order[] = the batch's tiles, heaviest first inside each sample-count range; scratch holds 192 words */
+void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
+                            uint32_t* scratch, uint32_t* order, cudaStream_t st);
+/* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4, 8 or 16) */
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A);
 void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A);
 

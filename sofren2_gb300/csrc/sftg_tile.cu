@@ -287,7 +287,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     uint32_t* items = (uint32_t*)(setups + SETUP_CAP);                     /* set-up index << 8 | slab */
     __shared__ uint32_t s_nsetup, s_nitems, s_next;
     __shared__ float s_red[2][RASTER_THREADS / 32];
-    const uint32_t gtile = tile0 + blockIdx.x;                             /* batch-wide tile index */
+    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x];              /* batch-wide tile index, heaviest first */
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
     const float* ss = A.ss + (size_t)F->ss_base * 576;
@@ -407,7 +407,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     __shared__ int s_nlights;
     __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
 
-    const uint32_t gtile = tile0 + blockIdx.x / (uint32_t)split;            /* batch-wide tile index */
+    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x / (uint32_t)split];   /* batch-wide tile index, heaviest first */
     const int part = (int)(blockIdx.x % (uint32_t)split);
     const int nblk = TILE_BLOCKS / split;
     const sftg_frame* F = A.frames + A.tile_view[gtile];
@@ -757,20 +757,21 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                     att = att * att;
                     const bool alive = att > 0.f;
                     if (!(__ballot_sync(gmask, alive) & gmask)) continue;
-                    const v3 Ln = vnorm_fast(Lr);
-                    const float ndl = vmax(vdot(N, Ln), 0.f);
-                    const bool lit = (ndl > 0.f) && alive && in_tri;
-                    float msh = 0.f;
+                    v3 Ln = mk3(0.f, 0.f, 0.f);
+                    float ndl = 0.f;
+                    bool lit = false;
+                    if (!lm) {
+                        Ln = vnorm_fast(Lr);
+                        ndl = vmax(vdot(N, Ln), 0.f);
+                        lit = (ndl > 0.f) && alive && in_tri;
+                    }
+                    /* every cached proxy's "between" test first (independent, so they overlap),
+                     * then the block-level skip as the OR over the block's lanes */
                     const int np = s_npc[i];
+                    uint32_t rmask = 0, bmask = 0;
                     if (np > 0) {
-                        const float lrl = fsqrt(d2);
                         const float rd2 = rcpr(d2);   /* loop-invariant: the reference recomputes the same value per proxy */
-                        const float bk = 0.2f, b4 = 0.25f / 0.2f;
-                        /* every proxy's "between" test first (independent, so they overlap), then
-                         * the block-level skip as the OR over the block's lanes, then the smooth-max
-                         * blend over the surviving proxies in index order */
                         const bool want = lm ? in_tri : lit;
-                        uint32_t rmask = 0;
 #pragma unroll 4
                         for (int pi = 0; pi < np; pi++) {
                             const proxy_cache& q = pcache[i * SFTG_MAX_LIGHT_PROXIES + pi];
@@ -780,10 +781,26 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                             const float cd2 = fma_(-wdv, tf, q.wdw);
                             rmask |= (uint32_t)(btw && (cd2 < q.rb2) && want) << pi;
                         }
-                        uint32_t bmask = rmask;
+                        bmask = rmask;
                         bmask |= __shfl_xor_sync(gmask, bmask, 1);
                         bmask |= __shfl_xor_sync(gmask, bmask, 2);
                         bmask |= __shfl_xor_sync(gmask, bmask, 4);
+                    }
+                    if (lm && !bmask) {
+                        /* lightmapped and no proxy shadows the block: si = 1, drop = 0 * att and the
+                         * light leaves lms unchanged, unless att is not finite on a covered lane */
+                        if (!(__ballot_sync(gmask, in_tri && !(att <= 3.402823466e38f)) & gmask)) {
+                            if (shadow_out && S == 1 && ((tri_lanes >> gl) & 1u) && i < 16)
+                                shadow_out[((size_t)gy * W + gx) * 16 + i] = 1.f;
+                            continue;
+                        }
+                    }
+                    if (lm) Ln = vnorm_fast(Lr);
+                    float msh = 0.f;
+                    if (bmask) {
+                        const float lrl = fsqrt(d2);
+                        const float bk = 0.2f, b4 = 0.25f / 0.2f;
+                        /* the smooth-max blend over the surviving proxies in index order */
                         while (bmask) {
                             const int pi = __ffs(bmask) - 1;
                             bmask &= bmask - 1;
@@ -860,6 +877,57 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
             }
         }
     }
+}
+
+/* ---------------------------------------------------------------- tile order
+ * The reference's workers take tiles in descending payload count (sofren2.c:6815-6857) so the
+ * heaviest start first.  Here the same idea keeps the tail of the raster and resolve grids
+ * short: tiles are bucketed by floor(log2(count + 1)) inside their sample-count range and the
+ * launches walk the buckets heaviest first.  Order affects scheduling only, never results. */
+#define ORDER_BUCKETS 32
+
+__device__ __forceinline__ uint32_t order_bucket(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t t) {
+    const int S = frames[tile_view[t]].samples;
+    const uint32_t si = S == 1 ? 0u : (S == 2 ? 1u : 2u);
+    const uint32_t key = 31u - (uint32_t)__clz(tile_count[t] + 1u);          /* 0..31, heavier = larger */
+    return si * ORDER_BUCKETS + (ORDER_BUCKETS - 1u - key);
+}
+
+__global__ void k_order_count(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_view,
+                              const uint32_t* __restrict__ tile_count, uint32_t n_tiles, uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t h[3 * ORDER_BUCKETS];
+    for (int i = threadIdx.x; i < 3 * ORDER_BUCKETS; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n_tiles) atomicAdd(&h[order_bucket(frames, tile_view, tile_count, t)], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * ORDER_BUCKETS; i += blockDim.x) if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void k_order_scatter(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_view,
+                                const uint32_t* __restrict__ tile_count, uint32_t n_tiles, const uint32_t* __restrict__ hist,
+                                uint32_t* __restrict__ cursor, uint32_t* __restrict__ order)
+{
+    __shared__ uint32_t base[3 * ORDER_BUCKETS];
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int i = 0; i < 3 * ORDER_BUCKETS; i++) { base[i] = run; run += hist[i]; }
+    }
+    __syncthreads();
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const uint32_t b = order_bucket(frames, tile_view, tile_count, t);
+    order[base[b] + atomicAdd(&cursor[b], 1u)] = t;
+}
+
+void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
+                            uint32_t* scratch, uint32_t* order, cudaStream_t st) {
+    if (!n_tiles) return;
+    cudaMemsetAsync(scratch, 0, 2 * 3 * ORDER_BUCKETS * sizeof(uint32_t), st);
+    const uint32_t g = (n_tiles + 255) / 256;
+    k_order_count<<<g, 256, 0, st>>>(frames, tile_view, tile_count, n_tiles, scratch);
+    k_order_scatter<<<g, 256, 0, st>>>(frames, tile_view, tile_count, n_tiles, scratch, scratch + 3 * ORDER_BUCKETS, order);
 }
 
 /* ---------------------------------------------------------------- host-side launch helpers */
