@@ -62,6 +62,12 @@ struct sftg_ctx {
     cudaEvent_t ev[6] = { nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
     float timings[5] = { 0, 0, 0, 0, 0 };
     int launches = 0;
+    /* the last batch's launch sequence as an instantiated CUDA graph, replayed while the
+     * batch layout (every pointer, count and knob the launches take) stays the same */
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_key = 0;
+    int graph_launches = 0;
+    bool use_graphs = true;
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
     sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 8 };   /* measured best on the single-view workloads */
@@ -116,6 +122,7 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     for (int i = 0; i < 6; i++) cudaEventCreate(&ctx->ev[i]);
     if (cudaMallocHost((void**)&ctx->h_status, 64) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     sftg_tile_configure(227 * 1024);
+    { const char* e = getenv("SFTG_NO_GRAPHS"); if (e && *e && *e != '0') ctx->use_graphs = false; }
     *out = ctx;
     return SFTG_OK;
 }
@@ -132,6 +139,7 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     for (int i = 0; i < 6; i++) if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -541,37 +549,51 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     return 0;
 }
 
+/* Phase events: inside a stream capture they must become event-record nodes of the graph
+ * (cudaEventRecordExternal) so that replays still time the phases. */
+static cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
+}
+
 static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     const uint32_t n_rec = B.total_ss * 16;
     cudaStream_t st = ctx->stream;
     ctx->launches = 0;
+    CK(cudaGetLastError());   /* nothing pending from earlier calls: every launch below is checked */
     CK(cudaMemsetAsync(B.status, 0, 64, st));
-    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(record_event(ctx->ev[0], st));
     if (B.total_prox) CK(cudaMemsetAsync(B.light_vis, 0, (size_t)B.total_prox * 64, st));   /* columns past the lights stay 0 */
     if (B.total_packets) {
         sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
                               B.pairs, B.n_pairs, B.max_pairs, B.light_vis, B.status, st);
         ctx->launches += 4;
+        CK(cudaGetLastError());
     }
-    CK(cudaEventRecord(ctx->ev[1], st));
+    CK(record_event(ctx->ev[1], st));
     if (B.n_jobs) {
         k_geometry<<<(B.n_jobs + 3) / 4, 128, 0, st>>>(B.frames, B.jobs, B.n_jobs, B.ss, B.recs, B.clip_cnt, B.mrect);
         ctx->launches++;
+        CK(cudaGetLastError());
     }
     if (n_rec) {
         scan_u32(B.clip_cnt, B.clip_base, n_rec, B.scan_tmp, B.totals + 0, st, &ctx->launches);
         k_clip<<<(n_rec + 255) / 256, 256, 0, st>>>(B.frames, B.n_views, B.ss, B.clip_cnt, B.clip_base, B.clips, B.clip_rect, B.mrect, n_rec);
         ctx->launches++;
+        CK(cudaGetLastError());
     } else {
         CK(cudaMemsetAsync(B.totals, 0, 8, st));
     }
-    CK(cudaEventRecord(ctx->ev[2], st));
+    CK(record_event(ctx->ev[2], st));
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
     scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ctx->launches);
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
     sftg_launch_tile_order(B.frames, B.tile_view, B.tile_count, B.total_tiles, B.order_scratch, B.tile_order, st);
     ctx->launches += 4;
-    CK(cudaEventRecord(ctx->ev[3], st));
+    CK(cudaGetLastError());
+    CK(record_event(ctx->ev[3], st));
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));
     sftg_tile_args A;
     A.frames = B.frames; A.tile_view = B.tile_view; A.ss = B.ss; A.clips = B.clips; A.clip_base = B.clip_base;
@@ -580,11 +602,58 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
     for (int si = 0; si < 3; si++)
         if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], st, A); ctx->launches++; }
-    CK(cudaEventRecord(ctx->ev[4], st));
+    CK(cudaGetLastError());
+    CK(record_event(ctx->ev[4], st));
     for (int si = 0; si < 3; si++)
         if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ctx->launches++; }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev[5], st));
+    CK(record_event(ctx->ev[5], st));
+    return 0;
+}
+
+static uint64_t fnv(uint64_t h, const void* p, size_t n) {
+    const unsigned char* c = (const unsigned char*)p;
+    for (size_t i = 0; i < n; i++) { h ^= c[i]; h *= 1099511628211ull; }
+    return h;
+}
+
+/* Every value launch_batch passes to a launch: arena pointers, counts, ranges and knobs. */
+static uint64_t batch_key(const sftg_ctx* ctx, const batch_bufs& B) {
+    uint64_t h = 1469598103934665603ull;
+    const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.ss, B.recs, B.clip_cnt, B.clip_base,
+                           B.mrect, B.clips, B.clip_rect, B.tile_count, B.tile_start, B.tile_order, B.order_scratch, B.tile_pay,
+                           B.light_vis, B.packets, B.pairs, B.n_pairs, B.scan_tmp, B.status, B.totals, B.vis, B.zrange,
+                           B.vis_depth, B.vis_id, B.shadow };
+    h = fnv(h, ptrs, sizeof(ptrs));
+    const uint32_t cnt[] = { B.max_pairs, B.n_views, B.total_ss, B.n_jobs, B.total_tiles, B.total_prox, B.total_packets, B.max_inst,
+                             B.s_tile0[0], B.s_tile0[1], B.s_tile0[2], B.s_tiles[0], B.s_tiles[1], B.s_tiles[2] };
+    h = fnv(h, cnt, sizeof(cnt));
+    h = fnv(h, &B.color_total, sizeof(B.color_total));
+    h = fnv(h, &ctx->tuning, sizeof(ctx->tuning));
+    return h;
+}
+
+/* launch_batch through a CUDA graph: captured on the first batch of a layout, replayed after. */
+static int launch_batch_graph(sftg_ctx* ctx, const batch_bufs& B) {
+    const uint64_t key = batch_key(ctx, B);
+    if (!ctx->graph || key != ctx->graph_key) {
+        if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = launch_batch(ctx, B);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return rc ? rc : set_err(ctx, SFTG_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&ctx->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) { ctx->graph = nullptr; return set_err(ctx, SFTG_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ie)); }
+        ctx->graph_key = key;
+        ctx->graph_launches = ctx->launches;
+    }
+    CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    ctx->launches = ctx->graph_launches;
     return 0;
 }
 
@@ -604,7 +673,7 @@ static int batch_common(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, 
             if (!fds[v].clear && host_color && host_color[v])
                 CK(cudaMemcpy2DAsync(ctx->d_color + B.plan[v].color_off, (size_t)fds[v].width * 4, host_color[v], pitch_of(v),
                                      (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyHostToDevice, ctx->stream));
-        if ((rc = launch_batch(ctx, B))) return rc;
+        if ((rc = (dbg || !ctx->use_graphs) ? launch_batch(ctx, B) : launch_batch_graph(ctx, B))) return rc;
         CK(cudaMemcpyAsync(ctx->h_status, B.status, 4, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaMemcpyAsync(ctx->h_status + 2, B.totals, 8, cudaMemcpyDeviceToHost, ctx->stream));
         for (uint32_t v = 0; v < nv; v++)
@@ -618,7 +687,11 @@ static int batch_common(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, 
             while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
             continue;
         }
-        for (int k = 0; k < 5; k++) { float t = 0.f; cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]); ctx->timings[k] = t; }
+        for (int k = 0; k < 5; k++) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]) != cudaSuccess) { t = 0.f; cudaGetLastError(); }
+            ctx->timings[k] = t;
+        }
         if (dbg) {
             const sftg_frame_desc* fd = &fds[0];
             const int W = fd->width, H = fd->height, S = fd->samples, tiles = (int)B.total_tiles;
