@@ -79,7 +79,7 @@ typedef struct sftg_frame_desc {
     float view_proj[16];
     float frustum_n[6][3], frustum_d[6];     /* normalised planes (sft_set_camera) */
     float ambient[3], lightmap_brightness;
-    uint32_t clear, clear_color, shadows, debug_mode;
+    uint32_t clear, clear_color, shadows, debug_mode;   /* debug_mode: enum sft_debug_mode (sofren2.c:59-67) */
     uint32_t n_point;
     const float* point_lights;               /* per light: pos[3], color[3] (rgb * intensity), radius, 1/radius^2 */
     uint32_t n_dir;
@@ -90,6 +90,7 @@ typedef struct sftg_frame_desc {
     const float* proxies;                    /* per world proxy: posa[3], posb[3], radius, pad */
     const void* tlas_nodes;                  /* sft_bvh_node images built on the host */
     uint32_t tlas_count, tlas_root;
+    int32_t debug_texture;                   /* texture of SFT_DEBUG_CHECKERBOARD (the base material's albedo) */
 } sftg_frame_desc;
 
 /* optional per-frame outputs for parity checks (any pointer may be NULL; host memory) */

@@ -282,6 +282,7 @@ static struct sft__state {
     u32* mat_gen; i32* mat_next; i32 mat_cap, mat_free;
     i32 n_transient;
     sft_mat_handle base_mat;
+    sft_tex_handle checker_tex;    /* the base material's albedo, for SFT_DEBUG_CHECKERBOARD */
     sftg_debug_out* debug;
     char err[512];
     /* batched submission: frames recorded by sft_present between sft_batch_begin / _submit */
@@ -484,6 +485,7 @@ SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads) {
     const sft_tex_handle checker = sft_texture_create(256, 256, px);
     free(px);
     sft__s->base_mat = sft_material_create(checker, 0xFFFFFFFFu, 2.f);
+    sft__s->checker_tex = checker;
     SFT__LOG("initialized GPU renderer %dx%d, %d sample(s)\n", width, height, sft__s->samples);
 }
 
@@ -891,6 +893,7 @@ SFT_FUNC void sft_present(void) {
     fd.ambient[0] = s->ambient.x; fd.ambient[1] = s->ambient.y; fd.ambient[2] = s->ambient.z;
     fd.lightmap_brightness = s->lightmap_brightness;
     fd.clear = s->clear; fd.clear_color = s->clear_color; fd.shadows = s->shadows; fd.debug_mode = (u32)s->debug_mode;
+    fd.debug_texture = sft__tex_device(s->checker_tex);
     fd.n_point = s->n_point; fd.point_lights = s->point;
     fd.n_dir = s->n_dir; fd.dir_lights = s->dir;
     fd.n_instances = s->n_inst; fd.instances = s->inst;

@@ -16,6 +16,7 @@
  *   present_ns                   wall time of sft_present
  *
  * usage: ref_harness <scene.sfts> <out.dump> [frame_index=-1 (all)] [threads=1] [repeat=1]
+ * SFT_DEBUG_MODE=<n> in the environment selects a debug view (sft_set_debug_mode).
  * The MSAA sample count is fixed at compile time (SFT_USE_AA / SFT_AA_SAMPLES), as in the reference.
  */
 #define _GNU_SOURCE
@@ -203,6 +204,7 @@ int main(int argc, char** argv) {
     if (!sc.n_frames) return 4;
 
     sft_init((i32)sc.frames[0].width, (i32)sc.frames[0].height, threads);
+    if (getenv("SFT_DEBUG_MODE")) sft_set_debug_mode((enum sft_debug_mode)atoi(getenv("SFT_DEBUG_MODE")));
     sft_tex_handle* texs = (sft_tex_handle*)calloc(sc.n_textures + 1, sizeof(sft_tex_handle));
     for (u32 i = 0; i < sc.n_textures; i++) texs[i] = sft_texture_create((i32)sc.textures[i].w, (i32)sc.textures[i].h, sc.textures[i].argb);
     sft_mat_handle* mats = (sft_mat_handle*)calloc(sc.n_materials + 1, sizeof(sft_mat_handle));

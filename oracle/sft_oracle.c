@@ -402,6 +402,8 @@ typedef struct {
     f32* depth; u32* vid;        /* per tile buffers, S * 4096 each, all tiles */
     u32* color;
     mat4* inst_T; const mat4** inst_bones;
+    int debug_mode;              /* enum sft_debug_mode (sofren2.c:59-67) */
+    otex checker;                /* the base material's 256x256 checkerboard (sofren2.c:8062-8080) */
 } octx;
 
 static void list_push(olist* l, u64 v) {
@@ -1087,6 +1089,42 @@ typedef struct { vec3 pa, pb, ab, W; f32 abdab, wdw, rb2, pr, pr2, vis_mult; } o
 
 static const otex* tex_of(const octx* c, u32 tex_index_plus1) { return tex_index_plus1 ? &c->tex[tex_index_plus1 - 1] : NULL; }
 
+/* tile overlays of the debug views, drawn after the tile's resolve (sft__debug_draw_tile_overlay,
+ * 5731-5807); depth is the tile's sample-0 depth plane */
+static u32 half_blend(u32 bg, u32 ov) { return ((bg & 0xFEFEFEFEu) >> 1) + ((ov & 0xFEFEFEFEu) >> 1); }
+
+static void debug_overlay(octx* c, i32 tmx, i32 tmy, i32 lim_x, i32 lim_y, f32 zmin, f32 zmax, i32 ntl, const f32* depth) {
+    const i32 W = c->W;
+    if (c->debug_mode == 2) {
+        for (i32 y = tmy; y < lim_y; y++)
+            for (i32 x = tmx; x < lim_x; x++) {
+                u32* p = &c->color[y * W + x];
+                if (x == tmx || x == lim_x - 1 || y == tmy || y == lim_y - 1) *p = 0xFF00FF00u;
+                else if ((x % 16 == 0) || (y % 16 == 0)) *p = half_blend(*p, 0xFF004400u);
+            }
+    } else if (c->debug_mode == 3) {
+        f32 dd = 0.f;
+        if (zmin <= zmax && zmin > EPS) { const f32 near_w = 1.f / zmax, far_w = 1.f / zmin; dd = far_w - near_w; }
+        const u32 border = dd > 16.f ? 0xFFFF0000u : 0xFF00FF00u;
+        for (i32 y = tmy; y < lim_y; y++)
+            for (i32 x = tmx; x < lim_x; x++) {
+                u32* p = &c->color[y * W + x];
+                if (x == tmx || x == lim_x - 1 || y == tmy || y == lim_y - 1) { *p = border; continue; }
+                const f32 iw = depth[(y - tmy) * TILE + (x - tmx)];
+                if (iw <= EPS) continue;
+                const f32 lz = 1.f / iw;
+                const f32 q = lz / 100.f;
+                const f32 nz = q < 0.f ? 0.f : (q > 1.f ? 1.f : q);
+                const u32 it = (u32)(nz * 255.f);
+                *p = 0xFF000000u | (it << 16) | (it << 8) | it;
+            }
+    } else {
+        const u32 heat = ntl == 0 ? 0xFF222288u : (ntl < 4 ? 0xFF00FF00u : 0xFFFF0000u);
+        for (i32 y = tmy; y < lim_y; y++)
+            for (i32 x = tmx; x < lim_x; x++) c->color[y * W + x] = half_blend(c->color[y * W + x], heat);
+    }
+}
+
 /* sft__resolve_tile (5809-6753) */
 static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f32* shadow_out) {
     const sfts_frame* f = c->f;
@@ -1237,6 +1275,7 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
                 const f32 dx1 = T.sx[1] - T.sx[0], dx2 = T.sx[2] - T.sx[0], dy1 = T.sy[1] - T.sy[0], dy2 = T.sy[2] - T.sy[0];
                 const f32 idet = rcpr(dx1 * dy2 - dx2 * dy1);
                 f32 cu[8], cv[8], clu[8], clv[8]; vec3 P[8], N[8], V[8];
+                f32 BU[8], BV[8], BW[8];   /* kept for the wireframe view */
                 for (int l = 0; l < 8; l++) {
                     const f32 pxs = pxf[l] - T.sx[0], pys = pyf[l] - T.sy[0];
                     const f32 rbu = (pxs * dy2 - pys * dx2) * idet;
@@ -1248,6 +1287,7 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
                         const f32 bs = rcpr(bu + (bv + bw));
                         bu = bu * bs; bv = bv * bs; bw = bw * bs;
                     }
+                    BU[l] = bu; BV[l] = bv; BW[l] = bw;
                     const f32 iz = fmaf(bw, T.iw[0], fmaf(bu, T.iw[1], bv * T.iw[2]));
                     const f32 z = rcpr(iz);
                     const f32 w0 = (bw * T.iw[0]) * z, w1 = (bu * T.iw[1]) * z, w2 = (bv * T.iw[2]) * z;
@@ -1266,6 +1306,7 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
                     const omat* mt = &c->mats[sm->material];
                     base = mt->base; shin = mt->shin; tx = mt->tex >= 0 ? &c->tex[mt->tex] : NULL;
                 }
+                if (c->debug_mode == 5) { tx = &c->checker; base = 0xFFFFFFFFu; }   /* checkerboard view (6373-6376) */
                 const f32 i255 = 1.f / 255.f;
                 const f32 br_ = (f32)((base >> 16) & 0xFF) * i255, bg_ = (f32)((base >> 8) & 0xFF) * i255, bb_ = (f32)(base & 0xFF) * i255;
                 /* D7 LOD (5501-5541) from the first lane holding the triangle */
@@ -1416,6 +1457,15 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
                         }
                     }
                 }
+                if (c->debug_mode == 1) {   /* wireframe view (6645-6671): edges where a barycentric is under its screen-space width */
+                    const f32 dbu_dx = (0.f - dy2) * idet, dbu_dy = dx2 * idet;
+                    const f32 dbv_dx = dy1 * idet, dbv_dy = (0.f - dx1) * idet;
+                    const f32 fw_u = fabsf(dbu_dx) + fabsf(dbu_dy), fw_v = fabsf(dbv_dx) + fabsf(dbv_dy);
+                    const f32 dbw_dx = 0.f - (dbu_dx + dbv_dx), dbw_dy = 0.f - (dbu_dy + dbv_dy);
+                    const f32 fw_w = fabsf(dbw_dx) + fabsf(dbw_dy);
+                    for (int l = 0; l < 8; l++)
+                        if (BU[l] < fw_u || BV[l] < fw_v || BW[l] < fw_w) { out[0][l] = 0.f; out[1][l] = 1.f; out[2][l] = 0.f; }
+                }
                 if (S == 1) {
                     for (u32 a = tri_lanes; a; a &= a - 1) {
                         const i32 l = ctz32(a);
@@ -1444,6 +1494,7 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
             }
         }
     }
+    if (c->debug_mode >= 2 && c->debug_mode <= 4) debug_overlay(c, tmx, tmy, lim_x, lim_y, zmin, zmax, ntl, depth);
 }
 
 /* ------------------------------------------------------------ driver */
@@ -1615,6 +1666,13 @@ static int load_scene(octx* c, const sfts_scene* sc) {
             }
         blas_build(m);
     }
+    {   /* the checkerboard of sft_init (8062-8080): 32x32 squares */
+        u32* px = (u32*)malloc(256 * 256 * 4);
+        for (i32 y = 0, i = 0; y < 256; y++)
+            for (i32 x = 0; x < 256; x++, i++) px[i] = (((x / 32) % 2) ^ ((y / 32) % 2)) ? 0xFFAFFFAFu : 0xFF555555u;
+        tex_create(&c->checker, 256, 256, px);
+        free(px);
+    }
     return 0;
 }
 
@@ -1657,6 +1715,14 @@ int sfto_light_vis(void* hp, uint8_t* out, uint32_t cap_proxies) {
     const u32 n = h->c.nprox < cap_proxies ? h->c.nprox : cap_proxies;
     for (u32 p = 0; p < n; p++) memcpy(out + 64 * p, h->c.prox[p].vis, 64);
     return (int)h->c.nprox;
+}
+
+/* enum sft_debug_mode for the following renders (0 = none) */
+int sfto_set_debug_mode(void* hp, int mode) {
+    oracle_handle* h = (oracle_handle*)hp;
+    if (!h || mode < 0 || mode > 5) return -1;
+    h->c.debug_mode = mode;
+    return 0;
 }
 
 void sfto_close(void* hp) { free(hp); }

@@ -301,6 +301,8 @@ struct batch_bufs {
     sftg_clip_tri* clips; int4* clip_rect;
     uint32_t* tile_count; uint32_t* tile_start;
     uint32_t* tile_order; uint32_t* order_scratch;
+    uint8_t* tile_nlights;   /* per tile: its light list length (debug views) */
+    bool any_overlay;        /* a view asks for a tile overlay (debug modes 2-4) */
     uint64_t* tile_pay;
     uint8_t* light_vis;
     void* packets; uint2* pairs; uint32_t* n_pairs; uint32_t max_pairs;
@@ -430,7 +432,8 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     auto acc = [&](size_t bytes) { need = ((need + 255) & ~(size_t)255) + bytes; };
     acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
-    acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(1024); acc(ctx->tile_cap * 8);
+    acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(1024); acc(total_tiles + 16);
+    acc(ctx->tile_cap * 8);
     acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
     acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
     acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
@@ -467,6 +470,9 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     B.tile_start = bp.take<uint32_t>(total_tiles);
     B.tile_order = bp.take<uint32_t>(total_tiles);
     B.order_scratch = bp.take<uint32_t>(256);
+    B.tile_nlights = bp.take<uint8_t>((size_t)total_tiles + 16);
+    B.any_overlay = false;
+    for (uint32_t v = 0; v < nv; v++) if (fds[v].debug_mode >= 2 && fds[v].debug_mode <= 4) B.any_overlay = true;
     B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
     B.light_vis = bp.take<uint8_t>((size_t)total_prox * 64 + 64);
     B.packets = bp.take<char>((size_t)total_packets * sftg_packet_bytes() + 64);
@@ -497,6 +503,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
         F->hw = (float)W * 0.5f; F->hh = (float)H * 0.5f; F->vpx = 0.f; F->vpy = 0.f;
         F->cols = (W + 63) / 64; F->rows = (H + 63) / 64; F->tiles = (int32_t)P.tiles; F->debug_mode = (int32_t)fd->debug_mode;
         F->clear = fd->clear; F->clear_color = fd->clear_color; F->shadows = fd->shadows;
+        F->debug_tex = fd->debug_texture;
         memcpy(F->cam, fd->cam_pos, 12);
         memcpy(F->vp, fd->view_proj, 64);
         for (int p = 0; p < 6; p++) {
@@ -597,7 +604,7 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));
     sftg_tile_args A;
     A.frames = B.frames; A.tile_view = B.tile_view; A.ss = B.ss; A.clips = B.clips; A.clip_base = B.clip_base;
-    A.tile_order = B.tile_order;
+    A.tile_order = B.tile_order; A.tile_nlights = B.tile_nlights;
     A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
     for (int si = 0; si < 3; si++)
@@ -606,6 +613,7 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     CK(record_event(ctx->ev[4], st));
     for (int si = 0; si < 3; si++)
         if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ctx->launches++; }
+    if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ctx->launches++; }
     CK(cudaGetLastError());
     CK(record_event(ctx->ev[5], st));
     return 0;
@@ -620,7 +628,9 @@ static uint64_t fnv(uint64_t h, const void* p, size_t n) {
 /* Every value launch_batch passes to a launch: arena pointers, counts, ranges and knobs. */
 static uint64_t batch_key(const sftg_ctx* ctx, const batch_bufs& B) {
     uint64_t h = 1469598103934665603ull;
-    const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.ss, B.recs, B.clip_cnt, B.clip_base,
+    const uint32_t ov = B.any_overlay ? 1u : 0u;
+    h = fnv(h, &ov, sizeof(ov));
+    const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights,
                            B.mrect, B.clips, B.clip_rect, B.tile_count, B.tile_start, B.tile_order, B.order_scratch, B.tile_pay,
                            B.light_vis, B.packets, B.pairs, B.n_pairs, B.scan_tmp, B.status, B.totals, B.vis, B.zrange,
                            B.vis_depth, B.vis_id, B.shadow };

@@ -25,6 +25,7 @@ struct sftg_tile_args {
     const sftg_clip_tri* clips;
     const uint32_t* clip_base;     /* exclusive scan of clip counts: a view's first slot is clip_base[ss_base * 16] */
     const uint32_t* tile_order;    /* launch order of the tiles (heaviest first within each sample count) */
+    uint8_t* tile_nlights;         /* per tile: light list length, written by the resolve for the debug overlays */
     const uint32_t* tile_start;
     const uint32_t* tile_count;
     const uint64_t* tile_pay;
@@ -61,5 +62,7 @@ void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view,
 /* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4, 8 or 16) */
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A);
 void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A);
+/* tile overlays of the debug views 2-4 (sft__debug_draw_tile_overlay), after every resolve */
+void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
 
 #define SFTG_SCAN_ELEMS_PER_BLOCK 4096

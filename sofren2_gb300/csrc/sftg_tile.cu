@@ -460,7 +460,10 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                 n = min(SFTG_MAX_TILE_LIGHTS, n + __popc(bal));
             }
         }
-        if (lane == 0) s_nlights = n;
+        if (lane == 0) {
+            s_nlights = n;
+            if (part == 0) A.tile_nlights[gtile] = (uint8_t)n;
+        }
     }
     __syncthreads();
     const int ntl = s_nlights;
@@ -692,6 +695,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
             /* material (6350-6382) */
             uint32_t base = 0xFFFFFFFFu; int ti = -1; float shin = 4.f;
             if (info.material >= 0) { const sftg_mat mt = F->mats[info.material]; base = mt.base_color; ti = mt.tex; shin = mt.shininess; }
+            if (F->debug_mode == 5) { ti = F->debug_tex; base = 0xFFFFFFFFu; }   /* checkerboard view (6373-6376) */
             const float i255 = 1.f / 255.f;
             const float bcol[3] = { (float)((base >> 16) & 0xFF) * i255, (float)((base >> 8) & 0xFF) * i255, (float)(base & 0xFF) * i255 };
             /* D7 LOD from the first covered lane's derivatives (5501-5541) */
@@ -854,6 +858,14 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                     out[0] = fma_(out[0], dif[0], spc[0]); out[1] = fma_(out[1], dif[1], spc[1]); out[2] = fma_(out[2], dif[2], spc[2]);
                 }
             }
+            if (F->debug_mode == 1) {   /* wireframe view (6645-6671): edges where a barycentric is under its screen width */
+                const float dbu_dx = (0.f - dy2) * idet, dbu_dy = dx2 * idet;
+                const float dbv_dx = dy1 * idet, dbv_dy = (0.f - dx1) * idet;
+                const float fw_u = fabsf(dbu_dx) + fabsf(dbu_dy), fw_v = fabsf(dbv_dx) + fabsf(dbv_dy);
+                const float dbw_dx = 0.f - (dbu_dx + dbv_dx), dbw_dy = 0.f - (dbu_dy + dbv_dy);
+                const float fw_w = fabsf(dbw_dx) + fabsf(dbw_dy);
+                if (bu < fw_u || bv < fw_v || bw < fw_w) { out[0] = 0.f; out[1] = 1.f; out[2] = 0.f; }
+            }
             if (S == 1) {
                 if ((tri_lanes >> gl) & 1u) {
                     uint32_t px = 0xFF000000u;
@@ -928,6 +940,62 @@ void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view,
     const uint32_t g = (n_tiles + 255) / 256;
     k_order_count<<<g, 256, 0, st>>>(frames, tile_view, tile_count, n_tiles, scratch);
     k_order_scatter<<<g, 256, 0, st>>>(frames, tile_view, tile_count, n_tiles, scratch, scratch + 3 * ORDER_BUCKETS, order);
+}
+
+/* ---------------------------------------------------------------- debug overlays
+ * sft__debug_draw_tile_overlay (5731-5807): tile borders and a 16-pixel grid (view 2), sample-0
+ * linear depth with a border coloured by the tile's depth span (view 3), a heat tint from the
+ * tile's light count (view 4).  One CTA per tile, after every tile has been resolved; each
+ * overlay touches only its own tile, as in the reference where it follows that tile's resolve. */
+__device__ __forceinline__ uint32_t half_blend(uint32_t bg, uint32_t ov) { return ((bg & 0xFEFEFEFEu) >> 1) + ((ov & 0xFEFEFEFEu) >> 1); }
+
+__global__ void __launch_bounds__(256) k_debug_overlay(const sftg_tile_args A)
+{
+    const uint32_t gtile = blockIdx.x;
+    const sftg_frame* F = A.frames + A.tile_view[gtile];
+    const int mode = F->debug_mode;
+    if (mode < 2 || mode > 4) return;
+    const int tile = (int)(gtile - F->tile_base);
+    const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
+    const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
+    const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
+    uint32_t* color = F->color_dev;
+    const int W = F->width;
+    const float2* depth = A.vis + F->vis_base + (size_t)tile * F->samples * SFTG_TILE_PX;   /* sample 0 plane first */
+    const float2 zr = A.zrange[gtile];
+    const int ntl = A.tile_nlights[gtile];
+    uint32_t border = 0xFF00FF00u, heat = 0;
+    if (mode == 3) {
+        float dd = 0.f;
+        if (zr.x <= zr.y && zr.x > 1e-6f) { const float near_w = fdiv(1.f, zr.y), far_w = fdiv(1.f, zr.x); dd = far_w - near_w; }
+        border = dd > 16.f ? 0xFFFF0000u : 0xFF00FF00u;
+    }
+    if (mode == 4) heat = ntl == 0 ? 0xFF222288u : (ntl < 4 ? 0xFF00FF00u : 0xFFFF0000u);
+    for (int i = threadIdx.x; i < SFTG_TILE_PX; i += blockDim.x) {
+        const int x = tmx + (i & (SFTG_TILE - 1)), y = tmy + (i >> 6);
+        if (x >= lim_x || y >= lim_y) continue;
+        uint32_t* p = &color[(size_t)y * W + x];
+        const bool edge = x == tmx || x == lim_x - 1 || y == tmy || y == lim_y - 1;
+        if (mode == 2) {
+            if (edge) *p = 0xFF00FF00u;
+            else if ((x % 16 == 0) || (y % 16 == 0)) *p = half_blend(*p, 0xFF004400u);
+        } else if (mode == 3) {
+            if (edge) { *p = border; continue; }
+            const float iw = depth[i].x;
+            if (iw <= 1e-6f) continue;
+            const float lz = fdiv(1.f, iw);
+            const float q = fdiv(lz, 100.f);
+            const float nz = q < 0.f ? 0.f : (q > 1.f ? 1.f : q);
+            const uint32_t it = (uint32_t)(nz * 255.f);
+            *p = 0xFF000000u | (it << 16) | (it << 8) | it;
+        } else {
+            *p = half_blend(*p, heat);
+        }
+    }
+}
+
+void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
+    if (tiles) k_debug_overlay<<<tiles, 256, 0, st>>>(A);
 }
 
 /* ---------------------------------------------------------------- host-side launch helpers */

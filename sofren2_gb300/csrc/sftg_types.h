@@ -122,7 +122,8 @@ typedef struct sftg_frame {
     float ambient[3], lightmap_brightness;
     uint32_t n_point, n_dir, n_proxies, n_inst;
     uint32_t total_ss, n_jobs, tlas_root, tlas_count;
-    uint32_t clip_cap, tile_cap, pad3[2];        /* capacities of the clip pool and tile payload buffer */
+    uint32_t clip_cap, tile_cap;                 /* capacities of the clip pool and tile payload buffer */
+    int32_t debug_tex, pad3;                     /* checkerboard texture of the debug view */
     /* where this view's rows start in the batch-wide arrays (all 0 for a single frame) */
     uint32_t view, ss_base;        /* screen-space cache slot; batch records start at ss_base * 16 */
     uint32_t tile_base, prox_base; /* global tile index; global proxy index (light_vis rows) */

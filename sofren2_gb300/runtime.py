@@ -46,7 +46,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sft_get_frame_timings": (v, [p]), "sftx_scene_load": (p, [p, u64]), "sftx_scene_free": (v, [p]),
         "sftx_scene_frame_count": (u32, [p]), "sftx_scene_render": (i32, [p, u32, p, i32]),
         "sftx_scene_frame_size": (u32, [p, u32, p, p]), "sft_get_launch_count": (i32, []),
-        "sft_get_cuda_stream": (p, []),
+        "sft_get_cuda_stream": (p, []), "sft_set_debug_mode": (v, [i32]),
         "sftx_scene_render_batch": (i32, [p, p, p, u32, p, p]),
         "sftx_scene_autotune_batch": (i32, [p, p, p, u32, i32]),
         "sftx_scene_render_ex": (i32, [p, u32, p, i32, u32]),
@@ -106,6 +106,10 @@ class Renderer:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_debug_mode(self, mode: int):
+        """enum sft_debug_mode: 0 none, 1 wireframe, 2 tiles, 3 depth, 4 light count, 5 checkerboard."""
+        self.lib.sft_set_debug_mode(mode)
 
     def set_samples(self, samples: int):
         self.lib.sft_set_msaa_samples(samples)

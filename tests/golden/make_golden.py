@@ -30,7 +30,7 @@ def main(names: list[str]) -> None:
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={ref_dir}"], check=True)
     path = os.path.join(HERE, "golden.json")
     golden = json.load(open(path)) if os.path.exists(path) else {}
-    for name in names or list(gc.CASES):
+    for name in [n for n in names if n in gc.CASES] if names else list(gc.CASES):
         blob = gc.blob(name)
         entry = {"generator": gc.CASES[name][0], "kwargs": gc.CASES[name][1], "scene_sha256": gc.sha(memoryview(blob)),
                  "samples": {}}
@@ -42,6 +42,14 @@ def main(names: list[str]) -> None:
             entry["samples"][str(S)] = d
             print(name, S, "payloads", int(frame["tile_counts"].sum()), "clips", d["clip_used"], flush=True)
         golden[name] = entry
+    if not names or "debug" in names:
+        # colour digests of the debug views (sft_set_debug_mode through SFT_DEBUG_MODE)
+        dbg = {}
+        for name, mode, S in gc.DEBUG_CASES:
+            frame = reference_dump(gc.blob(name), S, debug_mode=mode)[0]
+            dbg[f"{name}/{mode}/{S}"] = gc.sha(frame["color"])
+            print("debug", name, mode, S, flush=True)
+        golden["debug_views"] = dbg
     json.dump(golden, open(path, "w"), indent=1, sort_keys=True)
 
 

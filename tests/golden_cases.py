@@ -25,6 +25,8 @@ CASES = {
 # cases the CPU oracle re-checks in the default (not-gpu) test run; the big configurations are
 # checked on the GPU against their digests, and against the oracle in the slow tier
 FAST = ["small", "config1", "skinned_small", "atrium_small", "variety", "variety_noclear"]
+# debug views (enum sft_debug_mode 1..5) over a few cases: (case, mode, samples)
+DEBUG_CASES = [(n, m, S) for n in ("small", "variety", "atrium_small") for m in (1, 2, 3, 4, 5) for S in (1, 4)]
 SAMPLES = {name: (1, 2, 4) for name in CASES}
 SAMPLES["config2"] = (2,)
 SAMPLES["config3"] = (4,)

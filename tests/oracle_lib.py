@@ -37,6 +37,7 @@ def lib():
         L.sfto_render.argtypes = [C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_char_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]
         L.sfto_close.restype, L.sfto_close.argtypes = None, [C.c_void_p]
+        L.sfto_set_debug_mode.restype, L.sfto_set_debug_mode.argtypes = C.c_int, [C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -47,6 +48,10 @@ class Oracle:
         self.h = lib().sfto_open(self._buf.ctypes.data_as(C.c_void_p), len(blob))
         if not self.h:
             raise RuntimeError("oracle rejected the scene blob")
+
+    def set_debug_mode(self, mode: int) -> None:
+        if lib().sfto_set_debug_mode(self.h, mode) != 0:
+            raise ValueError(f"bad debug mode {mode}")
 
     def close(self):
         if self.h:
@@ -85,10 +90,11 @@ def reference_available(samples: int) -> bool:
     return os.path.exists(os.path.join(REF_DIR, f"ref_harness_{samples}x"))
 
 
-def reference_dump(blob: bytes, samples: int, frame: int = -1) -> list[dict]:
+def reference_dump(blob: bytes, samples: int, frame: int = -1, debug_mode: int = 0) -> list[dict]:
     with tempfile.TemporaryDirectory() as td:
         sp, dp = os.path.join(td, "s.sfts"), os.path.join(td, "r.dump")
         open(sp, "wb").write(blob)
+        env = dict(os.environ, SFT_DEBUG_MODE=str(debug_mode))
         subprocess.run([os.path.join(REF_DIR, f"ref_harness_{samples}x"), sp, dp, str(frame)], check=True,
-                       stdout=subprocess.DEVNULL)
+                       stdout=subprocess.DEVNULL, env=env)
         return read_dump(dp)

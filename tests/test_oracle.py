@@ -75,3 +75,18 @@ def test_oracle_detects_undefined_packet_frustum():
         assert o.render_dump(0, 1)["invalid_packets"] > 0
     finally:
         o.close()
+
+
+@pytest.mark.parametrize("case", gc.DEBUG_CASES, ids=lambda c: f"{c[0]}-{c[1]}-{c[2]}x")
+def test_oracle_debug_views_match_reference(golden, case):
+    """Debug views (wireframe, tile grid, depth, light count, checkerboard) against the
+    reference's own renders with sft_set_debug_mode."""
+    name, mode, S = case
+    sc = gc.scene(name)
+    o = Oracle(gc.blob(name))
+    try:
+        o.set_debug_mode(mode)
+        color, _, _ = o.render_color(0, S, sc.frames[0].width, sc.frames[0].height)
+    finally:
+        o.close()
+    assert gc.sha(color) == golden["debug_views"][f"{name}/{mode}/{S}"]
