@@ -154,14 +154,17 @@ int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_
 #define SFTG_NOALLOC_SCRATCH_BYTES (4u << 20)
 int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* frame, uint8_t* light_vis);
 
-/* Scheduling knobs.  None of them changes a result: they set how the same work is cut into
- * CTAs and warps.  No counterpart in the reference (its SIMD width and tile size are fixed;
+/* Scheduling knobs.  None but occl_ray_prune changes a result: they set how the same work is cut
+ * into CTAs and warps.  No counterpart in the reference (its SIMD width and tile size are fixed;
  * the 64x64 tile stays fixed here too, because the per-tile payload lists are part of the
  * render path's observable output). */
 typedef struct sftg_tuning {
     int32_t resolve_split[3];     /* resolve CTAs per 64x64 tile at 1x, 2x, 4x: 1, 2, 4, 8 or 16 (default 16, 8, 16) */
     int32_t raster_slab_rows[3];  /* tile rows per raster work item at 1x, 2x, 4x: 4..64 (default 8, 8, 4) */
     int32_t geom_job_width;       /* meshlets per geometry warp: 1..8 (default 8, the reference's job) */
+    int32_t occl_ray_prune;       /* 1: also cull BLAS children no unblocked shadow ray reaches (faster; can differ
+                                     from the reference only where a ray grazes a triangle's plane); default 0.
+                                     The only knob that is not result-neutral: sftg_autotune leaves it as set */
 } sftg_tuning;
 int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out);
 int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* tuning);

@@ -70,7 +70,7 @@ struct sftg_ctx {
     bool use_graphs = true;
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
-    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 8 };   /* measured best on the single-view workloads */
+    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 8, 0 };   /* measured best on the single-view workloads */
 };
 
 static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
@@ -575,7 +575,8 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     if (B.total_prox) CK(cudaMemsetAsync(B.light_vis, 0, (size_t)B.total_prox * 64, st));   /* columns past the lights stay 0 */
     if (B.total_packets) {
         sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
-                              B.pairs, B.n_pairs, B.max_pairs, B.light_vis, B.status, st);
+                              B.pairs, B.n_pairs, B.max_pairs, SFTG_OCC_ITEMS_PER_PAIR, B.light_vis, B.status,
+                              ctx->tuning.occl_ray_prune, st);
         ctx->launches += 4;
         CK(cudaGetLastError());
     }
@@ -746,7 +747,7 @@ static bool tuning_valid(const sftg_tuning* t) {
         if (!(sp == 1 || sp == 2 || sp == 4 || sp == 8 || sp == 16)) return false;
         if (sl < 4 || sl > 64) return false;
     }
-    return t->geom_job_width >= 1 && t->geom_job_width <= 8;
+    return t->geom_job_width >= 1 && t->geom_job_width <= 8 && (t->occl_ray_prune == 0 || t->occl_ray_prune == 1);
 }
 
 extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
@@ -872,7 +873,7 @@ extern "C" int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* fd, 
     const size_t o_F = take(sizeof(sftg_frame)), o_inst = take((uint64_t)(fd->n_instances + 1) * sizeof(sftg_inst));
     const size_t o_pl = take((uint64_t)lc * sizeof(sftg_point_light)), o_px = take((uint64_t)np * sizeof(sftg_proxy));
     const size_t o_tl = take((uint64_t)fd->tlas_count * 256), o_pk = take((uint64_t)n_packets * sftg_packet_bytes());
-    const size_t o_pr = take(max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) * 8 + 8), o_np = take(16), o_st = take(16), o_lv = take((uint64_t)np * 64);
+    const size_t o_pr = take(max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR_NOALLOC) * 8 + 8), o_np = take(16), o_st = take(16), o_lv = take((uint64_t)np * 64);
     const size_t o_pv = take((uint64_t)n_packets * 2), o_xv = take((uint64_t)np * 2);
     if (off > SFTG_NOALLOC_SCRATCH_BYTES)
         return set_err(ctx, SFTG_E_LIMIT, "frame needs %zu bytes of occlusion scratch; the static scratch holds %u (%u proxies, %u lights, %u instances)",
@@ -922,8 +923,8 @@ extern "C" int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* fd, 
         CK(cudaMemsetAsync(d + o_pv, 0, (size_t)n_packets * 2, st));
         CK(cudaMemsetAsync(d + o_xv, 0, (size_t)np * 2, st));
         sftg_launch_occlusion((const sftg_frame*)(d + o_F), (const uint16_t*)(d + o_pv), n_packets, (const uint16_t*)(d + o_xv), np,
-                              fd->n_instances, d + o_pk, (uint2*)(d + o_pr), (uint32_t*)(d + o_np), (uint32_t)max_pairs,
-                              (uint8_t*)(d + o_lv), (uint32_t*)(d + o_st), st);
+                              fd->n_instances, d + o_pk, (uint2*)(d + o_pr), (uint32_t*)(d + o_np), (uint32_t)max_pairs, SFTG_OCC_ITEMS_PER_PAIR_NOALLOC,
+                              (uint8_t*)(d + o_lv), (uint32_t*)(d + o_st), 0, st);
         CK(cudaGetLastError());
     }
     uint32_t status = 0;

@@ -49,12 +49,15 @@ __global__ void k_scan_top(uint32_t* sums, uint32_t nb, uint32_t* total_out);
 __global__ void k_scan_down(const uint32_t* in, uint32_t n, const uint32_t* sums, uint32_t* out);
 size_t sftg_packet_bytes();
 /* BLAS sub-walk items per (packet, instance) pair: the pair buffer holds max_pairs pairs, then
- * max_pairs * SFTG_OCC_ITEMS_PER_PAIR items; the counter word after n_pairs counts the items */
+ * max_pairs * items_per_pair items; the counter word after n_pairs counts the items.  A walk
+ * whose items do not fit keeps the rest of its subtree on its own stack. */
 #define SFTG_OCC_ITEMS_PER_PAIR 64
+#define SFTG_OCC_ITEMS_PER_PAIR_NOALLOC 64
 /* packet_view maps a batch-wide shadow packet to its view, prox_view a batch-wide proxy */
 void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view, uint32_t n_packets, const uint16_t* prox_view,
                            uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
-                           uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st);
+                           uint32_t max_pairs, uint32_t items_per_pair, uint8_t* light_vis, uint32_t* status, int ray_prune,
+                           cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
 /* order[] = the batch's tiles, heaviest first inside each sample-count range; scratch holds 192 words */
 void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,

@@ -236,6 +236,57 @@ struct occ_walk {
     uint32_t full;
 };
 
+/* The packet's 8 rays in model space, shared by the warp, for the ray-box prune below. */
+struct occ_rays { float ox[8], oy[8], oz[8], ix[8], iy[8], iz[8], tmax[8]; };
+
+/* Optional second cull (sftg_tuning.occl_ray_prune) of the children the frustum test kept: child
+ * c (lane & 7) survives if one of the rays still unblocked, (lane >> 3) or (lane >> 3) + 4,
+ * passes through its box grown by a margin.  A well-conditioned any-hit test only reports
+ * triangles within rounding of the ray, so the result is unchanged; but when a ray grazes a
+ * triangle's plane (|a| just above the test's 1e-6 threshold while its true value is rounding
+ * noise) the reference's u, v and t are noise and it can report a hit far from the ray, which
+ * this cull would skip.  That is why it is off by default. */
+SFTG_D uint32_t ray_box_mask(const sftg_bvh_node* nd, const occ_rays& R, uint32_t open_rays, int lane) {
+    const int c = lane & 7;
+    const float lo[3] = { nd->mn[0][c], nd->mn[1][c], nd->mn[2][c] };
+    const float hi[3] = { nd->mx[0][c], nd->mx[1][c], nd->mx[2][c] };
+    float blo[3], bhi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float m = 1e-4f * (fabsf(lo[a]) + fabsf(hi[a]) + (hi[a] - lo[a])) + 1e-5f;
+        blo[a] = lo[a] - m; bhi[a] = hi[a] + m;
+    }
+    bool hit = false;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int r = (lane >> 3) + 4 * h;
+        if (!((open_rays >> r) & 1u)) continue;
+        const float o[3] = { R.ox[r], R.oy[r], R.oz[r] }, id[3] = { R.ix[r], R.iy[r], R.iz[r] };
+        float tn = -3.0e38f, tf = 3.0e38f;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float t1 = (blo[a] - o[a]) * id[a], t2 = (bhi[a] - o[a]) * id[a];
+            tn = fmaxf(tn, fminf(t1, t2)); tf = fminf(tf, fmaxf(t1, t2));
+        }
+        const float tm = R.tmax[r] * 1.0001f + 1e-4f;
+        hit = hit || (tn <= tf && tf >= -1e-4f && tn <= tm);
+    }
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, hit);
+    return (b | (b >> 8) | (b >> 16) | (b >> 24)) & 0xFFu;
+}
+
+/* lanes 0..7 publish their ray; inverse directions with zero components made huge, not infinite */
+SFTG_D void occ_rays_publish(const occ_walk& w, occ_rays& R, int lane) {
+    if (lane < 8) {
+        R.ox[lane] = w.lo.x; R.oy[lane] = w.lo.y; R.oz[lane] = w.lo.z;
+        R.ix[lane] = w.ld.x != 0.f ? 1.f / w.ld.x : copysignf(1e30f, w.ld.x);
+        R.iy[lane] = w.ld.y != 0.f ? 1.f / w.ld.y : copysignf(1e30f, w.ld.y);
+        R.iz[lane] = w.ld.z != 0.f ? 1.f / w.ld.z : copysignf(1e30f, w.ld.z);
+        R.tmax[lane] = w.tmax;
+    }
+    __syncwarp();
+}
+
 SFTG_D void occ_pair_setup(const sftg_inst* I, const sftg_packet* P, int lane, occ_walk& w) {
     const frustum6 pf = P->f;
     const float* M = I->T;
@@ -272,8 +323,8 @@ SFTG_D void occ_pair_setup(const sftg_inst* I, const sftg_packet* P, int lane, o
  * pushed after all when the item list is full).  Returns the rays found blocked. */
 template <bool EXPAND>
 SFTG_D uint32_t occ_walk_from(const sftg_frame* F, const sftg_inst* I, const sftg_model& Md, const occ_walk& w, uint32_t sat,
-                              uint32_t start, uint32_t pair, uint32_t* stack, uint2* items, uint32_t* n_items, uint32_t max_items,
-                              uint32_t* status, int lane) {
+                              uint32_t start, uint32_t pair, uint32_t* stack, const occ_rays& R, bool prune, uint2* items,
+                              uint32_t* n_items, uint32_t max_items, uint32_t* status, int lane) {
     const int r = lane & 7, kq = lane >> 3;
     const uint32_t full = w.full;
     int top = 1;
@@ -287,6 +338,7 @@ SFTG_D uint32_t occ_walk_from(const sftg_frame* F, const sftg_inst* I, const sft
         const uint32_t ni = ent & 0x1FFFFFFFu, depth = ent >> 29;
         const sftg_bvh_node* nd = &blas[ni];
         uint32_t m = node_mask(nd, w.mf, lane);
+        if (prune && m) m &= ray_box_mask(nd, R, full & ~sat, lane);
         if (!nd->leaf) {
             while (m) {
                 const int c = __ffs(m) - 1; m &= m - 1;
@@ -355,9 +407,11 @@ SFTG_D uint32_t occ_hits_now(const sftg_packet* P) { return *(volatile const uin
 __global__ void __launch_bounds__(OCC_WARPS * 32)
 k_occl_blas_expand(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, sftg_packet* __restrict__ packets,
                    const uint2* __restrict__ pairs, const uint32_t* __restrict__ n_pairs, uint32_t max_pairs,
-                   uint2* __restrict__ items, uint32_t* __restrict__ n_items, uint32_t max_items, uint32_t* __restrict__ status)
+                   uint2* __restrict__ items, uint32_t* __restrict__ n_items, uint32_t max_items, uint32_t* __restrict__ status,
+                   int prune)
 {
     __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
+    __shared__ occ_rays s_rays[OCC_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t np = min(*n_pairs, max_pairs);
     for (uint32_t item = blockIdx.x * OCC_WARPS + warp; item < np; item += gridDim.x * OCC_WARPS) {
@@ -368,8 +422,9 @@ k_occl_blas_expand(const sftg_frame* __restrict__ frames, const uint16_t* __rest
         const sftg_model Md = F->models[I->model];
         occ_walk w;
         occ_pair_setup(I, P, lane, w);
-        const uint32_t sat = occ_walk_from<true>(F, I, Md, w, occ_hits_now(P) & w.full, Md.blas_root, item, s_stack[warp], items,
-                                                 n_items, max_items, status, lane);
+        occ_rays_publish(w, s_rays[warp], lane);
+        const uint32_t sat = occ_walk_from<true>(F, I, Md, w, occ_hits_now(P) & w.full, Md.blas_root, item, s_stack[warp],
+                                                 s_rays[warp], prune != 0, items, n_items, max_items, status, lane);
         if (lane == 0 && sat) atomicOr(&P->hits, sat);
         __syncwarp();
     }
@@ -378,9 +433,10 @@ k_occl_blas_expand(const sftg_frame* __restrict__ frames, const uint16_t* __rest
 __global__ void __launch_bounds__(OCC_WARPS * 32)
 k_occl_blas_walk(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ packet_view, sftg_packet* __restrict__ packets,
                  const uint2* __restrict__ pairs, const uint2* __restrict__ items, const uint32_t* __restrict__ n_items,
-                 uint32_t max_items, uint32_t* __restrict__ status)
+                 uint32_t max_items, uint32_t* __restrict__ status, int prune)
 {
     __shared__ uint32_t s_stack[OCC_WARPS][OCC_STACK];
+    __shared__ occ_rays s_rays[OCC_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t ni = min(*n_items, max_items);
     for (uint32_t it = blockIdx.x * OCC_WARPS + warp; it < ni; it += gridDim.x * OCC_WARPS) {
@@ -394,7 +450,9 @@ k_occl_blas_walk(const sftg_frame* __restrict__ frames, const uint16_t* __restri
         const sftg_model Md = F->models[I->model];
         occ_walk w;
         occ_pair_setup(I, P, lane, w);
-        const uint32_t sat = occ_walk_from<false>(F, I, Md, w, known, itm.y, 0, s_stack[warp], nullptr, nullptr, 0, status, lane);
+        occ_rays_publish(w, s_rays[warp], lane);
+        const uint32_t sat = occ_walk_from<false>(F, I, Md, w, known, itm.y, 0, s_stack[warp], s_rays[warp], prune != 0, nullptr,
+                                                  nullptr, 0, status, lane);
         if (lane == 0 && (sat & ~known)) atomicOr(&P->hits, sat);
         __syncwarp();
     }
@@ -422,7 +480,8 @@ size_t sftg_packet_bytes() { return sizeof(sftg_packet); }
 
 void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view, uint32_t n_packets, const uint16_t* prox_view,
                            uint32_t n_proxies, uint32_t max_inst, void* packets, uint2* pairs, uint32_t* n_pairs,
-                           uint32_t max_pairs, uint8_t* light_vis, uint32_t* status, cudaStream_t st) {
+                           uint32_t max_pairs, uint32_t items_per_pair, uint8_t* light_vis, uint32_t* status, int ray_prune,
+                           cudaStream_t st) {
     cudaMemsetAsync(n_pairs, 0, 8, st);   /* pair and item counters */
     if (!n_packets) return;
     k_occl_tlas<<<(n_packets + OCC_WARPS - 1) / OCC_WARPS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, n_packets,
@@ -430,14 +489,14 @@ void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view
     /* the item list shares the pair buffer's tail: pairs take [0, max_pairs), items the rest */
     uint2* items = pairs + max_pairs;
     uint32_t* n_items = n_pairs + 1;
-    const uint32_t max_items = max_pairs * SFTG_OCC_ITEMS_PER_PAIR;
+    const uint32_t max_items = max_pairs * items_per_pair;
     const uint64_t want = (uint64_t)n_packets * (max_inst ? max_inst : 1);
     const uint32_t mp = want < max_pairs ? (uint32_t)want : max_pairs;
     const uint32_t g1 = (mp + OCC_WARPS - 1) / OCC_WARPS;
     k_occl_blas_expand<<<g1 < OCC_GRID_CTAS ? g1 : OCC_GRID_CTAS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, (sftg_packet*)packets,
                                                                                          pairs, n_pairs, max_pairs, items, n_items,
-                                                                                         max_items, status);
+                                                                                         max_items, status, ray_prune);
     k_occl_blas_walk<<<OCC_GRID_CTAS, OCC_WARPS * 32, 0, st>>>(frames, packet_view, (sftg_packet*)packets, pairs, items, n_items,
-                                                               max_items, status);
+                                                               max_items, status, ray_prune);
     k_occl_finalize<<<(n_proxies * 64 + 255) / 256, 256, 0, st>>>(frames, prox_view, n_proxies, (const sftg_packet*)packets, light_vis);
 }

@@ -201,12 +201,13 @@ class Renderer:
         return self.tuning()
 
     def tuning(self) -> dict:
-        t = np.zeros(7, np.int32)
+        t = np.zeros(8, np.int32)
         self.lib.sftg_get_tuning(self.lib.sft_get_gpu_context(), _ptr(t))
-        return {"resolve_split": t[0:3].tolist(), "raster_slab_rows": t[3:6].tolist(), "geom_job_width": int(t[6])}
+        return {"resolve_split": t[0:3].tolist(), "raster_slab_rows": t[3:6].tolist(), "geom_job_width": int(t[6]),
+                "occl_ray_prune": int(t[7])}
 
-    def set_tuning(self, resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=8) -> None:
-        t = np.array([*resolve_split, *raster_slab_rows, geom_job_width], np.int32)
+    def set_tuning(self, resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=8, occl_ray_prune=0) -> None:
+        t = np.array([*resolve_split, *raster_slab_rows, geom_job_width, occl_ray_prune], np.int32)
         if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
             raise ValueError("tuning out of range")
 

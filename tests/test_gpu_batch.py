@@ -90,6 +90,7 @@ TUNINGS = [
     dict(resolve_split=(8, 1, 2), raster_slab_rows=(64, 4, 16), geom_job_width=3),
     dict(resolve_split=(2, 8, 1), raster_slab_rows=(16, 64, 4), geom_job_width=5),
     dict(resolve_split=(16, 16, 16), raster_slab_rows=(4, 4, 4), geom_job_width=8),
+    dict(resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=8, occl_ray_prune=1),
 ]
 
 
