@@ -7,14 +7,15 @@
  * reference's per-frame mmap arenas, sofren2.c:9456-9564); it grows between frames when a
  * frame needs more and never inside one.
  *
- * Frame sequence on one stream (sft_present, sofren2.c:8139-8289):
+ * Frame sequence (sft_present, sofren2.c:8139-8289), replayed as one CUDA graph per layout:
  *   1. one H2D copy of the frame block: constants, instances, bones, jobs, lights, proxies, TLAS
- *   2. k_occl_*           light visibility of every shadow proxy (8163-8280)
+ *   2. k_occl_*           light visibility of every shadow proxy (8163-8280), on a second
+ *                         stream beside steps 3-5, joined before the resolve
  *   3. k_geometry         cull, skin, transform, project, batch setup (4901-5145)
  *   4. scan + k_clip      near-plane clipping in emission order (4691-4772)
- *   5. k_bin (count), scan, k_bin (write)   per-tile payload lists (4619-4688)
+ *   5. k_bin (count), scan, k_bin (write), tile order   per-tile payload lists (4619-4688)
  *   6. k_raster, k_resolve  per-tile raster into a shared-memory visibility buffer, then
- *                         the resolve, four CTAs per tile (6756-6813)
+ *                         the resolve, several CTAs per tile (6756-6813)
  *   7. D2H of the colour buffer into the caller's pitch
  */
 #include <cuda_runtime.h>
@@ -40,6 +41,8 @@ struct dpool {   /* growable device buffer */
 struct sftg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;            /* proxy occlusion runs here, beside geometry, binning and raster */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_geo = nullptr;
     char err[512] = { 0 };
     /* resident */
     dpool texels, texs, mats, ml_attr, ml_inds, ml_cull, ml_info, skin_j, skin_w, blas, models;
@@ -120,6 +123,10 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     for (int i = 0; i < 6; i++) cudaEventCreate(&ctx->ev[i]);
+    if (cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
+    cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+    cudaEventCreate(&ctx->ev_geo);
     if (cudaMallocHost((void**)&ctx->h_status, 64) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
     sftg_tile_configure(227 * 1024);
     { const char* e = getenv("SFTG_NO_GRAPHS"); if (e && *e && *e != '0') ctx->use_graphs = false; }
@@ -140,6 +147,10 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     for (int i = 0; i < 6; i++) if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->ev_geo) cudaEventDestroy(ctx->ev_geo);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -572,15 +583,27 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     CK(cudaGetLastError());   /* nothing pending from earlier calls: every launch below is checked */
     CK(cudaMemsetAsync(B.status, 0, 64, st));
     CK(record_event(ctx->ev[0], st));
-    if (B.total_prox) CK(cudaMemsetAsync(B.light_vis, 0, (size_t)B.total_prox * 64, st));   /* columns past the lights stay 0 */
-    if (B.total_packets) {
-        sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
-                              B.pairs, B.n_pairs, B.max_pairs, SFTG_OCC_ITEMS_PER_PAIR, B.light_vis, B.status,
-                              ctx->tuning.occl_ray_prune, st);
-        ctx->launches += 4;
-        CK(cudaGetLastError());
+    /* proxy occlusion only feeds the resolve: it runs on the second stream, forked here and
+     * joined before the resolve, overlapping geometry, binning and raster */
+    const bool occl = B.total_prox || B.total_packets;
+    if (occl) {
+        cudaStream_t so = ctx->stream2;
+        CK(cudaEventRecord(ctx->ev_fork, st));
+        CK(cudaStreamWaitEvent(so, ctx->ev_fork, 0));
+        if (B.total_prox) CK(cudaMemsetAsync(B.light_vis, 0, (size_t)B.total_prox * 64, so));   /* columns past the lights stay 0 */
+        if (B.total_packets) {
+            sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
+                                  B.pairs, B.n_pairs, B.max_pairs, SFTG_OCC_ITEMS_PER_PAIR, B.light_vis, B.status,
+                                  ctx->tuning.occl_ray_prune, so);
+            ctx->launches += 4;
+            CK(cudaGetLastError());
+        }
+        CK(record_event(ctx->ev[1], so));
+        CK(cudaEventRecord(ctx->ev_join, so));
+    } else {
+        CK(record_event(ctx->ev[1], st));
     }
-    CK(record_event(ctx->ev[1], st));
+    CK(record_event(ctx->ev_geo, st));
     if (B.n_jobs) {
         k_geometry<<<(B.n_jobs + 3) / 4, 128, 0, st>>>(B.frames, B.jobs, B.n_jobs, B.ss, B.recs, B.clip_cnt, B.mrect);
         ctx->launches++;
@@ -612,6 +635,7 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
         if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], st, A); ctx->launches++; }
     CK(cudaGetLastError());
     CK(record_event(ctx->ev[4], st));
+    if (occl) CK(cudaStreamWaitEvent(st, ctx->ev_join, 0));
     for (int si = 0; si < 3; si++)
         if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ctx->launches++; }
     if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ctx->launches++; }
@@ -698,9 +722,9 @@ static int batch_common(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, 
             while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
             continue;
         }
-        for (int k = 0; k < 5; k++) {
+        for (int k = 0; k < 5; k++) {   /* geometry is timed from its own start: occlusion runs beside it */
             float t = 0.f;
-            if (cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]) != cudaSuccess) { t = 0.f; cudaGetLastError(); }
+            if (cudaEventElapsedTime(&t, k == 1 ? ctx->ev_geo : ctx->ev[k], ctx->ev[k + 1]) != cudaSuccess) { t = 0.f; cudaGetLastError(); }
             ctx->timings[k] = t;
         }
         if (dbg) {
