@@ -161,7 +161,7 @@ int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* frame, uint8_t*
 typedef struct sftg_tuning {
     int32_t resolve_split[3];     /* resolve CTAs per 64x64 tile at 1x, 2x, 4x: 1, 2, 4, 8 or 16 (default 16, 8, 16) */
     int32_t raster_slab_rows[3];  /* tile rows per raster work item at 1x, 2x, 4x: 4..64 (default 8, 8, 4) */
-    int32_t geom_job_width;       /* meshlets per geometry warp: 1..8 (default 8, the reference's job) */
+    int32_t geom_job_width;       /* meshlets per geometry warp: 1..8 (default 1; the reference's job is 8) */
     int32_t occl_ray_prune;       /* 1: also cull BLAS children no unblocked shadow ray reaches (faster; can differ
                                      from the reference only where a ray grazes a triangle's plane); default 0.
                                      The only knob that is not result-neutral: sftg_autotune leaves it as set */

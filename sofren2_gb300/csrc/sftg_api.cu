@@ -73,7 +73,7 @@ struct sftg_ctx {
     bool use_graphs = true;
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
-    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 8, 0 };   /* measured best on the single-view workloads */
+    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
 };
 
 static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
@@ -811,9 +811,9 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
     int rc;
     if ((rc = batch_common(ctx, fds, n_views, nullptr, nullptr, nullptr, nullptr))) return rc;   /* warm: arena, tables */
     {
-        const int widths[4] = { 2, 4, 8, 1 };
+        const int widths[4] = { 1, 2, 4, 8 };
         float bt = 1e30f;
-        for (int k = 0; k < 3; k++) {
+        for (int k = 0; k < 4; k++) {
             ctx->tuning = best; ctx->tuning.geom_job_width = widths[k];
             float t;
             if ((rc = time_phase(ctx, fds, n_views, reps, 1, &t))) { ctx->tuning = best; return rc; }

@@ -28,7 +28,6 @@
 #define RASTER_THREADS 512        /* raster CTA: 64 groups of 8 */
 #define SETUP_CAP RASTER_THREADS  /* triangle set-ups per round: 64 payloads x 8 lanes */
 #define MIN_SLAB_ROWS 4           /* smallest raster work item (rows); the slab height is a tuning knob */
-#define ITEM_CAP (SETUP_CAP * (SFTG_TILE / MIN_SLAB_ROWS))
 
 struct tri_setup {
     float A[3], B[3], se[3];
@@ -38,6 +37,41 @@ struct tri_setup {
     uint32_t order;
     int trivial;
 };
+
+/* tri_setup as kept in shared memory (56 B): the guard-band pads are recomputed from A and B,
+ * the bounds are tile-local bytes (0..64) and the trivial-accept flag rides in order's top bit
+ * (order = list position * 8 + lane stays below 2^31) */
+struct tri_setup_packed {
+    float A[3], B[3], se[3];
+    float sz, dzdx, dzdy;
+    uint32_t bounds;       /* ax0 | ax1 << 8 | miny << 16 | maxy << 24, tile-local */
+    uint32_t order_triv;
+};
+
+SFTG_D tri_setup_packed pack_setup(const tri_setup& T, int tmx, int tmy) {
+    tri_setup_packed P;
+#pragma unroll
+    for (int k = 0; k < 3; k++) { P.A[k] = T.A[k]; P.B[k] = T.B[k]; P.se[k] = T.se[k]; }
+    P.sz = T.sz; P.dzdx = T.dzdx; P.dzdy = T.dzdy;
+    P.bounds = (uint32_t)(T.ax0 - tmx) | ((uint32_t)(T.ax1 - tmx) << 8) | ((uint32_t)(T.miny - tmy) << 16) | ((uint32_t)(T.maxy - tmy) << 24);
+    P.order_triv = T.order | (T.trivial ? 0x80000000u : 0u);
+    return P;
+}
+
+template <int S>
+SFTG_D tri_setup unpack_setup(const tri_setup_packed& P, int tmx, int tmy) {
+    tri_setup T;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        T.A[k] = P.A[k]; T.B[k] = P.B[k]; T.se[k] = P.se[k];
+        T.pad[k] = S > 1 ? 0.375f * (fabsf(P.A[k]) + fabsf(P.B[k])) : 0.f;   /* as in tri_setup_one */
+    }
+    T.sz = P.sz; T.dzdx = P.dzdx; T.dzdy = P.dzdy;
+    T.ax0 = tmx + (int)(P.bounds & 0xFFu); T.ax1 = tmx + (int)((P.bounds >> 8) & 0xFFu);
+    T.miny = tmy + (int)((P.bounds >> 16) & 0xFFu); T.maxy = tmy + (int)(P.bounds >> 24);
+    T.order = P.order_triv & 0x7FFFFFFFu; T.trivial = (int)(P.order_triv >> 31);
+    return T;
+}
 
 struct proxy_cache {   /* sft_light_proxy_cache (sofren2.c:991-998) */
     float pa[3], pb[3], ab[3], W[3];
@@ -283,7 +317,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
-    tri_setup* setups = (tri_setup*)(smem + (size_t)S * SFTG_TILE_PX * 8);
+    tri_setup_packed* setups = (tri_setup_packed*)(smem + (size_t)S * SFTG_TILE_PX * 8);
     uint32_t* items = (uint32_t*)(setups + SETUP_CAP);                     /* set-up index << 8 | slab */
     __shared__ uint32_t s_nsetup, s_nitems, s_next;
     __shared__ float s_red[2][RASTER_THREADS / 32];
@@ -338,7 +372,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
                     tri_setup T;
                     if (tri_setup_one<S>(sx[0], sy[0], iw[0], sx[1], sy[1], iw[1], sx[2], sy[2], iw[2], tmx, tmy, p * 8 + l, T)) {
                         const uint32_t slot = atomicAdd(&s_nsetup, 1u);
-                        setups[slot] = T;
+                        setups[slot] = pack_setup(T, tmx, tmy);
                         const uint32_t nslab = (uint32_t)(T.maxy - T.miny) / (uint32_t)slab_rows + 1u;
                         const uint32_t ib = atomicAdd(&s_nitems, nslab);
                         for (uint32_t k = 0; k < nslab; k++) items[ib + k] = (slot << 8) | k;
@@ -354,7 +388,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
             idx = __shfl_sync(gmask, idx, lane & ~7);
             if (idx >= nitem) break;
             const uint32_t it = items[idx];
-            const tri_setup T = setups[it >> 8];
+            const tri_setup T = unpack_setup<S>(setups[it >> 8], tmx, tmy);
             const int y0 = T.miny + (int)(it & 0xFFu) * slab_rows;
             const int y1 = min(y0 + slab_rows - 1, T.maxy);
             tri_raster<S>(T, y0, y1, grp_lane, gmask, tmx, tmy, keys);
@@ -999,13 +1033,17 @@ void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_
 }
 
 /* ---------------------------------------------------------------- host-side launch helpers */
-static size_t raster_smem(int S) { return (size_t)S * SFTG_TILE_PX * 8 + (size_t)SETUP_CAP * sizeof(tri_setup) + (size_t)ITEM_CAP * 4; }
+/* keys, packed set-ups, then the work items of one round: up to SETUP_CAP * (64 / slab_rows) */
+static size_t raster_smem(int S, int slab_rows) {
+    return (size_t)S * SFTG_TILE_PX * 8 + (size_t)SETUP_CAP * sizeof(tri_setup_packed) +
+           (size_t)SETUP_CAP * ((SFTG_TILE + slab_rows - 1) / slab_rows) * 4;
+}
 
 cudaError_t sftg_tile_configure(int max_dynamic_smem) {
     cudaError_t e = cudaSuccess;
     const int S_[3] = { 1, 2, 4 };
     for (int k = 0; k < 3 && e == cudaSuccess; k++) {
-        const int need = (int)raster_smem(S_[k]);
+        const int need = (int)raster_smem(S_[k], MIN_SLAB_ROWS);
         const int v = need < max_dynamic_smem ? need : max_dynamic_smem;
         if (S_[k] == 1) e = cudaFuncSetAttribute(k_raster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
         if (S_[k] == 2) e = cudaFuncSetAttribute(k_raster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
@@ -1016,7 +1054,7 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
 
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
-    const size_t sm = raster_smem(S);
+    const size_t sm = raster_smem(S, slab_rows);
     if (S == 1) k_raster<1><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
     else if (S == 2) k_raster<2><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
     else k_raster<4><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);

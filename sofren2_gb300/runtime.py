@@ -206,7 +206,7 @@ class Renderer:
         return {"resolve_split": t[0:3].tolist(), "raster_slab_rows": t[3:6].tolist(), "geom_job_width": int(t[6]),
                 "occl_ray_prune": int(t[7])}
 
-    def set_tuning(self, resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=8, occl_ray_prune=0) -> None:
+    def set_tuning(self, resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=1, occl_ray_prune=0) -> None:
         t = np.array([*resolve_split, *raster_slab_rows, geom_job_width, occl_ray_prune], np.int32)
         if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
             raise ValueError("tuning out of range")
