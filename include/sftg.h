@@ -173,6 +173,39 @@ int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* tuning);
  * fastest in the context and copies it to *out (optional). */
 int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, int32_t reps, sftg_tuning* out);
 
+/* Skeletal animation on the GPU (sft_pose_update, sofren2.c:8952-9108).  A skeleton (bones in
+ * sft_bone's layout, sofren2.c:1000-1009) with its animations (samplers / channels,
+ * sofren2.c:1023-1049) is uploaded once; sftg_pose_eval then evaluates any number of
+ * (skeleton, animation, time) requests in one launch, one warp per request.  Results are the
+ * reference's posed bone matrices (inverse bind x global) and, optionally, the globals; they
+ * equal the reference's up to the rounding of the device's acosf / sinf / cosf against the host
+ * libm's inside the quaternion slerp (a few ulp). */
+typedef struct sftg_bone_desc {
+    float inverse_bind[16], local_bind[16];   /* row-major sftmat */
+    int32_t parent;                           /* -1 for a root; any order */
+    float base_t[3], base_r[4], base_s[3];    /* rest pose TRS (quaternion x y z w) */
+} sftg_bone_desc;
+typedef struct sftg_sampler_desc {
+    const float* inputs;                      /* count keyframe times, ascending */
+    const float* outputs;                     /* count * 4 floats (xyz or xyzw per key) */
+    int32_t count, is_step;
+} sftg_sampler_desc;
+typedef struct sftg_channel_desc { int32_t sampler, node, path; } sftg_channel_desc;   /* path: 0 T, 1 R, 2 S */
+typedef struct sftg_animation_desc {
+    const sftg_sampler_desc* samplers;
+    const sftg_channel_desc* channels;
+    int32_t sampler_count, channel_count;
+    float duration;
+} sftg_animation_desc;
+typedef struct sftg_pose_request { int32_t skeleton, animation; float time; } sftg_pose_request;
+#define SFTG_MAX_BONES 128
+int sftg_skeleton_upload(sftg_ctx* ctx, const sftg_bone_desc* bones, uint32_t bone_count, const sftg_animation_desc* anims,
+                         uint32_t anim_count, int32_t* out_skeleton);
+/* posed (and global, optional) receive for request k, at float offset 16 * (sum of the bone counts
+ * of requests 0..k-1), its bones' matrices; host memory.  A request whose animation index is out
+ * of range leaves its matrices untouched, as sft_pose_update returns early. */
+int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* requests, uint32_t n, float* posed, float* global);
+
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */

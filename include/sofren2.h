@@ -20,6 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include "sftg.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -153,6 +154,7 @@ SFT_FUNC void sft_set_color_buffer(u32* buf, i32 pitch_in_bytes);
 /* drawing (811, 823-824) */
 SFT_FUNC void sft_draw_instance(const sft_instance* instance);
 SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena);
+SFT_FUNC void sft_pose_update(sft_pose* pose, i32 anim_id, f32 time);
 
 /* lights (827-832) */
 SFT_FUNC void sft_set_ambient_light(f32 r, f32 g, f32 b);
@@ -187,6 +189,11 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
                                      u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
                                      sft_arena* arena);
 SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model);
+/* extension: the model's skeleton and animation tracks, what the reference's GLB loader fills
+ * (sft_bone / sft_animation, sofren2.c:1000-1049); uploaded for sft_pose_update, which then
+ * evaluates poses on the GPU.  bone_count must be the model's.  Returns 0 or an sftg error. */
+SFT_FUNC i32 sft_model_set_skeleton(sft_model* model, const sftg_bone_desc* bones, u32 bone_count,
+                                    const sftg_animation_desc* anims, u32 anim_count);
 /* extension: MSAA samples (1, 2, 4) of the shared library build; SFT_AA_SAMPLES sets it in SFT_IMPL builds */
 SFT_FUNC void sft_set_msaa_samples(i32 samples);
 /* extension: last error text of the GPU runtime ("" when none) */
@@ -247,6 +254,7 @@ typedef struct sft__item { u32 id; f32 mn[3], mx[3], c[3]; } sft__item;
 
 struct sft_model {
     i32 device_id;
+    i32 skeleton_id;              /* sftg skeleton with the model's animations, -1 when none */
     u32 mesh_count, total_meshlets, bone_count;
     u32* mesh_first;              /* per mesh: first model meshlet */
     u32* mesh_meshlets;
@@ -697,7 +705,7 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
                                      sft_arena* arena) {
     (void)arena;
     sft_model* m = (sft_model*)calloc(1, sizeof(sft_model));
-    m->mesh_count = mesh_count; m->bone_count = bone_count;
+    m->mesh_count = mesh_count; m->bone_count = bone_count; m->skeleton_id = -1;
     m->mesh_first = (u32*)calloc(mesh_count + 1, 4); m->mesh_meshlets = (u32*)calloc(mesh_count + 1, 4);
     sftg_mesh_desc* md = (sftg_mesh_desc*)calloc(mesh_count + 1, sizeof(sftg_mesh_desc));
     u32 total = 0;
@@ -940,6 +948,28 @@ SFT_FUNC i32 sft_batch_submit(void) {
     s->n_batch = 0;
     if (rc) fprintf(stderr, "sofren2-gb300: sft_batch_submit failed (%d): %s\n", rc, sftg_last_error(s->gpu));
     return rc;
+}
+
+SFT_FUNC i32 sft_model_set_skeleton(sft_model* model, const sftg_bone_desc* bones, u32 bone_count,
+                                    const sftg_animation_desc* anims, u32 anim_count) {
+    if (!model || bone_count != model->bone_count) return SFTG_E_ARG;
+    int32_t id = -1;
+    const int rc = sftg_skeleton_upload(sft__s->gpu, bones, bone_count, anims, anim_count, &id);
+    if (rc) { fprintf(stderr, "sofren2-gb300: skeleton upload failed (%d): %s\n", rc, sftg_last_error(sft__s->gpu)); return rc; }
+    model->skeleton_id = id;
+    return 0;
+}
+
+/* sft_pose_update (sofren2.c:8952-9108): the animation sampled at `time` (wrapped by the clip's
+ * duration), evaluated on the GPU (sftg_pose_eval) into pose->global_matrices and
+ * pose->posed_bone_matrices.  Nothing happens for a model without animations or an animation
+ * index out of range, as in the reference. */
+SFT_FUNC void sft_pose_update(sft_pose* pose, i32 anim_id, f32 time) {
+    if (!pose || !pose->model || pose->model->skeleton_id < 0 || !pose->model->bone_count) return;
+    sftg_pose_request r;
+    r.skeleton = pose->model->skeleton_id; r.animation = anim_id; r.time = time;
+    const int rc = sftg_pose_eval(sft__s->gpu, &r, 1, (float*)pose->posed_bone_matrices, (float*)pose->global_matrices);
+    if (rc) fprintf(stderr, "sofren2-gb300: sft_pose_update failed (%d): %s\n", rc, sftg_last_error(sft__s->gpu));
 }
 
 SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena) {

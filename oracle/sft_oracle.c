@@ -1717,6 +1717,149 @@ int sfto_light_vis(void* hp, uint8_t* out, uint32_t cap_proxies) {
     return (int)h->c.nprox;
 }
 
+/* ------------------------------------------------------------ skeletal pose (sft_pose_update, 8952-9108)
+ * Pose blob (little endian): "SFTP", bone count, bones {f32 inverse_bind[16], f32 local_bind[16],
+ * i32 parent, f32 base_t[3], f32 base_r[4], f32 base_s[3]}, animation count, per animation
+ * {f32 duration, u32 samplers, u32 channels, samplers {u32 count, u32 is_step, f32 inputs[count],
+ * f32 outputs[count * 4]}, channels {i32 sampler, i32 node, i32 path}}, request count, requests
+ * {i32 animation, f32 time}.  Output per request: bones x 16 posed floats, then bones x 16 global. */
+typedef struct { f32 inv[16], loc[16]; i32 parent; f32 bt[3], br[4], bs[3]; } opbone;
+typedef struct { u32 count, is_step; const f32* in; const f32* out; } opsmp;
+typedef struct { i32 sampler, node, path; } opch;
+typedef struct { f32 duration; u32 ns, nc; opsmp* smp; opch* ch; } opanim;
+
+static void pmul(const f32* a, const f32* b, f32* r) {   /* sft_m_mul (1668): left-to-right sums */
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            r[i * 4 + j] = a[i * 4 + 0] * b[0 * 4 + j] + a[i * 4 + 1] * b[1 * 4 + j] + a[i * 4 + 2] * b[2 * 4 + j] + a[i * 4 + 3] * b[3 * 4 + j];
+}
+static void pqnorm(f32* q) {   /* sft_q_norm (1908) */
+    const f32 l2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (0.f != l2) { const f32 il = 1.f / sqrtf(l2); q[0] *= il; q[1] *= il; q[2] *= il; q[3] *= il; }
+}
+static void pslerp(const f32* a, const f32* bi, f32 t, f32* r) {   /* sft_q_slerp (1857) */
+    f32 b[4] = { bi[0], bi[1], bi[2], bi[3] };
+    f32 dot = a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+    if (dot < 0.f) { b[0] = -b[0]; b[1] = -b[1]; b[2] = -b[2]; b[3] = -b[3]; dot = -dot; }
+    if (dot > 0.9995f) { for (int k = 0; k < 4; k++) r[k] = a[k] + t * (b[k] - a[k]); pqnorm(r); return; }
+    const f32 th0 = acosf(dot), th = th0 * t, st = sinf(th), is0 = 1.f / sinf(th0);
+    const f32 s0 = cosf(th) - dot * st * is0, s1 = st * is0;
+    for (int k = 0; k < 4; k++) r[k] = a[k] * s0 + b[k] * s1;
+    pqnorm(r);
+}
+static void pquat(const f32* q, f32* m) {   /* sft_m_from_quat (1822) */
+    const f32 x2 = q[0] + q[0], y2 = q[1] + q[1], z2 = q[2] + q[2];
+    const f32 xx = q[0] * x2, xy = q[0] * y2, xz = q[0] * z2, yy = q[1] * y2, yz = q[1] * z2, zz = q[2] * z2;
+    const f32 wx = q[3] * x2, wy = q[3] * y2, wz = q[3] * z2;
+    const f32 r[16] = { 1.f - (yy + zz), xy + wz, xz - wy, 0.f, xy - wz, 1.f - (xx + zz), yz + wx, 0.f,
+                        xz + wy, yz - wx, 1.f - (xx + yy), 0.f, 0.f, 0.f, 0.f, 1.f };
+    memcpy(m, r, 64);
+}
+
+static void pose_update(const opbone* bones, i32 nb, const opanim* an, f32 time, f32* posed, f32* global) {
+    if (an->duration > EPS) time = fmodf(time, an->duration);
+    f32 tp[128][3], tr[128][4], ts[128][3]; u8 mask[128];
+    memset(mask, 0, sizeof(mask));
+    for (u32 i = 0; i < an->nc; i++) {
+        const opch* ch = &an->ch[i];
+        const opsmp* sm = &an->smp[ch->sampler];
+        if (ch->node < 0 || ch->node >= nb) continue;
+        i32 f0 = 0, f1 = 0; f32 t = 0.f;
+        if (time <= sm->in[0]) { f0 = f1 = 0; }
+        else if (time >= sm->in[sm->count - 1]) { f0 = f1 = (i32)sm->count - 1; }
+        else {
+            i32 low = 0, high = (i32)sm->count - 1;
+            while (low <= high) {
+                const i32 mid = low + (high - low) / 2;
+                if (time < sm->in[mid]) high = mid - 1;
+                else if (time >= sm->in[mid + 1]) low = mid + 1;
+                else { f0 = mid; f1 = mid + 1; break; }
+            }
+            const f32 dt = sm->in[f1] - sm->in[f0];
+            t = (dt > 0.0001f) ? (time - sm->in[f0]) / dt : 0.f;
+        }
+        if (ch->path == 1) {
+            if (sm->is_step) memcpy(tr[ch->node], sm->out + f0 * 4, 16);
+            else pslerp(sm->out + f0 * 4, sm->out + f1 * 4, t, tr[ch->node]);
+            mask[ch->node] |= 2;
+        } else {
+            f32 v[3];
+            for (int k = 0; k < 3; k++) {
+                const f32 v0 = sm->out[f0 * 4 + k], v1 = sm->out[f1 * 4 + k];
+                v[k] = sm->is_step ? v0 : v0 + (v1 - v0) * t;
+            }
+            if (ch->path == 0) { memcpy(tp[ch->node], v, 12); mask[ch->node] |= 1; }
+            else if (ch->path == 2) { memcpy(ts[ch->node], v, 12); mask[ch->node] |= 4; }
+        }
+    }
+    for (i32 b = 0; b < nb; b++) {
+        f32* g = global + b * 16;
+        if (mask[b]) {
+            const f32* p = (mask[b] & 1) ? tp[b] : bones[b].bt;
+            const f32* q = (mask[b] & 2) ? tr[b] : bones[b].br;
+            const f32* sc = (mask[b] & 4) ? ts[b] : bones[b].bs;
+            const f32 T[16] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, p[0], p[1], p[2], 1 };
+            const f32 S[16] = { sc[0], 0, 0, 0, 0, sc[1], 0, 0, 0, 0, sc[2], 0, 0, 0, 0, 1 };
+            f32 R[16], RT[16];
+            pquat(q, R); pmul(R, T, RT); pmul(S, RT, g);
+        } else {
+            memcpy(g, bones[b].loc, 64);
+        }
+    }
+    u8 done[128]; memset(done, 0, sizeof(done));
+    i32 count = 0;
+    while (count < nb)
+        for (i32 b = 0; b < nb; b++) {
+            if (done[b]) continue;
+            const i32 par = bones[b].parent;
+            if (par < 0) { done[b] = 1; count++; }
+            else if (done[par]) { f32 r[16]; pmul(global + b * 16, global + par * 16, r); memcpy(global + b * 16, r, 64); done[b] = 1; count++; }
+        }
+    for (i32 b = 0; b < nb; b++) pmul(bones[b].inv, global + b * 16, posed + b * 16);
+}
+
+/* Evaluates every request of a pose blob; out receives per request bones x 16 posed floats
+ * followed by bones x 16 global floats.  Returns the request count, or a negative error. */
+int sfto_pose_eval(const uint8_t* blob, uint64_t size, float* out, uint64_t out_floats) {
+    const uint8_t* p = blob; const uint8_t* e = blob + size;
+#define TAKE(n) ((size_t)(e - p) >= (size_t)(n) ? (p += (n), p - (n)) : NULL)
+    const uint8_t* q = TAKE(8);
+    if (!q || memcmp(q, "SFTP", 4)) return -1;
+    u32 nb; memcpy(&nb, q + 4, 4);
+    if (nb == 0 || nb > 128) return -2;
+    const opbone* bones = (const opbone*)TAKE((size_t)nb * sizeof(opbone));
+    q = TAKE(4); if (!q || !bones) return -3;
+    u32 na; memcpy(&na, q, 4);
+    opanim* an = (opanim*)calloc(na + 1, sizeof(opanim));
+    for (u32 a = 0; a < na; a++) {
+        q = TAKE(12); if (!q) { free(an); return -4; }
+        memcpy(&an[a].duration, q, 4); memcpy(&an[a].ns, q + 4, 4); memcpy(&an[a].nc, q + 8, 4);
+        an[a].smp = (opsmp*)calloc(an[a].ns + 1, sizeof(opsmp));
+        for (u32 k = 0; k < an[a].ns; k++) {
+            q = TAKE(8); if (!q) return -5;
+            memcpy(&an[a].smp[k].count, q, 4); memcpy(&an[a].smp[k].is_step, q + 4, 4);
+            an[a].smp[k].in = (const f32*)TAKE(an[a].smp[k].count * 4);
+            an[a].smp[k].out = (const f32*)TAKE(an[a].smp[k].count * 16);
+            if (!an[a].smp[k].in || !an[a].smp[k].out || !an[a].smp[k].count) return -6;
+        }
+        an[a].ch = (opch*)TAKE(an[a].nc * sizeof(opch));
+        if (an[a].nc && !an[a].ch) return -7;
+    }
+    q = TAKE(4); if (!q) return -8;
+    u32 nr; memcpy(&nr, q, 4);
+    const uint8_t* rq = TAKE((size_t)nr * 8);
+    if (!rq || out_floats < (uint64_t)nr * nb * 32) return -9;
+    for (u32 r = 0; r < nr; r++) {
+        i32 ai; f32 t; memcpy(&ai, rq + 8 * r, 4); memcpy(&t, rq + 8 * r + 4, 4);
+        if (ai < 0 || (u32)ai >= na) continue;
+        pose_update(bones, (i32)nb, &an[ai], t, out + (size_t)r * nb * 32, out + (size_t)r * nb * 32 + (size_t)nb * 16);
+    }
+    for (u32 a = 0; a < na; a++) free(an[a].smp);
+    free(an);
+#undef TAKE
+    return (int)nr;
+}
+
 /* enum sft_debug_mode for the following renders (0 = none) */
 int sfto_set_debug_mode(void* hp, int mode) {
     oracle_handle* h = (oracle_handle*)hp;

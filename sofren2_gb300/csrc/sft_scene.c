@@ -223,6 +223,12 @@ SFTX_EXPORT int sftx_scene_render(void* p, uint32_t frame, uint32_t* color, int3
     return sftx_scene_render_ex(p, frame, color, pitch_bytes, 0xFFFFFFFFu);
 }
 
+/* the i-th model of a loaded scene (for direct sft_* calls on it), or NULL */
+SFTX_EXPORT void* sftx_scene_model(void* p, uint32_t i) {
+    sftx_scene* s = (sftx_scene*)p;
+    return (s && i < s->n_model) ? (void*)s->model[i] : NULL;
+}
+
 SFTX_EXPORT void sftx_scene_free(void* p) {
     sftx_scene* s = (sftx_scene*)p;
     if (!s) return;

@@ -74,6 +74,10 @@ struct sftg_ctx {
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
     sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
+    /* skeletons and animations (sftg_skeleton_upload) */
+    dpool p_skels, p_bones, p_anims, p_samplers, p_channels, p_keys, p_order, p_levels, p_pose_io;
+    std::vector<sftg_skel_dev> h_skels;
+    uint32_t n_bones = 0, n_anims = 0, n_samplers = 0, n_channels = 0, n_keys = 0, n_order = 0, n_levels = 0;
 };
 
 static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
@@ -139,7 +143,8 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     dpool* pools[] = { &ctx->texels, &ctx->texs, &ctx->mats, &ctx->ml_attr, &ctx->ml_inds, &ctx->ml_cull, &ctx->ml_info,
-                       &ctx->skin_j, &ctx->skin_w, &ctx->blas, &ctx->models };
+                       &ctx->skin_j, &ctx->skin_w, &ctx->blas, &ctx->models, &ctx->p_skels, &ctx->p_bones, &ctx->p_anims,
+                       &ctx->p_samplers, &ctx->p_channels, &ctx->p_keys, &ctx->p_order, &ctx->p_levels, &ctx->p_pose_io };
     for (dpool* p : pools) if (p->ptr) cudaFree(p->ptr);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->d_color) cudaFree(ctx->d_color);
@@ -762,6 +767,139 @@ extern "C" int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* fd
 extern "C" int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, uint32_t* const* colors,
                                   const int32_t* pitch_bytes, const uint32_t** out_device_colors) {
     return batch_common(ctx, fds, n_views, colors, pitch_bytes, nullptr, out_device_colors);
+}
+
+/* ------------------------------------------------------------------ skeletal poses */
+/* appends n records of T to a pool whose element count is tracked in count (pool_append aligns
+ * byte offsets to 256, so element arrays are appended at exact element offsets instead) */
+template <class T>
+static int pool_push(sftg_ctx* ctx, dpool& p, uint32_t& count, const T* src, size_t n) {
+    const size_t off = (size_t)count * sizeof(T);
+    int rc = pool_reserve(ctx, p, off + n * sizeof(T) + 16);
+    if (rc) return rc;
+    if (n) CK(cudaMemcpyAsync((char*)p.ptr + off, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    p.size = off + n * sizeof(T);
+    count += (uint32_t)n;
+    return 0;
+}
+
+extern "C" int sftg_skeleton_upload(sftg_ctx* ctx, const sftg_bone_desc* bones, uint32_t bone_count, const sftg_animation_desc* anims,
+                                    uint32_t anim_count, int32_t* out_skeleton) {
+    if (!ctx || !bones || !bone_count || (anim_count && !anims)) return SFTG_E_ARG;
+    if (bone_count > SFTG_MAX_BONES) return set_err(ctx, SFTG_E_LIMIT, "skeleton of %u bones (at most %d)", bone_count, SFTG_MAX_BONES);
+    CK(cudaSetDevice(ctx->device));
+    /* parents first, level by level; parent indices must be in range and acyclic */
+    std::vector<int> depth(bone_count, -1);
+    for (uint32_t b = 0; b < bone_count; b++) {
+        if (bones[b].parent >= (int32_t)bone_count) return set_err(ctx, SFTG_E_ARG, "bone %u: parent %d out of range", b, bones[b].parent);
+        int d = 0, q = (int)b;
+        while (bones[q].parent >= 0) { q = bones[q].parent; if (++d > (int)bone_count) return set_err(ctx, SFTG_E_ARG, "bone hierarchy has a cycle"); }
+        depth[b] = d;
+    }
+    const int levels = *std::max_element(depth.begin(), depth.end()) + 1;
+    std::vector<uint16_t> order, lv;
+    for (int L = 0; L < levels; L++) {
+        lv.push_back((uint16_t)order.size());
+        for (uint32_t b = 0; b < bone_count; b++) if (depth[b] == L) order.push_back((uint16_t)b);
+    }
+    lv.push_back((uint16_t)order.size());
+    std::vector<sftg_bone_dev> bd(bone_count);
+    for (uint32_t b = 0; b < bone_count; b++) {
+        memcpy(bd[b].inverse_bind, bones[b].inverse_bind, 64); memcpy(bd[b].local_bind, bones[b].local_bind, 64);
+        bd[b].parent = bones[b].parent;
+        memcpy(bd[b].base_t, bones[b].base_t, 12); memcpy(bd[b].base_r, bones[b].base_r, 16); memcpy(bd[b].base_s, bones[b].base_s, 12);
+    }
+    sftg_skel_dev sk;
+    memset(&sk, 0, sizeof(sk));
+    sk.bone_base = ctx->n_bones; sk.bone_count = bone_count;
+    sk.anim_base = ctx->n_anims; sk.anim_count = anim_count;
+    sk.order_base = ctx->n_order; sk.level_base = ctx->n_levels; sk.level_count = (uint32_t)levels;
+    std::vector<sftg_anim_dev> ad(anim_count);
+    std::vector<sftg_sampler_dev> sd;
+    std::vector<sftg_channel_desc> cd;
+    std::vector<float> keys;
+    for (uint32_t a = 0; a < anim_count; a++) {
+        const sftg_animation_desc& A = anims[a];
+        if (A.sampler_count < 0 || A.channel_count < 0 || (A.sampler_count && !A.samplers) || (A.channel_count && !A.channels))
+            return set_err(ctx, SFTG_E_ARG, "animation %u: bad arrays", a);
+        ad[a].sampler_base = ctx->n_samplers + (uint32_t)sd.size(); ad[a].channel_base = ctx->n_channels + (uint32_t)cd.size();
+        ad[a].sampler_count = A.sampler_count; ad[a].channel_count = A.channel_count; ad[a].duration = A.duration;
+        for (int k = 0; k < A.sampler_count; k++) {
+            const sftg_sampler_desc& S = A.samplers[k];
+            if (S.count < 1 || !S.inputs || !S.outputs) return set_err(ctx, SFTG_E_ARG, "animation %u sampler %d: no keyframes", a, k);
+            sftg_sampler_dev d;
+            d.input_base = ctx->n_keys + (uint32_t)keys.size(); keys.insert(keys.end(), S.inputs, S.inputs + S.count);
+            d.output_base = ctx->n_keys + (uint32_t)keys.size(); keys.insert(keys.end(), S.outputs, S.outputs + (size_t)S.count * 4);
+            d.count = S.count; d.is_step = S.is_step;
+            sd.push_back(d);
+        }
+        for (int k = 0; k < A.channel_count; k++) {
+            const sftg_channel_desc& C = A.channels[k];
+            if (C.sampler < 0 || C.sampler >= A.sampler_count || C.path < 0 || C.path > 2)
+                return set_err(ctx, SFTG_E_ARG, "animation %u channel %d: bad sampler or path", a, k);
+            cd.push_back(C);
+        }
+    }
+    int rc;
+    if ((rc = pool_push(ctx, ctx->p_bones, ctx->n_bones, bd.data(), bd.size())) ||
+        (rc = pool_push(ctx, ctx->p_anims, ctx->n_anims, ad.data(), ad.size())) ||
+        (rc = pool_push(ctx, ctx->p_samplers, ctx->n_samplers, sd.data(), sd.size())) ||
+        (rc = pool_push(ctx, ctx->p_channels, ctx->n_channels, cd.data(), cd.size())) ||
+        (rc = pool_push(ctx, ctx->p_keys, ctx->n_keys, keys.data(), keys.size())) ||
+        (rc = pool_push(ctx, ctx->p_order, ctx->n_order, order.data(), order.size())) ||
+        (rc = pool_push(ctx, ctx->p_levels, ctx->n_levels, lv.data(), lv.size())))
+        return rc;
+    ctx->h_skels.push_back(sk);
+    uint32_t ns = (uint32_t)ctx->h_skels.size() - 1;
+    if ((rc = pool_push(ctx, ctx->p_skels, ns, &sk, 1))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (out_skeleton) *out_skeleton = (int32_t)ctx->h_skels.size() - 1;
+    return SFTG_OK;
+}
+
+extern "C" int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* reqs, uint32_t n, float* posed, float* global) {
+    if (!ctx || (n && (!reqs || !posed))) return SFTG_E_ARG;
+    if (!n) return SFTG_OK;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<uint32_t> off(n);
+    uint32_t total = 0;
+    for (uint32_t k = 0; k < n; k++) {
+        if (reqs[k].skeleton < 0 || (size_t)reqs[k].skeleton >= ctx->h_skels.size())
+            return set_err(ctx, SFTG_E_ARG, "pose request %u: bad skeleton %d", k, reqs[k].skeleton);
+        off[k] = total;
+        total += ctx->h_skels[reqs[k].skeleton].bone_count;
+    }
+    /* device io: requests, offsets, posed, global */
+    const size_t b_req = ((size_t)n * sizeof(sftg_pose_request) + 255) & ~(size_t)255, b_off = ((size_t)n * 4 + 255) & ~(size_t)255;
+    const size_t b_mat = (size_t)total * 64;
+    int rc = pool_reserve(ctx, ctx->p_pose_io, b_req + b_off + 2 * b_mat + 256);
+    if (rc) return rc;
+    char* io = (char*)ctx->p_pose_io.ptr;
+    sftg_pose_request* d_req = (sftg_pose_request*)io;
+    uint32_t* d_off = (uint32_t*)(io + b_req);
+    float* d_posed = (float*)(io + b_req + b_off);
+    float* d_global = global ? d_posed + (size_t)total * 16 : nullptr;
+    CK(cudaMemcpyAsync(d_req, reqs, (size_t)n * sizeof(sftg_pose_request), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_off, off.data(), (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    sftg_pose_tables T;
+    T.skels = (const sftg_skel_dev*)ctx->p_skels.ptr; T.bones = (const sftg_bone_dev*)ctx->p_bones.ptr;
+    T.anims = (const sftg_anim_dev*)ctx->p_anims.ptr; T.samplers = (const sftg_sampler_dev*)ctx->p_samplers.ptr;
+    T.channels = (const sftg_channel_desc*)ctx->p_channels.ptr; T.keys = (const float*)ctx->p_keys.ptr;
+    T.order = (const uint16_t*)ctx->p_order.ptr; T.levels = (const uint16_t*)ctx->p_levels.ptr;
+    sftg_launch_pose(T, d_req, d_off, n, d_posed, d_global, ctx->stream);
+    CK(cudaGetLastError());
+    std::vector<float> hp((size_t)total * 16), hg(global ? (size_t)total * 16 : 0);
+    CK(cudaMemcpyAsync(hp.data(), d_posed, b_mat, cudaMemcpyDeviceToHost, ctx->stream));
+    if (global) CK(cudaMemcpyAsync(hg.data(), d_global, b_mat, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    /* a request with an out-of-range animation leaves its matrices as they were */
+    for (uint32_t k = 0; k < n; k++) {
+        const sftg_skel_dev& sk = ctx->h_skels[reqs[k].skeleton];
+        if (reqs[k].animation < 0 || (uint32_t)reqs[k].animation >= sk.anim_count) continue;
+        memcpy(posed + (size_t)off[k] * 16, hp.data() + (size_t)off[k] * 16, (size_t)sk.bone_count * 64);
+        if (global) memcpy(global + (size_t)off[k] * 16, hg.data() + (size_t)off[k] * 16, (size_t)sk.bone_count * 64);
+    }
+    return SFTG_OK;
 }
 
 /* ------------------------------------------------------------------ tuning */

@@ -2,6 +2,7 @@
 #pragma once
 #include <stdint.h>
 #include "sftg_types.h"
+#include "../../include/sftg.h"
 
 /* one 8-triangle batch of a drawn meshlet after setup (sofren2.c:4775-4884) */
 struct __align__(16) sftg_batch_rec {
@@ -67,5 +68,27 @@ void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cu
 void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A);
 /* tile overlays of the debug views 2-4 (sft__debug_draw_tile_overlay), after every resolve */
 void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
+
+/* skeletons and animations on the device (sftg_skeleton_upload) */
+struct sftg_bone_dev {
+    float inverse_bind[16], local_bind[16];
+    int32_t parent;
+    float base_t[3], base_r[4], base_s[3];
+};
+struct sftg_skel_dev { uint32_t bone_base, bone_count, anim_base, anim_count, order_base, level_base, level_count, pad; };
+struct sftg_anim_dev { uint32_t sampler_base, channel_base; int32_t sampler_count, channel_count; float duration; uint32_t pad[3]; };
+struct sftg_sampler_dev { uint32_t input_base, output_base; int32_t count, is_step; };
+struct sftg_pose_tables {
+    const sftg_skel_dev* skels;
+    const sftg_bone_dev* bones;
+    const sftg_anim_dev* anims;
+    const sftg_sampler_dev* samplers;
+    const sftg_channel_desc* channels;
+    const float* keys;
+    const uint16_t* order;         /* per skeleton: bones parents-first */
+    const uint16_t* levels;        /* per skeleton: level_count + 1 starts into order */
+};
+void sftg_launch_pose(const sftg_pose_tables& T, const sftg_pose_request* reqs, const uint32_t* out_off, uint32_t n, float* posed,
+                      float* global, cudaStream_t st);
 
 #define SFTG_SCAN_ELEMS_PER_BLOCK 4096

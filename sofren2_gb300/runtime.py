@@ -52,6 +52,8 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftx_scene_render_ex": (i32, [p, u32, p, i32, u32]),
         "sftx_serve": (i32, [p, p, u32, u32, u64, i32, p, u32, p, p, p]),
         "sft_get_gpu_context": (p, []), "sftg_get_tuning": (i32, [p, p]), "sftg_set_tuning": (i32, [p, p]),
+        "sftg_skeleton_upload": (i32, [p, p, u32, p, u32, p]), "sftg_pose_eval": (i32, [p, p, u32, p, p]),
+        "sftg_last_error": (C.c_char_p, [p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -62,6 +64,28 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
 
 def _ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class SftgBoneDesc(C.Structure):
+    _fields_ = [("inverse_bind", C.c_float * 16), ("local_bind", C.c_float * 16), ("parent", C.c_int32),
+                ("base_t", C.c_float * 3), ("base_r", C.c_float * 4), ("base_s", C.c_float * 3)]
+
+
+class SftgSamplerDesc(C.Structure):
+    _fields_ = [("inputs", C.c_void_p), ("outputs", C.c_void_p), ("count", C.c_int32), ("is_step", C.c_int32)]
+
+
+class SftgChannelDesc(C.Structure):
+    _fields_ = [("sampler", C.c_int32), ("node", C.c_int32), ("path", C.c_int32)]
+
+
+class SftgAnimationDesc(C.Structure):
+    _fields_ = [("samplers", C.c_void_p), ("channels", C.c_void_p), ("sampler_count", C.c_int32),
+                ("channel_count", C.c_int32), ("duration", C.c_float)]
+
+
+class SftgPoseRequest(C.Structure):
+    _fields_ = [("skeleton", C.c_int32), ("animation", C.c_int32), ("time", C.c_float)]
 
 
 class SftxRequest(C.Structure):
@@ -233,6 +257,50 @@ class Renderer:
             raise RuntimeError(f"serving loop failed ({rc}): " + (self.lib.sft_get_last_error() or b"").decode())
         stats = {"batches": st.batches, "max_batch": st.max_batch, "peak_bytes": st.peak_bytes}
         return done[:n].astype(np.float64) * 1e-9, batch[:n].copy(), stats
+
+    def skeleton_upload(self, rig: dict) -> int:
+        """Uploads a rig (scenes.pose_rig layout) with sftg_skeleton_upload; returns its index."""
+        ctx = self.lib.sft_get_gpu_context()
+        nb = len(rig["bones"])
+        bones = (SftgBoneDesc * nb)()
+        for i, bd in enumerate(rig["bones"]):
+            bones[i].inverse_bind[:] = [float(x) for x in np.asarray(bd["inverse_bind"], np.float32).reshape(-1)]
+            bones[i].local_bind[:] = [float(x) for x in np.asarray(bd["local_bind"], np.float32).reshape(-1)]
+            bones[i].parent = bd["parent"]
+            bones[i].base_t[:] = [float(x) for x in bd["base_t"]]
+            bones[i].base_r[:] = [float(x) for x in bd["base_r"]]
+            bones[i].base_s[:] = [float(x) for x in bd["base_s"]]
+        keep = []   # arrays that must outlive the call
+        anims = (SftgAnimationDesc * max(1, len(rig["anims"])))()
+        for a, an in enumerate(rig["anims"]):
+            smp = (SftgSamplerDesc * len(an["samplers"]))()
+            for k, (ins, outs, step) in enumerate(an["samplers"]):
+                i_arr = np.ascontiguousarray(ins, np.float32); o_arr = np.ascontiguousarray(outs, np.float32)
+                keep += [i_arr, o_arr]
+                smp[k] = SftgSamplerDesc(i_arr.ctypes.data, o_arr.ctypes.data, len(i_arr), int(step))
+            chs = (SftgChannelDesc * max(1, len(an["channels"])))(*[SftgChannelDesc(*c) for c in an["channels"]])
+            keep += [smp, chs]
+            anims[a] = SftgAnimationDesc(C.cast(smp, C.c_void_p), C.cast(chs, C.c_void_p), len(an["samplers"]),
+                                         len(an["channels"]), float(an["duration"]))
+        out = C.c_int32(-1)
+        rc = self.lib.sftg_skeleton_upload(ctx, bones, nb, anims, len(rig["anims"]), C.byref(out))
+        if rc != 0:
+            raise RuntimeError("skeleton upload failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
+        return out.value
+
+    def pose_eval(self, requests: list[tuple[int, int, float]], bone_counts: list[int]) -> tuple[np.ndarray, np.ndarray]:
+        """Evaluates [(skeleton, animation, time)] in one sftg_pose_eval; returns (posed, global)
+        as flat float32 arrays, request k at offset 16 * sum(bone_counts[:k])."""
+        ctx = self.lib.sft_get_gpu_context()
+        n = len(requests)
+        reqs = (SftgPoseRequest * max(1, n))(*[SftgPoseRequest(s, a, float(t)) for s, a, t in requests])
+        total = sum(bone_counts)
+        posed = np.zeros(total * 16, np.float32)
+        glob = np.zeros(total * 16, np.float32)
+        rc = self.lib.sftg_pose_eval(ctx, reqs, n, _ptr(posed), _ptr(glob))
+        if rc != 0:
+            raise RuntimeError("pose evaluation failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
+        return posed, glob
 
     def render_debug(self, h, frame: int, total_ss: int, n_proxies: int, payload_cap: int = 1 << 22,
                      clip_cap: int = 1 << 16) -> dict:

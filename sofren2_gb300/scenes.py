@@ -1098,6 +1098,101 @@ def config5(seed=5001, n_scenes=16, frames_per_scene=24, quick=False) -> tuple[l
     return scenes_out, samples
 
 
+def _quat(axis, ang):
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    h = 0.5 * ang
+    return np.array([*(axis * np.sin(h)), np.cos(h)], np.float32)
+
+
+def _trs_matrix(t, q, sc):
+    x, y, z, w = [float(v) for v in q]
+    r = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y + w * z), 2 * (x * z - w * y), 0],
+                  [2 * (x * y - w * z), 1 - 2 * (x * x + z * z), 2 * (y * z + w * x), 0],
+                  [2 * (x * z + w * y), 2 * (y * z - w * x), 1 - 2 * (x * x + y * y), 0], [0, 0, 0, 1]])
+    m = np.diag([sc[0], sc[1], sc[2], 1.0]) @ r
+    m[3, :3] += np.asarray(t)
+    return m.astype(np.float32)
+
+
+def pose_rig(seed=6001, n_bones=22, n_keys=30) -> dict:
+    """A seeded skeleton with two animations, in the layout of sft_bone / sft_animation
+    (sofren2.c:1000-1049): a random bone tree, rest TRS and bind matrices, animation 0 rotating
+    every bone (30 linear keys, with sign flips and near-identical neighbours to reach both slerp
+    branches) plus a root translation and a stepped scale, animation 1 with stepped rotations of
+    half the bones and two channels driving the same node and path (the later one must win)."""
+    rng = np.random.default_rng(seed)
+    bones = []
+    for b in range(n_bones):
+        parent = -1 if b == 0 else int(rng.integers(0, b))
+        t = rng.uniform(-0.3, 0.3, 3).astype(np.float32)
+        q = _quat(rng.normal(size=3), rng.uniform(-0.6, 0.6))
+        sc = rng.uniform(0.9, 1.1, 3).astype(np.float32)
+        inv = _trs_matrix(rng.uniform(-1, 1, 3), _quat(rng.normal(size=3), rng.uniform(-3, 3)), rng.uniform(0.8, 1.2, 3))
+        bones.append(dict(parent=parent, base_t=t, base_r=q, base_s=sc, local_bind=_trs_matrix(t, q, sc), inverse_bind=inv))
+
+    def keys(n, duration):
+        return np.sort(np.concatenate([[0.0], rng.uniform(0, duration, n - 2), [duration]])).astype(np.float32)
+
+    def rot_track(n, duration):
+        out = np.zeros((n, 4), np.float32)
+        axis = rng.normal(size=3)
+        for k in range(n):
+            q = _quat(axis + 0.2 * rng.normal(size=3), rng.uniform(-2.5, 2.5))
+            if k % 7 == 3:
+                q = -q                      # same rotation, opposite sign: dot < 0
+            if k % 11 == 5 and k > 0:
+                q = out[k - 1] + np.float32(1e-4)   # near-identical neighbour: lerp branch
+                q = (q / np.linalg.norm(q)).astype(np.float32)
+            out[k] = q
+        return keys(n, duration), out
+
+    anims = []
+    samplers, channels = [], []
+    for b in range(n_bones):
+        ins, outs = rot_track(n_keys, 1.0)
+        samplers.append((ins, outs, 0)); channels.append((len(samplers) - 1, b, 1))
+    t_out = np.zeros((n_keys, 4), np.float32); t_out[:, :3] = rng.uniform(-0.5, 0.5, (n_keys, 3))
+    samplers.append((keys(n_keys, 1.0), t_out, 0)); channels.append((len(samplers) - 1, 0, 0))
+    s_out = np.zeros((8, 4), np.float32); s_out[:, :3] = rng.uniform(0.8, 1.2, (8, 3))
+    samplers.append((keys(8, 1.0), s_out, 1)); channels.append((len(samplers) - 1, 5, 2))
+    anims.append(dict(duration=np.float32(1.0), samplers=samplers, channels=channels))
+    samplers, channels = [], []
+    for b in range(0, n_bones, 2):
+        ins, outs = rot_track(12, 0.8)
+        samplers.append((ins, outs, 1)); channels.append((len(samplers) - 1, b, 1))
+    ins, outs = rot_track(12, 0.8)
+    samplers.append((ins, outs, 0)); channels.append((len(samplers) - 1, 2, 1))   # second channel on bone 2
+    channels.append((0, n_bones + 3, 1))                                            # node out of range: skipped
+    anims.append(dict(duration=np.float32(0.8), samplers=samplers, channels=channels))
+    return dict(bones=bones, anims=anims)
+
+
+def pose_requests(rig: dict, n: int, seed: int = 7) -> list[tuple[int, float]]:
+    """(animation, time) requests: times inside, before and after the clip (fmodf wraps them),
+    exactly on keyframes, and a few with an out-of-range animation index."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        a = int(rng.integers(0, len(rig["anims"])))
+        kind = k % 6
+        if kind == 0:
+            t = float(rng.uniform(0, 1))
+        elif kind == 1:
+            t = float(rng.uniform(1, 5))
+        elif kind == 2:
+            t = float(rng.uniform(-1, 0))
+        elif kind == 3:
+            ins = rig["anims"][a]["samplers"][0][0]
+            t = float(ins[int(rng.integers(0, len(ins)))])
+        elif kind == 4:
+            t = 0.0
+        else:
+            a, t = (-1 if k % 12 == 5 else 7), 0.5
+        out.append((a, np.float32(t)))
+    return out
+
+
 def config3(width=1920, height=1080, seed=3001) -> Scene:
     """Large static scene (rendered with 4x MSAA): about 262k triangles of boxes and
     semicircular arches forming a 30x15x15 m atrium, 25 textures of 1024x1024, a baked

@@ -50,6 +50,15 @@ def main(names: list[str]) -> None:
             dbg[f"{name}/{mode}/{S}"] = gc.sha(frame["color"])
             print("debug", name, mode, S, flush=True)
         golden["debug_views"] = dbg
+    if not names or "pose" in names:
+        # sft_pose_update of the reference on a seeded rig (oracle/pose_harness.c)
+        from oracle_lib import pose_blob, reference_pose
+        from sofren2_gb300 import scenes
+        rig = scenes.pose_rig()
+        req = scenes.pose_requests(rig, 60)
+        out = reference_pose(pose_blob(rig, req), len(rig["bones"]), len(req))
+        golden["pose"] = {"rig_seed": 6001, "requests": len(req), "sha256": gc.sha(out)}
+        print("pose", golden["pose"]["sha256"][:16], flush=True)
     json.dump(golden, open(path, "w"), indent=1, sort_keys=True)
 
 

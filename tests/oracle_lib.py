@@ -86,6 +86,53 @@ class Oracle:
         return color, int(ns[0]), sh
 
 
+def pose_blob(rig: dict, requests: list) -> bytes:
+    """The pose blob of sfto_pose_eval / oracle/pose_harness.c."""
+    import struct
+    out = [b"SFTP", struct.pack("<I", len(rig["bones"]))]
+    for bd in rig["bones"]:
+        out.append(np.asarray(bd["inverse_bind"], "<f4").tobytes() + np.asarray(bd["local_bind"], "<f4").tobytes())
+        out.append(struct.pack("<i", bd["parent"]))
+        out.append(np.asarray(bd["base_t"], "<f4").tobytes() + np.asarray(bd["base_r"], "<f4").tobytes() +
+                   np.asarray(bd["base_s"], "<f4").tobytes())
+    out.append(struct.pack("<I", len(rig["anims"])))
+    for an in rig["anims"]:
+        out.append(struct.pack("<fII", float(an["duration"]), len(an["samplers"]), len(an["channels"])))
+        for ins, outs, step in an["samplers"]:
+            out.append(struct.pack("<II", len(ins), step) + np.asarray(ins, "<f4").tobytes() + np.asarray(outs, "<f4").tobytes())
+        for smp, node, path in an["channels"]:
+            out.append(struct.pack("<iii", smp, node, path))
+    out.append(struct.pack("<I", len(requests)))
+    for a, t in requests:
+        out.append(struct.pack("<if", a, float(t)))
+    return b"".join(out)
+
+
+def oracle_pose(blob: bytes, n_bones: int, n_req: int) -> np.ndarray:
+    """[request][posed 0 / global 1][bone][16] from the oracle's restatement."""
+    L = lib()
+    L.sfto_pose_eval.restype = C.c_int
+    L.sfto_pose_eval.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
+    out = np.zeros(n_req * n_bones * 32, np.float32)
+    buf = np.frombuffer(blob, np.uint8)
+    rc = L.sfto_pose_eval(buf.ctypes.data_as(C.c_void_p), len(blob), out.ctypes.data_as(C.c_void_p), out.size)
+    if rc != n_req:
+        raise RuntimeError(f"oracle pose evaluation failed ({rc})")
+    return out.reshape(n_req, 2, n_bones, 16)
+
+
+def reference_pose(blob: bytes, n_bones: int, n_req: int) -> np.ndarray:
+    with tempfile.TemporaryDirectory() as td:
+        ip, op = os.path.join(td, "p.bin"), os.path.join(td, "o.bin")
+        open(ip, "wb").write(blob)
+        subprocess.run([os.path.join(REF_DIR, "pose_harness"), ip, op], check=True)
+        return np.fromfile(op, np.float32).reshape(n_req, 2, n_bones, 16)
+
+
+def reference_pose_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "pose_harness"))
+
+
 def reference_available(samples: int) -> bool:
     return os.path.exists(os.path.join(REF_DIR, f"ref_harness_{samples}x"))
 

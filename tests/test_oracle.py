@@ -90,3 +90,19 @@ def test_oracle_debug_views_match_reference(golden, case):
     finally:
         o.close()
     assert gc.sha(color) == golden["debug_views"][f"{name}/{mode}/{S}"]
+
+
+def test_oracle_pose_matches_reference(golden):
+    """The oracle's sft_pose_update restatement against the reference's own output on a seeded
+    rig: every slerp branch, stepped and linear samplers, wrapped and clamped times, a later
+    channel overriding an earlier one, an out-of-range node, out-of-range animations."""
+    from oracle_lib import oracle_pose, pose_blob, reference_pose, reference_pose_available
+    from sofren2_gb300 import scenes
+    rig = scenes.pose_rig()
+    req = scenes.pose_requests(rig, golden["pose"]["requests"])
+    blob = pose_blob(rig, req)
+    o = oracle_pose(blob, len(rig["bones"]), len(req))
+    assert gc.sha(o) == golden["pose"]["sha256"]
+    if reference_pose_available():
+        r = reference_pose(blob, len(rig["bones"]), len(req))
+        assert np.array_equal(o.view(np.uint32), r.view(np.uint32))
