@@ -118,6 +118,12 @@ int sftg_texture_upload(sftg_ctx* ctx, const uint32_t* texels, uint64_t n_texels
 int sftg_texture_update_desc(sftg_ctx* ctx, int32_t index, const sftg_texture_desc* desc_or_null);
 int sftg_material_set(sftg_ctx* ctx, int32_t index, int32_t texture, uint32_t base_color, float shininess);
 int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* desc, int32_t* out_model);
+/* A model for one frame only: the geometry of the reference's dynamic meshes (sft_dmesh_*,
+ * sofren2.c:8720-8951), which lives in its per-frame scratch arena.  sftg_transient_reset drops
+ * every transient model uploaded since the last reset (after the frames that draw them);
+ * transient models uploaded before a resident one stay until the context is destroyed. */
+int sftg_model_upload_transient(sftg_ctx* ctx, const sftg_model_desc* desc, int32_t* out_model);
+void sftg_transient_reset(sftg_ctx* ctx);
 
 /* Renders one frame into `color` (host memory, pitch in bytes; width*4 when 0).  When the frame
  * does not clear, the current content of `color` is read first (the reference keeps it). */

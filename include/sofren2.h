@@ -77,7 +77,15 @@ typedef struct sft_arena { u8* base; u64 max_size; u64 committed_size; u64 offse
 
 typedef struct sft_model sft_model;      /* host mirror of a device-resident model */
 typedef struct sft_dmesh sft_dmesh;
-typedef struct sft_dmesh_qb sft_dmesh_qb;
+/* a batch of quads reserved in a dynamic mesh's current meshlet: the caller writes 4 vertices
+ * per quad at vert_offset .. (sofren2.c:1167-1173) */
+typedef struct sft_dmesh_qb {
+    f32 *x, *y, *z;
+    f32 *nx, *ny, *nz;
+    f32 *u, *v;
+    u32 vert_offset;
+    u32 allocated_count;
+} sft_dmesh_qb;
 
 typedef struct sft_pose {
     const sft_model* model;
@@ -151,8 +159,20 @@ SFT_FUNC void sft_set_clear(u8 enabled);
 SFT_FUNC void sft_set_clear_color(u32 color);
 SFT_FUNC void sft_set_color_buffer(u32* buf, i32 pitch_in_bytes);
 
-/* drawing (811, 823-824) */
+/* drawing (811-824) */
 SFT_FUNC void sft_draw_instance(const sft_instance* instance);
+SFT_FUNC void sft_draw_cube(sft_dmesh* dm);
+SFT_FUNC void sft_draw_cube_inv(sft_dmesh* dm);
+SFT_FUNC void sft_draw_sphere(sft_dmesh* dm, i32 rings, i32 slices);
+SFT_FUNC void sft_draw_capsule(sft_dmesh* dm, sftvec start_pos, sftvec end_pos, f32 radius, i32 slices, i32 rings);
+SFT_FUNC void sft_draw_cylinder(sft_dmesh* dm, sftvec start_pos, sftvec end_pos, f32 start_radius, f32 end_radius, i32 sides);
+SFT_FUNC sft_dmesh* sft_dmesh_begin(enum sft_dmesh_type type, sft_mat_handle material, u32 max_prims);
+SFT_FUNC void sft_dmesh_push_quad(sft_dmesh* dm, sftvec p0, sftvec p1, sftvec p2, sftvec p3, f32 u0, f32 v0, f32 u1, f32 v1, sftvec normal);
+SFT_FUNC void sft_dmesh_push_quad_4n(sft_dmesh* dm, sftvec p0, sftvec p1, sftvec p2, sftvec p3, f32 u0, f32 v0, f32 u1, f32 v1,
+                                     sftvec n0, sftvec n1, sftvec n2, sftvec n3);
+SFT_FUNC void sft_dmesh_push_tri(sft_dmesh* dm, sftvec p0, sftvec p1, sftvec p2, f32 u0, f32 v0, f32 u1, f32 v1, f32 u2, f32 v2, sftvec normal);
+SFT_FUNC u8 sft_dmesh_alloc_quads(sft_dmesh* dm, u32 count, sft_dmesh_qb* out_batch);
+SFT_FUNC void sft_dmesh_end(sft_dmesh* dm, const sftmat* opt_transform);
 SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena);
 SFT_FUNC void sft_pose_update(sft_pose* pose, i32 anim_id, f32 time);
 
@@ -293,6 +313,10 @@ static struct sft__state {
     sft_tex_handle checker_tex;    /* the base material's albedo, for SFT_DEBUG_CHECKERBOARD */
     sftg_debug_out* debug;
     char err[512];
+    /* dynamic meshes of the current frame: index templates, open meshes, transient models */
+    u8 dmesh_quad_inds[512], dmesh_tri_inds[512];
+    struct sft_dmesh* dmesh_list;
+    struct sft__transient* transient_list;
     /* batched submission: frames recorded by sft_present between sft_batch_begin / _submit */
     u8 batching; u32 n_batch, cap_batch;
     sftg_frame_desc* batch_fd; u32** batch_color; i32* batch_pitch; void** batch_mem;
@@ -494,6 +518,23 @@ SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads) {
     free(px);
     sft__s->base_mat = sft_material_create(checker, 0xFFFFFFFFu, 2.f);
     sft__s->checker_tex = checker;
+    /* dmesh index templates (sofren2.c:8089-8122): 16 quads (32 triangles) or 21 triangles of a
+     * 64-vertex meshlet in the 8-lane batch layout; unused triangles stay (0, 0, 0) */
+    for (u32 tri = 0; tri < 128; tri++) {
+        const u32 off = (tri / 8) * 32, lane = tri % 8;
+        if (tri < 32) {
+            const u8 bv = (u8)((tri / 2) * 4);
+            sft__s->dmesh_quad_inds[off + lane] = bv;
+            sft__s->dmesh_quad_inds[off + 8 + lane] = (tri % 2 == 0) ? (u8)(bv + 1) : (u8)(bv + 2);
+            sft__s->dmesh_quad_inds[off + 16 + lane] = (tri % 2 == 0) ? (u8)(bv + 2) : (u8)(bv + 3);
+        }
+        if (tri < 21) {
+            const u8 bv = (u8)(tri * 3);
+            sft__s->dmesh_tri_inds[off + lane] = bv;
+            sft__s->dmesh_tri_inds[off + 8 + lane] = (u8)(bv + 1);
+            sft__s->dmesh_tri_inds[off + 16 + lane] = (u8)(bv + 2);
+        }
+    }
     SFT__LOG("initialized GPU renderer %dx%d, %d sample(s)\n", width, height, sft__s->samples);
 }
 
@@ -518,9 +559,268 @@ SFT_FUNC i32 sft_get_launch_count(void) { return sft__s ? sftg_last_launch_count
 SFT_FUNC void* sft_get_cuda_stream(void) { return sft__s ? sftg_stream(sft__s->gpu) : NULL; }
 
 SFT_FUNC void sft_frame_begin(void) { }
+/* ---------------------------------------------------------------- dynamic meshes (sofren2.c:8480-8951)
+ * Geometry pushed between sft_dmesh_begin and sft_dmesh_end is packed into 64-vertex meshlets
+ * with fixed index templates, exactly as the reference does in its scratch arena; at the end it
+ * is uploaded as a transient model (sftg_model_upload_transient) and drawn as an instance this
+ * frame.  Meshes and transient models are released at sft_frame_end. */
+struct sft_dmesh {
+    enum sft_dmesh_type type;
+    sft_mat_handle material;
+    u32 max_meshlets, curr_meshlet, curr_vert, max_verts_per_chunk;
+    f32* attr;                 /* [meshlet][10][64]: x y z nx ny nz u v lu lv */
+    f32* cull;                 /* [meshlet][8]: sphere centre, radius, cone axis, cutoff */
+    u8* inds;                  /* [meshlet][512] */
+    struct sft_dmesh* next;
+};
+struct sft__transient { sft_model* model; struct sft__transient* next; };
+
+static void sft__dmesh_release_frame(void) {
+    struct sft__state* s = sft__s;
+    for (struct sft_dmesh* d = s->dmesh_list; d;) { struct sft_dmesh* n = d->next; free(d->attr); free(d->cull); free(d->inds); free(d); d = n; }
+    s->dmesh_list = NULL;
+    for (struct sft__transient* t = s->transient_list; t;) {
+        struct sft__transient* n = t->next;
+        free(t->model->mesh_first); free(t->model->mesh_meshlets); free(t->model); free(t);
+        t = n;
+    }
+    if (s->transient_list) sftg_transient_reset(s->gpu);
+    s->transient_list = NULL;
+}
+
+SFT_FUNC sft_dmesh* sft_dmesh_begin(enum sft_dmesh_type type, sft_mat_handle material, u32 max_prims) {
+    if (0 == max_prims) return NULL;
+    const u32 max_verts = (SFT_DMESH_QUADS == type) ? 64 : 63;
+    const u32 total_verts = max_prims * ((SFT_DMESH_QUADS == type) ? 4 : 3);
+    const u32 max_meshlets = (((total_verts + max_verts - 1) / max_verts) + 8 - 1) & ~(u32)(8 - 1);
+    sft_dmesh* dm = (sft_dmesh*)calloc(1, sizeof(sft_dmesh));
+    dm->type = type; dm->material = material;
+    dm->max_meshlets = max_meshlets; dm->max_verts_per_chunk = max_verts;
+    dm->attr = (f32*)calloc((size_t)max_meshlets * 640, 4);
+    dm->cull = (f32*)calloc((size_t)max_meshlets * 8, 4);
+    dm->inds = (u8*)calloc((size_t)max_meshlets * 512, 1);
+    dm->next = sft__s->dmesh_list;
+    sft__s->dmesh_list = dm;
+    return dm;
+}
+
+/* sft__dmesh_finalize_chunk (2816-2879) */
+static void sft__dmesh_finalize(sft_dmesh* dm) {
+    if (0 == dm->curr_vert || dm->curr_meshlet >= dm->max_meshlets) return;
+    f32* a = dm->attr + (size_t)dm->curr_meshlet * 640;
+    for (u32 i = dm->curr_vert; i < 64; i++)   /* trailing vertices collapse onto vertex 0 */
+        for (u32 k = 0; k < 10; k++) a[k * 64 + i] = a[k * 64];
+    f32 mn[3] = { 1e30f, 1e30f, 1e30f }, mx[3] = { -1e30f, -1e30f, -1e30f };
+    for (u32 i = 0; i < dm->curr_vert; i++)
+        for (u32 k = 0; k < 3; k++) {
+            const f32 v = a[k * 64 + i];
+            if (v < mn[k]) mn[k] = v;
+            if (v > mx[k]) mx[k] = v;
+        }
+    const f32 cx = (mn[0] + mx[0]) * 0.5f, cy = (mn[1] + mx[1]) * 0.5f, cz = (mn[2] + mx[2]) * 0.5f;
+    const f32 dx = mx[0] - cx, dy = mx[1] - cy, dz = mx[2] - cz;
+    f32* c = dm->cull + (size_t)dm->curr_meshlet * 8;
+    c[0] = cx; c[1] = cy; c[2] = cz; c[3] = sqrtf(dx * dx + dy * dy + dz * dz);
+    c[4] = 0.f; c[5] = 0.f; c[6] = 1.f; c[7] = 2.f;   /* cone test always passes */
+    memcpy(dm->inds + (size_t)dm->curr_meshlet * 512, SFT_DMESH_QUADS == dm->type ? sft__s->dmesh_quad_inds : sft__s->dmesh_tri_inds, 512);
+    dm->curr_meshlet++;
+    dm->curr_vert = 0;
+}
+
+SFT_FUNC void sft_dmesh_push_quad_4n(sft_dmesh* dm, sftvec p0, sftvec p1, sftvec p2, sftvec p3, f32 u0, f32 v0, f32 u1, f32 v1,
+                                     sftvec n0, sftvec n1, sftvec n2, sftvec n3) {
+    if (dm->curr_vert >= dm->max_verts_per_chunk) sft__dmesh_finalize(dm);
+    if (dm->curr_meshlet >= dm->max_meshlets) return;
+    f32* a = dm->attr + (size_t)dm->curr_meshlet * 640;
+    const u32 v = dm->curr_vert;
+    const sftvec P[4] = { p0, p1, p2, p3 }, N[4] = { n0, n1, n2, n3 };
+    const f32 U[4] = { u0, u1, u1, u0 }, V[4] = { v0, v0, v1, v1 };
+    for (u32 k = 0; k < 4; k++) {
+        a[v + k] = P[k].x; a[64 + v + k] = P[k].y; a[128 + v + k] = P[k].z;
+        a[192 + v + k] = N[k].x; a[256 + v + k] = N[k].y; a[320 + v + k] = N[k].z;
+        a[384 + v + k] = U[k]; a[448 + v + k] = V[k]; a[512 + v + k] = 0.f; a[576 + v + k] = 0.f;
+    }
+    dm->curr_vert += 4;
+}
+
+SFT_FUNC void sft_dmesh_push_quad(sft_dmesh* dm, sftvec p0, sftvec p1, sftvec p2, sftvec p3, f32 u0, f32 v0, f32 u1, f32 v1, sftvec normal) {
+    sft_dmesh_push_quad_4n(dm, p0, p1, p2, p3, u0, v0, u1, v1, normal, normal, normal, normal);
+}
+
+SFT_FUNC void sft_dmesh_push_tri(sft_dmesh* dm, sftvec p0, sftvec p1, sftvec p2, f32 u0, f32 v0, f32 u1, f32 v1, f32 u2, f32 v2, sftvec normal) {
+    if (dm->curr_vert >= dm->max_verts_per_chunk) sft__dmesh_finalize(dm);
+    if (dm->curr_meshlet >= dm->max_meshlets) return;
+    f32* a = dm->attr + (size_t)dm->curr_meshlet * 640;
+    const u32 v = dm->curr_vert;
+    const sftvec P[3] = { p0, p1, p2 };
+    const f32 U[3] = { u0, u1, u2 }, V[3] = { v0, v1, v2 };
+    for (u32 k = 0; k < 3; k++) {
+        a[v + k] = P[k].x; a[64 + v + k] = P[k].y; a[128 + v + k] = P[k].z;
+        a[192 + v + k] = normal.x; a[256 + v + k] = normal.y; a[320 + v + k] = normal.z;
+        a[384 + v + k] = U[k]; a[448 + v + k] = V[k]; a[512 + v + k] = 0.f; a[576 + v + k] = 0.f;
+    }
+    dm->curr_vert += 3;
+}
+
+SFT_FUNC u8 sft_dmesh_alloc_quads(sft_dmesh* dm, u32 count, sft_dmesh_qb* out) {
+    u32 room = (dm->max_verts_per_chunk - dm->curr_vert) / 4;
+    if (0 == room) { sft__dmesh_finalize(dm); room = dm->max_verts_per_chunk / 4; }
+    if (dm->curr_meshlet >= dm->max_meshlets) return 0;
+    const u32 n = count < room ? count : room;
+    f32* a = dm->attr + (size_t)dm->curr_meshlet * 640;
+    out->x = a; out->y = a + 64; out->z = a + 128; out->nx = a + 192; out->ny = a + 256; out->nz = a + 320;
+    out->u = a + 384; out->v = a + 448;
+    out->vert_offset = dm->curr_vert;
+    out->allocated_count = n;
+    dm->curr_vert += n * 4;
+    return 1;
+}
+
+SFT_FUNC void sft_dmesh_end(sft_dmesh* dm, const sftmat* opt_transform) {
+    if (!dm) return;
+    if (dm->curr_vert > 0) sft__dmesh_finalize(dm);
+    if (0 == dm->curr_meshlet) return;
+    sftg_mesh_desc md;
+    memset(&md, 0, sizeof(md));
+    md.meshlet_count = dm->curr_meshlet; md.attr = dm->attr; md.inds = dm->inds; md.cull = dm->cull;
+    md.material = (dm->material == SFT_INVALID_HANDLE) ? -1 : (i32)SFT_MAT_INDEX(dm->material);
+    md.lightmap_texture = -1;
+    sftg_model_desc d;
+    memset(&d, 0, sizeof(d));
+    d.mesh_count = 1; d.meshes = &md;
+    sft_model* m = (sft_model*)calloc(1, sizeof(sft_model));
+    m->skeleton_id = -1; m->mesh_count = 1; m->total_meshlets = dm->curr_meshlet;
+    m->mesh_first = (u32*)calloc(2, 4); m->mesh_meshlets = (u32*)calloc(2, 4); m->mesh_meshlets[0] = dm->curr_meshlet;
+    if (sftg_model_upload_transient(sft__s->gpu, &d, &m->device_id)) {
+        fprintf(stderr, "sofren2-gb300: dynamic mesh upload failed: %s\n", sftg_last_error(sft__s->gpu));
+        free(m->mesh_first); free(m->mesh_meshlets); free(m);
+        return;
+    }
+    struct sft__transient* t = (struct sft__transient*)calloc(1, sizeof(*t));
+    t->model = m; t->next = sft__s->transient_list; sft__s->transient_list = t;
+    sft_instance inst;
+    memset(&inst, 0, sizeof(inst));
+    inst.model = m;
+    inst.transform = opt_transform ? *opt_transform : sft_m_identity();
+    sft_draw_instance(&inst);
+}
+
+/* the reference's shape helpers (1556-1590) */
+static sftvec sft__v_face_normal(sftvec a, sftvec b, sftvec c) { return sft_v_norm(sft_v_cross(sft_v_sub(b, a), sft_v_sub(c, a))); }
+static sftvec sft__v_perpendicular(sftvec v) {
+    f32 mn = fabsf(v.x);
+    sftvec ax = { 1.f, 0.f, 0.f };
+    if (fabsf(v.y) < mn) { mn = fabsf(v.y); ax = SFT_V(0.f, 1.f, 0.f); }
+    if (fabsf(v.z) < mn) ax = SFT_V(0.f, 0.f, 1.f);
+    return SFT_V(v.y * ax.z - v.z * ax.y, v.z * ax.x - v.x * ax.z, v.x * ax.y - v.y * ax.x);
+}
+
+SFT_FUNC void sft_draw_cube(sft_dmesh* dm) {   /* 8480-8506 */
+    sft_dmesh_push_quad(dm, SFT_V(-0.5f, -0.5f, -0.5f), SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(0.5f, 0.5f, -0.5f), SFT_V(0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 0.f, -1.f));
+    sft_dmesh_push_quad(dm, SFT_V(0.5f, -0.5f, -0.5f), SFT_V(0.5f, 0.5f, -0.5f), SFT_V(0.5f, 0.5f, 0.5f), SFT_V(0.5f, -0.5f, 0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(1.f, 0.f, 0.f));
+    sft_dmesh_push_quad(dm, SFT_V(0.5f, -0.5f, 0.5f), SFT_V(0.5f, 0.5f, 0.5f), SFT_V(-0.5f, 0.5f, 0.5f), SFT_V(-0.5f, -0.5f, 0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 0.f, 1.f));
+    sft_dmesh_push_quad(dm, SFT_V(-0.5f, -0.5f, 0.5f), SFT_V(-0.5f, 0.5f, 0.5f), SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(-0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(-1.f, 0.f, 0.f));
+    sft_dmesh_push_quad(dm, SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(-0.5f, 0.5f, 0.5f), SFT_V(0.5f, 0.5f, 0.5f), SFT_V(0.5f, 0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 1.f, 0.f));
+    sft_dmesh_push_quad(dm, SFT_V(0.5f, -0.5f, 0.5f), SFT_V(-0.5f, -0.5f, 0.5f), SFT_V(-0.5f, -0.5f, -0.5f), SFT_V(0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, -1.f, 0.f));
+}
+
+SFT_FUNC void sft_draw_cube_inv(sft_dmesh* dm) {   /* 8508-8529 */
+    sft_dmesh_push_quad(dm, SFT_V(0.5f, 0.5f, -0.5f), SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(-0.5f, -0.5f, -0.5f), SFT_V(0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 0.f, 1.f));
+    sft_dmesh_push_quad(dm, SFT_V(0.5f, 0.5f, 0.5f), SFT_V(0.5f, 0.5f, -0.5f), SFT_V(0.5f, -0.5f, -0.5f), SFT_V(0.5f, -0.5f, 0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(-1.f, 0.f, 0.f));
+    sft_dmesh_push_quad(dm, SFT_V(-0.5f, 0.5f, 0.5f), SFT_V(0.5f, 0.5f, 0.5f), SFT_V(0.5f, -0.5f, 0.5f), SFT_V(-0.5f, -0.5f, 0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 0.f, -1.f));
+    sft_dmesh_push_quad(dm, SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(-0.5f, 0.5f, 0.5f), SFT_V(-0.5f, -0.5f, 0.5f), SFT_V(-0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(1.f, 0.f, 0.f));
+    sft_dmesh_push_quad(dm, SFT_V(0.5f, 0.5f, 0.5f), SFT_V(-0.5f, 0.5f, 0.5f), SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(0.5f, 0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, -1.f, 0.f));
+    sft_dmesh_push_quad(dm, SFT_V(-0.5f, -0.5f, -0.5f), SFT_V(-0.5f, -0.5f, 0.5f), SFT_V(0.5f, -0.5f, 0.5f), SFT_V(0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 1.f, 0.f));
+}
+
+SFT_FUNC void sft_draw_sphere(sft_dmesh* dm, i32 rings, i32 slices) {   /* 8531-8577: rings of quads, rotated incrementally */
+    const f32 ring_angle = SFT_PI / (rings + 1);
+    const f32 slice_angle = 2.f * SFT_PI / slices;
+    const f32 cr = cosf(ring_angle), sr = sinf(ring_angle), cs = cosf(slice_angle), ss = sinf(slice_angle);
+    sftvec v[4] = { { 0.f, 0.f, 0.f }, { 0.f, 0.f, 0.f }, { 0.f, 1.f, 0.f }, { sr, cr, 0.f } };
+    for (i32 i = 0; i <= rings; i++) {
+        for (i32 j = 0; j < slices; j++) {
+            v[0] = v[2]; v[1] = v[3];
+            v[2] = SFT_V(cs * v[2].x - ss * v[2].z, v[2].y, ss * v[2].x + cs * v[2].z);
+            v[3] = SFT_V(cs * v[3].x - ss * v[3].z, v[3].y, ss * v[3].x + cs * v[3].z);
+            sft_dmesh_push_quad_4n(dm, v[0], v[2], v[3], v[1], 0.f, 0.f, 1.f, 1.f,
+                                   sft_v_norm(v[0]), sft_v_norm(v[2]), sft_v_norm(v[3]), sft_v_norm(v[1]));
+        }
+        v[2] = v[3];
+        v[3] = SFT_V(cr * v[3].x + sr * v[3].y, -sr * v[3].x + cr * v[3].y, v[3].z);
+    }
+}
+
+/* one vertex of a capsule cap ring (8600-8630) */
+static sftvec sft__cap_vertex(sftvec c, sftvec b0, sftvec b1, sftvec b2, f32 r, f32 sa, f32 ra, i32 j, i32 i) {
+    const f32 rs = sinf(sa * (j)) * cosf(ra * (i)), rc = cosf(sa * (j)) * cosf(ra * (i)), s0 = sinf(ra * (i));
+    return SFT_V(c.x + (s0 * b0.x + rs * b1.x + rc * b2.x) * r, c.y + (s0 * b0.y + rs * b1.y + rc * b2.y) * r,
+                 c.z + (s0 * b0.z + rs * b1.z + rc * b2.z) * r);
+}
+
+SFT_FUNC void sft_draw_capsule(sft_dmesh* dm, sftvec start_pos, sftvec end_pos, f32 radius, i32 slices, i32 rings) {   /* 8579-8668 */
+    if (slices < 3) slices = 3;
+    sftvec dir = sft_v_sub(end_pos, start_pos);
+    const u8 sphere_case = (0.f == dir.x && 0.f == dir.y && 0.f == dir.z);
+    if (sphere_case) dir = SFT_V(0.f, 1.f, 0.f);
+    sftvec b0 = sft_v_norm(dir);
+    const sftvec b1 = sft_v_norm(sft__v_perpendicular(dir));
+    const sftvec b2 = sft_v_norm(sft_v_cross(b1, dir));
+    sftvec cc = end_pos;
+    const f32 sa = 2.f * SFT_PI / slices, ra = 0.5f * SFT_PI / rings;
+    for (i32 c = 0; c < 2; c++) {
+        for (i32 i = 0; i < rings; i++)
+            for (i32 j = 0; j < slices; j++) {
+                const sftvec w1 = sft__cap_vertex(cc, b0, b1, b2, radius, sa, ra, j + 0, i + 0);
+                const sftvec w2 = sft__cap_vertex(cc, b0, b1, b2, radius, sa, ra, j + 1, i + 0);
+                const sftvec w3 = sft__cap_vertex(cc, b0, b1, b2, radius, sa, ra, j + 0, i + 1);
+                const sftvec w4 = sft__cap_vertex(cc, b0, b1, b2, radius, sa, ra, j + 1, i + 1);
+                const sftvec fc = sft_v_mul(sft_v_add(sft_v_add(w1, w2), sft_v_add(w3, w4)), 0.25f);
+                const sftvec fn = sft_v_norm(sft_v_sub(fc, cc));
+                if (0 == c) sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, fn);
+                else sft_dmesh_push_quad(dm, w3, w4, w2, w1, 0.f, 0.f, 1.f, 1.f, fn);
+            }
+        cc = start_pos;
+        b0 = sft_v_mul(b0, -1.f);
+    }
+    if (!sphere_case)
+        for (i32 j = 0; j < slices; j++) {
+            const f32 rs1 = sinf(sa * (j + 0)) * radius, rc1 = cosf(sa * (j + 0)) * radius;
+            const f32 rs2 = sinf(sa * (j + 1)) * radius, rc2 = cosf(sa * (j + 1)) * radius;
+            const sftvec w1 = SFT_V(start_pos.x + rs1 * b1.x + rc1 * b2.x, start_pos.y + rs1 * b1.y + rc1 * b2.y, start_pos.z + rs1 * b1.z + rc1 * b2.z);
+            const sftvec w2 = SFT_V(start_pos.x + rs2 * b1.x + rc2 * b2.x, start_pos.y + rs2 * b1.y + rc2 * b2.y, start_pos.z + rs2 * b1.z + rc2 * b2.z);
+            const sftvec w3 = SFT_V(end_pos.x + rs1 * b1.x + rc1 * b2.x, end_pos.y + rs1 * b1.y + rc1 * b2.y, end_pos.z + rs1 * b1.z + rc1 * b2.z);
+            const sftvec w4 = SFT_V(end_pos.x + rs2 * b1.x + rc2 * b2.x, end_pos.y + rs2 * b1.y + rc2 * b2.y, end_pos.z + rs2 * b1.z + rc2 * b2.z);
+            sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(w3, w1, w2));
+        }
+}
+
+SFT_FUNC void sft_draw_cylinder(sft_dmesh* dm, sftvec start_pos, sftvec end_pos, f32 start_radius, f32 end_radius, i32 sides) {   /* 8672-8718 */
+    if (sides < 3) sides = 3;
+    const sftvec dir = sft_v_sub(end_pos, start_pos);
+    if (0 == dir.x && 0 == dir.y && 0 == dir.z) return;
+    const sftvec b1 = sft_v_norm(sft__v_perpendicular(dir));
+    const sftvec b2 = sft_v_norm(sft_v_cross(b1, dir));
+    const f32 ang = (2.f * SFT_PI) / sides;
+    for (i32 i = 0; i < sides; i++) {
+        const f32 s1 = sinf(ang * (i + 0)) * start_radius, c1 = cosf(ang * (i + 0)) * start_radius;
+        const f32 s2 = sinf(ang * (i + 1)) * start_radius, c2 = cosf(ang * (i + 1)) * start_radius;
+        const f32 s3 = sinf(ang * (i + 0)) * end_radius, c3 = cosf(ang * (i + 0)) * end_radius;
+        const f32 s4 = sinf(ang * (i + 1)) * end_radius, c4 = cosf(ang * (i + 1)) * end_radius;
+        const sftvec w1 = SFT_V(start_pos.x + s1 * b1.x + c1 * b2.x, start_pos.y + s1 * b1.y + c1 * b2.y, start_pos.z + s1 * b1.z + c1 * b2.z);
+        const sftvec w2 = SFT_V(start_pos.x + s2 * b1.x + c2 * b2.x, start_pos.y + s2 * b1.y + c2 * b2.y, start_pos.z + s2 * b1.z + c2 * b2.z);
+        const sftvec w3 = SFT_V(end_pos.x + s3 * b1.x + c3 * b2.x, end_pos.y + s3 * b1.y + c3 * b2.y, end_pos.z + s3 * b1.z + c3 * b2.z);
+        const sftvec w4 = SFT_V(end_pos.x + s4 * b1.x + c4 * b2.x, end_pos.y + s4 * b1.y + c4 * b2.y, end_pos.z + s4 * b1.z + c4 * b2.z);
+        if (start_radius > 0) sft_dmesh_push_quad(dm, start_pos, w2, w1, w1, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(start_pos, w2, w1));
+        sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(w3, w1, w2));
+        if (end_radius > 0) sft_dmesh_push_quad(dm, end_pos, w3, w4, w4, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(end_pos, w3, w4));
+    }
+}
+
 SFT_FUNC void sft_frame_end(void) {
     sft__s->n_inst_claimed = 0; sft__s->n_inst = 0; sft__s->total_ss = 0;
     sft__s->n_point = 0; sft__s->n_dir = 0; sft__s->n_prox = 0; sft__s->n_bones = 0; sft__s->n_transient = 0;
+    if (!sft__s->batching) sft__dmesh_release_frame();   /* a batch keeps them until it is submitted */
 }
 
 /* ---------------------------------------------------------------- frame setup */
@@ -946,6 +1246,7 @@ SFT_FUNC i32 sft_batch_submit(void) {
     const int rc = sftg_frames_render(s->gpu, s->batch_fd, s->n_batch, any_host ? s->batch_color : NULL, s->batch_pitch, NULL);
     for (u32 i = 0; i < s->n_batch; i++) free(s->batch_mem[i]);
     s->n_batch = 0;
+    sft__dmesh_release_frame();
     if (rc) fprintf(stderr, "sofren2-gb300: sft_batch_submit failed (%d): %s\n", rc, sftg_last_error(s->gpu));
     return rc;
 }

@@ -74,6 +74,10 @@ struct sftg_ctx {
     uint32_t* d_color = nullptr;
     size_t d_color_cap = 0;
     sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
+    /* transient models (one frame's dynamic meshes): pool marks where they start */
+    bool tr_live = false, tr_pinned = false;
+    uint32_t tr_meshlets = 0, tr_skin = 0, tr_blas = 0;
+    size_t tr_models = 0;
     /* skeletons and animations (sftg_skeleton_upload) */
     dpool p_skels, p_bones, p_anims, p_samplers, p_channels, p_keys, p_order, p_levels, p_pose_io;
     std::vector<sftg_skel_dev> h_skels;
@@ -196,9 +200,14 @@ extern "C" int sftg_material_set(sftg_ctx* ctx, int32_t index, int32_t texture, 
     return SFTG_OK;
 }
 
-extern "C" int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model) {
+static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model, bool transient) {
     if (!ctx || !d || !out_model) return SFTG_E_ARG;
     CK(cudaSetDevice(ctx->device));
+    if (transient && !ctx->tr_live) {   /* where the frame's transient models start */
+        ctx->tr_live = true; ctx->tr_pinned = false;
+        ctx->tr_meshlets = ctx->n_meshlets; ctx->tr_skin = ctx->n_skin; ctx->tr_blas = ctx->n_blas; ctx->tr_models = ctx->h_models.size();
+    }
+    if (!transient && ctx->tr_live) ctx->tr_pinned = true;   /* a resident model after them: they stay */
     uint32_t total = 0;
     for (uint32_t k = 0; k < d->mesh_count; k++) total += d->meshes[k].meshlet_count;
     std::vector<float> attr((size_t)total * 640), cull((size_t)total * 8);
@@ -272,6 +281,29 @@ extern "C" int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_
     ctx->tables_dirty = true;
     *out_model = (int32_t)ctx->h_models.size() - 1;
     return SFTG_OK;
+}
+
+extern "C" int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model) {
+    return model_upload(ctx, d, out_model, false);
+}
+
+extern "C" int sftg_model_upload_transient(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model) {
+    return model_upload(ctx, d, out_model, true);
+}
+
+extern "C" void sftg_transient_reset(sftg_ctx* ctx) {
+    if (!ctx || !ctx->tr_live) return;
+    if (!ctx->tr_pinned) {   /* drop the transient tail of every pool and table */
+        ctx->n_meshlets = ctx->tr_meshlets; ctx->n_skin = ctx->tr_skin; ctx->n_blas = ctx->tr_blas;
+        ctx->h_models.resize(ctx->tr_models);
+        ctx->h_mesh_skinned.resize(ctx->tr_models); ctx->h_mesh_first.resize(ctx->tr_models); ctx->h_mesh_count.resize(ctx->tr_models);
+        ctx->ml_attr.size = (size_t)ctx->n_meshlets * 2560; ctx->ml_inds.size = (size_t)ctx->n_meshlets * 512;
+        ctx->ml_cull.size = (size_t)ctx->n_meshlets * 32; ctx->ml_info.size = (size_t)ctx->n_meshlets * sizeof(sftg_meshlet_info);
+        ctx->skin_j.size = (size_t)ctx->n_skin * 512; ctx->skin_w.size = (size_t)ctx->n_skin * 256;
+        ctx->blas.size = (size_t)ctx->n_blas * 256;
+        ctx->tables_dirty = true;
+    }
+    ctx->tr_live = false; ctx->tr_pinned = false;
 }
 
 static int sync_tables(sftg_ctx* ctx) {

@@ -59,6 +59,19 @@ def main(names: list[str]) -> None:
         out = reference_pose(pose_blob(rig, req), len(rig["bones"]), len(req))
         golden["pose"] = {"rig_seed": 6001, "requests": len(req), "sha256": gc.sha(out)}
         print("pose", golden["pose"]["sha256"][:16], flush=True)
+    if not names or "dmesh" in names:
+        # the dynamic-mesh scene (oracle/dmesh_scene.h) rendered by the reference, per frame
+        import tempfile
+        import numpy as np
+        dm = {}
+        for S in (1, 4):
+            with tempfile.TemporaryDirectory() as td:
+                op = os.path.join(td, "dm.bin")
+                subprocess.run([os.path.join(ROOT, "oracle", "_ref", f"dmesh_harness_{S}x"), op], check=True)
+                frames = np.fromfile(op, np.uint32).reshape(-1, 360, 640)
+                dm[str(S)] = [gc.sha(f) for f in frames]
+        golden["dmesh"] = dm
+        print("dmesh", {k: [h[:12] for h in v] for k, v in dm.items()}, flush=True)
     json.dump(golden, open(path, "w"), indent=1, sort_keys=True)
 
 
