@@ -212,6 +212,28 @@ int sftg_skeleton_upload(sftg_ctx* ctx, const sftg_bone_desc* bones, uint32_t bo
  * of range leaves its matrices untouched, as sft_pose_update returns early. */
 int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* requests, uint32_t n, float* posed, float* global);
 
+/* Ray queries against resident models (sft_raycast_instance, sofren2.c:3733-3837), any number in
+ * one launch, one thread per ray.  A ray names a model and its instance transform; results equal
+ * the reference's bit for bit, including its treatment of the transform: the ray enters model
+ * space through the transposed rotation rows alone (sft_m_mul_vec adds no translation) and the
+ * hit position leaves it the same way.  Skinned models are queried in their bind pose, as in the
+ * reference.  A ray whose model is not resident, or has no BLAS, gives hit 0 and distance
+ * max_dist; hit 2 marks a walk whose stack overflowed (a BLAS deeper than 18 levels). */
+typedef struct sftg_ray {
+    float transform[16];       /* the instance's transform, row-major sftmat */
+    float origin[3], dir[3];   /* world space; dir need not be normalised */
+    float max_dist;
+    int32_t model;             /* resident model (sftg_model_upload) */
+} sftg_ray;
+typedef struct sftg_ray_hit {  /* sft_ray_hit (sofren2.c:895-900) */
+    uint32_t hit;
+    float distance, pos[3], normal[3];
+} sftg_ray_hit;
+/* host arrays; returns when hits is filled (SFTG_E_DEVICE_STATUS if a walk overflowed) */
+int sftg_raycast(sftg_ctx* ctx, const sftg_ray* rays, uint32_t n, sftg_ray_hit* hits);
+/* device arrays, queued on the context's stream (sftg_stream); returns without waiting */
+int sftg_raycast_device(sftg_ctx* ctx, const sftg_ray* d_rays, uint32_t n, sftg_ray_hit* d_hits);
+
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */

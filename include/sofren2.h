@@ -100,6 +100,9 @@ typedef struct sft_instance {
     sftmat* posed_bone_matrices;
 } sft_instance;
 
+/* sofren2.c:895-900 */
+typedef struct sft_ray_hit { u8 hit; f32 distance; sftvec pos; sftvec normal; } sft_ray_hit;
+
 /* capsule shadow proxy in model (or bone) space, sofren2.c:985-989 */
 typedef struct sft_shadow_proxy { sftvec posa, posb; f32 radius; u32 bone_ind; } sft_shadow_proxy;
 
@@ -138,6 +141,15 @@ SFT_FUNC sftmat sft_m_proj(f32 fov_deg, f32 aspect, f32 near_z, f32 far_z);
 SFT_FUNC sftmat sft_m_mul(sftmat a, sftmat b);
 SFT_FUNC sftmat sft_m_qinv(sftmat m);
 SFT_FUNC sftmat sft_m_view_look_at(sftvec pos, sftvec target, sftvec up);
+SFT_FUNC sftmat sft_m_model_look_at(sftvec pos, sftvec target, sftvec up);
+SFT_FUNC sftmat sft_m_ortho(f32 left, f32 right, f32 bottom, f32 top, f32 near_z, f32 far_z);
+SFT_FUNC sftvec sft_m_mul_vec(sftmat m, sftvec v);
+SFT_FUNC sftvec sft_m_mul_quat(sftmat m, sftquat v);
+SFT_FUNC void sft_m_decompose(sftmat m, sftvec* pos, sftvec* rot, sftvec* scale);
+SFT_FUNC sftquat sft_q_invert(sftquat q);
+SFT_FUNC sftvec sft_v_face_normal(sftvec a, sftvec b, sftvec c);
+SFT_FUNC sftvec sft_v_perpendicular(sftvec v);
+SFT_FUNC sftvec sft_v_rotate_by_quat(sftvec v, sftquat q);
 SFT_FUNC sftmat sft_m_from_quat(sftquat q);
 SFT_FUNC sftquat sft_q_mul(sftquat a, sftquat b);
 SFT_FUNC sftquat sft_q_slerp(sftquat a, sftquat b, f32 t);
@@ -175,6 +187,11 @@ SFT_FUNC u8 sft_dmesh_alloc_quads(sft_dmesh* dm, u32 count, sft_dmesh_qb* out_ba
 SFT_FUNC void sft_dmesh_end(sft_dmesh* dm, const sftmat* opt_transform);
 SFT_FUNC sft_pose* sft_pose_create(const sft_model* model, sft_arena* arena);
 SFT_FUNC void sft_pose_update(sft_pose* pose, i32 anim_id, f32 time);
+/* ray queries (sofren2.c:3733): answered on the GPU; the batch form is one launch for n rays,
+ * ray k against insts[k] */
+SFT_FUNC sft_ray_hit sft_raycast_instance(const sft_instance* inst, sftvec origin, sftvec dir, f32 max_dist);
+SFT_FUNC void sft_raycast_batch(const sft_instance* const* insts, const sftvec* origins, const sftvec* dirs, const f32* max_dists,
+                                u32 n, sft_ray_hit* out);
 
 /* lights (827-832) */
 SFT_FUNC void sft_set_ambient_light(f32 r, f32 g, f32 b);
@@ -209,6 +226,8 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
                                      u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
                                      sft_arena* arena);
 SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model);
+/* model loading (sofren2.c:859-862): QSF2 files; GLB needs cgltf and is not provided */
+SFT_FUNC sft_model* sft_model_load_qsf(const char* path, sft_arena* arena);
 /* extension: the model's skeleton and animation tracks, what the reference's GLB loader fills
  * (sft_bone / sft_animation, sofren2.c:1000-1049); uploaded for sft_pose_update, which then
  * evaluates poses on the GPU.  bone_count must be the model's.  Returns 0 or an sftg error. */
@@ -409,6 +428,78 @@ SFT_FUNC sftquat sft_q_slerp(sftquat a, sftquat b, f32 t) {
     const f32 s0 = cosf(th) - dot * st * is0, s1 = st * is0;
     sftquat r = { a.x * s0 + b.x * s1, a.y * s0 + b.y * s1, a.z * s0 + b.z * s1, a.w * s0 + b.w * s1 };
     return sft_q_norm(r);
+}
+
+/* the remaining scalar helpers of the public math set (sofren2.c:1556-1600, 1657-1800, 1894) */
+SFT_FUNC sftmat sft_m_model_look_at(sftvec pos, sftvec target, sftvec up) {
+    const sftvec fwd = sft_v_norm(sft_v_sub(target, pos));
+    up = sft_v_norm(sft_v_sub(up, sft_v_mul(fwd, sft_v_dot(up, fwd))));
+    const sftvec right = sft_v_cross(up, fwd);
+    sftmat r;
+    r.m[0][0] = right.x; r.m[0][1] = right.y; r.m[0][2] = right.z; r.m[0][3] = 0.f;
+    r.m[1][0] = up.x; r.m[1][1] = up.y; r.m[1][2] = up.z; r.m[1][3] = 0.f;
+    r.m[2][0] = fwd.x; r.m[2][1] = fwd.y; r.m[2][2] = fwd.z; r.m[2][3] = 0.f;
+    r.m[3][0] = pos.x; r.m[3][1] = pos.y; r.m[3][2] = pos.z; r.m[3][3] = 1.f;
+    return r;
+}
+SFT_FUNC sftmat sft_m_ortho(f32 left, f32 right, f32 bottom, f32 top, f32 near_z, f32 far_z) {
+    sftmat r;
+    memset(&r, 0, sizeof(r));
+    r.m[0][0] = 2.f / (right - left); r.m[1][1] = 2.f / (top - bottom); r.m[2][2] = 1.f / (far_z - near_z);
+    r.m[3][0] = -(right + left) / (right - left); r.m[3][1] = -(top + bottom) / (top - bottom);
+    r.m[3][2] = -near_z / (far_z - near_z); r.m[3][3] = 1.f;
+    return r;
+}
+SFT_FUNC sftvec sft_m_mul_vec(sftmat m, sftvec v) {
+    sftvec r = { v.x * m.m[0][0] + v.y * m.m[1][0] + v.z * m.m[2][0], v.x * m.m[0][1] + v.y * m.m[1][1] + v.z * m.m[2][1],
+                 v.x * m.m[0][2] + v.y * m.m[1][2] + v.z * m.m[2][2] };
+    return r;
+}
+SFT_FUNC sftvec sft_m_mul_quat(sftmat m, sftquat v) {
+    sftvec r = { v.x * m.m[0][0] + v.y * m.m[1][0] + v.z * m.m[2][0] + v.w * m.m[3][0],
+                 v.x * m.m[0][1] + v.y * m.m[1][1] + v.z * m.m[2][1] + v.w * m.m[3][1],
+                 v.x * m.m[0][2] + v.y * m.m[1][2] + v.z * m.m[2][2] + v.w * m.m[3][2] };
+    return r;
+}
+/* translation from row 3, scale from the basis rows' lengths, rotation as x-y-z Euler angles
+ * (a rotation about y near +-90 degrees puts all of x's and z's share into x) */
+SFT_FUNC void sft_m_decompose(sftmat m, sftvec* pos, sftvec* rot, sftvec* scale) {
+    if (pos) { pos->x = m.m[3][0]; pos->y = m.m[3][1]; pos->z = m.m[3][2]; }
+    f32 sx = sqrtf(m.m[0][0] * m.m[0][0] + m.m[0][1] * m.m[0][1] + m.m[0][2] * m.m[0][2]);
+    f32 sy = sqrtf(m.m[1][0] * m.m[1][0] + m.m[1][1] * m.m[1][1] + m.m[1][2] * m.m[1][2]);
+    f32 sz = sqrtf(m.m[2][0] * m.m[2][0] + m.m[2][1] * m.m[2][1] + m.m[2][2] * m.m[2][2]);
+    if (scale) { scale->x = sx; scale->y = sy; scale->z = sz; }
+    if (!rot) return;
+    if (sx < SFT_EPSILON) sx = 1.f;
+    if (sy < SFT_EPSILON) sy = 1.f;
+    if (sz < SFT_EPSILON) sz = 1.f;
+    const f32 r00 = m.m[0][0] / sx, r01 = m.m[0][1] / sx, r02 = m.m[0][2] / sx;
+    const f32 r11 = m.m[1][1] / sy, r12 = m.m[1][2] / sy, r21 = m.m[2][1] / sz, r22 = m.m[2][2] / sz;
+    rot->y = -asinf(r02 < -1.f ? -1.f : (r02 > 1.f ? 1.f : r02));
+    if (cosf(rot->y) > SFT_EPSILON) { rot->x = atan2f(r12, r22); rot->z = atan2f(r01, r00); }
+    else { rot->x = atan2f(-r21, r11); rot->z = 0.f; }
+}
+SFT_FUNC sftquat sft_q_invert(sftquat q) {
+    sftquat r = q;
+    const f32 l2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+    if (0.f != l2) { const f32 il = 1.f / l2; r.x *= -il; r.y *= -il; r.z *= -il; r.w *= il; }
+    return r;
+}
+SFT_FUNC sftvec sft_v_face_normal(sftvec a, sftvec b, sftvec c) { return sft_v_norm(sft_v_cross(sft_v_sub(b, a), sft_v_sub(c, a))); }
+SFT_FUNC sftvec sft_v_perpendicular(sftvec v) {
+    f32 mn = fabsf(v.x);
+    sftvec ax = { 1.f, 0.f, 0.f };
+    if (fabsf(v.y) < mn) { mn = fabsf(v.y); ax.x = 0.f; ax.y = 1.f; ax.z = 0.f; }
+    if (fabsf(v.z) < mn) { ax.x = 0.f; ax.y = 0.f; ax.z = 1.f; }
+    sftvec r = { v.y * ax.z - v.z * ax.y, v.z * ax.x - v.x * ax.z, v.x * ax.y - v.y * ax.x };
+    return r;
+}
+SFT_FUNC sftvec sft_v_rotate_by_quat(sftvec v, sftquat q) {
+    sftvec r;
+    r.x = v.x * (q.x * q.x + q.w * q.w - q.y * q.y - q.z * q.z) + v.y * (2 * q.x * q.y - 2 * q.w * q.z) + v.z * (2 * q.x * q.z + 2 * q.w * q.y);
+    r.y = v.x * (2 * q.w * q.z + 2 * q.x * q.y) + v.y * (q.w * q.w - q.x * q.x + q.y * q.y - q.z * q.z) + v.z * (-2 * q.w * q.x + 2 * q.y * q.z);
+    r.z = v.x * (-2 * q.w * q.y + 2 * q.x * q.z) + v.y * (2 * q.w * q.x + 2 * q.y * q.z) + v.z * (q.w * q.w - q.x * q.x - q.y * q.y + q.z * q.z);
+    return r;
 }
 
 /* ---------------------------------------------------------------- arenas (sofren2.c:9456-9564) */
@@ -705,15 +796,6 @@ SFT_FUNC void sft_dmesh_end(sft_dmesh* dm, const sftmat* opt_transform) {
     sft_draw_instance(&inst);
 }
 
-/* the reference's shape helpers (1556-1590) */
-static sftvec sft__v_face_normal(sftvec a, sftvec b, sftvec c) { return sft_v_norm(sft_v_cross(sft_v_sub(b, a), sft_v_sub(c, a))); }
-static sftvec sft__v_perpendicular(sftvec v) {
-    f32 mn = fabsf(v.x);
-    sftvec ax = { 1.f, 0.f, 0.f };
-    if (fabsf(v.y) < mn) { mn = fabsf(v.y); ax = SFT_V(0.f, 1.f, 0.f); }
-    if (fabsf(v.z) < mn) ax = SFT_V(0.f, 0.f, 1.f);
-    return SFT_V(v.y * ax.z - v.z * ax.y, v.z * ax.x - v.x * ax.z, v.x * ax.y - v.y * ax.x);
-}
 
 SFT_FUNC void sft_draw_cube(sft_dmesh* dm) {   /* 8480-8506 */
     sft_dmesh_push_quad(dm, SFT_V(-0.5f, -0.5f, -0.5f), SFT_V(-0.5f, 0.5f, -0.5f), SFT_V(0.5f, 0.5f, -0.5f), SFT_V(0.5f, -0.5f, -0.5f), 0.f, 0.f, 1.f, 1.f, SFT_V(0.f, 0.f, -1.f));
@@ -764,7 +846,7 @@ SFT_FUNC void sft_draw_capsule(sft_dmesh* dm, sftvec start_pos, sftvec end_pos, 
     const u8 sphere_case = (0.f == dir.x && 0.f == dir.y && 0.f == dir.z);
     if (sphere_case) dir = SFT_V(0.f, 1.f, 0.f);
     sftvec b0 = sft_v_norm(dir);
-    const sftvec b1 = sft_v_norm(sft__v_perpendicular(dir));
+    const sftvec b1 = sft_v_norm(sft_v_perpendicular(dir));
     const sftvec b2 = sft_v_norm(sft_v_cross(b1, dir));
     sftvec cc = end_pos;
     const f32 sa = 2.f * SFT_PI / slices, ra = 0.5f * SFT_PI / rings;
@@ -791,7 +873,7 @@ SFT_FUNC void sft_draw_capsule(sft_dmesh* dm, sftvec start_pos, sftvec end_pos, 
             const sftvec w2 = SFT_V(start_pos.x + rs2 * b1.x + rc2 * b2.x, start_pos.y + rs2 * b1.y + rc2 * b2.y, start_pos.z + rs2 * b1.z + rc2 * b2.z);
             const sftvec w3 = SFT_V(end_pos.x + rs1 * b1.x + rc1 * b2.x, end_pos.y + rs1 * b1.y + rc1 * b2.y, end_pos.z + rs1 * b1.z + rc1 * b2.z);
             const sftvec w4 = SFT_V(end_pos.x + rs2 * b1.x + rc2 * b2.x, end_pos.y + rs2 * b1.y + rc2 * b2.y, end_pos.z + rs2 * b1.z + rc2 * b2.z);
-            sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(w3, w1, w2));
+            sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, sft_v_face_normal(w3, w1, w2));
         }
 }
 
@@ -799,7 +881,7 @@ SFT_FUNC void sft_draw_cylinder(sft_dmesh* dm, sftvec start_pos, sftvec end_pos,
     if (sides < 3) sides = 3;
     const sftvec dir = sft_v_sub(end_pos, start_pos);
     if (0 == dir.x && 0 == dir.y && 0 == dir.z) return;
-    const sftvec b1 = sft_v_norm(sft__v_perpendicular(dir));
+    const sftvec b1 = sft_v_norm(sft_v_perpendicular(dir));
     const sftvec b2 = sft_v_norm(sft_v_cross(b1, dir));
     const f32 ang = (2.f * SFT_PI) / sides;
     for (i32 i = 0; i < sides; i++) {
@@ -811,9 +893,9 @@ SFT_FUNC void sft_draw_cylinder(sft_dmesh* dm, sftvec start_pos, sftvec end_pos,
         const sftvec w2 = SFT_V(start_pos.x + s2 * b1.x + c2 * b2.x, start_pos.y + s2 * b1.y + c2 * b2.y, start_pos.z + s2 * b1.z + c2 * b2.z);
         const sftvec w3 = SFT_V(end_pos.x + s3 * b1.x + c3 * b2.x, end_pos.y + s3 * b1.y + c3 * b2.y, end_pos.z + s3 * b1.z + c3 * b2.z);
         const sftvec w4 = SFT_V(end_pos.x + s4 * b1.x + c4 * b2.x, end_pos.y + s4 * b1.y + c4 * b2.y, end_pos.z + s4 * b1.z + c4 * b2.z);
-        if (start_radius > 0) sft_dmesh_push_quad(dm, start_pos, w2, w1, w1, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(start_pos, w2, w1));
-        sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(w3, w1, w2));
-        if (end_radius > 0) sft_dmesh_push_quad(dm, end_pos, w3, w4, w4, 0.f, 0.f, 1.f, 1.f, sft__v_face_normal(end_pos, w3, w4));
+        if (start_radius > 0) sft_dmesh_push_quad(dm, start_pos, w2, w1, w1, 0.f, 0.f, 1.f, 1.f, sft_v_face_normal(start_pos, w2, w1));
+        sft_dmesh_push_quad(dm, w3, w1, w2, w4, 0.f, 0.f, 1.f, 1.f, sft_v_face_normal(w3, w1, w2));
+        if (end_radius > 0) sft_dmesh_push_quad(dm, end_pos, w3, w4, w4, 0.f, 0.f, 1.f, 1.f, sft_v_face_normal(end_pos, w3, w4));
     }
 }
 
@@ -1000,10 +1082,21 @@ SFT_FUNC void sft_material_release(sft_mat_handle mat) {
 }
 
 /* ---------------------------------------------------------------- models */
+static sft_model* sft__model_create(const sft_mesh_data* meshes, u32 mesh_count, const sft_shadow_proxy* proxies, u32 proxy_count,
+                                    u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count, const void* blas_nodes,
+                                    u32 blas_count, u32 blas_root);
+
 SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count, const sft_shadow_proxy* proxies,
                                      u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
                                      sft_arena* arena) {
     (void)arena;
+    return sft__model_create(meshes, mesh_count, proxies, proxy_count, bone_count, lightmaps, lightmap_count, NULL, 0, 0);
+}
+
+/* a model from meshlet arrays; the BLAS is built (blas_nodes NULL) or taken as given */
+static sft_model* sft__model_create(const sft_mesh_data* meshes, u32 mesh_count, const sft_shadow_proxy* proxies, u32 proxy_count,
+                                    u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count, const void* blas_nodes,
+                                    u32 blas_count, u32 blas_root) {
     sft_model* m = (sft_model*)calloc(1, sizeof(sft_model));
     m->mesh_count = mesh_count; m->bone_count = bone_count; m->skeleton_id = -1;
     m->mesh_first = (u32*)calloc(mesh_count + 1, 4); m->mesh_meshlets = (u32*)calloc(mesh_count + 1, 4);
@@ -1024,11 +1117,17 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
     if (proxy_count) memcpy(m->proxies, proxies, proxy_count * sizeof(sft_shadow_proxy));
     /* BLAS over every non-padding triangle, in meshlet / batch / lane order (sofren2.c:3526-3617) */
     u32 ntri = 0;
+    if (blas_nodes && blas_count) {   /* prebuilt (a QSF2 file carries its BLAS) */
+        m->blas = (sft__node*)calloc(blas_count + 1, sizeof(sft__node));
+        memcpy(m->blas, blas_nodes, (size_t)blas_count * sizeof(sft__node));
+        m->blas_count = blas_count; m->blas_root = blas_root;
+    } else {
     for (u32 k = 0; k < mesh_count; k++)
         for (u32 j = 0; j < meshes[k].meshlet_count; j++) {
             const u8* in = meshes[k].inds + (size_t)j * 512;
             for (u32 t = 0; t < 128; t++) { const u32 b = t >> 3, l = t & 7; if (!(in[b * 32 + l] == in[b * 32 + 8 + l] && in[b * 32 + 8 + l] == in[b * 32 + 16 + l])) ntri++; }
         }
+    }
     if (ntri) {
         sft__item* it = (sft__item*)malloc(ntri * sizeof(sft__item));
         u32 q = 0;
@@ -1054,6 +1153,8 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
         m->blas = (sft__node*)calloc((size_t)ntri * 2 + 1, sizeof(sft__node));
         m->blas_root = sft__bvh_build(it, ntri, m->blas, &m->blas_count, NULL, NULL);
         free(it);
+    }
+    if (m->blas_count) {
         const sft__node* root = &m->blas[m->blas_root];
         for (int a = 0; a < 3; a++) { m->root_min[a] = 1e30f; m->root_max[a] = -1e30f; }
         for (u32 c = 0; c < root->count; c++)
@@ -1069,6 +1170,108 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
     free(md);
     return m;
 }
+/* sft_model_load_qsf (sofren2.c:7816-7967): a QSF2 file's textures (each becomes a white
+ * material of shininess 2), lightmap pages, meshes (meshlet positions and attributes, flat
+ * triangle indices swizzled into the 8-lane batch layout, bounding spheres and cones) and its
+ * prebuilt BLAS, uploaded as one resident model.  NULL (with a message) when the file cannot be
+ * read.  The arena is not used: model data lives in the device pools. */
+SFT_FUNC sft_model* sft_model_load_qsf(const char* path, sft_arena* arena) {
+    (void)arena;
+    FILE* f = fopen(path, "rb");
+    if (!f) { fprintf(stderr, "sofren2-gb300: failed to open '%s'\n", path); return NULL; }
+#define SFT__RD(p, n) (fread((p), 1, (n), f) == (size_t)(n))
+    char magic[4]; u32 version = 0; u64 game_off = 0;
+    if (!SFT__RD(magic, 4) || memcmp(magic, "QSF2", 4) || !SFT__RD(&version, 4) || version != 2 || !SFT__RD(&game_off, 8)) {
+        fclose(f); fprintf(stderr, "sofren2-gb300: '%s' is not a QSF2 version 2 file\n", path); return NULL;
+    }
+    u32 tex_count = 0;
+    int ok = SFT__RD(&tex_count, 4);
+    sft_mat_handle* mats = (sft_mat_handle*)calloc(tex_count + 1, sizeof(sft_mat_handle));
+    for (u32 i = 0; ok && i < tex_count; i++) {
+        u32 wh[2];
+        ok = SFT__RD(wh, 8) && wh[0] && wh[1] && (u64)wh[0] * wh[1] < (1ull << 28);
+        if (!ok) break;
+        u32* px = (u32*)malloc((size_t)wh[0] * wh[1] * 4);
+        ok = SFT__RD(px, (size_t)wh[0] * wh[1] * 4);
+        if (ok) mats[i] = sft_material_create(sft_texture_create((i32)wh[0], (i32)wh[1], px), 0xFFFFFFFFu, 2.f);
+        free(px);
+    }
+    u32 lm_count = 0;
+    ok = ok && SFT__RD(&lm_count, 4);
+    sft_tex_handle* lms = (sft_tex_handle*)calloc(lm_count + 1, sizeof(sft_tex_handle));
+    for (u32 i = 0; ok && i < lm_count; i++) {
+        u32 wh[2];
+        ok = SFT__RD(wh, 8) && wh[0] && wh[1] && (u64)wh[0] * wh[1] < (1ull << 28);
+        if (!ok) break;
+        u32* px = (u32*)malloc((size_t)wh[0] * wh[1] * 4);
+        ok = SFT__RD(px, (size_t)wh[0] * wh[1] * 4);
+        if (ok) lms[i] = sft_texture_create((i32)wh[0], (i32)wh[1], px);
+        free(px);
+    }
+    u32 hdr[4] = { 0, 0, 0, 0 };   /* mesh count, total meshlets, BLAS nodes, BLAS root */
+    ok = ok && SFT__RD(hdr, 16) && hdr[0] < (1u << 16) && hdr[1] < (1u << 24);
+    sft_mesh_data* md = (sft_mesh_data*)calloc(hdr[0] + 1, sizeof(sft_mesh_data));
+    for (u32 k = 0; ok && k < hdr[0]; k++) {
+        u32 mh[4];   /* meshlet count, model meshlet offset, texture index, lightmap page */
+        ok = SFT__RD(mh, 16) && mh[0] < (1u << 24);
+        if (!ok) break;
+        const u32 mc = mh[0];
+        f32* attr = (f32*)calloc((size_t)mc * 640 + 1, 4);
+        u8* inds = (u8*)calloc((size_t)mc * 512 + 1, 1);
+        f32* cull = (f32*)calloc((size_t)mc * 8 + 1, 4);
+        f32* tmp = (f32*)malloc(((size_t)mc * 448 + 1) * 4);
+        u8* flat = (u8*)malloc((size_t)mc * 384 + 1);
+        ok = SFT__RD(tmp, (size_t)mc * 768);
+        for (u32 j = 0; ok && j < mc; j++) memcpy(attr + (size_t)j * 640, tmp + (size_t)j * 192, 768);   /* x y z */
+        ok = ok && SFT__RD(tmp, (size_t)mc * 1792);
+        for (u32 j = 0; ok && j < mc; j++) memcpy(attr + (size_t)j * 640 + 192, tmp + (size_t)j * 448, 1792);   /* nx..lv */
+        ok = ok && SFT__RD(flat, (size_t)mc * 384);
+        for (u32 j = 0; ok && j < mc; j++)
+            for (u32 tri = 0; tri < 128; tri++) {
+                const u32 off = (tri / 8) * 32, lane = tri % 8;
+                for (u32 c = 0; c < 3; c++) inds[(size_t)j * 512 + off + c * 8 + lane] = flat[(size_t)j * 384 + tri * 3 + c];
+            }
+        /* sphere centre x y z, radius; box min / max (unused); cone axis x y z, cutoff */
+        for (u32 a = 0; ok && a < 14; a++) {
+            ok = SFT__RD(tmp, (size_t)mc * 4);
+            const int dst = a < 4 ? (int)a : (a >= 10 ? (int)a - 6 : -1);
+            if (ok && dst >= 0) for (u32 j = 0; j < mc; j++) cull[(size_t)j * 8 + dst] = tmp[j];
+        }
+        free(tmp); free(flat);
+        md[k].meshlet_count = mc; md[k].attr = attr; md[k].inds = inds; md[k].cull = cull;
+        md[k].material = mh[2] < tex_count ? mats[mh[2]] : sft__s->base_mat;
+        md[k].lightmap_page = mh[3];
+    }
+    u16* mesh_of = (u16*)malloc(((size_t)hdr[1] + 1) * 2);
+    ok = ok && SFT__RD(mesh_of, (size_t)hdr[1] * 2);
+    void* blas = malloc((size_t)hdr[2] * 256 + 1);
+    ok = ok && SFT__RD(blas, (size_t)hdr[2] * 256);
+    fclose(f);
+#undef SFT__RD
+    /* the BLAS must stay inside the model: inner children are nodes, leaf payloads are
+     * (meshlet << 7 | triangle) of this model's meshlets */
+    if (ok && hdr[2]) {
+        u32 sum = 0;
+        for (u32 k = 0; k < hdr[0]; k++) sum += md[k].meshlet_count;
+        ok = sum == hdr[1] && hdr[3] < hdr[2];
+        const sft__node* nodes = (const sft__node*)blas;
+        for (u32 i = 0; ok && i < hdr[2]; i++) {
+            ok = nodes[i].count <= 8;
+            for (u32 c = 0; ok && c < nodes[i].count; c++) {
+                const u32 ch = nodes[i].child[c];
+                if (ch == 0xFFFFFFFFu) continue;
+                ok = nodes[i].leaf ? ((ch & 0x7FFFFFFFu) >> 7) < hdr[1] : ch < hdr[2];
+            }
+        }
+    }
+    sft_model* m = NULL;
+    if (ok) m = sft__model_create(md, hdr[0], NULL, 0, 0, lms, lm_count, hdr[2] ? blas : NULL, hdr[2], hdr[3]);
+    else fprintf(stderr, "sofren2-gb300: '%s' is truncated or malformed\n", path);
+    for (u32 k = 0; k < hdr[0]; k++) { free((void*)md[k].attr); free((void*)md[k].inds); free((void*)md[k].cull); }
+    free(md); free(mesh_of); free(blas); free(mats); free(lms);
+    return m;
+}
+
 SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model) { return model ? model->total_meshlets : 0; }
 SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, u32* out_root) {
     if (out_count) *out_count = model ? model->blas_count : 0;
@@ -1259,6 +1462,39 @@ SFT_FUNC i32 sft_model_set_skeleton(sft_model* model, const sftg_bone_desc* bone
     if (rc) { fprintf(stderr, "sofren2-gb300: skeleton upload failed (%d): %s\n", rc, sftg_last_error(sft__s->gpu)); return rc; }
     model->skeleton_id = id;
     return 0;
+}
+
+/* sft_raycast_instance (sofren2.c:3733-3837) through sftg_raycast: the instance's model and
+ * transform with the ray; a NULL instance or model, or a model without a BLAS, gives no hit at
+ * max_dist as in the reference */
+SFT_FUNC void sft_raycast_batch(const sft_instance* const* insts, const sftvec* origins, const sftvec* dirs, const f32* max_dists,
+                                u32 n, sft_ray_hit* out) {
+    if (!n) return;
+    sftg_ray* rays = (sftg_ray*)calloc(n, sizeof(sftg_ray));
+    sftg_ray_hit* hits = (sftg_ray_hit*)calloc(n, sizeof(sftg_ray_hit));
+    for (u32 k = 0; k < n; k++) {
+        const sft_instance* in = insts[k];
+        if (in) memcpy(rays[k].transform, &in->transform, 64);
+        rays[k].origin[0] = origins[k].x; rays[k].origin[1] = origins[k].y; rays[k].origin[2] = origins[k].z;
+        rays[k].dir[0] = dirs[k].x; rays[k].dir[1] = dirs[k].y; rays[k].dir[2] = dirs[k].z;
+        rays[k].max_dist = max_dists[k];
+        rays[k].model = in && in->model && in->model->blas_count ? in->model->device_id : -1;
+    }
+    sft__check(sftg_raycast(sft__s->gpu, rays, n, hits), "sftg_raycast");
+    for (u32 k = 0; k < n; k++) {
+        memset(&out[k], 0, sizeof(out[k]));
+        out[k].hit = (u8)hits[k].hit;
+        out[k].distance = hits[k].distance;
+        out[k].pos = SFT_V(hits[k].pos[0], hits[k].pos[1], hits[k].pos[2]);
+        out[k].normal = SFT_V(hits[k].normal[0], hits[k].normal[1], hits[k].normal[2]);
+    }
+    free(rays); free(hits);
+}
+
+SFT_FUNC sft_ray_hit sft_raycast_instance(const sft_instance* inst, sftvec origin, sftvec dir, f32 max_dist) {
+    sft_ray_hit h;
+    sft_raycast_batch(&inst, &origin, &dir, &max_dist, 1, &h);
+    return h;
 }
 
 /* sft_pose_update (sofren2.c:8952-9108): the animation sampled at `time` (wrapped by the clip's

@@ -216,6 +216,32 @@ int main(int argc, char** argv) {
     sft_model** models = (sft_model**)calloc(sc.n_models + 1, sizeof(sft_model*));
     for (u32 i = 0; i < sc.n_models; i++) models[i] = build_model(&sc, &sc.models[i], mats, texs, &model_arena);
 
+    if (getenv("SFT_RAYCAST")) {
+        /* ray query mode: sft_raycast_instance for each 96-byte ray record of the file named by
+         * SFT_RAYCAST (transform[16], origin[3], dir[3], max_dist, model); writes 32-byte hit
+         * records (hit, distance, pos[3], normal[3]) to the output path, and renders nothing */
+        FILE* rf = fopen(getenv("SFT_RAYCAST"), "rb");
+        FILE* of = fopen(argv[2], "wb");
+        if (!rf || !of) return 5;
+        struct { f32 T[16]; f32 o[3], dir[3]; f32 max_dist; i32 model; } ray;
+        while (fread(&ray, sizeof(ray), 1, rf) == 1) {
+            if (ray.model < 0 || (u32)ray.model >= sc.n_models) return 6;
+            sft_instance inst;
+            memset(&inst, 0, sizeof(inst));
+            inst.model = models[ray.model];
+            memcpy(&inst.transform, ray.T, 64);
+            const sft_ray_hit hit = sft_raycast_instance(&inst, SFT_V(ray.o[0], ray.o[1], ray.o[2]),
+                                                         SFT_V(ray.dir[0], ray.dir[1], ray.dir[2]), ray.max_dist);
+            u32 out[8] = { 0 };
+            out[0] = hit.hit ? 1u : 0u;
+            memcpy(&out[1], &hit.distance, 4);
+            memcpy(&out[2], &hit.pos, 12);
+            memcpy(&out[5], &hit.normal, 12);
+            fwrite(out, 4, 8, of);
+        }
+        fclose(rf); fclose(of);
+        return 0;
+    }
     sfts_dump d = { fopen(argv[2], "wb") };
     if (!d.f) return 5;
     for (u32 i = 0; i < sc.n_models; i++)

@@ -1860,6 +1860,121 @@ int sfto_pose_eval(const uint8_t* blob, uint64_t size, float* out, uint64_t out_
     return (int)nr;
 }
 
+/* ------------------------------------------------------------ ray queries
+ * sft_raycast_instance (sofren2.c:3733-3837) and sft__intersect_triangle (3705-3731): the ray is
+ * taken into model space by sft_m_qinv of the instance transform and sft_m_mul_vec, which adds
+ * no translation (the reference's behaviour, kept), the direction is normalised and the distance
+ * limit scaled by its length, and the BLAS is walked depth first from a stack (children in slot
+ * order, inner children pushed, leaf triangles tested in place).  A hit shortens the limit, so
+ * among equal distances the first triangle found wins.  Records: ray = transform[16], origin[3],
+ * dir[3], max_dist, model (96 B); hit = hit, distance, pos[3], normal[3] (32 B). */
+typedef struct { f32 T[4][4]; f32 o[3], d[3]; f32 max_dist; i32 model; } oray;
+typedef struct { u32 hit; f32 dist; f32 pos[3]; f32 nrm[3]; } ohit;
+
+static int ray_tri(vec3 ro, vec3 rd, vec3 v0, vec3 v1, vec3 v2, f32* t) {   /* sft__intersect_triangle */
+    const vec3 e1 = vsub(v1, v0), e2 = vsub(v2, v0), p = scross(rd, e2);
+    const f32 det = sdot(e1, p);
+    if (fabsf(det) < EPS) return 0;
+    const f32 inv = 1.f / det;
+    const vec3 tv = vsub(ro, v0);
+    const f32 u = sdot(tv, p) * inv;
+    if (u < 0.f || u > 1.f) return 0;
+    const vec3 q = scross(tv, e1);
+    const f32 v = sdot(rd, q) * inv;
+    if (v < 0.f || u + v > 1.f) return 0;
+    *t = sdot(e2, q) * inv;
+    return *t > EPS;
+}
+
+static vec3 rot3(const f32 m[4][4], vec3 v) {   /* sft_m_mul_vec (1679): rows 0-2 only */
+    vec3 r = { v.x * m[0][0] + v.y * m[1][0] + v.z * m[2][0], v.x * m[0][1] + v.y * m[1][1] + v.z * m[2][1],
+               v.x * m[0][2] + v.y * m[1][2] + v.z * m[2][2] };
+    return r;
+}
+
+static f32 ray_inv(f32 d) { return 1.f / (fabsf(d) > EPS ? d : EPS * (f32)(d < 0 ? -1 : 1)); }
+
+static ohit raycast_one(const omodel* m, const oray* r) {
+    ohit h;
+    memset(&h, 0, sizeof(h));
+    h.dist = r->max_dist;
+    if (!m->blas_count) return h;
+    f32 inv[4][4];   /* sft_m_qinv (1693-1711) */
+    for (int i = 0; i < 3; i++) { for (int j = 0; j < 3; j++) inv[i][j] = r->T[j][i]; inv[i][3] = 0.f; }
+    for (int j = 0; j < 3; j++) inv[3][j] = -(r->T[3][0] * inv[0][j] + r->T[3][1] * inv[1][j] + r->T[3][2] * inv[2][j]);
+    inv[3][3] = 1.f;
+    const vec3 o = { r->o[0], r->o[1], r->o[2] }, d = { r->d[0], r->d[1], r->d[2] };
+    const vec3 lo = rot3(inv, o);
+    vec3 ld = rot3(inv, d);
+    const f32 inv_scale = 1.f / sqrtf(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z);
+    ld = vscale(ld, inv_scale);
+    const f32 ix = ray_inv(ld.x), iy = ray_inv(ld.y), iz = ray_inv(ld.z);
+    u32 stack[256];
+    i32 sp = 0;
+    stack[sp++] = m->blas_root;
+    f32 lmax = r->max_dist / inv_scale;
+    const onode* nodes = (const onode*)m->blas;
+    while (sp > 0) {
+        const onode* n = &nodes[stack[--sp]];
+        for (u32 c = 0; c < n->count; c++) {
+            if (n->child[c] == 0xFFFFFFFFu) continue;
+            const f32 tx1 = (n->mn[0][c] - lo.x) * ix, tx2 = (n->mx[0][c] - lo.x) * ix;
+            const f32 ty1 = (n->mn[1][c] - lo.y) * iy, ty2 = (n->mx[1][c] - lo.y) * iy;
+            const f32 tz1 = (n->mn[2][c] - lo.z) * iz, tz2 = (n->mx[2][c] - lo.z) * iz;
+#define RMIN(a, b) ((a) < (b) ? (a) : (b))
+#define RMAX(a, b) ((a) > (b) ? (a) : (b))
+            const f32 tmin = RMAX(RMAX(RMIN(tx1, tx2), RMIN(ty1, ty2)), RMIN(tz1, tz2));
+            const f32 tmax = RMIN(RMIN(RMAX(tx1, tx2), RMAX(ty1, ty2)), RMAX(tz1, tz2));
+#undef RMIN
+#undef RMAX
+            if (!(tmax >= tmin && tmax > 0.f && tmin < lmax)) continue;
+            if (!n->leaf) { if (sp < 256) stack[sp++] = n->child[c]; continue; }
+            const u32 pay = n->child[c] & ~0x80000000u, mi = pay >> 7, tri = pay & 127u;
+            const sfts_meshlet* ml = m->ml[mi];
+            const u32 off = (tri / 8) * 32, lane = tri % 8;
+            const u8 i0 = ml->inds[off + lane], i1 = ml->inds[off + 8 + lane], i2 = ml->inds[off + 16 + lane];
+            const f32* X = ml->attr;
+            const vec3 v0 = { X[i0], X[64 + i0], X[128 + i0] }, v1 = { X[i1], X[64 + i1], X[128 + i1] }, v2 = { X[i2], X[64 + i2], X[128 + i2] };
+            f32 t;
+            if (ray_tri(lo, ld, v0, v1, v2, &t) && t < lmax) {
+                lmax = t;
+                h.hit = 1;
+                h.dist = t * inv_scale;
+                const vec3 lh = vadd(lo, vscale(ld, t));
+                const vec3 ln = snorm(scross(vsub(v1, v0), vsub(v2, v0)));   /* sft_v_face_normal */
+                const vec3 wp = rot3(r->T, lh), wn = snorm(rot3(r->T, ln));
+                h.pos[0] = wp.x; h.pos[1] = wp.y; h.pos[2] = wp.z;
+                h.nrm[0] = wn.x; h.nrm[1] = wn.y; h.nrm[2] = wn.z;
+            }
+        }
+    }
+    return h;
+}
+
+/* rays (96 B records) against the scene's models; returns 0, or -1 for a bad model index */
+int sfto_raycast(void* hp, const void* rays, uint32_t n, void* hits) {
+    oracle_handle* h = (oracle_handle*)hp;
+    if (!h) return -1;
+    const oray* R = (const oray*)rays;
+    ohit* H = (ohit*)hits;
+    for (uint32_t k = 0; k < n; k++) {
+        if (R[k].model < 0 || (uint32_t)R[k].model >= h->sc.n_models) return -1;
+        H[k] = raycast_one(&h->c.models[R[k].model], &R[k]);
+    }
+    return 0;
+}
+
+/* BLAS of model `mi` as sft_bvh_node images (256 B each): copies up to cap nodes into out and
+ * returns the node count; *root receives the root index */
+int sfto_model_blas(void* hp, uint32_t mi, uint8_t* out, uint32_t cap, uint32_t* root) {
+    oracle_handle* h = (oracle_handle*)hp;
+    if (!h || mi >= h->sc.n_models) return -1;
+    const omodel* m = &h->c.models[mi];
+    if (out) memcpy(out, m->blas, (size_t)(m->blas_count < cap ? m->blas_count : cap) * 256);
+    if (root) *root = m->blas_root;
+    return (int)m->blas_count;
+}
+
 /* enum sft_debug_mode for the following renders (0 = none) */
 int sfto_set_debug_mode(void* hp, int mode) {
     oracle_handle* h = (oracle_handle*)hp;

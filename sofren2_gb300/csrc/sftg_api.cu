@@ -80,6 +80,7 @@ struct sftg_ctx {
     size_t tr_models = 0;
     /* skeletons and animations (sftg_skeleton_upload) */
     dpool p_skels, p_bones, p_anims, p_samplers, p_channels, p_keys, p_order, p_levels, p_pose_io;
+    dpool p_ray_io;                            /* staging of sftg_raycast */
     std::vector<sftg_skel_dev> h_skels;
     uint32_t n_bones = 0, n_anims = 0, n_samplers = 0, n_channels = 0, n_keys = 0, n_order = 0, n_levels = 0;
 };
@@ -148,7 +149,7 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     dpool* pools[] = { &ctx->texels, &ctx->texs, &ctx->mats, &ctx->ml_attr, &ctx->ml_inds, &ctx->ml_cull, &ctx->ml_info,
                        &ctx->skin_j, &ctx->skin_w, &ctx->blas, &ctx->models, &ctx->p_skels, &ctx->p_bones, &ctx->p_anims,
-                       &ctx->p_samplers, &ctx->p_channels, &ctx->p_keys, &ctx->p_order, &ctx->p_levels, &ctx->p_pose_io };
+                       &ctx->p_samplers, &ctx->p_channels, &ctx->p_keys, &ctx->p_order, &ctx->p_levels, &ctx->p_pose_io, &ctx->p_ray_io };
     for (dpool* p : pools) if (p->ptr) cudaFree(p->ptr);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->d_color) cudaFree(ctx->d_color);
@@ -931,6 +932,37 @@ extern "C" int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* reqs, uint
         memcpy(posed + (size_t)off[k] * 16, hp.data() + (size_t)off[k] * 16, (size_t)sk.bone_count * 64);
         if (global) memcpy(global + (size_t)off[k] * 16, hg.data() + (size_t)off[k] * 16, (size_t)sk.bone_count * 64);
     }
+    return SFTG_OK;
+}
+
+/* ------------------------------------------------------------------ ray queries */
+extern "C" int sftg_raycast_device(sftg_ctx* ctx, const sftg_ray* d_rays, uint32_t n, sftg_ray_hit* d_hits) {
+    if (!ctx || (n && (!d_rays || !d_hits))) return SFTG_E_ARG;
+    if (!n) return SFTG_OK;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_tables(ctx);   /* the device model table follows uploads lazily */
+    if (rc) return rc;
+    sftg_launch_raycast(d_rays, n, (const sftg_model*)ctx->models.ptr, (uint32_t)ctx->h_models.size(), (const sftg_bvh_node*)ctx->blas.ptr,
+                        (const float*)ctx->ml_attr.ptr, (const uint8_t*)ctx->ml_inds.ptr, d_hits, ctx->stream);
+    CK(cudaGetLastError());
+    return SFTG_OK;
+}
+
+extern "C" int sftg_raycast(sftg_ctx* ctx, const sftg_ray* rays, uint32_t n, sftg_ray_hit* hits) {
+    if (!ctx || (n && (!rays || !hits))) return SFTG_E_ARG;
+    if (!n) return SFTG_OK;
+    CK(cudaSetDevice(ctx->device));
+    const size_t b_ray = ((size_t)n * sizeof(sftg_ray) + 255) & ~(size_t)255;
+    int rc = pool_reserve(ctx, ctx->p_ray_io, b_ray + (size_t)n * sizeof(sftg_ray_hit) + 256);
+    if (rc) return rc;
+    sftg_ray* d_rays = (sftg_ray*)ctx->p_ray_io.ptr;
+    sftg_ray_hit* d_hits = (sftg_ray_hit*)((char*)ctx->p_ray_io.ptr + b_ray);
+    CK(cudaMemcpyAsync(d_rays, rays, (size_t)n * sizeof(sftg_ray), cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = sftg_raycast_device(ctx, d_rays, n, d_hits))) return rc;
+    CK(cudaMemcpyAsync(hits, d_hits, (size_t)n * sizeof(sftg_ray_hit), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t k = 0; k < n; k++)
+        if (hits[k].hit == 2) return set_err(ctx, SFTG_E_DEVICE_STATUS, "ray %u: BLAS walk overflowed its stack", k);
     return SFTG_OK;
 }
 

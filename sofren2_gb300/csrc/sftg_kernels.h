@@ -88,6 +88,8 @@ struct sftg_pose_tables {
     const uint16_t* order;         /* per skeleton: bones parents-first */
     const uint16_t* levels;        /* per skeleton: level_count + 1 starts into order */
 };
+void sftg_launch_raycast(const sftg_ray* rays, uint32_t n, const sftg_model* models, uint32_t n_models, const sftg_bvh_node* blas,
+                         const float* ml_attr, const uint8_t* ml_inds, sftg_ray_hit* hits, cudaStream_t st);
 void sftg_launch_pose(const sftg_pose_tables& T, const sftg_pose_request* reqs, const uint32_t* out_off, uint32_t n, float* posed,
                       float* global, cudaStream_t st);
 

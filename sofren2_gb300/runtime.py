@@ -53,7 +53,9 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftx_serve": (i32, [p, p, u32, u32, u64, i32, p, u32, p, p, p]),
         "sft_get_gpu_context": (p, []), "sftg_get_tuning": (i32, [p, p]), "sftg_set_tuning": (i32, [p, p]),
         "sftg_skeleton_upload": (i32, [p, p, u32, p, u32, p]), "sftg_pose_eval": (i32, [p, p, u32, p, p]),
-        "sftg_last_error": (C.c_char_p, [p]),
+        "sftg_last_error": (C.c_char_p, [p]), "sftx_scene_model": (p, [p, u32]),
+        "sft_raycast_batch": (v, [p, p, p, p, u32, p]), "sftg_raycast": (i32, [p, p, u32, p]),
+        "sftg_raycast_device": (i32, [p, p, u32, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -86,6 +88,22 @@ class SftgAnimationDesc(C.Structure):
 
 class SftgPoseRequest(C.Structure):
     _fields_ = [("skeleton", C.c_int32), ("animation", C.c_int32), ("time", C.c_float)]
+
+
+# sftg_ray / sftg_ray_hit records (include/sftg.h)
+RAY_DTYPE = np.dtype([("T", "<f4", (16,)), ("o", "<f4", (3,)), ("d", "<f4", (3,)), ("max_dist", "<f4"), ("model", "<i4")])
+HIT_DTYPE = np.dtype([("hit", "<u4"), ("dist", "<f4"), ("pos", "<f4", (3,)), ("nrm", "<f4", (3,))])
+
+
+class SftInstance(C.Structure):
+    """sft_instance (include/sofren2.h, sofren2.c:1198-1203)."""
+    _fields_ = [("model", C.c_void_p), ("transform", C.c_float * 16), ("ss_meshlet_offset", C.c_uint32),
+                ("posed_bone_matrices", C.c_void_p)]
+
+
+class SftRayHit(C.Structure):
+    """sft_ray_hit (sofren2.c:895-900)."""
+    _fields_ = [("hit", C.c_uint8), ("distance", C.c_float), ("pos", C.c_float * 3), ("normal", C.c_float * 3)]
 
 
 class SftxRequest(C.Structure):
@@ -301,6 +319,40 @@ class Renderer:
         if rc != 0:
             raise RuntimeError("pose evaluation failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
         return posed, glob
+
+    def raycast(self, h, rays: np.ndarray) -> np.ndarray:
+        """sft_raycast_batch over RAY_DTYPE records whose `model` indexes the models of scene h
+        (one sft_instance per ray with that model and transform); HIT_DTYPE records."""
+        r = np.ascontiguousarray(rays, RAY_DTYPE)
+        n = len(r)
+        insts = (SftInstance * max(1, n))()
+        ptrs = (C.c_void_p * max(1, n))()
+        models = {}
+        for k in range(n):
+            mi = int(r[k]["model"])
+            if mi not in models:
+                models[mi] = self.lib.sftx_scene_model(h, mi)
+                if not models[mi]:
+                    raise ValueError(f"scene has no model {mi}")
+            insts[k].model = models[mi]
+            C.memmove(insts[k].transform, r[k]["T"].ctypes.data, 64)
+            ptrs[k] = C.addressof(insts[k])
+        o = np.ascontiguousarray(r["o"], np.float32)
+        d = np.ascontiguousarray(r["d"], np.float32)
+        md = np.ascontiguousarray(r["max_dist"], np.float32)
+        hits = (SftRayHit * max(1, n))()
+        self.lib.sft_raycast_batch(ptrs, _ptr(o), _ptr(d), _ptr(md), n, hits)
+        out = np.zeros(n, HIT_DTYPE)
+        for k in range(n):
+            out[k] = (hits[k].hit, hits[k].distance, tuple(hits[k].pos), tuple(hits[k].normal))
+        return out
+
+    def raycast_device(self, d_rays: int, n: int, d_hits: int) -> None:
+        """sftg_raycast_device on device arrays of sftg_ray / sftg_ray_hit (raw pointers), queued
+        on the library's stream."""
+        ctx = self.lib.sft_get_gpu_context()
+        if self.lib.sftg_raycast_device(ctx, C.c_void_p(d_rays), n, C.c_void_p(d_hits)) != 0:
+            raise RuntimeError("raycast failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
 
     def render_debug(self, h, frame: int, total_ss: int, n_proxies: int, payload_cap: int = 1 << 22,
                      clip_cap: int = 1 << 16) -> dict:

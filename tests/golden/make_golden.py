@@ -72,6 +72,32 @@ def main(names: list[str]) -> None:
                 dm[str(S)] = [gc.sha(f) for f in frames]
         golden["dmesh"] = dm
         print("dmesh", {k: [h[:12] for h in v] for k, v in dm.items()}, flush=True)
+    if not names or "qsf" in names:
+        # the QSF scene (oracle/qsf_scene.h) over the atrium_small atrium written as a QSF2 file,
+        # loaded and rendered by the reference, per frame
+        import tempfile
+        import numpy as np
+        data = gc.qsf_model()
+        q = {"file": gc.sha(np.frombuffer(data, np.uint8))}
+        for S in (1, 4):
+            with tempfile.TemporaryDirectory() as td:
+                qp, op = os.path.join(td, "m.qsf"), os.path.join(td, "q.bin")
+                open(qp, "wb").write(data)
+                subprocess.run([os.path.join(ROOT, "oracle", "_ref", f"qsf_harness_{S}x"), qp, op], check=True)
+                frames = np.fromfile(op, np.uint32).reshape(-1, 360, 640)
+                q[str(S)] = [gc.sha(f) for f in frames]
+        golden["qsf"] = q
+        print("qsf", {k: (v[:12] if isinstance(v, str) else [h[:12] for h in v]) for k, v in q.items()}, flush=True)
+    if not names or "raycast" in names:
+        # sft_raycast_instance of the reference over seeded rays per case (golden_cases.rays)
+        from oracle_lib import reference_raycast
+        rc = {}
+        for n in gc.RAY_CASES:
+            r = gc.rays(n)
+            hits = reference_raycast(gc.blob(n), r)
+            rc[n] = {"rays": gc.sha(r), "hits": gc.sha(hits), "n_hit": int(hits["hit"].sum())}
+        golden["raycast"] = rc
+        print("raycast", {k: (v["hits"][:12], v["n_hit"]) for k, v in rc.items()}, flush=True)
     json.dump(golden, open(path, "w"), indent=1, sort_keys=True)
 
 

@@ -48,6 +48,68 @@ def blob(name: str) -> bytes:
     return _cache[key]
 
 
+def qsf_model() -> bytes:
+    """The atrium_small atrium (model 0) as a QSF2 file, with the BLAS the oracle builds for it."""
+    key = ("qsf",)
+    if key not in _cache:
+        from oracle_lib import Oracle, qsf_bytes
+        blas, root = Oracle(blob("atrium_small")).model_blas(0)
+        _cache[key] = qsf_bytes(scene("atrium_small"), 0, blas, root)
+    return _cache[key]
+
+
+# ray queries (sft_raycast_instance): cases and rays per case
+RAY_CASES = ["small", "atrium_small", "skinned_small", "variety"]
+N_RAYS = 4096
+
+
+def rays(name: str, n: int = N_RAYS, seed: int = 0):
+    """Seeded ray records (oracle_lib.RAY_DTYPE) against the models of a case, with the frame-0
+    instance transforms, some scaled by 2 or 0.5: 60% aimed at points of the model's bounds as
+    the reference places them (transform rows 0-2, no translation), 20% in random directions,
+    10% along coordinate axes (zero direction components), 8% with a short distance limit, and
+    two rays of zero direction."""
+    from oracle_lib import RAY_DTYPE
+    sc = scene(name)
+    fr = sc.frames[0]
+    insts = [(mi, np.asarray(T, np.float32).reshape(4, 4)) for mi, T, _ in fr.instances]
+    bounds = {}
+    for mi, _ in insts:
+        if mi not in bounds:
+            pos = np.concatenate([ms.attr.reshape(ms.n, 10, 64)[:, 0:3].transpose(0, 2, 1).reshape(-1, 3) for ms in sc.models[mi].meshes])
+            bounds[mi] = (pos.min(0), pos.max(0))
+    rng = np.random.default_rng(seed + sum(name.encode()))
+    out = np.zeros(n, RAY_DTYPE)
+    cam = np.asarray(fr.cam_pos, np.float32)
+    for k in range(n):
+        mi, T = insts[rng.integers(len(insts))]
+        T = T.copy()
+        u = rng.random()
+        if u < 0.15:
+            T[:3, :3] *= np.float32(2.0)
+        elif u < 0.3:
+            T[:3, :3] *= np.float32(0.5)
+        lo, hi = bounds[mi]
+        o = (cam + rng.normal(0, 1.5, 3)).astype(np.float32)
+        kind = rng.random()
+        if kind < 0.6:
+            p = (lo + rng.random(3) * (hi - lo)).astype(np.float32)
+            d = (p @ T[:3, :3] - o).astype(np.float32)
+        elif kind < 0.8:
+            d = rng.normal(0, 1, 3).astype(np.float32)
+        else:
+            d = np.zeros(3, np.float32)
+            d[rng.integers(3)] = np.float32(rng.choice([-1.0, 1.0]) * rng.uniform(0.5, 2.0))
+        out[k]["T"] = T.reshape(-1)
+        out[k]["o"] = o
+        out[k]["d"] = d
+        out[k]["max_dist"] = np.float32(rng.uniform(0.5, 3.0) if rng.random() < 0.08 else 1000.0)
+        out[k]["model"] = mi
+    for k in (n - 2, n - 1):
+        out[k]["d"] = 0.0
+    return out
+
+
 def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 

@@ -49,6 +49,28 @@ class Oracle:
         if not self.h:
             raise RuntimeError("oracle rejected the scene blob")
 
+    def model_blas(self, mi: int) -> tuple[bytes, int]:
+        """(node images, root index) of model mi's BLAS, built by the oracle's restated builder."""
+        L = lib()
+        L.sfto_model_blas.restype = C.c_int
+        L.sfto_model_blas.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]
+        root = C.c_uint32(0)
+        n = L.sfto_model_blas(self.h, mi, None, 0, C.byref(root))
+        buf = np.zeros(max(1, n) * 256, np.uint8)
+        L.sfto_model_blas(self.h, mi, buf.ctypes.data_as(C.c_void_p), n, C.byref(root))
+        return buf[: n * 256].tobytes(), int(root.value)
+
+    def raycast(self, rays: np.ndarray) -> np.ndarray:
+        """The oracle's sft_raycast_instance restatement for each RAY_DTYPE record."""
+        L = lib()
+        L.sfto_raycast.restype = C.c_int
+        L.sfto_raycast.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+        r = np.ascontiguousarray(rays, RAY_DTYPE)
+        out = np.zeros(len(r), HIT_DTYPE)
+        if L.sfto_raycast(self.h, r.ctypes.data_as(C.c_void_p), len(r), out.ctypes.data_as(C.c_void_p)) != 0:
+            raise ValueError("ray with a bad model index")
+        return out
+
     def set_debug_mode(self, mode: int) -> None:
         if lib().sfto_set_debug_mode(self.h, mode) != 0:
             raise ValueError(f"bad debug mode {mode}")
@@ -84,6 +106,52 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle render failed ({rc})")
         return color, int(ns[0]), sh
+
+
+def qsf_bytes(scene, mi: int, blas: bytes, blas_root: int) -> bytes:
+    """Model mi of a scenes.Scene written in the reference's QSF2 layout (sft_model_load_qsf,
+    sofren2.c:7816-7967): textures (each becomes a white material of shininess 2), lightmap
+    pages, the model header, per mesh its meshlets (positions, then normals / UVs / lightmap
+    UVs), flat indices, bounding spheres, boxes and cones, then the meshlet-to-mesh table and
+    the BLAS nodes."""
+    import struct
+    m = scene.models[mi]
+    tex_ids = sorted({scene.materials[mat][0] for mat in m.materials if mat >= 0 and scene.materials[mat][0] >= 0})
+    tex_pos = {t: i for i, t in enumerate(tex_ids)}
+    out = [b"QSF2", struct.pack("<IQ", 2, 0), struct.pack("<I", len(tex_ids))]
+    for t in tex_ids:
+        tx = scene.textures[t]
+        out.append(struct.pack("<II", tx.shape[1], tx.shape[0]) + tx.astype("<u4").tobytes())
+    out.append(struct.pack("<I", len(m.lightmaps)))
+    for t in m.lightmaps:
+        tx = scene.textures[t]
+        out.append(struct.pack("<II", tx.shape[1], tx.shape[0]) + tx.astype("<u4").tobytes())
+    total = sum(ms.n for ms in m.meshes)
+    out.append(struct.pack("<IIII", len(m.meshes), total, len(blas) // 256, blas_root))
+    first = 0
+    for ms, mat, page in zip(m.meshes, m.materials, m.lightmap_pages):
+        tex = scene.materials[mat][0] if mat >= 0 else -1
+        out.append(struct.pack("<IIII", ms.n, first, tex_pos.get(tex, 0xFFFFFFFF), page))
+        attr = ms.attr.reshape(ms.n, 10, 64).astype("<f4")
+        out.append(attr[:, 0:3].tobytes())                     # sft_meshlet: x y z
+        out.append(attr[:, 3:10].tobytes())                    # attribs: nx ny nz u v lu lv
+        flat = np.zeros((ms.n, 128, 3), np.uint8)
+        ind = ms.inds.reshape(ms.n, 16, 32)
+        for k in range(3):
+            flat[:, :, k] = ind[:, :, 8 * k:8 * k + 8].reshape(ms.n, 128)
+        out.append(flat.tobytes())
+        cull = ms.cull.reshape(ms.n, 8).astype("<f4")
+        pos = attr[:, 0:3]
+        for k in range(4):                                     # sphere centre x y z, radius
+            out.append(np.ascontiguousarray(cull[:, k]).tobytes())
+        out.append(pos.min(axis=2).T.copy().tobytes())         # box min x y z
+        out.append(pos.max(axis=2).T.copy().tobytes())         # box max x y z
+        for k in range(4, 8):                                  # cone axis x y z, cutoff
+            out.append(np.ascontiguousarray(cull[:, k]).tobytes())
+        first += ms.n
+    out.append(np.concatenate([np.full(ms.n, i, "<u2") for i, ms in enumerate(m.meshes)]).tobytes())
+    out.append(blas)
+    return b"".join(out)
 
 
 def pose_blob(rig: dict, requests: list) -> bytes:
@@ -135,6 +203,22 @@ def reference_pose_available() -> bool:
 
 def reference_available(samples: int) -> bool:
     return os.path.exists(os.path.join(REF_DIR, f"ref_harness_{samples}x"))
+
+
+RAY_DTYPE = np.dtype([("T", "<f4", (16,)), ("o", "<f4", (3,)), ("d", "<f4", (3,)), ("max_dist", "<f4"), ("model", "<i4")])
+HIT_DTYPE = np.dtype([("hit", "<u4"), ("dist", "<f4"), ("pos", "<f4", (3,)), ("nrm", "<f4", (3,))])
+
+
+def reference_raycast(blob: bytes, rays: np.ndarray) -> np.ndarray:
+    """sft_raycast_instance of the unmodified reference for each ray record (RAY_DTYPE) over the
+    scene's models (oracle/ref_harness.c, SFT_RAYCAST mode); HIT_DTYPE records."""
+    with tempfile.TemporaryDirectory() as td:
+        sp, rp, hp = os.path.join(td, "s.sfts"), os.path.join(td, "r.bin"), os.path.join(td, "h.bin")
+        open(sp, "wb").write(blob)
+        np.ascontiguousarray(rays, RAY_DTYPE).tofile(rp)
+        env = dict(os.environ, SFT_RAYCAST=rp)
+        subprocess.run([os.path.join(REF_DIR, "ref_harness_1x"), sp, hp], check=True, stdout=subprocess.DEVNULL, env=env)
+        return np.fromfile(hp, HIT_DTYPE)
 
 
 def reference_dump(blob: bytes, samples: int, frame: int = -1, debug_mode: int = 0) -> list[dict]:
