@@ -83,11 +83,34 @@ def main(names: list[str]) -> None:
             with tempfile.TemporaryDirectory() as td:
                 qp, op = os.path.join(td, "m.qsf"), os.path.join(td, "q.bin")
                 open(qp, "wb").write(data)
-                subprocess.run([os.path.join(ROOT, "oracle", "_ref", f"qsf_harness_{S}x"), qp, op], check=True)
+                subprocess.run([os.path.join(ROOT, "oracle", "_ref", f"qsf_harness_{S}x"), "atrium", qp, op], check=True)
                 frames = np.fromfile(op, np.uint32).reshape(-1, 360, 640)
                 q[str(S)] = [gc.sha(f) for f in frames]
         golden["qsf"] = q
         print("qsf", {k: (v[:12] if isinstance(v, str) else [h[:12] for h in v]) for k, v in q.items()}, flush=True)
+    if not names or "maps" in names:
+        # the viewer's frame loop (oracle/map_scene.h) over the reference's own QSF2 maps at 1600x900,
+        # per frame, and its ray queries; `make ref` copies the maps to oracle/_ref/res
+        import hashlib
+        import tempfile
+        import numpy as np
+        maps = {}
+        for m in gc.QSF_MAPS:
+            mp = os.path.join(ROOT, "oracle", "_ref", "res", m + ".qsf")
+            e = {"file": hashlib.sha256(open(mp, "rb").read()).hexdigest()}
+            for S in (1, 4):
+                with tempfile.TemporaryDirectory() as td:
+                    op = os.path.join(td, "m.bin")
+                    subprocess.run([os.path.join(ROOT, "oracle", "_ref", f"qsf_harness_{S}x"), "map", mp, op, "1600", "900"], check=True)
+                    frames = np.fromfile(op, np.uint32).reshape(-1, 900, 1600)
+                    e[str(S)] = [gc.sha(f) for f in frames]
+                    rays = np.fromfile(op + ".rays", np.uint32)
+                    if S == 1:
+                        e["rays"] = gc.sha(rays)
+                    assert gc.sha(rays) == e["rays"], "ray queries depend on the MSAA build"
+            maps[m] = e
+        golden["qsf_maps"] = maps
+        print("qsf_maps", {k: [h[:10] for h in v["1"]] for k, v in maps.items()}, flush=True)
     if not names or "raycast" in names:
         # sft_raycast_instance of the reference over seeded rays per case (golden_cases.rays)
         from oracle_lib import reference_raycast

@@ -58,6 +58,9 @@ def qsf_model() -> bytes:
     return _cache[key]
 
 
+# the reference's own QSF2 maps (res/*.qsf), copied beside the reference builds by `make ref`
+QSF_MAPS = ["simple", "simpleb"]
+
 # ray queries (sft_raycast_instance): cases and rays per case
 RAY_CASES = ["small", "atrium_small", "skinned_small", "variety"]
 N_RAYS = 4096
