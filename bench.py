@@ -7,7 +7,9 @@ posed bones) and sft_present through the library, i.e. proxy occlusion, geometry
 tile raster and resolve on the GPU.  The default workload is the skinned-characters scene
 (eight ~6k-triangle humanoids on a 22-joint skeleton, ground of 64x64 quads, four point
 lights, 512x512 textures) at 1920x1080 with 2x MSAA; `--config 1|3` selects the static
-640x360 scene or the 262k-triangle lightmapped atrium at 1920x1080 with 4x MSAA.
+640x360 scene or the 262k-triangle lightmapped atrium at 1920x1080 with 4x MSAA; `--config 4|5`
+the batched multi-view and served workloads; `--config 6` ray queries (2^20 rays against the
+atrium scene, rays/s).
 
   value   frames/s with the scene resident in device memory and the colour left there
   e2e     frames/s through the public API into a host colour buffer (pinned staging of the
@@ -42,6 +44,7 @@ CONFIGS = {
     3: dict(gen="config3", samples=4, name="atrium_1080p_4xmsaa", width=1920, height=1080),
     4: dict(gen="config4", samples=None, name="multiview_96_views_6_scenes", width=None, height=None),
     5: dict(gen="config5", samples=None, name="served_16_scenes_poisson", width=None, height=None),
+    6: dict(gen="config3", samples=None, name="raycast_atrium_1m_rays", width=None, height=None, rays=1 << 20),
 }
 SERVE_RATES = (100, 500, 1000, 2000, 5000)   # requests/s offered
 SERVE_BUDGET = 150 << 30                      # device-memory admission budget, bytes
@@ -453,6 +456,123 @@ def run_serve(args, cfg) -> dict:
     return line
 
 
+def run_raycast(args, cfg) -> dict:
+    """Ray queries (sft_raycast_instance, one GPU launch per step): 2^20 seeded rays against the
+    instances of the atrium scene (the 262k-triangle atrium and four characters).  `value` with
+    the rays resident in device memory (sftg_raycast_device), `e2e` through sftg_raycast with
+    pinned host arrays (rays H2D, hits D2H inside the timed region)."""
+    import torch
+    import torch.distributed as dist
+    from sofren2_gb300 import runtime, scenes
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    os.environ["SFT_CUDA_DEVICE"] = str(local)
+    dev = torch.device("cuda", local)
+    sc = getattr(scenes, cfg["gen"])()
+    blob = sc.to_bytes()
+    R = runtime.Renderer(640, 360, 1)
+    h = R.load_scene(blob)
+    n = cfg["rays"]
+    rays = scenes.ray_batch(sc, n)
+    ids = np.array([R.model_device_id(h, mi) for mi in range(len(sc.models))], np.int32)
+    rays_dev = rays.copy()
+    rays_dev["model"] = ids[rays["model"]]
+    R.render_device(h, 0)                         # resident tables in place
+    d_rays = torch.from_numpy(rays_dev.view(np.uint8).copy()).to(dev)
+    d_hits = torch.empty(n * 32, dtype=torch.uint8, device=dev)
+    pin_rays = torch.from_numpy(rays_dev.view(np.uint8).copy()).pin_memory()
+    pin_hits = torch.empty(n * 32, dtype=torch.uint8).pin_memory()
+    host_rays = pin_rays.numpy().view(runtime.RAY_DTYPE)
+    host_hits = pin_hits.numpy().view(runtime.HIT_DTYPE)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(R.stream(), device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(step, k):
+        times = []
+        for _ in range(k):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return times
+
+    dev_step = lambda: R.raycast_device(d_rays.data_ptr(), n, d_hits.data_ptr())   # noqa: E731
+    e2e_step = lambda: R.raycast_host(host_rays, host_hits)                         # noqa: E731
+    for _ in range(args.warmup):
+        dev_step()
+        e2e_step()
+    torch.cuda.synchronize()
+    got = d_hits.cpu().numpy().view(runtime.HIT_DTYPE)
+    assert got.tobytes() == host_hits.tobytes(), "device and host raycast entry points disagree"
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dev_times = timed(dev_step, args.steps)
+    e2e_times = timed(e2e_step, args.steps)
+    clk = clocks.stop()
+    ms_dev, ms_e2e = max_over_ranks([float(np.sum(dev_times)), float(np.sum(e2e_times))], device=f"cuda:{local}")
+    peaks = _peaks()
+    per_launch = float(np.mean(dev_times))
+    alg = n * (96 + 32)
+    achieved = alg / (per_launch * 1e-3) / 1e9
+    line = {
+        "metric": "rays_per_second", "value": job_throughput(args.steps * n, world, ms_dev), "unit": "rays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded rays against the seeded atrium scene)",
+        "config": {"workload": cfg["name"], "rays": n, "hit_fraction": float((host_hits["hit"] == 1).mean()),
+                   "l2": "flushed between steps (512 MiB device write, outside the timed events)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": job_throughput(args.steps * n, world, ms_e2e), "unit": "rays/s",
+                "h2d_bytes_per_step": int(n * 96), "d2h_bytes_per_step": int(n * 32)},
+        "gpu_launches": int(args.steps),
+        "roofline": {"kernel": "k_raycast", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "algorithmic_bytes": alg,
+                     "peak_source": peaks["src"],
+                     "note": "latency-bound divergent BLAS walks; algorithmic bytes are the ray and hit records only"},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = raycast_cpu_baseline(blob, rays, seconds=args.cpu_seconds)
+    R.free_scene(h)
+    R.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def raycast_cpu_baseline(blob: bytes, rays: np.ndarray, seconds: float = 12.0, chunk: int = 1 << 15) -> dict:
+    """The oracle's scalar sft_raycast_instance restatement on one host core, over consecutive
+    chunks of the same rays until `seconds` have passed."""
+    from oracle_lib import Oracle, build_oracle
+    build_oracle()
+    o = Oracle(blob)
+    done, t = 0, 0.0
+    try:
+        while t < seconds and done < len(rays):
+            r = rays[done:done + chunk]
+            t0 = time.perf_counter()
+            o.raycast(r)
+            t += time.perf_counter() - t0
+            done += len(r)
+    finally:
+        o.close()
+    return {"value": done / t, "unit": "rays/s", "cores": 1, "kind": "port",
+            "sample": f"the first {done} rays of the same batch (oracle/sft_oracle.c sfto_raycast, one thread, as "
+                      "the reference's sft_raycast_instance runs on the calling thread)"}
+
+
 def cpu_baseline(blob: bytes, samples: int, width: int, height: int, seconds: float = 12.0, frame: int = 0) -> dict:
     """The oracle restatement of the reference algorithm, timed on the host cores."""
     from oracle_lib import Oracle, build_oracle
@@ -485,6 +605,30 @@ def run_reference(args, cfg) -> dict | None:
     from oracle_lib import Oracle, build_oracle
     build_oracle()
     threads = os.cpu_count() or 1
+    if args.config == 6:   # bounded sample: 2^15 rays per step, consecutive chunks of the batch
+        sc = getattr(scenes, cfg["gen"])()
+        rays = scenes.ray_batch(sc, cfg["rays"])
+        o = Oracle(sc.to_bytes())
+        chunk, times = 1 << 15, []
+        try:
+            for k in range(max(1, args.warmup) + args.steps):
+                r = rays[(k * chunk) % len(rays):][:chunk]
+                t0 = time.perf_counter()
+                o.raycast(r)
+                if k >= max(1, args.warmup):
+                    times.append((time.perf_counter() - t0) / len(r))
+        finally:
+            o.close()
+        rps = len(times) / sum(times)
+        return {"metric": "rays_per_second", "value": rps, "unit": "rays/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * chunk / rps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded rays against the seeded atrium scene)", "impl": "reference",
+                "config": {"workload": cfg["name"], "rays": cfg["rays"], "sample": f"{chunk} rays per step"},
+                "cpu_baseline": {"value": rps, "unit": "rays/s", "cores": 1, "kind": "port",
+                                 "sample": f"{len(times)} steps of {chunk} rays after {max(1, args.warmup)} warm-up, scalar "
+                                           "restatement of sft_raycast_instance (oracle/sft_oracle.c), one thread"},
+                "e2e": {"value": rps, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if args.config == 5:   # bounded sample: the first frame of each scene, cycling
         scs, smp = scenes.config5()
         jobs = [(sc.to_bytes(), 0, S, sc.frames[0].width, sc.frames[0].height) for sc, S in zip(scs, smp)]
@@ -540,6 +684,8 @@ def main():
         line = run_batch(args, cfg)
     elif args.config == 5:
         line = run_serve(args, cfg)
+    elif args.config == 6:
+        line = run_raycast(args, cfg)
     else:
         line = run_ours(args, cfg)
     if line is not None:

@@ -438,6 +438,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
     __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
+    __shared__ sftg_point_light s_pl[SFTG_MAX_TILE_LIGHTS];   /* the tile's lights, in list order */
     __shared__ int s_nlights;
     __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
 
@@ -501,6 +502,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     }
     __syncthreads();
     const int ntl = s_nlights;
+    if (tid < ntl) s_pl[tid] = F->point[s_lights[tid]];   /* read after the barrier that follows D3 */
 
     /* World bounds of every triangle visible in this quarter tile, for the proxy filter below. */
     __shared__ float s_bnd[TILE_THREADS / 32][6];
@@ -787,13 +789,26 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                     }
                 }
                 /* D10 point lights and capsule shadows (6474-6607) */
+                /* A lightmapped surface and a light with no cached proxy: msh = 0, si = 1 and the
+                 * light multiplies lms by 1 - 0 * att, a no-op unless att is NaN (att is in [0, 1]
+                 * or NaN).  The reference's path below reaches that product only when some lane
+                 * of the block has att > 0 and some covered lane has a NaN att; such lights are
+                 * gathered as bits and applied after the loop (NaN absorbs the other factors, so
+                 * order does not matter).  Not used while per-light shadow factors are captured. */
+                const bool lm_quick = lm && shadow_out == nullptr;
+                uint32_t q_alive = 0, q_nan = 0;
                 for (int i = 0; i < ntl; i++) {
-                    const sftg_point_light L = F->point[s_lights[i]];
+                    const sftg_point_light& L = s_pl[i];
                     const v3 Lr = sub3(mk3(L.pos[0], L.pos[1], L.pos[2]), P);
                     const float d2 = vdot(Lr, Lr);
                     float att = vmax(0.f, fma_(-d2, L.inv_radius_sqr, 1.f));
                     att = att * att;
                     const bool alive = att > 0.f;
+                    if (lm_quick && s_npc[i] == 0) {
+                        q_alive |= (uint32_t)alive << i;
+                        q_nan |= (uint32_t)(in_tri && !(att <= 3.402823466e38f)) << i;
+                        continue;
+                    }
                     if (!(__ballot_sync(gmask, alive) & gmask)) continue;
                     v3 Ln = mk3(0.f, 0.f, 0.f);
                     float ndl = 0.f;
@@ -884,6 +899,13 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                             spc[0] = fma_(term, L.color[0], spc[0]); spc[1] = fma_(term, L.color[1], spc[1]); spc[2] = fma_(term, L.color[2], spc[2]);
                         }
                     }
+                }
+                if (lm_quick) {   /* uniform over the block's 8 lanes, as the shuffles need */
+                    uint32_t ga = q_alive;
+                    ga |= __shfl_xor_sync(gmask, ga, 1);
+                    ga |= __shfl_xor_sync(gmask, ga, 2);
+                    ga |= __shfl_xor_sync(gmask, ga, 4);
+                    if (ga & q_nan) lms = __int_as_float(0x7FFFFFFF);
                 }
                 if (lm) {
                     const float mod = fma_(lms, 1.f - 0.4f, 0.4f);

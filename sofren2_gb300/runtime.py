@@ -347,6 +347,24 @@ class Renderer:
             out[k] = (hits[k].hit, hits[k].distance, tuple(hits[k].pos), tuple(hits[k].normal))
         return out
 
+    def model_device_id(self, h, mi: int) -> int:
+        """The resident model id (sftg_model_upload) of model mi of scene h: sft_model's first field."""
+        p = self.lib.sftx_scene_model(h, mi)
+        if not p:
+            raise ValueError(f"scene has no model {mi}")
+        return C.c_int32.from_address(p).value
+
+    def raycast_host(self, rays: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
+        """sftg_raycast on host arrays of RAY_DTYPE records whose `model` is a resident model id;
+        hits go to `out` (HIT_DTYPE) when given."""
+        r = np.ascontiguousarray(rays, RAY_DTYPE)
+        if out is None:
+            out = np.zeros(len(r), HIT_DTYPE)
+        ctx = self.lib.sft_get_gpu_context()
+        if self.lib.sftg_raycast(ctx, _ptr(r), len(r), _ptr(out)) != 0:
+            raise RuntimeError("raycast failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
+        return out
+
     def raycast_device(self, d_rays: int, n: int, d_hits: int) -> None:
         """sftg_raycast_device on device arrays of sftg_ray / sftg_ray_hit (raw pointers), queued
         on the library's stream."""

@@ -1198,3 +1198,40 @@ def config3(width=1920, height=1080, seed=3001) -> Scene:
     semicircular arches forming a 30x15x15 m atrium, 25 textures of 1024x1024, a baked
     lightmap page, four skinned characters, sixteen point lights covering the floor."""
     return atrium_scene(width, height, seed)
+
+
+RAY_RECORD = np.dtype([("T", "<f4", (16,)), ("o", "<f4", (3,)), ("d", "<f4", (3,)), ("max_dist", "<f4"), ("model", "<i4")])
+
+
+def ray_batch(sc: Scene, n: int, seed: int = 6001, frame: int = 0) -> np.ndarray:
+    """n ray queries (sftg_ray records; `model` is the scene's model index) against the instances
+    of one frame: origins scattered around the camera, 70% aimed at points of a model's bounds
+    as sft_raycast_instance places the model (transform rows 0-2, no translation), 20% random
+    directions, 10% along coordinate axes; distance limit 1000, 10% a short one."""
+    rng = np.random.default_rng(seed)
+    fr = sc.frames[frame]
+    insts = [(mi, np.asarray(T, np.float32).reshape(4, 4)) for mi, T, _ in fr.instances]
+    lo, hi = {}, {}
+    for mi, _ in insts:
+        if mi not in lo:
+            pos = np.concatenate([ms.attr.reshape(ms.n, 10, 64)[:, 0:3].transpose(0, 2, 1).reshape(-1, 3) for ms in sc.models[mi].meshes])
+            lo[mi], hi[mi] = pos.min(0), pos.max(0)
+    pick = rng.integers(0, len(insts), n)
+    out = np.zeros(n, RAY_RECORD)
+    Ts = np.stack([T for _, T in insts])
+    out["T"] = Ts[pick].reshape(n, 16)
+    out["model"] = np.array([mi for mi, _ in insts], np.int32)[pick]
+    o = (np.asarray(fr.cam_pos, np.float32) + rng.normal(0, 1.5, (n, 3))).astype(np.float32)
+    out["o"] = o
+    L = np.stack([lo[mi] for mi, _ in insts])[pick]
+    Hh = np.stack([hi[mi] for mi, _ in insts])[pick]
+    p = (L + rng.random((n, 3)) * (Hh - L)).astype(np.float32)
+    aimed = np.einsum("nj,njk->nk", p, Ts[pick][:, :3, :3]).astype(np.float32) - o
+    rand_d = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    axis_d = np.zeros((n, 3), np.float32)
+    axis_d[np.arange(n), rng.integers(0, 3, n)] = rng.choice([-1.0, 1.0], n)
+    kind = rng.random(n)
+    d = np.where((kind < 0.7)[:, None], aimed, np.where((kind < 0.9)[:, None], rand_d, axis_d))
+    out["d"] = d.astype(np.float32)
+    out["max_dist"] = np.where(rng.random(n) < 0.1, rng.uniform(0.5, 3.0, n), 1000.0).astype(np.float32)
+    return out
