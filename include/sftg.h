@@ -234,6 +234,23 @@ int sftg_raycast(sftg_ctx* ctx, const sftg_ray* rays, uint32_t n, sftg_ray_hit* 
 /* device arrays, queued on the context's stream (sftg_stream); returns without waiting */
 int sftg_raycast_device(sftg_ctx* ctx, const sftg_ray* d_rays, uint32_t n, sftg_ray_hit* d_hits);
 
+/* Overlapping batches.  A context has SFTG_MAX_LANES submission lanes, each with its own streams,
+ * frame arena and colour pool; lane 0 serves the synchronous calls above.  sftg_frames_submit
+ * queues a batch (as sftg_frames_render would render it) on lane 1..SFTG_MAX_LANES-1 and returns
+ * without waiting, so that batches submitted on different lanes run on the GPU at the same time;
+ * the frame descriptions, everything they point at and the colour buffers must stay valid until
+ * sftg_lane_wait returns.  sftg_lane_done is 1 once the lane's batch has finished (or the lane is
+ * idle) and 0 while it runs; sftg_lane_wait waits for it, re-renders it when a capacity had to
+ * grow, and returns its status.  A batch with a view that keeps the caller's pixels (clear off)
+ * completes inside sftg_frames_submit.  Each view's pixels are those it would get alone. */
+#define SFTG_MAX_LANES 8
+int sftg_frames_submit(sftg_ctx* ctx, uint32_t lane, const sftg_frame_desc* frames, uint32_t n_views, uint32_t* const* colors,
+                       const int32_t* pitch_bytes);
+int sftg_lane_done(sftg_ctx* ctx, uint32_t lane);
+int sftg_lane_wait(sftg_ctx* ctx, uint32_t lane);
+/* Kernels launched by every batch finished so far, on all lanes (a running total). */
+uint64_t sftg_launch_total(const sftg_ctx* ctx);
+
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);
 /* Number of kernels launched by the last frame. */

@@ -261,6 +261,14 @@ SFT_FUNC const void* sft_batch_peek(u32 i);
  * (sftg_autotune, reps renders per candidate) and drop them; ends the batch */
 SFT_FUNC i32 sft_batch_autotune(i32 reps);
 SFT_FUNC void* sft_get_gpu_context(void);
+/* extension: overlapping batches.  sft_batch_submit_async ends the batch like sft_batch_submit
+ * but queues it on submission lane `lane` (1 to SFTG_MAX_LANES - 1) and returns at once; the
+ * colour buffers must stay untouched until sft_batch_wait(lane) returns, which waits for the
+ * batch and gives its status.  sft_batch_done(lane) is 1 once the lane's batch has finished
+ * (or the lane is idle), 0 while it runs.  Batches on different lanes overlap on the GPU. */
+SFT_FUNC i32 sft_batch_submit_async(u32 lane);
+SFT_FUNC i32 sft_batch_done(u32 lane);
+SFT_FUNC i32 sft_batch_wait(u32 lane);
 
 #ifdef __cplusplus
 }
@@ -339,6 +347,8 @@ static struct sft__state {
     /* batched submission: frames recorded by sft_present between sft_batch_begin / _submit */
     u8 batching; u32 n_batch, cap_batch;
     sftg_frame_desc* batch_fd; u32** batch_color; i32* batch_pitch; void** batch_mem;
+    /* batches handed to submission lanes, kept until sft_batch_wait */
+    struct { sftg_frame_desc* fd; u32** color; i32* pitch; void** mem; u32 n; } lane[SFTG_MAX_LANES];
 } *sft__s;
 
 /* ---------------------------------------------------------------- math (sofren2.c:1503-1918) */
@@ -631,6 +641,7 @@ SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads) {
 
 SFT_FUNC void sft_release(void) {
     if (!sft__s) return;
+    for (u32 l = 1; l < SFTG_MAX_LANES; l++) if (sft__s->lane[l].n) sft_batch_wait(l);
     sftg_destroy(sft__s->gpu);
     for (i32 i = 0; i < sft__s->tex_cap; i++) free(sft__s->tex[i].level0);
     free(sft__s->tex); free(sft__s->mat_gen); free(sft__s->mat_next);
@@ -1452,6 +1463,50 @@ SFT_FUNC i32 sft_batch_submit(void) {
     sft__dmesh_release_frame();
     if (rc) fprintf(stderr, "sofren2-gb300: sft_batch_submit failed (%d): %s\n", rc, sftg_last_error(s->gpu));
     return rc;
+}
+
+static void sft__lane_free(u32 lane) {
+    struct sft__state* s = sft__s;
+    for (u32 i = 0; i < s->lane[lane].n; i++) free(s->lane[lane].mem[i]);
+    free(s->lane[lane].fd); free(s->lane[lane].color); free(s->lane[lane].pitch); free(s->lane[lane].mem);
+    memset(&s->lane[lane], 0, sizeof(s->lane[lane]));
+}
+
+SFT_FUNC i32 sft_batch_wait(u32 lane) {
+    struct sft__state* s = sft__s;
+    if (!s || lane == 0 || lane >= SFTG_MAX_LANES) return SFTG_E_ARG;
+    if (!s->lane[lane].n) return 0;
+    const int rc = sftg_lane_wait(s->gpu, lane);
+    sft__lane_free(lane);
+    if (rc) fprintf(stderr, "sofren2-gb300: sft_batch_wait failed (%d): %s\n", rc, sftg_last_error(s->gpu));
+    return rc;
+}
+
+SFT_FUNC i32 sft_batch_submit_async(u32 lane) {
+    struct sft__state* s = sft__s;
+    s->batching = 0;
+    if (lane == 0 || lane >= SFTG_MAX_LANES) return SFTG_E_ARG;
+    if (s->lane[lane].n) { const i32 w = sft_batch_wait(lane); if (w) return w; }
+    if (!s->n_batch) return 0;
+    /* the recorded frames move to the lane and stay there until sft_batch_wait */
+    s->lane[lane].fd = s->batch_fd; s->lane[lane].color = s->batch_color; s->lane[lane].pitch = s->batch_pitch;
+    s->lane[lane].mem = s->batch_mem; s->lane[lane].n = s->n_batch;
+    s->batch_fd = NULL; s->batch_color = NULL; s->batch_pitch = NULL; s->batch_mem = NULL;
+    s->n_batch = 0; s->cap_batch = 0;
+    u8 any_host = 0;
+    for (u32 i = 0; i < s->lane[lane].n; i++) any_host |= s->lane[lane].color[i] != NULL;
+    const int rc = sftg_frames_submit(s->gpu, lane, s->lane[lane].fd, s->lane[lane].n, any_host ? s->lane[lane].color : NULL,
+                                      s->lane[lane].pitch);
+    if (rc) {
+        fprintf(stderr, "sofren2-gb300: sft_batch_submit_async failed (%d): %s\n", rc, sftg_last_error(s->gpu));
+        sft__lane_free(lane);
+    }
+    return rc;
+}
+
+SFT_FUNC i32 sft_batch_done(u32 lane) {
+    if (!sft__s || lane >= SFTG_MAX_LANES) return SFTG_E_ARG;
+    return sft__s->lane[lane].n ? sftg_lane_done(sft__s->gpu, lane) : 1;
 }
 
 SFT_FUNC i32 sft_model_set_skeleton(sft_model* model, const sftg_bone_desc* bones, u32 bone_count,

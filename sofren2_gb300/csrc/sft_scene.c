@@ -205,6 +205,45 @@ SFTX_EXPORT int sftx_scene_render_batch(void* const* scenes, const uint32_t* fra
     return sft_batch_submit();
 }
 
+/* Renders n views as `lanes` batches queued on submission lanes 1..lanes without waiting in
+ * between, so that they overlap on the GPU, then waits for all of them.  Views go to the batch
+ * with the least work so far (pixels x samples), heaviest first. */
+SFTX_EXPORT int sftx_scene_render_lanes(void* const* scenes, const uint32_t* frames, const int32_t* samples, uint32_t n,
+                                        uint32_t* const* colors, const int32_t* pitch_bytes, uint32_t lanes) {
+    if (lanes < 1 || lanes > SFTG_MAX_LANES - 1) return -1;
+    uint32_t* order = (uint32_t*)malloc((size_t)(n ? n : 1) * 4);
+    uint32_t* group = (uint32_t*)malloc((size_t)(n ? n : 1) * 4);
+    double* cost = (double*)malloc((size_t)(n ? n : 1) * sizeof(double));
+    double load[SFTG_MAX_LANES] = { 0 };
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t w = 0, h = 0;
+        sftx_scene_frame_size(scenes[i], frames[i], &w, &h);
+        cost[i] = (double)w * h * samples[i];
+        order[i] = i;
+    }
+    for (uint32_t i = 1; i < n; i++)   /* heaviest first (insertion sort; n is small) */
+        for (uint32_t j = i; j > 0 && cost[order[j]] > cost[order[j - 1]]; j--) { const uint32_t t = order[j]; order[j] = order[j - 1]; order[j - 1] = t; }
+    for (uint32_t k = 0; k < n; k++) {
+        uint32_t g = 0;
+        for (uint32_t q = 1; q < lanes; q++) if (load[q] < load[g]) g = q;
+        group[order[k]] = g;
+        load[g] += cost[order[k]];
+    }
+    int rc = 0;
+    for (uint32_t g = 0; g < lanes; g++) {
+        sft_batch_begin();
+        for (uint32_t i = 0; i < n; i++) {
+            if (group[i] != g) continue;
+            sft_set_msaa_samples(samples[i]);
+            if (sftx_scene_render(scenes[i], frames[i], colors ? colors[i] : NULL, pitch_bytes ? pitch_bytes[i] : 0)) rc = -1;
+        }
+        if (sft_batch_submit_async(g + 1)) rc = -1;
+    }
+    for (uint32_t g = 0; g < lanes; g++) if (sft_batch_wait(g + 1)) rc = -1;
+    free(order); free(group); free(cost);
+    return rc;
+}
+
 /* Tunes the scheduling knobs on n (scene, frame, samples) views rendered as one batch. */
 SFTX_EXPORT int sftx_scene_autotune_batch(void* const* scenes, const uint32_t* frames, const int32_t* samples, uint32_t n,
                                           int32_t reps) {

@@ -38,11 +38,42 @@ struct dpool {   /* growable device buffer */
     size_t size = 0, cap = 0;
 };
 
-struct sftg_ctx {
-    int device = 0;
+/* One submission slot: its streams, phase events, frame arena, pinned staging, colour pool and
+ * the cached graph of its last batch layout.  Lane 0 serves the synchronous calls; lanes 1 and
+ * up serve sftg_frames_submit, so that batches on different lanes overlap on the GPU. */
+struct sftg_lane {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;            /* proxy occlusion runs here, beside geometry, binning and raster */
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_geo = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_geo = nullptr, ev_done = nullptr;
+    cudaEvent_t ev[6] = { nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
+    void* arena = nullptr;
+    size_t arena_cap = 0;
+    void* h_stage = nullptr;     /* pinned staging for the frame block */
+    size_t h_stage_cap = 0;
+    uint32_t* h_status = nullptr;
+    uint32_t* d_color = nullptr;
+    size_t d_color_cap = 0;
+    /* the last batch's launch sequence as an instantiated CUDA graph, replayed while the
+     * batch layout (every pointer, count and knob the launches take) stays the same */
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_key = 0;
+    uint64_t seen_key = 0;       /* layout of the previous batch: a graph is captured when it repeats */
+    int graph_launches = 0;
+    float timings[5] = { 0, 0, 0, 0, 0 };
+    int launches = 0;
+    /* a batch in flight (sftg_frames_submit): what sftg_lane_wait needs to finish it */
+    bool busy = false;
+    const sftg_frame_desc* fds = nullptr;
+    uint32_t nv = 0;
+    std::vector<uint32_t*> colors;
+    std::vector<int32_t> pitch;
+};
+
+struct sftg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;             /* lane 0's stream: uploads and the synchronous calls */
+    cudaEvent_t ev_upload = nullptr;           /* orders other lanes after the uploads queued before them */
+    sftg_lane lanes[SFTG_MAX_LANES];
     char err[512] = { 0 };
     /* resident */
     dpool texels, texs, mats, ml_attr, ml_inds, ml_cull, ml_info, skin_j, skin_w, blas, models;
@@ -55,24 +86,12 @@ struct sftg_ctx {
     std::vector<std::vector<uint32_t>> h_mesh_count;
     uint32_t n_meshlets = 0, n_skin = 0, n_blas = 0;
     bool tables_dirty = true;
-    /* per frame */
-    void* arena = nullptr;
-    size_t arena_cap = 0;
-    void* h_stage = nullptr;     /* pinned staging for the frame block */
-    size_t h_stage_cap = 0;
-    uint32_t* h_status = nullptr;
+    /* per frame: capacities shared by the lanes (they only grow), the last finished batch's figures */
     uint64_t tile_cap = 1u << 20, clip_cap = 1u << 16;
-    cudaEvent_t ev[6] = { nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
     float timings[5] = { 0, 0, 0, 0, 0 };
     int launches = 0;
-    /* the last batch's launch sequence as an instantiated CUDA graph, replayed while the
-     * batch layout (every pointer, count and knob the launches take) stays the same */
-    cudaGraphExec_t graph = nullptr;
-    uint64_t graph_key = 0;
-    int graph_launches = 0;
+    uint64_t launch_total = 0;                 /* kernels of every finished batch, on all lanes */
     bool use_graphs = true;
-    uint32_t* d_color = nullptr;
-    size_t d_color_cap = 0;
     sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
     /* transient models (one frame's dynamic meshes): pool marks where they start */
     bool tr_live = false, tr_pinned = false;
@@ -96,8 +115,16 @@ static int set_err(sftg_ctx* c, int code, const char* fmt, ...) {
 
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return set_err(ctx, SFTG_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); } while (0)
 
+/* Waits for every lane's work: resident pools are about to move or be overwritten. */
+static int wait_lanes(sftg_ctx* ctx) {
+    for (int l = 0; l < SFTG_MAX_LANES; l++)
+        if (ctx->lanes[l].stream) CK(cudaStreamSynchronize(ctx->lanes[l].stream));
+    return 0;
+}
+
 static int pool_reserve(sftg_ctx* ctx, dpool& p, size_t bytes) {
     if (bytes <= p.cap) return 0;
+    if (int rc = wait_lanes(ctx)) return rc;
     size_t nc = p.cap ? p.cap : 1 << 20;
     while (nc < bytes) nc *= 2;
     void* np = nullptr;
@@ -122,6 +149,8 @@ static int pool_append(sftg_ctx* ctx, dpool& p, const void* src, size_t bytes, s
     return 0;
 }
 
+extern "C" void sftg_destroy(sftg_ctx* ctx);
+
 extern "C" int sftg_create(int device, sftg_ctx** out) {
     if (!out) return SFTG_E_ARG;
     sftg_ctx* ctx = new sftg_ctx();
@@ -130,13 +159,19 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) { delete ctx; return SFTG_E_CUDA; }
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
-    for (int i = 0; i < 6; i++) cudaEventCreate(&ctx->ev[i]);
-    if (cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
-    cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
-    cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
-    cudaEventCreate(&ctx->ev_geo);
-    if (cudaMallocHost((void**)&ctx->h_status, 64) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
+    for (int l = 0; l < SFTG_MAX_LANES; l++) {
+        sftg_lane& ln = ctx->lanes[l];
+        if (cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&ln.stream2, cudaStreamNonBlocking) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
+        for (int i = 0; i < 6; i++) cudaEventCreate(&ln.ev[i]);
+        cudaEventCreateWithFlags(&ln.ev_fork, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ln.ev_join, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ln.ev_done, cudaEventDisableTiming);
+        cudaEventCreate(&ln.ev_geo);
+        if (cudaMallocHost((void**)&ln.h_status, 64) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
+    }
+    ctx->stream = ctx->lanes[0].stream;
+    cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming);
     sftg_tile_configure(227 * 1024);
     { const char* e = getenv("SFTG_NO_GRAPHS"); if (e && *e && *e != '0') ctx->use_graphs = false; }
     *out = ctx;
@@ -146,22 +181,27 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
 extern "C" void sftg_destroy(sftg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    for (int l = 0; l < SFTG_MAX_LANES; l++) if (ctx->lanes[l].stream) cudaStreamSynchronize(ctx->lanes[l].stream);
     dpool* pools[] = { &ctx->texels, &ctx->texs, &ctx->mats, &ctx->ml_attr, &ctx->ml_inds, &ctx->ml_cull, &ctx->ml_info,
                        &ctx->skin_j, &ctx->skin_w, &ctx->blas, &ctx->models, &ctx->p_skels, &ctx->p_bones, &ctx->p_anims,
                        &ctx->p_samplers, &ctx->p_channels, &ctx->p_keys, &ctx->p_order, &ctx->p_levels, &ctx->p_pose_io, &ctx->p_ray_io };
     for (dpool* p : pools) if (p->ptr) cudaFree(p->ptr);
-    if (ctx->arena) cudaFree(ctx->arena);
-    if (ctx->d_color) cudaFree(ctx->d_color);
-    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
-    if (ctx->h_status) cudaFreeHost(ctx->h_status);
-    for (int i = 0; i < 6; i++) if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
-    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
-    if (ctx->ev_geo) cudaEventDestroy(ctx->ev_geo);
-    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
-    cudaStreamDestroy(ctx->stream);
+    for (int l = 0; l < SFTG_MAX_LANES; l++) {
+        sftg_lane& ln = ctx->lanes[l];
+        if (ln.arena) cudaFree(ln.arena);
+        if (ln.d_color) cudaFree(ln.d_color);
+        if (ln.h_stage) cudaFreeHost(ln.h_stage);
+        if (ln.h_status) cudaFreeHost(ln.h_status);
+        for (int i = 0; i < 6; i++) if (ln.ev[i]) cudaEventDestroy(ln.ev[i]);
+        if (ln.graph) cudaGraphExecDestroy(ln.graph);
+        if (ln.ev_fork) cudaEventDestroy(ln.ev_fork);
+        if (ln.ev_join) cudaEventDestroy(ln.ev_join);
+        if (ln.ev_done) cudaEventDestroy(ln.ev_done);
+        if (ln.ev_geo) cudaEventDestroy(ln.ev_geo);
+        if (ln.stream2) cudaStreamDestroy(ln.stream2);
+        if (ln.stream) cudaStreamDestroy(ln.stream);
+    }
+    if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
     delete ctx;
 }
 
@@ -295,6 +335,7 @@ extern "C" int sftg_model_upload_transient(sftg_ctx* ctx, const sftg_model_desc*
 extern "C" void sftg_transient_reset(sftg_ctx* ctx) {
     if (!ctx || !ctx->tr_live) return;
     if (!ctx->tr_pinned) {   /* drop the transient tail of every pool and table */
+        wait_lanes(ctx);     /* a lane in flight may still read it */
         ctx->n_meshlets = ctx->tr_meshlets; ctx->n_skin = ctx->tr_skin; ctx->n_blas = ctx->tr_blas;
         ctx->h_models.resize(ctx->tr_models);
         ctx->h_mesh_skinned.resize(ctx->tr_models); ctx->h_mesh_first.resize(ctx->tr_models); ctx->h_mesh_count.resize(ctx->tr_models);
@@ -382,7 +423,7 @@ static int sample_slot(int S) { return S == 1 ? 0 : (S == 2 ? 1 : 2); }
  * (screen-space cache, batch records, clip pool, tile lists, light_vis, visibility buffers) are
  * laid out view after view, with tiles numbered by sample count first (1, 2, 4) so that each
  * raster/resolve specialisation covers one contiguous tile range. */
-static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, bool want_debug, batch_bufs& B) {
+static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds, uint32_t nv, bool want_debug, batch_bufs& B) {
     if (!nv || nv > 65535) return set_err(ctx, SFTG_E_ARG, "a batch holds 1 to 65535 views, not %u", nv);
     if (want_debug && nv != 1) return set_err(ctx, SFTG_E_ARG, "debug capture covers single-view submissions only");
     B.plan.assign(nv, view_plan{});
@@ -488,26 +529,26 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
     const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
     if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
-    if (need > ctx->arena_cap) {
-        if (ctx->arena) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->arena); ctx->arena = nullptr; }
+    if (need > ln.arena_cap) {
+        if (ln.arena) { cudaStreamSynchronize(ln.stream); cudaFree(ln.arena); ln.arena = nullptr; }
         size_t nc = need + need / 4;
-        if (cudaMalloc(&ctx->arena, nc) != cudaSuccess) { ctx->arena_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "frame arena of %zu bytes", nc); }
-        ctx->arena_cap = nc;
+        if (cudaMalloc(&ln.arena, nc) != cudaSuccess) { ln.arena_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "frame arena of %zu bytes", nc); }
+        ln.arena_cap = nc;
     }
-    if (color_total * 4 > ctx->d_color_cap) {
-        if (ctx->d_color) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->d_color); }
-        if (cudaMalloc((void**)&ctx->d_color, color_total * 4) != cudaSuccess) { ctx->d_color = nullptr; ctx->d_color_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "colour buffers"); }
-        ctx->d_color_cap = color_total * 4;
+    if (color_total * 4 > ln.d_color_cap) {
+        if (ln.d_color) { cudaStreamSynchronize(ln.stream); cudaFree(ln.d_color); }
+        if (cudaMalloc((void**)&ln.d_color, color_total * 4) != cudaSuccess) { ln.d_color = nullptr; ln.d_color_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "colour buffers"); }
+        ln.d_color_cap = color_total * 4;
     }
-    if (stage_bytes > ctx->h_stage_cap) {
-        if (ctx->h_stage) { cudaStreamSynchronize(ctx->stream); cudaFreeHost(ctx->h_stage); }
+    if (stage_bytes > ln.h_stage_cap) {
+        if (ln.h_stage) { cudaStreamSynchronize(ln.stream); cudaFreeHost(ln.h_stage); }
         size_t nc = stage_bytes + stage_bytes / 4 + 4096;
-        if (cudaMallocHost(&ctx->h_stage, nc) != cudaSuccess) { ctx->h_stage = nullptr; ctx->h_stage_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "pinned staging"); }
-        ctx->h_stage_cap = nc;
+        if (cudaMallocHost(&ln.h_stage, nc) != cudaSuccess) { ln.h_stage = nullptr; ln.h_stage_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "pinned staging"); }
+        ln.h_stage_cap = nc;
     }
-    char* hs = (char*)ctx->h_stage;
-    char* ds = (char*)ctx->arena;
-    bump bp{ ds, stage_bytes, ctx->arena_cap };
+    char* hs = (char*)ln.h_stage;
+    char* ds = (char*)ln.arena;
+    bump bp{ ds, stage_bytes, ln.arena_cap };
     B.ss = bp.take<float>((size_t)total_ss * 576);
     B.recs = bp.take<sftg_batch_rec>(n_rec);
     B.clip_cnt = bp.take<uint32_t>(n_rec);
@@ -566,7 +607,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
         F->clip_cap = (uint32_t)ctx->clip_cap; F->tile_cap = (uint32_t)ctx->tile_cap;
         F->view = v; F->ss_base = P.ss_base; F->tile_base = P.tile_base; F->prox_base = P.prox_base;
         F->packet_base = P.packet_base; F->n_packets = P.n_packets; F->vis_base = P.vis_base;
-        F->color_dev = ctx->d_color + P.color_off;
+        F->color_dev = ln.d_color + P.color_off;
         F->inst = (const sftg_inst*)(ds + o_inst) + P.inst_off;
         F->bones = (const float*)(ds + o_bones) + P.bone_off;
         F->jobs = (const sftg_job*)(ds + o_jobs);
@@ -601,7 +642,7 @@ static int build_batch(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, b
     B.tile_view = (const uint16_t*)(ds + o_tv);
     B.packet_view = (const uint16_t*)(ds + o_pv);
     B.prox_view = (const uint16_t*)(ds + o_xv);
-    CK(cudaMemcpyAsync(ds, hs, stage_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ds, hs, stage_bytes, cudaMemcpyHostToDevice, ln.stream));
     return 0;
 }
 
@@ -614,55 +655,55 @@ static cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
     return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
 }
 
-static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
+static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     const uint32_t n_rec = B.total_ss * 16;
-    cudaStream_t st = ctx->stream;
-    ctx->launches = 0;
+    cudaStream_t st = ln.stream;
+    ln.launches = 0;
     CK(cudaGetLastError());   /* nothing pending from earlier calls: every launch below is checked */
     CK(cudaMemsetAsync(B.status, 0, 64, st));
-    CK(record_event(ctx->ev[0], st));
+    CK(record_event(ln.ev[0], st));
     /* proxy occlusion only feeds the resolve: it runs on the second stream, forked here and
      * joined before the resolve, overlapping geometry, binning and raster */
     const bool occl = B.total_prox || B.total_packets;
     if (occl) {
-        cudaStream_t so = ctx->stream2;
-        CK(cudaEventRecord(ctx->ev_fork, st));
-        CK(cudaStreamWaitEvent(so, ctx->ev_fork, 0));
+        cudaStream_t so = ln.stream2;
+        CK(cudaEventRecord(ln.ev_fork, st));
+        CK(cudaStreamWaitEvent(so, ln.ev_fork, 0));
         if (B.total_prox) CK(cudaMemsetAsync(B.light_vis, 0, (size_t)B.total_prox * 64, so));   /* columns past the lights stay 0 */
         if (B.total_packets) {
             sftg_launch_occlusion(B.frames, B.packet_view, B.total_packets, B.prox_view, B.total_prox, B.max_inst, B.packets,
                                   B.pairs, B.n_pairs, B.max_pairs, SFTG_OCC_ITEMS_PER_PAIR, B.light_vis, B.status,
                                   ctx->tuning.occl_ray_prune, so);
-            ctx->launches += 4;
+            ln.launches += 4;
             CK(cudaGetLastError());
         }
-        CK(record_event(ctx->ev[1], so));
-        CK(cudaEventRecord(ctx->ev_join, so));
+        CK(record_event(ln.ev[1], so));
+        CK(cudaEventRecord(ln.ev_join, so));
     } else {
-        CK(record_event(ctx->ev[1], st));
+        CK(record_event(ln.ev[1], st));
     }
-    CK(record_event(ctx->ev_geo, st));
+    CK(record_event(ln.ev_geo, st));
     if (B.n_jobs) {
         k_geometry<<<(B.n_jobs + 3) / 4, 128, 0, st>>>(B.frames, B.jobs, B.n_jobs, B.ss, B.recs, B.clip_cnt, B.mrect);
-        ctx->launches++;
+        ln.launches++;
         CK(cudaGetLastError());
     }
     if (n_rec) {
-        scan_u32(B.clip_cnt, B.clip_base, n_rec, B.scan_tmp, B.totals + 0, st, &ctx->launches);
+        scan_u32(B.clip_cnt, B.clip_base, n_rec, B.scan_tmp, B.totals + 0, st, &ln.launches);
         k_clip<<<(n_rec + 255) / 256, 256, 0, st>>>(B.frames, B.n_views, B.ss, B.clip_cnt, B.clip_base, B.clips, B.clip_rect, B.mrect, n_rec);
-        ctx->launches++;
+        ln.launches++;
         CK(cudaGetLastError());
     } else {
         CK(cudaMemsetAsync(B.totals, 0, 8, st));
     }
-    CK(record_event(ctx->ev[2], st));
+    CK(record_event(ln.ev[2], st));
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
-    scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ctx->launches);
+    scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ln.launches);
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
     sftg_launch_tile_order(B.frames, B.tile_view, B.tile_count, B.total_tiles, B.order_scratch, B.tile_order, st);
-    ctx->launches += 4;
+    ln.launches += 4;
     CK(cudaGetLastError());
-    CK(record_event(ctx->ev[3], st));
+    CK(record_event(ln.ev[3], st));
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));
     sftg_tile_args A;
     A.frames = B.frames; A.tile_view = B.tile_view; A.ss = B.ss; A.clips = B.clips; A.clip_base = B.clip_base;
@@ -670,15 +711,15 @@ static int launch_batch(sftg_ctx* ctx, const batch_bufs& B) {
     A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
     for (int si = 0; si < 3; si++)
-        if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], st, A); ctx->launches++; }
+        if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], st, A); ln.launches++; }
     CK(cudaGetLastError());
-    CK(record_event(ctx->ev[4], st));
-    if (occl) CK(cudaStreamWaitEvent(st, ctx->ev_join, 0));
+    CK(record_event(ln.ev[4], st));
+    if (occl) CK(cudaStreamWaitEvent(st, ln.ev_join, 0));
     for (int si = 0; si < 3; si++)
-        if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ctx->launches++; }
-    if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ctx->launches++; }
+        if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ln.launches++; }
+    if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ln.launches++; }
     CK(cudaGetLastError());
-    CK(record_event(ctx->ev[5], st));
+    CK(record_event(ln.ev[5], st));
     return 0;
 }
 
@@ -706,83 +747,133 @@ static uint64_t batch_key(const sftg_ctx* ctx, const batch_bufs& B) {
     return h;
 }
 
-/* launch_batch through a CUDA graph: captured on the first batch of a layout, replayed after. */
-static int launch_batch_graph(sftg_ctx* ctx, const batch_bufs& B) {
+/* launch_batch through a CUDA graph: captured when a batch repeats the previous batch's layout,
+ * replayed while the layout stays.  A layout seen once (a served batch of new requests) is
+ * launched directly, without the cost of a capture it would not reuse. */
+static int launch_batch_graph(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     const uint64_t key = batch_key(ctx, B);
-    if (!ctx->graph || key != ctx->graph_key) {
-        if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = launch_batch(ctx, B);
+    const uint64_t prev = ln.seen_key;
+    ln.seen_key = key;
+    if ((!ln.graph || key != ln.graph_key) && key != prev) return launch_batch(ctx, ln, B);
+    if (!ln.graph || key != ln.graph_key) {
+        if (ln.graph) { cudaGraphExecDestroy(ln.graph); ln.graph = nullptr; }
+        CK(cudaStreamBeginCapture(ln.stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = launch_batch(ctx, ln, B);
         cudaGraph_t g = nullptr;
-        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        const cudaError_t e = cudaStreamEndCapture(ln.stream, &g);
         if (rc || e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
             return rc ? rc : set_err(ctx, SFTG_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
         }
-        const cudaError_t ie = cudaGraphInstantiate(&ctx->graph, g, 0);
+        const cudaError_t ie = cudaGraphInstantiate(&ln.graph, g, 0);
         cudaGraphDestroy(g);
-        if (ie != cudaSuccess) { ctx->graph = nullptr; return set_err(ctx, SFTG_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ie)); }
-        ctx->graph_key = key;
-        ctx->graph_launches = ctx->launches;
+        if (ie != cudaSuccess) { ln.graph = nullptr; return set_err(ctx, SFTG_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ie)); }
+        ln.graph_key = key;
+        ln.graph_launches = ln.launches;
     }
-    CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-    ctx->launches = ctx->graph_launches;
+    CK(cudaGraphLaunch(ln.graph, ln.stream));
+    ln.launches = ln.graph_launches;
     return 0;
 }
 
-/* Renders a batch of views.  host_color[v] (optional) receives view v's colour with pitch
- * pitch_bytes[v]; out_dev[v] (optional) its device colour buffer, valid until the next call. */
+/* Queues a batch on a lane: the frame block, the caller's pixels for views that keep them, the
+ * launches (one graph replay unless debug capture or graphs are off), the status read-back, the
+ * colour read-back (deferred to finish_batch when a view keeps the caller's pixels, so that a
+ * re-render still starts from them) and the lane's completion event. */
+static int submit_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds, uint32_t nv, uint32_t* const* host_color,
+                        const int32_t* pitch_bytes, sftg_debug_out* dbg, batch_bufs& B, bool& defer_colors) {
+    auto pitch_of = [&](uint32_t v) { return (pitch_bytes && pitch_bytes[v] > 0) ? (size_t)pitch_bytes[v] : (size_t)fds[v].width * 4; };
+    if (&ln != &ctx->lanes[0]) {   /* after every upload queued so far on lane 0's stream */
+        CK(cudaEventRecord(ctx->ev_upload, ctx->stream));
+        CK(cudaStreamWaitEvent(ln.stream, ctx->ev_upload, 0));
+    }
+    int rc;
+    if ((rc = build_batch(ctx, ln, fds, nv, dbg != nullptr, B))) return rc;
+    defer_colors = false;
+    for (uint32_t v = 0; v < nv; v++)   /* the reference blends over / keeps the caller's pixels */
+        if (!fds[v].clear && host_color && host_color[v]) {
+            defer_colors = true;
+            CK(cudaMemcpy2DAsync(ln.d_color + B.plan[v].color_off, (size_t)fds[v].width * 4, host_color[v], pitch_of(v),
+                                 (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyHostToDevice, ln.stream));
+        }
+    if ((rc = (dbg || !ctx->use_graphs) ? launch_batch(ctx, ln, B) : launch_batch_graph(ctx, ln, B))) return rc;
+    CK(cudaMemcpyAsync(ln.h_status, B.status, 4, cudaMemcpyDeviceToHost, ln.stream));
+    CK(cudaMemcpyAsync(ln.h_status + 2, B.totals, 8, cudaMemcpyDeviceToHost, ln.stream));
+    if (!defer_colors)
+        for (uint32_t v = 0; v < nv; v++)
+            if (host_color && host_color[v])
+                CK(cudaMemcpy2DAsync(host_color[v], pitch_of(v), ln.d_color + B.plan[v].color_off, (size_t)fds[v].width * 4,
+                                     (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyDeviceToHost, ln.stream));
+    CK(cudaEventRecord(ln.ev_done, ln.stream));
+    return 0;
+}
+
+#define BATCH_REDO 1   /* finish_batch: a capacity was exceeded and has been grown; queue the batch again */
+
+/* Waits for the lane's batch and checks it: capacities, phase timings, deferred colour
+ * read-back, debug buffers, device colour pointers and the device status word. */
+static int finish_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds, uint32_t nv, uint32_t* const* host_color,
+                        const int32_t* pitch_bytes, const batch_bufs& B, bool defer_colors, sftg_debug_out* dbg,
+                        const uint32_t** out_dev) {
+    CK(cudaEventSynchronize(ln.ev_done));
+    const uint32_t clip_total = ln.h_status[2], pay_total = ln.h_status[3];
+    if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap) {   /* capacity exceeded: grow and redo the batch */
+        while (ctx->clip_cap < clip_total) ctx->clip_cap *= 2;
+        while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
+        return BATCH_REDO;
+    }
+    for (int k = 0; k < 5; k++) {   /* geometry is timed from its own start: occlusion runs beside it */
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, k == 1 ? ln.ev_geo : ln.ev[k], ln.ev[k + 1]) != cudaSuccess) { t = 0.f; cudaGetLastError(); }
+        ln.timings[k] = t;
+        ctx->timings[k] = t;
+    }
+    ctx->launches = ln.launches;
+    ctx->launch_total += (uint64_t)ln.launches;
+    if (defer_colors) {
+        auto pitch_of = [&](uint32_t v) { return (pitch_bytes && pitch_bytes[v] > 0) ? (size_t)pitch_bytes[v] : (size_t)fds[v].width * 4; };
+        for (uint32_t v = 0; v < nv; v++)
+            if (host_color && host_color[v])
+                CK(cudaMemcpy2DAsync(host_color[v], pitch_of(v), ln.d_color + B.plan[v].color_off, (size_t)fds[v].width * 4,
+                                     (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyDeviceToHost, ln.stream));
+        CK(cudaStreamSynchronize(ln.stream));
+    }
+    if (dbg) {
+        const sftg_frame_desc* fd = &fds[0];
+        const int W = fd->width, H = fd->height, S = fd->samples, tiles = (int)B.total_tiles;
+        if (dbg->vis_depth) CK(cudaMemcpy(dbg->vis_depth, B.vis_depth, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
+        if (dbg->vis_id) CK(cudaMemcpy(dbg->vis_id, B.vis_id, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
+        if (dbg->tile_counts) CK(cudaMemcpy(dbg->tile_counts, B.tile_count, (size_t)tiles * 4, cudaMemcpyDeviceToHost));
+        if (dbg->tile_payload_total) *dbg->tile_payload_total = pay_total;
+        if (dbg->tile_payloads && pay_total <= dbg->tile_payload_cap) CK(cudaMemcpy(dbg->tile_payloads, B.tile_pay, (size_t)pay_total * 8, cudaMemcpyDeviceToHost));
+        if (dbg->ss_cache) CK(cudaMemcpy(dbg->ss_cache, B.ss, (size_t)B.total_ss * 2304, cudaMemcpyDeviceToHost));
+        if (dbg->light_vis && fd->n_proxies) CK(cudaMemcpy(dbg->light_vis, B.light_vis, (size_t)fd->n_proxies * 64, cudaMemcpyDeviceToHost));
+        if (dbg->clip_total) *dbg->clip_total = clip_total;
+        if (dbg->clip_tris && clip_total <= dbg->clip_cap) CK(cudaMemcpy(dbg->clip_tris, B.clips, (size_t)clip_total * sizeof(sftg_clip_tri), cudaMemcpyDeviceToHost));
+        if (dbg->shadow && S == 1) CK(cudaMemcpy(dbg->shadow, B.shadow, (size_t)W * H * 16 * 4, cudaMemcpyDeviceToHost));
+        if (dbg->status) *dbg->status = ln.h_status[0];
+    }
+    if (out_dev) for (uint32_t v = 0; v < nv; v++) out_dev[v] = ln.d_color + B.plan[v].color_off;
+    if (ln.h_status[0] & 1u) return set_err(ctx, SFTG_E_DEVICE_STATUS, "occlusion traversal exceeded its stack bound");
+    return SFTG_OK;
+}
+
+/* Renders a batch of views on lane 0 and waits for it.  host_color[v] (optional) receives view
+ * v's colour with pitch pitch_bytes[v]; out_dev[v] (optional) its device colour buffer, valid
+ * until the next synchronous call. */
 static int batch_common(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t nv, uint32_t* const* host_color, const int32_t* pitch_bytes,
                         sftg_debug_out* dbg, const uint32_t** out_dev) {
     if (!ctx || !fds) return SFTG_E_ARG;
     CK(cudaSetDevice(ctx->device));
     int rc = sync_tables(ctx);
     if (rc) return rc;
-    auto pitch_of = [&](uint32_t v) { return (pitch_bytes && pitch_bytes[v] > 0) ? (size_t)pitch_bytes[v] : (size_t)fds[v].width * 4; };
+    sftg_lane& ln = ctx->lanes[0];
     for (int attempt = 0; attempt < 4; attempt++) {
         batch_bufs B;
-        if ((rc = build_batch(ctx, fds, nv, dbg != nullptr, B))) return rc;
-        for (uint32_t v = 0; v < nv; v++)   /* the reference blends over / keeps the caller's pixels */
-            if (!fds[v].clear && host_color && host_color[v])
-                CK(cudaMemcpy2DAsync(ctx->d_color + B.plan[v].color_off, (size_t)fds[v].width * 4, host_color[v], pitch_of(v),
-                                     (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyHostToDevice, ctx->stream));
-        if ((rc = (dbg || !ctx->use_graphs) ? launch_batch(ctx, B) : launch_batch_graph(ctx, B))) return rc;
-        CK(cudaMemcpyAsync(ctx->h_status, B.status, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaMemcpyAsync(ctx->h_status + 2, B.totals, 8, cudaMemcpyDeviceToHost, ctx->stream));
-        for (uint32_t v = 0; v < nv; v++)
-            if (host_color && host_color[v])
-                CK(cudaMemcpy2DAsync(host_color[v], pitch_of(v), ctx->d_color + B.plan[v].color_off, (size_t)fds[v].width * 4,
-                                     (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
-        const uint32_t clip_total = ctx->h_status[2], pay_total = ctx->h_status[3];
-        if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap) {   /* capacity exceeded: grow and redo the batch */
-            while (ctx->clip_cap < clip_total) ctx->clip_cap *= 2;
-            while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
-            continue;
-        }
-        for (int k = 0; k < 5; k++) {   /* geometry is timed from its own start: occlusion runs beside it */
-            float t = 0.f;
-            if (cudaEventElapsedTime(&t, k == 1 ? ctx->ev_geo : ctx->ev[k], ctx->ev[k + 1]) != cudaSuccess) { t = 0.f; cudaGetLastError(); }
-            ctx->timings[k] = t;
-        }
-        if (dbg) {
-            const sftg_frame_desc* fd = &fds[0];
-            const int W = fd->width, H = fd->height, S = fd->samples, tiles = (int)B.total_tiles;
-            if (dbg->vis_depth) CK(cudaMemcpy(dbg->vis_depth, B.vis_depth, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
-            if (dbg->vis_id) CK(cudaMemcpy(dbg->vis_id, B.vis_id, (size_t)tiles * S * 4096 * 4, cudaMemcpyDeviceToHost));
-            if (dbg->tile_counts) CK(cudaMemcpy(dbg->tile_counts, B.tile_count, (size_t)tiles * 4, cudaMemcpyDeviceToHost));
-            if (dbg->tile_payload_total) *dbg->tile_payload_total = pay_total;
-            if (dbg->tile_payloads && pay_total <= dbg->tile_payload_cap) CK(cudaMemcpy(dbg->tile_payloads, B.tile_pay, (size_t)pay_total * 8, cudaMemcpyDeviceToHost));
-            if (dbg->ss_cache) CK(cudaMemcpy(dbg->ss_cache, B.ss, (size_t)B.total_ss * 2304, cudaMemcpyDeviceToHost));
-            if (dbg->light_vis && fd->n_proxies) CK(cudaMemcpy(dbg->light_vis, B.light_vis, (size_t)fd->n_proxies * 64, cudaMemcpyDeviceToHost));
-            if (dbg->clip_total) *dbg->clip_total = clip_total;
-            if (dbg->clip_tris && clip_total <= dbg->clip_cap) CK(cudaMemcpy(dbg->clip_tris, B.clips, (size_t)clip_total * sizeof(sftg_clip_tri), cudaMemcpyDeviceToHost));
-            if (dbg->shadow && S == 1) CK(cudaMemcpy(dbg->shadow, B.shadow, (size_t)W * H * 16 * 4, cudaMemcpyDeviceToHost));
-            if (dbg->status) *dbg->status = ctx->h_status[0];
-        }
-        if (out_dev) for (uint32_t v = 0; v < nv; v++) out_dev[v] = ctx->d_color + B.plan[v].color_off;
-        if (ctx->h_status[0] & 1u) return set_err(ctx, SFTG_E_DEVICE_STATUS, "occlusion traversal exceeded its stack bound");
-        return SFTG_OK;
+        bool defer = false;
+        if ((rc = submit_batch(ctx, ln, fds, nv, host_color, pitch_bytes, dbg, B, defer))) return rc;
+        rc = finish_batch(ctx, ln, fds, nv, host_color, pitch_bytes, B, defer, dbg, out_dev);
+        if (rc != BATCH_REDO) return rc;
     }
     return set_err(ctx, SFTG_E_NOMEM, "frame capacities did not converge");
 }
@@ -800,6 +891,74 @@ extern "C" int sftg_frame_render_device(sftg_ctx* ctx, const sftg_frame_desc* fd
 extern "C" int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, uint32_t* const* colors,
                                   const int32_t* pitch_bytes, const uint32_t** out_device_colors) {
     return batch_common(ctx, fds, n_views, colors, pitch_bytes, nullptr, out_device_colors);
+}
+
+/* ------------------------------------------------------------------ overlapping batches */
+extern "C" int sftg_frames_submit(sftg_ctx* ctx, uint32_t lane, const sftg_frame_desc* fds, uint32_t n_views, uint32_t* const* colors,
+                                  const int32_t* pitch_bytes) {
+    if (!ctx || !fds || !n_views) return SFTG_E_ARG;
+    if (lane == 0 || lane >= SFTG_MAX_LANES) return set_err(ctx, SFTG_E_ARG, "lane %u: lanes 1 to %d take submissions", lane, SFTG_MAX_LANES - 1);
+    sftg_lane& ln = ctx->lanes[lane];
+    if (ln.busy) return set_err(ctx, SFTG_E_ARG, "lane %u has a batch in flight", lane);
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_tables(ctx);
+    if (rc) return rc;
+    ln.fds = fds; ln.nv = n_views;
+    ln.colors.assign(n_views, nullptr);
+    ln.pitch.assign(n_views, 0);
+    for (uint32_t v = 0; v < n_views; v++) {
+        if (colors) ln.colors[v] = colors[v];
+        if (pitch_bytes) ln.pitch[v] = pitch_bytes[v];
+    }
+    batch_bufs B;
+    bool defer = false;
+    if ((rc = submit_batch(ctx, ln, fds, n_views, ln.colors.data(), ln.pitch.data(), nullptr, B, defer))) return rc;
+    ln.busy = true;
+    if (defer) {   /* a view keeps the caller's pixels: finish now, so that a re-render can start from them */
+        ln.busy = false;
+        rc = finish_batch(ctx, ln, fds, n_views, ln.colors.data(), ln.pitch.data(), B, true, nullptr, nullptr);
+        for (int attempt = 0; rc == BATCH_REDO && attempt < 4; attempt++) {
+            batch_bufs B2;
+            if ((rc = submit_batch(ctx, ln, fds, n_views, ln.colors.data(), ln.pitch.data(), nullptr, B2, defer))) return rc;
+            rc = finish_batch(ctx, ln, fds, n_views, ln.colors.data(), ln.pitch.data(), B2, defer, nullptr, nullptr);
+        }
+        if (rc == BATCH_REDO) return set_err(ctx, SFTG_E_NOMEM, "frame capacities did not converge");
+        ln.busy = rc == SFTG_OK;   /* sftg_lane_wait then returns at once */
+        ln.fds = nullptr;
+        return rc;
+    }
+    return SFTG_OK;
+}
+
+extern "C" int sftg_lane_done(sftg_ctx* ctx, uint32_t lane) {
+    if (!ctx || lane >= SFTG_MAX_LANES) return SFTG_E_ARG;
+    sftg_lane& ln = ctx->lanes[lane];
+    if (!ln.busy || !ln.fds) return 1;
+    const cudaError_t e = cudaEventQuery(ln.ev_done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return set_err(ctx, SFTG_E_CUDA, "lane %u: %s", lane, cudaGetErrorString(e));
+}
+
+extern "C" int sftg_lane_wait(sftg_ctx* ctx, uint32_t lane) {
+    if (!ctx || lane == 0 || lane >= SFTG_MAX_LANES) return SFTG_E_ARG;
+    sftg_lane& ln = ctx->lanes[lane];
+    if (!ln.busy) return SFTG_OK;
+    ln.busy = false;
+    if (!ln.fds) return SFTG_OK;   /* finished inside sftg_frames_submit */
+    CK(cudaSetDevice(ctx->device));
+    const sftg_frame_desc* fds = ln.fds;
+    ln.fds = nullptr;
+    batch_bufs none;
+    int rc = finish_batch(ctx, ln, fds, ln.nv, ln.colors.data(), ln.pitch.data(), none, false, nullptr, nullptr);
+    for (int attempt = 0; rc == BATCH_REDO && attempt < 4; attempt++) {
+        batch_bufs B;
+        bool defer = false;
+        if ((rc = submit_batch(ctx, ln, fds, ln.nv, ln.colors.data(), ln.pitch.data(), nullptr, B, defer))) return rc;
+        rc = finish_batch(ctx, ln, fds, ln.nv, ln.colors.data(), ln.pitch.data(), B, defer, nullptr, nullptr);
+    }
+    if (rc == BATCH_REDO) return set_err(ctx, SFTG_E_NOMEM, "frame capacities did not converge");
+    return rc;
 }
 
 /* ------------------------------------------------------------------ skeletal poses */
@@ -1055,6 +1214,7 @@ extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {
 }
 
 extern "C" int sftg_last_launch_count(const sftg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+extern "C" uint64_t sftg_launch_total(const sftg_ctx* ctx) { return ctx ? ctx->launch_total : 0; }
 
 extern "C" void* sftg_stream(const sftg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 

@@ -379,6 +379,7 @@ k_bin(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_v
         const uint32_t s = F->ss_base + base + tid;
         bool hit = false;
         if (base + tid < n_ss) { const int4 q = mrect[s]; hit = rect_has(q.x, q.y, q.z, q.w, tx, ty); }
+        if (!__syncthreads_or(hit)) continue;   /* no meshlet of this chunk touches the tile */
         /* ordered compaction of hit meshlets */
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
         if (lane == 0) s_wsum[warp] = __popc(bal);
@@ -395,22 +396,32 @@ k_bin(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_v
             if (lane == 0) s_cnt[h] = c;
         }
         __syncthreads();
-        if (out) {
-            /* exclusive scan of the hit counts (nh <= 256), then ordered writes */
-            if (tid == 0) {
-                uint32_t acc = 0;
-                for (uint32_t h = 0; h < nh; h++) { const uint32_t c = s_cnt[h]; s_cnt[h] = acc; acc += c; }
-                s_wsum[0] = acc;
+        if (warp == 0) {   /* exclusive scan of the hit counts (nh <= 256, 8 per lane); total in s_wsum[0] */
+            uint32_t v[BIN_THREADS / 32], local = 0;
+#pragma unroll
+            for (int k = 0; k < BIN_THREADS / 32; k++) {
+                const uint32_t h = (uint32_t)lane * (BIN_THREADS / 32) + k;
+                v[k] = h < nh ? s_cnt[h] : 0u;
+                local += v[k];
             }
-            __syncthreads();
+            uint32_t incl = local;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) { const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o); if (lane >= o) incl += t; }
+            uint32_t acc = incl - local;
+#pragma unroll
+            for (int k = 0; k < BIN_THREADS / 32; k++) {
+                const uint32_t h = (uint32_t)lane * (BIN_THREADS / 32) + k;
+                if (h < nh) s_cnt[h] = acc;
+                acc += v[k];
+            }
+            if (lane == 31) s_wsum[0] = incl;
+        }
+        __syncthreads();
+        if (out) {   /* ordered writes */
             for (uint32_t h = warp; h < nh; h += BIN_THREADS / 32)
                 bin_meshlet(recs, clip_cnt, clip_base, clip_rect, F->clip_cap, vclip, s_hits[h], tx, ty, lane, out + running + s_cnt[h]);
-            running += s_wsum[0];
-        } else {
-            if (tid == 0) { uint32_t acc = 0; for (uint32_t h = 0; h < nh; h++) acc += s_cnt[h]; s_wsum[0] = acc; }
-            __syncthreads();
-            running += s_wsum[0];
         }
+        running += s_wsum[0];
         __syncthreads();
     }
     if (!out && tid == 0) tile_count[gtile] = running;

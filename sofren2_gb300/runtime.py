@@ -56,6 +56,9 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftg_last_error": (C.c_char_p, [p]), "sftx_scene_model": (p, [p, u32]),
         "sft_raycast_batch": (v, [p, p, p, p, u32, p]), "sftg_raycast": (i32, [p, p, u32, p]),
         "sftg_raycast_device": (i32, [p, p, u32, p]),
+        "sft_batch_begin": (v, []), "sft_batch_submit": (i32, []), "sft_batch_submit_async": (i32, [u32]),
+        "sft_batch_done": (i32, [u32]), "sft_batch_wait": (i32, [u32]),
+        "sftx_scene_render_lanes": (i32, [p, p, p, u32, p, p, u32]), "sftg_launch_total": (u64, [p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -113,7 +116,8 @@ class SftxRequest(C.Structure):
 
 
 class SftxServeStats(C.Structure):
-    _fields_ = [("batches", C.c_uint64), ("max_batch", C.c_uint64), ("peak_bytes", C.c_uint64), ("errors", C.c_uint64)]
+    _fields_ = [("batches", C.c_uint64), ("max_batch", C.c_uint64), ("peak_bytes", C.c_uint64), ("errors", C.c_uint64),
+                ("max_inflight", C.c_uint64)]
 
 
 def request_device_bytes(width: int, height: int, samples: int, meshlets: int) -> int:
@@ -181,6 +185,10 @@ class Renderer:
     def stream(self) -> int:
         return self.lib.sft_get_cuda_stream() or 0
 
+    def launch_total(self) -> int:
+        """Kernels launched by every batch finished so far, on all submission lanes."""
+        return int(self.lib.sftg_launch_total(self.lib.sft_get_gpu_context()))
+
     def launch_count(self) -> int:
         return int(self.lib.sft_get_launch_count())
 
@@ -199,8 +207,10 @@ class Renderer:
             raise RuntimeError("render failed: " + (err or b"").decode())
         return color
 
-    def render_batch(self, views: list[tuple], colors: list[np.ndarray | None] | None = None) -> list[np.ndarray | None]:
-        """Renders views [(scene handle, frame, samples), ...] in one batched submission.
+    def render_batch(self, views: list[tuple], colors: list[np.ndarray | None] | None = None,
+                     lanes: int = 0) -> list[np.ndarray | None]:
+        """Renders views [(scene handle, frame, samples), ...] in one batched submission, or with
+        lanes >= 1 as that many batches overlapping on submission lanes 1..lanes.
 
         colors: None (every colour stays on the device) or one array (or None) per view; a
         missing array is allocated.  Returns the per-view colour arrays (None for device-only)."""
@@ -223,7 +233,10 @@ class Renderer:
                 ptrs[i] = c.ctypes.data
                 pitch[i] = c.strides[0]
             cp = ptrs
-        rc = self.lib.sftx_scene_render_batch(hs, _ptr(fr), _ptr(sm), n, cp, _ptr(pitch))
+        if lanes:
+            rc = self.lib.sftx_scene_render_lanes(hs, _ptr(fr), _ptr(sm), n, cp, _ptr(pitch), lanes)
+        else:
+            rc = self.lib.sftx_scene_render_batch(hs, _ptr(fr), _ptr(sm), n, cp, _ptr(pitch))
         self.lib.sft_set_msaa_samples(self.samples)
         if rc != 0:
             raise RuntimeError("batch render failed: " + (self.lib.sft_get_last_error() or b"").decode())
@@ -253,12 +266,18 @@ class Renderer:
         if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
             raise ValueError("tuning out of range")
 
-    def serve(self, handles: list, requests: list[tuple], max_batch: int, budget_bytes: int, plain: bool,
+    SERVE_MODES = {"batched": 0, "plain": 1, "overlap": 2}
+
+    def serve(self, handles: list, requests: list[tuple], max_batch: int, budget_bytes: int, mode,
               colors: list[np.ndarray]) -> tuple[np.ndarray, np.ndarray, dict]:
         """Runs the native serving loop (sftx_serve) over requests
         [(arrival_s, scene index, frame, samples, max point lights, device bytes)], sorted by
-        arrival.  colors is the ring of host colour buffers (at least max_batch, each as large as
-        the largest request).  Returns (completion times in s, batch index per request, stats)."""
+        arrival, in mode "overlap" (continuous batching over submission lanes), "batched" (one
+        batch at a time) or "plain" (one request at a time; True and False select "plain" and
+        "batched").  colors is the ring of host colour buffers (at least max_batch, each as large
+        as the largest request).  Returns (completion times in s, batch index per request, stats)."""
+        if isinstance(mode, bool):
+            mode = "plain" if mode else "batched"
         n = len(requests)
         reqs = (SftxRequest * max(1, n))()
         for k, (t, si, f, S, nl, nb) in enumerate(requests):
@@ -268,12 +287,12 @@ class Renderer:
         done = np.zeros(max(1, n), np.uint64)
         batch = np.zeros(max(1, n), np.uint32)
         st = SftxServeStats()
-        rc = self.lib.sftx_serve(hs, reqs, n, max_batch, budget_bytes, 1 if plain else 0, cp, len(colors), _ptr(done),
+        rc = self.lib.sftx_serve(hs, reqs, n, max_batch, budget_bytes, self.SERVE_MODES[mode], cp, len(colors), _ptr(done),
                                  _ptr(batch), C.byref(st))
         self.lib.sft_set_msaa_samples(self.samples)
         if rc != 0:
             raise RuntimeError(f"serving loop failed ({rc}): " + (self.lib.sft_get_last_error() or b"").decode())
-        stats = {"batches": st.batches, "max_batch": st.max_batch, "peak_bytes": st.peak_bytes}
+        stats = {"batches": st.batches, "max_batch": st.max_batch, "peak_bytes": st.peak_bytes, "max_inflight": st.max_inflight}
         return done[:n].astype(np.float64) * 1e-9, batch[:n].copy(), stats
 
     def skeleton_upload(self, rig: dict) -> int:

@@ -130,3 +130,16 @@ def test_autotune_keeps_results(renderer, golden, handles):
             renderer.free_scene(h)
     finally:
         renderer.set_tuning(**saved)
+
+
+@pytest.mark.parametrize("lanes", [2, 3, 7])
+def test_batch_split_over_lanes_equals_single_views(renderer, handles, lanes):
+    """The mixed views as `lanes` batches overlapping on submission lanes give every view its
+    lone pixels, twice in a row (the second time replaying each lane's captured graph)."""
+    views = [(handles[n], 0, S) for S in (4, 1, 2) for n in MIXED]
+    inits = [_initial(renderer, h, f, 300 + i) for i, (h, f, _) in enumerate(views)]
+    alone = _alone(renderer, views, inits)
+    for _ in range(2):
+        got = renderer.render_batch(views, [i.copy() for i in inits], lanes=lanes)
+        for k, (a, b) in enumerate(zip(alone, got)):
+            assert np.array_equal(a, b), f"view {k} differs when the batch is split over {lanes} lanes"

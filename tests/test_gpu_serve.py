@@ -1,6 +1,8 @@
-"""Served rendering (sftx_serve, the native continuous-batching loop): every request's pixels
-are the ones a lone render of it produces, whether it was served in a batch, alone (plain) or
-under a memory budget that forces one request per batch."""
+"""Served rendering (sftx_serve, the native serving loop): every request's pixels are the ones a
+lone render of it produces, whether it was served with batches overlapping on the GPU (overlap,
+continuous batching over submission lanes), one batch at a time, alone (plain) or under a memory
+budget that forces one request per batch; and batches queued on different submission lanes
+(sft_batch_submit_async) without waiting in between give every view its lone pixels."""
 import numpy as np
 import pytest
 
@@ -46,23 +48,65 @@ def _check(colors, sizes, alone):
         assert np.array_equal(got, a), f"request {k} differs from its lone render"
 
 
-@pytest.mark.parametrize("plain", [False, True])
-def test_served_equals_alone(renderer, served, plain):
+@pytest.mark.parametrize("mode", ["overlap", "batched", "plain"])
+def test_served_equals_alone(renderer, served, mode):
     hs, reqs, sizes, alone = served
     colors = _ring(sizes, len(reqs))
-    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=1 << 40, plain=plain, colors=colors)
+    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=1 << 40, mode=mode, colors=colors)
     _check(colors, sizes, alone)
     assert np.all(done >= np.array([r[0] for r in reqs]))
-    if plain:
+    if mode == "plain":
         assert st["max_batch"] == 1 and st["batches"] == len(reqs)
     else:
         assert 1 < st["max_batch"] <= 8 and st["batches"] < len(reqs)
+    if mode == "overlap":
+        assert 1 <= st["max_inflight"] <= 7
+
+
+def test_overlap_with_a_small_colour_ring(renderer, served):
+    """8 colour buffers for 24 requests: a ring slot is handed out again only after its request
+    has finished, so the last 8 requests' slots hold their lone pixels."""
+    hs, reqs, sizes, alone = served
+    colors = _ring(sizes, 8)
+    done, batch, st = renderer.serve(hs, reqs, max_batch=4, budget_bytes=1 << 40, mode="overlap", colors=colors)
+    n = len(reqs)
+    for k in range(n - 8, n):
+        w, h = sizes[k]
+        assert np.array_equal(colors[k % 8][: w * h].reshape(h, w), alone[k]), f"request {k} differs from its lone render"
+
+
+def test_batches_on_lanes_overlap(renderer, served):
+    hs, reqs, sizes, alone = served
+    lib = renderer.lib
+    colors = _ring(sizes, len(reqs))
+    groups = [list(range(0, 8)), list(range(8, 14)), list(range(14, 24))]
+    for lane, g in zip((1, 2, 3), groups):   # three batches queued before any is waited for
+        lib.sft_batch_begin()
+        for k in g:
+            _, si, f, S, nl, _ = reqs[k]
+            renderer.set_samples(S)
+            assert lib.sftx_scene_render_ex(hs[si], f, colors[k].ctypes.data, 0, nl) == 0
+        assert lib.sft_batch_submit_async(lane) == 0
+    renderer.set_samples(1)
+    for lane in (3, 1, 2):
+        assert lib.sft_batch_wait(lane) == 0
+        assert lib.sft_batch_done(lane) == 1
+    _check(colors, sizes, alone)
 
 
 def test_memory_budget_limits_batches(renderer, served):
     hs, reqs, sizes, alone = served
     colors = _ring(sizes, len(reqs))
     budget = min(r[5] for r in reqs)   # any two requests exceed it: one request per batch
-    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=budget, plain=False, colors=colors)
+    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=budget, mode="batched", colors=colors)
     _check(colors, sizes, alone)
     assert st["max_batch"] == 1
+
+
+def test_memory_budget_limits_overlapping_batches(renderer, served):
+    hs, reqs, sizes, alone = served
+    colors = _ring(sizes, len(reqs))
+    budget = min(r[5] for r in reqs)   # one request in flight at a time over all lanes
+    done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=budget, mode="overlap", colors=colors)
+    _check(colors, sizes, alone)
+    assert st["max_batch"] == 1 and st["max_inflight"] == 1
