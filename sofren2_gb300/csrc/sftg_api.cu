@@ -44,7 +44,9 @@ struct dpool {   /* growable device buffer */
 struct sftg_lane {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;            /* proxy occlusion runs here, beside geometry, binning and raster */
+    cudaStream_t stream3 = nullptr;            /* the 1x and 2x tile ranges of raster and resolve, beside the 4x range */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_geo = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_split[2] = { nullptr, nullptr }, ev_merge[2] = { nullptr, nullptr };
     cudaEvent_t ev[6] = { nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
     void* arena = nullptr;
     size_t arena_cap = 0;
@@ -84,10 +86,15 @@ struct sftg_ctx {
     std::vector<std::vector<uint8_t>> h_mesh_skinned;  /* per model, per mesh */
     std::vector<std::vector<uint32_t>> h_mesh_first;   /* per model, per mesh: first meshlet */
     std::vector<std::vector<uint32_t>> h_mesh_count;
+    /* per model: its geometry jobs for one instance (inst and view 0, skinned = the mesh has
+     * skin), built for job width tmpl_jw and the model's pool base; rebuilt when either changes */
+    struct job_tmpl { uint32_t jw = 0, meshlet_base = ~0u, total = ~0u; std::vector<sftg_job> jobs; };
+    std::vector<job_tmpl> h_job_tmpl;
+    std::vector<sftg_job> tmp_jobs;
     uint32_t n_meshlets = 0, n_skin = 0, n_blas = 0;
     bool tables_dirty = true;
     /* per frame: capacities shared by the lanes (they only grow), the last finished batch's figures */
-    uint64_t tile_cap = 1u << 20, clip_cap = 1u << 16;
+    uint64_t tile_cap = 1u << 20, clip_cap = 1u << 16, stile_cap = 1u << 18;
     float timings[5] = { 0, 0, 0, 0, 0 };
     int launches = 0;
     uint64_t launch_total = 0;                 /* kernels of every finished batch, on all lanes */
@@ -162,7 +169,12 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     for (int l = 0; l < SFTG_MAX_LANES; l++) {
         sftg_lane& ln = ctx->lanes[l];
         if (cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&ln.stream2, cudaStreamNonBlocking) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
+            cudaStreamCreateWithFlags(&ln.stream2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&ln.stream3, cudaStreamNonBlocking) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
+        for (int k = 0; k < 2; k++) {
+            cudaEventCreateWithFlags(&ln.ev_split[k], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&ln.ev_merge[k], cudaEventDisableTiming);
+        }
         for (int i = 0; i < 6; i++) cudaEventCreate(&ln.ev[i]);
         cudaEventCreateWithFlags(&ln.ev_fork, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&ln.ev_join, cudaEventDisableTiming);
@@ -199,6 +211,11 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
         if (ln.ev_done) cudaEventDestroy(ln.ev_done);
         if (ln.ev_geo) cudaEventDestroy(ln.ev_geo);
         if (ln.stream2) cudaStreamDestroy(ln.stream2);
+        if (ln.stream3) cudaStreamDestroy(ln.stream3);
+        for (int k = 0; k < 2; k++) {
+            if (ln.ev_split[k]) cudaEventDestroy(ln.ev_split[k]);
+            if (ln.ev_merge[k]) cudaEventDestroy(ln.ev_merge[k]);
+        }
         if (ln.stream) cudaStreamDestroy(ln.stream);
     }
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
@@ -316,6 +333,7 @@ static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_mo
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->n_meshlets += total; ctx->n_skin += nskin; ctx->n_blas += d->blas_count;
     ctx->h_models.push_back(md);
+    if (ctx->h_job_tmpl.size() >= ctx->h_models.size()) ctx->h_job_tmpl[ctx->h_models.size() - 1].jw = 0;   /* id reused */
     ctx->h_mesh_skinned.push_back(mesh_sk);
     ctx->h_mesh_first.push_back(mesh_first);
     ctx->h_mesh_count.push_back(mesh_cnt);
@@ -375,7 +393,7 @@ struct bump {
 
 /* Placement of one view inside a batch: where its rows start in the batch-wide arrays. */
 struct view_plan {
-    uint32_t ss_base, total_ss, tile_base, tiles, prox_base, packet_base, n_packets;
+    uint32_t ss_base, total_ss, tile_base, tiles, prox_base, packet_base, n_packets, stile_base, stiles, scols;
     uint32_t inst_off, bone_off, pl_off, dl_off, tl_off;
     uint64_t vis_base, color_off;
 };
@@ -383,7 +401,8 @@ struct view_plan {
 struct batch_bufs {
     sftg_frame* frames;  /* device copies of the views' frame blocks */
     const sftg_job* jobs;
-    const uint16_t* tile_view; const uint16_t* packet_view; const uint16_t* prox_view;
+    const uint16_t* tile_view; const uint16_t* packet_view; const uint16_t* prox_view; const uint16_t* stile_view;
+    uint32_t* stile_count; uint32_t* stile_start; uint32_t* stile_list;   /* super-tile meshlet lists */
     float* ss;
     sftg_batch_rec* recs;
     uint32_t* clip_cnt; uint32_t* clip_base;
@@ -398,10 +417,10 @@ struct batch_bufs {
     void* packets; uint2* pairs; uint32_t* n_pairs; uint32_t max_pairs;
     uint32_t* scan_tmp;
     uint32_t* status;
-    uint32_t* totals;    /* [0] clip total, [1] tile payload total */
+    uint32_t* totals;    /* [0] clip total, [1] tile payload total, [2] super-tile list total */
     float* vis_depth; uint32_t* vis_id; float* shadow;
     float2* vis; float2* zrange;
-    uint32_t n_views, total_ss, n_jobs, total_tiles, total_prox, total_packets, max_inst;
+    uint32_t n_views, total_ss, n_jobs, total_tiles, total_prox, total_packets, max_inst, total_stiles;
     uint32_t s_tile0[3], s_tiles[3];   /* batch-wide tile range of the views with 1, 2 and 4 samples */
     uint64_t color_total;              /* pixels over all views */
     std::vector<view_plan> plan;
@@ -429,7 +448,8 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     B.plan.assign(nv, view_plan{});
     B.n_views = nv;
     std::vector<sftg_inst> inst;
-    std::vector<sftg_job> jobs;
+    std::vector<sftg_job>& jobs = ctx->tmp_jobs;   /* capacity kept between batches */
+    jobs.clear();
     std::vector<float> bones;
     uint32_t total_ss = 0, total_prox = 0, total_packets = 0, max_inst = 0, n_pl = 0, n_dl = 0, n_tl = 0;
     uint64_t max_pairs = 0, color_total = 0;
@@ -457,18 +477,33 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
                 I.bones = (int32_t)((bones.size() - P.bone_off) / 16);
                 bones.insert(bones.end(), id.bones, id.bones + (size_t)id.bone_count * 16);
             }
-            for (uint32_t k = 0; k < md.mesh_count; k++) {
-                const uint32_t first = ctx->h_mesh_first[id.model][k], cnt = ctx->h_mesh_count[id.model][k];
-                const uint32_t sk = ctx->h_mesh_skinned[id.model][k] && I.bones >= 0;
-                const uint32_t jw = (uint32_t)ctx->tuning.geom_job_width;
-                for (uint32_t s = 0; s < cnt; s += 8) {   /* the reference's groups of 8, cut into jobs of jw */
-                    const uint32_t gc = (cnt - s) < 8 ? (cnt - s) : 8;
-                    for (uint32_t k = 0; k < gc; k += jw) {
-                        sftg_job j; j.inst = i; j.first = first + s + k; j.count = (uint16_t)((gc - k) < jw ? (gc - k) : jw);
-                        j.skinned = (uint16_t)sk; j.view = v; j.group_first = first + s;
-                        jobs.push_back(j);
+            const uint32_t jw = (uint32_t)ctx->tuning.geom_job_width;
+            if (ctx->h_job_tmpl.size() <= (size_t)id.model) ctx->h_job_tmpl.resize((size_t)id.model + 1);
+            sftg_ctx::job_tmpl& T = ctx->h_job_tmpl[id.model];
+            if (T.jw != jw || T.meshlet_base != md.meshlet_base || T.total != md.total_meshlets) {
+                T.jobs.clear();
+                for (uint32_t k = 0; k < md.mesh_count; k++) {
+                    const uint32_t first = ctx->h_mesh_first[id.model][k], cnt = ctx->h_mesh_count[id.model][k];
+                    const uint32_t sk = ctx->h_mesh_skinned[id.model][k];
+                    for (uint32_t s = 0; s < cnt; s += 8) {   /* the reference's groups of 8, cut into jobs of jw */
+                        const uint32_t gc = (cnt - s) < 8 ? (cnt - s) : 8;
+                        for (uint32_t q = 0; q < gc; q += jw) {
+                            sftg_job j; j.inst = 0; j.first = first + s + q; j.count = (uint16_t)((gc - q) < jw ? (gc - q) : jw);
+                            j.skinned = (uint16_t)sk; j.view = 0; j.group_first = first + s;
+                            T.jobs.push_back(j);
+                        }
                     }
                 }
+                T.jw = jw; T.meshlet_base = md.meshlet_base; T.total = md.total_meshlets;
+            }
+            const size_t j0 = jobs.size();
+            jobs.resize(j0 + T.jobs.size());
+            sftg_job* jd = jobs.data() + j0;
+            const uint16_t has_bones = I.bones >= 0 ? 1 : 0;
+            for (size_t q = 0; q < T.jobs.size(); q++) {
+                sftg_job j = T.jobs[q];
+                j.inst = i; j.view = v; j.skinned = (uint16_t)(j.skinned & has_bones);
+                jd[q] = j;
             }
             lss += md.total_meshlets;
             inst.push_back(I);
@@ -499,6 +534,17 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
         }
         B.s_tiles[si] = total_tiles - B.s_tile0[si];
     }
+    uint32_t total_stiles = 0;
+    for (uint32_t v = 0; v < nv; v++) {
+        view_plan& P = B.plan[v];
+        const uint32_t cols = (uint32_t)((fds[v].width + 63) / 64), rows = (uint32_t)((fds[v].height + 63) / 64);
+        /* coarse lists pay off once a tile would scan more than four chunks of meshlet slots */
+        const bool coarse = P.total_ss > 4u * 256u;
+        P.scols = coarse ? (cols + SFTG_STILE - 1) / SFTG_STILE : 0u;
+        P.stiles = P.scols * ((rows + SFTG_STILE - 1) / SFTG_STILE);
+        P.stile_base = total_stiles; total_stiles += P.stiles;
+    }
+    B.total_stiles = total_stiles;
     B.total_ss = total_ss; B.n_jobs = (uint32_t)jobs.size(); B.total_tiles = total_tiles; B.total_prox = total_prox;
     B.total_packets = total_packets; B.max_inst = max_inst; B.max_pairs = (uint32_t)max_pairs; B.color_total = color_total;
     const size_t n_rec = (size_t)total_ss * 16;
@@ -516,6 +562,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     const size_t o_tv = stage_take((size_t)total_tiles * 2 + 16);
     const size_t o_pv = stage_take((size_t)total_packets * 2 + 16);
     const size_t o_xv = stage_take((size_t)total_prox * 2 + 16);
+    const size_t o_sv = stage_take((size_t)total_stiles * 2 + 16);
     const size_t stage_bytes = so;
     /* device arena layout */
     size_t need = stage_bytes + 4096;
@@ -524,8 +571,9 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
     acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(1024); acc(total_tiles + 16);
     acc(ctx->tile_cap * 8);
+    acc((size_t)total_stiles * 4); acc((size_t)total_stiles * 4); acc(ctx->stile_cap * 4);
     acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
-    acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
+    acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles + total_stiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
     acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
     const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
     if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
@@ -564,11 +612,14 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     B.any_overlay = false;
     for (uint32_t v = 0; v < nv; v++) if (fds[v].debug_mode >= 2 && fds[v].debug_mode <= 4) B.any_overlay = true;
     B.tile_pay = bp.take<uint64_t>(ctx->tile_cap);
+    B.stile_count = bp.take<uint32_t>(total_stiles);
+    B.stile_start = bp.take<uint32_t>(total_stiles);
+    B.stile_list = bp.take<uint32_t>(ctx->stile_cap);
     B.light_vis = bp.take<uint8_t>((size_t)total_prox * 64 + 64);
     B.packets = bp.take<char>((size_t)total_packets * sftg_packet_bytes() + 64);
     B.pairs = bp.take<uint2>((size_t)max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1);   /* pairs, then BLAS sub-walk items */
     B.n_pairs = bp.take<uint32_t>(16);
-    B.scan_tmp = bp.take<uint32_t>((n_rec + total_tiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
+    B.scan_tmp = bp.take<uint32_t>((n_rec + total_tiles + total_stiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16);
     B.status = bp.take<uint32_t>(16);
     B.totals = bp.take<uint32_t>(16);
     B.vis = bp.take<float2>(vis_total);
@@ -583,6 +634,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     uint16_t* tv = (uint16_t*)(hs + o_tv);
     uint16_t* pv = (uint16_t*)(hs + o_pv);
     uint16_t* xv = (uint16_t*)(hs + o_xv);
+    uint16_t* sv = (uint16_t*)(hs + o_sv);
     for (uint32_t v = 0; v < nv; v++) {
         const sftg_frame_desc* fd = &fds[v];
         const view_plan& P = B.plan[v];
@@ -604,7 +656,8 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
         F->lightmap_brightness = fd->lightmap_brightness;
         F->n_point = fd->n_point; F->n_dir = fd->n_dir; F->n_proxies = fd->n_proxies; F->n_inst = fd->n_instances;
         F->total_ss = P.total_ss; F->n_jobs = B.n_jobs; F->tlas_root = fd->tlas_root; F->tlas_count = fd->tlas_count;
-        F->clip_cap = (uint32_t)ctx->clip_cap; F->tile_cap = (uint32_t)ctx->tile_cap;
+        F->clip_cap = (uint32_t)ctx->clip_cap; F->tile_cap = (uint32_t)ctx->tile_cap; F->stile_cap = (uint32_t)ctx->stile_cap;
+        F->stile_base = P.stile_base; F->scols = P.scols;
         F->view = v; F->ss_base = P.ss_base; F->tile_base = P.tile_base; F->prox_base = P.prox_base;
         F->packet_base = P.packet_base; F->n_packets = P.n_packets; F->vis_base = P.vis_base;
         F->color_dev = ln.d_color + P.color_off;
@@ -633,6 +686,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
         for (uint32_t t = 0; t < P.tiles; t++) tv[P.tile_base + t] = (uint16_t)v;
         for (uint32_t k = 0; k < P.n_packets; k++) pv[P.packet_base + k] = (uint16_t)v;
         for (uint32_t p = 0; p < fd->n_proxies; p++) xv[P.prox_base + p] = (uint16_t)v;
+        for (uint32_t t = 0; t < P.stiles; t++) sv[P.stile_base + t] = (uint16_t)v;
     }
     memcpy(hs + o_inst, inst.data(), inst.size() * sizeof(sftg_inst));
     if (!bones.empty()) memcpy(hs + o_bones, bones.data(), bones.size() * 4);
@@ -642,6 +696,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     B.tile_view = (const uint16_t*)(ds + o_tv);
     B.packet_view = (const uint16_t*)(ds + o_pv);
     B.prox_view = (const uint16_t*)(ds + o_xv);
+    B.stile_view = (const uint16_t*)(ds + o_sv);
     CK(cudaMemcpyAsync(ds, hs, stage_bytes, cudaMemcpyHostToDevice, ln.stream));
     return 0;
 }
@@ -697,9 +752,19 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
         CK(cudaMemsetAsync(B.totals, 0, 8, st));
     }
     CK(record_event(ln.ev[2], st));
-    k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, nullptr, nullptr);
+    if (B.total_stiles) {
+        k_coarse<<<B.total_stiles, 256, 0, st>>>(B.frames, B.stile_view, B.mrect, B.stile_count, nullptr, nullptr);
+        scan_u32(B.stile_count, B.stile_start, B.total_stiles, B.scan_tmp, B.totals + 2, st, &ln.launches);
+        k_coarse<<<B.total_stiles, 256, 0, st>>>(B.frames, B.stile_view, B.mrect, B.stile_count, B.stile_start, B.stile_list);
+        ln.launches += 2;
+    } else {
+        CK(cudaMemsetAsync(B.totals + 2, 0, 4, st));
+    }
+    k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect,
+                                         B.stile_count, B.stile_start, B.stile_list, B.tile_count, nullptr, nullptr);
     scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ln.launches);
-    k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect, B.tile_count, B.tile_start, B.tile_pay);
+    k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect,
+                                         B.stile_count, B.stile_start, B.stile_list, B.tile_count, B.tile_start, B.tile_pay);
     sftg_launch_tile_order(B.frames, B.tile_view, B.tile_count, B.total_tiles, B.order_scratch, B.tile_order, st);
     ln.launches += 4;
     CK(cudaGetLastError());
@@ -710,13 +775,29 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     A.tile_order = B.tile_order; A.tile_nlights = B.tile_nlights;
     A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
-    for (int si = 0; si < 3; si++)
-        if (B.s_tiles[si]) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], st, A); ln.launches++; }
+    /* With views of several sample counts, the 4x tile range runs on the main stream and the 1x
+     * and 2x ranges beside it on a third stream, so that one range's tail overlaps the others. */
+    const bool split_s = B.s_tiles[2] && (B.s_tiles[0] || B.s_tiles[1]);
+    auto per_range = [&](int k, auto&& launch) -> int {
+        if (!split_s) {
+            for (int si = 0; si < 3; si++) if (B.s_tiles[si]) { launch(si, st); ln.launches++; }
+            return 0;
+        }
+        CK(cudaEventRecord(ln.ev_split[k], st));
+        CK(cudaStreamWaitEvent(ln.stream3, ln.ev_split[k], 0));
+        launch(2, st); ln.launches++;
+        for (int si = 0; si < 2; si++) if (B.s_tiles[si]) { launch(si, ln.stream3); ln.launches++; }
+        CK(cudaEventRecord(ln.ev_merge[k], ln.stream3));
+        CK(cudaStreamWaitEvent(st, ln.ev_merge[k], 0));
+        return 0;
+    };
+    int prc = per_range(0, [&](int si, cudaStream_t s) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], s, A); });
+    if (prc) return prc;
     CK(cudaGetLastError());
     CK(record_event(ln.ev[4], st));
     if (occl) CK(cudaStreamWaitEvent(st, ln.ev_join, 0));
-    for (int si = 0; si < 3; si++)
-        if (B.s_tiles[si]) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], st, A); ln.launches++; }
+    prc = per_range(1, [&](int si, cudaStream_t s) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], s, A); });
+    if (prc) return prc;
     if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ln.launches++; }
     CK(cudaGetLastError());
     CK(record_event(ln.ev[5], st));
@@ -734,12 +815,14 @@ static uint64_t batch_key(const sftg_ctx* ctx, const batch_bufs& B) {
     uint64_t h = 1469598103934665603ull;
     const uint32_t ov = B.any_overlay ? 1u : 0u;
     h = fnv(h, &ov, sizeof(ov));
-    const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights,
+    const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.stile_view, B.stile_count, B.stile_start,
+                           B.stile_list, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights,
                            B.mrect, B.clips, B.clip_rect, B.tile_count, B.tile_start, B.tile_order, B.order_scratch, B.tile_pay,
                            B.light_vis, B.packets, B.pairs, B.n_pairs, B.scan_tmp, B.status, B.totals, B.vis, B.zrange,
                            B.vis_depth, B.vis_id, B.shadow };
     h = fnv(h, ptrs, sizeof(ptrs));
     const uint32_t cnt[] = { B.max_pairs, B.n_views, B.total_ss, B.n_jobs, B.total_tiles, B.total_prox, B.total_packets, B.max_inst,
+                             B.total_stiles,
                              B.s_tile0[0], B.s_tile0[1], B.s_tile0[2], B.s_tiles[0], B.s_tiles[1], B.s_tiles[2] };
     h = fnv(h, cnt, sizeof(cnt));
     h = fnv(h, &B.color_total, sizeof(B.color_total));
@@ -798,7 +881,7 @@ static int submit_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
         }
     if ((rc = (dbg || !ctx->use_graphs) ? launch_batch(ctx, ln, B) : launch_batch_graph(ctx, ln, B))) return rc;
     CK(cudaMemcpyAsync(ln.h_status, B.status, 4, cudaMemcpyDeviceToHost, ln.stream));
-    CK(cudaMemcpyAsync(ln.h_status + 2, B.totals, 8, cudaMemcpyDeviceToHost, ln.stream));
+    CK(cudaMemcpyAsync(ln.h_status + 2, B.totals, 12, cudaMemcpyDeviceToHost, ln.stream));
     if (!defer_colors)
         for (uint32_t v = 0; v < nv; v++)
             if (host_color && host_color[v])
@@ -816,10 +899,11 @@ static int finish_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
                         const int32_t* pitch_bytes, const batch_bufs& B, bool defer_colors, sftg_debug_out* dbg,
                         const uint32_t** out_dev) {
     CK(cudaEventSynchronize(ln.ev_done));
-    const uint32_t clip_total = ln.h_status[2], pay_total = ln.h_status[3];
-    if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap) {   /* capacity exceeded: grow and redo the batch */
+    const uint32_t clip_total = ln.h_status[2], pay_total = ln.h_status[3], stile_total = ln.h_status[4];
+    if (clip_total > ctx->clip_cap || pay_total > ctx->tile_cap || stile_total > ctx->stile_cap) {   /* capacity exceeded: grow and redo */
         while (ctx->clip_cap < clip_total) ctx->clip_cap *= 2;
         while (ctx->tile_cap < pay_total) ctx->tile_cap *= 2;
+        while (ctx->stile_cap < stile_total) ctx->stile_cap *= 2;
         return BATCH_REDO;
     }
     for (int k = 0; k < 5; k++) {   /* geometry is timed from its own start: occlusion runs beside it */

@@ -11,9 +11,13 @@
  *   k_clip      near-plane clipping of straddling triangles (4691-4772, 4264-4381); clip
  *               slots come from an exclusive scan of per-batch clip counts, which numbers
  *               them in the reference's single-worker emission order.
+ *   k_coarse    one CTA per super-tile (4 x 4 tiles) lists, in slot order, the meshlets of its
+ *               view whose tile rectangle overlaps it; run once to count and once to write.
  *   k_bin       one CTA per tile builds that tile's payload list in the reference's order
  *               (meshlet, batch, clipped triangles before the batch payload) with ordered
- *               warp-aggregated compaction; run once to count and once to write.
+ *               warp-aggregated compaction over its super-tile's meshlet list (every meshlet
+ *               that touches the tile is on it, in slot order); run once to count and once
+ *               to write.
  *   k_scan_*    a three-phase exclusive scan used for clip slots and tile list offsets.
  */
 #include "sftg_types.h"
@@ -351,9 +355,47 @@ SFTG_D uint32_t bin_meshlet(const sftg_batch_rec* recs, const uint32_t* clip_cnt
 }
 
 __global__ void __launch_bounds__(BIN_THREADS)
+k_coarse(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ stile_view, const int4* __restrict__ mrect,
+         uint32_t* __restrict__ stile_count, const uint32_t* __restrict__ stile_start, uint32_t* __restrict__ stile_list)
+{
+    __shared__ uint32_t s_wsum[BIN_THREADS / 32];
+    const int gst = blockIdx.x;                         /* batch-wide super-tile index */
+    const sftg_frame* F = frames + stile_view[gst];
+    const int st = gst - (int)F->stile_base;
+    const int sx0 = (st % (int)F->scols) * SFTG_STILE, sy0 = (st / (int)F->scols) * SFTG_STILE;
+    const int sx1 = sx0 + SFTG_STILE - 1, sy1 = sy0 + SFTG_STILE - 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t* out = nullptr;
+    if (stile_list) {
+        /* over capacity: the host grows the lists and re-renders; write nothing */
+        if ((uint64_t)stile_start[gst] + stile_count[gst] > F->stile_cap) return;
+        out = stile_list + stile_start[gst];
+    }
+    uint32_t running = 0;
+    for (uint32_t base = 0; base < F->total_ss; base += BIN_THREADS) {
+        const uint32_t s = F->ss_base + base + tid;
+        bool hit = false;
+        if (base + tid < F->total_ss) {
+            const int4 q = mrect[s];   /* inclusive tile rectangle x0, x1, y0, y1; empty when x0 > x1 */
+            hit = q.x <= q.y && q.z <= q.w && q.x <= sx1 && q.y >= sx0 && q.z <= sy1 && q.w >= sy0;
+        }
+        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
+        if (lane == 0) s_wsum[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t off = 0, tot = 0;
+        for (int w = 0; w < BIN_THREADS / 32; w++) { if (w < warp) off += s_wsum[w]; tot += s_wsum[w]; }
+        if (out && hit) out[running + off + __popc(bal & ((1u << lane) - 1u))] = s;
+        running += tot;
+        __syncthreads();
+    }
+    if (!stile_list && tid == 0) stile_count[gst] = running;
+}
+
+__global__ void __launch_bounds__(BIN_THREADS)
 k_bin(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_view, const sftg_batch_rec* __restrict__ recs,
       const uint32_t* __restrict__ clip_cnt, const uint32_t* __restrict__ clip_base, const int4* __restrict__ clip_rect,
-      const int4* __restrict__ mrect, uint32_t* __restrict__ tile_count, const uint32_t* __restrict__ tile_start,
+      const int4* __restrict__ mrect, const uint32_t* __restrict__ stile_count, const uint32_t* __restrict__ stile_start,
+      const uint32_t* __restrict__ stile_list, uint32_t* __restrict__ tile_count, const uint32_t* __restrict__ tile_start,
       uint64_t* __restrict__ tile_pay)
 {
     __shared__ uint32_t s_hits[BIN_THREADS];
@@ -374,11 +416,25 @@ k_bin(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_v
         if ((uint64_t)tile_start[gtile] + tile_count[gtile] > F->tile_cap) return;
         out = tile_pay + tile_start[gtile];
     }
+    /* the meshlets that can touch this tile: its super-tile's list, in slot order, or every slot
+     * of the view when the view has no coarse lists (scols == 0) */
+    uint32_t n_cand = n_ss;
+    const uint32_t* cand = nullptr;
+    if (F->scols) {
+        const uint32_t gst = F->stile_base + (uint32_t)((ty / SFTG_STILE) * (int)F->scols + tx / SFTG_STILE);
+        n_cand = stile_count[gst];
+        if ((uint64_t)stile_start[gst] + n_cand > F->stile_cap) n_cand = 0;   /* lists overflowed: the host re-renders */
+        cand = stile_list + stile_start[gst];
+    }
     uint32_t running = 0;
-    for (uint32_t base = 0; base < n_ss; base += BIN_THREADS) {
-        const uint32_t s = F->ss_base + base + tid;
+    for (uint32_t base = 0; base < n_cand; base += BIN_THREADS) {
+        uint32_t s = 0;
         bool hit = false;
-        if (base + tid < n_ss) { const int4 q = mrect[s]; hit = rect_has(q.x, q.y, q.z, q.w, tx, ty); }
+        if (base + tid < n_cand) {
+            s = cand ? cand[base + tid] : F->ss_base + base + tid;
+            const int4 q = mrect[s];
+            hit = rect_has(q.x, q.y, q.z, q.w, tx, ty);
+        }
         if (!__syncthreads_or(hit)) continue;   /* no meshlet of this chunk touches the tile */
         /* ordered compaction of hit meshlets */
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);

@@ -42,8 +42,12 @@ __global__ void k_geometry(const sftg_frame* frames, const sftg_job* jobs, uint3
                            uint32_t* clip_cnt, int4* mrect);
 __global__ void k_clip(const sftg_frame* frames, uint32_t n_views, const float* ss, const uint32_t* clip_cnt,
                        const uint32_t* clip_base, sftg_clip_tri* clips, int4* clip_rect, int4* mrect, uint32_t n_records);
+#define SFTG_STILE 4   /* tiles per side of a super-tile (coarse binning) */
+__global__ void k_coarse(const sftg_frame* frames, const uint16_t* stile_view, const int4* mrect, uint32_t* stile_count,
+                         const uint32_t* stile_start, uint32_t* stile_list);
 __global__ void k_bin(const sftg_frame* frames, const uint16_t* tile_view, const sftg_batch_rec* recs, const uint32_t* clip_cnt,
-                      const uint32_t* clip_base, const int4* clip_rect, const int4* mrect, uint32_t* tile_count,
+                      const uint32_t* clip_base, const int4* clip_rect, const int4* mrect, const uint32_t* stile_count,
+                      const uint32_t* stile_start, const uint32_t* stile_list, uint32_t* tile_count,
                       const uint32_t* tile_start, uint64_t* tile_pay);
 __global__ void k_scan_reduce(const uint32_t* in, uint32_t n, uint32_t* sums);
 __global__ void k_scan_top(uint32_t* sums, uint32_t nb, uint32_t* total_out);

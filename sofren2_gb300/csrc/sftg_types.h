@@ -123,11 +123,13 @@ typedef struct sftg_frame {
     uint32_t n_point, n_dir, n_proxies, n_inst;
     uint32_t total_ss, n_jobs, tlas_root, tlas_count;
     uint32_t clip_cap, tile_cap;                 /* capacities of the clip pool and tile payload buffer */
-    int32_t debug_tex, pad3;                     /* checkerboard texture of the debug view */
+    int32_t debug_tex;                           /* checkerboard texture of the debug view */
+    uint32_t stile_cap;                          /* capacity of the super-tile meshlet lists */
     /* where this view's rows start in the batch-wide arrays (all 0 for a single frame) */
     uint32_t view, ss_base;        /* screen-space cache slot; batch records start at ss_base * 16 */
     uint32_t tile_base, prox_base; /* global tile index; global proxy index (light_vis rows) */
     uint32_t packet_base, n_packets;
+    uint32_t stile_base, scols;    /* global index of the first super-tile (4 x 4 tiles); super-tile columns */
     uint64_t vis_base;             /* float2 offset of this view's visibility buffer */
     uint32_t* color_dev;           /* this view's colour buffer, width * height */
     /* per-frame arrays */
