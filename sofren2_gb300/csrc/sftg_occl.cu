@@ -188,31 +188,39 @@ k_occl_tlas(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ 
     int top = 1;
     if (lane == 0) s_stack[warp][0] = F->tlas_root;
     __syncwarp();
+    /* lane c < 8 handles child c of each node: pushes (inner nodes) and pair emission (leaves)
+     * are warp-aggregated; the pairs' order does not matter (hits are OR-ed) */
     while (top > 0) {
         const uint32_t ni = s_stack[warp][--top];
         __syncwarp();
         const sftg_bvh_node* nd = &F->tlas[ni];
-        uint32_t m = node_mask(nd, pf, lane);
-        while (m) {
-            const int c = __ffs(m) - 1; m &= m - 1;
-            const uint32_t ch = nd->child[c];
-            if (ch == SFTG_INVALID) continue;
-            if (!nd->leaf) {
-                if (top >= OCC_STACK || ch >= F->tlas_count) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); return; }
-                if (lane == 0) s_stack[warp][top] = ch;
-                top++;
-                __syncwarp();
-                continue;
-            }
-            const uint32_t ii = ch & ~0x80000000u;
-            if (ii >= F->n_inst) continue;
+        const uint32_t m = node_mask(nd, pf, lane);
+        const uint32_t ch = lane < 8 ? nd->child[lane] : SFTG_INVALID;
+        const bool mine = lane < 8 && ((m >> lane) & 1u) && ch != SFTG_INVALID;
+        if (!nd->leaf) {
+            if (__ballot_sync(0xFFFFFFFFu, mine && ch >= F->tlas_count)) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); return; }
+            const uint32_t pm = __ballot_sync(0xFFFFFFFFu, mine);
+            if (top + __popc(pm) > OCC_STACK) { if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW); return; }
+            if (mine) s_stack[warp][top + __popc(pm & ((1u << lane) - 1u))] = ch;
+            top += __popc(pm);
+            __syncwarp();
+            continue;
+        }
+        bool emit = false;
+        const uint32_t ii = ch & ~0x80000000u;
+        if (mine && ii < F->n_inst) {
             const sftg_model Md = F->models[F->inst[ii].model];
-            if (Md.bone_count > 0 || Md.blas_count == 0) continue;   /* static instances only */
-            if (lane == 0) {
-                const uint32_t slot = atomicAdd(n_pairs, 1u);
-                if (slot < max_pairs) pairs[slot] = make_uint2(pk, ii);
-                else atomicOr(status, OCC_PAIR_OVERFLOW);
-            }
+            emit = !(Md.bone_count > 0 || Md.blas_count == 0);   /* static instances only */
+        }
+        const uint32_t em = __ballot_sync(0xFFFFFFFFu, emit);
+        if (!em) continue;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(n_pairs, (uint32_t)__popc(em));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (emit) {
+            const uint32_t slot = base + __popc(em & ((1u << lane) - 1u));
+            if (slot < max_pairs) pairs[slot] = make_uint2(pk, ii);
+            else atomicOr(status, OCC_PAIR_OVERFLOW);
         }
     }
 }
@@ -340,25 +348,33 @@ SFTG_D uint32_t occ_walk_from(const sftg_frame* F, const sftg_inst* I, const sft
         uint32_t m = node_mask(nd, w.mf, lane);
         if (prune && m) m &= ray_box_mask(nd, R, full & ~sat, lane);
         if (!nd->leaf) {
-            while (m) {
-                const int c = __ffs(m) - 1; m &= m - 1;
-                const uint32_t ch = nd->child[c];
-                if (ch == SFTG_INVALID) continue;
-                if (top >= OCC_STACK || ch >= Md.blas_count || ch >= (1u << 29) || ++guard > (1u << 24)) {
+            /* lane c < 8 takes child c: one ballot for the checks, one atomic for the items, one
+             * stack write per lane (the stack keeps the children in slot order) */
+            const uint32_t ch = lane < 8 ? nd->child[lane] : SFTG_INVALID;
+            const bool mine = lane < 8 && ((m >> lane) & 1u) && ch != SFTG_INVALID;
+            const uint32_t tm = __ballot_sync(0xFFFFFFFFu, mine);
+            guard += (uint32_t)__popc(tm);
+            if (__ballot_sync(0xFFFFFFFFu, mine && (ch >= Md.blas_count || ch >= (1u << 29))) || guard > (1u << 24)) {
+                if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW);
+                return sat;
+            }
+            if (!tm) continue;
+            uint32_t pm = tm;
+            if (EXPAND && depth + 1 >= OCC_EXPAND_DEPTH) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(n_items, (uint32_t)__popc(tm));
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                const bool placed = mine && base + __popc(tm & ((1u << lane) - 1u)) < max_items;
+                if (placed) items[base + __popc(tm & ((1u << lane) - 1u))] = make_uint2(pair, ch);
+                pm = tm & ~__ballot_sync(0xFFFFFFFFu, placed);   /* children without an item slot are walked here */
+            }
+            if (pm) {
+                if (top + __popc(pm) > OCC_STACK) {
                     if (lane == 0) atomicOr(status, OCC_STACK_OVERFLOW);
                     return sat;
                 }
-                if (EXPAND && depth + 1 >= OCC_EXPAND_DEPTH) {
-                    uint32_t slot = 0;
-                    if (lane == 0) slot = atomicAdd(n_items, 1u);
-                    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-                    if (slot < max_items) {
-                        if (lane == 0) items[slot] = make_uint2(pair, ch);
-                        continue;
-                    }
-                }
-                if (lane == 0) stack[top] = ch | (EXPAND ? (depth + 1) << 29 : 0u);
-                top++;
+                if ((pm >> lane) & 1u) stack[top + __popc(pm & ((1u << lane) - 1u))] = ch | (EXPAND ? (depth + 1) << 29 : 0u);
+                top += __popc(pm);
                 __syncwarp();
             }
             continue;
