@@ -166,11 +166,15 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) { delete ctx; return SFTG_E_CUDA; }
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return SFTG_E_CUDA; }
+    /* the occlusion stream gets the lowest priority: it only has to finish before the resolve, so
+     * the critical-path kernels (geometry, binning, raster) take free SMs first */
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
     for (int l = 0; l < SFTG_MAX_LANES; l++) {
         sftg_lane& ln = ctx->lanes[l];
-        if (cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&ln.stream2, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&ln.stream3, cudaStreamNonBlocking) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
+        if (cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&ln.stream2, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&ln.stream3, cudaStreamNonBlocking, prio_high) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
         for (int k = 0; k < 2; k++) {
             cudaEventCreateWithFlags(&ln.ev_split[k], cudaEventDisableTiming);
             cudaEventCreateWithFlags(&ln.ev_merge[k], cudaEventDisableTiming);
@@ -848,7 +852,7 @@ static int launch_batch_graph(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B)
             if (g) cudaGraphDestroy(g);
             return rc ? rc : set_err(ctx, SFTG_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
         }
-        const cudaError_t ie = cudaGraphInstantiate(&ln.graph, g, 0);
+        const cudaError_t ie = cudaGraphInstantiate(&ln.graph, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) { ln.graph = nullptr; return set_err(ctx, SFTG_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ie)); }
         ln.graph_key = key;
@@ -1269,17 +1273,17 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
         std::vector<sftg_frame_desc> sub;
         for (uint32_t v = 0; v < n_views; v++) if (fds[v].samples == (1 << si)) sub.push_back(fds[v]);
         if (sub.empty()) continue;
-        const int slabs[4] = { 4, 8, 16, 64 };
+        const int slabs[5] = { 4, 8, 16, 32, 64 };
         float bt = 1e30f;
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < 5; k++) {
             ctx->tuning = best; ctx->tuning.raster_slab_rows[si] = slabs[k];
             float t;
             if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 3, &t))) { ctx->tuning = best; return rc; }
             if (t < bt) { bt = t; best.raster_slab_rows[si] = slabs[k]; }
         }
-        const int splits[4] = { 4, 8, 16, 2 };
+        const int splits[5] = { 4, 8, 16, 2, 1 };
         bt = 1e30f;
-        for (int k = 0; k < 3; k++) {
+        for (int k = 0; k < 5; k++) {
             ctx->tuning = best; ctx->tuning.resolve_split[si] = splits[k];
             float t;
             if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
