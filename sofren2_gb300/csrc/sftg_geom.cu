@@ -213,67 +213,91 @@ SFTG_D cvert lerp_cv(const cvert& a, const cvert& b, float t) {
     return r;
 }
 
-/* one thread per batch record with clip outputs (clipping is rare) */
+/* Batch records with clip outputs (clipping is rare).  Each warp scans 32 records; the records
+ * that clip are taken four at a time, one per 8-lane group, lane tl of the group clipping
+ * triangle tl of the batch.  A triangle's clip slots follow those of the batch's earlier
+ * triangles (exclusive scan over the group), the reference's order. */
 __global__ void k_clip(const sftg_frame* __restrict__ frames, uint32_t n_views, const float* __restrict__ ss,
                        const uint32_t* __restrict__ clip_cnt, const uint32_t* __restrict__ clip_base,
                        sftg_clip_tri* __restrict__ clips, int4* __restrict__ clip_rect, int4* __restrict__ mrect,
                        uint32_t n_records)
 {
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n_records || clip_cnt[r] == 0) return;
-    const uint32_t ssi = r / 16, b = r % 16;
-    /* the view, then the instance, owning this screen-space slot (both laid out in order) */
-    uint32_t v = 0;
-    for (uint32_t k = 0; k < n_views; k++) if (frames[k].ss_base <= ssi && frames[k].total_ss) v = k;
-    const sftg_frame* F = frames + v;
-    const uint32_t lss = ssi - F->ss_base;
-    uint32_t ii = 0;
-    for (uint32_t k = 0; k < F->n_inst; k++) if (F->inst[k].ss_offset <= lss) ii = k;
-    const sftg_inst* I = &F->inst[ii];
-    const uint32_t m = lss - I->ss_offset, g = I->meshlet_base + m;
-    const float* at = F->ml_attr + (size_t)g * 640;
-    const float* S = ss + (size_t)ssi * 576;
-    const uint8_t* ind = F->ml_inds + (size_t)g * 512;
-    const float* VP = F->vp;
-    const float hw = F->hw, hh = F->hh;
-    uint32_t slot = clip_base[r];
-    int4 mr = mrect[ssi];
-    bool grew = false;
-    for (int tl = 0; tl < 8; tl++) {
+    const int lane = threadIdx.x & 31, gl = lane & 7, gshift = lane & ~7;
+    const uint32_t gmask = 0xFFu << gshift;
+    const uint32_t r_lane = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t pending = __ballot_sync(0xFFFFFFFFu, r_lane < n_records && clip_cnt[r_lane] != 0);
+    const uint32_t r_base = r_lane - (uint32_t)lane;
+    while (pending) {
+        /* group g takes the g-th pending record */
+        uint32_t pick = pending;
+        for (int g = 0; g < (lane >> 3) && pick; g++) pick &= pick - 1;
+        const bool have = pick != 0;
+        const uint32_t r = r_base + (have ? (uint32_t)(__ffs(pick) - 1) : 0u);
+        for (int g = 0; g < 4 && pending; g++) pending &= pending - 1;
+        if (!have) continue;   /* whole group: the same pick on its 8 lanes */
+        const uint32_t ssi = r / 16, b = r % 16;
+        /* the view, then the instance, owning this screen-space slot (both laid out in order) */
+        uint32_t v = 0;
+        for (uint32_t k = 0; k < n_views; k++) if (frames[k].ss_base <= ssi && frames[k].total_ss) v = k;
+        const sftg_frame* F = frames + v;
+        const uint32_t lss = ssi - F->ss_base;
+        uint32_t ii = 0;
+        for (uint32_t k = 0; k < F->n_inst; k++) if (F->inst[k].ss_offset <= lss) ii = k;
+        const sftg_inst* I = &F->inst[ii];
+        const uint32_t m = lss - I->ss_offset, g = I->meshlet_base + m;
+        const float* at = F->ml_attr + (size_t)g * 640;
+        const float* S = ss + (size_t)ssi * 576;
+        const uint8_t* ind = F->ml_inds + (size_t)g * 512;
+        const float* VP = F->vp;
+        const float hw = F->hw, hh = F->hh;
+        const int tl = gl;
         const uint32_t q[3] = { ind[b * 32 + tl], ind[b * 32 + 8 + tl], ind[b * 32 + 16 + tl] };
-        if (!((int)(q[0] | q[1] | q[2]) > 0)) continue;
         cvert in[3];
-        for (int k = 0; k < 3; k++) {
-            const uint32_t v = q[k];
-            const float wx = S[192 + v], wy = S[256 + v], wz = S[320 + v];
-            in[k].w = fma_(wx, VP[3], fma_(wy, VP[7], fma_(wz, VP[11], VP[15])));
-            in[k].tx = fma_(wx, VP[0], fma_(wy, VP[4], fma_(wz, VP[8], VP[12])));
-            in[k].ty = fma_(wx, VP[1], fma_(wy, VP[5], fma_(wz, VP[9], VP[13])));
-            in[k].tz = fma_(wx, VP[2], fma_(wy, VP[6], fma_(wz, VP[10], VP[14])));
-            in[k].u = at[384 + v]; in[k].v = at[448 + v]; in[k].lu = at[512 + v]; in[k].lv = at[576 + v];
-            in[k].px = wx; in[k].py = wy; in[k].pz = wz;
-            in[k].nx = S[384 + v]; in[k].ny = S[448 + v]; in[k].nz = S[512 + v];
+        cvert out[2][3];
+        int nc = 0;
+        if ((int)(q[0] | q[1] | q[2]) > 0) {
+            for (int k = 0; k < 3; k++) {
+                const uint32_t vv = q[k];
+                const float wx = S[192 + vv], wy = S[256 + vv], wz = S[320 + vv];
+                in[k].w = fma_(wx, VP[3], fma_(wy, VP[7], fma_(wz, VP[11], VP[15])));
+                in[k].tx = fma_(wx, VP[0], fma_(wy, VP[4], fma_(wz, VP[8], VP[12])));
+                in[k].ty = fma_(wx, VP[1], fma_(wy, VP[5], fma_(wz, VP[9], VP[13])));
+                in[k].tz = fma_(wx, VP[2], fma_(wy, VP[6], fma_(wz, VP[10], VP[14])));
+                in[k].u = at[384 + vv]; in[k].v = at[448 + vv]; in[k].lu = at[512 + vv]; in[k].lv = at[576 + vv];
+                in[k].px = wx; in[k].py = wy; in[k].pz = wz;
+                in[k].nx = S[384 + vv]; in[k].ny = S[448 + vv]; in[k].nz = S[512 + vv];
+            }
+            const bool a = in[0].tz >= 0.f, bb = in[1].tz >= 0.f, c = in[2].tz >= 0.f;
+            const bool ai = a && bb && c, ao = (in[0].tz < 0.f) && (in[1].tz < 0.f) && (in[2].tz < 0.f);
+            if (!(ai || ao)) {
+                /* sft__clip_triangle_near_plane (4264-4349) */
+                const int mask = (int)a | ((int)bb << 1) | ((int)c << 2);
+                float d[3] = { in[0].tz, in[1].tz, in[2].tz };
+                if (mask == 1 || mask == 2 || mask == 4) {
+                    const int ia = mask >> 1, ib = (ia == 2) ? 0 : ia + 1, ic = (ia == 0) ? 2 : ia - 1;
+                    const float tab = fdiv(d[ia], d[ia] - d[ib]), tac = fdiv(d[ia], d[ia] - d[ic]);
+                    out[0][0] = in[ia]; out[0][1] = lerp_cv(in[ia], in[ib], tab); out[0][2] = lerp_cv(in[ia], in[ic], tac);
+                    nc = 1;
+                } else {
+                    const int io = (~mask & 7) >> 1, ia = (io == 0) ? 2 : io - 1, ic = (io == 2) ? 0 : io + 1;
+                    const float tab = fdiv(d[ia], d[ia] - d[io]), tcb = fdiv(d[ic], d[ic] - d[io]);
+                    const cvert nab = lerp_cv(in[ia], in[io], tab), ncb = lerp_cv(in[ic], in[io], tcb);
+                    out[0][0] = in[ia]; out[0][1] = nab; out[0][2] = in[ic];
+                    out[1][0] = nab; out[1][1] = ncb; out[1][2] = in[ic];
+                    nc = 2;
+                }
+            }
         }
-        const bool a = in[0].tz >= 0.f, bb = in[1].tz >= 0.f, c = in[2].tz >= 0.f;
-        const bool ai = a && bb && c, ao = (in[0].tz < 0.f) && (in[1].tz < 0.f) && (in[2].tz < 0.f);
-        if (ai || ao) continue;
-        /* sft__clip_triangle_near_plane (4264-4349) */
-        const int mask = (int)a | ((int)bb << 1) | ((int)c << 2);
-        cvert out[2][3]; int nc = 0;
-        float d[3] = { in[0].tz, in[1].tz, in[2].tz };
-        if (mask == 1 || mask == 2 || mask == 4) {
-            const int ia = mask >> 1, ib = (ia == 2) ? 0 : ia + 1, ic = (ia == 0) ? 2 : ia - 1;
-            const float tab = fdiv(d[ia], d[ia] - d[ib]), tac = fdiv(d[ia], d[ia] - d[ic]);
-            out[0][0] = in[ia]; out[0][1] = lerp_cv(in[ia], in[ib], tab); out[0][2] = lerp_cv(in[ia], in[ic], tac);
-            nc = 1;
-        } else {
-            const int io = (~mask & 7) >> 1, ia = (io == 0) ? 2 : io - 1, ic = (io == 2) ? 0 : io + 1;
-            const float tab = fdiv(d[ia], d[ia] - d[io]), tcb = fdiv(d[ic], d[ic] - d[io]);
-            const cvert nab = lerp_cv(in[ia], in[io], tab), ncb = lerp_cv(in[ic], in[io], tcb);
-            out[0][0] = in[ia]; out[0][1] = nab; out[0][2] = in[ic];
-            out[1][0] = nab; out[1][1] = ncb; out[1][2] = in[ic];
-            nc = 2;
+        /* exclusive scan of the output counts over the group's 8 triangles */
+        int incl = nc;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const int t = __shfl_up_sync(gmask, incl, o, 8);
+            if (gl >= o) incl += t;
         }
+        uint32_t slot = clip_base[r] + (uint32_t)(incl - nc);
+        int4 mr = make_int4(0x7FFFFFFF, (int)0x80000000, 0x7FFFFFFF, (int)0x80000000);
+        bool grew = false;
         for (int k = 0; k < nc; k++, slot++) {
             if (slot >= F->clip_cap) continue;   /* over capacity: the host grows the pool and re-renders */
             sftg_clip_tri ct;
@@ -304,10 +328,12 @@ __global__ void k_clip(const sftg_frame* __restrict__ frames, uint32_t n_views, 
             }
             clip_rect[slot] = rc;
         }
-    }
-    if (grew) {   /* several batches of one meshlet may clip: widen the meshlet rectangle atomically */
-        atomicMin(&mrect[ssi].x, mr.x); atomicMax(&mrect[ssi].y, mr.y);
-        atomicMin(&mrect[ssi].z, mr.z); atomicMax(&mrect[ssi].w, mr.w);
+        /* several triangles and batches of one meshlet may clip: widen its rectangle atomically
+         * (min / max commute, so the result does not depend on the order) */
+        if (grew) {
+            atomicMin(&mrect[ssi].x, mr.x); atomicMax(&mrect[ssi].y, mr.y);
+            atomicMin(&mrect[ssi].z, mr.z); atomicMax(&mrect[ssi].w, mr.w);
+        }
     }
 }
 
