@@ -433,6 +433,11 @@ struct batch_bufs {
 static void scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, uint32_t* total, cudaStream_t st, int* launches) {
     const uint32_t nb = (n + SFTG_SCAN_ELEMS_PER_BLOCK - 1) / SFTG_SCAN_ELEMS_PER_BLOCK;
     if (!nb) return;
+    if (n <= SFTG_SCAN_SMALL) {
+        k_scan_small<<<1, 1024, 0, st>>>(in, n, out, total);
+        *launches += 1;
+        return;
+    }
     k_scan_reduce<<<nb, 1024, 0, st>>>(in, n, tmp);
     k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, total);
     k_scan_down<<<nb, 1024, 0, st>>>(in, n, tmp, out);
@@ -769,8 +774,7 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     scan_u32(B.tile_count, B.tile_start, B.total_tiles, B.scan_tmp, B.totals + 1, st, &ln.launches);
     k_bin<<<B.total_tiles, 256, 0, st>>>(B.frames, B.tile_view, B.recs, B.clip_cnt, B.clip_base, B.clip_rect, B.mrect,
                                          B.stile_count, B.stile_start, B.stile_list, B.tile_count, B.tile_start, B.tile_pay);
-    sftg_launch_tile_order(B.frames, B.tile_view, B.tile_count, B.total_tiles, B.order_scratch, B.tile_order, st);
-    ln.launches += 4;
+    ln.launches += 2 + sftg_launch_tile_order(B.frames, B.tile_view, B.tile_count, B.total_tiles, B.order_scratch, B.tile_order, st);
     CK(cudaGetLastError());
     CK(record_event(ln.ev[3], st));
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));

@@ -558,6 +558,21 @@ __global__ void k_scan_top(uint32_t* __restrict__ sums, uint32_t nb, uint32_t* _
     if (threadIdx.x == 0 && total_out) *total_out = carry;
 }
 
+/* the whole scan in one CTA for small inputs (n <= SFTG_SCAN_SMALL): each thread a run of
+ * consecutive elements, one block scan of the run sums */
+__global__ void __launch_bounds__(SCAN_BLOCK)
+k_scan_small(const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ out, uint32_t* __restrict__ total_out) {
+    __shared__ uint32_t s_w[33];
+    const uint32_t per = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    const uint32_t i0 = threadIdx.x * per;
+    uint32_t acc = 0;
+    for (uint32_t k = 0; k < per; k++) { const uint32_t i = i0 + k; if (i < n) acc += in[i]; }
+    uint32_t tot;
+    uint32_t e = block_excl_scan(acc, s_w, &tot);
+    for (uint32_t k = 0; k < per; k++) { const uint32_t i = i0 + k; if (i < n) { const uint32_t x = in[i]; out[i] = e; e += x; } }
+    if (threadIdx.x == 0 && total_out) *total_out = tot;
+}
+
 __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t n, const uint32_t* __restrict__ sums, uint32_t* __restrict__ out) {
     __shared__ uint32_t s_w[33];
     const uint32_t base = blockIdx.x * SCAN_BLOCK * 4;

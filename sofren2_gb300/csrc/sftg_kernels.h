@@ -52,6 +52,8 @@ __global__ void k_bin(const sftg_frame* frames, const uint16_t* tile_view, const
 __global__ void k_scan_reduce(const uint32_t* in, uint32_t n, uint32_t* sums);
 __global__ void k_scan_top(uint32_t* sums, uint32_t nb, uint32_t* total_out);
 __global__ void k_scan_down(const uint32_t* in, uint32_t n, const uint32_t* sums, uint32_t* out);
+#define SFTG_SCAN_SMALL (1024u * 32u)   /* inputs up to this size are scanned by one CTA */
+__global__ void k_scan_small(const uint32_t* in, uint32_t n, uint32_t* out, uint32_t* total_out);
 size_t sftg_packet_bytes();
 /* BLAS sub-walk items per (packet, instance) pair: the pair buffer holds max_pairs pairs, then
  * max_pairs * items_per_pair items; the counter word after n_pairs counts the items.  A walk
@@ -65,7 +67,7 @@ void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view
                            cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
 /* order[] = the batch's tiles, heaviest first inside each sample-count range; scratch holds 192 words */
-void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
+int sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
                             uint32_t* scratch, uint32_t* order, cudaStream_t st);
 /* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4, 8 or 16) */
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A);

@@ -989,13 +989,42 @@ __global__ void k_order_scatter(const sftg_frame* __restrict__ frames, const uin
     order[base[b] + atomicAdd(&cursor[b], 1u)] = t;
 }
 
-void sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
-                            uint32_t* scratch, uint32_t* order, cudaStream_t st) {
-    if (!n_tiles) return;
+/* the same order in one CTA for small tile counts: histogram, bucket starts and scatter in
+ * shared memory */
+__global__ void __launch_bounds__(1024)
+k_order_small(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ tile_view, const uint32_t* __restrict__ tile_count,
+              uint32_t n_tiles, uint32_t* __restrict__ order)
+{
+    __shared__ uint32_t h[3 * ORDER_BUCKETS], base[3 * ORDER_BUCKETS];
+    for (int i = threadIdx.x; i < 3 * ORDER_BUCKETS; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < n_tiles; t += blockDim.x) atomicAdd(&h[order_bucket(frames, tile_view, tile_count, t)], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int i = 0; i < 3 * ORDER_BUCKETS; i++) { base[i] = run; run += h[i]; }
+    }
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < n_tiles; t += blockDim.x) {
+        const uint32_t b = order_bucket(frames, tile_view, tile_count, t);
+        order[atomicAdd(&base[b], 1u)] = t;
+    }
+}
+
+#define ORDER_SMALL 8192u   /* tile counts up to this are ordered by one CTA */
+
+int sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
+                           uint32_t* scratch, uint32_t* order, cudaStream_t st) {
+    if (!n_tiles) return 0;
+    if (n_tiles <= ORDER_SMALL) {
+        k_order_small<<<1, 1024, 0, st>>>(frames, tile_view, tile_count, n_tiles, order);
+        return 1;
+    }
     cudaMemsetAsync(scratch, 0, 2 * 3 * ORDER_BUCKETS * sizeof(uint32_t), st);
     const uint32_t g = (n_tiles + 255) / 256;
     k_order_count<<<g, 256, 0, st>>>(frames, tile_view, tile_count, n_tiles, scratch);
     k_order_scatter<<<g, 256, 0, st>>>(frames, tile_view, tile_count, n_tiles, scratch, scratch + 3 * ORDER_BUCKETS, order);
+    return 2;
 }
 
 /* ---------------------------------------------------------------- debug overlays
