@@ -127,7 +127,9 @@ class ClockSampler:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_resolve launch of the
 # workload, from one full ncu capture of that launch on a GB300 (the 6th launch of
 # `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`)
-RESOLVE_TRAFFIC = {"skinned_1080p_2xmsaa": 38515968 + 15360, "atrium_1080p_4xmsaa": 76697856 + 3112704}
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_resolve launch, from the ncu captures
+# summarised in profiles/k_resolve_*.md (same kernel code as this build's resolve)
+RESOLVE_TRAFFIC = {"skinned_1080p_2xmsaa": 38522624 + 108800, "atrium_1080p_4xmsaa": 76634880 + 4921088}
 
 
 def _algorithmic_resolve_bytes(width: int, height: int, samples: int) -> float:

@@ -762,9 +762,9 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     }
     CK(record_event(ln.ev[2], st));
     if (B.total_stiles) {
-        k_coarse<<<B.total_stiles, 256, 0, st>>>(B.frames, B.stile_view, B.mrect, B.stile_count, nullptr, nullptr);
+        k_coarse<<<B.total_stiles, 1024, 0, st>>>(B.frames, B.stile_view, B.mrect, B.stile_count, nullptr, nullptr);
         scan_u32(B.stile_count, B.stile_start, B.total_stiles, B.scan_tmp, B.totals + 2, st, &ln.launches);
-        k_coarse<<<B.total_stiles, 256, 0, st>>>(B.frames, B.stile_view, B.mrect, B.stile_count, B.stile_start, B.stile_list);
+        k_coarse<<<B.total_stiles, 1024, 0, st>>>(B.frames, B.stile_view, B.mrect, B.stile_count, B.stile_start, B.stile_list);
         ln.launches += 2;
     } else {
         CK(cudaMemsetAsync(B.totals + 2, 0, 4, st));

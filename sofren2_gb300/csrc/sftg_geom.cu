@@ -380,11 +380,13 @@ SFTG_D uint32_t bin_meshlet(const sftg_batch_rec* recs, const uint32_t* clip_cnt
     return total;
 }
 
-__global__ void __launch_bounds__(BIN_THREADS)
+#define COARSE_THREADS 1024   /* a super-tile scans its view's meshlet slots 1024 at a time */
+
+__global__ void __launch_bounds__(COARSE_THREADS)
 k_coarse(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ stile_view, const int4* __restrict__ mrect,
          uint32_t* __restrict__ stile_count, const uint32_t* __restrict__ stile_start, uint32_t* __restrict__ stile_list)
 {
-    __shared__ uint32_t s_wsum[BIN_THREADS / 32];
+    __shared__ uint32_t s_wsum[COARSE_THREADS / 32];
     const int gst = blockIdx.x;                         /* batch-wide super-tile index */
     const sftg_frame* F = frames + stile_view[gst];
     const int st = gst - (int)F->stile_base;
@@ -398,7 +400,7 @@ k_coarse(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ sti
         out = stile_list + stile_start[gst];
     }
     uint32_t running = 0;
-    for (uint32_t base = 0; base < F->total_ss; base += BIN_THREADS) {
+    for (uint32_t base = 0; base < F->total_ss; base += COARSE_THREADS) {
         const uint32_t s = F->ss_base + base + tid;
         bool hit = false;
         if (base + tid < F->total_ss) {
@@ -409,7 +411,7 @@ k_coarse(const sftg_frame* __restrict__ frames, const uint16_t* __restrict__ sti
         if (lane == 0) s_wsum[warp] = __popc(bal);
         __syncthreads();
         uint32_t off = 0, tot = 0;
-        for (int w = 0; w < BIN_THREADS / 32; w++) { if (w < warp) off += s_wsum[w]; tot += s_wsum[w]; }
+        for (int w = 0; w < COARSE_THREADS / 32; w++) { if (w < warp) off += s_wsum[w]; tot += s_wsum[w]; }
         if (out && hit) out[running + off + __popc(bal & ((1u << lane) - 1u))] = s;
         running += tot;
         __syncthreads();

@@ -26,6 +26,33 @@ int main(int argc, char** argv) {
     sft_arena_init(&arena, 1ull << 26);
     if (sft_model_load_qsf("/nonexistent/model.qsf", &arena)) return 5;
     if (sft_model_load_qsf(argv[0], &arena)) return 6;   /* an ELF file: wrong magic */
+    {   /* the same file cut short, at several points: NULL, no crash */
+        FILE* f = fopen(argv[2], "rb");
+        if (!f) return 7;
+        fseek(f, 0, SEEK_END);
+        const long size = ftell(f);
+        fseek(f, 0, SEEK_SET);
+        unsigned char* buf = (unsigned char*)malloc((size_t)size);
+        if (fread(buf, 1, (size_t)size, f) != (size_t)size) return 7;
+        fclose(f);
+        char cut[4096];
+        snprintf(cut, sizeof(cut), "%s.cut", argv[3]);
+        /* cut points inside the model data; near the end only when no game-data section (which
+         * the loader does not read) follows the model */
+        unsigned long long game_off = 0;
+        memcpy(&game_off, buf + 8, 8);
+        const long points[6] = { 10, 40, size / 3, size / 2, size - 300, size - 1 };
+        const int n_points = game_off ? 4 : 6;
+        for (int k = 0; k < n_points; k++) {
+            FILE* o = fopen(cut, "wb");
+            if (!o) return 7;
+            fwrite(buf, 1, (size_t)points[k], o);
+            fclose(o);
+            if (sft_model_load_qsf(cut, &arena)) return 8;
+        }
+        remove(cut);
+        free(buf);
+    }
     if (!(map ? map_scene_setup(argv[2], &arena) : qsf_scene_setup(argv[2], &arena))) return 4;
     u32* color = (u32*)calloc((size_t)w * h, 4);
     FILE* out = fopen(argv[3], "wb");
