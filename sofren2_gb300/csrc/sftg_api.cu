@@ -400,6 +400,8 @@ struct view_plan {
     uint32_t ss_base, total_ss, tile_base, tiles, prox_base, packet_base, n_packets, stile_base, stiles, scols;
     uint32_t inst_off, bone_off, pl_off, dl_off, tl_off;
     uint64_t vis_base, color_off;
+    uint32_t* direct;   /* the caller's pinned colour buffer, written by the kernels in place; else null */
+    int32_t direct_pitch;   /* its row stride in pixels */
 };
 
 struct batch_bufs {
@@ -451,7 +453,22 @@ static int sample_slot(int S) { return S == 1 ? 0 : (S == 2 ? 1 : 2); }
  * (screen-space cache, batch records, clip pool, tile lists, light_vis, visibility buffers) are
  * laid out view after view, with tiles numbered by sample count first (1, 2, 4) so that each
  * raster/resolve specialisation covers one contiguous tile range. */
-static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds, uint32_t nv, bool want_debug, batch_bufs& B) {
+/* The device-visible address of a caller's colour buffer the kernels can write in place: page-
+ * locked host memory (registered or allocated by CUDA) with a clearing view and a pitch of whole
+ * pixels.  Writes then reach host memory over the chip-to-chip link as the resolve stores them,
+ * and the frame needs no device-to-host copy.  Null for any other buffer (copied as before). */
+static uint32_t* direct_color(const sftg_frame_desc& fd, uint32_t* host, int32_t pitch_bytes) {
+    if (!host || !fd.clear) return nullptr;
+    const size_t pitch = pitch_bytes > 0 ? (size_t)pitch_bytes : (size_t)fd.width * 4;
+    if (pitch % 4 || pitch < (size_t)fd.width * 4) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return (uint32_t*)at.devicePointer;
+}
+
+static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds, uint32_t nv, bool want_debug, batch_bufs& B,
+                       uint32_t* const* host_color = nullptr, const int32_t* pitch_bytes = nullptr) {
     if (!nv || nv > 65535) return set_err(ctx, SFTG_E_ARG, "a batch holds 1 to 65535 views, not %u", nv);
     if (want_debug && nv != 1) return set_err(ctx, SFTG_E_ARG, "debug capture covers single-view submissions only");
     B.plan.assign(nv, view_plan{});
@@ -527,6 +544,8 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
         if (fd->n_instances > max_inst) max_inst = fd->n_instances;
         n_pl += fd->n_point; n_dl += fd->n_dir; n_tl += fd->tlas_count;
         P.color_off = color_total; color_total += (uint64_t)W * H;
+        P.direct = direct_color(*fd, host_color ? host_color[v] : nullptr, pitch_bytes ? pitch_bytes[v] : 0);
+        P.direct_pitch = P.direct ? (pitch_bytes && pitch_bytes[v] > 0 ? pitch_bytes[v] / 4 : W) : W;
     }
     if (max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) > 0xFFFFFFF0ull || total_ss > (1u << 26)) return set_err(ctx, SFTG_E_LIMIT, "batch too large for one submission");
     uint32_t total_tiles = 0;
@@ -650,7 +669,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
         const int W = fd->width, H = fd->height;
         sftg_frame* F = (sftg_frame*)(hs + o_F) + v;
         memset(F, 0, sizeof(*F));
-        F->width = W; F->height = H; F->samples = fd->samples; F->pitch = W;
+        F->width = W; F->height = H; F->samples = fd->samples; F->pitch = P.direct_pitch;
         F->hw = (float)W * 0.5f; F->hh = (float)H * 0.5f; F->vpx = 0.f; F->vpy = 0.f;
         F->cols = (W + 63) / 64; F->rows = (H + 63) / 64; F->tiles = (int32_t)P.tiles; F->debug_mode = (int32_t)fd->debug_mode;
         F->clear = fd->clear; F->clear_color = fd->clear_color; F->shadows = fd->shadows;
@@ -669,7 +688,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
         F->stile_base = P.stile_base; F->scols = P.scols;
         F->view = v; F->ss_base = P.ss_base; F->tile_base = P.tile_base; F->prox_base = P.prox_base;
         F->packet_base = P.packet_base; F->n_packets = P.n_packets; F->vis_base = P.vis_base;
-        F->color_dev = ln.d_color + P.color_off;
+        F->color_dev = P.direct ? P.direct : ln.d_color + P.color_off;
         F->inst = (const sftg_inst*)(ds + o_inst) + P.inst_off;
         F->bones = (const float*)(ds + o_bones) + P.bone_off;
         F->jobs = (const sftg_job*)(ds + o_jobs);
@@ -879,10 +898,10 @@ static int submit_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
         CK(cudaStreamWaitEvent(ln.stream, ctx->ev_upload, 0));
     }
     int rc;
-    if ((rc = build_batch(ctx, ln, fds, nv, dbg != nullptr, B))) return rc;
+    if ((rc = build_batch(ctx, ln, fds, nv, dbg != nullptr, B, host_color, pitch_bytes))) return rc;
     defer_colors = false;
     for (uint32_t v = 0; v < nv; v++)   /* the reference blends over / keeps the caller's pixels */
-        if (!fds[v].clear && host_color && host_color[v]) {
+        if (!fds[v].clear && host_color && host_color[v] && !B.plan[v].direct) {
             defer_colors = true;
             CK(cudaMemcpy2DAsync(ln.d_color + B.plan[v].color_off, (size_t)fds[v].width * 4, host_color[v], pitch_of(v),
                                  (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyHostToDevice, ln.stream));
@@ -892,7 +911,7 @@ static int submit_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
     CK(cudaMemcpyAsync(ln.h_status + 2, B.totals, 12, cudaMemcpyDeviceToHost, ln.stream));
     if (!defer_colors)
         for (uint32_t v = 0; v < nv; v++)
-            if (host_color && host_color[v])
+            if (host_color && host_color[v] && !B.plan[v].direct)
                 CK(cudaMemcpy2DAsync(host_color[v], pitch_of(v), ln.d_color + B.plan[v].color_off, (size_t)fds[v].width * 4,
                                      (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyDeviceToHost, ln.stream));
     CK(cudaEventRecord(ln.ev_done, ln.stream));
@@ -925,7 +944,7 @@ static int finish_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
     if (defer_colors) {
         auto pitch_of = [&](uint32_t v) { return (pitch_bytes && pitch_bytes[v] > 0) ? (size_t)pitch_bytes[v] : (size_t)fds[v].width * 4; };
         for (uint32_t v = 0; v < nv; v++)
-            if (host_color && host_color[v])
+            if (host_color && host_color[v] && !B.plan[v].direct)
                 CK(cudaMemcpy2DAsync(host_color[v], pitch_of(v), ln.d_color + B.plan[v].color_off, (size_t)fds[v].width * 4,
                                      (size_t)fds[v].width * 4, fds[v].height, cudaMemcpyDeviceToHost, ln.stream));
         CK(cudaStreamSynchronize(ln.stream));
@@ -945,7 +964,7 @@ static int finish_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
         if (dbg->shadow && S == 1) CK(cudaMemcpy(dbg->shadow, B.shadow, (size_t)W * H * 16 * 4, cudaMemcpyDeviceToHost));
         if (dbg->status) *dbg->status = ln.h_status[0];
     }
-    if (out_dev) for (uint32_t v = 0; v < nv; v++) out_dev[v] = ln.d_color + B.plan[v].color_off;
+    if (out_dev) for (uint32_t v = 0; v < nv; v++) out_dev[v] = B.plan[v].direct ? B.plan[v].direct : ln.d_color + B.plan[v].color_off;
     if (ln.h_status[0] & 1u) return set_err(ctx, SFTG_E_DEVICE_STATUS, "occlusion traversal exceeded its stack bound");
     return SFTG_OK;
 }

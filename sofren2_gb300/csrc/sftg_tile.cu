@@ -451,6 +451,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     const sftg_clip_tri* clips = A.clips + (F->total_ss ? A.clip_base[(size_t)F->ss_base * 16] : 0u);
     const uint8_t* light_vis = A.light_vis + (size_t)F->prox_base * 64;
     uint32_t* color = F->color_dev;
+    const int CP = F->pitch;   /* colour row stride in pixels (the caller's buffer when written directly) */
     float* shadow_out = A.shadow_out;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
@@ -654,10 +655,10 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
         for (int s = 0; s < S; s++) act |= asm_[s];
         float acc[3] = { 0.f, 0.f, 0.f };
         if (S == 1) {
-            if (F->clear && inb && vids[0] == SFTG_INVALID) color[gy * W + gx] = cc;
+            if (F->clear && inb && vids[0] == SFTG_INVALID) color[gy * CP + gx] = cc;
         } else {
             if (!act) {
-                if (F->clear && inb) color[gy * W + gx] = cc;
+                if (F->clear && inb) color[gy * CP + gx] = cc;
                 continue;
             }
             const float ew = (float)ecount * inv_s;
@@ -666,7 +667,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
             else if (any_e) {
                 float bg[3] = { 0.f, 0.f, 0.f };
                 if (gx < sw && gy < sh) {
-                    const uint32_t q = color[gy * W + gx];
+                    const uint32_t q = color[gy * CP + gx];
                     bg[0] = (float)((q >> 16) & 0xFF) * (1.f / 255.f); bg[1] = (float)((q >> 8) & 0xFF) * (1.f / 255.f); bg[2] = (float)(q & 0xFF) * (1.f / 255.f);
                 }
                 acc[0] = bg[0] * ew; acc[1] = bg[1] * ew; acc[2] = bg[2] * ew;
@@ -927,7 +928,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                     uint32_t px = 0xFF000000u;
 #pragma unroll
                     for (int k = 0; k < 3; k++) px |= ((uint32_t)cvtt(vmax(0.f, vmin(out[k], 1.f)) * 255.f)) << (16 - 8 * k);
-                    color[gy * W + gx] = px;
+                    color[gy * CP + gx] = px;
                 }
             } else {
                 const float wgt = in_tri ? (float)hits * inv_s : 0.f;
@@ -941,7 +942,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                 uint32_t px = 0xFF000000u;
 #pragma unroll
                 for (int k = 0; k < 3; k++) px |= ((uint32_t)cvtt(vmin(acc[k], 1.f) * 255.f)) << (16 - 8 * k);
-                color[gy * W + gx] = px;
+                color[gy * CP + gx] = px;
             }
         }
     }
@@ -1045,7 +1046,6 @@ __global__ void __launch_bounds__(256) k_debug_overlay(const sftg_tile_args A)
     const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
     const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
     uint32_t* color = F->color_dev;
-    const int W = F->width;
     const float2* depth = A.vis + F->vis_base + (size_t)tile * F->samples * SFTG_TILE_PX;   /* sample 0 plane first */
     const float2 zr = A.zrange[gtile];
     const int ntl = A.tile_nlights[gtile];
@@ -1059,7 +1059,7 @@ __global__ void __launch_bounds__(256) k_debug_overlay(const sftg_tile_args A)
     for (int i = threadIdx.x; i < SFTG_TILE_PX; i += blockDim.x) {
         const int x = tmx + (i & (SFTG_TILE - 1)), y = tmy + (i >> 6);
         if (x >= lim_x || y >= lim_y) continue;
-        uint32_t* p = &color[(size_t)y * W + x];
+        uint32_t* p = &color[(size_t)y * F->pitch + x];
         const bool edge = x == tmx || x == lim_x - 1 || y == tmy || y == lim_y - 1;
         if (mode == 2) {
             if (edge) *p = 0xFF00FF00u;
