@@ -319,7 +319,11 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
     tri_setup_packed* setups = (tri_setup_packed*)(smem + (size_t)S * SFTG_TILE_PX * 8);
     uint32_t* items = (uint32_t*)(setups + SETUP_CAP);                     /* set-up index << 8 | slab */
-    __shared__ uint32_t s_nsetup, s_nitems, s_next;
+    __shared__ uint32_t s_nsetup, s_nbig, s_nsmall, s_next;
+    /* work items of a round: long slabs from the front of the array, short ones from the back,
+     * and the queue hands out the long ones first, so that a round does not end on one group
+     * still walking a long slab (items touch keys only through atomicMax: order is free) */
+    const uint32_t items_cap = (uint32_t)SETUP_CAP * (uint32_t)((SFTG_TILE + slab_rows - 1) / slab_rows);
     __shared__ float s_red[2][RASTER_THREADS / 32];
     const uint32_t gtile = A.tile_order[tile0 + blockIdx.x];              /* batch-wide tile index, heaviest first */
     const sftg_frame* F = A.frames + A.tile_view[gtile];
@@ -338,7 +342,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     const int grp_lane = tid & 7;
     const uint32_t gmask = 0xFFu << (lane & ~7);
     for (uint32_t pbase = 0; pbase < count; pbase += SETUP_CAP / 8) {
-        if (tid == 0) { s_nsetup = 0; s_nitems = 0; s_next = 0; }
+        if (tid == 0) { s_nsetup = 0; s_nbig = 0; s_nsmall = 0; s_next = 0; }
         __syncthreads();
         {
             const uint32_t p = pbase + (tid >> 3);
@@ -374,20 +378,26 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
                         const uint32_t slot = atomicAdd(&s_nsetup, 1u);
                         setups[slot] = pack_setup(T, tmx, tmy);
                         const uint32_t nslab = (uint32_t)(T.maxy - T.miny) / (uint32_t)slab_rows + 1u;
-                        const uint32_t ib = atomicAdd(&s_nitems, nslab);
-                        for (uint32_t k = 0; k < nslab; k++) items[ib + k] = (slot << 8) | k;
+                        const int rows = min(T.maxy - T.miny + 1, slab_rows), chunks = (T.ax1 - T.ax0) >> 3;
+                        if (S == 4 || rows * chunks >= 16) {   /* measured: the 4x raster keeps arrival order */
+                            const uint32_t ib = atomicAdd(&s_nbig, nslab);
+                            for (uint32_t k = 0; k < nslab; k++) items[ib + k] = (slot << 8) | k;
+                        } else {
+                            const uint32_t ib = atomicAdd(&s_nsmall, nslab);
+                            for (uint32_t k = 0; k < nslab; k++) items[items_cap - 1u - (ib + k)] = (slot << 8) | k;
+                        }
                     }
                 }
             }
         }
         __syncthreads();
-        const uint32_t nitem = s_nitems;
+        const uint32_t nbig = s_nbig, nitem = nbig + s_nsmall;
         while (true) {
             uint32_t idx = 0;
             if (grp_lane == 0) idx = atomicAdd(&s_next, 1u);
             idx = __shfl_sync(gmask, idx, lane & ~7);
             if (idx >= nitem) break;
-            const uint32_t it = items[idx];
+            const uint32_t it = idx < nbig ? items[idx] : items[items_cap - 1u - (idx - nbig)];
             const tri_setup T = unpack_setup<S>(setups[it >> 8], tmx, tmy);
             const int y0 = T.miny + (int)(it & 0xFFu) * slab_rows;
             const int y1 = min(y0 + slab_rows - 1, T.maxy);
