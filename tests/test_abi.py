@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def _declared(header: str) -> set[str]:
     src = open(os.path.join(ROOT, "include", header)).read()
     src = src.split("#ifdef SFT_IMPL")[0]
-    return set(re.findall(r"^(?:SFT_FUNC|int|void|const char\*)\s+[\w\s\*]*?\b((?:sft|sftg)_\w+)\s*\(", src, re.M))
+    return set(re.findall(r"^(?:SFT_FUNC|int|void|uint64_t|const char\*)\s+[\w\s\*]*?\b((?:sft|sftg)_\w+)\s*\(", src, re.M))
 
 
 @pytest.fixture(scope="module")
@@ -89,3 +89,23 @@ def test_scene_generation_is_platform_independent():
     a = scenes.static_shapes_scene(64, 64, seed=3, n_spheres=2, n_cubes=1, tex_size=16).to_bytes()
     b = scenes.static_shapes_scene(64, 64, seed=3, n_spheres=2, n_cubes=1, tex_size=16).to_bytes()
     assert a == b
+
+
+def test_serve_and_lane_calls_reject_bad_arguments(lib_path):
+    """Argument checks that return before any GPU work: the serving loop without buffers or with
+    an unknown mode, and the lane calls without a context."""
+    lib = C.CDLL(lib_path)
+    lib.sftx_serve.restype = C.c_int
+    lib.sftx_serve.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, C.c_void_p, C.c_uint32,
+                               C.c_void_p, C.c_void_p, C.c_void_p]
+    dummy = (C.c_void_p * 1)()
+    done = (C.c_uint64 * 1)()
+    assert lib.sftx_serve(None, None, 0, 8, 1 << 30, 0, dummy, 8, done, None, None) == -1      # no scenes
+    assert lib.sftx_serve(dummy, None, 0, 8, 1 << 30, 0, None, 8, done, None, None) == -1      # no colours
+    assert lib.sftx_serve(dummy, None, 0, 8, 1 << 30, 0, dummy, 4, done, None, None) == -1     # ring < max_batch
+    assert lib.sftx_serve(dummy, None, 0, 8, 1 << 30, 7, dummy, 8, done, None, None) == -1     # unknown mode
+    for fn, args in (("sftg_frames_submit", (None, 1, None, 1, None, None)), ("sftg_lane_done", (None, 1)),
+                     ("sftg_lane_wait", (None, 1))):
+        f = getattr(lib, fn)
+        f.restype = C.c_int
+        assert f(*args) == -2, fn   # SFTG_E_ARG

@@ -3,6 +3,8 @@ lone render of it produces, whether it was served with batches overlapping on th
 continuous batching over submission lanes), one batch at a time, alone (plain) or under a memory
 budget that forces one request per batch; and batches queued on different submission lanes
 (sft_batch_submit_async) without waiting in between give every view its lone pixels."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -110,3 +112,34 @@ def test_memory_budget_limits_overlapping_batches(renderer, served):
     done, batch, st = renderer.serve(hs, reqs, max_batch=8, budget_bytes=budget, mode="overlap", colors=colors)
     _check(colors, sizes, alone)
     assert st["max_batch"] == 1 and st["max_inflight"] == 1
+
+
+def test_lane_submission_errors(renderer, served):
+    """sftg_frames_submit refuses lane 0 (the synchronous lane), lanes past the last and a lane
+    with a batch in flight; the batch in flight then finishes normally."""
+    hs, reqs, sizes, alone = served
+    lib = renderer.lib
+    lib.sft_batch_peek.restype = C.c_void_p
+    lib.sft_batch_peek.argtypes = [C.c_uint32]
+    lib.sftg_frames_submit.restype = C.c_int
+    lib.sftg_frames_submit.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    lib.sftg_lane_done.restype = C.c_int
+    lib.sftg_lane_done.argtypes = [C.c_void_p, C.c_uint32]
+    lib.sftg_lane_wait.restype = C.c_int
+    lib.sftg_lane_wait.argtypes = [C.c_void_p, C.c_uint32]
+    ctx = lib.sft_get_gpu_context()
+    _, si, f, S, nl, _ = reqs[0]
+    lib.sft_batch_begin()
+    renderer.set_samples(S)
+    assert lib.sftx_scene_render_ex(hs[si], f, None, 0, nl) == 0
+    desc = lib.sft_batch_peek(0)
+    assert desc
+    assert lib.sftg_frames_submit(ctx, 0, desc, 1, None, None) == -2
+    assert lib.sftg_frames_submit(ctx, 8, desc, 1, None, None) == -2
+    assert lib.sftg_frames_submit(ctx, 1, desc, 1, None, None) == 0
+    assert lib.sftg_frames_submit(ctx, 1, desc, 1, None, None) == -2   # busy
+    assert lib.sftg_lane_done(ctx, 1) in (0, 1)
+    assert lib.sftg_lane_wait(ctx, 1) == 0
+    assert lib.sftg_lane_done(ctx, 1) == 1
+    assert lib.sft_batch_submit() == 0   # the recorded frame, rendered on the synchronous lane
+    renderer.set_samples(1)
