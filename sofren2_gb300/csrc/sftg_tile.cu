@@ -341,13 +341,18 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     for (int i = tid; i < S * SFTG_TILE_PX; i += RASTER_THREADS) keys[i] = 0ull;
     const int grp_lane = tid & 7;
     const uint32_t gmask = 0xFFu << (lane & ~7);
-    for (uint32_t pbase = 0; pbase < count; pbase += SETUP_CAP / 8) {
+    /* the payloads in equal rounds of at most SETUP_CAP / 8 (a short last round would leave most
+     * groups idle at its barrier) */
+    const uint32_t rounds = (count + SETUP_CAP / 8 - 1) / (SETUP_CAP / 8);
+    const uint32_t per_round = rounds ? (count + rounds - 1) / rounds : 1u;
+    for (uint32_t pbase = 0; pbase < count; pbase += per_round) {
+        const uint32_t pend = min(count, pbase + per_round);
         if (tid == 0) { s_nsetup = 0; s_nbig = 0; s_nsmall = 0; s_next = 0; }
         __syncthreads();
         {
             const uint32_t p = pbase + (tid >> 3);
             const int l = grp_lane;
-            if (p < count) {
+            if (p < pend) {
                 const uint64_t pay = list[p];
                 const uint32_t raw = (uint32_t)(pay >> 56);
                 float sx[3], sy[3], iw[3];
