@@ -122,17 +122,17 @@ SFTG_D void fetch_tri(const sftg_frame* F, const float* ss, const sftg_clip_tri*
     t.inst = ii; t.m = m;
 }
 
-/* Grows [mn, mx] by the world positions the resolve can interpolate on triangle `vid`.
- * Interpolated positions are convex combinations of the three world vertices, up to the
- * rounding of the barycentrics: at 1x they are not clamped, and a pixel centre inside a sliver
- * can get a weight of about -eps * extent^2 / det.  The box is widened by twice that bound
- * times the triangle's extent, plus a relative margin for the interpolation's own rounding. */
-SFTG_D void tri_bounds_acc(const sftg_frame* F, const float* ss, const sftg_clip_tri* clips, uint32_t vid, float* mn, float* mx) {
-    float X[3][3], sx[3], sy[3];
+/* Grows [mn, mx] by the world position the resolve interpolates on triangle `vid` at pixel
+ * centre (pxf, pyf): the same barycentrics, MSAA clamp, perspective weights and interpolation as
+ * the shading loop (D6 below), so the box holds exactly the points the proxy tests use. */
+template <int S>
+SFTG_D void pixel_pos_acc(const sftg_frame* F, const float* ss, const sftg_clip_tri* clips, uint32_t vid, float pxf, float pyf,
+                          float* mn, float* mx) {
+    float sx[3], sy[3], iw[3], px[3], py[3], pz[3];
     if (vid & 0x80000000u) {
         const sftg_clip_tri* c = &clips[vid & 0x7FFFFFFFu];
 #pragma unroll
-        for (int k = 0; k < 3; k++) { X[0][k] = c->px[k]; X[1][k] = c->py[k]; X[2][k] = c->pz[k]; sx[k] = c->sx[k]; sy[k] = c->sy[k]; }
+        for (int k = 0; k < 3; k++) { sx[k] = c->sx[k]; sy[k] = c->sy[k]; iw[k] = c->iw[k]; px[k] = c->px[k]; py[k] = c->py[k]; pz[k] = c->pz[k]; }
     } else {
         const uint32_t ii = (vid >> 25) & 63, m = (vid >> 7) & 0x3FFFF, tri = vid & 127;
         const sftg_inst* I = &F->inst[ii];
@@ -143,19 +143,28 @@ SFTG_D void tri_bounds_acc(const sftg_frame* F, const float* ss, const sftg_clip
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const uint32_t v = ind[b * 32 + 8 * k + l];
-            X[0][k] = Sc[192 + v]; X[1][k] = Sc[256 + v]; X[2][k] = Sc[320 + v]; sx[k] = Sc[v]; sy[k] = Sc[64 + v];
+            sx[k] = Sc[v]; sy[k] = Sc[64 + v]; iw[k] = Sc[128 + v]; px[k] = Sc[192 + v]; py[k] = Sc[256 + v]; pz[k] = Sc[320 + v];
         }
     }
     const float dx1 = sx[1] - sx[0], dx2 = sx[2] - sx[0], dy1 = sy[1] - sy[0], dy2 = sy[2] - sy[0];
-    const float det = fabsf(dx1 * dy2 - dx2 * dy1);
-    const float ext = fmaxf(fmaxf(fabsf(dx1), fabsf(dx2)), fmaxf(fabsf(dy1), fabsf(dy2))) + 2.f;
-    const float delta = fminf(1e-5f + 4e-6f * (ext * ext) / fmaxf(det, 1e-30f), 1e6f);
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const float lo = fminf(X[a][0], fminf(X[a][1], X[a][2])), hi = fmaxf(X[a][0], fmaxf(X[a][1], X[a][2]));
-        const float e = (hi - lo) * (2.f * delta) + 1e-4f * (fabsf(lo) + fabsf(hi)) + 1e-5f;
-        mn[a] = fminf(mn[a], lo - e); mx[a] = fmaxf(mx[a], hi + e);
+    const float idet = rcpr(dx1 * dy2 - dx2 * dy1);
+    const float pxs = pxf - sx[0], pys = pyf - sy[0];
+    const float rbu = (pxs * dy2 - pys * dx2) * idet;
+    const float rbv = (pys * dx1 - pxs * dy1) * idet;
+    const float rbw = (1.f - rbu) - rbv;
+    float bu = rbu, bv = rbv, bw = rbw;
+    if (S > 1) {
+        bu = vmax(0.f, rbu); bv = vmax(0.f, rbv); bw = vmax(0.f, rbw);
+        const float bs = rcpr(bu + (bv + bw));
+        bu = bu * bs; bv = bv * bs; bw = bw * bs;
     }
+    const float iz = fma_(bw, iw[0], fma_(bu, iw[1], bv * iw[2]));
+    const float z = rcpr(iz);
+    const float w0 = (bw * iw[0]) * z, w1 = (bu * iw[1]) * z, w2 = (bv * iw[2]) * z;
+    const float P[3] = { fma_(w0, px[0], fma_(w1, px[1], w2 * px[2])), fma_(w0, py[0], fma_(w1, py[1], w2 * py[2])),
+                         fma_(w0, pz[0], fma_(w1, pz[1], w2 * pz[2])) };
+#pragma unroll
+    for (int a = 0; a < 3; a++) { mn[a] = fminf(mn[a], P[a]); mx[a] = fmaxf(mx[a], P[a]); }
 }
 
 /* edge / depth setup of one triangle lane (5211-5311), false when culled or off-tile */
@@ -520,7 +529,8 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     const int ntl = s_nlights;
     if (tid < ntl) s_pl[tid] = F->point[s_lights[tid]];   /* read after the barrier that follows D3 */
 
-    /* World bounds of every triangle visible in this quarter tile, for the proxy filter below. */
+    /* World box of every surface point this CTA shades (per covered pixel and distinct sample
+     * triangle, interpolated as the shading loop does), for the proxy filter below. */
     __shared__ float s_bnd[TILE_THREADS / 32][6];
     const int sw = (int)(F->hw * 2.f), sh = (int)(F->hh * 2.f);
     const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
@@ -534,10 +544,12 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
             const int gx = tmx + (blk & 15) * 4 + ix0, gy = tmy + (blk >> 4) * 2 + iy0;
             if (gx >= lim_x || gy >= lim_y) continue;
             const int pind = (gy - tmy) * SFTG_TILE + (gx - tmx);
+            const float pxf = ((float)(gx - ix0) + 0.5f) + (float)ix0, pyf = ((float)(gy - iy0) + 0.5f) + (float)iy0;
+            last = SFTG_INVALID;
 #pragma unroll
             for (int s = 0; s < S; s++) {
                 const uint32_t vid = __float_as_uint(vis[s * SFTG_TILE_PX + pind].y);
-                if (vid != SFTG_INVALID && vid != last) { last = vid; tri_bounds_acc(F, ss, clips, vid, mn, mx); }
+                if (vid != SFTG_INVALID && vid != last) { last = vid; pixel_pos_acc<S>(F, ss, clips, vid, pxf, pyf, mn, mx); }
             }
         }
 #pragma unroll
