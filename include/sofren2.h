@@ -262,9 +262,9 @@ SFT_FUNC const void* sft_batch_peek(u32 i);
 SFT_FUNC i32 sft_batch_autotune(i32 reps);
 SFT_FUNC void* sft_get_gpu_context(void);
 /* extension: overlapping batches.  sft_batch_submit_async ends the batch like sft_batch_submit
- * but queues it on submission lane `lane` (1 to SFTG_MAX_LANES - 1) and returns at once; the
- * colour buffers must stay untouched until sft_batch_wait(lane) returns, which waits for the
- * batch and gives its status.  sft_batch_done(lane) is 1 once the lane's batch has finished
+ * but queues it on submission lane `lane` (1 to SFTG_MAX_LANES - 1) and returns at once (a
+ * batch still on that lane is waited for first); the colour buffers must stay untouched until
+ * sft_batch_wait(lane) returns, which waits for the batch and gives its status.  sft_batch_done(lane) is 1 once the lane's batch has finished
  * (or the lane is idle), 0 while it runs.  Batches on different lanes overlap on the GPU. */
 SFT_FUNC i32 sft_batch_submit_async(u32 lane);
 SFT_FUNC i32 sft_batch_done(u32 lane);
