@@ -46,7 +46,7 @@ CONFIGS = {
     5: dict(gen="config5", samples=None, name="served_16_scenes_poisson", width=None, height=None),
     6: dict(gen="config3", samples=None, name="raycast_atrium_1m_rays", width=None, height=None, rays=1 << 20),
 }
-SERVE_RATES = (100, 500, 1000, 2000, 5000)   # requests/s offered
+SERVE_RATES = (100, 500, 1000, 1500, 2000, 5000)   # requests/s offered
 SERVE_BUDGET = 150 << 30                      # device-memory admission budget, bytes
 
 
@@ -466,8 +466,9 @@ def run_serve(args, cfg) -> dict:
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     top = points[-1]["batched"]
-    # latency headline: the highest offered rate the batched loop still keeps up with
-    kept = [p for p in points if p["batched"]["frames_per_second"] >= 0.97 * p["rate"]] or points[:1]
+    # latency headline: the highest offered rate the serving loop sustains (served at >= 99 % of the
+    # offered rate over the run, so that its queue does not grow)
+    kept = [p for p in points if p["batched"]["frames_per_second"] >= 0.99 * p["rate"]] or points[:1]
     sla = kept[-1]
     line = {
         "metric": "frames_per_second", "value": top["frames_per_second"], "unit": "frames/s", "n_gpus": 1,

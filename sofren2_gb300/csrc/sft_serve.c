@@ -83,7 +83,8 @@ static uint32_t sftx_admit(const sftx_request* reqs, uint32_t n, uint32_t next, 
 }
 
 static int sftx_serve_overlap(void* const* scenes, const sftx_request* reqs, uint32_t n, uint32_t max_batch, uint64_t budget,
-                              uint32_t* const* colors, uint32_t n_colors, uint64_t* done_ns, uint32_t* batch_of, sftx_serve_stats* st) {
+                              uint32_t lanes, uint32_t* const* colors, uint32_t n_colors, uint64_t* done_ns, uint32_t* batch_of,
+                              sftx_serve_stats* st) {
     uint32_t first[SFTG_MAX_LANES] = { 0 }, last[SFTG_MAX_LANES] = { 0 };
     uint64_t lbytes[SFTG_MAX_LANES] = { 0 }, lbatch[SFTG_MAX_LANES] = { 0 };
     int busy[SFTG_MAX_LANES] = { 0 };
@@ -106,7 +107,7 @@ static int sftx_serve_overlap(void* const* scenes, const sftx_request* reqs, uin
             progressed = 1;
         }
         uint32_t lane = 0;
-        for (uint32_t l = 1; l < SFTG_MAX_LANES && !lane; l++) if (!busy[l]) lane = l;
+        for (uint32_t l = 1; l <= lanes && !lane; l++) if (!busy[l]) lane = l;
         const uint64_t now = sftx_now_ns() - t0;
         if (lane && next < n && reqs[next].arrival_ns <= now) {
             uint64_t bytes = 0;
@@ -149,16 +150,18 @@ static int sftx_serve_overlap(void* const* scenes, const sftx_request* reqs, uin
 /* Serves n requests sorted by arrival.  colors[k % n_colors] (pitch: the request's width * 4)
  * receives request k's pixels; n_colors must be at least max_batch (in SFTX_SERVE_OVERLAP, the
  * requests in flight are also limited to n_colors).  done_ns[k] is the completion time of
- * request k from the start of the run, batch_of[k] (optional) its batch. */
-SFTX_EXPORT int sftx_serve(void* const* scenes, const sftx_request* reqs, uint32_t n, uint32_t max_batch, uint64_t budget_bytes,
-                           int mode, uint32_t* const* colors, uint32_t n_colors, uint64_t* done_ns, uint32_t* batch_of,
-                           sftx_serve_stats* stats) {
+ * request k from the start of the run, batch_of[k] (optional) its batch.  In SFTX_SERVE_OVERLAP,
+ * at most `lanes` batches (1 to SFTG_MAX_LANES - 1) are on the GPU at once. */
+SFTX_EXPORT int sftx_serve_ex(void* const* scenes, const sftx_request* reqs, uint32_t n, uint32_t max_batch, uint64_t budget_bytes,
+                              int mode, uint32_t lanes, uint32_t* const* colors, uint32_t n_colors, uint64_t* done_ns,
+                              uint32_t* batch_of, sftx_serve_stats* stats) {
     if (!scenes || (!reqs && n) || !colors || !done_ns || max_batch == 0 || n_colors < max_batch) return -1;
     if (mode != SFTX_SERVE_BATCHED && mode != SFTX_SERVE_PLAIN && mode != SFTX_SERVE_OVERLAP) return -1;
+    if (mode == SFTX_SERVE_OVERLAP && (lanes < 1 || lanes > SFTG_MAX_LANES - 1)) return -1;
     sftx_serve_stats st;
     memset(&st, 0, sizeof(st));
     if (mode == SFTX_SERVE_OVERLAP) {
-        sftx_serve_overlap(scenes, reqs, n, max_batch, budget_bytes, colors, n_colors, done_ns, batch_of, &st);
+        sftx_serve_overlap(scenes, reqs, n, max_batch, budget_bytes, lanes, colors, n_colors, done_ns, batch_of, &st);
         if (stats) *stats = st;
         return st.errors ? -2 : 0;
     }
@@ -196,4 +199,11 @@ SFTX_EXPORT int sftx_serve(void* const* scenes, const sftx_request* reqs, uint32
     }
     if (stats) *stats = st;
     return st.errors ? -2 : 0;
+}
+
+SFTX_EXPORT int sftx_serve(void* const* scenes, const sftx_request* reqs, uint32_t n, uint32_t max_batch, uint64_t budget_bytes,
+                           int mode, uint32_t* const* colors, uint32_t n_colors, uint64_t* done_ns, uint32_t* batch_of,
+                           sftx_serve_stats* stats) {
+    return sftx_serve_ex(scenes, reqs, n, max_batch, budget_bytes, mode, SFTG_MAX_LANES - 1, colors, n_colors, done_ns, batch_of,
+                         stats);
 }

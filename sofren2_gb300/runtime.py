@@ -51,6 +51,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftx_scene_autotune_batch": (i32, [p, p, p, u32, i32]),
         "sftx_scene_render_ex": (i32, [p, u32, p, i32, u32]),
         "sftx_serve": (i32, [p, p, u32, u32, u64, i32, p, u32, p, p, p]),
+        "sftx_serve_ex": (i32, [p, p, u32, u32, u64, i32, u32, p, u32, p, p, p]),
         "sft_get_gpu_context": (p, []), "sftg_get_tuning": (i32, [p, p]), "sftg_set_tuning": (i32, [p, p]),
         "sftg_skeleton_upload": (i32, [p, p, u32, p, u32, p]), "sftg_pose_eval": (i32, [p, p, u32, p, p]),
         "sftg_last_error": (C.c_char_p, [p]), "sftx_scene_model": (p, [p, u32]),
@@ -269,13 +270,14 @@ class Renderer:
     SERVE_MODES = {"batched": 0, "plain": 1, "overlap": 2}
 
     def serve(self, handles: list, requests: list[tuple], max_batch: int, budget_bytes: int, mode,
-              colors: list[np.ndarray]) -> tuple[np.ndarray, np.ndarray, dict]:
+              colors: list[np.ndarray], lanes: int = 7) -> tuple[np.ndarray, np.ndarray, dict]:
         """Runs the native serving loop (sftx_serve) over requests
         [(arrival_s, scene index, frame, samples, max point lights, device bytes)], sorted by
         arrival, in mode "overlap" (continuous batching over submission lanes), "batched" (one
         batch at a time) or "plain" (one request at a time; True and False select "plain" and
         "batched").  colors is the ring of host colour buffers (at least max_batch, each as large
-        as the largest request).  Returns (completion times in s, batch index per request, stats)."""
+        as the largest request; in "overlap", at most `lanes` batches are in flight).  Returns
+        (completion times in s, batch index per request, stats)."""
         if isinstance(mode, bool):
             mode = "plain" if mode else "batched"
         n = len(requests)
@@ -287,7 +289,7 @@ class Renderer:
         done = np.zeros(max(1, n), np.uint64)
         batch = np.zeros(max(1, n), np.uint32)
         st = SftxServeStats()
-        rc = self.lib.sftx_serve(hs, reqs, n, max_batch, budget_bytes, self.SERVE_MODES[mode], cp, len(colors), _ptr(done),
+        rc = self.lib.sftx_serve_ex(hs, reqs, n, max_batch, budget_bytes, self.SERVE_MODES[mode], lanes, cp, len(colors), _ptr(done),
                                  _ptr(batch), C.byref(st))
         self.lib.sft_set_msaa_samples(self.samples)
         if rc != 0:
