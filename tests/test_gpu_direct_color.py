@@ -66,3 +66,23 @@ def test_pinned_and_pageable_views_in_one_batch(renderer):
     finally:
         for h in hs:
             renderer.free_scene(h)
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3, 4, 5])
+def test_debug_views_into_pinned_buffer(renderer, mode):
+    """The debug views (the overlays read and blend the colour in place) give the same pixels
+    in a page-locked buffer with a padded pitch as through the copy path."""
+    h = renderer.load_scene(gc.blob("variety"))
+    try:
+        renderer.set_debug_mode(mode)
+        for S in (1, 4):
+            renderer.set_samples(S)
+            w, hh = renderer.frame_size(h, 0)
+            ref = renderer.render(h, 0)
+            keep, buf = _pinned(hh, w, 16)
+            got = renderer.render(h, 0, buf[:, :w])
+            assert np.array_equal(got, ref), f"debug view {mode} at {S}x differs in a pinned buffer"
+    finally:
+        renderer.set_debug_mode(0)
+        renderer.set_samples(1)
+        renderer.free_scene(h)

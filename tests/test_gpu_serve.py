@@ -143,3 +143,15 @@ def test_lane_submission_errors(renderer, served):
     assert lib.sftg_lane_done(ctx, 1) == 1
     assert lib.sft_batch_submit() == 0   # the recorded frame, rendered on the synchronous lane
     renderer.set_samples(1)
+
+
+def test_overlap_into_pinned_buffers(renderer, served):
+    """Batches in flight on several lanes, each writing its frames straight into page-locked
+    request buffers: every request still gets its lone pixels."""
+    torch = pytest.importorskip("torch")
+    hs, reqs, sizes, alone = served
+    big = max(w * h for w, h in sizes)
+    keep = [torch.zeros(big, dtype=torch.int32).pin_memory() for _ in reqs]
+    colors = [t.numpy().view(np.uint32) for t in keep]
+    done, batch, st = renderer.serve(hs, reqs, max_batch=4, budget_bytes=1 << 40, mode="overlap", colors=colors)
+    _check(colors, sizes, alone)
