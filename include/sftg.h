@@ -64,6 +64,8 @@ typedef struct sftg_model_desc {
     uint32_t bone_count;
     const void* blas_nodes;    /* sft_bvh_node images, 256 B each */
     uint32_t blas_count, blas_root;
+    uint32_t build_blas;       /* 1 with no blas_nodes: build the BLAS on the device at upload,
+                                  sft__blas_build_model (sofren2.c:3526-3617) */
 } sftg_model_desc;
 
 typedef struct sftg_instance_desc {
@@ -118,6 +120,10 @@ int sftg_texture_upload(sftg_ctx* ctx, const uint32_t* texels, uint64_t n_texels
 int sftg_texture_update_desc(sftg_ctx* ctx, int32_t index, const sftg_texture_desc* desc_or_null);
 int sftg_material_set(sftg_ctx* ctx, int32_t index, int32_t texture, uint32_t base_color, float shininess);
 int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* desc, int32_t* out_model);
+/* A resident model's BLAS: node count and root index, and `count` node images from `first`
+ * copied into `dst` (256 B each) when dst is not NULL.  Replaces reading sft_model.blas_nodes
+ * (sofren2.c:1107-1108) for a BLAS that was built on the device. */
+int sftg_model_blas(sftg_ctx* ctx, int32_t model, uint32_t first, uint32_t count, void* dst, uint32_t* out_count, uint32_t* out_root);
 /* A model for one frame only: the geometry of the reference's dynamic meshes (sft_dmesh_*,
  * sofren2.c:8720-8951), which lives in its per-frame scratch arena.  sftg_transient_reset drops
  * every transient model uploaded since the last reset (after the frames that draw them);
@@ -250,6 +256,9 @@ int sftg_lane_done(sftg_ctx* ctx, uint32_t lane);
 int sftg_lane_wait(sftg_ctx* ctx, uint32_t lane);
 /* Kernels launched by every batch finished so far, on all lanes (a running total). */
 uint64_t sftg_launch_total(const sftg_ctx* ctx);
+/* Wall time in ms of the last BLAS built on the device at model upload (query and build; no
+ * counterpart in the reference, whose build is host code), and its triangle count. */
+double sftg_last_blas_build(const sftg_ctx* ctx, uint32_t* out_items);
 
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);

@@ -220,8 +220,8 @@ SFT_FUNC void sft_arena_commit_if_needed(sft_arena* arena, u64 required_bytes);
 SFT_FUNC void sft_arena_frame_begin(sft_arena* arena);
 
 /* extension: build a model from meshlet data (the reference's loaders produce the same
- * arrays, sofren2.c:6918-7045); builds the BLAS like sft__blas_build_model (3526-3617) and
- * uploads everything to the GPU.  lightmaps are texture handles indexed by lightmap_page. */
+ * arrays, sofren2.c:6918-7045); uploads everything to the GPU and builds the BLAS there like
+ * sft__blas_build_model (3526-3617).  lightmaps are texture handles indexed by lightmap_page. */
 SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count, const sft_shadow_proxy* proxies,
                                      u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
                                      sft_arena* arena);
@@ -530,7 +530,8 @@ SFT_FUNC void sft_arena_frame_begin(sft_arena* arena) { arena->offset = 0; }
 
 /* ---------------------------------------------------------------- BVH build (sofren2.c:2895-3062)
  * The TLAS is rebuilt every frame on the host exactly as the reference does, so the proxy
- * occlusion traversal visits the same nodes; the BLAS uses the same builder at model creation. */
+ * occlusion traversal visits the same nodes.  A model's BLAS is built by the same steps on the
+ * device at upload (sftg_blas.cu). */
 static void sft__sort_items(sft__item* it, i32 count, int axis) {
     if (count <= 1) return;
     const f32 pivot = it[count / 2].c[axis];
@@ -1126,59 +1127,35 @@ static sft_model* sft__model_create(const sft_mesh_data* meshes, u32 mesh_count,
     m->proxy_count = proxy_count;
     m->proxies = (sft_shadow_proxy*)calloc(proxy_count + 1, sizeof(sft_shadow_proxy));
     if (proxy_count) memcpy(m->proxies, proxies, proxy_count * sizeof(sft_shadow_proxy));
-    /* BLAS over every non-padding triangle, in meshlet / batch / lane order (sofren2.c:3526-3617) */
-    u32 ntri = 0;
-    if (blas_nodes && blas_count) {   /* prebuilt (a QSF2 file carries its BLAS) */
+    /* BLAS over every non-padding triangle, in meshlet / batch / lane order (sofren2.c:3526-3617):
+     * taken from the caller (a QSF2 file carries its BLAS) or built on the device at upload */
+    if (blas_nodes && blas_count) {
         m->blas = (sft__node*)calloc(blas_count + 1, sizeof(sft__node));
         memcpy(m->blas, blas_nodes, (size_t)blas_count * sizeof(sft__node));
         m->blas_count = blas_count; m->blas_root = blas_root;
-    } else {
-    for (u32 k = 0; k < mesh_count; k++)
-        for (u32 j = 0; j < meshes[k].meshlet_count; j++) {
-            const u8* in = meshes[k].inds + (size_t)j * 512;
-            for (u32 t = 0; t < 128; t++) { const u32 b = t >> 3, l = t & 7; if (!(in[b * 32 + l] == in[b * 32 + 8 + l] && in[b * 32 + 8 + l] == in[b * 32 + 16 + l])) ntri++; }
-        }
-    }
-    if (ntri) {
-        sft__item* it = (sft__item*)malloc(ntri * sizeof(sft__item));
-        u32 q = 0;
-        for (u32 k = 0; k < mesh_count; k++)
-            for (u32 j = 0; j < meshes[k].meshlet_count; j++) {
-                const u8* in = meshes[k].inds + (size_t)j * 512;
-                const f32* at = meshes[k].attr + (size_t)j * 640;
-                const u32 g = m->mesh_first[k] + j;
-                for (u32 t = 0; t < 128; t++) {
-                    const u32 b = t >> 3, l = t & 7;
-                    const u32 i0 = in[b * 32 + l], i1 = in[b * 32 + 8 + l], i2 = in[b * 32 + 16 + l];
-                    if (i0 == i1 && i1 == i2) continue;
-                    sft__item* o = &it[q++];
-                    for (int a = 0; a < 3; a++) {
-                        const f32 p0 = at[a * 64 + i0], p1 = at[a * 64 + i1], p2 = at[a * 64 + i2];
-                        const f32 m12 = p1 < p2 ? p1 : p2, x12 = p1 > p2 ? p1 : p2;
-                        o->mn[a] = p0 < m12 ? p0 : m12; o->mx[a] = p0 > x12 ? p0 : x12;
-                        o->c[a] = (o->mn[a] + o->mx[a]) * 0.5f;
-                    }
-                    o->id = (g << 7) | t;
-                }
-            }
-        m->blas = (sft__node*)calloc((size_t)ntri * 2 + 1, sizeof(sft__node));
-        m->blas_root = sft__bvh_build(it, ntri, m->blas, &m->blas_count, NULL, NULL);
-        free(it);
-    }
-    if (m->blas_count) {
-        const sft__node* root = &m->blas[m->blas_root];
-        for (int a = 0; a < 3; a++) { m->root_min[a] = 1e30f; m->root_max[a] = -1e30f; }
-        for (u32 c = 0; c < root->count; c++)
-            for (int a = 0; a < 3; a++) {
-                if (root->mn[a][c] < m->root_min[a]) m->root_min[a] = root->mn[a][c];
-                if (root->mx[a][c] > m->root_max[a]) m->root_max[a] = root->mx[a][c];
-            }
     }
     sftg_model_desc d; memset(&d, 0, sizeof(d));
     d.mesh_count = mesh_count; d.meshes = md; d.bone_count = bone_count;
     d.blas_nodes = m->blas; d.blas_count = m->blas_count; d.blas_root = m->blas_root;
+    d.build_blas = m->blas ? 0u : 1u;
     sft__check(sftg_model_upload(sft__s->gpu, &d, &m->device_id), "model upload");
     free(md);
+    sft__node root;
+    memset(&root, 0, sizeof(root));
+    if (!m->blas) {   /* node images stay on the device; sft_model_get_blas reads them back */
+        sft__check(sftg_model_blas(sft__s->gpu, m->device_id, 0, 0, NULL, &m->blas_count, &m->blas_root), "BLAS query");
+        if (m->blas_count) sft__check(sftg_model_blas(sft__s->gpu, m->device_id, m->blas_root, 1, &root, NULL, NULL), "BLAS root read");
+    } else if (m->blas_count) {
+        root = m->blas[m->blas_root];
+    }
+    if (m->blas_count) {   /* the model's box from the BLAS root slots, for the TLAS */
+        for (int a = 0; a < 3; a++) { m->root_min[a] = 1e30f; m->root_max[a] = -1e30f; }
+        for (u32 c = 0; c < root.count; c++)
+            for (int a = 0; a < 3; a++) {
+                if (root.mn[a][c] < m->root_min[a]) m->root_min[a] = root.mn[a][c];
+                if (root.mx[a][c] > m->root_max[a]) m->root_max[a] = root.mx[a][c];
+            }
+    }
     return m;
 }
 /* sft_model_load_qsf (sofren2.c:7816-7967): a QSF2 file's textures (each becomes a white
@@ -1287,6 +1264,11 @@ SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model) { return model 
 SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, u32* out_root) {
     if (out_count) *out_count = model ? model->blas_count : 0;
     if (out_root) *out_root = model ? model->blas_root : 0;
+    if (model && !model->blas && model->blas_count) {   /* built on the device: read once, keep */
+        sft_model* mm = (sft_model*)model;
+        mm->blas = (sft__node*)calloc((size_t)model->blas_count + 1, sizeof(sft__node));
+        if (sftg_model_blas(sft__s->gpu, model->device_id, 0, model->blas_count, mm->blas, NULL, NULL)) { free(mm->blas); mm->blas = NULL; }
+    }
     return model ? model->blas : NULL;
 }
 

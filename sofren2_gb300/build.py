@@ -22,7 +22,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libsofren2_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["sftg_geom.cu", "sftg_tile.cu", "sftg_occl.cu", "sftg_pose.cu", "sftg_ray.cu", "sftg_api.cu"]
+CU_SOURCES = ["sftg_geom.cu", "sftg_tile.cu", "sftg_occl.cu", "sftg_pose.cu", "sftg_ray.cu", "sftg_blas.cu", "sftg_api.cu"]
 C_SOURCES = ["sft_lib.c", "sft_scene.c", "sft_serve.c"]
 
 

@@ -25,6 +25,7 @@
 #include <string.h>
 #include <algorithm>
 #include <vector>
+#include <chrono>
 
 #include "../../include/sftg.h"
 #include "sftg_types.h"
@@ -98,6 +99,8 @@ struct sftg_ctx {
     float timings[5] = { 0, 0, 0, 0, 0 };
     int launches = 0;
     uint64_t launch_total = 0;                 /* kernels of every finished batch, on all lanes */
+    double blas_ms = 0.0;                      /* wall time of the last device BLAS build */
+    uint32_t blas_items = 0;                   /* and its triangle count */
     bool use_graphs = true;
     sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
     /* transient models (one frame's dynamic meshes): pool marks where they start */
@@ -305,7 +308,7 @@ static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_mo
     md.total_meshlets = total;
     md.bone_count = d->bone_count;
     md.mesh_count = d->mesh_count;
-    md.blas_base = ctx->n_blas; md.blas_root = d->blas_root; md.blas_count = d->blas_count;
+    md.blas_base = ctx->n_blas; md.blas_root = d->blas_nodes ? d->blas_root : 0; md.blas_count = d->blas_nodes ? d->blas_count : 0;
     int rc;
     /* meshlet pools are indexed by meshlet, so they append at exact element offsets */
     if ((rc = pool_reserve(ctx, ctx->ml_attr, ((size_t)ctx->n_meshlets + total) * 2560))) return rc;
@@ -329,13 +332,33 @@ static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_mo
         ctx->skin_j.size = ((size_t)ctx->n_skin + nskin) * 512;
         ctx->skin_w.size = ((size_t)ctx->n_skin + nskin) * 256;
     }
-    if (d->blas_count) {
+    if (d->blas_count && d->blas_nodes) {
         if ((rc = pool_reserve(ctx, ctx->blas, ((size_t)ctx->n_blas + d->blas_count) * 256))) return rc;
         CK(cudaMemcpyAsync((char*)ctx->blas.ptr + (size_t)ctx->n_blas * 256, d->blas_nodes, (size_t)d->blas_count * 256, cudaMemcpyHostToDevice, ctx->stream));
         ctx->blas.size = ((size_t)ctx->n_blas + d->blas_count) * 256;
+    } else if (d->build_blas && total) {   /* built from the meshlets just uploaded */
+        md.blas_count = 0; md.blas_root = 0;
+        sftg_blas_job* job = nullptr;
+        uint32_t n_items = 0, n_nodes = 0, status = 0;
+        const auto t0 = std::chrono::steady_clock::now();
+        cudaError_t e = sftg_blas_begin(&job, (const float*)((const char*)ctx->ml_attr.ptr + (size_t)ctx->n_meshlets * 2560),
+                                        (const uint8_t*)ctx->ml_inds.ptr + (size_t)ctx->n_meshlets * 512, total, ctx->stream, &n_items, &n_nodes);
+        if (e == cudaSuccess && n_nodes) {
+            if ((rc = pool_reserve(ctx, ctx->blas, ((size_t)ctx->n_blas + n_nodes) * 256))) { sftg_blas_end(job); return rc; }
+            e = sftg_blas_finish(job, (sftg_bvh_node*)((char*)ctx->blas.ptr + (size_t)ctx->n_blas * 256), &status);
+            if (e == cudaSuccess && !status) {
+                ctx->blas.size = ((size_t)ctx->n_blas + n_nodes) * 256;
+                md.blas_count = n_nodes;
+            }
+        }
+        sftg_blas_end(job);
+        ctx->blas_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        ctx->blas_items = n_items;
+        if (e != cudaSuccess) return set_err(ctx, SFTG_E_CUDA, "BLAS build: %s", cudaGetErrorString(e));
+        if (status) return set_err(ctx, SFTG_E_DEVICE_STATUS, "BLAS build: a device work list overflowed");
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    ctx->n_meshlets += total; ctx->n_skin += nskin; ctx->n_blas += d->blas_count;
+    ctx->n_meshlets += total; ctx->n_skin += nskin; ctx->n_blas += md.blas_count;
     ctx->h_models.push_back(md);
     if (ctx->h_job_tmpl.size() >= ctx->h_models.size()) ctx->h_job_tmpl[ctx->h_models.size() - 1].jw = 0;   /* id reused */
     ctx->h_mesh_skinned.push_back(mesh_sk);
@@ -348,6 +371,20 @@ static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_mo
 
 extern "C" int sftg_model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model) {
     return model_upload(ctx, d, out_model, false);
+}
+
+extern "C" int sftg_model_blas(sftg_ctx* ctx, int32_t model, uint32_t first, uint32_t count, void* dst, uint32_t* out_count, uint32_t* out_root) {
+    if (!ctx || model < 0 || (size_t)model >= ctx->h_models.size()) return SFTG_E_ARG;
+    const sftg_model& md = ctx->h_models[model];
+    if (out_count) *out_count = md.blas_count;
+    if (out_root) *out_root = md.blas_root;
+    if (!dst || !count) return SFTG_OK;
+    if (first > md.blas_count || count > md.blas_count - first)
+        return set_err(ctx, SFTG_E_ARG, "nodes %u..%u of a BLAS of %u", first, first + count, md.blas_count);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(dst, (const char*)ctx->blas.ptr + ((size_t)md.blas_base + first) * 256, (size_t)count * 256, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SFTG_OK;
 }
 
 extern "C" int sftg_model_upload_transient(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_model) {
@@ -1326,6 +1363,10 @@ extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {
 
 extern "C" int sftg_last_launch_count(const sftg_ctx* ctx) { return ctx ? ctx->launches : 0; }
 extern "C" uint64_t sftg_launch_total(const sftg_ctx* ctx) { return ctx ? ctx->launch_total : 0; }
+extern "C" double sftg_last_blas_build(const sftg_ctx* ctx, uint32_t* out_items) {
+    if (out_items) *out_items = ctx ? ctx->blas_items : 0;
+    return ctx ? ctx->blas_ms : 0.0;
+}
 
 extern "C" void* sftg_stream(const sftg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 

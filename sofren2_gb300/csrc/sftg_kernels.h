@@ -96,6 +96,14 @@ struct sftg_pose_tables {
 };
 void sftg_launch_raycast(const sftg_ray* rays, uint32_t n, const sftg_model* models, uint32_t n_models, const sftg_bvh_node* blas,
                          const float* ml_attr, const uint8_t* ml_inds, sftg_ray_hit* hits, cudaStream_t st);
+/* BLAS construction on the device (sftg_blas.cu): begin counts the model's triangles and lays
+ * out the tree's shape (node count known on return), finish builds the node images into dst
+ * (status 1: a device work list overflowed), end releases the job. */
+struct sftg_blas_job;
+cudaError_t sftg_blas_begin(sftg_blas_job** out, const float* attr, const uint8_t* inds, uint32_t nm, cudaStream_t st,
+                            uint32_t* n_items, uint32_t* n_nodes);
+cudaError_t sftg_blas_finish(sftg_blas_job* job, sftg_bvh_node* dst, uint32_t* status);
+void sftg_blas_end(sftg_blas_job* job);
 void sftg_launch_pose(const sftg_pose_tables& T, const sftg_pose_request* reqs, const uint32_t* out_off, uint32_t n, float* posed,
                       float* global, cudaStream_t st);
 

@@ -60,6 +60,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sft_batch_begin": (v, []), "sft_batch_submit": (i32, []), "sft_batch_submit_async": (i32, [u32]),
         "sft_batch_done": (i32, [u32]), "sft_batch_wait": (i32, [u32]),
         "sftx_scene_render_lanes": (i32, [p, p, p, u32, p, p, u32]), "sftg_launch_total": (u64, [p]),
+        "sft_model_get_blas": (p, [p, p, p]), "sftg_last_blas_build": (C.c_double, [p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -374,6 +375,24 @@ class Renderer:
         if not p:
             raise ValueError(f"scene has no model {mi}")
         return C.c_int32.from_address(p).value
+
+    def last_blas_build(self) -> tuple[float, int]:
+        """(wall ms, triangles) of the last BLAS built on the device at model creation."""
+        n = C.c_uint32(0)
+        ms = self.lib.sftg_last_blas_build(self.lib.sft_get_gpu_context(), C.byref(n))
+        return float(ms), int(n.value)
+
+    def model_blas(self, h, mi: int) -> tuple[bytes, int]:
+        """(node images, root index) of model mi of scene h through sft_model_get_blas: the BLAS
+        the device built at model creation, read back."""
+        p = self.lib.sftx_scene_model(h, mi)
+        if not p:
+            raise ValueError(f"scene has no model {mi}")
+        n, root = C.c_uint32(0), C.c_uint32(0)
+        nodes = self.lib.sft_model_get_blas(p, C.byref(n), C.byref(root))
+        if n.value and not nodes:
+            raise RuntimeError("BLAS read-back failed: " + (self.lib.sft_get_last_error() or b"").decode())
+        return (C.string_at(nodes, n.value * 256) if n.value else b""), int(root.value)
 
     def raycast_host(self, rays: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
         """sftg_raycast on host arrays of RAY_DTYPE records whose `model` is a resident model id;

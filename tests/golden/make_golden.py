@@ -50,6 +50,15 @@ def main(names: list[str]) -> None:
             dbg[f"{name}/{mode}/{S}"] = gc.sha(frame["color"])
             print("debug", name, mode, S, flush=True)
         golden["debug_views"] = dbg
+    if not names or "blas" in names:
+        # every model's BLAS node images as the reference builds them (the harness's blas
+        # sections), for the golden cases and the BLAS edge models
+        bl = {}
+        for name in gc.BLAS_CASES:
+            frame = reference_dump(gc.blas_blob(name), 1, frame=0)[0]
+            bl[name] = {"nodes": [len(b) // 256 for b in frame["blas"]], "sha256": [gc.sha(b) for b in frame["blas"]]}
+            print("blas", name, bl[name]["nodes"], flush=True)
+        golden["blas"] = bl
     if not names or "pose" in names:
         # sft_pose_update of the reference on a seeded rig (oracle/pose_harness.c)
         from oracle_lib import pose_blob, reference_pose

@@ -113,6 +113,65 @@ def rays(name: str, n: int = N_RAYS, seed: int = 0):
     return out
 
 
+# BLAS builds (sft__blas_build_model, sofren2.c:3526-3617) checked model by model: every case's
+# models and the edge models of blas_edge_scene
+BLAS_CASES = list(CASES) + ["blas_edges"]
+
+
+def blas_edge_scene():
+    """Models at the edges of the BLAS builder (sofren2.c:2895-3062): 5 triangles (one leaf),
+    9 (one split), one triangle repeated 3000 times (every centroid equal), 6000 triangles on a
+    lattice in the plane z = 1 (no z extent, equal coordinates along x and y), three meshes of
+    5, 130 and 7 triangles (padding inside the model's meshlet run), and 60000 triangles with
+    coordinates on a 1/64 grid (ranges longer than one shared-memory sort, with ties)."""
+    key = ("blas_edges",)
+    if key in _cache:
+        return _cache[key]
+    sc = scenes.Scene()
+    mat = sc.add_material(sc.add_texture(np.full((4, 4), 0xFFFFFFFF, np.uint32)))
+    rng = np.random.default_rng(2967)
+
+    def raw(pos, tris):
+        pos = np.asarray(pos, np.float32).reshape(-1, 3)
+        nrm = np.tile(np.float32([0, 0, 1]), (len(pos), 1))
+        return scenes.RawMesh(pos, nrm, np.zeros((len(pos), 2), np.float32), tris)
+
+    def soup(n, grid=None):
+        p = rng.uniform(-4, 4, (n, 3)).astype(np.float32)
+        e = rng.uniform(-0.3, 0.3, (n, 2, 3)).astype(np.float32)
+        v = np.concatenate([p[:, None], p[:, None] + e], axis=1).reshape(-1, 3)
+        if grid:
+            v = (np.round(v * grid) / grid).astype(np.float32)
+        return raw(v, np.arange(3 * n).reshape(-1, 3))
+
+    def add(meshes):
+        ms = [scenes.build_meshlets(m) for m in meshes]
+        sc.add_model(scenes.Model(ms, [mat] * len(ms)))
+
+    add([soup(5)])
+    add([soup(9)])
+    add([raw([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.zeros((3000, 3), np.int64) + np.arange(3))])
+    g = np.stack(np.meshgrid(np.arange(41), np.arange(41), indexing="ij"), -1).reshape(-1, 2).astype(np.float32) * 0.25
+    lat = np.concatenate([g, np.ones((len(g), 1), np.float32)], 1)
+    q = np.array([[i * 41 + j, (i + 1) * 41 + j, i * 41 + j + 1] for i in range(40) for j in range(40)]
+                 + [[(i + 1) * 41 + j + 1, i * 41 + j + 1, (i + 1) * 41 + j] for i in range(40) for j in range(40)])
+    add([raw(lat, np.concatenate([q, q[: 6000 - len(q)]]) if len(q) < 6000 else q[:6000])])
+    add([soup(5), soup(130), soup(7)])
+    add([soup(60000, grid=64)])
+    sc.frames.append(scenes._camera_frame(64, 64))
+    _cache[key] = sc
+    return sc
+
+
+def blas_blob(name: str) -> bytes:
+    if name == "blas_edges":
+        key = ("blob", name)
+        if key not in _cache:
+            _cache[key] = blas_edge_scene().to_bytes()
+        return _cache[key]
+    return blob(name)
+
+
 def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def _declared(header: str) -> set[str]:
     src = open(os.path.join(ROOT, "include", header)).read()
     src = src.split("#ifdef SFT_IMPL")[0]
-    return set(re.findall(r"^(?:SFT_FUNC|int|void|uint64_t|const char\*)\s+[\w\s\*]*?\b((?:sft|sftg)_\w+)\s*\(", src, re.M))
+    return set(re.findall(r"^(?:SFT_FUNC|int|void|uint64_t|double|const char\*)\s+[\w\s\*]*?\b((?:sft|sftg)_\w+)\s*\(", src, re.M))
 
 
 @pytest.fixture(scope="module")
