@@ -45,6 +45,7 @@ CONFIGS = {
     4: dict(gen="config4", samples=None, name="multiview_96_views_6_scenes", width=None, height=None),
     5: dict(gen="config5", samples=None, name="served_16_scenes_poisson", width=None, height=None),
     6: dict(gen="config3", samples=None, name="raycast_atrium_1m_rays", width=None, height=None, rays=1 << 20),
+    7: dict(gen="config3", samples=None, name="blas_build_atrium_249k_triangles", width=None, height=None, model=0),
 }
 SERVE_RATES = (100, 500, 1000, 1500, 2000, 5000)   # requests/s offered
 SERVE_BUDGET = 150 << 30                      # device-memory admission budget, bytes
@@ -589,6 +590,116 @@ def run_raycast(args, cfg) -> dict:
     return line if rank == 0 else None
 
 
+def blas_scene(cfg):
+    """The model whose BLAS is built (the atrium of the atrium scene: 7785 meshlets, 249120
+    triangles), alone in a scene with one plain material, so creating it is meshlet upload and
+    BLAS build only."""
+    from sofren2_gb300 import scenes
+    src = getattr(scenes, cfg["gen"])().models[cfg["model"]]
+    sc = scenes.Scene()
+    mat = sc.add_material(sc.add_texture(np.full((4, 4), 0xFFFFFFFF, np.uint32)))
+    sc.add_model(scenes.Model(src.meshes, [mat] * len(src.meshes)))
+    sc.frames.append(scenes._camera_frame(64, 64))
+    return sc
+
+
+def run_blas(args, cfg) -> dict:
+    """BLAS construction (sft__blas_build_model) on the device, one build per step.  `value`:
+    triangles/s over the build's span on the upload stream between two CUDA events (meshlets
+    already resident: the build starts after their upload has finished).  `e2e`: sft_model_create
+    from host meshlet arrays (scene load: meshlet upload + build + root read-back), wall clock
+    around the synchronous call, which returns with the model resident."""
+    import torch
+    import torch.distributed as dist
+    from sofren2_gb300 import runtime
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    os.environ["SFT_CUDA_DEVICE"] = str(local)
+    sc = blas_scene(cfg)
+    blob = sc.to_bytes()
+    ms = sc.models[0].meshes
+    n_meshlets = sum(m.n for m in ms)
+    R = runtime.Renderer(64, 64, 1)
+    for _ in range(args.warmup):
+        R.free_scene(R.load_scene(blob))
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream_ms, wall_ms, build_wall = [], [], []
+    st = {}
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        h = R.load_scene(blob)
+        wall_ms.append(1e3 * (time.perf_counter() - t0))
+        st = R.last_blas_build()
+        stream_ms.append(st["stream_ms"])
+        build_wall.append(st["wall_ms"])
+        R.free_scene(h)
+    clk = clocks.stop()
+    ms_dev, ms_e2e = max_over_ranks([float(np.sum(stream_ms)), float(np.sum(wall_ms))], device=f"cuda:{local}")
+    tris = st["triangles"]
+    h = R.load_scene(blob)
+    n_nodes = len(R.model_blas(h, 0)[0]) // 256
+    R.free_scene(h)
+    peaks = _peaks()
+    alg = n_meshlets * (2560 + 512) + n_nodes * 256
+    per_build = float(np.mean(stream_ms))
+    achieved = alg / (per_build * 1e-3) / 1e9
+    line = {
+        "metric": "triangles_per_second", "value": job_throughput(args.steps * tris, world, ms_dev), "unit": "triangles/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the seeded atrium model)",
+        "config": {"workload": cfg["name"], "meshlets": n_meshlets, "triangles": tris, "nodes": n_nodes,
+                   "l2": "inputs of 24 MB written by the upload just before each build (L2-resident, as at model creation)",
+                   "parallelism": f"replicas x{world}", "host_wall_ms_per_build": float(np.mean(build_wall))},
+        "e2e": {"value": job_throughput(args.steps * tris, world, ms_e2e), "unit": "triangles/s",
+                "h2d_bytes_per_step": int(n_meshlets * (2560 + 512 + 32)), "d2h_bytes_per_step": 256},
+        "gpu_launches": int(st["launches"]) * args.steps,
+        "roofline": {"kernel": "BLAS build (all kernels)", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None, "algorithmic_bytes": alg,
+                     "peak_source": peaks["src"],
+                     "note": "latency bound: 15 dependent sort levels and host reads of the work-list counters; "
+                             "algorithmic bytes are the meshlet positions and indices read and the node images written"},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = blas_cpu_baseline(blob, tris, seconds=args.cpu_seconds)
+    R.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def blas_cpu_baseline(blob: bytes, tris: int, seconds: float = 12.0) -> dict:
+    """The oracle's restated BLAS builder (the reference's recursive build, one thread) on the
+    same model, repeated until `seconds` have passed."""
+    from oracle_lib import Oracle, build_oracle
+    build_oracle()
+    o = Oracle(blob)
+    times = []
+    try:
+        t_end = time.perf_counter() + seconds
+        while time.perf_counter() < t_end or len(times) < 2:
+            t0 = time.perf_counter()
+            o.blas_rebuild(0, 1)
+            times.append(time.perf_counter() - t0)
+            if len(times) >= 500:
+                break
+    finally:
+        o.close()
+    return {"value": tris * len(times) / sum(times), "unit": "triangles/s", "cores": 1, "kind": "port",
+            "sample": f"{len(times)} builds of the same model (oracle/sft_oracle.c blas_build, one thread, as the "
+                      "reference builds at load time on the calling thread)"}
+
+
 def raycast_cpu_baseline(blob: bytes, rays: np.ndarray, seconds: float = 12.0, chunk: int = 1 << 15) -> dict:
     """The oracle's scalar sft_raycast_instance restatement on one host core, over consecutive
     chunks of the same rays until `seconds` have passed."""
@@ -666,6 +777,29 @@ def run_reference(args, cfg) -> dict | None:
                                  "sample": f"{len(times)} steps of {chunk} rays after {max(1, args.warmup)} warm-up, scalar "
                                            "restatement of sft_raycast_instance (oracle/sft_oracle.c), one thread"},
                 "e2e": {"value": rps, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.config == 7:   # each step one build of the same model
+        sc = blas_scene(cfg)
+        o = Oracle(sc.to_bytes())
+        tris = sum(int(m.tri_count.sum()) for m in sc.models[0].meshes)
+        times = []
+        try:
+            for k in range(max(1, args.warmup) + args.steps):
+                t0 = time.perf_counter()
+                o.blas_rebuild(0, 1)
+                if k >= max(1, args.warmup):
+                    times.append(time.perf_counter() - t0)
+        finally:
+            o.close()
+        tps = tris * len(times) / sum(times)
+        return {"metric": "triangles_per_second", "value": tps, "unit": "triangles/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (the seeded atrium model)", "impl": "reference",
+                "config": {"workload": cfg["name"], "triangles": tris},
+                "cpu_baseline": {"value": tps, "unit": "triangles/s", "cores": 1, "kind": "port",
+                                 "sample": f"{len(times)} builds after {max(1, args.warmup)} warm-up, restated recursive builder "
+                                           "(oracle/sft_oracle.c), one thread"},
+                "e2e": {"value": tps, "unit": "triangles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if args.config == 5:   # bounded sample: the first frame of each scene, cycling
         scs, smp = scenes.config5()
         jobs = [(sc.to_bytes(), 0, S, sc.frames[0].width, sc.frames[0].height) for sc, S in zip(scs, smp)]
@@ -723,6 +857,8 @@ def main():
         line = run_serve(args, cfg)
     elif args.config == 6:
         line = run_raycast(args, cfg)
+    elif args.config == 7:
+        line = run_blas(args, cfg)
     else:
         line = run_ours(args, cfg)
     if line is not None:

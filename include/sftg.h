@@ -256,9 +256,10 @@ int sftg_lane_done(sftg_ctx* ctx, uint32_t lane);
 int sftg_lane_wait(sftg_ctx* ctx, uint32_t lane);
 /* Kernels launched by every batch finished so far, on all lanes (a running total). */
 uint64_t sftg_launch_total(const sftg_ctx* ctx);
-/* Wall time in ms of the last BLAS built on the device at model upload (query and build; no
- * counterpart in the reference, whose build is host code), and its triangle count. */
-double sftg_last_blas_build(const sftg_ctx* ctx, uint32_t* out_items);
+/* The last BLAS built on the device at model upload (no counterpart in the reference, whose build
+ * is host code): wall time in ms, the span of the build on the upload stream between two CUDA
+ * events in ms, its triangle count and the kernels it launched. */
+int sftg_last_blas_build(const sftg_ctx* ctx, double* wall_ms, double* stream_ms, uint32_t* items, uint32_t* launches);
 
 /* Device time in ms of the last frame, split as [occlusion, geometry+clip, binning, raster, resolve]. */
 int sftg_last_timings(const sftg_ctx* ctx, float* out5);

@@ -1975,6 +1975,19 @@ int sfto_model_blas(void* hp, uint32_t mi, uint8_t* out, uint32_t cap, uint32_t*
     return (int)m->blas_count;
 }
 
+/* Builds model `mi`'s BLAS again `reps` times from its meshlets (the timed CPU side of the BLAS
+ * builder's measurement); returns the node count of the last build. */
+int sfto_blas_rebuild(void* hp, uint32_t mi, uint32_t reps) {
+    oracle_handle* h = (oracle_handle*)hp;
+    if (!h || mi >= h->sc.n_models) return -1;
+    omodel* m = &h->c.models[mi];
+    for (uint32_t r = 0; r < reps; r++) {
+        free(m->blas); m->blas = NULL; m->blas_count = 0;
+        blas_build(m);
+    }
+    return (int)m->blas_count;
+}
+
 /* enum sft_debug_mode for the following renders (0 = none) */
 int sfto_set_debug_mode(void* hp, int mode) {
     oracle_handle* h = (oracle_handle*)hp;

@@ -99,8 +99,9 @@ struct sftg_ctx {
     float timings[5] = { 0, 0, 0, 0, 0 };
     int launches = 0;
     uint64_t launch_total = 0;                 /* kernels of every finished batch, on all lanes */
-    double blas_ms = 0.0;                      /* wall time of the last device BLAS build */
-    uint32_t blas_items = 0;                   /* and its triangle count */
+    double blas_ms = 0.0, blas_stream_ms = 0.0; /* last device BLAS build: wall time, upload-stream span */
+    uint32_t blas_items = 0, blas_launches = 0; /* and its triangles and kernels */
+    cudaEvent_t ev_blas[2] = { nullptr, nullptr };
     bool use_graphs = true;
     sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
     /* transient models (one frame's dynamic meshes): pool marks where they start */
@@ -226,6 +227,7 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
         if (ln.stream) cudaStreamDestroy(ln.stream);
     }
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
+    for (int k = 0; k < 2; k++) if (ctx->ev_blas[k]) cudaEventDestroy(ctx->ev_blas[k]);
     delete ctx;
 }
 
@@ -340,7 +342,10 @@ static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_mo
         md.blas_count = 0; md.blas_root = 0;
         sftg_blas_job* job = nullptr;
         uint32_t n_items = 0, n_nodes = 0, status = 0;
+        for (int k = 0; k < 2; k++) if (!ctx->ev_blas[k]) CK(cudaEventCreate(&ctx->ev_blas[k]));
+        CK(cudaStreamSynchronize(ctx->stream));   /* the meshlets are in place */
         const auto t0 = std::chrono::steady_clock::now();
+        CK(cudaEventRecord(ctx->ev_blas[0], ctx->stream));
         cudaError_t e = sftg_blas_begin(&job, (const float*)((const char*)ctx->ml_attr.ptr + (size_t)ctx->n_meshlets * 2560),
                                         (const uint8_t*)ctx->ml_inds.ptr + (size_t)ctx->n_meshlets * 512, total, ctx->stream, &n_items, &n_nodes);
         if (e == cudaSuccess && n_nodes) {
@@ -351,8 +356,14 @@ static int model_upload(sftg_ctx* ctx, const sftg_model_desc* d, int32_t* out_mo
                 md.blas_count = n_nodes;
             }
         }
+        ctx->blas_launches = sftg_blas_launches(job);
         sftg_blas_end(job);
+        float ev_ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_blas[1], ctx->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev_blas[1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ev_ms, ctx->ev_blas[0], ctx->ev_blas[1]);
         ctx->blas_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        ctx->blas_stream_ms = ev_ms;
         ctx->blas_items = n_items;
         if (e != cudaSuccess) return set_err(ctx, SFTG_E_CUDA, "BLAS build: %s", cudaGetErrorString(e));
         if (status) return set_err(ctx, SFTG_E_DEVICE_STATUS, "BLAS build: a device work list overflowed");
@@ -1363,9 +1374,13 @@ extern "C" int sftg_last_timings(const sftg_ctx* ctx, float* out5) {
 
 extern "C" int sftg_last_launch_count(const sftg_ctx* ctx) { return ctx ? ctx->launches : 0; }
 extern "C" uint64_t sftg_launch_total(const sftg_ctx* ctx) { return ctx ? ctx->launch_total : 0; }
-extern "C" double sftg_last_blas_build(const sftg_ctx* ctx, uint32_t* out_items) {
-    if (out_items) *out_items = ctx ? ctx->blas_items : 0;
-    return ctx ? ctx->blas_ms : 0.0;
+extern "C" int sftg_last_blas_build(const sftg_ctx* ctx, double* wall_ms, double* stream_ms, uint32_t* items, uint32_t* launches) {
+    if (!ctx) return SFTG_E_ARG;
+    if (wall_ms) *wall_ms = ctx->blas_ms;
+    if (stream_ms) *stream_ms = ctx->blas_stream_ms;
+    if (items) *items = ctx->blas_items;
+    if (launches) *launches = ctx->blas_launches;
+    return SFTG_OK;
 }
 
 extern "C" void* sftg_stream(const sftg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }

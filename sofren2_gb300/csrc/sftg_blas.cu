@@ -420,6 +420,7 @@ struct sftg_blas_job {
     const float* attr = nullptr;
     const uint8_t* inds = nullptr;
     uint32_t* d_cnt = nullptr;      /* [nm] counts, then [nm] offsets, then total */
+    uint32_t launches = 0;          /* kernels launched by begin and finish */
     /* plan */
     std::vector<blas_pnode> nodes;
     std::vector<std::vector<uint32_t>> by_depth;
@@ -469,6 +470,7 @@ cudaError_t sftg_blas_begin(sftg_blas_job** out, const float* attr, const uint8_
     k_blas_count<<<(nm + 7) / 8, 256, 0, st>>>(inds, nm, J->d_cnt);
     k_blas_offsets<<<1, 1024, 0, st>>>(J->d_cnt, nm, J->d_cnt + nm, J->d_cnt + 2 * (size_t)nm);
     BK(cudaGetLastError());
+    J->launches += 2;
     uint32_t total = 0;
     BK(cudaMemcpyAsync(&total, J->d_cnt + 2 * (size_t)nm, 4, cudaMemcpyDeviceToHost, st));
     BK(cudaStreamSynchronize(st));
@@ -553,21 +555,26 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     if (err == cudaSuccess) {
         k_blas_items<<<(J->nm + 7) / 8, 256, 0, st>>>(J->attr, J->inds, J->nm, J->d_cnt + J->nm, n, it, ids, perm);
         err = cudaGetLastError();
+        J->launches++;
     }
     uint32_t* h_ctr = nullptr;
     if (err == cudaSuccess) err = cudaMallocHost((void**)&h_ctr, 16);
     for (size_t L = 0; err == cudaSuccess && L < J->by_level.size(); L++) {
-        if (lv_span_cnt[L])
+        if (lv_span_cnt[L]) {
             k_blas_sort_small<true><<<lv_span_cnt[L], BLAS_SMALL_THREADS, BLAS_SMALL_SMEM, st>>>(d_spans + lv_span_off[L], nullptr, lv_span_cnt[L],
                                                                                                  d_tasks, it, n, key, perm);
+            J->launches++;
+        }
         if (lv_big_cnt[L]) {
             k_blas_axis<<<lv_big_cnt[L], BLAS_BIG_THREADS, 0, st>>>(d_big + lv_big_off[L], lv_big_cnt[L], it, n, perm, key);
+            J->launches++;
             const uint2* curl = d_big + lv_big_off[L];
             uint32_t ncur = lv_big_cnt[L], flip = 0;
             err = cudaMemsetAsync(ctr, 0, 8, st);
             while (err == cudaSuccess && ncur) {
                 if ((err = cudaMemsetAsync(ctr, 0, 4, st)) != cudaSuccess) break;
                 k_blas_part_big<<<ncur, BLAS_BIG_THREADS, 0, st>>>(curl, ncur, key, perm, Lp, Rp, lists[flip], list_cap, small, small_cap, ctr);
+                J->launches++;
                 if ((err = cudaGetLastError()) != cudaSuccess) break;
                 if ((err = cudaMemcpyAsync(h_ctr, ctr, 12, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
                 if ((err = cudaStreamSynchronize(st)) != cudaSuccess) break;
@@ -577,7 +584,10 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
             }
             if (err != cudaSuccess || *status) break;
             const uint32_t ns = h_ctr[1] < small_cap ? h_ctr[1] : 0;
-            if (ns) k_blas_sort_small<false><<<ns, BLAS_SMALL_THREADS, BLAS_SMALL_SMEM, st>>>(nullptr, small, ns, nullptr, it, n, key, perm);
+            if (ns) {
+                k_blas_sort_small<false><<<ns, BLAS_SMALL_THREADS, BLAS_SMALL_SMEM, st>>>(nullptr, small, ns, nullptr, it, n, key, perm);
+                J->launches++;
+            }
         }
         if (err == cudaSuccess) err = cudaGetLastError();
     }
@@ -585,12 +595,15 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         const uint32_t cnt = (uint32_t)J->by_depth[dd].size();
         k_blas_nodes<<<(cnt + 127) / 128, 128, 0, st>>>(d_pn, d_didx + depth_off[dd], cnt, it, ids, perm, n, bnd, dst);
         err = cudaGetLastError();
+        J->launches++;
     }
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);
     if (h_ctr) cudaFreeHost(h_ctr);
     cudaFreeAsync(d, st);
     return err;
 }
+
+uint32_t sftg_blas_launches(const sftg_blas_job* J) { return J ? J->launches : 0; }
 
 void sftg_blas_end(sftg_blas_job* J) {
     if (!J) return;

@@ -103,6 +103,7 @@ struct sftg_blas_job;
 cudaError_t sftg_blas_begin(sftg_blas_job** out, const float* attr, const uint8_t* inds, uint32_t nm, cudaStream_t st,
                             uint32_t* n_items, uint32_t* n_nodes);
 cudaError_t sftg_blas_finish(sftg_blas_job* job, sftg_bvh_node* dst, uint32_t* status);
+uint32_t sftg_blas_launches(const sftg_blas_job* job);
 void sftg_blas_end(sftg_blas_job* job);
 void sftg_launch_pose(const sftg_pose_tables& T, const sftg_pose_request* reqs, const uint32_t* out_off, uint32_t n, float* posed,
                       float* global, cudaStream_t st);

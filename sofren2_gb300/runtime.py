@@ -60,7 +60,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sft_batch_begin": (v, []), "sft_batch_submit": (i32, []), "sft_batch_submit_async": (i32, [u32]),
         "sft_batch_done": (i32, [u32]), "sft_batch_wait": (i32, [u32]),
         "sftx_scene_render_lanes": (i32, [p, p, p, u32, p, p, u32]), "sftg_launch_total": (u64, [p]),
-        "sft_model_get_blas": (p, [p, p, p]), "sftg_last_blas_build": (C.c_double, [p, p]),
+        "sft_model_get_blas": (p, [p, p, p]), "sftg_last_blas_build": (i32, [p, p, p, p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -376,11 +376,12 @@ class Renderer:
             raise ValueError(f"scene has no model {mi}")
         return C.c_int32.from_address(p).value
 
-    def last_blas_build(self) -> tuple[float, int]:
-        """(wall ms, triangles) of the last BLAS built on the device at model creation."""
-        n = C.c_uint32(0)
-        ms = self.lib.sftg_last_blas_build(self.lib.sft_get_gpu_context(), C.byref(n))
-        return float(ms), int(n.value)
+    def last_blas_build(self) -> dict:
+        """The last BLAS built on the device at model creation: wall and stream-event ms,
+        triangles, kernels launched."""
+        w, s, n, k = C.c_double(0), C.c_double(0), C.c_uint32(0), C.c_uint32(0)
+        self.lib.sftg_last_blas_build(self.lib.sft_get_gpu_context(), C.byref(w), C.byref(s), C.byref(n), C.byref(k))
+        return {"wall_ms": w.value, "stream_ms": s.value, "triangles": n.value, "launches": k.value}
 
     def model_blas(self, h, mi: int) -> tuple[bytes, int]:
         """(node images, root index) of model mi of scene h through sft_model_get_blas: the BLAS

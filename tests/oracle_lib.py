@@ -60,6 +60,13 @@ class Oracle:
         L.sfto_model_blas(self.h, mi, buf.ctypes.data_as(C.c_void_p), n, C.byref(root))
         return buf[: n * 256].tobytes(), int(root.value)
 
+    def blas_rebuild(self, mi: int, reps: int = 1) -> int:
+        """Builds model mi's BLAS again `reps` times with the oracle's restated builder (timing)."""
+        L = lib()
+        L.sfto_blas_rebuild.restype = C.c_int
+        L.sfto_blas_rebuild.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+        return int(L.sfto_blas_rebuild(self.h, mi, reps))
+
     def raycast(self, rays: np.ndarray) -> np.ndarray:
         """The oracle's sft_raycast_instance restatement for each RAY_DTYPE record."""
         L = lib()
