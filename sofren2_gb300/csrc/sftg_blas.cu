@@ -30,12 +30,15 @@
 #include "sftg_kernels.h"
 #include <vector>
 #include <cstring>
+#include <algorithm>
 
 #define BLAS_CAP 4096            /* positions one shared-memory CTA sorts */
 #define BLAS_BIG_THREADS 1024
 #define BLAS_SMALL_THREADS 512
 #define BLAS_SMALL_WARPS (BLAS_SMALL_THREADS / 32)
-#define BLAS_SMALL_SMEM (BLAS_CAP * 4 * 2 + BLAS_CAP * 2 * 2 + (BLAS_CAP / 2) * 4 * 2)
+#define BLAS_SEQ 32              /* pieces of at most this many positions: one thread each */
+#define BLAS_SEQ_STACK 16        /* pending disjoint pieces of >= 2 positions within BLAS_SEQ */
+#define BLAS_SMALL_SMEM (BLAS_CAP * 4 * 2 + BLAS_CAP * 2 * 2 + (BLAS_CAP / 2) * 4 * 3)
 
 struct blas_pnode {              /* a node of the plan */
     uint32_t start, count;       /* item range; a leaf when count <= 8 */
@@ -297,12 +300,38 @@ __device__ __forceinline__ void warp_partition(float* Ks, uint32_t* Ps, uint16_t
     __syncwarp();
 }
 
+/* The reference's quicksort itself on [s, s + m) of the shared-memory arrays, by
+ * one thread, the recursion kept as a stack of the pending (disjoint) pieces.  The scans carry
+ * bounds that the pivot sentinel already guarantees. */
+__device__ __forceinline__ void seq_quicksort(float* Ks, uint32_t* Ps, int s, int m) {
+    int st_s[BLAS_SEQ_STACK], st_m[BLAS_SEQ_STACK], sp = 0;
+    st_s[sp] = s; st_m[sp] = m; sp++;
+    while (sp > 0) {
+        sp--;
+        const int b = st_s[sp], c = st_m[sp];
+        const float p = Ks[b + c / 2];
+        int i = 0, j = c - 1;
+        while (i <= j) {
+            while (i < c && Ks[b + i] < p) i++;
+            while (j >= 0 && Ks[b + j] > p) j--;
+            if (i <= j) {
+                const float kt = Ks[b + i]; Ks[b + i] = Ks[b + j]; Ks[b + j] = kt;
+                const uint32_t pt = Ps[b + i]; Ps[b + i] = Ps[b + j]; Ps[b + j] = pt;
+                i++; j--;
+            }
+        }
+        if (j > 0 && sp < BLAS_SEQ_STACK) { st_s[sp] = b; st_m[sp] = j + 1; sp++; }
+        if (c - i > 1 && sp < BLAS_SEQ_STACK) { st_s[sp] = b + i; st_m[sp] = c - i; sp++; }
+    }
+}
+
 /* One CTA finishes the quicksorts inside one span of at most BLAS_CAP positions.
  * PLAN: the span holds whole ranges of one level (tasks[z .. z + w)); each warp takes ranges,
  *       picks their axes and writes their keys.  Otherwise the span is one piece of a long
  *       range whose keys are already in global memory.
  * The pieces of a round are disjoint; each warp partitions its pieces and queues the parts of
- * two or more positions for the next round. */
+ * more than BLAS_SEQ positions for the next round; parts of 2 to BLAS_SEQ positions are
+ * finished after the rounds, one thread each. */
 template <bool PLAN>
 __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const uint4* __restrict__ spans, const uint2* __restrict__ list,
                                                                        uint32_t nspans, const uint2* __restrict__ tasks,
@@ -314,7 +343,8 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
     uint16_t* Lp = (uint16_t*)(Ps + BLAS_CAP);
     uint16_t* Rp = Lp + BLAS_CAP;
     uint32_t* lst0 = (uint32_t*)(Rp + BLAS_CAP);   /* two lists of BLAS_CAP / 2 pieces */
-    __shared__ int ncnt[2];
+    uint32_t* seq = lst0 + BLAS_CAP;                /* short pieces, BLAS_CAP / 2 */
+    __shared__ int ncnt[3];
     if (blockIdx.x >= nspans) return;
     uint32_t s0, m0;
     if (PLAN) { s0 = spans[blockIdx.x].x; m0 = spans[blockIdx.x].y; }
@@ -323,7 +353,7 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t x = threadIdx.x; x < m0; x += BLAS_SMALL_THREADS) Ps[x] = perm[s0 + x];
     if (!PLAN) for (uint32_t x = threadIdx.x; x < m0; x += BLAS_SMALL_THREADS) Ks[x] = key[s0 + x];
-    if (threadIdx.x == 0) { ncnt[0] = 0; ncnt[1] = 0; }
+    if (threadIdx.x == 0) { ncnt[0] = 0; ncnt[1] = 0; ncnt[2] = 0; }
     __syncthreads();
     if (PLAN) {
         const uint32_t t0 = spans[blockIdx.x].z, nt = spans[blockIdx.x].w;
@@ -343,10 +373,14 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
             warp_bounds(lo, hi);
             const float* c = it + (size_t)(6 + pick_axis(lo, hi)) * n;
             for (uint32_t x = lane; x < tc; x += 32) Ks[ts + x] = c[Ps[ts + x]];
-            if (lane == 0) { const int k = atomicAdd(&ncnt[0], 1); if (k < BLAS_CAP / 2) lst0[k] = (ts << 16) | tc; }
+            if (lane == 0) {
+                const int q = tc > BLAS_SEQ ? 0 : 2;
+                const int k = atomicAdd(&ncnt[q], 1);
+                if (k < BLAS_CAP / 2) (q ? seq : lst0)[k] = (ts << 16) | tc;
+            }
         }
     } else if (threadIdx.x == 0 && m0 >= 2) {
-        lst0[0] = m0; ncnt[0] = 1;
+        if (m0 > BLAS_SEQ) { lst0[0] = m0; ncnt[0] = 1; } else { seq[0] = m0; ncnt[2] = 1; }
     }
     int cur = 0;
     for (;;) {
@@ -363,12 +397,21 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
             int i, j;
             warp_partition(Ks, Ps, Lp, Rp, s, m, lane, i, j);
             if (lane == 0) {
-                if (j >= 1) { const int k = atomicAdd(&ncnt[cur ^ 1], 1); if (k < BLAS_CAP / 2) out_l[k] = ((uint32_t)s << 16) | (uint32_t)(j + 1); }
-                if (m - i >= 2) { const int k = atomicAdd(&ncnt[cur ^ 1], 1); if (k < BLAS_CAP / 2) out_l[k] = ((uint32_t)(s + i) << 16) | (uint32_t)(m - i); }
+                const uint32_t ps[2] = { (uint32_t)s, (uint32_t)(s + i) };
+                const int pm[2] = { j + 1, m - i };
+                for (int h = 0; h < 2; h++) {
+                    if (pm[h] < 2) continue;
+                    const int q = pm[h] > BLAS_SEQ ? (cur ^ 1) : 2;
+                    const int k = atomicAdd(&ncnt[q], 1);
+                    if (k < BLAS_CAP / 2) (q == 2 ? seq : out_l)[k] = (ps[h] << 16) | (uint32_t)pm[h];
+                }
             }
         }
         cur ^= 1;
     }
+    const int ns = min(ncnt[2], BLAS_CAP / 2);
+    for (int k = threadIdx.x; k < ns; k += BLAS_SMALL_THREADS) seq_quicksort(Ks, Ps, (int)(seq[k] >> 16), (int)(seq[k] & 0xFFFFu));
+    __syncthreads();
     for (uint32_t x = threadIdx.x; x < m0; x += BLAS_SMALL_THREADS) perm[s0 + x] = Ps[x];
 }
 
@@ -490,6 +533,11 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     std::vector<uint2> tasks, big;
     std::vector<uint4> spans;
     std::vector<uint32_t> lv_task_off, lv_span_off, lv_span_cnt, lv_big_off, lv_big_cnt;
+    /* short ranges are packed into spans of about n / (3 x SMs) positions (three CTAs fit an SM),
+     * so that deep levels of many small ranges still fill the GPU */
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t span_target = std::min<uint32_t>(BLAS_CAP, std::max<uint32_t>(256, n / (3u * (uint32_t)std::max(sms, 1))));
     for (size_t L = 0; L < J->by_level.size(); L++) {
         const std::vector<uint2>& T = J->by_level[L];
         lv_task_off.push_back((uint32_t)tasks.size());
@@ -501,7 +549,7 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
             if (T[k].y > BLAS_CAP) { big.push_back(T[k]); k++; continue; }
             const uint32_t s0 = T[k].x;
             uint32_t e = k + 1;
-            while (e < T.size() && T[e].y <= BLAS_CAP && T[e].x + T[e].y - s0 <= BLAS_CAP) e++;
+            while (e < T.size() && T[e].y <= BLAS_CAP && T[e].x + T[e].y - s0 <= span_target) e++;
             spans.push_back(make_uint4(s0, T[e - 1].x + T[e - 1].y - s0, t_base + k, e - k));
             k = e;
         }
