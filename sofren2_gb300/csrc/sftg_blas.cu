@@ -33,7 +33,6 @@
 #include <algorithm>
 
 #define BLAS_CAP 4096            /* positions one shared-memory CTA sorts */
-#define BLAS_BIG_THREADS 1024
 #define BLAS_SMALL_THREADS 512
 #define BLAS_SMALL_WARPS (BLAS_SMALL_THREADS / 32)
 #define BLAS_SEQ 32              /* pieces of at most this many positions: one thread each */
@@ -139,34 +138,69 @@ __device__ __forceinline__ void warp_bounds(float* lo, float* hi) {
         }
 }
 
-/* one CTA per long range: its axis and its keys in global memory */
-__global__ void __launch_bounds__(BLAS_BIG_THREADS) k_blas_axis(const uint2* __restrict__ ranges, uint32_t nr, const float* __restrict__ it,
-                                                               uint32_t n, const uint32_t* __restrict__ perm, float* __restrict__ key) {
-    __shared__ float sb[32][6];
-    __shared__ int s_axis;
-    if (blockIdx.x >= nr) return;
-    const uint32_t s = ranges[blockIdx.x].x, m = ranges[blockIdx.x].y;
-    float lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
-    for (uint32_t x = threadIdx.x; x < m; x += BLAS_BIG_THREADS) {
-        const uint32_t q = perm[s + x];
-        for (int a = 0; a < 3; a++) {
-            const float c = it[(size_t)(6 + a) * n + q];
-            if (c < lo[a]) lo[a] = c;
-            if (c > hi[a]) hi[a] = c;
-        }
-    }
+/* Long ranges are cut into chunks of BLAS_CHUNK positions; a chunk is (piece, start within the
+ * piece, length), and the chunks of one piece are consecutive in the chunk table. */
+#define BLAS_CHUNK 2048
+#define BLAS_CHUNK_THREADS 256
+#define BLAS_CHUNK_PER_THREAD (BLAS_CHUNK / BLAS_CHUNK_THREADS)
+
+__device__ __forceinline__ void block_bounds_256(float* lo, float* hi, float (*sb)[6]) {
     warp_bounds(lo, hi);
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) for (int a = 0; a < 3; a++) { sb[w][a] = lo[a]; sb[w][3 + a] = hi[a]; }
     __syncthreads();
     if (w == 0) {
-        for (int a = 0; a < 3; a++) { lo[a] = sb[lane][a]; hi[a] = sb[lane][3 + a]; }
+        for (int a = 0; a < 3; a++) { lo[a] = lane < BLAS_CHUNK_THREADS / 32 ? sb[lane][a] : 1e30f; hi[a] = lane < BLAS_CHUNK_THREADS / 32 ? sb[lane][3 + a] : -1e30f; }
         warp_bounds(lo, hi);
-        if (lane == 0) s_axis = pick_axis(lo, hi);
     }
-    __syncthreads();
-    const float* c = it + (size_t)(6 + s_axis) * n;
-    for (uint32_t x = threadIdx.x; x < m; x += BLAS_BIG_THREADS) key[s + x] = c[perm[s + x]];
+}
+
+/* centroid bounds of each chunk of the long ranges */
+__global__ void __launch_bounds__(BLAS_CHUNK_THREADS) k_blas_chunk_bounds(const uint2* __restrict__ pieces, const uint4* __restrict__ chunks,
+                                                                        uint32_t nch, const float* __restrict__ it, uint32_t n,
+                                                                        const uint32_t* __restrict__ perm, float* __restrict__ part) {
+    __shared__ float sb[BLAS_CHUNK_THREADS / 32][6];
+    if (blockIdx.x >= nch) return;
+    const uint4 c = chunks[blockIdx.x];
+    const uint32_t s = pieces[c.x].x + c.y;
+    float lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
+    for (uint32_t x = threadIdx.x; x < c.z; x += BLAS_CHUNK_THREADS) {
+        const uint32_t q = perm[s + x];
+        for (int a = 0; a < 3; a++) {
+            const float v = it[(size_t)(6 + a) * n + q];
+            if (v < lo[a]) lo[a] = v;
+            if (v > hi[a]) hi[a] = v;
+        }
+    }
+    block_bounds_256(lo, hi, sb);
+    if (threadIdx.x == 0) for (int a = 0; a < 3; a++) { part[(size_t)blockIdx.x * 6 + a] = lo[a]; part[(size_t)blockIdx.x * 6 + 3 + a] = hi[a]; }
+}
+
+/* one warp per long range: its split axis from the chunk bounds */
+__global__ void k_blas_range_axis(const uint2* __restrict__ pchunk, uint32_t np, const float* __restrict__ part, uint8_t* __restrict__ axis) {
+    const uint32_t pi = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (pi >= np) return;
+    const uint2 pc = pchunk[pi];
+    float lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
+    for (uint32_t k = lane; k < pc.y; k += 32)
+        for (int a = 0; a < 3; a++) {
+            const float l = part[(size_t)(pc.x + k) * 6 + a], h = part[(size_t)(pc.x + k) * 6 + 3 + a];
+            if (l < lo[a]) lo[a] = l;
+            if (h > hi[a]) hi[a] = h;
+        }
+    warp_bounds(lo, hi);
+    if (lane == 0) axis[pi] = (uint8_t)pick_axis(lo, hi);
+}
+
+/* the keys of the long ranges: centroids along each range's axis, in the current order */
+__global__ void __launch_bounds__(BLAS_CHUNK_THREADS) k_blas_chunk_keys(const uint2* __restrict__ pieces, const uint4* __restrict__ chunks,
+                                                                      uint32_t nch, const uint8_t* __restrict__ axis, const float* __restrict__ it,
+                                                                      uint32_t n, const uint32_t* __restrict__ perm, float* __restrict__ key) {
+    if (blockIdx.x >= nch) return;
+    const uint4 c = chunks[blockIdx.x];
+    const uint32_t s = pieces[c.x].x + c.y;
+    const float* cv = it + (size_t)(6 + axis[c.x]) * n;
+    for (uint32_t x = threadIdx.x; x < c.z; x += BLAS_CHUNK_THREADS) key[s + x] = cv[perm[s + x]];
 }
 
 /* ------------------------------------------------------------------------------ partitions */
@@ -181,87 +215,147 @@ __device__ __forceinline__ void final_ij(int l_last, int r_last, int l_next, int
     }
 }
 
-__device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t* ws, uint32_t& total) {
+__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* ws) {
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t s = v;
-    for (int d = 1; d < 32; d <<= 1) { const uint32_t o = __shfl_up_sync(0xffffffffu, s, d); if (lane >= (uint32_t)d) s += o; }
-    if (lane == 31) ws[w] = s;
+    uint32_t sc = v;
+    for (int d = 1; d < 32; d <<= 1) { const uint32_t o = __shfl_up_sync(0xffffffffu, sc, d); if (lane >= (uint32_t)d) sc += o; }
+    if (lane == 31) ws[w] = sc;
     __syncthreads();
-    if (w == 0) {
-        uint32_t t = ws[lane];
-        for (int d = 1; d < 32; d <<= 1) { const uint32_t o = __shfl_up_sync(0xffffffffu, t, d); if (lane >= (uint32_t)d) t += o; }
-        ws[lane] = t;
-    }
-    __syncthreads();
-    const uint32_t r = s - v + (w ? ws[w - 1] : 0);
-    total = ws[31];
-    __syncthreads();
-    return r;
+    uint32_t before = 0;
+    for (uint32_t k = 0; k < w; k++) before += ws[k];
+    return before + sc - v;
 }
 
-__device__ __forceinline__ void push_piece(uint32_t s, uint32_t m, uint2* next, uint32_t next_cap, uint2* small, uint32_t small_cap, uint32_t* ctr) {
-    if (m > BLAS_CAP) {
-        const uint32_t k = atomicAdd(&ctr[0], 1u);
-        if (k < next_cap) next[k] = make_uint2(s, m); else atomicOr(&ctr[2], 1u);
-    } else {
-        const uint32_t k = atomicAdd(&ctr[1], 1u);
-        if (k < small_cap) small[k] = make_uint2(s, m); else atomicOr(&ctr[2], 1u);
-    }
-}
-
-/* one CTA partitions one long piece in global memory; the pieces it leaves go to the next
- * round (still long) or to the shared-memory sorter */
-__global__ void __launch_bounds__(BLAS_BIG_THREADS) k_blas_part_big(const uint2* __restrict__ list, uint32_t nl, float* __restrict__ key,
-                                                                   uint32_t* __restrict__ perm, uint32_t* __restrict__ Lp,
-                                                                   uint32_t* __restrict__ Rp, uint2* next, uint32_t next_cap,
-                                                                   uint2* small, uint32_t small_cap, uint32_t* ctr) {
-    __shared__ uint32_t ws[32];
-    __shared__ uint32_t s_tot[3];
-    if (blockIdx.x >= nl) return;
-    const uint32_t s = list[blockIdx.x].x, m = list[blockIdx.x].y;
-    const float p = key[s + m / 2];
-    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x < 3) s_tot[threadIdx.x] = 0;
+/* Partition round over every long piece, step 1: per chunk, how many positions stop the left
+ * scan (fi) and the right scan (fj) for the piece's pivot. */
+__global__ void __launch_bounds__(BLAS_CHUNK_THREADS) k_blas_part_count(const uint2* __restrict__ pieces, const uint4* __restrict__ chunks,
+                                                                      const uint32_t* __restrict__ rs, const float* __restrict__ key,
+                                                                      uint2* __restrict__ cc) {
+    __shared__ uint32_t s_c[2];
+    if (blockIdx.x >= rs[1]) return;
+    const uint4 c = chunks[blockIdx.x];
+    const uint2 pc = pieces[c.x];
+    const float p = key[pc.x + pc.y / 2];
+    if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
+    __syncthreads();
     uint32_t ci = 0, cj = 0;
-    for (uint32_t x = threadIdx.x; x < m; x += BLAS_BIG_THREADS) {
-        const float k = key[s + x];
+    for (uint32_t x = threadIdx.x; x < c.z; x += BLAS_CHUNK_THREADS) {
+        const float k = key[pc.x + c.y + x];
         ci += !(k < p); cj += !(k > p);
     }
-    __syncthreads();
     for (int d = 16; d > 0; d >>= 1) { ci += __shfl_xor_sync(0xffffffffu, ci, d); cj += __shfl_xor_sync(0xffffffffu, cj, d); }
-    if (lane == 0) { atomicAdd(&s_tot[0], ci); atomicAdd(&s_tot[1], cj); }
+    if ((threadIdx.x & 31) == 0) { atomicAdd(&s_c[0], ci); atomicAdd(&s_c[1], cj); }
     __syncthreads();
-    const uint32_t CI = s_tot[0], CJ = s_tot[1];
-    uint32_t carry_i = 0, carry_j = 0, valid = 0;
-    for (uint32_t base = 0; base < m; base += BLAS_BIG_THREADS) {
-        const uint32_t x = base + threadIdx.x;
-        const bool in = x < m;
-        const float k = in ? key[s + x] : 0.f;
-        const bool fi = in && !(k < p), fj = in && !(k > p);
-        uint32_t tot;
-        const uint32_t ex = block_excl_scan_1024((fi ? 1u : 0u) | (fj ? 0x10000u : 0u), ws, tot);
-        const uint32_t r = carry_i + (ex & 0xFFFFu), pj = carry_j + (ex >> 16);
-        if (fi) { Lp[s + r] = x; valid += (r < CJ - pj); }
-        if (fj) Rp[s + (CJ - 1 - pj)] = x;
-        carry_i += tot & 0xFFFFu; carry_j += tot >> 16;
+    if (threadIdx.x == 0) cc[blockIdx.x] = make_uint2(s_c[0], s_c[1]);
+}
+
+/* step 2, one warp per piece: each chunk's counts before it within the piece, the piece's totals */
+__global__ void k_blas_part_prefix(const uint2* __restrict__ pchunk, const uint32_t* __restrict__ rs, const uint2* __restrict__ cc,
+                                   uint2* __restrict__ cpre, uint2* __restrict__ ptot, uint32_t* __restrict__ kc) {
+    const uint32_t pi = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (pi >= rs[0]) return;
+    const uint2 pc = pchunk[pi];
+    uint32_t ri = 0, rj = 0;
+    for (uint32_t base = 0; base < pc.y; base += 32) {
+        const uint32_t k = base + lane;
+        const uint2 v = k < pc.y ? cc[pc.x + k] : make_uint2(0, 0);
+        uint32_t si = v.x, sj = v.y;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t oi = __shfl_up_sync(0xffffffffu, si, d), oj = __shfl_up_sync(0xffffffffu, sj, d);
+            if (lane >= (uint32_t)d) { si += oi; sj += oj; }
+        }
+        if (k < pc.y) cpre[pc.x + k] = make_uint2(ri + si - v.x, rj + sj - v.y);
+        ri += __shfl_sync(0xffffffffu, si, 31); rj += __shfl_sync(0xffffffffu, sj, 31);
+    }
+    if (lane == 0) { ptot[pi] = make_uint2(ri, rj); kc[pi] = 0; }
+}
+
+/* step 3, per chunk: the rank of every stop (left stops counted from the piece's start, right
+ * stops from its end), written as position lists Lp / Rp, and how many left stops are swapped */
+__global__ void __launch_bounds__(BLAS_CHUNK_THREADS) k_blas_part_rank(const uint2* __restrict__ pieces, const uint4* __restrict__ chunks,
+                                                                     const uint32_t* __restrict__ rs, const float* __restrict__ key,
+                                                                     const uint2* __restrict__ cpre,
+                                                                     const uint2* __restrict__ ptot, uint32_t* __restrict__ Lp,
+                                                                     uint32_t* __restrict__ Rp, uint32_t* __restrict__ kc) {
+    __shared__ uint32_t ws[BLAS_CHUNK_THREADS / 32];
+    __shared__ uint32_t s_valid;
+    if (blockIdx.x >= rs[1]) return;
+    const uint4 c = chunks[blockIdx.x];
+    const uint2 pc = pieces[c.x];
+    const uint32_t s = pc.x, CJ = ptot[c.x].y;
+    const float p = key[s + pc.y / 2];
+    if (threadIdx.x == 0) s_valid = 0;
+    const uint32_t x0 = c.y + threadIdx.x * BLAS_CHUNK_PER_THREAD, xe = c.y + c.z;
+    uint32_t ni = 0, nj = 0;
+    for (int e = 0; e < BLAS_CHUNK_PER_THREAD; e++) {
+        const uint32_t x = x0 + e;
+        if (x < xe) { const float k = key[s + x]; ni += !(k < p); nj += !(k > p); }
+    }
+    const uint32_t ex = block_excl_scan_256(ni | (nj << 16), ws);
+    uint32_t r = cpre[blockIdx.x].x + (ex & 0xFFFFu), pj = cpre[blockIdx.x].y + (ex >> 16), valid = 0;
+    for (int e = 0; e < BLAS_CHUNK_PER_THREAD; e++) {
+        const uint32_t x = x0 + e;
+        if (x >= xe) break;
+        const float k = key[s + x];
+        if (!(k < p)) { Lp[s + r] = x; valid += (r < CJ - pj); r++; }
+        if (!(k > p)) { Rp[s + (CJ - 1 - pj)] = x; pj++; }
     }
     for (int d = 16; d > 0; d >>= 1) valid += __shfl_xor_sync(0xffffffffu, valid, d);
-    if (lane == 0) atomicAdd(&s_tot[2], valid);
+    if ((threadIdx.x & 31) == 0 && valid) atomicAdd(&s_valid, valid);
     __syncthreads();
-    const uint32_t K = s_tot[2];
-    for (uint32_t r = threadIdx.x; r < K; r += BLAS_BIG_THREADS) {
+    if (threadIdx.x == 0 && s_valid) atomicAdd(&kc[c.x], s_valid);
+}
+
+/* step 4: the k-th left stop swaps with the k-th right stop for k < K; chunk c takes the ranks
+ * in its own position range */
+__global__ void __launch_bounds__(BLAS_CHUNK_THREADS) k_blas_part_swap(const uint2* __restrict__ pieces, const uint4* __restrict__ chunks,
+                                                                     const uint32_t* __restrict__ rs, const uint32_t* __restrict__ kc,
+                                                                     const uint32_t* __restrict__ Lp, const uint32_t* __restrict__ Rp,
+                                                                     float* __restrict__ key, uint32_t* __restrict__ perm) {
+    if (blockIdx.x >= rs[1]) return;
+    const uint4 c = chunks[blockIdx.x];
+    const uint32_t s = pieces[c.x].x, K = kc[c.x];
+    const uint32_t re = min(c.y + c.z, K);
+    for (uint32_t r = c.y + threadIdx.x; r < re; r += BLAS_CHUNK_THREADS) {
         const uint32_t a = s + Lp[s + r], b = s + Rp[s + r];
         const float ka = key[a]; key[a] = key[b]; key[b] = ka;
         const uint32_t pa = perm[a]; perm[a] = perm[b]; perm[b] = pa;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int i, j;
-        final_ij((int)Lp[s + K - 1], (int)Rp[s + K - 1], K < CI ? (int)Lp[s + K] : 0x7fffffff, K < CJ ? (int)Rp[s + K] : -1, i, j);
-        if (j >= 1) push_piece(s, (uint32_t)j + 1, next, next_cap, small, small_cap, ctr);
-        if ((int)m - i >= 2) push_piece(s + (uint32_t)i, m - (uint32_t)i, next, next_cap, small, small_cap, ctr);
+}
+
+/* step 5, one thread per piece: where the scans end, and the parts left to sort: long parts with
+ * their chunks to the next round's tables (counts in rs_next: pieces, chunks), the others to the
+ * shared-memory sorter.  ctr: [0] overflow, [1] short pieces.  Each round's counts live on the
+ * device, so rounds are launched without waiting for the host. */
+__global__ void k_blas_part_children(const uint2* __restrict__ pieces, const uint32_t* __restrict__ rs, const uint2* __restrict__ ptot,
+                                     const uint32_t* __restrict__ kc, const uint32_t* __restrict__ Lp, const uint32_t* __restrict__ Rp,
+                                     uint2* __restrict__ next, uint2* __restrict__ next_pchunk, uint4* __restrict__ next_chunks,
+                                     uint32_t list_cap, uint32_t chunk_cap, uint2* __restrict__ small, uint32_t small_cap,
+                                     uint32_t* __restrict__ rs_next, uint32_t* __restrict__ ctr) {
+    const uint32_t pi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pi >= rs[0]) return;
+    const uint32_t s = pieces[pi].x, m = pieces[pi].y, K = kc[pi], CI = ptot[pi].x, CJ = ptot[pi].y;
+    if (K == 0 || K > CI || K > CJ) { atomicOr(&ctr[0], 1u); return; }
+    int i, j;
+    final_ij((int)Lp[s + K - 1], (int)Rp[s + K - 1], K < CI ? (int)Lp[s + K] : 0x7fffffff, K < CJ ? (int)Rp[s + K] : -1, i, j);
+    const uint32_t ps[2] = { s, s + (uint32_t)i };
+    const int pm[2] = { j + 1, (int)m - i };
+    for (int h = 0; h < 2; h++) {
+        if (pm[h] < 2) continue;
+        const uint32_t len = (uint32_t)pm[h];
+        if (len > BLAS_CAP) {
+            const uint32_t k = atomicAdd(&rs_next[0], 1u);
+            const uint32_t nc = (len + BLAS_CHUNK - 1) / BLAS_CHUNK;
+            const uint32_t base = atomicAdd(&rs_next[1], nc);
+            if (k >= list_cap || base + nc > chunk_cap) { atomicOr(&ctr[0], 1u); continue; }
+            next[k] = make_uint2(ps[h], len);
+            next_pchunk[k] = make_uint2(base, nc);
+            for (uint32_t q = 0; q < nc; q++) next_chunks[base + q] = make_uint4(k, q * BLAS_CHUNK, min(BLAS_CHUNK, len - q * BLAS_CHUNK), 0);
+        } else {
+            const uint32_t k = atomicAdd(&ctr[1], 1u);
+            if (k < small_cap) small[k] = make_uint2(ps[h], len); else atomicOr(&ctr[0], 1u);
+        }
     }
-    (void)w;
 }
 
 /* one warp partitions the piece [s, s + m) of the shared-memory arrays */
@@ -345,6 +439,8 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
     uint32_t* lst0 = (uint32_t*)(Rp + BLAS_CAP);   /* two lists of BLAS_CAP / 2 pieces */
     uint32_t* seq = lst0 + BLAS_CAP;                /* short pieces, BLAS_CAP / 2 */
     __shared__ int ncnt[3];
+    __shared__ float sbnd[BLAS_SMALL_WARPS][6];
+    __shared__ int s_axis;
     if (blockIdx.x >= nspans) return;
     uint32_t s0, m0;
     if (PLAN) { s0 = spans[blockIdx.x].x; m0 = spans[blockIdx.x].y; }
@@ -357,26 +453,79 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
     __syncthreads();
     if (PLAN) {
         const uint32_t t0 = spans[blockIdx.x].z, nt = spans[blockIdx.x].w;
-        for (uint32_t t = w; t < nt; t += BLAS_SMALL_WARPS) {
-            const uint2 tk = tasks[t0 + t];
+        if (nt == 1) {   /* one range: the whole CTA gathers its bounds and keys */
+            const uint2 tk = tasks[t0];
             const uint32_t ts = tk.x - s0, tc = tk.y;
-            if (ts + tc > m0 || tc < 2) continue;
+            const bool ok = ts + tc <= m0 && tc >= 2;
             float lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
-            for (uint32_t x = lane; x < tc; x += 32) {
-                const uint32_t q = Ps[ts + x];
+            if (ok)
+                for (uint32_t x = threadIdx.x; x < tc; x += BLAS_SMALL_THREADS) {
+                    const uint32_t q = Ps[ts + x];
+                    for (int a = 0; a < 3; a++) {
+                        const float c = it[(size_t)(6 + a) * n + q];
+                        if (c < lo[a]) lo[a] = c;
+                        if (c > hi[a]) hi[a] = c;
+                    }
+                }
+            warp_bounds(lo, hi);
+            if (lane == 0) for (int a = 0; a < 3; a++) { sbnd[w][a] = lo[a]; sbnd[w][3 + a] = hi[a]; }
+            __syncthreads();
+            if (w == 0) {
                 for (int a = 0; a < 3; a++) {
-                    const float c = it[(size_t)(6 + a) * n + q];
-                    if (c < lo[a]) lo[a] = c;
-                    if (c > hi[a]) hi[a] = c;
+                    lo[a] = lane < BLAS_SMALL_WARPS ? sbnd[lane][a] : 1e30f;
+                    hi[a] = lane < BLAS_SMALL_WARPS ? sbnd[lane][3 + a] : -1e30f;
+                }
+                warp_bounds(lo, hi);
+                if (lane == 0) s_axis = pick_axis(lo, hi);
+            }
+            __syncthreads();
+            if (ok) {
+                const float* c = it + (size_t)(6 + s_axis) * n;
+                for (uint32_t x = threadIdx.x; x < tc; x += BLAS_SMALL_THREADS) Ks[ts + x] = c[Ps[ts + x]];
+                if (threadIdx.x == 0) {
+                    const int q = tc > BLAS_SEQ ? 0 : 2;
+                    (q ? seq : lst0)[0] = (ts << 16) | tc; ncnt[q] = 1;
                 }
             }
-            warp_bounds(lo, hi);
-            const float* c = it + (size_t)(6 + pick_axis(lo, hi)) * n;
-            for (uint32_t x = lane; x < tc; x += 32) Ks[ts + x] = c[Ps[ts + x]];
-            if (lane == 0) {
-                const int q = tc > BLAS_SEQ ? 0 : 2;
-                const int k = atomicAdd(&ncnt[q], 1);
-                if (k < BLAS_CAP / 2) (q ? seq : lst0)[k] = (ts << 16) | tc;
+        } else {
+            for (uint32_t t = w; t < nt; t += BLAS_SMALL_WARPS) {
+                const uint2 tk = tasks[t0 + t];
+                const uint32_t ts = tk.x - s0, tc = tk.y;
+                if (ts + tc > m0 || tc < 2) continue;
+                float lo[3] = { 1e30f, 1e30f, 1e30f }, hi[3] = { -1e30f, -1e30f, -1e30f };
+                for (uint32_t b = lane; b < tc; b += 128) {   /* four elements' loads in flight per lane */
+                    uint32_t q[4];
+                    float v[4][3];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) q[u] = b + 32u * u < tc ? Ps[ts + b + 32u * u] : 0xFFFFFFFFu;
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        for (int a = 0; a < 3; a++) v[u][a] = q[u] != 0xFFFFFFFFu ? it[(size_t)(6 + a) * n + q[u]] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        if (q[u] != 0xFFFFFFFFu)
+                            for (int a = 0; a < 3; a++) {
+                                if (v[u][a] < lo[a]) lo[a] = v[u][a];
+                                if (v[u][a] > hi[a]) hi[a] = v[u][a];
+                            }
+                }
+                warp_bounds(lo, hi);
+                const float* c = it + (size_t)(6 + pick_axis(lo, hi)) * n;
+                for (uint32_t b = lane; b < tc; b += 128) {
+                    uint32_t q[4];
+                    float v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) q[u] = b + 32u * u < tc ? Ps[ts + b + 32u * u] : 0xFFFFFFFFu;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) v[u] = q[u] != 0xFFFFFFFFu ? c[q[u]] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) if (q[u] != 0xFFFFFFFFu) Ks[ts + b + 32u * u] = v[u];
+                }
+                if (lane == 0) {
+                    const int q = tc > BLAS_SEQ ? 0 : 2;
+                    const int k = atomicAdd(&ncnt[q], 1);
+                    if (k < BLAS_CAP / 2) (q ? seq : lst0)[k] = (ts << 16) | tc;
+                }
             }
         }
     } else if (threadIdx.x == 0 && m0 >= 2) {
@@ -530,9 +679,10 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     if (!n) return cudaSuccess;
     cudaStream_t st = J->st;
     /* tasks of every level, spans of the short ones, and the node plan, in one upload */
-    std::vector<uint2> tasks, big;
-    std::vector<uint4> spans;
-    std::vector<uint32_t> lv_task_off, lv_span_off, lv_span_cnt, lv_big_off, lv_big_cnt;
+    std::vector<uint2> tasks, big, big_pchunk;
+    std::vector<uint4> spans, big_chunks;
+    std::vector<uint32_t> lv_task_off, lv_span_off, lv_span_cnt, lv_big_off, lv_big_cnt, lv_chunk_off, lv_chunk_cnt, lv_rounds;
+    std::vector<uint32_t> lv_rs;   /* per level: the first round's piece and chunk counts */
     /* short ranges are packed into spans of about n / (3 x SMs) positions (three CTAs fit an SM),
      * so that deep levels of many small ranges still fill the GPU */
     int dev = 0, sms = 152;
@@ -543,10 +693,17 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         lv_task_off.push_back((uint32_t)tasks.size());
         lv_span_off.push_back((uint32_t)spans.size());
         lv_big_off.push_back((uint32_t)big.size());
+        lv_chunk_off.push_back((uint32_t)big_chunks.size());
         const uint32_t t_base = (uint32_t)tasks.size();
         uint32_t k = 0;
         while (k < T.size()) {
-            if (T[k].y > BLAS_CAP) { big.push_back(T[k]); k++; continue; }
+            if (T[k].y > BLAS_CAP) {   /* a long range: its chunks, numbered within the level */
+                const uint32_t pi = (uint32_t)big.size() - lv_big_off.back(), c0 = (uint32_t)big_chunks.size() - lv_chunk_off.back();
+                const uint32_t nc = (T[k].y + BLAS_CHUNK - 1) / BLAS_CHUNK;
+                for (uint32_t q = 0; q < nc; q++) big_chunks.push_back(make_uint4(pi, q * BLAS_CHUNK, std::min<uint32_t>(BLAS_CHUNK, T[k].y - q * BLAS_CHUNK), 0));
+                big_pchunk.push_back(make_uint2(c0, nc));
+                big.push_back(T[k]); k++; continue;
+            }
             const uint32_t s0 = T[k].x;
             uint32_t e = k + 1;
             while (e < T.size() && T[e].y <= BLAS_CAP && T[e].x + T[e].y - s0 <= span_target) e++;
@@ -556,21 +713,33 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         tasks.insert(tasks.end(), T.begin(), T.end());
         lv_span_cnt.push_back((uint32_t)spans.size() - lv_span_off.back());
         lv_big_cnt.push_back((uint32_t)big.size() - lv_big_off.back());
+        lv_chunk_cnt.push_back((uint32_t)big_chunks.size() - lv_chunk_off.back());
+        lv_rs.push_back(lv_big_cnt.back()); lv_rs.push_back(lv_chunk_cnt.back());
+        /* rounds until the longest range's parts fit if its pivots split evenly, and one more */
+        uint32_t longest = 0, r = 1;
+        for (const uint2& t : T) longest = std::max(longest, t.y);
+        while (longest > BLAS_CAP) { longest = (longest + 1) / 2; r++; }
+        lv_rounds.push_back(r);
     }
     std::vector<uint32_t> depth_idx, depth_off;
     for (size_t d = 0; d < J->by_depth.size(); d++) {
         depth_off.push_back((uint32_t)depth_idx.size());
         depth_idx.insert(depth_idx.end(), J->by_depth[d].begin(), J->by_depth[d].end());
     }
-    const uint32_t list_cap = n / BLAS_CAP + 4, small_cap = n / 2 + 4;
+    const uint32_t list_cap = n / BLAS_CAP + 4, small_cap = n / 2 + 4, chunk_cap = n / BLAS_CHUNK + list_cap + 4;
     /* device scratch: items, ids, perm, key, Lp, Rp, bounds, lists, counters, plan */
     size_t o = 0;
     auto take = [&](size_t bytes) { const size_t r = o; o += (bytes + 255) & ~(size_t)255; return r; };
     const size_t o_it = take((size_t)n * 36), o_ids = take((size_t)n * 4), o_perm = take((size_t)n * 4), o_key = take((size_t)n * 4);
     const size_t o_lp = take((size_t)n * 4), o_rp = take((size_t)n * 4), o_bnd = take((size_t)nn * 24);
     const size_t o_l0 = take((size_t)list_cap * 8), o_l1 = take((size_t)list_cap * 8), o_sm = take((size_t)small_cap * 8);
-    const size_t o_ctr = take(16);
+    const size_t o_pc0 = take((size_t)list_cap * 8), o_pc1 = take((size_t)list_cap * 8);
+    const size_t o_ch0 = take((size_t)chunk_cap * 16), o_ch1 = take((size_t)chunk_cap * 16);
+    const size_t o_cc = take((size_t)chunk_cap * 8), o_cpre = take((size_t)chunk_cap * 8), o_part = take((size_t)chunk_cap * 24);
+    const size_t o_ptot = take((size_t)list_cap * 8), o_kc = take((size_t)list_cap * 4), o_axis = take((size_t)list_cap);
+    const size_t o_ctr = take(32);   /* round counts A, B; overflow; short pieces */
     const size_t o_tasks = take(tasks.size() * 8 + 8), o_spans = take(spans.size() * 16 + 16), o_big = take(big.size() * 8 + 8);
+    const size_t o_bpc = take(big_pchunk.size() * 8 + 8), o_bch = take(big_chunks.size() * 16 + 16), o_lvrs = take(lv_rs.size() * 4 + 8);
     const size_t o_pn = take((size_t)nn * sizeof(blas_pnode)), o_didx = take(depth_idx.size() * 4 + 4);
     const size_t o_plan = o_tasks, plan_bytes = o - o_tasks;
     char* d = nullptr;
@@ -579,6 +748,9 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     memcpy(h.data() + (o_tasks - o_plan), tasks.data(), tasks.size() * 8);
     memcpy(h.data() + (o_spans - o_plan), spans.data(), spans.size() * 16);
     memcpy(h.data() + (o_big - o_plan), big.data(), big.size() * 8);
+    memcpy(h.data() + (o_bpc - o_plan), big_pchunk.data(), big_pchunk.size() * 8);
+    memcpy(h.data() + (o_bch - o_plan), big_chunks.data(), big_chunks.size() * 16);
+    memcpy(h.data() + (o_lvrs - o_plan), lv_rs.data(), lv_rs.size() * 4);
     memcpy(h.data() + (o_pn - o_plan), J->nodes.data(), (size_t)nn * sizeof(blas_pnode));
     memcpy(h.data() + (o_didx - o_plan), depth_idx.data(), depth_idx.size() * 4);
     cudaError_t err = cudaMemcpyAsync(d + o_plan, h.data(), plan_bytes, cudaMemcpyHostToDevice, st);
@@ -590,11 +762,24 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     uint32_t* Rp = (uint32_t*)(d + o_rp);
     float* bnd = (float*)(d + o_bnd);
     uint2* lists[2] = { (uint2*)(d + o_l0), (uint2*)(d + o_l1) };
+    uint2* pchs[2] = { (uint2*)(d + o_pc0), (uint2*)(d + o_pc1) };
+    uint4* chs[2] = { (uint4*)(d + o_ch0), (uint4*)(d + o_ch1) };
+    uint2* cc = (uint2*)(d + o_cc);
+    uint2* cpre = (uint2*)(d + o_cpre);
+    float* part = (float*)(d + o_part);
+    uint2* ptot = (uint2*)(d + o_ptot);
+    uint32_t* kc = (uint32_t*)(d + o_kc);
+    uint8_t* axis = (uint8_t*)(d + o_axis);
     uint2* small = (uint2*)(d + o_sm);
     uint32_t* ctr = (uint32_t*)(d + o_ctr);
     const uint2* d_tasks = (const uint2*)(d + o_tasks);
     const uint4* d_spans = (const uint4*)(d + o_spans);
     const uint2* d_big = (const uint2*)(d + o_big);
+    const uint2* d_bpc = (const uint2*)(d + o_bpc);
+    const uint4* d_bch = (const uint4*)(d + o_bch);
+    const uint32_t* d_lvrs = (const uint32_t*)(d + o_lvrs);
+    uint32_t* rsb = ctr;              /* rsb[0..1], rsb[2..3]: pieces and chunks of a round */
+    uint32_t* cst = ctr + 4;          /* cst[0] overflow, cst[1] short pieces */
     const blas_pnode* d_pn = (const blas_pnode*)(d + o_pn);
     const uint32_t* d_didx = (const uint32_t*)(d + o_didx);
     if (err == cudaSuccess) err = cudaFuncSetAttribute(k_blas_sort_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, BLAS_SMALL_SMEM);
@@ -605,33 +790,52 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         err = cudaGetLastError();
         J->launches++;
     }
-    uint32_t* h_ctr = nullptr;
-    if (err == cudaSuccess) err = cudaMallocHost((void**)&h_ctr, 16);
+    static thread_local uint32_t* h_ctr = nullptr;   /* pinned read-back of the round state */
+    if (err == cudaSuccess && !h_ctr) err = cudaMallocHost((void**)&h_ctr, 32);
     for (size_t L = 0; err == cudaSuccess && L < J->by_level.size(); L++) {
         if (lv_span_cnt[L]) {
             k_blas_sort_small<true><<<lv_span_cnt[L], BLAS_SMALL_THREADS, BLAS_SMALL_SMEM, st>>>(d_spans + lv_span_off[L], nullptr, lv_span_cnt[L],
                                                                                                  d_tasks, it, n, key, perm);
             J->launches++;
         }
-        if (lv_big_cnt[L]) {
-            k_blas_axis<<<lv_big_cnt[L], BLAS_BIG_THREADS, 0, st>>>(d_big + lv_big_off[L], lv_big_cnt[L], it, n, perm, key);
-            J->launches++;
-            const uint2* curl = d_big + lv_big_off[L];
-            uint32_t ncur = lv_big_cnt[L], flip = 0;
-            err = cudaMemsetAsync(ctr, 0, 8, st);
-            while (err == cudaSuccess && ncur) {
-                if ((err = cudaMemsetAsync(ctr, 0, 4, st)) != cudaSuccess) break;
-                k_blas_part_big<<<ncur, BLAS_BIG_THREADS, 0, st>>>(curl, ncur, key, perm, Lp, Rp, lists[flip], list_cap, small, small_cap, ctr);
-                J->launches++;
-                if ((err = cudaGetLastError()) != cudaSuccess) break;
-                if ((err = cudaMemcpyAsync(h_ctr, ctr, 12, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+        if (lv_big_cnt[L]) {   /* long ranges: axis and keys, then partition rounds until every part fits */
+            const uint2* cur_p = d_big + lv_big_off[L];
+            const uint2* cur_pc = d_bpc + lv_big_off[L];
+            const uint4* cur_c = d_bch + lv_chunk_off[L];
+            const uint32_t np = lv_big_cnt[L], nch = lv_chunk_cnt[L];
+            k_blas_chunk_bounds<<<nch, BLAS_CHUNK_THREADS, 0, st>>>(cur_p, cur_c, nch, it, n, perm, part);
+            k_blas_range_axis<<<(np + 3) / 4, 128, 0, st>>>(cur_pc, np, part, axis);
+            k_blas_chunk_keys<<<nch, BLAS_CHUNK_THREADS, 0, st>>>(cur_p, cur_c, nch, axis, it, n, perm, key);
+            J->launches += 3;
+            err = cudaMemsetAsync(ctr, 0, 32, st);
+            const uint32_t* rs_cur = d_lvrs + 2 * L;
+            const uint32_t grid_ch = chunk_cap, grid_p4 = (list_cap + 3) / 4, grid_p128 = (list_cap + 127) / 128;
+            uint32_t k = 0, rounds = lv_rounds[L];
+            while (err == cudaSuccess) {
+                for (uint32_t q = 0; q < rounds && err == cudaSuccess; q++, k++) {
+                    uint32_t* rs_next = rsb + 2 * (k & 1);
+                    if ((err = cudaMemsetAsync(rs_next, 0, 8, st)) != cudaSuccess) break;
+                    k_blas_part_count<<<grid_ch, BLAS_CHUNK_THREADS, 0, st>>>(cur_p, cur_c, rs_cur, key, cc);
+                    k_blas_part_prefix<<<grid_p4, 128, 0, st>>>(cur_pc, rs_cur, cc, cpre, ptot, kc);
+                    k_blas_part_rank<<<grid_ch, BLAS_CHUNK_THREADS, 0, st>>>(cur_p, cur_c, rs_cur, key, cpre, ptot, Lp, Rp, kc);
+                    k_blas_part_swap<<<grid_ch, BLAS_CHUNK_THREADS, 0, st>>>(cur_p, cur_c, rs_cur, kc, Lp, Rp, key, perm);
+                    k_blas_part_children<<<grid_p128, 128, 0, st>>>(cur_p, rs_cur, ptot, kc, Lp, Rp, lists[k & 1], pchs[k & 1], chs[k & 1],
+                                                                    list_cap, chunk_cap, small, small_cap, rs_next, cst);
+                    J->launches += 5;
+                    err = cudaGetLastError();
+                    rs_cur = rs_next; cur_p = lists[k & 1]; cur_pc = pchs[k & 1]; cur_c = chs[k & 1];
+                }
+                if (err != cudaSuccess) break;
+                /* one read-back per level (more only if its ranges split unevenly) */
+                if ((err = cudaMemcpyAsync(h_ctr, ctr, 24, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
                 if ((err = cudaStreamSynchronize(st)) != cudaSuccess) break;
-                if (h_ctr[2]) { *status = 1; break; }
-                ncur = h_ctr[0] < list_cap ? h_ctr[0] : 0;
-                curl = lists[flip]; flip ^= 1;
+                const uint32_t* hrs = h_ctr + 2 * ((k - 1) & 1);
+                if (h_ctr[4] || hrs[0] > list_cap || hrs[1] > chunk_cap) { *status = 1; break; }
+                if (hrs[0] == 0) break;
+                rounds = 2;
             }
             if (err != cudaSuccess || *status) break;
-            const uint32_t ns = h_ctr[1] < small_cap ? h_ctr[1] : 0;
+            const uint32_t ns = h_ctr[5] < small_cap ? h_ctr[5] : 0;
             if (ns) {
                 k_blas_sort_small<false><<<ns, BLAS_SMALL_THREADS, BLAS_SMALL_SMEM, st>>>(nullptr, small, ns, nullptr, it, n, key, perm);
                 J->launches++;
@@ -646,7 +850,6 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         J->launches++;
     }
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);
-    if (h_ctr) cudaFreeHost(h_ctr);
     cudaFreeAsync(d, st);
     return err;
 }
