@@ -7,7 +7,7 @@
  *              box and centroid (3526-3617); one warp per meshlet, a ballot keeps the order
  *   shape      a node of more than 8 items splits its range by count (halves, quarters, eighths),
  *              so node numbering, ranges and the list of sorted ranges depend on the item count
- *              only; the host lays them out (blas_plan) and the device does every data-dependent
+ *              only; the host lays them out (plan_node) and the device does every data-dependent
  *              step
  *   sorts      a sorted range at split depth d of a node at depth t sorts at level 3t + d; the
  *              ranges of one level are disjoint and read the order the previous level left.
@@ -16,15 +16,18 @@
  *              fj = !(key > pivot), the scans stop at the fi positions from the left and at the fj
  *              positions from the right, and the k-th left stop swaps with the k-th right stop
  *              while it lies at or before it.  Where the scans stop after the last swap follows
- *              from the next stops and the last swapped pair.  A range longer than BLAS_CAP is
- *              partitioned by one CTA in global memory until its pieces fit; pieces and short
- *              ranges are finished by one CTA in shared memory, one warp per piece.
+ *              from the next stops and the last swapped pair.
+ *   long       ranges longer than BLAS_CAP: chunks of BLAS_CHUNK positions, partition rounds of
+ *              five kernels over all long pieces of a level, round counts kept on the device
+ *   short      ranges and pieces of at most BLAS_CAP: one CTA per span in shared memory, one
+ *              warp per piece per round, pieces of at most BLAS_SEQ positions finished by one
+ *              thread with the sequential quicksort
  *   nodes      leaves and inner nodes written bottom-up, depth by depth, each node's box the
  *              union of its slots in slot order
  * Comparisons and the centroid (mn + mx) * 0.5 are IEEE single precision as in the reference.
- * Output is bit-identical to the host builder: every permutation step is the sequential one.
- * Overflow of a device work list (not reachable for consistent sizes) sets an error word that
- * the host reads.
+ * The node images are byte-identical to the reference's: every permutation step is the
+ * sequential one.  Overflow of a device work list (not reachable for consistent sizes) sets an
+ * error word that the host reads.
  */
 #include "sftg_types.h"
 #include "sftg_kernels.h"
@@ -394,7 +397,7 @@ __device__ __forceinline__ void warp_partition(float* Ks, uint32_t* Ps, uint16_t
     __syncwarp();
 }
 
-/* The reference's quicksort itself on [s, s + m) of the shared-memory arrays, by
+/* The reference's quicksort itself (sofren2.c:2895-2924) on [s, s + m) of the shared-memory arrays, by
  * one thread, the recursion kept as a stack of the pending (disjoint) pieces.  The scans carry
  * bounds that the pivot sentinel already guarantees. */
 __device__ __forceinline__ void seq_quicksort(float* Ks, uint32_t* Ps, int s, int m) {
