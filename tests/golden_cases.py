@@ -122,8 +122,9 @@ def blas_edge_scene():
     """Models at the edges of the BLAS builder (sofren2.c:2895-3062): 5 triangles (one leaf),
     9 (one split), one triangle repeated 3000 times (every centroid equal), 6000 triangles on a
     lattice in the plane z = 1 (no z extent, equal coordinates along x and y), three meshes of
-    5, 130 and 7 triangles (padding inside the model's meshlet run), and 60000 triangles with
-    coordinates on a 1/64 grid (ranges longer than one shared-memory sort, with ties)."""
+    5, 130 and 7 triangles (padding inside the model's meshlet run), 60000 triangles with
+    coordinates on a 1/64 grid (ranges longer than one shared-memory sort, with ties), a single
+    triangle, and 40 triangles that are all padding (three equal indices: no BLAS at all)."""
     key = ("blas_edges",)
     if key in _cache:
         return _cache[key]
@@ -145,7 +146,8 @@ def blas_edge_scene():
         return raw(v, np.arange(3 * n).reshape(-1, 3))
 
     def add(meshes):
-        ms = [scenes.build_meshlets(m) for m in meshes]
+        with np.errstate(invalid="ignore"):   # a lone triangle's cone: sqrt of a rounding-negative 1 - d^2
+            ms = [scenes.build_meshlets(m) for m in meshes]
         sc.add_model(scenes.Model(ms, [mat] * len(ms)))
 
     add([soup(5)])
@@ -158,6 +160,8 @@ def blas_edge_scene():
     add([raw(lat, np.concatenate([q, q[: 6000 - len(q)]]) if len(q) < 6000 else q[:6000])])
     add([soup(5), soup(130), soup(7)])
     add([soup(60000, grid=64)])
+    add([soup(1)])
+    add([raw(rng.uniform(-1, 1, (40, 3)), np.repeat(np.arange(40), 3).reshape(-1, 3))])
     sc.frames.append(scenes._camera_frame(64, 64))
     _cache[key] = sc
     return sc

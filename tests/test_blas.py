@@ -3,6 +3,7 @@
 all centroids equal, a flat lattice, padding between meshes, 60000 triangles on a grid), as
 node images byte for byte against the reference's own build.  The oracle is pinned on the CPU;
 the device build (at model creation) is read back through sft_model_get_blas."""
+import numpy as np
 import pytest
 
 import golden_cases as gc
@@ -17,7 +18,7 @@ def test_oracle_blas_matches_reference(golden, name):
         nodes, root = o.model_blas(mi)
         assert len(nodes) // 256 == n, f"model {mi}: {len(nodes) // 256} nodes, reference {n}"
         assert root == 0
-        assert gc.sha(nodes) == digest, f"model {mi} differs from the reference's BLAS"
+        assert gc.sha(np.frombuffer(nodes, np.uint8)) == digest, f"model {mi} differs from the reference's BLAS"
 
 
 @pytest.mark.gpu
@@ -30,7 +31,7 @@ def test_gpu_blas_matches_reference(renderer, golden, name):
             nodes, root = renderer.model_blas(h, mi)
             assert len(nodes) // 256 == n, f"model {mi}: {len(nodes) // 256} nodes, reference {n}"
             assert root == 0
-            if gc.sha(nodes) != digest:
+            if gc.sha(np.frombuffer(nodes, np.uint8)) != digest:
                 ref, _ = Oracle(gc.blas_blob(name)).model_blas(mi)
                 bad = [k for k in range(n) if nodes[k * 256:(k + 1) * 256] != ref[k * 256:(k + 1) * 256]]
                 pytest.fail(f"model {mi}: {len(bad)} of {n} nodes differ from the reference's BLAS; first {bad[:5]}")
