@@ -670,7 +670,10 @@ cudaError_t sftg_blas_begin(sftg_blas_job** out, const float* attr, const uint8_
     BK(cudaMemcpyAsync(&total, J->d_cnt + 2 * (size_t)nm, 4, cudaMemcpyDeviceToHost, st));
     BK(cudaStreamSynchronize(st));
     J->n = total;
-    if (total) plan_node(*J, 0, total, 0);
+    if (total) {
+        J->nodes.reserve(total / 3 + 16);
+        plan_node(*J, 0, total, 0);
+    }
     *n_items = total;
     *n_nodes = (uint32_t)J->nodes.size();
     return cudaSuccess;
@@ -747,16 +750,27 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     const size_t o_plan = o_tasks, plan_bytes = o - o_tasks;
     char* d = nullptr;
     BK(cudaMallocAsync((void**)&d, o, st));
-    std::vector<char> h(plan_bytes);
-    memcpy(h.data() + (o_tasks - o_plan), tasks.data(), tasks.size() * 8);
-    memcpy(h.data() + (o_spans - o_plan), spans.data(), spans.size() * 16);
-    memcpy(h.data() + (o_big - o_plan), big.data(), big.size() * 8);
-    memcpy(h.data() + (o_bpc - o_plan), big_pchunk.data(), big_pchunk.size() * 8);
-    memcpy(h.data() + (o_bch - o_plan), big_chunks.data(), big_chunks.size() * 16);
-    memcpy(h.data() + (o_lvrs - o_plan), lv_rs.data(), lv_rs.size() * 4);
-    memcpy(h.data() + (o_pn - o_plan), J->nodes.data(), (size_t)nn * sizeof(blas_pnode));
-    memcpy(h.data() + (o_didx - o_plan), depth_idx.data(), depth_idx.size() * 4);
-    cudaError_t err = cudaMemcpyAsync(d + o_plan, h.data(), plan_bytes, cudaMemcpyHostToDevice, st);
+    /* the plan goes up from a page-locked staging buffer kept per host thread; the previous
+     * build's copy out of it finished when that build synchronised its stream */
+    static thread_local char* stage = nullptr;
+    static thread_local size_t stage_cap = 0;
+    if (plan_bytes > stage_cap) {
+        if (stage) cudaFreeHost(stage);
+        stage = nullptr; stage_cap = 0;
+        const size_t cap = plan_bytes + plan_bytes / 4;
+        if (cudaMallocHost((void**)&stage, cap) != cudaSuccess) { cudaFreeAsync(d, st); return cudaErrorMemoryAllocation; }
+        stage_cap = cap;
+    }
+    char* h = stage;
+    memcpy(h + (o_tasks - o_plan), tasks.data(), tasks.size() * 8);
+    memcpy(h + (o_spans - o_plan), spans.data(), spans.size() * 16);
+    memcpy(h + (o_big - o_plan), big.data(), big.size() * 8);
+    memcpy(h + (o_bpc - o_plan), big_pchunk.data(), big_pchunk.size() * 8);
+    memcpy(h + (o_bch - o_plan), big_chunks.data(), big_chunks.size() * 16);
+    memcpy(h + (o_lvrs - o_plan), lv_rs.data(), lv_rs.size() * 4);
+    memcpy(h + (o_pn - o_plan), J->nodes.data(), (size_t)nn * sizeof(blas_pnode));
+    memcpy(h + (o_didx - o_plan), depth_idx.data(), depth_idx.size() * 4);
+    cudaError_t err = cudaMemcpyAsync(d + o_plan, h, plan_bytes, cudaMemcpyHostToDevice, st);
     float* it = (float*)(d + o_it);
     uint32_t* ids = (uint32_t*)(d + o_ids);
     uint32_t* perm = (uint32_t*)(d + o_perm);
@@ -852,7 +866,8 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         err = cudaGetLastError();
         J->launches++;
     }
-    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    const cudaError_t se = cudaStreamSynchronize(st);   /* also on error: the staged plan is reused */
+    if (err == cudaSuccess) err = se;
     cudaFreeAsync(d, st);
     return err;
 }
