@@ -39,6 +39,8 @@
 #define BLAS_SMALL_THREADS 512
 #define BLAS_SMALL_WARPS (BLAS_SMALL_THREADS / 32)
 #define BLAS_SEQ 32              /* pieces of at most this many positions: one thread each */
+#define BLAS_CTA_PIECE 1024      /* pieces longer than this: partitioned by the whole CTA */
+#define BLAS_BIGQ 8              /* pending such pieces (disjoint, so at most 3 within BLAS_CAP) */
 #define BLAS_SEQ_STACK 16        /* pending disjoint pieces of >= 2 positions within BLAS_SEQ */
 #define BLAS_SMALL_SMEM (BLAS_CAP * 4 * 2 + BLAS_CAP * 2 * 2 + (BLAS_CAP / 2) * 4 * 3)
 
@@ -422,6 +424,52 @@ __device__ __forceinline__ void seq_quicksort(float* Ks, uint32_t* Ps, int s, in
     }
 }
 
+/* The whole CTA partitions the piece [s, s + m) of the shared-memory arrays (m > BLAS_CTA_PIECE):
+ * the same stop ranks as warp_partition, with one block scan over contiguous runs of positions.
+ * Returns i, j (relative) in s_ij; every thread takes part. */
+__device__ __forceinline__ void cta_partition(float* Ks, uint32_t* Ps, uint16_t* Lp, uint16_t* Rp, int s, int m, uint32_t* ws,
+                                              uint32_t* s_tot, int* s_ij) {
+    const float p = Ks[s + m / 2];
+    const int E = (m + BLAS_SMALL_THREADS - 1) / BLAS_SMALL_THREADS;
+    const int x0 = (int)threadIdx.x * E, xe = min(x0 + E, m);
+    uint32_t ni = 0, nj = 0;
+    for (int x = x0; x < xe; x++) { const float k = Ks[s + x]; ni += !(k < p); nj += !(k > p); }
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t v = ni | (nj << 16);
+    uint32_t sc = v;
+    for (int d = 1; d < 32; d <<= 1) { const uint32_t o = __shfl_up_sync(0xffffffffu, sc, d); if (lane >= (uint32_t)d) sc += o; }
+    if (lane == 31) ws[w] = sc;
+    if (threadIdx.x == 0) s_tot[0] = 0;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (uint32_t k = 0; k < BLAS_SMALL_WARPS; k++) { if (k < w) before += ws[k]; all += ws[k]; }
+    const uint32_t ex = before + sc - v;
+    const int CI = (int)(all & 0xFFFFu), CJ = (int)(all >> 16);
+    int r = (int)(ex & 0xFFFFu), pj = (int)(ex >> 16);
+    uint32_t valid = 0;
+    for (int x = x0; x < xe; x++) {
+        const float k = Ks[s + x];
+        if (!(k < p)) { Lp[s + r] = (uint16_t)(s + x); valid += (r < CJ - pj); r++; }
+        if (!(k > p)) { Rp[s + CJ - 1 - pj] = (uint16_t)(s + x); pj++; }
+    }
+    valid = __reduce_add_sync(0xffffffffu, valid);
+    if (lane == 0 && valid) atomicAdd(&s_tot[0], valid);
+    __syncthreads();
+    const int K = (int)s_tot[0];
+    for (int q = (int)threadIdx.x; q < K; q += BLAS_SMALL_THREADS) {
+        const int a = Lp[s + q], b = Rp[s + q];
+        const float ka = Ks[a]; Ks[a] = Ks[b]; Ks[b] = ka;
+        const uint32_t pa = Ps[a]; Ps[a] = Ps[b]; Ps[b] = pa;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int i, j;
+        final_ij((int)Lp[s + K - 1] - s, (int)Rp[s + K - 1] - s, K < CI ? (int)Lp[s + K] - s : 0x7fffffff, K < CJ ? (int)Rp[s + K] - s : -1, i, j);
+        s_ij[0] = i; s_ij[1] = j;
+    }
+    __syncthreads();
+}
+
 /* One CTA finishes the quicksorts inside one span of at most BLAS_CAP positions.
  * PLAN: the span holds whole ranges of one level (tasks[z .. z + w)); each warp takes ranges,
  *       picks their axes and writes their keys.  Otherwise the span is one piece of a long
@@ -444,6 +492,8 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
     __shared__ int ncnt[3];
     __shared__ float sbnd[BLAS_SMALL_WARPS][6];
     __shared__ int s_axis;
+    __shared__ uint32_t bigq[BLAS_BIGQ], ws[BLAS_SMALL_WARPS], s_tot[1];
+    __shared__ int nbig, s_ij[2];
     if (blockIdx.x >= nspans) return;
     uint32_t s0, m0;
     if (PLAN) { s0 = spans[blockIdx.x].x; m0 = spans[blockIdx.x].y; }
@@ -452,7 +502,7 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t x = threadIdx.x; x < m0; x += BLAS_SMALL_THREADS) Ps[x] = perm[s0 + x];
     if (!PLAN) for (uint32_t x = threadIdx.x; x < m0; x += BLAS_SMALL_THREADS) Ks[x] = key[s0 + x];
-    if (threadIdx.x == 0) { ncnt[0] = 0; ncnt[1] = 0; ncnt[2] = 0; }
+    if (threadIdx.x == 0) { ncnt[0] = 0; ncnt[1] = 0; ncnt[2] = 0; nbig = 0; }
     __syncthreads();
     if (PLAN) {
         const uint32_t t0 = spans[blockIdx.x].z, nt = spans[blockIdx.x].w;
@@ -486,8 +536,8 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
                 const float* c = it + (size_t)(6 + s_axis) * n;
                 for (uint32_t x = threadIdx.x; x < tc; x += BLAS_SMALL_THREADS) Ks[ts + x] = c[Ps[ts + x]];
                 if (threadIdx.x == 0) {
-                    const int q = tc > BLAS_SEQ ? 0 : 2;
-                    (q ? seq : lst0)[0] = (ts << 16) | tc; ncnt[q] = 1;
+                    if (tc > BLAS_CTA_PIECE) { bigq[0] = (ts << 16) | tc; nbig = 1; }
+                    else { const int q = tc > BLAS_SEQ ? 0 : 2; (q ? seq : lst0)[0] = (ts << 16) | tc; ncnt[q] = 1; }
                 }
             }
         } else {
@@ -525,14 +575,44 @@ __global__ void __launch_bounds__(BLAS_SMALL_THREADS) k_blas_sort_small(const ui
                     for (int u = 0; u < 4; u++) if (q[u] != 0xFFFFFFFFu) Ks[ts + b + 32u * u] = v[u];
                 }
                 if (lane == 0) {
-                    const int q = tc > BLAS_SEQ ? 0 : 2;
-                    const int k = atomicAdd(&ncnt[q], 1);
-                    if (k < BLAS_CAP / 2) (q ? seq : lst0)[k] = (ts << 16) | tc;
+                    if (tc > BLAS_CTA_PIECE) {
+                        const int k = atomicAdd(&nbig, 1);
+                        if (k < BLAS_BIGQ) bigq[k] = (ts << 16) | tc;
+                    } else {
+                        const int q = tc > BLAS_SEQ ? 0 : 2;
+                        const int k = atomicAdd(&ncnt[q], 1);
+                        if (k < BLAS_CAP / 2) (q ? seq : lst0)[k] = (ts << 16) | tc;
+                    }
                 }
             }
         }
     } else if (threadIdx.x == 0 && m0 >= 2) {
-        if (m0 > BLAS_SEQ) { lst0[0] = m0; ncnt[0] = 1; } else { seq[0] = m0; ncnt[2] = 1; }
+        if (m0 > BLAS_CTA_PIECE) { bigq[0] = m0; nbig = 1; }
+        else if (m0 > BLAS_SEQ) { lst0[0] = m0; ncnt[0] = 1; } else { seq[0] = m0; ncnt[2] = 1; }
+    }
+    /* long pieces first, one at a time by the whole CTA; their parts of at most BLAS_CTA_PIECE
+     * positions go to the warp rounds (or straight to the one-thread finish) */
+    for (;;) {
+        __syncthreads();
+        const int nb = min(nbig, BLAS_BIGQ);
+        if (nb == 0) break;
+        const uint32_t v = bigq[nb - 1];
+        __syncthreads();
+        if (threadIdx.x == 0) nbig = nb - 1;
+        const int s = (int)(v >> 16), m = (int)(v & 0xFFFFu);
+        cta_partition(Ks, Ps, Lp, Rp, s, m, ws, s_tot, s_ij);
+        if (threadIdx.x == 0) {
+            const int i = s_ij[0], j = s_ij[1];
+            const uint32_t ps[2] = { (uint32_t)s, (uint32_t)(s + i) };
+            const int pm[2] = { j + 1, m - i };
+            for (int h = 0; h < 2; h++) {
+                if (pm[h] < 2) continue;
+                const uint32_t e = (ps[h] << 16) | (uint32_t)pm[h];
+                if (pm[h] > BLAS_CTA_PIECE) { if (nbig < BLAS_BIGQ) bigq[nbig++] = e; }
+                else if (pm[h] > BLAS_SEQ) { if (ncnt[0] < BLAS_CAP / 2) lst0[ncnt[0]++] = e; }
+                else { if (ncnt[2] < BLAS_CAP / 2) seq[ncnt[2]++] = e; }
+            }
+        }
     }
     int cur = 0;
     for (;;) {
