@@ -1,7 +1,7 @@
 """BLAS construction (sft__blas_build_model, sofren2.c:3526-3617, over the 8-wide builder
 2895-3062): every model of the golden cases and of the BLAS edge models (one leaf, one split,
-all centroids equal, a flat lattice, padding between meshes, 60000 triangles on a grid), as
-node images byte for byte against the reference's own build.  The oracle is pinned on the CPU;
+all centroids equal, a flat lattice, padding between meshes, 60000 triangles on a grid, a single
+triangle, only padding), as node images byte for byte against the reference's own build.  The oracle is pinned on the CPU;
 the device build (at model creation) is read back through sft_model_get_blas."""
 import numpy as np
 import pytest
