@@ -46,6 +46,7 @@ CONFIGS = {
     5: dict(gen="config5", samples=None, name="served_16_scenes_poisson", width=None, height=None),
     6: dict(gen="config3", samples=None, name="raycast_atrium_1m_rays", width=None, height=None, rays=1 << 20),
     7: dict(gen="config3", samples=None, name="blas_build_atrium_249k_triangles", width=None, height=None, model=0),
+    8: dict(gen=None, samples=None, name="pose_22_bones_65536_requests", width=None, height=None, requests=1 << 16),
 }
 SERVE_RATES = (100, 500, 1000, 1500, 2000, 5000)   # requests/s offered
 SERVE_BUDGET = 150 << 30                      # device-memory admission budget, bytes
@@ -678,6 +679,126 @@ def run_blas(args, cfg) -> dict:
     return line if rank == 0 else None
 
 
+def run_pose(args, cfg) -> dict:
+    """Skeletal poses (sft_pose_update, one warp per request): 2^16 seeded (animation, time)
+    requests on the 22-bone rig, posed and global matrices out.  `value` through
+    sftg_pose_eval_device with requests and outputs in device memory; `e2e` through sftg_pose_eval
+    with page-locked host arrays (requests H2D, matrices D2H inside the timed region)."""
+    import torch
+    import torch.distributed as dist
+    from sofren2_gb300 import runtime, scenes
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    os.environ["SFT_CUDA_DEVICE"] = str(local)
+    dev = torch.device("cuda", local)
+    rig = scenes.pose_rig()
+    nb = len(rig["bones"])
+    n = cfg["requests"]
+    req = scenes.pose_requests(rig, n, seed=8)
+    R = runtime.Renderer(64, 64, 1)
+    sk = R.skeleton_upload(rig)
+    rec = np.zeros(n, runtime.POSE_REQUEST_DTYPE)
+    rec["skeleton"] = sk
+    rec["animation"] = [a for a, _ in req]
+    rec["time"] = [t for _, t in req]
+    off = (np.arange(n, dtype=np.uint32) * nb).astype(np.uint32)
+    d_req = torch.from_numpy(rec.view(np.uint8).copy()).to(dev)
+    d_off = torch.from_numpy(off.view(np.uint8).copy()).to(dev)
+    d_posed = torch.zeros(n * nb * 16, dtype=torch.float32, device=dev)
+    d_glob = torch.zeros(n * nb * 16, dtype=torch.float32, device=dev)
+    pin_req = torch.from_numpy(rec.view(np.uint8).copy()).pin_memory()
+    pin_posed = torch.zeros(n * nb * 16, dtype=torch.float32).pin_memory()
+    pin_glob = torch.zeros(n * nb * 16, dtype=torch.float32).pin_memory()
+    host_req = pin_req.numpy().view(runtime.POSE_REQUEST_DTYPE)
+    host_posed, host_glob = pin_posed.numpy(), pin_glob.numpy()
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(R.stream(), device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(step, k):
+        times = []
+        for _ in range(k):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return times
+
+    dev_step = lambda: R.pose_eval_device(d_req.data_ptr(), d_off.data_ptr(), n, d_posed.data_ptr(), d_glob.data_ptr())   # noqa: E731
+    e2e_step = lambda: R.pose_eval_host(host_req, host_posed, host_glob)                                                  # noqa: E731
+    for _ in range(args.warmup):
+        dev_step()
+        e2e_step()
+    torch.cuda.synchronize()
+    assert d_posed.cpu().numpy().tobytes() == host_posed.tobytes(), "device and host pose entry points disagree"
+    assert d_glob.cpu().numpy().tobytes() == host_glob.tobytes(), "device and host pose entry points disagree"
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dev_times = timed(dev_step, args.steps)
+    e2e_times = timed(e2e_step, args.steps)
+    clk = clocks.stop()
+    ms_dev, ms_e2e = max_over_ranks([float(np.sum(dev_times)), float(np.sum(e2e_times))], device=f"cuda:{local}")
+    peaks = _peaks()
+    per_launch = float(np.mean(dev_times))
+    alg = n * (12 + 4 + 2 * nb * 64)
+    achieved = alg / (per_launch * 1e-3) / 1e9
+    valid = int(((rec["animation"] >= 0) & (rec["animation"] < len(rig["anims"]))).sum())
+    line = {
+        "metric": "poses_per_second", "value": job_throughput(args.steps * n, world, ms_dev), "unit": "poses/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded rig and requests)",
+        "config": {"workload": cfg["name"], "requests": n, "bones": nb, "animations": len(rig["anims"]),
+                   "requests_in_range": valid,
+                   "l2": "flushed between steps (512 MiB device write, outside the timed events); outputs 184 MB per step",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": job_throughput(args.steps * n, world, ms_e2e), "unit": "poses/s",
+                "h2d_bytes_per_step": int(n * 12), "d2h_bytes_per_step": int(2 * n * nb * 64)},
+        "gpu_launches": int(args.steps),
+        "roofline": {"kernel": "k_pose", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "algorithmic_bytes": alg,
+                     "peak_source": peaks["src"],
+                     "note": "algorithmic bytes: request, offset and the posed and global matrices written; keys read from L2"},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = pose_cpu_baseline(rig, req, seconds=args.cpu_seconds)
+    R.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def pose_cpu_baseline(rig: dict, req: list, seconds: float = 12.0, chunk: int = 4096) -> dict:
+    """The oracle's restated sft_pose_update (bit-identical to the reference's) on one host core,
+    over consecutive chunks of the same requests until `seconds` have passed."""
+    from oracle_lib import build_oracle, oracle_pose, pose_blob
+    build_oracle()
+    nb = len(rig["bones"])
+    done, t = 0, 0.0
+    while t < seconds and done < len(req):
+        part = req[done:done + chunk]
+        blob = pose_blob(rig, part)
+        t0 = time.perf_counter()
+        oracle_pose(blob, nb, len(part))
+        t += time.perf_counter() - t0
+        done += len(part)
+    return {"value": done / t, "unit": "poses/s", "cores": 1, "kind": "port",
+            "sample": f"the first {done} requests of the same set (oracle/sft_oracle.c sfto_pose_eval, one thread, as "
+                      "the reference's sft_pose_update runs on the calling thread)"}
+
+
 def blas_cpu_baseline(blob: bytes, tris: int, seconds: float = 12.0) -> dict:
     """The oracle's restated BLAS builder (the reference's recursive build, one thread) on the
     same model, repeated until `seconds` have passed."""
@@ -777,6 +898,29 @@ def run_reference(args, cfg) -> dict | None:
                                  "sample": f"{len(times)} steps of {chunk} rays after {max(1, args.warmup)} warm-up, scalar "
                                            "restatement of sft_raycast_instance (oracle/sft_oracle.c), one thread"},
                 "e2e": {"value": rps, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.config == 8:   # bounded sample: 4096 requests per step, consecutive chunks of the set
+        from oracle_lib import oracle_pose, pose_blob
+        rig = scenes.pose_rig()
+        nb = len(rig["bones"])
+        req = scenes.pose_requests(rig, cfg["requests"], seed=8)
+        chunk, times = 4096, []
+        for k in range(max(1, args.warmup) + args.steps):
+            part = req[(k * chunk) % len(req):][:chunk]
+            blob = pose_blob(rig, part)
+            t0 = time.perf_counter()
+            oracle_pose(blob, nb, len(part))
+            if k >= max(1, args.warmup):
+                times.append((time.perf_counter() - t0) / len(part))
+        pps = len(times) / sum(times)
+        return {"metric": "poses_per_second", "value": pps, "unit": "poses/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * chunk / pps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded rig and requests)", "impl": "reference",
+                "config": {"workload": cfg["name"], "requests": cfg["requests"], "sample": f"{chunk} requests per step"},
+                "cpu_baseline": {"value": pps, "unit": "poses/s", "cores": 1, "kind": "port",
+                                 "sample": f"{len(times)} steps of {chunk} requests after {max(1, args.warmup)} warm-up, "
+                                           "restated sft_pose_update (oracle/sft_oracle.c), one thread"},
+                "e2e": {"value": pps, "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if args.config == 7:   # each step one build of the same model
         sc = blas_scene(cfg)
         o = Oracle(sc.to_bytes())
@@ -859,6 +1003,8 @@ def main():
         line = run_raycast(args, cfg)
     elif args.config == 7:
         line = run_blas(args, cfg)
+    elif args.config == 8:
+        line = run_pose(args, cfg)
     else:
         line = run_ours(args, cfg)
     if line is not None:

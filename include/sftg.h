@@ -217,6 +217,12 @@ int sftg_skeleton_upload(sftg_ctx* ctx, const sftg_bone_desc* bones, uint32_t bo
  * of requests 0..k-1), its bones' matrices; host memory.  A request whose animation index is out
  * of range leaves its matrices untouched, as sft_pose_update returns early. */
 int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* requests, uint32_t n, float* posed, float* global);
+/* The same on device arrays, asynchronous on the context's stream (sftg_stream): request k
+ * writes its bone_count matrices at d_posed + 16 * d_off[k] (and d_global, when not NULL); the
+ * caller sizes the outputs for its offsets.  Requests naming no uploaded skeleton, or an
+ * animation out of range, leave their matrices untouched. */
+int sftg_pose_eval_device(sftg_ctx* ctx, const sftg_pose_request* d_requests, const uint32_t* d_off, uint32_t n, float* d_posed,
+                          float* d_global);
 
 /* Ray queries against resident models (sft_raycast_instance, sofren2.c:3733-3837), any number in
  * one launch, one thread per ray.  A ray names a model and its instance transform; results equal

@@ -1208,6 +1208,27 @@ extern "C" int sftg_skeleton_upload(sftg_ctx* ctx, const sftg_bone_desc* bones, 
     return SFTG_OK;
 }
 
+static sftg_pose_tables pose_tables(const sftg_ctx* ctx) {
+    sftg_pose_tables T;
+    T.n_skels = (uint32_t)ctx->h_skels.size();
+    T.skels = (const sftg_skel_dev*)ctx->p_skels.ptr; T.bones = (const sftg_bone_dev*)ctx->p_bones.ptr;
+    T.anims = (const sftg_anim_dev*)ctx->p_anims.ptr; T.samplers = (const sftg_sampler_dev*)ctx->p_samplers.ptr;
+    T.channels = (const sftg_channel_desc*)ctx->p_channels.ptr; T.keys = (const float*)ctx->p_keys.ptr;
+    T.order = (const uint16_t*)ctx->p_order.ptr; T.levels = (const uint16_t*)ctx->p_levels.ptr;
+    return T;
+}
+
+extern "C" int sftg_pose_eval_device(sftg_ctx* ctx, const sftg_pose_request* d_reqs, const uint32_t* d_off, uint32_t n, float* d_posed,
+                                     float* d_global) {
+    if (!ctx || (n && (!d_reqs || !d_off || !d_posed))) return SFTG_E_ARG;
+    if (!n) return SFTG_OK;
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->h_skels.empty()) return set_err(ctx, SFTG_E_ARG, "no skeleton uploaded");
+    sftg_launch_pose(pose_tables(ctx), d_reqs, d_off, n, d_posed, d_global, ctx->stream);
+    CK(cudaGetLastError());
+    return SFTG_OK;
+}
+
 extern "C" int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* reqs, uint32_t n, float* posed, float* global) {
     if (!ctx || (n && (!reqs || !posed))) return SFTG_E_ARG;
     if (!n) return SFTG_OK;
@@ -1232,23 +1253,31 @@ extern "C" int sftg_pose_eval(sftg_ctx* ctx, const sftg_pose_request* reqs, uint
     float* d_global = global ? d_posed + (size_t)total * 16 : nullptr;
     CK(cudaMemcpyAsync(d_req, reqs, (size_t)n * sizeof(sftg_pose_request), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(d_off, off.data(), (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
-    sftg_pose_tables T;
-    T.skels = (const sftg_skel_dev*)ctx->p_skels.ptr; T.bones = (const sftg_bone_dev*)ctx->p_bones.ptr;
-    T.anims = (const sftg_anim_dev*)ctx->p_anims.ptr; T.samplers = (const sftg_sampler_dev*)ctx->p_samplers.ptr;
-    T.channels = (const sftg_channel_desc*)ctx->p_channels.ptr; T.keys = (const float*)ctx->p_keys.ptr;
-    T.order = (const uint16_t*)ctx->p_order.ptr; T.levels = (const uint16_t*)ctx->p_levels.ptr;
-    sftg_launch_pose(T, d_req, d_off, n, d_posed, d_global, ctx->stream);
+    sftg_launch_pose(pose_tables(ctx), d_req, d_off, n, d_posed, d_global, ctx->stream);
     CK(cudaGetLastError());
-    std::vector<float> hp((size_t)total * 16), hg(global ? (size_t)total * 16 : 0);
-    CK(cudaMemcpyAsync(hp.data(), d_posed, b_mat, cudaMemcpyDeviceToHost, ctx->stream));
-    if (global) CK(cudaMemcpyAsync(hg.data(), d_global, b_mat, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    /* a request with an out-of-range animation leaves its matrices as they were */
+    /* a request with an out-of-range animation leaves its matrices as they were: those are saved,
+     * the whole result is copied straight into the caller's arrays, and the saved ones put back */
+    std::vector<uint32_t> keep;
+    size_t keep_floats = 0;
     for (uint32_t k = 0; k < n; k++) {
         const sftg_skel_dev& sk = ctx->h_skels[reqs[k].skeleton];
-        if (reqs[k].animation < 0 || (uint32_t)reqs[k].animation >= sk.anim_count) continue;
-        memcpy(posed + (size_t)off[k] * 16, hp.data() + (size_t)off[k] * 16, (size_t)sk.bone_count * 64);
-        if (global) memcpy(global + (size_t)off[k] * 16, hg.data() + (size_t)off[k] * 16, (size_t)sk.bone_count * 64);
+        if (reqs[k].animation < 0 || (uint32_t)reqs[k].animation >= sk.anim_count) { keep.push_back(k); keep_floats += (size_t)sk.bone_count * 16; }
+    }
+    std::vector<float> saved(keep_floats * (global ? 2 : 1));
+    size_t q = 0;
+    for (uint32_t k : keep) {
+        const size_t c = (size_t)ctx->h_skels[reqs[k].skeleton].bone_count * 16;
+        memcpy(saved.data() + q, posed + (size_t)off[k] * 16, c * 4); q += c;
+        if (global) { memcpy(saved.data() + q, global + (size_t)off[k] * 16, c * 4); q += c; }
+    }
+    CK(cudaMemcpyAsync(posed, d_posed, b_mat, cudaMemcpyDeviceToHost, ctx->stream));
+    if (global) CK(cudaMemcpyAsync(global, d_global, b_mat, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    q = 0;
+    for (uint32_t k : keep) {
+        const size_t c = (size_t)ctx->h_skels[reqs[k].skeleton].bone_count * 16;
+        memcpy(posed + (size_t)off[k] * 16, saved.data() + q, c * 4); q += c;
+        if (global) { memcpy(global + (size_t)off[k] * 16, saved.data() + q, c * 4); q += c; }
     }
     return SFTG_OK;
 }

@@ -85,6 +85,7 @@ struct sftg_skel_dev { uint32_t bone_base, bone_count, anim_base, anim_count, or
 struct sftg_anim_dev { uint32_t sampler_base, channel_base; int32_t sampler_count, channel_count; float duration; uint32_t pad[3]; };
 struct sftg_sampler_dev { uint32_t input_base, output_base; int32_t count, is_step; };
 struct sftg_pose_tables {
+    uint32_t n_skels;              /* requests naming another skeleton leave their matrices untouched */
     const sftg_skel_dev* skels;
     const sftg_bone_dev* bones;
     const sftg_anim_dev* anims;

@@ -69,6 +69,7 @@ k_pose(const sftg_pose_tables T, const sftg_pose_request* __restrict__ reqs, con
     const int lane = threadIdx.x;
     if (k >= n) return;
     const sftg_pose_request R = reqs[k];
+    if (R.skeleton < 0 || (uint32_t)R.skeleton >= T.n_skels) return;
     const sftg_skel_dev sk = T.skels[R.skeleton];
     if (R.animation < 0 || R.animation >= (int)sk.anim_count) return;   /* sft_pose_update returns early */
     const sftg_anim_dev an = T.anims[sk.anim_base + R.animation];

@@ -60,7 +60,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sft_batch_begin": (v, []), "sft_batch_submit": (i32, []), "sft_batch_submit_async": (i32, [u32]),
         "sft_batch_done": (i32, [u32]), "sft_batch_wait": (i32, [u32]),
         "sftx_scene_render_lanes": (i32, [p, p, p, u32, p, p, u32]), "sftg_launch_total": (u64, [p]),
-        "sft_model_get_blas": (p, [p, p, p]), "sftg_last_blas_build": (i32, [p, p, p, p, p]),
+        "sft_model_get_blas": (p, [p, p, p]), "sftg_pose_eval_device": (i32, [p, p, p, u32, p, p]), "sftg_last_blas_build": (i32, [p, p, p, p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -93,6 +93,9 @@ class SftgAnimationDesc(C.Structure):
 
 class SftgPoseRequest(C.Structure):
     _fields_ = [("skeleton", C.c_int32), ("animation", C.c_int32), ("time", C.c_float)]
+
+
+POSE_REQUEST_DTYPE = np.dtype([("skeleton", "<i4"), ("animation", "<i4"), ("time", "<f4")])
 
 
 # sftg_ray / sftg_ray_hit records (include/sftg.h)
@@ -341,6 +344,25 @@ class Renderer:
         if rc != 0:
             raise RuntimeError("pose evaluation failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
         return posed, glob
+
+    def pose_eval_host(self, requests: np.ndarray, posed: np.ndarray, glob: np.ndarray | None = None) -> None:
+        """sftg_pose_eval on host arrays: POSE_REQUEST_DTYPE records in, float32 matrices out
+        (request k at 16 * the bone counts before it)."""
+        ctx = self.lib.sft_get_gpu_context()
+        r = np.ascontiguousarray(requests, POSE_REQUEST_DTYPE)
+        rc = self.lib.sftg_pose_eval(ctx, r.ctypes.data_as(C.c_void_p), len(r), posed.ctypes.data_as(C.c_void_p),
+                                     glob.ctypes.data_as(C.c_void_p) if glob is not None else None)
+        if rc != 0:
+            raise RuntimeError("pose evaluation failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
+
+    def pose_eval_device(self, d_requests: int, d_off: int, n: int, d_posed: int, d_global: int = 0) -> None:
+        """sftg_pose_eval_device on device pointers (SftgPoseRequest records, u32 offsets in
+        matrices, float outputs); asynchronous on the renderer's stream."""
+        ctx = self.lib.sft_get_gpu_context()
+        rc = self.lib.sftg_pose_eval_device(ctx, C.c_void_p(d_requests), C.c_void_p(d_off), n, C.c_void_p(d_posed),
+                                            C.c_void_p(d_global) if d_global else None)
+        if rc != 0:
+            raise RuntimeError("pose evaluation failed: " + (self.lib.sftg_last_error(ctx) or b"").decode())
 
     def raycast(self, h, rays: np.ndarray) -> np.ndarray:
         """sft_raycast_batch over RAY_DTYPE records whose `model` indexes the models of scene h
