@@ -7,7 +7,7 @@
  *              box and centroid (3526-3617); one warp per meshlet, a ballot keeps the order
  *   shape      a node of more than 8 items splits its range by count (halves, quarters, eighths),
  *              so node numbering, ranges and the list of sorted ranges depend on the item count
- *              only; the host lays them out (plan_node) and the device does every data-dependent
+ *              only; the host lays them out (sftg_blas_plan.h) and the device does every data-dependent
  *              step
  *   sorts      a sorted range at split depth d of a node at depth t sorts at level 3t + d; the
  *              ranges of one level are disjoint and read the order the previous level left.
@@ -31,6 +31,7 @@
  */
 #include "sftg_types.h"
 #include "sftg_kernels.h"
+#include "sftg_blas_plan.h"
 #include <vector>
 #include <cstring>
 #include <algorithm>
@@ -43,12 +44,6 @@
 #define BLAS_BIGQ 8              /* pending such pieces (disjoint, so at most 3 within BLAS_CAP) */
 #define BLAS_SEQ_STACK 16        /* pending disjoint pieces of >= 2 positions within BLAS_SEQ */
 #define BLAS_SMALL_SMEM (BLAS_CAP * 4 * 2 + BLAS_CAP * 2 * 2 + (BLAS_CAP / 2) * 4 * 3)
-
-struct blas_pnode {              /* a node of the plan */
-    uint32_t start, count;       /* item range; a leaf when count <= 8 */
-    uint32_t nchild;
-    uint32_t child[8];
-};
 
 /* ------------------------------------------------------------------------------ items */
 __device__ __forceinline__ bool tri_live(const uint8_t* in, uint32_t t) {
@@ -696,41 +691,8 @@ struct sftg_blas_job {
     const uint8_t* inds = nullptr;
     uint32_t* d_cnt = nullptr;      /* [nm] counts, then [nm] offsets, then total */
     uint32_t launches = 0;          /* kernels launched by begin and finish */
-    /* plan */
-    std::vector<blas_pnode> nodes;
-    std::vector<std::vector<uint32_t>> by_depth;
-    std::vector<std::vector<uint2>> by_level;
+    blas_plan plan;                 /* the tree's shape for n items */
 };
-
-static void plan_split(sftg_blas_job& J, uint32_t start, uint32_t count, uint32_t d, uint32_t level, uint32_t* st, uint32_t* cn, uint32_t& ng) {
-    if (!count) return;
-    if (d == 3 || count == 1) { st[ng] = start; cn[ng] = count; ng++; return; }
-    if (J.by_level.size() <= level + d) J.by_level.resize(level + d + 1);
-    J.by_level[level + d].push_back(make_uint2(start, count));
-    const uint32_t mid = count / 2;
-    plan_split(J, start, mid, d + 1, level, st, cn, ng);
-    plan_split(J, start + mid, count - mid, d + 1, level, st, cn, ng);
-}
-
-static uint32_t plan_node(sftg_blas_job& J, uint32_t start, uint32_t count, uint32_t depth) {
-    const uint32_t ni = (uint32_t)J.nodes.size();
-    blas_pnode p;
-    memset(&p, 0, sizeof(p));
-    p.start = start; p.count = count;
-    for (int i = 0; i < 8; i++) p.child[i] = 0xFFFFFFFFu;
-    J.nodes.push_back(p);
-    if (J.by_depth.size() <= depth) J.by_depth.resize(depth + 1);
-    J.by_depth[depth].push_back(ni);
-    if (count <= 8) return ni;
-    uint32_t st[8] = { 0 }, cn[8] = { 0 }, ng = 0;
-    plan_split(J, start, count, 0, 3 * depth, st, cn, ng);
-    for (uint32_t c = 0; c < ng; c++) {
-        const uint32_t ci = plan_node(J, st[c], cn[c], depth + 1);
-        J.nodes[ni].child[c] = ci;
-    }
-    J.nodes[ni].nchild = ng;
-    return ni;
-}
 
 #define BK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return e_; } while (0)
 
@@ -750,22 +712,20 @@ cudaError_t sftg_blas_begin(sftg_blas_job** out, const float* attr, const uint8_
     BK(cudaMemcpyAsync(&total, J->d_cnt + 2 * (size_t)nm, 4, cudaMemcpyDeviceToHost, st));
     BK(cudaStreamSynchronize(st));
     J->n = total;
-    if (total) {
-        J->nodes.reserve(total / 3 + 16);
-        plan_node(*J, 0, total, 0);
-    }
+    blas_plan_build(J->plan, total);
     *n_items = total;
-    *n_nodes = (uint32_t)J->nodes.size();
+    *n_nodes = (uint32_t)J->plan.nodes.size();
     return cudaSuccess;
 }
 
 cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* status) {
     *status = 0;
-    const uint32_t n = J->n, nn = (uint32_t)J->nodes.size();
+    const uint32_t n = J->n, nn = (uint32_t)J->plan.nodes.size();
     if (!n) return cudaSuccess;
     cudaStream_t st = J->st;
     /* tasks of every level, spans of the short ones, and the node plan, in one upload */
-    std::vector<uint2> tasks, big, big_pchunk;
+    std::vector<blas_range> tasks, big;
+    std::vector<uint2> big_pchunk;
     std::vector<uint4> spans, big_chunks;
     std::vector<uint32_t> lv_task_off, lv_span_off, lv_span_cnt, lv_big_off, lv_big_cnt, lv_chunk_off, lv_chunk_cnt, lv_rounds;
     std::vector<uint32_t> lv_rs;   /* per level: the first round's piece and chunk counts */
@@ -774,8 +734,8 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t span_target = std::min<uint32_t>(BLAS_CAP, std::max<uint32_t>(256, n / (3u * (uint32_t)std::max(sms, 1))));
-    for (size_t L = 0; L < J->by_level.size(); L++) {
-        const std::vector<uint2>& T = J->by_level[L];
+    for (size_t L = 0; L < J->plan.by_level.size(); L++) {
+        const std::vector<blas_range>& T = J->plan.by_level[L];
         lv_task_off.push_back((uint32_t)tasks.size());
         lv_span_off.push_back((uint32_t)spans.size());
         lv_big_off.push_back((uint32_t)big.size());
@@ -803,14 +763,14 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         lv_rs.push_back(lv_big_cnt.back()); lv_rs.push_back(lv_chunk_cnt.back());
         /* rounds until the longest range's parts fit if its pivots split evenly, and one more */
         uint32_t longest = 0, r = 1;
-        for (const uint2& t : T) longest = std::max(longest, t.y);
+        for (const blas_range& t : T) longest = std::max(longest, t.y);
         while (longest > BLAS_CAP) { longest = (longest + 1) / 2; r++; }
         lv_rounds.push_back(r);
     }
     std::vector<uint32_t> depth_idx, depth_off;
-    for (size_t d = 0; d < J->by_depth.size(); d++) {
+    for (size_t d = 0; d < J->plan.by_depth.size(); d++) {
         depth_off.push_back((uint32_t)depth_idx.size());
-        depth_idx.insert(depth_idx.end(), J->by_depth[d].begin(), J->by_depth[d].end());
+        depth_idx.insert(depth_idx.end(), J->plan.by_depth[d].begin(), J->plan.by_depth[d].end());
     }
     const uint32_t list_cap = n / BLAS_CAP + 4, small_cap = n / 2 + 4, chunk_cap = n / BLAS_CHUNK + list_cap + 4;
     /* device scratch: items, ids, perm, key, Lp, Rp, bounds, lists, counters, plan */
@@ -848,7 +808,7 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     memcpy(h + (o_bpc - o_plan), big_pchunk.data(), big_pchunk.size() * 8);
     memcpy(h + (o_bch - o_plan), big_chunks.data(), big_chunks.size() * 16);
     memcpy(h + (o_lvrs - o_plan), lv_rs.data(), lv_rs.size() * 4);
-    memcpy(h + (o_pn - o_plan), J->nodes.data(), (size_t)nn * sizeof(blas_pnode));
+    memcpy(h + (o_pn - o_plan), J->plan.nodes.data(), (size_t)nn * sizeof(blas_pnode));
     memcpy(h + (o_didx - o_plan), depth_idx.data(), depth_idx.size() * 4);
     cudaError_t err = cudaMemcpyAsync(d + o_plan, h, plan_bytes, cudaMemcpyHostToDevice, st);
     float* it = (float*)(d + o_it);
@@ -889,7 +849,7 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
     }
     static thread_local uint32_t* h_ctr = nullptr;   /* pinned read-back of the round state */
     if (err == cudaSuccess && !h_ctr) err = cudaMallocHost((void**)&h_ctr, 32);
-    for (size_t L = 0; err == cudaSuccess && L < J->by_level.size(); L++) {
+    for (size_t L = 0; err == cudaSuccess && L < J->plan.by_level.size(); L++) {
         if (lv_span_cnt[L]) {
             k_blas_sort_small<true><<<lv_span_cnt[L], BLAS_SMALL_THREADS, BLAS_SMALL_SMEM, st>>>(d_spans + lv_span_off[L], nullptr, lv_span_cnt[L],
                                                                                                  d_tasks, it, n, key, perm);
@@ -940,8 +900,8 @@ cudaError_t sftg_blas_finish(sftg_blas_job* J, sftg_bvh_node* dst, uint32_t* sta
         }
         if (err == cudaSuccess) err = cudaGetLastError();
     }
-    for (size_t dd = J->by_depth.size(); err == cudaSuccess && !*status && dd-- > 0;) {
-        const uint32_t cnt = (uint32_t)J->by_depth[dd].size();
+    for (size_t dd = J->plan.by_depth.size(); err == cudaSuccess && !*status && dd-- > 0;) {
+        const uint32_t cnt = (uint32_t)J->plan.by_depth[dd].size();
         k_blas_nodes<<<(cnt + 127) / 128, 128, 0, st>>>(d_pn, d_didx + depth_off[dd], cnt, it, ids, perm, n, bnd, dst);
         err = cudaGetLastError();
         J->launches++;
