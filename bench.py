@@ -9,7 +9,8 @@ tile raster and resolve on the GPU.  The default workload is the skinned-charact
 lights, 512x512 textures) at 1920x1080 with 2x MSAA; `--config 1|3` selects the static
 640x360 scene or the 262k-triangle lightmapped atrium at 1920x1080 with 4x MSAA; `--config 4|5`
 the batched multi-view and served workloads; `--config 6` ray queries (2^20 rays against the
-atrium scene, rays/s).
+atrium scene, rays/s); `--config 7` the BLAS build of the 249k-triangle atrium model at model
+creation (triangles/s); `--config 8` skeletal poses (2^16 requests on a 22-bone rig, poses/s).
 
   value   frames/s with the scene resident in device memory and the colour left there
   e2e     frames/s through the public API into a host colour buffer (pinned staging of the
