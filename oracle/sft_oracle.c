@@ -404,6 +404,9 @@ typedef struct {
     mat4* inst_T; const mat4** inst_bones;
     int debug_mode;              /* enum sft_debug_mode (sofren2.c:59-67) */
     otex checker;                /* the base material's 256x256 checkerboard (sofren2.c:8062-8080) */
+    int fp64;                    /* sfto_shadow_fp64: evaluate the capsule shadows in double too */
+    double fp64_max, fp64_sum;   /* largest and summed |FP32 - FP64| shadow intensity */
+    u64 fp64_n, fp64_big;        /* pixel x light evaluations, and those differing by more than 1e-5 */
 } octx;
 
 static void list_push(olist* l, u64 v) {
@@ -1085,7 +1088,7 @@ static void rast_payload(const octx* c, u64 payload, f32* depth, u32* vidb, i32 
     }
 }
 
-typedef struct { vec3 pa, pb, ab, W; f32 abdab, wdw, rb2, pr, pr2, vis_mult; } opc;   /* sft_light_proxy_cache 991-998 */
+typedef struct { vec3 pa, pb, ab, W; f32 abdab, wdw, rb2, pr, pr2, vis_mult; u32 vis; } opc;   /* sft_light_proxy_cache 991-998 (+ the visibility count) */
 
 static const otex* tex_of(const octx* c, u32 tex_index_plus1) { return tex_index_plus1 ? &c->tex[tex_index_plus1 - 1] : NULL; }
 
@@ -1126,6 +1129,67 @@ static void debug_overlay(octx* c, i32 tmx, i32 tmy, i32 lim_x, i32 lim_y, f32 z
 }
 
 /* sft__resolve_tile (5809-6753) */
+/* FP64 evaluation of the capsule shadow expression (sofren2.c:6522-6571) for one 4x2 block and
+ * one light, beside the FP32 one: the same proxies, lane gates, block-level skip and smooth
+ * maximum, with every quantity recomputed in double from the pixel positions, the light position
+ * and the proxies' endpoints, radii and visibility counts (where the FP32 path uses the table
+ * reciprocal, the fast normalisation and 0.3333333f).  Accumulates |FP32 - FP64| of the shadow
+ * intensity over the block's pixels. */
+static void shadow_check_fp64(octx* c, const vec3* P, vec3 lpos, const opc* pc, u32 npc, u32 gate, u32 lanes, const f32* ms32) {
+    double Lr[8][3], d2[8], lrl[8], Ln[8][3], ms[8];
+    for (int l = 0; l < 8; l++) {
+        Lr[l][0] = (double)lpos.x - P[l].x; Lr[l][1] = (double)lpos.y - P[l].y; Lr[l][2] = (double)lpos.z - P[l].z;
+        d2[l] = Lr[l][0] * Lr[l][0] + Lr[l][1] * Lr[l][1] + Lr[l][2] * Lr[l][2];
+        lrl[l] = sqrt(d2[l]);
+        for (int a = 0; a < 3; a++) Ln[l][a] = lrl[l] > 0.0 ? Lr[l][a] / lrl[l] : 0.0;
+        ms[l] = 0.0;
+    }
+    for (u32 p = 0; p < npc; p++) {
+        const opc* q = &pc[p];
+        const double pa[3] = { q->pa.x, q->pa.y, q->pa.z }, pb[3] = { q->pb.x, q->pb.y, q->pb.z };
+        double ab[3], W[3], abdab = 0.0, wdw = 0.0;
+        for (int a = 0; a < 3; a++) { ab[a] = pb[a] - pa[a]; abdab += ab[a] * ab[a]; }
+        const double lp[3] = { lpos.x, lpos.y, lpos.z };
+        for (int a = 0; a < 3; a++) { W[a] = (pa[a] + pb[a]) * 0.5 - lp[a]; wdw += W[a] * W[a]; }
+        const double br = (double)q->pr + sqrt(abdab) * 0.5, rb2 = br * br, pr2 = (double)q->pr * q->pr, vis = q->vis / 3.0;
+        u32 ray = 0;
+        for (int l = 0; l < 8; l++) {
+            const double wdv = -(W[0] * Lr[l][0] + W[1] * Lr[l][1] + W[2] * Lr[l][2]);
+            const double cd2 = wdw - wdv * (wdv / d2[l]);
+            if (wdv > 0.0 && wdv < d2[l] && cd2 < rb2 && (gate >> l & 1)) ray |= 1u << l;
+        }
+        if (!ray) continue;
+        for (int l = 0; l < 8; l++) {
+            double ao[3], abl = 0.0, abao = 0.0, lao = 0.0;
+            for (int a = 0; a < 3; a++) { ao[a] = (double)(a == 0 ? P[l].x : a == 1 ? P[l].y : P[l].z) - pa[a]; }
+            for (int a = 0; a < 3; a++) { abl += ab[a] * Ln[l][a]; abao += ab[a] * ao[a]; lao += Ln[l][a] * ao[a]; }
+            const double den = abdab - abl * abl, sden = den > 1e-6 ? den : 1e-6;
+            double t2 = (abao - abl * lao) / sden;
+            t2 = t2 < 0.0 ? 0.0 : (t2 > 1.0 ? 1.0 : t2);
+            const double t1 = t2 * abl - lao;
+            double dist2 = 0.0;
+            for (int a = 0; a < 3; a++) {
+                const double pr = (double)(a == 0 ? P[l].x : a == 1 ? P[l].y : P[l].z) + Ln[l][a] * t1, pcap = pa[a] + ab[a] * t2;
+                dist2 += (pr - pcap) * (pr - pcap);
+            }
+            double sv = 1.0 - dist2 / pr2;
+            if (sv < 0.0 || !(ray >> l & 1) || !(t1 > 1e-6 && t1 < lrl[l])) sv = 0.0;
+            sv *= vis;
+            const double h = 0.2 - fabs(ms[l] - sv), hp = h > 0.0 ? h : 0.0;
+            ms[l] = (ms[l] > sv ? ms[l] : sv) + hp * hp * (0.25 / 0.2);
+        }
+    }
+    for (int l = 0; l < 8; l++) {
+        if (!(lanes >> l & 1)) continue;
+        const f32 si32 = vmax(0.f, 1.f - ms32[l]);
+        const double si64 = 1.0 - ms[l] > 0.0 ? 1.0 - ms[l] : 0.0;
+        const double e = fabs((double)si32 - si64);
+        if (e > c->fp64_max) c->fp64_max = e;
+        c->fp64_sum += e; c->fp64_n++;
+        if (e > 1e-5) c->fp64_big++;
+    }
+}
+
 static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f32* shadow_out) {
     const sfts_frame* f = c->f;
     const i32 tmx = (tile % c->cols) * TILE, tmy = (tile / c->cols) * TILE;
@@ -1191,7 +1255,7 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
                     opc* q = &pcache[i][pcn];
                     q->pa = px->posa; q->pb = px->posb; q->ab = ab; q->W = Wv;
                     q->abdab = sdot(ab, ab); q->wdw = d2; q->rb2 = br * br; q->pr = px->radius; q->pr2 = px->radius * px->radius;
-                    q->vis_mult = (f32)vs * 0.3333333f;
+                    q->vis_mult = (f32)vs * 0.3333333f; q->vis = vs;
                     pcn++;
                 }
             }
@@ -1425,6 +1489,7 @@ static void resolve_tile(octx* c, i32 tile, const f32* depth, const u32* vidb, f
                                 }
                             }
                         }
+                        if (c->fp64) shadow_check_fp64(c, P, lpos, pcache[i], npc[i], lm ? tri_mask : lit, tri_lanes, ms_);
                         for (int l = 0; l < 8; l++) {
                             const f32 si = vmax(0.f, 1.f - ms_[l]);
                             if (shadow_out && (tri_lanes >> l & 1) && i < 16) {
@@ -1986,6 +2051,20 @@ int sfto_blas_rebuild(void* hp, uint32_t mi, uint32_t reps) {
         blas_build(m);
     }
     return (int)m->blas_count;
+}
+
+/* The capsule shadows of `frame` at `samples` evaluated in double beside the FP32 restatement
+ * (one thread): out[0] the largest |FP32 - FP64| shadow intensity, out[1] the mean, out[2] the
+ * number of pixel x light evaluations, out[3] how many differ by more than 1e-5. */
+int sfto_shadow_fp64(void* hp, uint32_t frame, int samples, double* out) {
+    oracle_handle* h = (oracle_handle*)hp;
+    if (!h || !out || frame >= h->sc.n_frames || !(samples == 1 || samples == 2 || samples == 4)) return -1;
+    h->c.fp64 = 1; h->c.fp64_max = 0.0; h->c.fp64_sum = 0.0; h->c.fp64_n = 0; h->c.fp64_big = 0;
+    const int rc = render_frame(&h->c, frame, samples, 1, NULL, NULL, NULL);
+    h->c.fp64 = 0;
+    out[0] = h->c.fp64_max; out[1] = h->c.fp64_n ? h->c.fp64_sum / (double)h->c.fp64_n : 0.0;
+    out[2] = (double)h->c.fp64_n; out[3] = (double)h->c.fp64_big;
+    return rc;
 }
 
 /* enum sft_debug_mode for the following renders (0 = none) */

@@ -60,6 +60,18 @@ class Oracle:
         L.sfto_model_blas(self.h, mi, buf.ctypes.data_as(C.c_void_p), n, C.byref(root))
         return buf[: n * 256].tobytes(), int(root.value)
 
+    def shadow_fp64(self, frame: int, samples: int) -> dict:
+        """The frame's capsule shadows evaluated in double beside the FP32 restatement (which is
+        the reference's arithmetic): largest and mean |FP32 - FP64| shadow intensity, the number
+        of pixel x light evaluations and how many differ by more than 1e-5."""
+        L = lib()
+        L.sfto_shadow_fp64.restype = C.c_int
+        L.sfto_shadow_fp64.argtypes = [C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]
+        out = np.zeros(4, np.float64)
+        if L.sfto_shadow_fp64(self.h, frame, samples, out.ctypes.data_as(C.c_void_p)) != 0:
+            raise RuntimeError("oracle FP64 shadow evaluation failed")
+        return {"max": float(out[0]), "mean": float(out[1]), "n": int(out[2]), "over_1e-5": int(out[3])}
+
     def blas_rebuild(self, mi: int, reps: int = 1) -> int:
         """Builds model mi's BLAS again `reps` times with the oracle's restated builder (timing)."""
         L = lib()
