@@ -65,9 +65,10 @@ def test_gpu_equals_oracle_random(renderer, seed, samples):
     assert not bad, (res, first_vid_mismatch(ref, out, cols, samples))
 
 
-def test_gpu_shadow_factors_vs_oracle_and_fp64(renderer):
+def test_gpu_shadow_factors_equal_oracle(renderer):
     """Per-pixel shadow intensity of every tile light (1x) is identical to the FP32 oracle
-    (the tolerance stated for shadow factors is 1e-5 absolute)."""
+    (the tolerance stated for shadow factors is 1e-5 absolute).  The FP32 values against an FP64
+    evaluation of the same expression are measured on the CPU in test_shadow_fp64.py."""
     sc = gc.scene("skinned_small")
     blob = gc.blob("skinned_small")
     w, h_ = sc.frames[0].width, sc.frames[0].height
