@@ -20,11 +20,12 @@ CASES = {
     "variety_noclear": ("variety_scene", dict(seed=4002, clear=0)),
     "config2": ("config2", dict()),
     "config3": ("config3", dict()),
+    "hand": ("hand_scene", dict()),
 }
 
 # cases the CPU oracle re-checks in the default (not-gpu) test run; the big configurations are
 # checked on the GPU against their digests, and against the oracle in the slow tier
-FAST = ["small", "config1", "skinned_small", "atrium_small", "variety", "variety_noclear"]
+FAST = ["small", "config1", "skinned_small", "atrium_small", "variety", "variety_noclear", "hand"]
 # debug views (enum sft_debug_mode 1..5) over a few cases: (case, mode, samples)
 DEBUG_CASES = [(n, m, S) for n in ("small", "variety", "atrium_small") for m in (1, 2, 3, 4, 5) for S in (1, 4)]
 SAMPLES = {name: (1, 2, 4) for name in CASES}
@@ -34,10 +35,57 @@ SAMPLES["config3"] = (4,)
 _cache: dict = {}
 
 
+def hand_scene(width: int = 200, height: int = 136):
+    """Hand-made edge cases in one view: a single triangle with a 1x1 texture, a triangle seen
+    edge-on (its plane holds the camera), two coplanar triangles sharing an edge with different
+    textures (the tie order on the shared edge), two floor triangles crossing the near plane
+    with one and with two vertices in front, and 17 point lights clustered so that some tiles
+    hold more than the 16-light cap, some one light and some none; a capsule proxy over the
+    single triangle casts shadows from the cluster."""
+    sc = scenes.Scene()
+    one = sc.add_material(sc.add_texture(np.array([[0xFF3080C0]], np.uint32)), 0xFFFFFFFF, 16.0)
+    ta = sc.add_material(sc.add_texture(scenes.value_noise_texture(8, 8, 91)), 0xFFFFFFFF, 8.0)
+    tb = sc.add_material(sc.add_texture(scenes.value_noise_texture(16, 8, 92, lattice=4)), 0xFFC0A080, 32.0)
+
+    def mesh(pos, nrm, tris):
+        pos = np.asarray(pos, np.float32)
+        nrm = np.tile(np.asarray(nrm, np.float32), (len(pos), 1))
+        uv = np.asarray([[0.1 + 0.8 * (k % 2), 0.1 + 0.4 * (k % 3)] for k in range(len(pos))], np.float32)
+        return scenes.build_meshlets(scenes.RawMesh(pos, nrm, uv, scenes._orient(pos, nrm, np.asarray(tris))))
+
+    towards = (0.0, 0.0, -1.0)
+    tri = mesh([(-1.2, 0.2, 3.0), (-0.6, 0.2, 3.0), (-0.9, 0.7, 3.0)], towards, [[0, 1, 2]])
+    edge = mesh([(0.2, 0.5, 2.0), (0.6, 0.75, 3.0), (0.4, 1.0, 4.0)], (1.0, 0.0, 0.0), [[0, 1, 2]])
+    q = [(0.6, -0.8, 2.5), (1.4, -0.8, 2.5), (1.4, -0.1, 2.5), (0.6, -0.1, 2.5)]
+    quad_a = mesh([q[0], q[1], q[2]], towards, [[0, 1, 2]])
+    quad_b = mesh([q[0], q[2], q[3]], towards, [[0, 1, 2]])
+    up = (0.0, 1.0, 0.0)
+    near1 = mesh([(-0.5, -0.25, -0.5), (0.5, -0.25, -0.5), (0.0, -0.25, 1.5)], up, [[0, 1, 2]])
+    near2 = mesh([(-0.9, -0.35, 1.2), (-0.3, -0.35, 1.2), (-0.6, -0.35, -0.4)], up, [[0, 1, 2]])
+    models = [
+        sc.add_model(scenes.Model([tri], [one], proxies=[((-1.0, 0.3, 2.7), (-0.8, 0.5, 2.7), 0.08, 0xFFFFFFFF)])),
+        sc.add_model(scenes.Model([edge], [ta])),
+        sc.add_model(scenes.Model([quad_a, quad_b], [ta, tb])),
+        sc.add_model(scenes.Model([near1, near2], [tb, ta])),
+    ]
+    fr = scenes._camera_frame(width, height)
+    for k in range(17):
+        a = 2.0 * np.pi * k / 17.0
+        fr.point_lights.append(((-0.9 + 0.25 * np.cos(a), 0.45 + 0.25 * np.sin(a), 2.4), 1.0, 0.9, 0.8, 0.1, 0.7))
+    fr.point_lights.append(((1.0, -0.45, 2.0), 0.7, 0.8, 1.0, 1.5, 1.0))
+    for mi in models:
+        fr.instances.append((mi, scenes.mat_identity(), None))
+    sc.frames.append(fr)
+    return sc
+
+
+_LOCAL = {"hand_scene": hand_scene}
+
+
 def scene(name: str):
     if name not in _cache:
         fn, kw = CASES[name]
-        _cache[name] = getattr(scenes, fn)(**kw)
+        _cache[name] = (_LOCAL.get(fn) or getattr(scenes, fn))(**kw)
     return _cache[name]
 
 
