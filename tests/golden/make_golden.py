@@ -59,6 +59,17 @@ def main(names: list[str]) -> None:
             bl[name] = {"nodes": [len(b) // 256 for b in frame["blas"]], "sha256": [gc.sha(b) for b in frame["blas"]]}
             print("blas", name, bl[name]["nodes"], flush=True)
         golden["blas"] = bl
+    if not names or "tlas" in names:
+        # frame 0's TLAS as the reference's host code builds it (padding bytes left out, as the
+        # reference leaves them unset)
+        from compare import _nodes_meaningful
+        tl = {}
+        for name in gc.CASES:
+            raw = reference_dump(gc.blob(name), 1, frame=0)[0].get("tlas")
+            nodes = _nodes_meaningful(raw) if raw is not None else None
+            tl[name] = {"nodes": 0 if nodes is None else int(nodes.shape[0]), "sha256": gc.sha(nodes if nodes is not None else b"")}
+            print("tlas", name, tl[name]["nodes"], flush=True)
+        golden["tlas"] = tl
     if not names or "pose" in names:
         # sft_pose_update of the reference on a seeded rig (oracle/pose_harness.c)
         from oracle_lib import pose_blob, reference_pose
