@@ -159,8 +159,9 @@ int sftg_frames_render(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_
  * rejected with SFTG_E_LIMIT before any device work.  light_vis (host, n_proxies * 64 bytes)
  * receives 3 - rays blocked per (proxy, light), 0 in columns past the light count: the rows
  * sftg_frame_render computes for the same frame.  The models must be on the device already
- * (a render since the last model upload).  The first call per device looks up the scratch
- * address: make it outside any stream capture.  The scratch is shared by all contexts on a
+ * (a render since the last model upload).  sftg_create looks up the scratch's device address
+ * once per device, so the 4 MiB are committed on the device when its first context is created,
+ * not during a call.  The scratch is shared by all contexts on a
  * device, so overlapping calls race: serialise them.  No counterpart in the reference, whose
  * CPU frame always has its arenas. */
 #define SFTG_NOALLOC_SCRATCH_BYTES (4u << 20)

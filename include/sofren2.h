@@ -21,6 +21,7 @@
 #include <string.h>
 #include <math.h>
 #include "sftg.h"
+#include "x86_approx_tables.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -154,6 +155,124 @@ SFT_FUNC sftmat sft_m_from_quat(sftquat q);
 SFT_FUNC sftquat sft_q_mul(sftquat a, sftquat b);
 SFT_FUNC sftquat sft_q_slerp(sftquat a, sftquat b, f32 t);
 SFT_FUNC sftquat sft_q_norm(sftquat q);
+
+/* SoA math (sofren2.c:780-792, 1921-2060): eight lanes, the width of the reference's AVX2 build,
+ * whose results these reproduce bit for bit on any host (x86-64 or aarch64): IEEE add, sub, mul,
+ * div and sqrt per lane, a fused multiply-add exactly where the reference calls fmadd / fnmadd,
+ * _mm256_max_ps's operand order, and RSQRTPS through the instruction's measured table
+ * (x86_approx_tables.h).  Compile the calling TU with -ffp-contract=off, as the reference must be.
+ * vf32 is a GCC/Clang vector of 8 floats (the same vector shape as __m256), so lanes can be
+ * read and written as v[i] or with ordinary operators.  Like the reference's SFT_INLINE helpers,
+ * these are static inline in every TU that includes this header, not library exports. */
+#ifndef SFT_INLINE
+    #define SFT_INLINE static inline
+#endif
+/* the helpers are static inline, so the calling convention of 32-byte vectors never crosses a TU */
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Wpsabi"
+typedef float vf32 __attribute__((vector_size(32)));
+typedef struct sftvvec { vf32 x, y, z; } sftvvec;
+typedef struct sftvquat { vf32 x, y, z, w; } sftvquat;
+typedef union sftvmat { sftvquat rows[4]; vf32 m[4][4]; } sftvmat;
+
+SFT_INLINE sftvvec sft_vv_add(sftvvec a, sftvvec b);
+SFT_INLINE sftvvec sft_vv_sub(sftvvec a, sftvvec b);
+SFT_INLINE sftvvec sft_vv_scale(sftvvec a, vf32 b);
+SFT_INLINE vf32 sft_vv_dot(sftvvec a, sftvvec b);
+SFT_INLINE sftvvec sft_vv_cross(sftvvec a, sftvvec b);
+SFT_INLINE vf32 sft_vv_length2(sftvvec v);
+SFT_INLINE vf32 sft_vv_length(sftvvec v);
+SFT_INLINE sftvvec sft_vv_norm(sftvvec v);
+SFT_INLINE sftvvec sft_vv_norm_fast(sftvvec v);
+SFT_INLINE sftvvec sft_vv_transform(sftvvec v, sftvmat vm);
+SFT_INLINE sftvvec sft_vv_transform_dir(sftvvec v, sftvmat vm);
+SFT_INLINE sftvmat sft_vm_broadcast(sftmat m);
+
+/* lane-wise fused multiply-add (_mm256_fmadd_ps) and -(a*b)+c (_mm256_fnmadd_ps) */
+SFT_INLINE vf32 sft__vfma(vf32 a, vf32 b, vf32 c) { vf32 r; for (int i = 0; i < 8; i++) r[i] = fmaf(a[i], b[i], c[i]); return r; }
+SFT_INLINE vf32 sft__vfnma(vf32 a, vf32 b, vf32 c) { vf32 r; for (int i = 0; i < 8; i++) r[i] = fmaf(-a[i], b[i], c[i]); return r; }
+SFT_INLINE vf32 sft__vset1(f32 s) { vf32 r = { s, s, s, s, s, s, s, s }; return r; }
+/* NaN lanes as x86 leaves them: from NaN-free inputs every NaN is born of an invalid operation
+ * (0 * inf, inf - inf, inf / inf), whose SSE/AVX result is the default NaN 0xFFC00000, and later
+ * arithmetic passes it on unchanged; aarch64 would give 0x7FC00000.  (NaN inputs also come out as
+ * 0xFFC00000, where x86 would keep their payload.) */
+SFT_INLINE vf32 sft__xnan(vf32 v) {
+    const u32 dnan = 0xFFC00000u;
+    for (int i = 0; i < 8; i++) if (v[i] != v[i]) memcpy((char*)&v + 4 * i, &dnan, 4);
+    return v;
+}
+SFT_INLINE sftvvec sft__xnan3(sftvvec v) { v.x = sft__xnan(v.x); v.y = sft__xnan(v.y); v.z = sft__xnan(v.z); return v; }
+
+SFT_INLINE sftvvec sft_vv_add(sftvvec a, sftvvec b) { sftvvec r = { a.x + b.x, a.y + b.y, a.z + b.z }; return sft__xnan3(r); }
+SFT_INLINE sftvvec sft_vv_sub(sftvvec a, sftvvec b) { sftvvec r = { a.x - b.x, a.y - b.y, a.z - b.z }; return sft__xnan3(r); }
+SFT_INLINE sftvvec sft_vv_scale(sftvvec a, vf32 b) { sftvvec r = { a.x * b, a.y * b, a.z * b }; return sft__xnan3(r); }
+/* x*x' + (y*y' + z*z'), three products rounded separately */
+SFT_INLINE vf32 sft_vv_dot(sftvvec a, sftvvec b) { const vf32 x = a.x * b.x, y = a.y * b.y, z = a.z * b.z; return sft__xnan(x + (y + z)); }
+SFT_INLINE sftvvec sft_vv_cross(sftvvec a, sftvvec b) {
+    sftvvec r = { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x };
+    return sft__xnan3(r);
+}
+SFT_INLINE vf32 sft_vv_length2(sftvvec v) { return sft_vv_dot(v, v); }
+SFT_INLINE vf32 sft_vv_length(sftvvec v) {
+    const vf32 d = sft_vv_dot(v, v);
+    vf32 r; for (int i = 0; i < 8; i++) r[i] = sqrtf(d[i]);
+    return sft__xnan(r);
+}
+/* v / max(|v|, SFT_EPSILON); max keeps _mm256_max_ps's rule (the second operand unless a > b) */
+SFT_INLINE sftvvec sft_vv_norm(sftvvec v) {
+    vf32 len = sft_vv_length(v);
+    for (int i = 0; i < 8; i++) len[i] = len[i] > SFT_EPSILON ? len[i] : SFT_EPSILON;
+    sftvvec r = { v.x / len, v.y / len, v.z / len };
+    return sft__xnan3(r);
+}
+/* RSQRTPS of one lane: the measured 11-bit estimate of x86 (zero and denormals give +-inf,
+ * negatives the default NaN, +inf gives 0, NaN stays NaN, quieted) */
+SFT_INLINE f32 sft__x86_rsqrt(f32 xf) {
+    static const u32 tab[2048] = SFT_X86_RSQRT_TABLE_INIT;
+    u32 x, s, e, m, out;
+    memcpy(&x, &xf, 4);
+    s = x & 0x80000000u; e = (x >> 23) & 0xFF; m = x & 0x7FFFFF;
+    if (e == 0xFF) out = m ? (x | 0x00400000u) : (s ? 0xFFC00000u : 0u);
+    else if (e == 0) out = s | 0x7F800000u;
+    else if (s) out = 0xFFC00000u;
+    else {
+        const u32 t = tab[(e & 1) * 1024 + (m >> 13)];
+        out = ((u32)(((380 - (i32)e) >> 1) + (i32)(t >> 23) - 1) << 23) | (t & 0x7FFFFF);
+    }
+    memcpy(&xf, &out, 4);
+    return xf;
+}
+/* one Newton step on the estimate: (0.5 * a) * fnmadd(|v|^2, a*a, 3); a zero vector gives
+ * 0 * inf there, so NaN lanes */
+SFT_INLINE sftvvec sft_vv_norm_fast(sftvvec v) {
+    const vf32 sq = sft_vv_dot(v, v);
+    vf32 a; for (int i = 0; i < 8; i++) a[i] = sft__x86_rsqrt(sq[i]);
+    const vf32 refined = (sft__vset1(0.5f) * a) * sft__vfnma(sq, a * a, sft__vset1(3.f));
+    sftvvec r = { v.x * refined, v.y * refined, v.z * refined };
+    return sft__xnan3(r);
+}
+/* row-vector transform, each component accumulated z, then y, then x, fused */
+SFT_INLINE sftvvec sft_vv_transform(sftvvec v, sftvmat vm) {
+    sftvvec r;
+    r.x = sft__vfma(v.x, vm.m[0][0], sft__vfma(v.y, vm.m[1][0], sft__vfma(v.z, vm.m[2][0], vm.m[3][0])));
+    r.y = sft__vfma(v.x, vm.m[0][1], sft__vfma(v.y, vm.m[1][1], sft__vfma(v.z, vm.m[2][1], vm.m[3][1])));
+    r.z = sft__vfma(v.x, vm.m[0][2], sft__vfma(v.y, vm.m[1][2], sft__vfma(v.z, vm.m[2][2], vm.m[3][2])));
+    return sft__xnan3(r);
+}
+SFT_INLINE sftvvec sft_vv_transform_dir(sftvvec v, sftvmat vm) {
+    sftvvec r;
+    r.x = sft__vfma(v.x, vm.m[0][0], sft__vfma(v.y, vm.m[1][0], v.z * vm.m[2][0]));
+    r.y = sft__vfma(v.x, vm.m[0][1], sft__vfma(v.y, vm.m[1][1], v.z * vm.m[2][1]));
+    r.z = sft__vfma(v.x, vm.m[0][2], sft__vfma(v.y, vm.m[1][2], v.z * vm.m[2][2]));
+    return sft__xnan3(r);
+}
+SFT_INLINE sftvmat sft_vm_broadcast(sftmat m) {
+    sftvmat vm;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) vm.m[i][j] = sft__vset1(m.m[i][j]);
+    return vm;
+}
+#pragma GCC diagnostic pop
 
 /* core (sofren2.c:795-800) */
 SFT_FUNC void sft_init(i32 width, i32 height, i32 requested_threads);

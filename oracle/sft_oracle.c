@@ -68,6 +68,11 @@ static f32 x86_rsqrt(f32 xf) {
 }
 /* sft_vf_rcp_refined (sofren2.c:633-638): approx * (2 - a*approx) with a fused fnmadd */
 static inline f32 rcpr(f32 a) { const f32 r = x86_rcp(a); return r * fmaf(-a, r, 2.f); }
+/* NaN bits as the reference leaves them in memory on x86: every NaN of the render path comes from
+ * an invalid operation (0 * inf in rcpr's fnmadd for w = +-0), whose SSE/AVX result is the default
+ * NaN 0xFFC00000, passed through unchanged by later mul/add/fma.  aarch64 produces 0x7FC00000 for the
+ * same operation, so floats stored to compared buffers go through this map on every host. */
+static inline f32 x86nan(f32 v) { return v != v ? u2f(0xFFC00000u) : v; }
 static inline f32 vmin(f32 a, f32 b) { return a < b ? a : b; }   /* _mm256_min_ps(a, b) */
 static inline f32 vmax(f32 a, f32 b) { return a > b ? a : b; }   /* _mm256_max_ps(a, b) */
 /* _mm256_cvttps_epi32: truncation, 0x80000000 when out of range or NaN */
@@ -858,7 +863,7 @@ static void geom_job(octx* c, u32 ii, u32 mesh_i, u32 start, u32 count) {
                 const f32 iw = rcpr(w);
                 const f32 sx = fmaf(tx, iw * hw, bias_x), sy = fmaf(ty, iw * scale_y, bias_y);
                 ctx[v] = tx; cty[v] = ty; ctz[v] = tz; cw[v] = w;
-                ss->sx[v] = sx; ss->sy[v] = sy; ss->iw[v] = iw;
+                ss->sx[v] = x86nan(sx); ss->sy[v] = x86nan(sy); ss->iw[v] = x86nan(iw);
             }
             for (u32 batch = 0; batch < 16; batch++) {
                 u32 I0[8], I1[8], I2[8];

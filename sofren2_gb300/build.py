@@ -75,11 +75,17 @@ def build_library(force: bool = False) -> str:
     return LIB
 
 
+def reference_dir() -> str:
+    """Where the reference's sources are read from to build the checkers: SFT_REFERENCE_DIR, else
+    the build container's checkout of the reference project."""
+    return os.environ.get("SFT_REFERENCE_DIR") or "/root/reference"
+
+
 def build_checkers() -> None:
     """CPU oracle always; the reference harness only where the reference sources exist (x86-64 + AVX2)."""
     oracle_dir = os.path.join(ROOT, "oracle")
     _run(["make", "-s", "-C", oracle_dir, "oracle"])
-    ref_dir = os.environ.get("SFT_REFERENCE_DIR", "/root/reference")
+    ref_dir = reference_dir()
     if os.path.exists(os.path.join(ref_dir, "sofren2.c")) and os.uname().machine == "x86_64":
         _run(["make", "-s", "-C", oracle_dir, "ref", f"REF_DIR={ref_dir}"])
 

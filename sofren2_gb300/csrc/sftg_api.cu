@@ -162,6 +162,8 @@ static int pool_append(sftg_ctx* ctx, dpool& p, const void* src, size_t bytes, s
 
 extern "C" void sftg_destroy(sftg_ctx* ctx);
 
+static cudaError_t noalloc_scratch_setup(int device);
+
 extern "C" int sftg_create(int device, sftg_ctx** out) {
     if (!out) return SFTG_E_ARG;
     sftg_ctx* ctx = new sftg_ctx();
@@ -193,6 +195,7 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     ctx->stream = ctx->lanes[0].stream;
     cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming);
     sftg_tile_configure(227 * 1024);
+    if (noalloc_scratch_setup(device) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
     { const char* e = getenv("SFTG_NO_GRAPHS"); if (e && *e && *e != '0') ctx->use_graphs = false; }
     *out = ctx;
     return SFTG_OK;
@@ -1432,10 +1435,26 @@ extern "C" void* sftg_stream(const sftg_ctx* ctx) { return ctx ? (void*)ctx->str
  * rows (columns at or beyond the light count are never written) and both maps (one view).
  *
  * The scratch is shared by every context on the device: two calls that overlap in time, from
- * any threads or contexts, race on it.  Callers serialise them. */
+ * any threads or contexts, race on it.  Callers serialise them.
+ *
+ * The array's device address is looked up when a context is created on the device
+ * (noalloc_scratch_setup, from sftg_create).  The lookup loads the module that holds the array,
+ * which is when the 4 MiB are committed on the device: with CUDA's lazy module loading that
+ * would otherwise happen inside the first allocation-free call. */
 #define SFTG_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SFTG_NOALLOC_SCRATCH_BYTES];
 static void* g_noalloc_addr[SFTG_NOALLOC_MAX_DEVICES];
+
+/* with `device` current: the host-side name g_noalloc_scratch is only a stand-in, the kernels
+ * need the address the runtime gives for it on this device */
+static cudaError_t noalloc_scratch_setup(int device) {
+    if (device < 0 || device >= SFTG_NOALLOC_MAX_DEVICES) return cudaSuccess;   /* the entry point refuses such devices */
+    if (g_noalloc_addr[device]) return cudaSuccess;
+    void* a = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+    if (e == cudaSuccess) g_noalloc_addr[device] = a;
+    return e;
+}
 
 extern "C" int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* fd, uint8_t* light_vis) {
     if (!ctx || !fd) return SFTG_E_ARG;
@@ -1462,11 +1481,7 @@ extern "C" int sftg_light_vis_noalloc(sftg_ctx* ctx, const sftg_frame_desc* fd, 
                        off, (unsigned)SFTG_NOALLOC_SCRATCH_BYTES, np, fd->n_point, fd->n_instances);
     if (!np) return SFTG_OK;
     CK(cudaSetDevice(ctx->device));
-    if (!g_noalloc_addr[ctx->device]) {   /* once per device; make this first call outside any stream capture */
-        void* a = nullptr;
-        CK(cudaGetSymbolAddress(&a, g_noalloc_scratch));
-        g_noalloc_addr[ctx->device] = a;
-    }
+    CK(noalloc_scratch_setup(ctx->device));   /* done by sftg_create; a no-op here */
     char* d = (char*)g_noalloc_addr[ctx->device];
     cudaStream_t st = ctx->stream;
     sftg_frame F;

@@ -137,7 +137,7 @@ k_geometry(const sftg_frame* __restrict__ frames, const sftg_job* __restrict__ j
             const float tz = fma_(pw.x, VP[2], fma_(pw.y, VP[6], fma_(pw.z, VP[10], VP[14])));
             const float iw = rcpr(w);
             const float sx = fma_(tx, iw * hw, bias_x), sy = fma_(ty, iw * scale_y, bias_y);
-            S[v] = sx; S[64 + v] = sy; S[128 + v] = iw;
+            S[v] = x86nan(sx); S[64 + v] = x86nan(sy); S[128 + v] = x86nan(iw);
             S[192 + v] = pw.x; S[256 + v] = pw.y; S[320 + v] = pw.z;
             S[384 + v] = nw.x; S[448 + v] = nw.y; S[512 + v] = nw.z;
             s_v[warp][0][v] = tx; s_v[warp][1][v] = ty; s_v[warp][2][v] = tz; s_v[warp][3][v] = w;

@@ -10,7 +10,7 @@
 
 #define SFTG_D __device__ __forceinline__
 
-/* measured RCPPS / RSQRTPS results (see gen_x86_approx_tables.c) */
+/* measured RCPPS / RSQRTPS results (written by oracle/gen_x86_approx_tables.c) */
 __device__ const uint32_t g_rcp_tab[2048] = SFT_X86_RCP_TABLE_INIT;
 __device__ const uint32_t g_rsq_tab[2048] = SFT_X86_RSQRT_TABLE_INIT;
 
@@ -31,6 +31,13 @@ SFTG_D float x86_rsqrt(float xf) {
     const int oe = ((380 - (int)e) >> 1) + (int)(t >> 23) - 1;
     return __uint_as_float(((uint32_t)oe << 23) | (t & 0x7FFFFF));
 }
+
+/* NaN bits as x86 leaves them in memory.  Every NaN on the render path comes from an invalid
+ * operation (0 * inf in rcpr's fnmadd for w = +-0, inf - inf), whose SSE/AVX result is the default
+ * NaN 0xFFC00000; later mul/add/fma pass a NaN operand through unchanged.  CUDA arithmetic returns
+ * its own canonical NaN instead, so floats stored to buffers that are compared bit for bit go
+ * through this map. */
+SFTG_D float x86nan(float v) { return v != v ? __uint_as_float(0xFFC00000u) : v; }
 
 SFTG_D float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 /* sft_vf_rcp_refined: approx * (2 - a * approx), the inner term fused (fnmadd) */

@@ -13,8 +13,8 @@
  * guard-band choices; the AA chunk skip is a group ballot.  The decoded visibility buffer
  * (depth, vid) goes to global memory, where it stays L2-resident, with the tile's depth range.
  *
- * k_resolve: four CTAs per tile, each a quarter of its 4x2 blocks, small shared memory for
- * high occupancy.  A group of 8 threads is one 4x2 block (the reference's AVX2 lanes).  For
+ * k_resolve: 1 to 16 CTAs per tile (a tuning knob per sample count), each a share of its 4x2
+ * blocks, small shared memory for high occupancy.  A group of 8 threads is one 4x2 block (the reference's AVX2 lanes).  For
  * each distinct triangle in the block (peeled in the reference's order) all 8 lanes shade it,
  * because the reference's LOD uses the first covered lane's screen derivatives (neighbour
  * lanes via shuffles) and its proxy loop skips a proxy for the whole block when no lane is

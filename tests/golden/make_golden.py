@@ -1,6 +1,6 @@
 """Regenerates tests/golden/golden.json from the reference itself.
 
-Requires the reference sources at /root/reference (or SFT_REFERENCE_DIR) on an x86-64 host
+Requires the reference sources (sofren2_gb300.build.reference_dir(): SFT_REFERENCE_DIR) on an x86-64 host
 with AVX2: `make -C oracle ref` compiles them unmodified into oracle/_ref, and each golden case
 (tests/golden_cases.py) is rendered by that binary with one worker thread.  Stored per case and
 sample count: the SHA-256 of the scene blob and of every dump section, the live meshlet list
@@ -26,7 +26,8 @@ from oracle_lib import reference_dump  # noqa: E402
 
 
 def main(names: list[str]) -> None:
-    ref_dir = os.environ.get("SFT_REFERENCE_DIR", "/root/reference")
+    from sofren2_gb300.build import reference_dir
+    ref_dir = reference_dir()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={ref_dir}"], check=True)
     path = os.path.join(HERE, "golden.json")
     golden = json.load(open(path)) if os.path.exists(path) else {}
@@ -79,6 +80,17 @@ def main(names: list[str]) -> None:
         out = reference_pose(pose_blob(rig, req), len(rig["bones"]), len(req))
         golden["pose"] = {"rig_seed": 6001, "requests": len(req), "sha256": gc.sha(out)}
         print("pose", golden["pose"]["sha256"][:16], flush=True)
+    if not names or "soa_math" in names:
+        # the reference's SoA math helpers (oracle/soa_harness.c) on tests/test_soa_math.soa_inputs()
+        import tempfile
+        import numpy as np
+        from test_soa_math import soa_inputs
+        with tempfile.TemporaryDirectory() as td:
+            ip, op = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+            soa_inputs().tofile(ip)
+            subprocess.run([os.path.join(ROOT, "oracle", "_ref", "soa_harness"), ip, op], check=True)
+            golden["soa_math"] = {"seed": 7001, "groups": 512, "sha256": gc.sha(np.fromfile(op, np.uint32))}
+        print("soa_math", golden["soa_math"]["sha256"][:16], flush=True)
     if not names or "dmesh" in names:
         # the dynamic-mesh scene (oracle/dmesh_scene.h) rendered by the reference, per frame
         import tempfile

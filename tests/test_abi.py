@@ -67,15 +67,9 @@ int main(void){uint64_t st=0x9E3779B97F4A7C15ull; unsigned bad=0;
     with tempfile.TemporaryDirectory() as td:
         c, exe = os.path.join(td, "t.c"), os.path.join(td, "t")
         open(c, "w").write(src)
-        subprocess.run(["gcc", "-O1", "-msse", "-I", os.path.join(ROOT, "sofren2_gb300", "csrc"), c, "-o", exe], check=True)
+        subprocess.run(["gcc", "-O1", "-msse", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0, f"{r.stdout.strip()} mismatching inputs"
-
-
-def test_product_and_oracle_tables_identical():
-    a = open(os.path.join(ROOT, "sofren2_gb300", "csrc", "x86_approx_tables.h")).read()
-    b = open(os.path.join(ROOT, "oracle", "x86_approx_tables.h")).read()
-    assert a == b
 
 
 def test_scene_generation_is_platform_independent():

@@ -41,6 +41,27 @@ def test_oracle_matches_reference_digests_full(golden, name):
         o.close()
 
 
+def test_oracle_hand_padding_rows_hold_x86_default_nan(golden):
+    """The hand case's meshlets hold 3 live vertices; the 61 padding slots sit at the camera
+    position, so w = 0 and rcp_refined(0) = RCPPS(0) * fnmadd(0, inf, 2) is an invalid operation.
+    x86 writes its default NaN 0xFFC00000 into sx, sy and inv_w there (sofren2.c:633-638,
+    5109-5122); the oracle must write the same bits on any host (aarch64's default NaN is
+    0x7FC00000), and no other NaN pattern may appear."""
+    o = Oracle(gc.blob("hand"))
+    try:
+        frame = o.render_dump(0, 1)
+    finally:
+        o.close()
+    g = golden["hand"]["samples"]["1"]
+    ss = frame["ss_cache"].view(np.uint32).reshape(-1, 9, 64)[np.asarray(g["live_meshlets"], dtype=np.int64)]
+    isnan = (ss & 0x7F800000) == 0x7F800000
+    isnan &= (ss & 0x007FFFFF) != 0
+    assert np.all(ss[isnan] == 0xFFC00000)
+    per_row = isnan.sum(axis=(0, 2))
+    assert per_row[0] == per_row[1] == per_row[2] > 0, per_row   # sx, sy, inv_w
+    assert per_row[3:].sum() == 0, per_row                        # world position and normal stay finite
+
+
 SEEDS = [11, 12, 13]
 
 

@@ -4,6 +4,7 @@ frame, and a frame too large for the static scratch is refused before any device
 
 Named to be collected last, so it also runs after every other GPU test in the session."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -44,6 +45,15 @@ def lib(renderer):
     return L
 
 
+def _device_free_bytes() -> int:
+    """cudaMemGetInfo's free bytes through the CUDA runtime the library itself loaded (found by
+    its soname among the process's loaded libraries, not loaded a second time)."""
+    rt = C.CDLL("libcudart.so.13", mode=os.RTLD_NOLOAD | os.RTLD_GLOBAL)
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
 def _recorded_frame(renderer, lib, h):
     """Records frame 0 of a loaded scene with sft_batch_begin and returns its sftg_frame_desc."""
     lib.sft_batch_begin()
@@ -67,12 +77,16 @@ def test_noalloc_matches_frame_render(renderer, lib, name):
         dbg.light_vis = ref.ctypes.data
         rc = lib.sftg_frame_render(ctx, fd, None, 0, C.byref(dbg))
         assert rc == 0, lib.sftg_last_error(ctx)
-        outs = []
+        outs, free = [], [_device_free_bytes()]
         for _ in range(2):
             out = np.full(n_prox * 64, 0xAB, np.uint8)
             rc = lib.sftg_light_vis_noalloc(ctx, fd, out.ctypes.data)
             assert rc == 0, lib.sftg_last_error(ctx)
             outs.append(out)
+            free.append(_device_free_bytes())
+        # the contract itself: the calls take no device memory (the scratch was committed when
+        # the context was created, so not even the first call changes the free bytes)
+        assert free[0] == free[1] == free[2], f"{name}: device free memory changed across the calls: {free}"
         assert np.array_equal(outs[0], ref), f"{name}: first allocation-free call differs from sftg_frame_render"
         assert np.array_equal(outs[1], ref), f"{name}: second allocation-free call differs from sftg_frame_render"
         lights = gc.n_lights(name)
