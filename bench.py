@@ -19,8 +19,12 @@ creation (triangles/s); `--config 8` skeletal poses (2^16 requests on a 22-bone 
 Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events on the library's
 stream with an L2 flush (a 512 MiB device write) between steps, outside the events.  Under
 torchrun each rank renders its own frames on its own GPU (replicas, weak scaling); the job
-time is the max over ranks.  `--impl reference` times the CPU restatement of the reference
-algorithm (oracle/sft_oracle.c) on all host cores over a bounded sample of frames.
+time is the max over ranks.  `--impl reference` times the reference's own render path
+(sofren2.c unmodified, built on this host by `make -C oracle ref_bench`: its NEON path on an
+aarch64 host, AVX2 on x86-64) with its own worker pool on all host cores, over a bounded sample
+of frames; where that build is absent, the CPU restatement of the reference algorithm
+(oracle/sft_oracle.c), and the line says which (`cpu_baseline.kind`).  The same two CPU legs,
+reference first, form the `cpu_baseline` of the frame workloads.
 """
 from __future__ import annotations
 
@@ -224,11 +228,12 @@ def run_ours(args, cfg) -> dict:
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": cfg["name"], "width": W, "height": H, "msaa": S, "global_batch": world,
-                   "triangles": int(sum(int((ms.inds.reshape(-1, 16, 32)[:, :, :24].reshape(-1, 16, 3, 8)).any(axis=2).sum())
-                                         for mi, _, _ in sc.frames[0].instances for ms in sc.models[mi].meshes)),
-                   "l2": "flushed between steps (512 MiB device write, outside the timed events)",
-                   "parallelism": f"replicas x{world}"},
+        "config": frame_config(cfg),
+        "workload_detail": {"global_batch": world,
+                            "triangles": int(sum(int((ms.inds.reshape(-1, 16, 32)[:, :, :24].reshape(-1, 16, 3, 8)).any(axis=2).sum())
+                                                 for mi, _, _ in sc.frames[0].instances for ms in sc.models[mi].meshes)),
+                            "l2": "flushed between steps (512 MiB device write, outside the timed events)",
+                            "parallelism": f"replicas x{world}"},
         "e2e": {"value": job_throughput(args.steps, world, ms_e2e), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(W * H * 4)},
         "gpu_launches": int(launches),
@@ -384,15 +389,19 @@ def run_batch(args, cfg) -> dict:
     }
     if rank == 0 and not args.no_cpu_baseline:
         # bounded sample: the first view of every scene, at its own size and MSAA
-        fps = []
+        fps, kinds = [], set()
         for si in range(len(scs)):
             k = next(i for i, v in enumerate(vlist) if v[0] == si)
             w, h, S = sizes[k]
             cb = cpu_baseline(blobs[si], S, w, h, seconds=args.cpu_seconds / len(scs), frame=vlist[k][1])
             fps.append(cb["value"])
+            kinds.add(cb["kind"])
+        kind = "reference" if kinds == {"reference"} else "port"
         line["cpu_baseline"] = {"value": len(fps) / sum(1.0 / f for f in fps), "unit": "frames/s", "cores": cb["cores"],
-                                "kind": "port", "sample": f"one view of each of the {len(scs)} scenes at its own size and "
-                                "MSAA, ~%.0f s each (oracle/sft_oracle.c, tile-parallel); harmonic mean" % (args.cpu_seconds / len(scs))}
+                                "kind": kind, "sample": f"one view of each of the {len(scs)} scenes at its own size and "
+                                "MSAA, ~%.0f s each (%s); harmonic mean" % (
+                                    args.cpu_seconds / len(scs),
+                                    cb["sample"].split(": ", 1)[-1] if kind == "reference" else "oracle/sft_oracle.c, tile-parallel")}
     for h in hs:
         R.free_scene(h)
     R.close()
@@ -843,7 +852,114 @@ def raycast_cpu_baseline(blob: bytes, rays: np.ndarray, seconds: float = 12.0, c
                       "the reference's sft_raycast_instance runs on the calling thread)"}
 
 
+def reference_frame_times(blob: bytes, samples: int, frame: int = 0, threads: int | None = None, repeat: int = 100000,
+                          seconds: float = 0.0) -> np.ndarray | None:
+    """Wall times (s) of whole frames (lights, camera, draws, sft_present) of the reference's own
+    render path: sofren2.c unmodified, built for this host by `make -C oracle ref_bench` (the NEON
+    path on aarch64, AVX2 on x86-64), run with its own worker pool, sft_init(w, h, threads).
+    `repeat` frames, or fewer once `seconds` have passed (at least 3).  None when that build is
+    absent on this host."""
+    import tempfile
+    exe = os.path.join(ROOT, "oracle", "_ref", f"ref_bench_{samples}x")
+    if not os.path.exists(exe):
+        return None
+    threads = threads or os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as td:
+        sp, tp = os.path.join(td, "scene.sfts"), os.path.join(td, "times.bin")
+        with open(sp, "wb") as f:
+            f.write(blob)
+        env = dict(os.environ, SFT_NO_DUMP="1", SFT_TIMES=tp)
+        if seconds > 0:
+            env["SFT_TIME_BUDGET_MS"] = str(int(seconds * 1e3))
+        r = subprocess.run([exe, sp, os.devnull, str(frame), str(threads), str(repeat)], env=env, capture_output=True, text=True)
+        if r.returncode != 0 or not os.path.exists(tp):
+            return None
+        return np.fromfile(tp, np.uint64).astype(np.float64) * 1e-9
+
+
+_REF_AGREEMENT: dict = {}
+
+
+def reference_agreement(blob: bytes, samples: int, width: int, height: int, frame: int = 0) -> float:
+    """Fraction of the pixels of the reference build's frame (ref_bench, one dumped render) within
+    4 LSB per channel of the oracle's frame, which equals the GPU's bit for bit.  A build that
+    renders something else (a broken SIMD path) must not be timed as the baseline."""
+    import hashlib
+    import tempfile
+    from oracle_io import read_dump
+    from oracle_lib import Oracle, build_oracle
+    key = (hashlib.sha1(blob).hexdigest(), samples, frame)
+    if key not in _REF_AGREEMENT:
+        exe = os.path.join(ROOT, "oracle", "_ref", f"ref_bench_{samples}x")
+        close = 0.0
+        with tempfile.TemporaryDirectory() as td:
+            sp, dp = os.path.join(td, "scene.sfts"), os.path.join(td, "r.dump")
+            with open(sp, "wb") as f:
+                f.write(blob)
+            r = subprocess.run([exe, sp, dp, str(frame), str(os.cpu_count() or 1)], capture_output=True)
+            if r.returncode == 0:
+                ref = read_dump(dp)[0]["color"].reshape(-1)
+                build_oracle()
+                o = Oracle(blob)
+                try:
+                    ours, _, _ = o.render_color(frame, samples, width, height, threads=os.cpu_count() or 1)
+                finally:
+                    o.close()
+                ours = np.asarray(ours).reshape(-1)
+                if ours.size == ref.size:
+                    a = np.stack([(ref >> k) & 0xFF for k in (16, 8, 0)]).astype(np.int32)
+                    b = np.stack([(ours >> k) & 0xFF for k in (16, 8, 0)]).astype(np.int32)
+                    close = float((np.abs(a - b).max(axis=0) <= 4).mean())
+        _REF_AGREEMENT[key] = close
+    return _REF_AGREEMENT[key]
+
+
+REF_AGREEMENT_MIN = 0.98   # of pixels within 4 LSB: the reference build renders the same frame
+
+
+def _reference_desc(threads: int) -> str:
+    import platform
+    if platform.machine() == "aarch64":
+        build = ("its NEON path, 4 lanes, gcc -O2 -flax-vector-conversions, two defects repaired at build time: "
+                 "the call GCC 13 rejects (vmovl_u16 of a uint16x8_t, sofren2.c:473) gets its low half, and "
+                 "sft_vf_fmsub's sign (c - a*b instead of a*b - c, sofren2.c:425) is corrected")
+    else:
+        build = "its AVX2 path, 8 lanes, gcc -O2 -mavx2 -mfma"
+    return (f"the reference's own code (sofren2.c, source unmodified; {build}) on {platform.machine()} with "
+            f"sft_init(w, h, {threads}), wall time of whole frames")
+
+
+def reference_frames(blob: bytes, samples: int, width: int, height: int, seconds: float, frame: int = 0,
+                     threads: int | None = None) -> dict | None:
+    """The reference's own render path timed on the host cores: frames/s over frames 2..N.  None
+    when its build is absent here or renders a frame that disagrees with the oracle's."""
+    threads = threads or os.cpu_count() or 1
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", f"ref_bench_{samples}x")):
+        return None
+    agree = reference_agreement(blob, samples, width, height, frame)
+    if agree < REF_AGREEMENT_MIN:
+        return None
+    t = reference_frame_times(blob, samples, frame, threads, seconds=seconds)
+    if t is None:
+        return None
+    steady = t[1:] if t.size > 1 else t
+    return {"value": float(steady.size / steady.sum()), "unit": "frames/s", "cores": threads, "kind": "reference",
+            "agreement": f"{agree:.5f} of its pixels within 4 LSB of the oracle's (= the GPU's) frame",
+            "sample": f"{steady.size} frames of the same workload after 1 untimed frame: {_reference_desc(threads)}"}
+
+
 def cpu_baseline(blob: bytes, samples: int, width: int, height: int, seconds: float = 12.0, frame: int = 0) -> dict:
+    """The reference's own CPU path timed on the host cores when it is built on this host, with the
+    oracle port's number beside it; the oracle port alone otherwise."""
+    ref = reference_frames(blob, samples, width, height, seconds * 0.6, frame)
+    port = port_frames(blob, samples, width, height, seconds * (0.4 if ref else 1.0), frame)
+    if ref is None:
+        return port
+    ref["port"] = {k: port[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    return ref
+
+
+def port_frames(blob: bytes, samples: int, width: int, height: int, seconds: float = 12.0, frame: int = 0) -> dict:
     """The oracle restatement of the reference algorithm, timed on the host cores."""
     from oracle_lib import Oracle, build_oracle
     build_oracle()
@@ -954,31 +1070,57 @@ def run_reference(args, cfg) -> dict | None:
         jobs = [(scs[si].to_bytes(), f, S, scs[si].frames[f].width, scs[si].frames[f].height) for si, f, S in picks]
     else:
         jobs = [(getattr(scenes, cfg["gen"])().to_bytes(), 0, cfg["samples"], cfg["width"], cfg["height"])]
-    oracles = [Oracle(j[0]) for j in jobs]
-    times = []
-    try:
-        for k in range(max(1, args.warmup)):
-            _, f, S, w, h = jobs[k % len(jobs)]
-            oracles[k % len(jobs)].render_color(f, S, w, h, threads=threads)
-        for k in range(args.steps):
-            _, f, S, w, h = jobs[k % len(jobs)]
-            t0 = time.perf_counter()
-            oracles[k % len(jobs)].render_color(f, S, w, h, threads=threads)
-            times.append(time.perf_counter() - t0)
-    finally:
-        for o in oracles:
-            o.close()
+    # the reference's own build when this host has it (each job: its warm-up frames, then its
+    # share of the K timed frames, in one process with the reference's worker pool)
+    times, kind = [], "reference"
+    warm = max(1, args.warmup)
+    agree = []
+    for j, (blob, f, S, w, h) in enumerate(jobs):
+        n = len(range(j, args.steps, len(jobs)))
+        if n == 0:
+            continue
+        t = None
+        if os.path.exists(os.path.join(ROOT, "oracle", "_ref", f"ref_bench_{S}x")):
+            agree.append(reference_agreement(blob, S, w, h, f))
+            if agree[-1] >= REF_AGREEMENT_MIN:
+                t = reference_frame_times(blob, S, f, threads, repeat=warm + n)
+        if t is None or t.size < warm + n:
+            times, kind = [], "port"
+            break
+        times.extend(t[warm:].tolist())
+    if kind == "port":
+        oracles = [Oracle(j[0]) for j in jobs]
+        try:
+            for k in range(warm):
+                _, f, S, w, h = jobs[k % len(jobs)]
+                oracles[k % len(jobs)].render_color(f, S, w, h, threads=threads)
+            for k in range(args.steps):
+                _, f, S, w, h = jobs[k % len(jobs)]
+                t0 = time.perf_counter()
+                oracles[k % len(jobs)].render_color(f, S, w, h, threads=threads)
+                times.append(time.perf_counter() - t0)
+        finally:
+            for o in oracles:
+                o.close()
+        why = ("absent on this host" if not agree else
+               f"renders frames that disagree with the oracle's ({min(agree):.4f} of pixels within 4 LSB)")
+        sample = (f"{len(times)} frames after {warm} warm-up, CPU restatement of the reference algorithm "
+                  f"(oracle/sft_oracle.c), tile-parallel; the reference's own build is {why}")
+    else:
+        sample = f"{len(times)} frames after {warm} warm-up frames per scene: {_reference_desc(threads)}"
     fps = len(times) / sum(times)
     return {"metric": "frames_per_second", "value": fps, "unit": "frames/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene)", "impl": "reference",
-            "config": ({"workload": cfg["name"], "width": cfg["width"], "height": cfg["height"], "msaa": cfg["samples"]}
-                       if args.config < 4 else {"workload": cfg["name"], "sample": "one view per step, cycling over the scenes"}),
-            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": f"{len(times)} frames after {max(1, args.warmup)} warm-up, CPU restatement "
-                                       "of the reference algorithm (oracle/sft_oracle.c), tile-parallel"},
+            "config": frame_config(cfg) if args.config < 4 else {"workload": cfg["name"], "sample": "one view per step, cycling over the scenes"},
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def frame_config(cfg) -> dict:
+    """The config dict of a single-view frame workload, the same in both arms."""
+    return {"workload": cfg["name"], "width": cfg["width"], "height": cfg["height"], "msaa": cfg["samples"]}
 
 
 def main():

@@ -17,11 +17,32 @@
  *
  * usage: ref_harness <scene.sfts> <out.dump> [frame_index=-1 (all)] [threads=1] [repeat=1]
  * SFT_DEBUG_MODE=<n> in the environment selects a debug view (sft_set_debug_mode).
+ * Timing runs: SFT_TIMES=<path> appends, per repetition, the wall time of the whole frame (lights,
+ * camera, draws, sft_present; u64 ns) to that file, SFT_TIME_BUDGET_MS=<ms> stops repeating once
+ * that much time has passed (after 3 repetitions), and SFT_NO_DUMP=1 writes no dump.  The same
+ * source builds the reference's NEON path on aarch64 (SFT_SIMD_WIDTH 4), where the index swizzle
+ * of the blob's 8-lane batches is converted to 4-lane batches.
  * The MSAA sample count is fixed at compile time (SFT_USE_AA / SFT_AA_SAMPLES), as in the reference.
  */
 #define _GNU_SOURCE
 #define SFT_IMPL
 #define SFT_NO_DEBUG
+#if defined(__aarch64__) && defined(SFT_NEON_BUILD_SHIM)
+/* The reference's NEON path (sofren2.c:387-519) needs two repairs to run, made here without
+ * touching its source.  arm_neon.h is included first, so these macros leave its own definitions
+ * alone and apply only to the reference's calls.
+ *  - It does not compile with GCC 13.  Its vector-type mismatches (vshrq_n_u32 on int32x4_t,
+ *    sofren2.c:497) pass with -flax-vector-conversions (oracle/Makefile); sofren2.c:473 widens
+ *    8 bytes to a uint16x8_t and hands that to vmovl_u16, which takes the 4-lane uint16x4_t: the
+ *    4-lane loader needs the low four, which the call gets here.
+ *  - sft_vf_fmsub(a, b, c) must be a*b - c (the AVX2 path's _mm256_fmsub_ps, sofren2.c:294, and
+ *    the scalar path, 550); the NEON path maps it to vfmsq_f32(c, a, b) = c - a*b (sofren2.c:425).
+ *    With the sign flipped every triangle fails the area test (4837) and the frame stays empty.
+ *    The negation gives a*b - c with the same single rounding (round to nearest is symmetric). */
+#include <arm_neon.h>
+#define vmovl_u16(x) vmovl_u16(vget_low_u16(x))
+#define vfmsq_f32(c, a, b) vnegq_f32(vfmsq_f32((c), (a), (b)))
+#endif
 #include "sofren2.c"
 #include "sfts_blob.h"
 #include <time.h>
@@ -86,7 +107,16 @@ static sft_model* build_model(const sfts_scene* sc, const sfts_model* src, const
                 memcpy(ms->meshlet_skins[j].w3, sl->weights + 3 * 64, 64);
                 ms->culling_bone_inds[j] = sl->culling_bone;
             }
+#if SFT_SIMD_WIDTH == 8
             memcpy(ms->inds[j].inds, sl->inds, 512);
+#else
+            /* the blob holds the AVX2 build's swizzle (batches of 8 triangles: v0 x8, v1 x8, v2 x8,
+             * pad x8); this build's batches are SFT_SIMD_WIDTH triangles wide (sofren2.c:2419-2438) */
+            for (u32 t = 0; t < 128; t++)
+                for (u32 v = 0; v < 4; v++)
+                    ms->inds[j].inds[(t / SFT_SIMD_WIDTH) * SFT_SIMD_WIDTH * 4 + v * SFT_SIMD_WIDTH + t % SFT_SIMD_WIDTH] =
+                        sl->inds[(t / 8) * 32 + v * 8 + t % 8];
+#endif
             for (int q = 0; q < 8; q++) (*fields[q])[j] = sl->cull[q];
             m->meshlet_mesh_inds[off + j] = (u16)k;
         }
@@ -256,7 +286,12 @@ int main(int argc, char** argv) {
         color = (u32*)aalloc((size_t)f->width * f->height * 4);
         sftmat* bones_store = NULL;
         uint64_t best = ~0ull;
+        FILE* times = getenv("SFT_TIMES") ? fopen(getenv("SFT_TIMES"), "ab") : NULL;
+        const uint64_t budget_ns = getenv("SFT_TIME_BUDGET_MS") ? (uint64_t)atoll(getenv("SFT_TIME_BUDGET_MS")) * 1000000ull : 0;
+        const uint64_t rep_start = now_ns();
         for (int rep = 0; rep < repeat; rep++) {
+            if (budget_ns && rep >= 3 && now_ns() - rep_start > budget_ns) break;   /* timing runs only */
+            const uint64_t tf0 = now_ns();
             sft_set_ambient_light(f->ambient[0], f->ambient[1], f->ambient[2]);
             for (u32 l = 0; l < f->n_dir; l++)
                 sft_draw_directional_light(SFT_V(f->dir[l].dir[0], f->dir[l].dir[1], f->dir[l].dir[2]), f->dir[l].r, f->dir[l].g, f->dir[l].b, f->dir[l].intensity);
@@ -292,18 +327,20 @@ int main(int argc, char** argv) {
             }
             /* mark the screen-space cache so culled meshlets stay recognisable (0xFF) */
             const u64 ss_bytes = (u64)sft_state->cmd_queue.total_ss_meshlets.count * sizeof(struct sft_ss_meshlet);
-            memset(sft_state->scratch_arena.base, 0xFF, ss_bytes + 64);
+            if (!getenv("SFT_NO_DUMP")) memset(sft_state->scratch_arena.base, 0xFF, ss_bytes + 64);
             const uint64_t t0 = now_ns();
             sft_present();
             const uint64_t t1 = now_ns();
             if (t1 - t0 < best) best = t1 - t0;
-            if (rep + 1 == repeat) {
+            if (times) { const uint64_t fns = t1 - tf0; fwrite(&fns, 8, 1, times); }
+            if (rep + 1 == repeat && !getenv("SFT_NO_DUMP")) {
                 dump_frame(&d, f->width, f->height, color);
                 const uint64_t ns = best;
                 sfts_dump_section(&d, "present_ns", "u64", &ns, 8);
             }
             sft_frame_end();
         }
+        if (times) fclose(times);
         free(bones_store);
     }
     fclose(d.f);

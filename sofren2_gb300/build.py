@@ -88,6 +88,13 @@ def build_checkers() -> None:
     ref_dir = reference_dir()
     if os.path.exists(os.path.join(ref_dir, "sofren2.c")) and os.uname().machine == "x86_64":
         _run(["make", "-s", "-C", oracle_dir, "ref", f"REF_DIR={ref_dir}"])
+    # the reference's own render path for the timed CPU baseline, native to this host (NEON on
+    # aarch64), from the copy of its source that `make ref` left beside the builds
+    if os.path.exists(os.path.join(oracle_dir, "_ref", "src", "sofren2.c")):
+        try:
+            _run(["make", "-s", "-C", oracle_dir, "ref_bench"])
+        except RuntimeError as e:   # the baseline then falls back to the oracle port, and says so
+            print(f"reference CPU build failed on this host: {str(e).splitlines()[-1][:300]}", file=sys.stderr)
 
 
 if __name__ == "__main__":
