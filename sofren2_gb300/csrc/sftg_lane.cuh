@@ -14,22 +14,33 @@
 __device__ const uint32_t g_rcp_tab[2048] = SFT_X86_RCP_TABLE_INIT;
 __device__ const uint32_t g_rsq_tab[2048] = SFT_X86_RSQRT_TABLE_INIT;
 
+/* RCPPS.  The common case (1 <= exponent <= 252, either sign) is one range check, the table
+ * load and the assembly of sign, exponent 253 - e and the 12-bit measured mantissa; the rest
+ * (zeros and denormals -> +-inf, tiny results -> +-0, inf -> +-0, NaN quieted) is the slow path. */
 SFTG_D float x86_rcp(float xf) {
-    const uint32_t x = __float_as_uint(xf), s = x & 0x80000000u, e = (x >> 23) & 0xFF, m = x & 0x7FFFFF;
+    const uint32_t x = __float_as_uint(xf), ax = x & 0x7FFFFFFFu;
+    if (ax - 0x00800000u < (253u << 23) - 0x00800000u)
+        return __uint_as_float((x & 0x80000000u) | ((253u << 23) - (ax & 0x7F800000u)) | __ldg(&g_rcp_tab[(x >> 12) & 0x7FFu]));
+    const uint32_t s = x & 0x80000000u, e = (x >> 23) & 0xFF, m = x & 0x7FFFFF;
     if (e == 0xFF) return __uint_as_float(m ? (x | 0x00400000u) : s);
     if (e == 0) return __uint_as_float(s | 0x7F800000u);
-    if (e >= 253) return __uint_as_float(s);
-    return __uint_as_float(s | ((253u - e) << 23) | __ldg(&g_rcp_tab[m >> 12]));
+    return __uint_as_float(s);   /* e >= 253 */
 }
 
+/* RSQRTPS.  Positive normal inputs take the fast path: index = exponent parity and the top 10
+ * mantissa bits, result exponent (380 - e) / 2 plus the entry's adjustment (its bits 23 and up,
+ * less one), mantissa from the entry. */
 SFTG_D float x86_rsqrt(float xf) {
-    const uint32_t x = __float_as_uint(xf), s = x & 0x80000000u, e = (x >> 23) & 0xFF, m = x & 0x7FFFFF;
+    const uint32_t x = __float_as_uint(xf);
+    if (x - 0x00800000u < 0x7F000000u) {
+        const uint32_t e = x >> 23;
+        const uint32_t t = __ldg(&g_rsq_tab[((e & 1u) << 10) | ((x >> 13) & 0x3FFu)]);
+        return __uint_as_float((((380u - e) >> 1) << 23) + t - (1u << 23));
+    }
+    const uint32_t s = x & 0x80000000u, e = (x >> 23) & 0xFF, m = x & 0x7FFFFF;
     if (e == 0xFF) { if (m) return __uint_as_float(x | 0x00400000u); return __uint_as_float(s ? 0xFFC00000u : 0u); }
     if (e == 0) return __uint_as_float(s | 0x7F800000u);
-    if (s) return __uint_as_float(0xFFC00000u);
-    const uint32_t t = __ldg(&g_rsq_tab[(e & 1) * 1024 + (m >> 13)]);
-    const int oe = ((380 - (int)e) >> 1) + (int)(t >> 23) - 1;
-    return __uint_as_float(((uint32_t)oe << 23) | (t & 0x7FFFFF));
+    return __uint_as_float(0xFFC00000u);   /* negative normal */
 }
 
 /* NaN bits as x86 leaves them in memory.  Every NaN on the render path comes from an invalid

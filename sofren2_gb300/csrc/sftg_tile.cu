@@ -457,7 +457,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
 /* One CTA per quarter tile: tile light list (5855-5934) and proxy cache (5936-5990), then one
  * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
 template <int S>
-__global__ void __launch_bounds__(TILE_THREADS, S == 4 ? 4 : 3)   /* 64 / 85 registers: occupancy measured best */
+__global__ void __launch_bounds__(TILE_THREADS, S == 1 ? 3 : 4)   /* 64 registers at 2x and 4x, 80 at 1x: measured best */
 k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
