@@ -345,6 +345,46 @@ SFT_FUNC sft_model* sft_model_create(const sft_mesh_data* meshes, u32 mesh_count
                                      u32 proxy_count, u32 bone_count, const sft_tex_handle* lightmaps, u32 lightmap_count,
                                      sft_arena* arena);
 SFT_FUNC u32 sft_model_get_meshlet_count(const sft_model* model);
+/* extension: load-time builders of the reference's GLB loader (sofren2.c:7426-7700), for callers
+ * that hold raw triangles instead of a .glb file.  One raw mesh is what the loader gathers per
+ * material before it builds meshlets: vertex streams and a triangle list. */
+typedef struct sft_raw_mesh {
+    u32 vertex_count, triangle_count;
+    const f32* pos;        /* [vertex][3] */
+    const f32* nrm;        /* [vertex][3] */
+    const f32* uv;         /* [vertex][2] */
+    const u16* joints;     /* [vertex][4] skeleton joint indices, or NULL for a static mesh */
+    const u8* weights;     /* [vertex][4], 255 = 1 (with joints) */
+    const i32* indices;    /* [triangle][3] vertex indices, in the winding the renderer draws */
+    sft_mat_handle material;
+} sft_raw_mesh;
+/* extension: a skeleton joint as the shadow-proxy fitter sees it: parent (-1 for a root) and the
+ * joint's bind position (sft_bone.parent_ind / bind_pos, sofren2.c:1000-1010) */
+typedef struct sft_raw_bone { i32 parent_ind; sftvec bind_pos; } sft_raw_bone;
+/* extension: the meshlets of one raw mesh as the reference's loader builds them (sofren2.c:
+ * 7467-7660): greedy growth over triangle adjacency (vertex reuse first, normal cone second, at
+ * most 64 vertices and 128 triangles), the 8-lane index swizzle, Welzl bounding spheres
+ * (2255-2289), normal cones, and for a skinned mesh the per-meshlet culling joint (6918-7045).
+ * Arrays in sft_mesh_data's layout; up to `cap` meshlets are written and the meshlet count is
+ * returned (call again with larger arrays when it exceeds cap).  joints, weights and
+ * culling_bones may be NULL for a static mesh.  Like the reference, Welzl draws from the C
+ * library's rand(): seed it (srand) for repeatable results. */
+SFT_FUNC u32 sft_mesh_build_meshlets(const sft_raw_mesh* mesh, u32 bone_count, u32 cap, f32* attr, u8* inds, f32* cull,
+                                     u16* joints, u8* weights, i32* culling_bones);
+/* extension: the shadow proxies the reference fits at load (sofren2.c:3064-3524): with a
+ * skeleton, one capsule per joint cluster (triangles voted to their heaviest joint, clusters
+ * merged by area into their parents down to `budget`, capsules anchored at the joints); without
+ * one, capsules fitted to the vertices under the BLAS nodes that splitting the largest volumes
+ * gives.  blas_nodes: the model's sft_bvh_node images (256 B each).  Writes up to cap proxies and
+ * returns their count (0 for budget <= 0 or no BLAS). */
+SFT_FUNC u32 sft_model_fit_shadow_proxies(const sft_mesh_data* meshes, u32 mesh_count, const void* blas_nodes, u32 blas_count,
+                                          u32 blas_root, const sft_raw_bone* bones, u32 bone_count, i32 budget,
+                                          sft_shadow_proxy* out, u32 cap);
+/* extension: a model from raw meshes, as sft_model_load_glb makes one from a file: meshlets built
+ * on the host (sft_mesh_build_meshlets), the BLAS on the GPU, then the shadow proxies fitted
+ * (sft_model_fit_shadow_proxies).  bones may be NULL (bone_count 0) for a static model. */
+SFT_FUNC sft_model* sft_model_build(const sft_raw_mesh* meshes, u32 mesh_count, const sft_raw_bone* bones, u32 bone_count,
+                                    i32 shadow_proxy_budget, sft_arena* arena);
 /* model loading (sofren2.c:859-862): QSF2 files; GLB needs cgltf and is not provided */
 SFT_FUNC sft_model* sft_model_load_qsf(const char* path, sft_arena* arena);
 /* extension: the model's skeleton and animation tracks, what the reference's GLB loader fills
@@ -1389,6 +1429,554 @@ SFT_FUNC const void* sft_model_get_blas(const sft_model* model, u32* out_count, 
         if (sftg_model_blas(sft__s->gpu, model->device_id, 0, model->blas_count, mm->blas, NULL, NULL)) { free(mm->blas); mm->blas = NULL; }
     }
     return model ? model->blas : NULL;
+}
+
+/* ---------------------------------------------------------------- load-time builders
+ * The meshlet builder and the shadow-proxy fitter of the reference's GLB loader, restated on
+ * the host; every float expression keeps the reference's operation order, so a model built from
+ * the same triangles (and the same rand() state) gets the reference's meshlets and proxies bit
+ * for bit. */
+#define SFT__CONE_LIMIT (-0.173648f)   /* a candidate's normal may turn at most 100 degrees from the cone axis (sofren2.c:152) */
+
+typedef struct { sftvec c; f32 r; } sft__sphere;
+
+/* spheres through 2, 3 and 4 points (sofren2.c:2180-2243) */
+static sft__sphere sft__sphere2(sftvec a, sftvec b) {
+    sft__sphere s;
+    s.c = sft_v_mul(sft_v_add(a, b), 0.5f);
+    s.r = sft_v_length(sft_v_sub(a, b)) * 0.5f;
+    return s;
+}
+static sft__sphere sft__sphere3(sftvec p0, sftvec p1, sftvec p2) {
+    const sftvec a = sft_v_sub(p1, p0), b = sft_v_sub(p2, p0), axb = sft_v_cross(a, b);
+    const f32 den = 2.f * sft_v_length2(axb);
+    if (den < SFT_EPSILON) return sft__sphere2(p0, p1);        /* degenerate: the first two points */
+    const sftvec num = sft_v_cross(sft_v_sub(sft_v_mul(b, sft_v_length2(a)), sft_v_mul(a, sft_v_length2(b))), axb);
+    sft__sphere s;
+    s.c = sft_v_add(p0, sft_v_div(num, den));
+    s.r = sft_v_length(sft_v_sub(s.c, p0));
+    return s;
+}
+static sft__sphere sft__sphere4(sftvec p0, sftvec p1, sftvec p2, sftvec p3) {
+    const sftvec r1 = sft_v_sub(p1, p0), r2 = sft_v_sub(p2, p0), r3 = sft_v_sub(p3, p0);
+    const f32 q1 = sft_v_length2(r1), q2 = sft_v_length2(r2), q3 = sft_v_length2(r3);
+    /* 2x2 minors of the rows r1, r2, r3 */
+    const f32 m23yz = r2.y * r3.z - r3.y * r2.z, m23xz = r2.x * r3.z - r3.x * r2.z, m23xy = r2.x * r3.y - r3.x * r2.y;
+    const f32 m13yz = r1.y * r3.z - r3.y * r1.z, m13xz = r1.x * r3.z - r3.x * r1.z, m13xy = r1.x * r3.y - r3.x * r1.y;
+    const f32 m12yz = r1.y * r2.z - r2.y * r1.z, m12xz = r1.x * r2.z - r2.x * r1.z, m12xy = r1.x * r2.y - r2.x * r1.y;
+    const f32 det = r1.x * m23yz - r1.y * m23xz + r1.z * m23xy;
+    if (fabsf(det) < SFT_EPSILON) return sft__sphere3(p0, p1, p2);   /* coplanar: the first three points */
+    const f32 f = 0.5f / det;
+    sftvec o;
+    o.x = f * (m23yz * q1 - m13yz * q2 + m12yz * q3);
+    o.y = f * (-m23xz * q1 + m13xz * q2 - m12xz * q3);
+    o.z = f * (m23xy * q1 - m13xy * q2 + m12xy * q3);
+    sft__sphere s;
+    s.c = sft_v_add(p0, o);
+    s.r = sft_v_length(o);
+    return s;
+}
+static sft__sphere sft__sphere_support(const sftvec* sup, i32 n) {
+    sft__sphere s;
+    memset(&s, 0, sizeof(s));
+    if (n == 1) s.c = sup[0];
+    else if (n == 2) s = sft__sphere2(sup[0], sup[1]);
+    else if (n == 3) s = sft__sphere3(sup[0], sup[1], sup[2]);
+    else if (n == 4) s = sft__sphere4(sup[0], sup[1], sup[2], sup[3]);
+    return s;
+}
+/* Welzl's minimal enclosing sphere (sofren2.c:2255-2278): a point drawn with rand() leaves the
+ * set, the sphere of the rest is found, and the point joins the support set if it lies outside
+ * (squared distance above r^2 + SFT_EPSILON).  pts is reordered. */
+static sft__sphere sft__welzl(sftvec* pts, i32 n, sftvec* sup, i32 ns) {
+    if (n == 0 || ns == 4) return sft__sphere_support(sup, ns);
+    const i32 k = rand() % n;
+    const sftvec p = pts[k];
+    pts[k] = pts[n - 1];
+    pts[n - 1] = p;
+    const sft__sphere s = sft__welzl(pts, n - 1, sup, ns);
+    if (sft_v_length2(sft_v_sub(p, s.c)) <= s.r * s.r + SFT_EPSILON) return s;
+    sup[ns] = p;
+    return sft__welzl(pts, n - 1, sup, ns + 1);
+}
+
+/* one meshlet under construction (sofren2.c:1235-1246) */
+typedef struct {
+    i32 gv[SFT_VERTS_PER_MESHLET];   /* local vertex -> mesh vertex */
+    u32 nv;
+    u8 tri[128 * 3];                  /* local indices */
+    u32 nt;
+    sftvec axis;                      /* running normal cone axis, renormalised after every triangle */
+} sft__mlet;
+
+/* how well a triangle fits the meshlet (sofren2.c:2325-2362): -1 when it does not (full, normal
+ * beyond the cone limit, more than 64 vertices), else vertices shared + half the cone alignment */
+static f32 sft__mlet_score(const sft__mlet* b, i32 v0, i32 v1, i32 v2, sftvec n) {
+    if (b->nt >= 128) return -1.f;
+    if (b->nt > 0 && sft_v_dot(b->axis, n) < SFT__CONE_LIMIT) return -1.f;
+    u32 fresh = 3, shared = 0;
+    for (u32 i = 0; i < b->nv; i++)
+        if (b->gv[i] == v0 || b->gv[i] == v1 || b->gv[i] == v2) { fresh--; shared++; }
+    if (b->nv + fresh > SFT_VERTS_PER_MESHLET) return -1.f;
+    f32 score = (f32)shared;
+    if (b->nt > 0) score += sft_v_dot(b->axis, n) * 0.5f;
+    return score;
+}
+/* sofren2.c:2364-2402 */
+static void sft__mlet_add(sft__mlet* b, i32 v0, i32 v1, i32 v2, sftvec n) {
+    const i32 g[3] = { v0, v1, v2 };
+    for (int k = 0; k < 3; k++) {
+        i32 l = -1;
+        for (u32 i = 0; i < b->nv; i++) if (b->gv[i] == g[k]) { l = (i32)i; break; }
+        if (l < 0) { l = (i32)b->nv; b->gv[b->nv++] = g[k]; }
+        b->tri[b->nt * 3 + k] = (u8)l;
+    }
+    b->axis = sft_v_norm(sft_v_add(b->axis, n));
+    b->nt++;
+}
+static sftvec sft__raw_pos(const sft_raw_mesh* m, i32 v) { sftvec p = { m->pos[v * 3], m->pos[v * 3 + 1], m->pos[v * 3 + 2] }; return p; }
+static sftvec sft__raw_tri_normal(const sft_raw_mesh* m, i32 t) {
+    const i32* ix = m->indices + (size_t)t * 3;
+    return sft_v_face_normal(sft__raw_pos(m, ix[0]), sft__raw_pos(m, ix[1]), sft__raw_pos(m, ix[2]));
+}
+
+/* writes meshlet `mi` of the output arrays (sofren2.c:6918-7045 and the cone of 7631-7651) */
+static void sft__mlet_emit(const sft__mlet* b, const sft_raw_mesh* m, u32 bone_count, i32* scratch, u32 mi, f32* attr, u8* inds,
+                           f32* cull, u16* joints, u8* weights, i32* culling_bones) {
+    u8* I = inds + (size_t)mi * 512;
+    for (u32 t = 0; t < 128; t++) {   /* batches of 8 triangles: v0 x8, v1 x8, v2 x8, 8 zero bytes */
+        const u32 bt = t >> 3, l = t & 7;
+        const int live = t < b->nt;
+        for (int k = 0; k < 3; k++) I[bt * 32 + k * 8 + l] = live ? b->tri[t * 3 + k] : 0;
+        I[bt * 32 + 24 + l] = 0;
+    }
+    f32* A = attr + (size_t)mi * 640;
+    const int skinned = m->joints && m->weights;
+    if (skinned && scratch) memset(scratch, 0, (size_t)bone_count * sizeof(i32));
+    i32 best = 0, best_w = 0;
+    sftvec pts[SFT_VERTS_PER_MESHLET];
+    for (u32 i = 0; i < SFT_VERTS_PER_MESHLET; i++) {
+        const int live = i < b->nv;
+        const i32 g = live ? b->gv[i] : 0;
+        A[0 * 64 + i] = live ? m->pos[g * 3 + 0] : 0.f;
+        A[1 * 64 + i] = live ? m->pos[g * 3 + 1] : 0.f;
+        A[2 * 64 + i] = live ? m->pos[g * 3 + 2] : 0.f;
+        A[3 * 64 + i] = live ? m->nrm[g * 3 + 0] : 0.f;
+        A[4 * 64 + i] = live ? m->nrm[g * 3 + 1] : 0.f;
+        A[5 * 64 + i] = live ? m->nrm[g * 3 + 2] : 0.f;
+        A[6 * 64 + i] = live ? m->uv[g * 2 + 0] : 0.f;
+        A[7 * 64 + i] = live ? m->uv[g * 2 + 1] : 0.f;
+        A[8 * 64 + i] = 0.f;   /* no lightmap coordinates from this path */
+        A[9 * 64 + i] = 0.f;
+        if (skinned) {
+            for (int k = 0; k < 4; k++) {
+                const u16 j = live ? m->joints[g * 4 + k] : 0;
+                const u8 w = live ? m->weights[g * 4 + k] : 0;
+                if (joints) joints[(size_t)mi * 256 + k * 64 + i] = j;
+                if (weights) weights[(size_t)mi * 256 + k * 64 + i] = w;
+                /* the joint carrying the most weight over the meshlet's vertices, first to lead wins */
+                if (live && j < bone_count && scratch) {
+                    scratch[j] += w;
+                    if (scratch[j] > best_w) { best_w = scratch[j]; best = j; }
+                }
+            }
+        }
+        if (live) pts[i] = sft__raw_pos(m, g);
+    }
+    if (culling_bones) culling_bones[mi] = skinned ? best : -1;
+    sft__sphere sph;
+    memset(&sph, 0, sizeof(sph));
+    if (b->nv > 0) { sftvec sup[4]; sph = sft__welzl(pts, (i32)b->nv, sup, 0); }
+    /* normal cone: the widest angle between the axis and a triangle's normal, plus a margin */
+    const sftvec axis = sft_v_norm(b->axis);
+    f32 min_dot = 1.f;
+    for (u32 t = 0; t < b->nt; t++) {
+        sftvec p[3];
+        for (int k = 0; k < 3; k++) { const u32 v = b->tri[t * 3 + k]; p[k].x = A[v]; p[k].y = A[64 + v]; p[k].z = A[128 + v]; }
+        const f32 d = sft_v_dot(sft_v_face_normal(p[0], p[1], p[2]), axis);
+        if (d < min_dot) min_dot = d;
+    }
+    const f32 sin_a = (min_dot < 0.f) ? 1.f : sqrtf(1.f - min_dot * min_dot);
+    f32* C = cull + (size_t)mi * 8;
+    C[0] = sph.c.x; C[1] = sph.c.y; C[2] = sph.c.z; C[3] = sph.r;
+    C[4] = axis.x; C[5] = axis.y; C[6] = axis.z; C[7] = sin_a + 0.02f;
+}
+
+SFT_FUNC u32 sft_mesh_build_meshlets(const sft_raw_mesh* m, u32 bone_count, u32 cap, f32* attr, u8* inds, f32* cull,
+                                     u16* joints, u8* weights, i32* culling_bones) {
+    if (!m || !m->triangle_count || !m->indices || !m->pos || !m->nrm || !m->uv) return 0;
+    const i32 nt = (i32)m->triangle_count, nv = (i32)m->vertex_count;
+    for (i32 k = 0; k < nt * 3; k++) if (m->indices[k] < 0 || m->indices[k] >= nv) return 0;   /* an index outside the vertices */
+    /* triangles around each vertex, in triangle order (sofren2.c:7467-7492) */
+    i32* first = (i32*)calloc((size_t)nv + 1, sizeof(i32));
+    i32* around = (i32*)malloc((size_t)nt * 3 * sizeof(i32));
+    i32* head = (i32*)malloc(((size_t)nv + 1) * sizeof(i32));
+    u8* used = (u8*)calloc((size_t)nt, 1);
+    u8* queued = (u8*)calloc((size_t)nt, 1);
+    i32* front = (i32*)malloc((size_t)nt * sizeof(i32));
+    i32* scratch = (i32*)calloc((size_t)bone_count + 1, sizeof(i32));
+    for (i32 k = 0; k < nt * 3; k++) first[m->indices[k]]++;
+    for (i32 v = 0, acc = 0; v <= nv; v++) { const i32 c = v < nv ? first[v] : 0; first[v] = acc; acc += c; }
+    memcpy(head, first, ((size_t)nv + 1) * sizeof(i32));
+    for (i32 t = 0; t < nt; t++)
+        for (int k = 0; k < 3; k++) around[head[m->indices[t * 3 + k]]++] = t;
+
+    u32 count = 0;
+    i32 left = nt, seed_from = 0;
+    sft__mlet b;
+    while (left > 0) {
+        b.nv = 0; b.nt = 0; b.axis.x = b.axis.y = b.axis.z = 0.f;
+        i32 fh = 0, ft = 0;   /* frontier: triangles next to the meshlet, [fh, ft) still open */
+        while (b.nv < SFT_VERTS_PER_MESHLET && b.nt < 128 && left > 0) {
+            i32 pick_slot = -1, pick;
+            sftvec pick_n;
+            if (fh == ft) {   /* empty frontier: the first unused triangle in index order seeds (or joins) */
+                pick = -1;
+                for (i32 t = seed_from; t < nt; t++) if (!used[t]) { pick = seed_from = t; break; }
+                if (pick < 0) break;
+                pick_n = sft__raw_tri_normal(m, pick);
+                const i32* ix = m->indices + (size_t)pick * 3;
+                if (b.nt > 0 && sft__mlet_score(&b, ix[0], ix[1], ix[2], pick_n) < 0.f) break;
+            } else {          /* the open frontier triangle with the best score, first of equals */
+                f32 best = -1.f;
+                for (i32 k = fh; k < ft; k++) {
+                    const i32 t = front[k];
+                    if (used[t]) continue;
+                    const i32* ix = m->indices + (size_t)t * 3;
+                    const sftvec n = sft__raw_tri_normal(m, t);
+                    const f32 s = sft__mlet_score(&b, ix[0], ix[1], ix[2], n);
+                    if (s > best) { best = s; pick_slot = k; pick_n = n; }
+                }
+                if (pick_slot < 0) { fh = ft = 0; continue; }   /* nothing fits: restart from a seed (flags stay set) */
+                pick = front[pick_slot];
+            }
+            const i32* ix = m->indices + (size_t)pick * 3;
+            sft__mlet_add(&b, ix[0], ix[1], ix[2], pick_n);
+            used[pick] = 1;
+            left--;
+            if (pick_slot >= 0) front[pick_slot] = front[fh++];
+            for (int k = 0; k < 3; k++)
+                for (i32 a = first[ix[k]]; a < first[ix[k] + 1]; a++) {
+                    const i32 t = around[a];
+                    if (!used[t] && !queued[t]) { front[ft++] = t; queued[t] = 1; }
+                }
+        }
+        for (i32 k = fh; k < ft; k++) queued[front[k]] = 0;
+        if (count < cap && attr && inds && cull)
+            sft__mlet_emit(&b, m, bone_count, scratch, count, attr, inds, cull, joints, weights, culling_bones);
+        else { sftvec pts[SFT_VERTS_PER_MESHLET], sup[4]; for (u32 i = 0; i < b.nv; i++) pts[i] = sft__raw_pos(m, b.gv[i]); if (b.nv) sft__welzl(pts, (i32)b.nv, sup, 0); }
+        count++;
+    }
+    free(first); free(around); free(head); free(used); free(queued); free(front); free(scratch);
+    return count;
+}
+
+/* ---- shadow proxies (sofren2.c:3064-3524) */
+
+/* a capsule around a point set (sofren2.c:3064-3135): the principal axis by ten power steps on
+ * the covariance, the extent along it, a radius between the mean (x1.8) and the largest (x0.95)
+ * distance to the axis segment, and ends pushed out by 0.625 r to seal joints */
+static sft_shadow_proxy sft__capsule_fit(const sftvec* v, i32 n) {
+    sft_shadow_proxy out;
+    memset(&out, 0, sizeof(out));
+    if (n == 0) return out;
+    sftvec c = { 0.f, 0.f, 0.f };
+    for (i32 i = 0; i < n; i++) c = sft_v_add(c, v[i]);
+    c = sft_v_mul(c, 1.f / n);
+    f32 cov[3][3];
+    memset(cov, 0, sizeof(cov));
+    for (i32 k = 0; k < n; k++) {
+        const sftvec d = sft_v_sub(v[k], c);
+        const f32 a[3] = { d.x, d.y, d.z };
+        for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) cov[i][j] += a[i] * a[j];
+    }
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) cov[i][j] /= n;
+    sftvec axis = sft_v_normf(1.f, 1.f, 1.f);
+    for (int it = 0; it < 10; it++) {
+        sftvec nx;
+        nx.x = cov[0][0] * axis.x + cov[0][1] * axis.y + cov[0][2] * axis.z;
+        nx.y = cov[1][0] * axis.x + cov[1][1] * axis.y + cov[1][2] * axis.z;
+        nx.z = cov[2][0] * axis.x + cov[2][1] * axis.y + cov[2][2] * axis.z;
+        const f32 len = sft_v_length(nx);
+        if (len < SFT_EPSILON) break;
+        axis = sft_v_mul(nx, 1.f / len);
+    }
+    f32 t0 = 1e9f, t1 = -1e9f;
+    for (i32 i = 0; i < n; i++) {
+        const f32 t = sft_v_dot(sft_v_sub(v[i], c), axis);
+        if (t < t0) t0 = t;
+        if (t > t1) t1 = t;
+    }
+    const sftvec ra = sft_v_add(c, sft_v_mul(axis, t0)), ab = sft_v_sub(sft_v_add(c, sft_v_mul(axis, t1)), ra);
+    const f32 len2 = sft_v_length2(ab);
+    f32 sum_r = 0.f, max_r = 0.f;
+    for (i32 i = 0; i < n; i++) {
+        f32 t = 0.f;
+        if (!(len2 < SFT_EPSILON)) {
+            t = sft_v_dot(sft_v_sub(v[i], ra), ab) / len2;
+            t = t < 0.f ? 0.f : (t > 1.f ? 1.f : t);
+        }
+        const f32 r = sqrtf(sft_v_length2(sft_v_sub(v[i], sft_v_add(ra, sft_v_mul(ab, t)))));
+        sum_r += r;
+        if (r > max_r) max_r = r;
+    }
+    const f32 ra_ = (sum_r / n) * 1.8f, rb_ = max_r * 0.95f;
+    const f32 r = ra_ < rb_ ? ra_ : rb_;
+    f32 s0 = t0 - r * 0.625f, s1 = t1 + r * 0.625f;
+    if (s0 > s1) s0 = s1 = (t0 + t1) * 0.5f;
+    out.posa = sft_v_add(c, sft_v_mul(axis, s0));
+    out.posb = sft_v_add(c, sft_v_mul(axis, s1));
+    out.radius = r;
+    return out;
+}
+
+typedef struct { const sft_mesh_data* meshes; u32 mesh_count; const sft__node* nodes; u32 node_count; } sft__pmodel;
+
+/* mesh and local meshlet of a model meshlet index */
+static const sft_mesh_data* sft__pm_meshlet(const sft__pmodel* pm, u32 g, u32* local) {
+    for (u32 k = 0; k < pm->mesh_count; k++) {
+        if (g < pm->meshes[k].meshlet_count) { *local = g; return &pm->meshes[k]; }
+        g -= pm->meshes[k].meshlet_count;
+    }
+    return NULL;
+}
+/* the triangle corners under a BLAS node, depth first in slot order (sofren2.c:3144-3197) */
+static void sft__pm_gather(const sft__pmodel* pm, u32 node, sftvec** v, i32* cap, i32* n, int depth) {
+    if (node >= pm->node_count || depth > 64) return;
+    const sft__node* nd = &pm->nodes[node];
+    for (u32 c = 0; c < nd->count && c < 8; c++) {
+        const u32 ch = nd->child[c];
+        if (ch == 0xFFFFFFFFu) continue;
+        if (!nd->leaf) { sft__pm_gather(pm, ch, v, cap, n, depth + 1); continue; }
+        const u32 pay = ch & 0x7FFFFFFFu, tri = pay & 127u;
+        u32 lm;
+        const sft_mesh_data* md = sft__pm_meshlet(pm, pay >> 7, &lm);
+        if (!md) continue;
+        const u8* I = md->inds + (size_t)lm * 512;
+        const f32* A = md->attr + (size_t)lm * 640;
+        const u32 bt = tri >> 3, l = tri & 7;
+        if (*n + 3 > *cap) { *cap = *cap ? *cap * 2 + 3 : 1024; *v = (sftvec*)realloc(*v, (size_t)*cap * sizeof(sftvec)); }
+        for (int k = 0; k < 3; k++) {
+            const u8 q = I[bt * 32 + k * 8 + l];
+            sftvec p = { A[q], A[64 + q], A[128 + q] };
+            (*v)[(*n)++] = p;
+        }
+    }
+}
+/* static model (sofren2.c:3209-3268): starting from the root, the non-leaf node of the largest
+ * child-box volume is replaced by its children until `budget` nodes; one capsule per node */
+static u32 sft__proxies_bvh(const sft__pmodel* pm, u32 root, i32 budget, sft_shadow_proxy* out, u32 cap) {
+    u32* act = (u32*)malloc((size_t)budget * sizeof(u32));
+    i32 n = 1;
+    act[0] = root;
+    while (n < budget) {
+        i32 big = -1;
+        f32 big_vol = -1.f;
+        for (i32 i = 0; i < n; i++) {
+            if (act[i] >= pm->node_count) continue;
+            const sft__node* nd = &pm->nodes[act[i]];
+            if (nd->leaf) continue;
+            f32 mn[3] = { 1e30f, 1e30f, 1e30f }, mx[3] = { -1e30f, -1e30f, -1e30f };
+            for (u32 c = 0; c < nd->count && c < 8; c++)
+                for (int a = 0; a < 3; a++) {
+                    if (nd->mn[a][c] < mn[a]) mn[a] = nd->mn[a][c];
+                    if (nd->mx[a][c] > mx[a]) mx[a] = nd->mx[a][c];
+                }
+            const f32 vol = (mx[0] - mn[0]) * (mx[1] - mn[1]) * (mx[2] - mn[2]);
+            if (vol > big_vol) { big_vol = vol; big = i; }
+        }
+        if (big < 0) break;
+        const sft__node* sp = &pm->nodes[act[big]];
+        act[big] = sp->child[0];
+        for (u32 c = 1; c < sp->count && c < 8 && n < budget; c++)
+            if (sp->child[c] != 0xFFFFFFFFu) act[n++] = sp->child[c];
+    }
+    for (i32 i = 0; i < n && (u32)i < cap; i++) {
+        sftvec* v = NULL;
+        i32 vc = 0, vn = 0;
+        sft__pm_gather(pm, act[i], &v, &vc, &vn, 0);
+        out[i] = sft__capsule_fit(v, vn);
+        out[i].bone_ind = 0xFFFFFFFFu;   /* not bound to a joint */
+        free(v);
+    }
+    free(act);
+    return (u32)n;
+}
+
+static u16 sft__cluster_of(const u16* map, u16 b) { while (map[b] != b) b = map[b]; return b; }
+
+/* skinned model (sofren2.c:3270-3505) */
+static u32 sft__proxies_bones(const sft__pmodel* pm, const sft_raw_bone* bones, u32 nb, i32 budget, sft_shadow_proxy* out, u32 cap) {
+    typedef struct { f32 area; sftvec csum; i32 tris; } clus;
+    u16* map = (u16*)malloc((size_t)nb * sizeof(u16));
+    clus* cl = (clus*)calloc(nb, sizeof(clus));
+    for (u32 i = 0; i < nb; i++) map[i] = (u16)i;
+    /* each live triangle votes, with its area and centre, for the joint of the largest single
+     * weight over its corners (first of equals) */
+    for (u32 k = 0; k < pm->mesh_count; k++) {
+        const sft_mesh_data* md = &pm->meshes[k];
+        if (!md->joints || !md->weights) continue;
+        for (u32 ml = 0; ml < md->meshlet_count; ml++) {
+            const u8* I = md->inds + (size_t)ml * 512;
+            const f32* A = md->attr + (size_t)ml * 640;
+            const u16* J = md->joints + (size_t)ml * 256;
+            const u8* W = md->weights + (size_t)ml * 256;
+            for (u32 t = 0; t < 128; t++) {
+                const u32 bt = t >> 3, l = t & 7;
+                const u8 q[3] = { I[bt * 32 + l], I[bt * 32 + 8 + l], I[bt * 32 + 16 + l] };
+                if (q[0] == q[1] && q[1] == q[2]) continue;   /* padding */
+                i32 bone = 0;
+                f32 wmax = -1.f;
+                for (int c = 0; c < 3; c++)
+                    for (int s = 0; s < 4; s++)
+                        if ((f32)W[s * 64 + q[c]] > wmax) { wmax = W[s * 64 + q[c]]; bone = J[s * 64 + q[c]]; }
+                if ((u32)bone >= nb) continue;
+                sftvec p[3];
+                for (int c = 0; c < 3; c++) { p[c].x = A[q[c]]; p[c].y = A[64 + q[c]]; p[c].z = A[128 + q[c]]; }
+                const f32 area = sft_v_length(sft_v_cross(sft_v_sub(p[1], p[0]), sft_v_sub(p[2], p[0]))) * 0.5f;
+                const sftvec ctr = sft_v_mul(sft_v_add(p[0], sft_v_add(p[1], p[2])), 0.333333f);
+                cl[bone].area += area;
+                cl[bone].csum = sft_v_add(cl[bone].csum, ctr);
+                cl[bone].tris += 1;
+            }
+        }
+    }
+    i32 active = 0;
+    for (u32 i = 0; i < nb; i++) if (cl[i].tris > 0) active++;
+    /* merge the smallest-area cluster into its parent's cluster (a root into the largest other
+     * cluster) until the budget holds */
+    while (active > budget && active > 1) {
+        i32 small = -1;
+        f32 amin = 1e30f;
+        for (u32 i = 0; i < nb; i++) if (cl[i].tris > 0 && cl[i].area < amin) { amin = cl[i].area; small = (i32)i; }
+        if (small < 0) break;
+        i32 target = -1;
+        const i32 parent = bones[small].parent_ind;
+        if (parent != -1) target = (parent >= 0 && (u32)parent < nb) ? sft__cluster_of(map, (u16)parent) : -1;
+        else {
+            f32 amax = -1.f;
+            for (u32 i = 0; i < nb; i++) if ((i32)i != small && cl[i].area > amax) { amax = cl[i].area; target = (i32)i; }
+        }
+        if (target < 0 || target == small) break;
+        map[small] = (u16)target;
+        cl[target].area += cl[small].area;
+        cl[target].csum = sft_v_add(cl[target].csum, cl[small].csum);
+        cl[target].tris += cl[small].tris;
+        cl[small].tris = 0;
+        active--;
+    }
+    /* every skinned vertex slot with weight goes to the cluster of its heaviest joint */
+    sftvec** cv = (sftvec**)calloc(nb, sizeof(sftvec*));
+    i32* ccap = (i32*)calloc(nb, sizeof(i32));
+    i32* cn = (i32*)calloc(nb, sizeof(i32));
+    for (u32 k = 0; k < pm->mesh_count; k++) {
+        const sft_mesh_data* md = &pm->meshes[k];
+        if (!md->joints || !md->weights) continue;
+        for (u32 ml = 0; ml < md->meshlet_count; ml++) {
+            const f32* A = md->attr + (size_t)ml * 640;
+            const u16* J = md->joints + (size_t)ml * 256;
+            const u8* W = md->weights + (size_t)ml * 256;
+            for (u32 v = 0; v < SFT_VERTS_PER_MESHLET; v++) {
+                u8 wmax = W[v];
+                u16 bone = J[v];
+                for (int s = 1; s < 4; s++) if (W[s * 64 + v] > wmax) { wmax = W[s * 64 + v]; bone = J[s * 64 + v]; }
+                if (wmax == 0 || bone >= nb) continue;
+                const u16 c = sft__cluster_of(map, bone);
+                if (cn[c] >= ccap[c]) { ccap[c] = ccap[c] ? ccap[c] * 2 : 1024; cv[c] = (sftvec*)realloc(cv[c], (size_t)ccap[c] * sizeof(sftvec)); }
+                sftvec p = { A[v], A[64 + v], A[128 + v] };
+                cv[c][cn[c]++] = p;
+            }
+        }
+    }
+    /* capsules anchored at the joint, along joint -> centroid of the cluster's triangle centres;
+     * radius between the mean (x2.2) and the largest (x0.9) distance to the axis */
+    u32 w = 0;
+    for (u32 i = 0; i < nb; i++) {
+        if (cl[i].tris > 0 && cn[i] > 0 && w < cap) {
+            const sftvec ctr = sft_v_mul(cl[i].csum, 1.f / cl[i].tris), anc = bones[i].bind_pos;
+            sftvec axis = sft_v_sub(ctr, anc);
+            const f32 al = sft_v_length(axis);
+            if (al > SFT_EPSILON) axis = sft_v_mul(axis, 1.f / al);
+            else { axis.x = 0.f; axis.y = 1.f; axis.z = 0.f; }
+            f32 t0 = 1e9f, t1 = -1e9f, sum_r = 0.f, max_r = 0.f;
+            for (i32 k = 0; k < cn[i]; k++) {
+                const f32 t = sft_v_dot(sft_v_sub(cv[i][k], anc), axis);
+                if (t < t0) t0 = t;
+                if (t > t1) t1 = t;
+                const f32 r = sqrtf(sft_v_length2(sft_v_sub(cv[i][k], sft_v_add(anc, sft_v_mul(axis, t)))));
+                sum_r += r;
+                if (r > max_r) max_r = r;
+            }
+            const f32 ra_ = (sum_r / cn[i]) * 2.2f, rb_ = max_r * 0.9f;
+            const f32 r = ra_ < rb_ ? ra_ : rb_;
+            const f32 e0 = t0 - r * 0.25f, e1 = t1 + r * 0.25f;
+            f32 s0 = 0.f < e0 ? 0.f : e0, s1 = 0.f > e1 ? 0.f : e1;
+            if (s0 > s1) s0 = s1 = (s0 + s1) * 0.5f;
+            out[w].posa = sft_v_add(anc, sft_v_mul(axis, s0));
+            out[w].posb = sft_v_add(anc, sft_v_mul(axis, s1));
+            out[w].radius = r;
+            out[w].bone_ind = i;
+            w++;
+        }
+        free(cv[i]);
+    }
+    /* the reference counts every active cluster; a cluster without vertices leaves a zero proxy */
+    for (u32 i = w; i < (u32)active && i < cap; i++) memset(&out[i], 0, sizeof(out[i]));
+    free(cv); free(ccap); free(cn); free(map); free(cl);
+    return (u32)active;
+}
+
+SFT_FUNC u32 sft_model_fit_shadow_proxies(const sft_mesh_data* meshes, u32 mesh_count, const void* blas_nodes, u32 blas_count,
+                                          u32 blas_root, const sft_raw_bone* bones, u32 bone_count, i32 budget,
+                                          sft_shadow_proxy* out, u32 cap) {
+    if (budget <= 0 || !blas_nodes || blas_count == 0 || !meshes) return 0;
+    sft__pmodel pm = { meshes, mesh_count, (const sft__node*)blas_nodes, blas_count };
+    if (bone_count > 0 && bones) return sft__proxies_bones(&pm, bones, bone_count, budget, out, out ? cap : 0);
+    return sft__proxies_bvh(&pm, blas_root, budget, out, out ? cap : 0);
+}
+
+SFT_FUNC sft_model* sft_model_build(const sft_raw_mesh* meshes, u32 mesh_count, const sft_raw_bone* bones, u32 bone_count,
+                                    i32 shadow_proxy_budget, sft_arena* arena) {
+    (void)arena;
+    if (!meshes || !mesh_count) return NULL;
+    sft_mesh_data* md = (sft_mesh_data*)calloc(mesh_count, sizeof(sft_mesh_data));
+    sft_model* m = NULL;
+    int ok = 1;
+    for (u32 k = 0; k < mesh_count && ok; k++) {
+        const sft_raw_mesh* r = &meshes[k];
+        const int skinned = r->joints && r->weights;
+        /* at most one meshlet per triangle: build straight into arrays of that size */
+        const u32 cap = r->triangle_count ? r->triangle_count : 1;
+        f32* attr = (f32*)calloc((size_t)cap * 640, sizeof(f32));
+        u8* inds = (u8*)calloc((size_t)cap * 512, 1);
+        f32* cull = (f32*)calloc((size_t)cap * 8, sizeof(f32));
+        u16* jn = skinned ? (u16*)calloc((size_t)cap * 256, sizeof(u16)) : NULL;
+        u8* wt = skinned ? (u8*)calloc((size_t)cap * 256, 1) : NULL;
+        i32* cb = skinned ? (i32*)calloc(cap, sizeof(i32)) : NULL;
+        const u32 n = sft_mesh_build_meshlets(r, bone_count, cap, attr, inds, cull, jn, wt, cb);
+        if (n == 0 && r->triangle_count) ok = 0;
+        md[k].meshlet_count = n; md[k].attr = attr; md[k].inds = inds; md[k].cull = cull;
+        md[k].joints = jn; md[k].weights = wt; md[k].culling_bones = cb;
+        md[k].material = r->material; md[k].lightmap_page = 0xFFFFFFFFu;
+    }
+    if (ok) m = sft__model_create(md, mesh_count, NULL, 0, bone_count, NULL, 0, NULL, 0, 0);
+    if (m && shadow_proxy_budget > 0) {
+        u32 nodes = 0, root = 0;
+        const void* blas = sft_model_get_blas(m, &nodes, &root);
+        if (blas && nodes) {
+            const u32 np = sft_model_fit_shadow_proxies(md, mesh_count, blas, nodes, root, bones, bone_count, shadow_proxy_budget, NULL, 0);
+            sft_shadow_proxy* px = (sft_shadow_proxy*)calloc((size_t)np + 1, sizeof(sft_shadow_proxy));
+            sft_model_fit_shadow_proxies(md, mesh_count, blas, nodes, root, bones, bone_count, shadow_proxy_budget, px, np);
+            free(m->proxies);
+            m->proxies = px; m->proxy_count = np;
+        }
+    }
+    for (u32 k = 0; k < mesh_count; k++) {
+        free((void*)md[k].attr); free((void*)md[k].inds); free((void*)md[k].cull);
+        free((void*)md[k].joints); free((void*)md[k].weights); free((void*)md[k].culling_bones);
+    }
+    free(md);
+    return m;
 }
 
 /* ---------------------------------------------------------------- draw (sofren2.c:8410-8478) */

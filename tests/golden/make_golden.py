@@ -91,6 +91,32 @@ def main(names: list[str]) -> None:
             subprocess.run([os.path.join(ROOT, "oracle", "_ref", "soa_harness"), ip, op], check=True)
             golden["soa_math"] = {"seed": 7001, "groups": 512, "sha256": gc.sha(np.fromfile(op, np.uint32))}
         print("soa_math", golden["soa_math"]["sha256"][:16], flush=True)
+    if not names or "model_build" in names:
+        # the reference's load-time builders on raw meshes (oracle/build_harness.c): meshlets, BLAS and
+        # proxies per model of tests/raw_models.py, and its renders of oracle/build_scene.h over them
+        import tempfile
+        import numpy as np
+        import raw_models as rm
+        mb = {}
+        with tempfile.TemporaryDirectory() as td:
+            for n in rm.models():
+                ip, op = os.path.join(td, n + ".bin"), os.path.join(td, n + ".out")
+                open(ip, "wb").write(rm.blob(n))
+                subprocess.run([os.path.join(ROOT, "oracle", "_ref", "build_harness"), ip, op], check=True)
+                out = rm.read_output(op, n, True)
+                mb[n] = {"meshlets": [int(d["n"]) for d in out["meshes"]], "meshlet_sha256": gc.sha(np.frombuffer(rm.meshlet_bytes(out), np.uint8)),
+                         "proxies": int(out["proxies"].shape[0]), "proxy_sha256": gc.sha(out["proxies"]),
+                         "blas_nodes": len(out["blas"]) // 256, "blas_root": out["blas_root"],
+                         "blas_sha256": gc.sha(np.frombuffer(out["blas"], np.uint8))}
+                print("model_build", n, mb[n]["meshlets"], mb[n]["proxies"], flush=True)
+            frames = {}
+            for S, exe in ((1, "build_harness"), (4, "build_harness_4x")):
+                fp = os.path.join(td, f"frames{S}.bin")
+                subprocess.run([os.path.join(ROOT, "oracle", "_ref", exe), "render", fp] +
+                               [os.path.join(td, n + ".bin") for n in ("ground", "shapes", "humanoid")], check=True)
+                frames[str(S)] = [gc.sha(f) for f in np.fromfile(fp, np.uint32).reshape(-1, 360, 640)]
+            mb["frames"] = frames
+        golden["model_build"] = mb
     if not names or "dmesh" in names:
         # the dynamic-mesh scene (oracle/dmesh_scene.h) rendered by the reference, per frame
         import tempfile
