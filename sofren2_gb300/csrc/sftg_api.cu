@@ -702,7 +702,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     B.status = bp.take<uint32_t>(16);
     B.totals = bp.take<uint32_t>(16);
     B.vis = bp.take<float2>(vis_total);
-    B.zrange = bp.take<float2>((size_t)total_tiles + 1);
+    B.zrange = bp.take<float2>((size_t)(total_tiles + 1) * sftg_raster_bands());   /* per raster band of each tile */
     B.vis_depth = nullptr; B.vis_id = nullptr; B.shadow = nullptr;
     if (want_debug) {
         B.vis_depth = bp.take<float>((size_t)total_tiles * S0 * 4096);

@@ -32,7 +32,7 @@ struct sftg_tile_args {
     const uint64_t* tile_pay;
     const uint8_t* light_vis;      /* [proxy][64] */
     float2* vis;                   /* (depth, vis id) per sample */
-    float2* zrange;                /* per tile */
+    float2* zrange;                /* per tile and raster band (sftg_raster_bands() entries per tile) */
     float* vis_depth;              /* debug capture of a single view, or null */
     uint32_t* vis_id;
     float* shadow_out;
@@ -66,6 +66,7 @@ void sftg_launch_occlusion(const sftg_frame* frames, const uint16_t* packet_view
                            uint32_t max_pairs, uint32_t items_per_pair, uint8_t* light_vis, uint32_t* status, int ray_prune,
                            cudaStream_t st);
 cudaError_t sftg_tile_configure(int max_dynamic_smem);
+int sftg_raster_bands(void);   /* raster CTAs (row bands) per 64x64 tile */
 /* order[] = the batch's tiles, heaviest first inside each sample-count range; scratch holds 192 words */
 int sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
                             uint32_t* scratch, uint32_t* order, cudaStream_t st);

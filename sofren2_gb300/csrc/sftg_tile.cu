@@ -2,7 +2,10 @@
  * Per-tile raster and resolve (sft__worker_phase_rasterize, sofren2.c:6756-6813,
  * sft__rast_simd_batch 5148-5499, sft__resolve_tile 5809-6753).
  *
- * k_raster: one CTA per 64x64 tile.  The reference walks the tile's list in order and keeps a
+ * k_raster: one to four CTAs per 64x64 tile, each owning a band of its rows (more for tiles with
+ * more payloads; every CTA sets up the tile's whole list and keeps the triangles that reach its
+ * band, whose rows it walks from the triangle's first row exactly as the one-CTA walk would).
+ * The reference walks the tile's list in order and keeps a
  * sample when z > stored z (strict), so a sample ends holding the largest z, and among equal z
  * the earliest triangle.  That final state does not depend on the order triangles are visited,
  * so each sample is a 64-bit shared-memory word (z bits << 32 | ~order) updated with atomicMax,
@@ -26,7 +29,17 @@
 
 #define TILE_THREADS 256          /* resolve CTA */
 #define RASTER_THREADS 512        /* raster CTA: 64 groups of 8 */
-#define SETUP_CAP RASTER_THREADS  /* triangle set-ups per round: 64 payloads x 8 lanes */
+/* A tile is rastered by 1, 2 or 4 CTAs, each owning a band of its rows, by its payload count: the
+ * frame's raster time is set by its heaviest tiles, which one CTA would walk alone. */
+#define RASTER_BANDS 4            /* raster CTAs launched per tile; those past the tile's band count exit */
+#define BANDS2_ABOVE 48           /* payloads above which a tile gets 2 bands */
+#define BANDS4_ABOVE 128          /* and 4 (1x and 2x; measured: at 4x two bands are best for every tile) */
+/* keys of one sample plane in shared memory: a whole tile, except at 4x, where every tile takes at
+ * least 2 bands so that the keys (S x 32 KB per tile) leave room for 2 CTAs per SM */
+template <int S> struct raster_plan {
+    static constexpr int min_bands = S == 4 ? 2 : 1, plane = SFTG_TILE_PX / min_bands, rows = SFTG_TILE / min_bands;
+};
+#define SETUP_CAP RASTER_THREADS  /* triangle set-ups per round: one per thread */
 #define MIN_SLAB_ROWS 4           /* smallest raster work item (rows); the slab height is a tuning knob */
 
 struct tri_setup {
@@ -90,6 +103,14 @@ __constant__ float c_ms_oy2[2] = { -0.25f, 0.25f };
 
 template <int S> SFTG_D float ms_ox(int s) { return S == 4 ? c_ms_ox4[s] : (S == 2 ? c_ms_ox2[s] : 0.f); }
 template <int S> SFTG_D float ms_oy(int s) { return S == 4 ? c_ms_oy4[s] : (S == 2 ? c_ms_oy2[s] : 0.f); }
+
+/* a tile's depth range (1/w of its samples above 1e-4): the union of its raster bands' ranges */
+SFTG_D float2 tile_zrange(const float2* zr, uint32_t gtile) {
+    float2 r = zr[(size_t)gtile * RASTER_BANDS];
+#pragma unroll
+    for (int b = 1; b < RASTER_BANDS; b++) { const float2 q = zr[(size_t)gtile * RASTER_BANDS + b]; r.x = fminf(r.x, q.x); r.y = fmaxf(r.y, q.y); }
+    return r;
+}
 
 SFTG_D uint64_t zkey(float z, uint32_t order) { return ((uint64_t)__float_as_uint(z) << 32) | (uint64_t)(0xFFFFFFFFu - order); }
 
@@ -215,7 +236,7 @@ SFTG_D bool tri_setup_one(float sx0, float sy0, float iw0, float sx1, float sy1,
 
 /* the incremental edge walk for pixel column `l` of one triangle (5345-5497) */
 template <int S>
-SFTG_D void tri_raster(const tri_setup& T, int y0, int y1, int l, uint32_t gmask, int tmx, int tmy, unsigned long long* keys) {
+SFTG_D void tri_raster(const tri_setup& T, int y0, int y1, int l, uint32_t gmask, int tmx, int ky0, unsigned long long* keys) {
     float de0[S], de1[S], de2[S], dz[S];
 #pragma unroll
     for (int s = 0; s < S; s++) {
@@ -234,13 +255,13 @@ SFTG_D void tri_raster(const tri_setup& T, int y0, int y1, int l, uint32_t gmask
     const uint32_t order = T.order;
     for (int y = y0; y <= y1; y++) {
         float e0 = e0r, e1 = e1r, e2 = e2r, z = zr;
-        int pi = (y - tmy) * SFTG_TILE + (T.ax0 - tmx) + l;
+        int pi = (y - ky0) * SFTG_TILE + (T.ax0 - tmx) + l;   /* keys hold the band's rows from ky0 */
         for (int x = T.ax0; x < T.ax1; x += 8, pi += 8) {
             if (T.trivial) {
 #pragma unroll
                 for (int s = 0; s < S; s++) {
                     const float zs = (S > 1) ? z + dz[s] : z;
-                    if (zs > 0.f) atomicMax(&keys[s * SFTG_TILE_PX + pi], zkey(zs, order));
+                    if (zs > 0.f) atomicMax(&keys[s * raster_plan<S>::plane + pi], zkey(zs, order));
                 }
             } else if (S == 1) {
                 if (e0 >= 0.f && e1 >= 0.f && e2 >= 0.f && z > 0.f) atomicMax(&keys[pi], zkey(z, order));
@@ -252,7 +273,7 @@ SFTG_D void tri_raster(const tri_setup& T, int y0, int y1, int l, uint32_t gmask
                         const float a = e0 + de0[s], b = e1 + de1[s], c = e2 + de2[s];
                         if (a >= 0.f && b >= 0.f && c >= 0.f) {
                             const float zs = z + dz[s];
-                            if (zs > 0.f) atomicMax(&keys[s * SFTG_TILE_PX + pi], zkey(zs, order));
+                            if (zs > 0.f) atomicMax(&keys[s * raster_plan<S>::plane + pi], zkey(zs, order));
                         }
                     }
                 }
@@ -325,16 +346,17 @@ __global__ void __launch_bounds__(RASTER_THREADS)
 k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned long long* keys = (unsigned long long*)smem;                  /* S * 4096 */
-    tri_setup_packed* setups = (tri_setup_packed*)(smem + (size_t)S * SFTG_TILE_PX * 8);
+    unsigned long long* keys = (unsigned long long*)smem;                  /* S planes, a band uses the first band_px of each */
+    tri_setup_packed* setups = (tri_setup_packed*)(smem + (size_t)S * raster_plan<S>::plane * 8);
     uint32_t* items = (uint32_t*)(setups + SETUP_CAP);                     /* set-up index << 8 | slab */
     __shared__ uint32_t s_nsetup, s_nbig, s_nsmall, s_next;
     /* work items of a round: long slabs from the front of the array, short ones from the back,
      * and the queue hands out the long ones first, so that a round does not end on one group
      * still walking a long slab (items touch keys only through atomicMax: order is free) */
-    const uint32_t items_cap = (uint32_t)SETUP_CAP * (uint32_t)((SFTG_TILE + slab_rows - 1) / slab_rows);
+    const uint32_t items_cap = (uint32_t)SETUP_CAP * (uint32_t)((raster_plan<S>::rows + slab_rows - 1) / slab_rows);
     __shared__ float s_red[2][RASTER_THREADS / 32];
-    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x];              /* batch-wide tile index, heaviest first */
+    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x / RASTER_BANDS];   /* batch-wide tile index, heaviest first */
+    const int band = (int)(blockIdx.x % RASTER_BANDS);
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
     const float* ss = A.ss + (size_t)F->ss_base * 576;
@@ -343,11 +365,18 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
     uint32_t count = A.tile_count[gtile];
     if ((uint64_t)A.tile_start[gtile] + count > F->tile_cap) count = 0;   /* overflowed frame, redone by the host */
+    const int bands = max(raster_plan<S>::min_bands, (S < 4 && count > BANDS4_ABOVE) ? 4 : (count > BANDS2_ABOVE ? 2 : 1));
+    if (band >= bands) {   /* not needed for this tile: an empty depth range for the readers' union */
+        if (threadIdx.x == 0) A.zrange[(size_t)gtile * RASTER_BANDS + band] = make_float2(1e9f, -1e9f);
+        return;
+    }
+    const int band_rows = SFTG_TILE / bands, band_px = band_rows * SFTG_TILE;
+    const int by0 = tmy + band * band_rows, by1 = by0 + band_rows - 1;   /* this CTA's rows */
     const uint64_t* list = A.tile_pay + A.tile_start[gtile];
     float* vis_depth = A.vis_depth;
     uint32_t* vis_id = A.vis_id;
 
-    for (int i = tid; i < S * SFTG_TILE_PX; i += RASTER_THREADS) keys[i] = 0ull;
+    for (int i = tid; i < S * band_px; i += RASTER_THREADS) keys[(i / band_px) * raster_plan<S>::plane + i % band_px] = 0ull;
     const int grp_lane = tid & 7;
     const uint32_t gmask = 0xFFu << (lane & ~7);
     /* the payloads in equal rounds of at most SETUP_CAP / 8 (a short last round would leave most
@@ -388,11 +417,15 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
                 }
                 if (active) {
                     tri_setup T;
-                    if (tri_setup_one<S>(sx[0], sy[0], iw[0], sx[1], sy[1], iw[1], sx[2], sy[2], iw[2], tmx, tmy, p * 8 + l, T)) {
+                    /* the set-up is the whole tile's (bounds clamped to the 64x64 tile, edge values from
+                     * its first row); the band keeps the triangles that reach its rows */
+                    if (tri_setup_one<S>(sx[0], sy[0], iw[0], sx[1], sy[1], iw[1], sx[2], sy[2], iw[2], tmx, tmy, p * 8 + l, T) &&
+                        T.maxy >= by0 && T.miny <= by1) {
                         const uint32_t slot = atomicAdd(&s_nsetup, 1u);
                         setups[slot] = pack_setup(T, tmx, tmy);
-                        const uint32_t nslab = (uint32_t)(T.maxy - T.miny) / (uint32_t)slab_rows + 1u;
-                        const int rows = min(T.maxy - T.miny + 1, slab_rows), chunks = (T.ax1 - T.ax0) >> 3;
+                        const int ys = max(T.miny, by0), ye = min(T.maxy, by1);
+                        const uint32_t nslab = (uint32_t)(ye - ys) / (uint32_t)slab_rows + 1u;
+                        const int rows = min(ye - ys + 1, slab_rows), chunks = (T.ax1 - T.ax0) >> 3;
                         if (S == 4 || rows * chunks >= 16) {   /* measured: the 4x raster keeps arrival order */
                             const uint32_t ib = atomicAdd(&s_nbig, nslab);
                             for (uint32_t k = 0; k < nslab; k++) items[ib + k] = (slot << 8) | k;
@@ -413,9 +446,9 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
             if (idx >= nitem) break;
             const uint32_t it = idx < nbig ? items[idx] : items[items_cap - 1u - (idx - nbig)];
             const tri_setup T = unpack_setup<S>(setups[it >> 8], tmx, tmy);
-            const int y0 = T.miny + (int)(it & 0xFFu) * slab_rows;
-            const int y1 = min(y0 + slab_rows - 1, T.maxy);
-            tri_raster<S>(T, y0, y1, grp_lane, gmask, tmx, tmy, keys);
+            const int y0 = max(T.miny, by0) + (int)(it & 0xFFu) * slab_rows;   /* rows before y0 are replayed */
+            const int y1 = min(y0 + slab_rows - 1, min(T.maxy, by1));
+            tri_raster<S>(T, y0, y1, grp_lane, gmask, tmx, by0, keys);
         }
         __syncthreads();
     }
@@ -423,8 +456,10 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     /* decode, store, depth range */
     float zmin = 1e9f, zmax = -1e9f;
     float2* tv = A.vis + F->vis_base + (size_t)tile * S * SFTG_TILE_PX;
-    for (int i = tid; i < S * SFTG_TILE_PX; i += RASTER_THREADS) {
-        const unsigned long long k = keys[i];
+    for (int i = tid; i < S * band_px; i += RASTER_THREADS) {
+        const int sp = i / band_px, pp = i % band_px;
+        const unsigned long long k = keys[sp * raster_plan<S>::plane + pp];
+        const int ti = sp * SFTG_TILE_PX + band * band_px + pp;              /* the same sample in the tile */
         float d = 0.f; uint32_t vid = SFTG_INVALID;
         if (k) {
             d = __uint_as_float((uint32_t)(k >> 32));
@@ -433,10 +468,10 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
             if ((pay >> 56) == 0) vid = (uint32_t)pay | 0x80000000u;
             else vid = ((uint32_t)(pay & 0xFFFFFF) << 25) | ((uint32_t)((pay >> 24) & 0xFFFFFF) << 7) | ((uint32_t)((pay >> 48) & 0xFF) * 8 + (order & 7));
         }
-        tv[i] = make_float2(d, __uint_as_float(vid));
+        tv[ti] = make_float2(d, __uint_as_float(vid));
         if (vis_id) {
-            vis_depth[(size_t)tile * S * SFTG_TILE_PX + i] = d;
-            vis_id[(size_t)tile * S * SFTG_TILE_PX + i] = vid;
+            vis_depth[(size_t)tile * S * SFTG_TILE_PX + ti] = d;
+            vis_id[(size_t)tile * S * SFTG_TILE_PX + ti] = vid;
         }
         if (d > 0.0001f) { zmin = fminf(zmin, d); zmax = fmaxf(zmax, d); }
     }
@@ -447,7 +482,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     if (tid == 0) {
         zmin = 1e9f; zmax = -1e9f;
         for (int w = 0; w < RASTER_THREADS / 32; w++) { zmin = fminf(zmin, s_red[0][w]); zmax = fmaxf(zmax, s_red[1][w]); }
-        A.zrange[gtile] = make_float2(zmin, zmax);
+        A.zrange[(size_t)gtile * RASTER_BANDS + band] = make_float2(zmin, zmax);   /* combined by the readers */
     }
 }
 
@@ -479,7 +514,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     float* shadow_out = A.shadow_out;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
-    const float2 zr = A.zrange[gtile];
+    const float2 zr = tile_zrange(A.zrange, gtile);
     const float zmin = zr.x, zmax = zr.y;
     const float2* vis = A.vis + F->vis_base + (size_t)tile * S * SFTG_TILE_PX;
 
@@ -1074,7 +1109,7 @@ __global__ void __launch_bounds__(256) k_debug_overlay(const sftg_tile_args A)
     const int lim_x = min(tmx + SFTG_TILE, sw), lim_y = min(tmy + SFTG_TILE, sh);
     uint32_t* color = F->color_dev;
     const float2* depth = A.vis + F->vis_base + (size_t)tile * F->samples * SFTG_TILE_PX;   /* sample 0 plane first */
-    const float2 zr = A.zrange[gtile];
+    const float2 zr = tile_zrange(A.zrange, gtile);
     const int ntl = A.tile_nlights[gtile];
     uint32_t border = 0xFF00FF00u, heat = 0;
     if (mode == 3) {
@@ -1113,9 +1148,12 @@ void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_
 /* ---------------------------------------------------------------- host-side launch helpers */
 /* keys, packed set-ups, then the work items of one round: up to SETUP_CAP * (64 / slab_rows) */
 static size_t raster_smem(int S, int slab_rows) {
-    return (size_t)S * SFTG_TILE_PX * 8 + (size_t)SETUP_CAP * sizeof(tri_setup_packed) +
-           (size_t)SETUP_CAP * ((SFTG_TILE + slab_rows - 1) / slab_rows) * 4;
+    const size_t plane = S == 4 ? raster_plan<4>::plane : SFTG_TILE_PX, rows = S == 4 ? raster_plan<4>::rows : SFTG_TILE;
+    return (size_t)S * plane * 8 + (size_t)SETUP_CAP * sizeof(tri_setup_packed) +
+           (size_t)SETUP_CAP * ((rows + slab_rows - 1) / slab_rows) * 4;
 }
+
+int sftg_raster_bands(void) { return RASTER_BANDS; }
 
 cudaError_t sftg_tile_configure(int max_dynamic_smem) {
     cudaError_t e = cudaSuccess;
@@ -1133,9 +1171,10 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
     const size_t sm = raster_smem(S, slab_rows);
-    if (S == 1) k_raster<1><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
-    else if (S == 2) k_raster<2><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
-    else k_raster<4><<<tiles, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
+    const uint32_t grid = tiles * RASTER_BANDS;
+    if (S == 1) k_raster<1><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
+    else if (S == 2) k_raster<2><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
+    else k_raster<4><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
 }
 
 void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A) {
