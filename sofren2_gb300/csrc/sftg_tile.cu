@@ -487,6 +487,13 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
 }
 
 /* ---------------------------------------------------------------- resolve */
+/* the tile's 4x2 block that a resolve CTA's b-th block is: at 4x the CTAs of a tile take every
+ * split-th block, so the costly ones (many triangles, many lights) spread over all of them
+ * (measured on the atrium at 4x: the slowest CTA of a tile took twice the mean with contiguous
+ * ranges); at 1x and 2x a contiguous range of rows keeps each CTA's surface points close together,
+ * which tightens the per-CTA proxy filter */
+template <int S>
+SFTG_D int block_of(int part, int split, int nblk, int b) { return S == 4 ? b * split + part : part * nblk + b; }
 #define TILE_BLOCKS (16 * 32)                 /* 4x2 blocks per 64x64 tile; a CTA resolves 1/split of them */
 
 /* One CTA per quarter tile: tile light list (5855-5934) and proxy cache (5936-5990), then one
@@ -575,7 +582,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
         uint32_t last = SFTG_INVALID;
         const int ix0 = tid & 3, iy0 = (tid >> 2) & 1;
         for (int b = tid >> 3; b < nblk; b += TILE_THREADS / 8) {
-            const int blk = part * nblk + b;
+            const int blk = block_of<S>(part, split, nblk, b);
             const int gx = tmx + (blk & 15) * 4 + ix0, gy = tmy + (blk >> 4) * 2 + iy0;
             if (gx >= lim_x || gy >= lim_y) continue;
             const int pind = (gy - tmy) * SFTG_TILE + (gx - tmx);
@@ -695,7 +702,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     const v3 cam = mk3(F->cam[0], F->cam[1], F->cam[2]);
 
     for (int b = grp; b < nblk; b += TILE_THREADS / 8) {
-        const int blk = part * nblk + b;
+        const int blk = block_of<S>(part, split, nblk, b);
         const int x = tmx + (blk & 15) * 4, y = tmy + (blk >> 4) * 2;
         if (x >= lim_x || y >= lim_y) continue;
         const int gx = x + ix, gy = y + iy;
