@@ -78,8 +78,8 @@ def _peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
-    return {"hbm_gbs": 6800.0, "src": "fallback"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured", "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0))}
+    return {"hbm_gbs": 6800.0, "src": "fallback", "sm_max_mhz": 2070.0}
 
 
 class ClockSampler:
@@ -131,12 +131,42 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_resolve launch of the
-# workload, from one full ncu capture of that launch on a GB300 (the 6th launch of
-# `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`)
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_resolve launch, from the ncu captures
-# summarised in profiles/k_resolve_*.md (same kernel code as this build's resolve)
-RESOLVE_TRAFFIC = {"skinned_1080p_2xmsaa": 38522624 + 108800, "atrium_1080p_4xmsaa": 76634880 + 4921088}
+# One k_resolve launch of the workload, from a full ncu capture of that launch on a GB300 (the 6th
+# launch of `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`, summarised in
+# profiles/k_resolve_*.md, same kernel code as this build's): DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum), warp instructions issued (smsp__inst_executed.sum), and the issue-active
+# and FMA-pipe fractions ncu measured over the kernel's active cycles.
+RESOLVE_PROFILE = {
+    "skinned_1080p_2xmsaa": {"traffic": 38543616 + 44544, "instructions": 155414816, "issue_active": 0.590, "fma_pipe": 0.219,
+                             "profile": "profiles/k_resolve_skinned_1080p_2x.md"},
+    "atrium_1080p_4xmsaa": {"traffic": 76679424 + 3172096, "instructions": 389862714, "issue_active": 0.596, "fma_pipe": 0.205,
+                            "profile": "profiles/k_resolve_atrium_1080p_4x.md"},
+    "static_640x360_1x": {"traffic": 2722560, "instructions": 5232418, "issue_active": 0.300, "fma_pipe": 0.067,
+                          "profile": "profiles/launches_static_640x360_1x.md"},
+}
+
+
+def resolve_roofline(name: str, W: int, H: int, S: int, tile_ms: float, clk: dict, peaks: dict) -> dict:
+    """k_resolve is issue bound (FP32 shading of lights x capsule proxies per pixel, DRAM a few %):
+    the roofline is its issue rate, warp instructions per launch (ncu) over the live CUDA-event
+    time, against 4 schedulers per SM at the SM clock sampled during the run.  The HBM form of
+    the contract (algorithmic bytes over time against the measured copy bandwidth) rides along."""
+    import torch
+    alg = _algorithmic_resolve_bytes(W, H, S)
+    gbs = alg / (tile_ms * 1e-3) / 1e9 if tile_ms > 0 else 0.0
+    prof = RESOLVE_PROFILE.get(name)
+    hbm = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
+           "traffic": prof["traffic"] if prof else None, "algorithmic_bytes": alg, "peak_source": peaks["src"]}
+    if not prof or tile_ms <= 0:
+        return {"kernel": "k_resolve", "bound": "hbm", **hbm, "note": "no ncu instruction count for this workload"}
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = float(clk.get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0)
+    peak = sms * 4 * mhz * 1e6
+    ach = prof["instructions"] / (tile_ms * 1e-3)
+    return {"kernel": "k_resolve", "bound": "issue", "achieved": ach, "peak": peak, "unit": "warp-instructions/s",
+            "frac": ach / peak, "traffic": prof["traffic"], "instructions_per_launch": prof["instructions"],
+            "peak_from": f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz (median SM clock sampled in the run)",
+            "ncu": {"issue_active": prof["issue_active"], "fma_pipe": prof["fma_pipe"], "source": prof["profile"]}, "hbm": hbm}
 
 
 def _algorithmic_resolve_bytes(width: int, height: int, samples: int) -> float:
@@ -220,8 +250,6 @@ def run_ours(args, cfg) -> dict:
     frames = args.steps * world
     peaks = _peaks()
     tile_ms = float(kern[4])
-    alg = _algorithmic_resolve_bytes(W, H, S)
-    achieved = alg / (tile_ms * 1e-3) / 1e9 if tile_ms > 0 else 0.0
     h2d = 4096 + sum(16 * 4 * (len(b) if b is not None else 0) for _, _, b in sc.frames[0].instances)
     line = {
         "metric": "frames_per_second", "value": job_throughput(args.steps, world, ms_dev), "unit": "frames/s",
@@ -239,11 +267,7 @@ def run_ours(args, cfg) -> dict:
         "gpu_launches": int(launches),
         "kernel_ms": {"occlusion": float(kern[0]), "geometry": float(kern[1]), "binning": float(kern[2]),
                       "raster": float(kern[3]), "resolve": tile_ms},
-        "roofline": {"kernel": "k_resolve", "bound": "hbm", "achieved": achieved,
-                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": RESOLVE_TRAFFIC.get(cfg["name"]), "algorithmic_bytes": alg, "peak_source": peaks["src"],
-                     "note": "the resolve is FP32/issue bound (lights x capsule proxies per pixel); "
-                             "HBM fraction of its algorithmic bytes shown per contract"},
+        "roofline": resolve_roofline(cfg["name"], W, H, S, tile_ms, clk, peaks),
         "clocks": clk,
         "wall_s": wall,
     }
