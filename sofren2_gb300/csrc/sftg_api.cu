@@ -103,7 +103,7 @@ struct sftg_ctx {
     uint32_t blas_items = 0, blas_launches = 0; /* and its triangles and kernels */
     cudaEvent_t ev_blas[2] = { nullptr, nullptr };
     bool use_graphs = true;
-    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0 };   /* measured best on the single-view workloads */
+    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0, { 0, 0, 0 } };   /* measured best on the single-view workloads */
     /* transient models (one frame's dynamic meshes): pool marks where they start */
     bool tr_live = false, tr_pinned = false;
     uint32_t tr_meshlets = 0, tr_skin = 0, tr_blas = 0;
@@ -869,7 +869,7 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
         CK(cudaStreamWaitEvent(st, ln.ev_merge[k], 0));
         return 0;
     };
-    int prc = per_range(0, [&](int si, cudaStream_t s) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], s, A); });
+    int prc = per_range(0, [&](int si, cudaStream_t s) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], ctx->tuning.raster_bands[si], s, A); });
     if (prc) return prc;
     CK(cudaGetLastError());
     CK(record_event(ln.ev[4], st));
@@ -1322,6 +1322,8 @@ static bool tuning_valid(const sftg_tuning* t) {
         const int sp = t->resolve_split[k], sl = t->raster_slab_rows[k];
         if (!(sp == 1 || sp == 2 || sp == 4 || sp == 8 || sp == 16)) return false;
         if (sl < 4 || sl > 64) return false;
+        const int rb = t->raster_bands[k];
+        if (!(rb == 0 || rb == 1 || rb == 2 || rb == 4)) return false;
     }
     return t->geom_job_width >= 1 && t->geom_job_width <= 8 && (t->occl_ray_prune == 0 || t->occl_ray_prune == 1);
 }
@@ -1334,7 +1336,7 @@ extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
 
 extern "C" int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* t) {
     if (!ctx || !t) return SFTG_E_ARG;
-    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8)");
+    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8, raster bands 0/1/2/4)");
     ctx->tuning = *t;
     return SFTG_OK;
 }
@@ -1353,9 +1355,9 @@ static int time_phase(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n, int
 }
 
 /* Coordinate search over the knobs that change only scheduling, never results: the geometry
- * job width against the geometry phase, then per sample count the raster slab height against
- * the raster phase and the resolve split against the resolve phase, each measured on the views
- * with that sample count.  Leaves the best setting in the context. */
+ * job width against the geometry phase, then per sample count the raster slab height and the
+ * raster bands against the raster phase and the resolve split against the resolve phase, each
+ * measured on the views with that sample count.  Leaves the best setting in the context. */
 extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, int32_t reps, sftg_tuning* out) {
     if (!ctx || !fds || !n_views) return SFTG_E_ARG;
     if (reps < 1) reps = 5;
@@ -1383,6 +1385,14 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
             float t;
             if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 3, &t))) { ctx->tuning = best; return rc; }
             if (t < bt) { bt = t; best.raster_slab_rows[si] = slabs[k]; }
+        }
+        const int bands[4] = { 0, 1, 2, 4 };
+        bt = 1e30f;
+        for (int k = 0; k < 4; k++) {
+            ctx->tuning = best; ctx->tuning.raster_bands[si] = bands[k];
+            float t;
+            if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 3, &t))) { ctx->tuning = best; return rc; }
+            if (t < bt) { bt = t; best.raster_bands[si] = bands[k]; }
         }
         const int splits[5] = { 4, 8, 16, 2, 1 };
         bt = 1e30f;

@@ -343,7 +343,7 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
  * light culling. */
 template <int S>
 __global__ void __launch_bounds__(RASTER_THREADS)
-k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
+k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S planes, a band uses the first band_px of each */
@@ -365,7 +365,8 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows)
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
     uint32_t count = A.tile_count[gtile];
     if ((uint64_t)A.tile_start[gtile] + count > F->tile_cap) count = 0;   /* overflowed frame, redone by the host */
-    const int bands = max(raster_plan<S>::min_bands, (S < 4 && count > BANDS4_ABOVE) ? 4 : (count > BANDS2_ABOVE ? 2 : 1));
+    const int bands = max(raster_plan<S>::min_bands,
+                          fixed_bands ? fixed_bands : ((S < 4 && count > BANDS4_ABOVE) ? 4 : (count > BANDS2_ABOVE ? 2 : 1)));
     if (band >= bands) {   /* not needed for this tile: an empty depth range for the readers' union */
         if (threadIdx.x == 0) A.zrange[(size_t)gtile * RASTER_BANDS + band] = make_float2(1e9f, -1e9f);
         return;
@@ -1175,13 +1176,13 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
     return e;
 }
 
-void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, cudaStream_t st, const sftg_tile_args& A) {
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, int bands, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
     const size_t sm = raster_smem(S, slab_rows);
     const uint32_t grid = tiles * RASTER_BANDS;
-    if (S == 1) k_raster<1><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
-    else if (S == 2) k_raster<2><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
-    else k_raster<4><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows);
+    if (S == 1) k_raster<1><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
+    else if (S == 2) k_raster<2><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
+    else k_raster<4><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
 }
 
 void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A) {
