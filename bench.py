@@ -906,8 +906,9 @@ _REF_AGREEMENT: dict = {}
 
 def reference_agreement(blob: bytes, samples: int, width: int, height: int, frame: int = 0) -> float:
     """Fraction of the pixels of the reference build's frame (ref_bench, one dumped render) within
-    4 LSB per channel of the oracle's frame, which equals the GPU's bit for bit.  A build that
-    renders something else (a broken SIMD path) must not be timed as the baseline."""
+    4 LSB per channel of the oracle's frame, which equals the GPU's bit for bit (0 when the mean
+    difference exceeds REF_MEAN_LSB_MAX).  A build that renders something else (a broken SIMD
+    path) must not be timed as the baseline."""
     import hashlib
     import tempfile
     from oracle_io import read_dump
@@ -934,11 +935,19 @@ def reference_agreement(blob: bytes, samples: int, width: int, height: int, fram
                     a = np.stack([(ref >> k) & 0xFF for k in (16, 8, 0)]).astype(np.int32)
                     b = np.stack([(ours >> k) & 0xFF for k in (16, 8, 0)]).astype(np.int32)
                     close = float((np.abs(a - b).max(axis=0) <= 4).mean())
+                    if np.abs(a - b).mean() > REF_MEAN_LSB_MAX:
+                        close = 0.0
         _REF_AGREEMENT[key] = close
     return _REF_AGREEMENT[key]
 
 
-REF_AGREEMENT_MIN = 0.98   # of pixels within 4 LSB: the reference build renders the same frame
+# The reference build renders the same frame: most pixels within 4 LSB per channel of the oracle's
+# and a small mean difference.  Its own platform differences stay below these: its NEON path
+# traces 4-wide proxy batches (other packet frustums, so some light visibility and shadows differ)
+# and groups pixels 2x2 for LOD and the shadow block rule (atrium 1080p 4x: 86.7 % within 4 LSB,
+# mean 3.2 LSB; skinned 1080p 2x: 99.0 %, 0.10).  A broken build (an empty frame) falls far below.
+REF_AGREEMENT_MIN = 0.80
+REF_MEAN_LSB_MAX = 8.0
 
 
 def _reference_desc(threads: int) -> str:
@@ -1127,7 +1136,7 @@ def run_reference(args, cfg) -> dict | None:
             for o in oracles:
                 o.close()
         why = ("absent on this host" if not agree else
-               f"renders frames that disagree with the oracle's ({min(agree):.4f} of pixels within 4 LSB)")
+               f"renders frames that disagree with the oracle's ({min(agree):.4f} of pixels within 4 LSB, or a large mean difference)")
         sample = (f"{len(times)} frames after {warm} warm-up, CPU restatement of the reference algorithm "
                   f"(oracle/sft_oracle.c), tile-parallel; the reference's own build is {why}")
     else:

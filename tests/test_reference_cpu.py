@@ -3,7 +3,8 @@
 AVX2 with GCC's default contraction on x86-64), renders the benchmark's scenes, and its frames
 agree with the oracle's (which equal the GPU's bit for bit): so the baseline does the same work.
 Its bits are not the parity target (other SIMD width, other reciprocal estimates, contracted
-multiply-adds), so the check is a tolerance: nearly every pixel within a few LSB per channel.
+multiply-adds), so the check is the tolerance bench.py applies before it times the build: most
+pixels within a few LSB per channel and a small mean difference.
 Skipped where that build is absent."""
 import os
 import subprocess
@@ -46,4 +47,6 @@ def test_reference_cpu_build_renders_the_bench_scene(gen, samples):
     d = np.abs(a - b).max(axis=0)
     close = float((d <= 4).mean())
     print(f"{gen}: {close:.5f} of pixels within 4 LSB, mean |d| {np.abs(a - b).mean():.4f}")
-    assert close > 0.98, f"{gen}: only {close:.4f} of pixels within 4 LSB of the oracle's frame"
+    import bench
+    assert close >= bench.REF_AGREEMENT_MIN, f"{gen}: only {close:.4f} of pixels within 4 LSB of the oracle's frame"
+    assert np.abs(a - b).mean() <= bench.REF_MEAN_LSB_MAX
