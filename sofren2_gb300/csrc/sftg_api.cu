@@ -646,7 +646,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     /* device arena layout */
     size_t need = stage_bytes + 4096;
     auto acc = [&](size_t bytes) { need = ((need + 255) & ~(size_t)255) + bytes; };
-    acc((size_t)total_ss * 2304); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
+    acc((size_t)total_ss * SFTG_SS_FLOATS * 4); acc(n_rec * sizeof(sftg_batch_rec)); acc(n_rec * 4); acc(n_rec * 4);
     acc((size_t)total_ss * 16 + 16); acc(ctx->clip_cap * sizeof(sftg_clip_tri)); acc(ctx->clip_cap * 16);
     acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc((size_t)total_tiles * 4); acc(1024); acc(total_tiles + 16);
     acc(ctx->tile_cap * 8);
@@ -676,7 +676,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     char* hs = (char*)ln.h_stage;
     char* ds = (char*)ln.arena;
     bump bp{ ds, stage_bytes, ln.arena_cap };
-    B.ss = bp.take<float>((size_t)total_ss * 576);
+    B.ss = bp.take<float>((size_t)total_ss * SFTG_SS_FLOATS);
     B.recs = bp.take<sftg_batch_rec>(n_rec);
     B.clip_cnt = bp.take<uint32_t>(n_rec);
     B.clip_base = bp.take<uint32_t>(n_rec);
@@ -1008,7 +1008,19 @@ static int finish_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds
         if (dbg->tile_counts) CK(cudaMemcpy(dbg->tile_counts, B.tile_count, (size_t)tiles * 4, cudaMemcpyDeviceToHost));
         if (dbg->tile_payload_total) *dbg->tile_payload_total = pay_total;
         if (dbg->tile_payloads && pay_total <= dbg->tile_payload_cap) CK(cudaMemcpy(dbg->tile_payloads, B.tile_pay, (size_t)pay_total * 8, cudaMemcpyDeviceToHost));
-        if (dbg->ss_cache) CK(cudaMemcpy(dbg->ss_cache, B.ss, (size_t)B.total_ss * 2304, cudaMemcpyDeviceToHost));
+        if (dbg->ss_cache) {   /* back to the reference's rows: sx sy inv_w wx wy wz wnx wny wnz, 64 each */
+            std::vector<float> all((size_t)B.total_ss * SFTG_SS_FLOATS + 1);
+            CK(cudaMemcpy(all.data(), B.ss, (size_t)B.total_ss * SFTG_SS_FLOATS * 4, cudaMemcpyDeviceToHost));
+            for (uint32_t k = 0; k < B.total_ss; k++) {
+                const float* rec = all.data() + (size_t)k * SFTG_SS_FLOATS;
+                float* r = dbg->ss_cache + (size_t)k * 576;
+                for (int v = 0; v < 64; v++) {
+                    for (int c = 0; c < 4; c++) r[c * 64 + v] = rec[SFTG_SS_A + v * 4 + c];
+                    for (int c = 0; c < 4; c++) r[(4 + c) * 64 + v] = rec[SFTG_SS_B + v * 4 + c];
+                    r[8 * 64 + v] = rec[SFTG_SS_C + v * 4];
+                }
+            }
+        }
         if (dbg->light_vis && fd->n_proxies) CK(cudaMemcpy(dbg->light_vis, B.light_vis, (size_t)fd->n_proxies * 64, cudaMemcpyDeviceToHost));
         if (dbg->clip_total) *dbg->clip_total = clip_total;
         if (dbg->clip_tris && clip_total <= dbg->clip_cap) CK(cudaMemcpy(dbg->clip_tris, B.clips, (size_t)clip_total * sizeof(sftg_clip_tri), cudaMemcpyDeviceToHost));

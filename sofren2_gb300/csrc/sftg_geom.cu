@@ -101,7 +101,7 @@ k_geometry(const sftg_frame* __restrict__ frames, const sftg_job* __restrict__ j
             continue;
         }
         const float* at = F->ml_attr + (size_t)g * 640;
-        float* S = ss + (size_t)ssi * 576;
+        float* S = ss + (size_t)ssi * SFTG_SS_FLOATS;
         const sftg_meshlet_info info = F->ml_info[g];
         /* ---- vertices: lane and lane + 32 (5015-5124) ---- */
 #pragma unroll
@@ -137,9 +137,11 @@ k_geometry(const sftg_frame* __restrict__ frames, const sftg_job* __restrict__ j
             const float tz = fma_(pw.x, VP[2], fma_(pw.y, VP[6], fma_(pw.z, VP[10], VP[14])));
             const float iw = rcpr(w);
             const float sx = fma_(tx, iw * hw, bias_x), sy = fma_(ty, iw * scale_y, bias_y);
-            S[v] = x86nan(sx); S[64 + v] = x86nan(sy); S[128 + v] = x86nan(iw);
-            S[192 + v] = pw.x; S[256 + v] = pw.y; S[320 + v] = pw.z;
-            S[384 + v] = nw.x; S[448 + v] = nw.y; S[512 + v] = nw.z;
+            /* vertex-major record (sftg_types.h, SFTG_SS_*): two float4 and one float per vertex */
+            ((float4*)(S + SFTG_SS_A))[v] = make_float4(x86nan(sx), x86nan(sy), x86nan(iw), pw.x);
+            ((float4*)(S + SFTG_SS_B))[v] = make_float4(pw.y, pw.z, nw.x, nw.y);
+            ((float4*)(S + SFTG_SS_C))[v] = make_float4(nw.z, at[384 + v], at[448 + v], at[512 + v]);
+            S[SFTG_SS_D + v] = at[576 + v];
             s_v[warp][0][v] = tx; s_v[warp][1][v] = ty; s_v[warp][2][v] = tz; s_v[warp][3][v] = w;
             s_v[warp][4][v] = sx; s_v[warp][5][v] = sy;
         }
@@ -246,7 +248,7 @@ __global__ void k_clip(const sftg_frame* __restrict__ frames, uint32_t n_views, 
         const sftg_inst* I = &F->inst[ii];
         const uint32_t m = lss - I->ss_offset, g = I->meshlet_base + m;
         const float* at = F->ml_attr + (size_t)g * 640;
-        const float* S = ss + (size_t)ssi * 576;
+        const float* S = ss + (size_t)ssi * SFTG_SS_FLOATS;
         const uint8_t* ind = F->ml_inds + (size_t)g * 512;
         const float* VP = F->vp;
         const float hw = F->hw, hh = F->hh;
@@ -258,14 +260,15 @@ __global__ void k_clip(const sftg_frame* __restrict__ frames, uint32_t n_views, 
         if ((int)(q[0] | q[1] | q[2]) > 0) {
             for (int k = 0; k < 3; k++) {
                 const uint32_t vv = q[k];
-                const float wx = S[192 + vv], wy = S[256 + vv], wz = S[320 + vv];
+                const float4 sa = ((const float4*)(S + SFTG_SS_A))[vv], sb = ((const float4*)(S + SFTG_SS_B))[vv];
+                const float wx = sa.w, wy = sb.x, wz = sb.y;
                 in[k].w = fma_(wx, VP[3], fma_(wy, VP[7], fma_(wz, VP[11], VP[15])));
                 in[k].tx = fma_(wx, VP[0], fma_(wy, VP[4], fma_(wz, VP[8], VP[12])));
                 in[k].ty = fma_(wx, VP[1], fma_(wy, VP[5], fma_(wz, VP[9], VP[13])));
                 in[k].tz = fma_(wx, VP[2], fma_(wy, VP[6], fma_(wz, VP[10], VP[14])));
                 in[k].u = at[384 + vv]; in[k].v = at[448 + vv]; in[k].lu = at[512 + vv]; in[k].lv = at[576 + vv];
                 in[k].px = wx; in[k].py = wy; in[k].pz = wz;
-                in[k].nx = S[384 + vv]; in[k].ny = S[448 + vv]; in[k].nz = S[512 + vv];
+                in[k].nx = sb.z; in[k].ny = sb.w; in[k].nz = S[SFTG_SS_C + 4 * vv];
             }
             const bool a = in[0].tz >= 0.f, bb = in[1].tz >= 0.f, c = in[2].tz >= 0.f;
             const bool ai = a && bb && c, ao = (in[0].tz < 0.f) && (in[1].tz < 0.f) && (in[2].tz < 0.f);

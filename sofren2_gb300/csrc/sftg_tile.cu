@@ -129,16 +129,18 @@ SFTG_D void fetch_tri(const sftg_frame* F, const float* ss, const sftg_clip_tri*
     const uint32_t g = I->meshlet_base + m;
     const uint8_t* ind = F->ml_inds + (size_t)g * 512;
     const float* at = F->ml_attr + (size_t)g * 640;
-    const float* Sc = ss + (size_t)(I->ss_offset + m) * 576;
+    const float* Sc = ss + (size_t)(I->ss_offset + m) * SFTG_SS_FLOATS;
     const uint32_t b = tri >> 3, l = tri & 7;
     const uint32_t q[3] = { ind[b * 32 + l], ind[b * 32 + 8 + l], ind[b * 32 + 16 + l] };
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const uint32_t v = q[k];
-        t.sx[k] = Sc[v]; t.sy[k] = Sc[64 + v]; t.iw[k] = Sc[128 + v];
-        t.u[k] = at[384 + v]; t.v[k] = at[448 + v]; t.lu[k] = at[512 + v]; t.lv[k] = at[576 + v];
-        t.px[k] = Sc[192 + v]; t.py[k] = Sc[256 + v]; t.pz[k] = Sc[320 + v];
-        t.nx[k] = Sc[384 + v]; t.ny[k] = Sc[448 + v]; t.nz[k] = Sc[512 + v];
+        const float4 a = ((const float4*)(Sc + SFTG_SS_A))[v], b4 = ((const float4*)(Sc + SFTG_SS_B))[v];
+        const float4 c4 = ((const float4*)(Sc + SFTG_SS_C))[v];
+        t.sx[k] = a.x; t.sy[k] = a.y; t.iw[k] = a.z;
+        t.u[k] = c4.y; t.v[k] = c4.z; t.lu[k] = c4.w; t.lv[k] = Sc[SFTG_SS_D + v];
+        t.px[k] = a.w; t.py[k] = b4.x; t.pz[k] = b4.y;
+        t.nx[k] = b4.z; t.ny[k] = b4.w; t.nz[k] = c4.x;
     }
     t.inst = ii; t.m = m;
 }
@@ -159,12 +161,13 @@ SFTG_D void pixel_pos_acc(const sftg_frame* F, const float* ss, const sftg_clip_
         const sftg_inst* I = &F->inst[ii];
         const uint32_t g = I->meshlet_base + m;
         const uint8_t* ind = F->ml_inds + (size_t)g * 512;
-        const float* Sc = ss + (size_t)(I->ss_offset + m) * 576;
+        const float* Sc = ss + (size_t)(I->ss_offset + m) * SFTG_SS_FLOATS;
         const uint32_t b = tri >> 3, l = tri & 7;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const uint32_t v = ind[b * 32 + 8 * k + l];
-            sx[k] = Sc[v]; sy[k] = Sc[64 + v]; iw[k] = Sc[128 + v]; px[k] = Sc[192 + v]; py[k] = Sc[256 + v]; pz[k] = Sc[320 + v];
+            const float4 a = ((const float4*)(Sc + SFTG_SS_A))[v], b4 = ((const float4*)(Sc + SFTG_SS_B))[v];
+            sx[k] = a.x; sy[k] = a.y; iw[k] = a.z; px[k] = a.w; py[k] = b4.x; pz[k] = b4.y;
         }
     }
     const float dx1 = sx[1] - sx[0], dx2 = sx[2] - sx[0], dy1 = sy[1] - sy[0], dy2 = sy[2] - sy[0];
@@ -359,7 +362,7 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
     const int band = (int)(blockIdx.x % RASTER_BANDS);
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
-    const float* ss = A.ss + (size_t)F->ss_base * 576;
+    const float* ss = A.ss + (size_t)F->ss_base * SFTG_SS_FLOATS;
     const sftg_clip_tri* clips = A.clips + (F->total_ss ? A.clip_base[(size_t)F->ss_base * 16] : 0u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
@@ -410,10 +413,10 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
                         const sftg_inst* I = &F->inst[ii];
                         const uint32_t g = I->meshlet_base + m;
                         const uint8_t* ind = F->ml_inds + (size_t)g * 512;
-                        const float* Sc = ss + (size_t)(I->ss_offset + m) * 576;
+                        const float* Sc = ss + (size_t)(I->ss_offset + m) * SFTG_SS_FLOATS;
                         const uint32_t q[3] = { ind[b * 32 + l], ind[b * 32 + 8 + l], ind[b * 32 + 16 + l] };
 #pragma unroll
-                        for (int k = 0; k < 3; k++) { sx[k] = Sc[q[k]]; sy[k] = Sc[64 + q[k]]; iw[k] = Sc[128 + q[k]]; }
+                        for (int k = 0; k < 3; k++) { const float4 a = ((const float4*)(Sc + SFTG_SS_A))[q[k]]; sx[k] = a.x; sy[k] = a.y; iw[k] = a.z; }
                     }
                 }
                 if (active) {
@@ -514,7 +517,7 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     const int nblk = TILE_BLOCKS / split;
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
-    const float* ss = A.ss + (size_t)F->ss_base * 576;
+    const float* ss = A.ss + (size_t)F->ss_base * SFTG_SS_FLOATS;
     const sftg_clip_tri* clips = A.clips + (F->total_ss ? A.clip_base[(size_t)F->ss_base * 16] : 0u);
     const uint8_t* light_vis = A.light_vis + (size_t)F->prox_base * 64;
     uint32_t* color = F->color_dev;

@@ -19,8 +19,13 @@
  * Per frame (one upload of a few KB, then a bump arena for scratch):
  *   sftg_frame        camera, frustum, display, lighting constants and array pointers
  *   sftg_inst         per instance: model, transform, screen-space cache offset, bones offset
- *   ss cache          f32[9][64] per drawn meshlet (sx sy inv_w wx wy wz wnx wny wnz),
- *                     the reference's sft_ss_meshlet (sofren2.c:1464-1477)
+ *   ss cache          SFTG_SS_FLOATS f32 per drawn meshlet: the values of the reference's
+ *                     sft_ss_meshlet (sofren2.c:1464-1477: sx sy inv_w wx wy wz wnx wny wnz per
+ *                     vertex) and the vertex's texture and lightmap coordinates, held vertex-
+ *                     major so that the resolve reads a vertex with three 16-byte loads and one
+ *                     word: float4[64] (sx, sy, inv_w, wx) at SFTG_SS_A, float4[64] (wy, wz,
+ *                     wnx, wny) at SFTG_SS_B, float4[64] (wnz, u, v, lu) at SFTG_SS_C, f32[64] lv
+ *                     at SFTG_SS_D; debug captures return the reference's [9][64] rows
  *   batch records     per (drawn meshlet, batch): u64 payload + tile rect + clip count
  *   tile lists        u64 payloads per tile, in the reference's single-worker order
  *   colour            u32 ARGB8888, pitch = width
@@ -36,6 +41,11 @@
 #define SFTG_MAX_LIGHT_PROXIES 16
 #define SFTG_MAX_INSTANCES 64
 #define SFTG_INVALID 0xFFFFFFFFu
+#define SFTG_SS_A 0                /* ss cache record: float offsets of its parts */
+#define SFTG_SS_B 256
+#define SFTG_SS_C 512
+#define SFTG_SS_D 768
+#define SFTG_SS_FLOATS 832         /* floats per record (3328 B) */
 
 typedef struct sftg_tex {
     int32_t w, h, levels, is_pot;

@@ -130,7 +130,7 @@ def request_device_bytes(width: int, height: int, samples: int, meshlets: int) -
     screen-space cache and batch records per meshlet, tile lists and clip pool at a generous
     estimate."""
     tiles = ((width + 63) // 64) * ((height + 63) // 64)
-    return tiles * samples * 4096 * 8 + width * height * 4 + meshlets * (2304 + 16 * 16 + 16 * 8 + 16) + tiles * 64 * 1024
+    return tiles * samples * 4096 * 8 + width * height * 4 + meshlets * (3328 + 16 * 16 + 16 * 8 + 16) + tiles * 64 * 1024
 
 
 class Renderer:
