@@ -478,9 +478,11 @@ def run_serve(args, cfg) -> dict:
                 "max_batch": int(st["max_batch"]), "max_batches_in_flight": int(st.get("max_inflight", 1)) or 1,
                 "peak_admitted_gb": st["peak_bytes"] / 2**30}
 
-    # warm-up: grow every device buffer to the largest batch the runs can form
+    # warm-up: grow every lane's buffers to the largest batch the runs can form (a lane growing
+    # while requests are timed stalls its batch), then run each mode over a short burst
     warm = make_requests(max(SERVE_RATES), 0.05, 1)
     warm = [(0.0,) + r[1:] for r in warm[:max_batch]]
+    R.serve_warm(hs, [r for rate in SERVE_RATES for r in make_requests(rate, 1.0, 7)], max_batch, SERVE_BUDGET, colors)
     for _ in range(args.warmup):
         R.serve(hs, warm, max_batch, SERVE_BUDGET, "overlap", colors)
         R.serve(hs, warm, max_batch, SERVE_BUDGET, "batched", colors)

@@ -201,6 +201,46 @@ SFTX_EXPORT int sftx_serve_ex(void* const* scenes, const sftx_request* reqs, uin
     return st.errors ? -2 : 0;
 }
 
+/* Grows every lane's buffers before a run, so that no lane first grows its frame arena, colour
+ * pool or pinned staging while requests are being timed.  The largest batch admission can form
+ * from reqs (the max_batch requests with the largest device estimates, taken in that order while
+ * they fit the budget) is rendered once on each of lanes 1..lanes, all queued before any is waited
+ * for, and once on lane 0 (SFTX_SERVE_BATCHED and SFTX_SERVE_PLAIN render there).  Its i-th view
+ * goes to colors[i % n_colors].  Returns 0, -1 for bad arguments, -2 when a render, submission or
+ * wait failed. */
+SFTX_EXPORT int sftx_serve_warm(void* const* scenes, const sftx_request* reqs, uint32_t n, uint32_t max_batch, uint64_t budget_bytes,
+                                uint32_t lanes, uint32_t* const* colors, uint32_t n_colors) {
+    if (!scenes || !reqs || !n || !colors || max_batch == 0 || n_colors < max_batch || max_batch > 4096) return -1;
+    if (lanes > SFTG_MAX_LANES - 1) return -1;
+    uint32_t pick[4096];
+    uint32_t np = 0;
+    for (uint32_t k = 0; k < n; k++) {   /* the max_batch largest estimates, largest first (earliest on ties) */
+        if (np == max_batch && reqs[k].device_bytes <= reqs[pick[np - 1]].device_bytes) continue;
+        uint32_t j = np < max_batch ? np++ : np - 1;
+        while (j > 0 && reqs[pick[j - 1]].device_bytes < reqs[k].device_bytes) { pick[j] = pick[j - 1]; j--; }
+        pick[j] = k;
+    }
+    uint32_t take = 0;
+    uint64_t bytes = 0;
+    while (take < np && (take == 0 || bytes + reqs[pick[take]].device_bytes <= budget_bytes)) bytes += reqs[pick[take++]].device_bytes;
+    int errors = 0;
+    for (uint32_t l = 0; l <= lanes; l++) {
+        const uint32_t lane = l < lanes ? l + 1 : 0;   /* the submission lanes first, lane 0 last */
+        sft_batch_begin();
+        for (uint32_t i = 0; i < take; i++) {
+            const sftx_request* r = &reqs[pick[i]];
+            sft_set_msaa_samples(r->samples);
+            if (sftx_scene_render_ex(scenes[r->scene], r->frame, colors[i % n_colors], 0, r->max_point_lights)) errors++;
+        }
+        if (lane) { if (sft_batch_submit_async(lane)) errors++; }
+        else {
+            for (uint32_t q = 1; q <= lanes; q++) if (sft_batch_wait(q)) errors++;
+            if (sft_batch_submit()) errors++;
+        }
+    }
+    return errors ? -2 : 0;
+}
+
 SFTX_EXPORT int sftx_serve(void* const* scenes, const sftx_request* reqs, uint32_t n, uint32_t max_batch, uint64_t budget_bytes,
                            int mode, uint32_t* const* colors, uint32_t n_colors, uint64_t* done_ns, uint32_t* batch_of,
                            sftx_serve_stats* stats) {

@@ -77,6 +77,12 @@ struct sftg_ctx {
     cudaStream_t stream = nullptr;             /* lane 0's stream: uploads and the synchronous calls */
     cudaEvent_t ev_upload = nullptr;           /* orders other lanes after the uploads queued before them */
     sftg_lane lanes[SFTG_MAX_LANES];
+    /* the lanes' frame arenas and colour buffers: stream-ordered allocations from this pool, so
+     * that a lane outgrowing its buffers frees and allocates on its own stream without
+     * synchronising the device (cudaFree would wait for every lane's batch in flight); freed
+     * blocks stay reserved in the pool for the next growth */
+    cudaMemPool_t lane_pool = nullptr;
+    std::vector<void*> retired_stage;          /* outgrown pinned staging: freed at sftg_destroy (cudaFreeHost synchronises) */
     char err[512] = { 0 };
     /* resident */
     dpool texels, texs, mats, ml_attr, ml_inds, ml_cull, ml_info, skin_j, skin_w, blas, models;
@@ -194,6 +200,16 @@ extern "C" int sftg_create(int device, sftg_ctx** out) {
     }
     ctx->stream = ctx->lanes[0].stream;
     cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming);
+    {
+        cudaMemPoolProps pp;
+        memset(&pp, 0, sizeof(pp));
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = device;
+        if (cudaMemPoolCreate(&ctx->lane_pool, &pp) != cudaSuccess) { ctx->lane_pool = nullptr; sftg_destroy(ctx); return SFTG_E_CUDA; }
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(ctx->lane_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     sftg_tile_configure(227 * 1024);
     if (noalloc_scratch_setup(device) != cudaSuccess) { sftg_destroy(ctx); return SFTG_E_CUDA; }
     { const char* e = getenv("SFTG_NO_GRAPHS"); if (e && *e && *e != '0') ctx->use_graphs = false; }
@@ -213,6 +229,7 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
         sftg_lane& ln = ctx->lanes[l];
         if (ln.arena) cudaFree(ln.arena);
         if (ln.d_color) cudaFree(ln.d_color);
+        ln.arena = nullptr; ln.d_color = nullptr;
         if (ln.h_stage) cudaFreeHost(ln.h_stage);
         if (ln.h_status) cudaFreeHost(ln.h_status);
         for (int i = 0; i < 6; i++) if (ln.ev[i]) cudaEventDestroy(ln.ev[i]);
@@ -230,6 +247,8 @@ extern "C" void sftg_destroy(sftg_ctx* ctx) {
         if (ln.stream) cudaStreamDestroy(ln.stream);
     }
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
+    for (void* p : ctx->retired_stage) cudaFreeHost(p);
+    if (ctx->lane_pool) cudaMemPoolDestroy(ctx->lane_pool);
     for (int k = 0; k < 2; k++) if (ctx->ev_blas[k]) cudaEventDestroy(ctx->ev_blas[k]);
     delete ctx;
 }
@@ -656,20 +675,29 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
     const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
     if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
+    /* growth: the lane's previous batch has finished (a lane takes a batch only once the last
+     * one was collected), so its buffers are free; other lanes keep running meanwhile */
     if (need > ln.arena_cap) {
-        if (ln.arena) { cudaStreamSynchronize(ln.stream); cudaFree(ln.arena); ln.arena = nullptr; }
+        if (ln.arena) { CK(cudaFreeAsync(ln.arena, ln.stream)); ln.arena = nullptr; }
         size_t nc = need + need / 4;
-        if (cudaMalloc(&ln.arena, nc) != cudaSuccess) { ln.arena_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "frame arena of %zu bytes", nc); }
+        if (cudaMallocFromPoolAsync(&ln.arena, nc, ctx->lane_pool, ln.stream) != cudaSuccess) {
+            ln.arena = nullptr; ln.arena_cap = 0; cudaGetLastError();
+            return set_err(ctx, SFTG_E_NOMEM, "frame arena of %zu bytes", nc);
+        }
         ln.arena_cap = nc;
     }
     if (color_total * 4 > ln.d_color_cap) {
-        if (ln.d_color) { cudaStreamSynchronize(ln.stream); cudaFree(ln.d_color); }
-        if (cudaMalloc((void**)&ln.d_color, color_total * 4) != cudaSuccess) { ln.d_color = nullptr; ln.d_color_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "colour buffers"); }
-        ln.d_color_cap = color_total * 4;
+        if (ln.d_color) { CK(cudaFreeAsync(ln.d_color, ln.stream)); ln.d_color = nullptr; }
+        const size_t nc = color_total * 4 + color_total;
+        if (cudaMallocFromPoolAsync((void**)&ln.d_color, nc, ctx->lane_pool, ln.stream) != cudaSuccess) {
+            ln.d_color = nullptr; ln.d_color_cap = 0; cudaGetLastError();
+            return set_err(ctx, SFTG_E_NOMEM, "colour buffers");
+        }
+        ln.d_color_cap = nc;
     }
     if (stage_bytes > ln.h_stage_cap) {
-        if (ln.h_stage) { cudaStreamSynchronize(ln.stream); cudaFreeHost(ln.h_stage); }
-        size_t nc = stage_bytes + stage_bytes / 4 + 4096;
+        if (ln.h_stage) ctx->retired_stage.push_back(ln.h_stage);
+        size_t nc = 2 * stage_bytes + 4096;
         if (cudaMallocHost(&ln.h_stage, nc) != cudaSuccess) { ln.h_stage = nullptr; ln.h_stage_cap = 0; return set_err(ctx, SFTG_E_NOMEM, "pinned staging"); }
         ln.h_stage_cap = nc;
     }

@@ -52,6 +52,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "sftx_scene_render_ex": (i32, [p, u32, p, i32, u32]),
         "sftx_serve": (i32, [p, p, u32, u32, u64, i32, p, u32, p, p, p]),
         "sftx_serve_ex": (i32, [p, p, u32, u32, u64, i32, u32, p, u32, p, p, p]),
+        "sftx_serve_warm": (i32, [p, p, u32, u32, u64, u32, p, u32]),
         "sft_get_gpu_context": (p, []), "sftg_get_tuning": (i32, [p, p]), "sftg_set_tuning": (i32, [p, p]),
         "sftg_skeleton_upload": (i32, [p, p, u32, p, u32, p]), "sftg_pose_eval": (i32, [p, p, u32, p, p]),
         "sftg_last_error": (C.c_char_p, [p]), "sftx_scene_model": (p, [p, u32]),
@@ -301,6 +302,22 @@ class Renderer:
             raise RuntimeError(f"serving loop failed ({rc}): " + (self.lib.sft_get_last_error() or b"").decode())
         stats = {"batches": st.batches, "max_batch": st.max_batch, "peak_bytes": st.peak_bytes, "max_inflight": st.max_inflight}
         return done[:n].astype(np.float64) * 1e-9, batch[:n].copy(), stats
+
+    def serve_warm(self, handles: list, requests: list[tuple], max_batch: int, budget_bytes: int,
+                   colors: list[np.ndarray], lanes: int = 7) -> None:
+        """Grows every submission lane (1..lanes, and lane 0) to the largest batch admission can
+        form from requests (sftx_serve_warm), so that a serving run that follows allocates
+        nothing while it is timed.  Same request tuples and colour ring as serve."""
+        n = len(requests)
+        reqs = (SftxRequest * max(1, n))()
+        for k, (t, si, f, S, nl, nb) in enumerate(requests):
+            reqs[k] = SftxRequest(int(t * 1e9), int(nb), si, f, S, nl)
+        hs = (C.c_void_p * len(handles))(*handles)
+        cp = (C.c_void_p * len(colors))(*[c.ctypes.data for c in colors])
+        rc = self.lib.sftx_serve_warm(hs, reqs, n, max_batch, budget_bytes, lanes, cp, len(colors))
+        self.lib.sft_set_msaa_samples(self.samples)
+        if rc != 0:
+            raise RuntimeError(f"serving warm-up failed ({rc}): " + (self.lib.sft_get_last_error() or b"").decode())
 
     def skeleton_upload(self, rig: dict) -> int:
         """Uploads a rig (scenes.pose_rig layout) with sftg_skeleton_upload; returns its index."""

@@ -65,6 +65,22 @@ def test_served_equals_alone(renderer, served, mode):
         assert 1 <= st["max_inflight"] <= 7
 
 
+def test_warm_then_serve(renderer, served):
+    """The warm-up renders the largest batch on every lane (the requests with the largest device
+    estimates, largest first, into the ring's first slots), then a served run over the grown lanes
+    still gives every request its lone pixels."""
+    hs, reqs, sizes, alone = served
+    colors = _ring(sizes, len(reqs))
+    renderer.serve_warm(hs, reqs, max_batch=5, budget_bytes=1 << 40, colors=colors, lanes=7)
+    order = sorted(range(len(reqs)), key=lambda k: (-reqs[k][5], k))[:5]
+    for slot, k in enumerate(order):
+        w, h = sizes[k]
+        assert np.array_equal(colors[slot][: w * h].reshape(h, w), alone[k]), f"warm-up slot {slot} (request {k})"
+    colors = _ring(sizes, len(reqs))
+    renderer.serve(hs, reqs, max_batch=8, budget_bytes=1 << 40, mode="overlap", colors=colors)
+    _check(colors, sizes, alone)
+
+
 def test_overlap_with_a_small_colour_ring(renderer, served):
     """8 colour buffers for 24 requests: a ring slot is handed out again only after its request
     has finished, so the last 8 requests' slots hold their lone pixels."""

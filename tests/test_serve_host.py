@@ -3,7 +3,8 @@ against fakes of the library calls it makes (tests/serve_fake.c): admission with
 and the device-memory budget (counted over every batch in flight), a request larger than the
 budget served alone, no more than `lanes` batches in flight and never two on one lane, failed
 renders, submissions and waits counted without stopping the loop, arrivals honoured, and the
-argument checks.  No GPU is involved."""
+argument checks; and the warm-up that grows every lane with the largest admissible batch before a
+run.  No GPU is involved."""
 import ctypes as C
 import os
 import shutil
@@ -32,6 +33,8 @@ def lib(tmp_path_factory):
     p, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
     L.sftx_serve_ex.restype = C.c_int
     L.sftx_serve_ex.argtypes = [p, p, u32, u32, u64, C.c_int, u32, p, u32, p, p, p]
+    L.sftx_serve_warm.restype = C.c_int
+    L.sftx_serve_warm.argtypes = [p, p, u32, u32, u64, u32, p, u32]
     L.fk_reset.argtypes = [u32, u32, u32, u32]
     L.fk_stats.argtypes = [p]
     L.fk_batch_size.restype, L.fk_batch_size.argtypes = u32, [u32]
@@ -129,3 +132,42 @@ def test_argument_checks(lib):
     assert serve(lib, r, max_batch=4, budget=100, mode=OVERLAP, lanes=0)[0] == -1
     assert serve(lib, r, max_batch=4, budget=100, mode=OVERLAP, lanes=8)[0] == -1
     assert serve(lib, r, max_batch=4, budget=100, mode=7)[0] == -1
+
+
+def warm(L, reqs, max_batch, budget, lanes, n_colors=None, fail=(NONE, NONE, NONE)):
+    n_colors = n_colors or max_batch
+    bufs = [np.zeros(4, np.uint32) for _ in range(n_colors)]
+    colors = (C.c_void_p * n_colors)(*[b.ctypes.data for b in bufs])
+    scenes = (C.c_void_p * 4)(*[C.c_void_p(0x1000 * (k + 1)) for k in range(4)])
+    r = np.ascontiguousarray(reqs, REQ)
+    L.fk_reset(3, *fail)
+    rc = L.sftx_serve_warm(scenes, r.ctypes.data, len(r), max_batch, budget, lanes, colors, n_colors)
+    fk = np.zeros(6, np.uint32)
+    L.fk_stats(fk.ctypes.data)
+    stats = dict(zip(("renders", "submits", "waits", "busy_submit", "max_busy", "nbatches"), map(int, fk)))
+    return rc, stats, [L.fk_batch_size(i) for i in range(stats["nbatches"])], [int(b[0]) for b in bufs]
+
+
+def test_warm_renders_the_largest_batch_on_every_lane(lib):
+    r = requests(50)
+    r["device_bytes"][[7, 20, 33, 41, 45]] = [50, 40, 40, 30, 30]   # ties go to the earlier request
+    rc, fk, sizes, firsts = warm(lib, r, max_batch=4, budget=1 << 30, lanes=3, n_colors=6)
+    assert rc == 0
+    assert sizes == [4, 4, 4, 4]                       # lanes 1-3, then lane 0
+    assert fk["max_busy"] == 3 and fk["busy_submit"] == 0 and fk["waits"] == 3
+    assert firsts[:4] == [8, 21, 34, 42]               # frame + 1 of requests 7, 20, 33, 41, largest first
+    # within the budget, largest first; a request over the budget on its own still warms alone
+    assert warm(lib, r, max_batch=4, budget=100, lanes=2)[2] == [2, 2, 2]
+    assert warm(lib, r, max_batch=4, budget=10, lanes=1)[2] == [1, 1]
+    # lane 0 only
+    rc, fk, sizes, _ = warm(lib, r, max_batch=8, budget=1 << 30, lanes=0)
+    assert rc == 0 and sizes == [8] and fk["waits"] == 0
+
+
+def test_warm_failures_and_argument_checks(lib):
+    r = requests(10)
+    assert warm(lib, r, max_batch=4, budget=1 << 30, lanes=2, fail=(5, NONE, NONE))[0] == -2
+    assert warm(lib, r, max_batch=4, budget=1 << 30, lanes=2, fail=(NONE, NONE, 1))[0] == -2
+    assert warm(lib, r, max_batch=4, budget=1 << 30, lanes=2, n_colors=3)[0] == -1
+    assert warm(lib, r, max_batch=4, budget=1 << 30, lanes=8)[0] == -1
+    assert warm(lib, r[:0], max_batch=4, budget=1 << 30, lanes=2)[0] == -1
