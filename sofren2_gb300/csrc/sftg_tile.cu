@@ -507,6 +507,10 @@ __global__ void __launch_bounds__(TILE_THREADS, S == 1 ? 3 : 4)   /* 64 register
 k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
+    /* the per-lane "between" test's operands of each cached proxy, in pcache's order: W (proxy
+     * centre minus light) with |W|^2 as one 16-byte load, and the squared bounding radius */
+    __shared__ float4 s_btw[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
+    __shared__ float s_rb2[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
     __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
     __shared__ sftg_point_light s_pl[SFTG_MAX_TILE_LIGHTS];   /* the tile's lights, in list order */
     __shared__ int s_nlights;
@@ -641,6 +645,8 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                     q->ab[0] = ab.x; q->ab[1] = ab.y; q->ab[2] = ab.z;
                     q->W[0] = Wv.x; q->W[1] = Wv.y; q->W[2] = Wv.z;
                     q->abdab = sdot(ab, ab); q->wdw = d2; q->rb2 = br * br; q->pr = px.radius; q->pr2 = px.radius * px.radius;
+                    s_btw[i * SFTG_MAX_LIGHT_PROXIES + n + rank] = make_float4(Wv.x, Wv.y, Wv.z, d2);
+                    s_rb2[i * SFTG_MAX_LIGHT_PROXIES + n + rank] = q->rb2;
                     q->vis_mult = (float)vs * 0.3333333f;
                 }
                 n = min(SFTG_MAX_LIGHT_PROXIES, n + __popc(bal));
@@ -689,7 +695,12 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
             }
             const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
             __syncwarp();
-            if (keep) pcache[i * SFTG_MAX_LIGHT_PROXIES + __popc(bal & ((1u << lane) - 1u))] = q;
+            if (keep) {
+                const int k = i * SFTG_MAX_LIGHT_PROXIES + __popc(bal & ((1u << lane) - 1u));
+                pcache[k] = q;
+                s_btw[k] = make_float4(q.W[0], q.W[1], q.W[2], q.wdw);
+                s_rb2[k] = q.rb2;
+            }
             if (lane == 0) s_npc[i] = (uint8_t)__popc(bal);
         }
         __syncthreads();
@@ -896,17 +907,23 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
                      * then the block-level skip as the OR over the block's lanes */
                     const int np = s_npc[i];
                     uint32_t rmask = 0, bmask = 0;
-                    if (np > 0) {
+                    const bool want = lm ? in_tri : lit;
+                    /* a lane's bit needs `want`: with no lane of the block wanting, every mask is 0 */
+                    if (np > 0 && (__ballot_sync(gmask, want) & gmask)) {
                         const float rd2 = rcpr(d2);   /* loop-invariant: the reference recomputes the same value per proxy */
-                        const bool want = lm ? in_tri : lit;
+                        const float nd2 = -d2;
+                        /* The reference's test with wdv = 0 - dot(W, Lr): wdv > 0 && wdv < d2, then
+                         * cd2 = fma(-wdv, wdv * rd2, |W|^2) < rb2.  With v = dot(W, Lr): wdv > 0 is
+                         * v < 0 (both false for a zero or NaN v), wdv < d2 is v > -d2, and for such
+                         * v, wdv = -v exactly, wdv * rd2 = -(v * rd2) (round to nearest is
+                         * symmetric) and cd2 = fma(-v, v * rd2, |W|^2): the same bits. */
 #pragma unroll 4
                         for (int pi = 0; pi < np; pi++) {
-                            const proxy_cache& q = pcache[i * SFTG_MAX_LIGHT_PROXIES + pi];
-                            const float wdv = 0.f - vdot(mk3(q.W[0], q.W[1], q.W[2]), Lr);
-                            const bool btw = wdv > 0.f && wdv < d2;
-                            const float tf = wdv * rd2;
-                            const float cd2 = fma_(-wdv, tf, q.wdw);
-                            rmask |= (uint32_t)(btw && (cd2 < q.rb2) && want) << pi;
+                            const float4 bt = s_btw[i * SFTG_MAX_LIGHT_PROXIES + pi];
+                            const float v = vdot(mk3(bt.x, bt.y, bt.z), Lr);
+                            const bool btw = v < 0.f && v > nd2;
+                            const float cd2 = fma_(-v, v * rd2, bt.w);
+                            rmask |= (uint32_t)(btw && (cd2 < s_rb2[i * SFTG_MAX_LIGHT_PROXIES + pi]) && want) << pi;
                         }
                         bmask = rmask;
                         bmask |= __shfl_xor_sync(gmask, bmask, 1);
