@@ -181,11 +181,16 @@ typedef struct sftg_tuning {
     int32_t raster_bands[3];      /* raster CTAs per 64x64 tile at 1x, 2x, 4x, each a band of its rows: 0 = by the
                                      tile's payload count (default: 1, 2 above 48 payloads, 4 above 128; at 4x 2),
                                      1, 2 or 4 = every tile (at 4x at least 2) */
+    int32_t tile_lights[3];       /* where a tile's light list and proxy selection are made at 1x, 2x, 4x: 1 = by each of
+                                     its resolve CTAs, 2 = once per tile by a launch before the resolve (its CTAs read
+                                     the result), 0 = 2 where the range has 16 CTAs per tile and at least 256 tiles,
+                                     else 1 (default) */
 } sftg_tuning;
 int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out);
 int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* tuning);
 /* Times the given views with each candidate setting (median of reps renders per candidate,
- * coordinate search: job width, then per sample count slab rows, raster bands and resolve split), keeps the
+ * coordinate search: job width, then per sample count slab rows, raster bands, resolve split and
+ * where the tile light lists are made), keeps the
  * fastest in the context and copies it to *out (optional). */
 int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, int32_t reps, sftg_tuning* out);
 

@@ -109,7 +109,7 @@ struct sftg_ctx {
     uint32_t blas_items = 0, blas_launches = 0; /* and its triangles and kernels */
     cudaEvent_t ev_blas[2] = { nullptr, nullptr };
     bool use_graphs = true;
-    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0, { 0, 0, 0 } };   /* measured best on the single-view workloads */
+    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0, { 0, 0, 0 }, { 0, 0, 0 } };   /* measured best on the single-view workloads */
     /* transient models (one frame's dynamic meshes): pool marks where they start */
     bool tr_live = false, tr_pinned = false;
     uint32_t tr_meshlets = 0, tr_skin = 0, tr_blas = 0;
@@ -487,6 +487,7 @@ struct batch_bufs {
     uint32_t* tile_count; uint32_t* tile_start;
     uint32_t* tile_order; uint32_t* order_scratch;
     uint8_t* tile_nlights;   /* per tile: its light list length (debug views) */
+    sftg_tile_lights* tile_lights;   /* per tile: lights and selected proxies, shared by its resolve CTAs */
     bool any_overlay;        /* a view asks for a tile overlay (debug modes 2-4) */
     uint64_t* tile_pay;
     uint8_t* light_vis;
@@ -672,7 +673,8 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     acc((size_t)total_stiles * 4); acc((size_t)total_stiles * 4); acc(ctx->stile_cap * 4);
     acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
     acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles + total_stiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
-    acc(vis_total * 8); acc((size_t)total_tiles * 8 + 8);
+    acc(vis_total * 8); acc((size_t)(total_tiles + 1) * sftg_raster_bands() * sizeof(float2));
+    acc((size_t)total_tiles * sizeof(sftg_tile_lights));
     const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
     if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
     /* growth: the lane's previous batch has finished (a lane takes a batch only once the last
@@ -731,12 +733,15 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     B.totals = bp.take<uint32_t>(16);
     B.vis = bp.take<float2>(vis_total);
     B.zrange = bp.take<float2>((size_t)(total_tiles + 1) * sftg_raster_bands());   /* per raster band of each tile */
+    B.tile_lights = bp.take<sftg_tile_lights>(total_tiles);
     B.vis_depth = nullptr; B.vis_id = nullptr; B.shadow = nullptr;
     if (want_debug) {
         B.vis_depth = bp.take<float>((size_t)total_tiles * S0 * 4096);
         B.vis_id = bp.take<uint32_t>((size_t)total_tiles * S0 * 4096);
         B.shadow = bp.take<float>((size_t)W0 * H0 * 16);
     }
+    if (bp.off > ln.arena_cap)   /* the sizing above and these takes disagree: refuse rather than overrun */
+        return set_err(ctx, SFTG_E_NOMEM, "frame arena layout of %zu bytes exceeds its %zu-byte sizing", bp.off, ln.arena_cap);
     /* fill the staging block */
     uint16_t* tv = (uint16_t*)(hs + o_tv);
     uint16_t* pv = (uint16_t*)(hs + o_pv);
@@ -878,7 +883,7 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     if (B.shadow) CK(cudaMemsetAsync(B.shadow, 0, B.color_total * 16 * 4, st));
     sftg_tile_args A;
     A.frames = B.frames; A.tile_view = B.tile_view; A.ss = B.ss; A.clips = B.clips; A.clip_base = B.clip_base;
-    A.tile_order = B.tile_order; A.tile_nlights = B.tile_nlights;
+    A.tile_order = B.tile_order; A.tile_nlights = B.tile_nlights; A.tile_lights = B.tile_lights;
     A.tile_start = B.tile_start; A.tile_count = B.tile_count; A.tile_pay = B.tile_pay; A.light_vis = B.light_vis;
     A.vis = B.vis; A.zrange = B.zrange; A.vis_depth = B.vis_depth; A.vis_id = B.vis_id; A.shadow_out = B.shadow;
     /* With views of several sample counts, the 4x tile range runs on the main stream and the 1x
@@ -902,7 +907,18 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
     CK(cudaGetLastError());
     CK(record_event(ln.ev[4], st));
     if (occl) CK(cudaStreamWaitEvent(st, ln.ev_join, 0));
-    prc = per_range(1, [&](int si, cudaStream_t s) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], s, A); });
+    /* per sample count: the tiles' light lists and proxy selections made once per tile (one more
+     * launch on the critical path) or by every resolve CTA of the tile (split-fold work) */
+    bool records[3];
+    for (int si = 0; si < 3; si++) {
+        const int m = ctx->tuning.tile_lights[si];
+        records[si] = m == 2 || (m == 0 && ctx->tuning.resolve_split[si] >= 16 && B.s_tiles[si] >= 256);
+        if (records[si] && B.s_tiles[si]) {   /* on st: every range's resolve waits for it (per_range forks after it) */
+            sftg_launch_tile_lights(B.s_tile0[si], B.s_tiles[si], st, A);
+            ln.launches++;
+        }
+    }
+    prc = per_range(1, [&](int si, cudaStream_t s) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], records[si], s, A); });
     if (prc) return prc;
     if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ln.launches++; }
     CK(cudaGetLastError());
@@ -922,7 +938,7 @@ static uint64_t batch_key(const sftg_ctx* ctx, const batch_bufs& B) {
     const uint32_t ov = B.any_overlay ? 1u : 0u;
     h = fnv(h, &ov, sizeof(ov));
     const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.stile_view, B.stile_count, B.stile_start,
-                           B.stile_list, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights,
+                           B.stile_list, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights, B.tile_lights,
                            B.mrect, B.clips, B.clip_rect, B.tile_count, B.tile_start, B.tile_order, B.order_scratch, B.tile_pay,
                            B.light_vis, B.packets, B.pairs, B.n_pairs, B.scan_tmp, B.status, B.totals, B.vis, B.zrange,
                            B.vis_depth, B.vis_id, B.shadow };
@@ -1364,6 +1380,7 @@ static bool tuning_valid(const sftg_tuning* t) {
         if (sl < 4 || sl > 64) return false;
         const int rb = t->raster_bands[k];
         if (!(rb == 0 || rb == 1 || rb == 2 || rb == 4)) return false;
+        if (t->tile_lights[k] < 0 || t->tile_lights[k] > 2) return false;
     }
     return t->geom_job_width >= 1 && t->geom_job_width <= 8 && (t->occl_ray_prune == 0 || t->occl_ray_prune == 1);
 }
@@ -1376,7 +1393,7 @@ extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
 
 extern "C" int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* t) {
     if (!ctx || !t) return SFTG_E_ARG;
-    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8, raster bands 0/1/2/4)");
+    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8, raster bands 0/1/2/4, tile lights 0/1/2)");
     ctx->tuning = *t;
     return SFTG_OK;
 }
@@ -1441,6 +1458,13 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
             float t;
             if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
             if (t < bt) { bt = t; best.resolve_split[si] = splits[k]; }
+        }
+        bt = 1e30f;
+        for (int k = 1; k <= 2; k++) {
+            ctx->tuning = best; ctx->tuning.tile_lights[si] = k;
+            float t;
+            if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
+            if (t < bt) { bt = t; best.tile_lights[si] = k; }
         }
     }
     ctx->tuning = best;

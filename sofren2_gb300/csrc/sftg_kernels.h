@@ -19,6 +19,18 @@ struct sftg_clip_tri {
 /* Arguments of the tile kernels.  Tiles are numbered batch-wide: tile_view maps a tile to its
  * view's frame block, whose tile_base, ss_base, prox_base and vis_base locate the view's rows in
  * the shared arrays. */
+/* A tile's lights and proxy selection, computed once per tile by k_tile_lights for all of the
+ * tile's resolve CTAs: the first SFTG_MAX_TILE_LIGHTS point lights in index order that reach the
+ * tile's depth range and rectangle (sofren2.c:5855-5934), and per light the first
+ * SFTG_MAX_LIGHT_PROXIES proxies in index order that see the light and can reach it (5936-5990). */
+struct sftg_tile_lights {
+    uint32_t proxy[SFTG_MAX_TILE_LIGHTS][SFTG_MAX_LIGHT_PROXIES];
+    uint16_t light[SFTG_MAX_TILE_LIGHTS];
+    uint8_t npc[SFTG_MAX_TILE_LIGHTS];
+    uint32_t nlights;
+    uint32_t pad[3];
+};
+
 struct sftg_tile_args {
     const sftg_frame* frames;
     const uint16_t* tile_view;
@@ -26,7 +38,9 @@ struct sftg_tile_args {
     const sftg_clip_tri* clips;
     const uint32_t* clip_base;     /* exclusive scan of clip counts: a view's first slot is clip_base[ss_base * 16] */
     const uint32_t* tile_order;    /* launch order of the tiles (heaviest first within each sample count) */
-    uint8_t* tile_nlights;         /* per tile: light list length, written by the resolve for the debug overlays */
+    uint8_t* tile_nlights;         /* per tile: light list length, for the debug overlays (k_tile_lights or the resolve) */
+    sftg_tile_lights* tile_lights; /* per tile, written by k_tile_lights, read by every resolve CTA of the tile
+                                      where the range's resolve is launched with records */
     const uint32_t* tile_start;
     const uint32_t* tile_count;
     const uint64_t* tile_pay;
@@ -72,7 +86,8 @@ int sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, 
                             uint32_t* scratch, uint32_t* order, cudaStream_t st);
 /* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4, 8 or 16) */
 void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, int bands, cudaStream_t st, const sftg_tile_args& A);
-void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A);
+void sftg_launch_tile_lights(uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, bool records, cudaStream_t st, const sftg_tile_args& A);
 /* tile overlays of the debug views 2-4 (sft__debug_draw_tile_overlay), after every resolve */
 void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
 

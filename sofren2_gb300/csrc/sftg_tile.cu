@@ -491,6 +491,105 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
 }
 
 /* ---------------------------------------------------------------- resolve */
+/* D2 (5855-5934), one warp: the first SFTG_MAX_TILE_LIGHTS point lights in index order whose
+ * depth range meets the tile's [zmin, zmax] and whose screen rectangle meets the tile.  Their
+ * indices go to out[]; returns their count on every lane. */
+SFTG_D int tile_light_list(const sftg_frame* F, float zmin, float zmax, int tmx, int tmy, int lane, uint16_t* out)
+{
+    int n = 0;
+    if (zmin <= zmax && F->n_point > 0) {
+        const float* vp = F->vp;
+        for (uint32_t base = 0; base < F->n_point && n < SFTG_MAX_TILE_LIGHTS; base += 32) {
+            const uint32_t l = base + lane;
+            bool pass = false;
+            if (l < F->n_point) {
+                const sftg_point_light L = F->point[l];
+                const float w = L.pos[0] * vp[3] + L.pos[1] * vp[7] + L.pos[2] * vp[11] + vp[15];
+                const float lmin = w - L.radius, lmax = w + L.radius;
+                pass = !(lmax <= 1e-6f);
+                if (pass) {
+                    const float smin = (lmin > 1e-6f) ? lmin : 1e-6f;
+                    const float iwmin = fdiv(1.f, lmax), iwmax = fdiv(1.f, smin);
+                    if (iwmax < zmin || iwmin > zmax) pass = false;
+                }
+                if (pass && w > L.radius) {
+                    const float tx = L.pos[0] * vp[0] + L.pos[1] * vp[4] + L.pos[2] * vp[8] + vp[12];
+                    const float ty = L.pos[0] * vp[1] + L.pos[1] * vp[5] + L.pos[2] * vp[9] + vp[13];
+                    const float sx = (fdiv(tx, w) + 1.f) * F->hw + F->vpx;
+                    const float sy = (fdiv(-ty, w) + 1.f) * F->hh + F->vpy;
+                    const float psx = fsqrt(vp[0] * vp[0] + vp[4] * vp[4] + vp[8] * vp[8]);
+                    const float psy = fsqrt(vp[1] * vp[1] + vp[5] * vp[5] + vp[9] * vp[9]);
+                    const float safe_w = (w - L.radius) > 1e-6f ? (w - L.radius) : 1e-6f;
+                    const float rx = fdiv((L.radius * psx) + fabsf(tx) * fdiv(L.radius, w), safe_w) * F->hw;
+                    const float ry = fdiv((L.radius * psy) + fabsf(ty) * fdiv(L.radius, w), safe_w) * F->hh;
+                    if (sx + rx < (float)tmx || sx - rx > (float)(tmx + SFTG_TILE) || sy + ry < (float)tmy || sy - ry > (float)(tmy + SFTG_TILE)) pass = false;
+                }
+            }
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
+            const int rank = __popc(bal & ((1u << lane) - 1u));
+            if (pass && n + rank < SFTG_MAX_TILE_LIGHTS) out[n + rank] = (uint16_t)l;
+            n = min(SFTG_MAX_TILE_LIGHTS, n + __popc(bal));
+        }
+    }
+    return n;
+}
+
+/* Per tile, once for all of its resolve CTAs: the light list (D2) and, per listed light, the
+ * selected proxies (D3: in index order, those whose light_vis entry is set and whose bounding
+ * sphere reaches the light's sphere, the first SFTG_MAX_LIGHT_PROXIES). */
+__global__ void __launch_bounds__(TILE_THREADS)
+k_tile_lights(const sftg_tile_args A, uint32_t tile0)
+{
+    __shared__ uint16_t s_lights[SFTG_MAX_TILE_LIGHTS];
+    __shared__ int s_nlights;
+    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x];
+    const sftg_frame* F = A.frames + A.tile_view[gtile];
+    const int tile = (int)(gtile - F->tile_base);
+    const uint8_t* light_vis = A.light_vis + (size_t)F->prox_base * 64;
+    sftg_tile_lights* TL = A.tile_lights + gtile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tmx = (tile % F->cols) * SFTG_TILE, tmy = (tile / F->cols) * SFTG_TILE;
+    const float2 zr = tile_zrange(A.zrange, gtile);
+    const float zmin = zr.x, zmax = zr.y;
+
+    if (warp == 0) {   /* D2 */
+        const int n = tile_light_list(F, zmin, zmax, tmx, tmy, lane, s_lights);
+        if (lane == 0) {
+            s_nlights = n;
+            A.tile_nlights[gtile] = (uint8_t)n;
+            TL->nlights = (uint32_t)n;
+        }
+    }
+    __syncthreads();
+    const int ntl = s_nlights;
+    if (tid < SFTG_MAX_TILE_LIGHTS) TL->light[tid] = tid < ntl ? s_lights[tid] : (uint16_t)0;
+    for (int i = warp; i < SFTG_MAX_TILE_LIGHTS; i += TILE_THREADS / 32) {
+        int n = 0;
+        if (i < ntl && F->shadows && F->n_proxies > 0) {
+            const sftg_point_light L = F->point[s_lights[i]];
+            for (uint32_t base = 0; base < F->n_proxies && n < SFTG_MAX_LIGHT_PROXIES; base += 32) {
+                const uint32_t p = base + lane;
+                bool take = false;
+                if (p < F->n_proxies && light_vis[(size_t)p * 64 + s_lights[i]]) {
+                    const sftg_proxy px = F->proxies[p];
+                    const v3 cc = mk3((px.posa[0] + px.posb[0]) * 0.5f, (px.posa[1] + px.posb[1]) * 0.5f, (px.posa[2] + px.posb[2]) * 0.5f);
+                    const v3 ab = mk3(px.posb[0] - px.posa[0], px.posb[1] - px.posa[1], px.posb[2] - px.posa[2]);
+                    const float cl = fsqrt(sdot(ab, ab));
+                    const float br = px.radius + (cl * 0.5f);
+                    const float cr = br + L.radius;
+                    const v3 Wv = sub3(cc, mk3(L.pos[0], L.pos[1], L.pos[2]));
+                    take = sdot(Wv, Wv) <= cr * cr;
+                }
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, take);
+                const int rank = __popc(bal & ((1u << lane) - 1u));
+                if (take && n + rank < SFTG_MAX_LIGHT_PROXIES) TL->proxy[i][n + rank] = p;
+                n = min(SFTG_MAX_LIGHT_PROXIES, n + __popc(bal));
+            }
+        }
+        if (lane == 0) TL->npc[i] = (uint8_t)n;
+    }
+}
+
 /* the tile's 4x2 block that a resolve CTA's b-th block is: at 4x the CTAs of a tile take every
  * split-th block, so the costly ones (many triangles, many lights) spread over all of them
  * (measured on the atrium at 4x: the slowest CTA of a tile took twice the mean with contiguous
@@ -504,7 +603,7 @@ SFTG_D int block_of(int part, int split, int nblk, int b) { return S == 4 ? b * 
  * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
 template <int S>
 __global__ void __launch_bounds__(TILE_THREADS, S == 1 ? 3 : 4)   /* 64 registers at 2x and 4x, 80 at 1x: measured best */
-k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
+k_resolve(const sftg_tile_args A, uint32_t tile0, int split, bool records)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
     /* the per-lane "between" test's operands of each cached proxy, in pcache's order: W (proxy
@@ -533,51 +632,22 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
     const float zmin = zr.x, zmax = zr.y;
     const float2* vis = A.vis + F->vis_base + (size_t)tile * S * SFTG_TILE_PX;
 
-    /* D2: tile light list, first 16 lights in index order that pass (5855-5934) */
-    if (warp == 0) {
-        int n = 0;
-        if (zmin <= zmax && F->n_point > 0) {
-            const float* vp = F->vp;
-            for (uint32_t base = 0; base < F->n_point && n < SFTG_MAX_TILE_LIGHTS; base += 32) {
-                const uint32_t l = base + lane;
-                bool pass = false;
-                if (l < F->n_point) {
-                    const sftg_point_light L = F->point[l];
-                    const float w = L.pos[0] * vp[3] + L.pos[1] * vp[7] + L.pos[2] * vp[11] + vp[15];
-                    const float lmin = w - L.radius, lmax = w + L.radius;
-                    pass = !(lmax <= 1e-6f);
-                    if (pass) {
-                        const float smin = (lmin > 1e-6f) ? lmin : 1e-6f;
-                        const float iwmin = fdiv(1.f, lmax), iwmax = fdiv(1.f, smin);
-                        if (iwmax < zmin || iwmin > zmax) pass = false;
-                    }
-                    if (pass && w > L.radius) {
-                        const float tx = L.pos[0] * vp[0] + L.pos[1] * vp[4] + L.pos[2] * vp[8] + vp[12];
-                        const float ty = L.pos[0] * vp[1] + L.pos[1] * vp[5] + L.pos[2] * vp[9] + vp[13];
-                        const float sx = (fdiv(tx, w) + 1.f) * F->hw + F->vpx;
-                        const float sy = (fdiv(-ty, w) + 1.f) * F->hh + F->vpy;
-                        const float psx = fsqrt(vp[0] * vp[0] + vp[4] * vp[4] + vp[8] * vp[8]);
-                        const float psy = fsqrt(vp[1] * vp[1] + vp[5] * vp[5] + vp[9] * vp[9]);
-                        const float safe_w = (w - L.radius) > 1e-6f ? (w - L.radius) : 1e-6f;
-                        const float rx = fdiv((L.radius * psx) + fabsf(tx) * fdiv(L.radius, w), safe_w) * F->hw;
-                        const float ry = fdiv((L.radius * psy) + fabsf(ty) * fdiv(L.radius, w), safe_w) * F->hh;
-                        if (sx + rx < (float)tmx || sx - rx > (float)(tmx + SFTG_TILE) || sy + ry < (float)tmy || sy - ry > (float)(tmy + SFTG_TILE)) pass = false;
-                    }
-                }
-                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
-                const int rank = __popc(bal & ((1u << lane) - 1u));
-                if (pass && n + rank < SFTG_MAX_TILE_LIGHTS) s_lights[n + rank] = (uint16_t)l;
-                n = min(SFTG_MAX_TILE_LIGHTS, n + __popc(bal));
+    const sftg_tile_lights* TL = A.tile_lights + gtile;
+    if (records) {   /* D2 and D3's selection come from the tile's record (k_tile_lights) */
+        if (tid < SFTG_MAX_TILE_LIGHTS) { s_lights[tid] = TL->light[tid]; s_npc[tid] = TL->npc[tid]; }
+        if (tid == 0) s_nlights = (int)TL->nlights;
+    } else {
+        if (warp == 0) {   /* D2 */
+            const int n = tile_light_list(F, zmin, zmax, tmx, tmy, lane, s_lights);
+            if (lane == 0) {
+                s_nlights = n;
+                if (part == 0) A.tile_nlights[gtile] = (uint8_t)n;
             }
-        }
-        if (lane == 0) {
-            s_nlights = n;
-            if (part == 0) A.tile_nlights[gtile] = (uint8_t)n;
         }
     }
     __syncthreads();
     const int ntl = s_nlights;
-    if (tid < ntl) s_pl[tid] = F->point[s_lights[tid]];   /* read after the barrier that follows D3 */
+    if (tid < ntl) s_pl[tid] = F->point[s_lights[tid]];
 
     /* World box of every surface point this CTA shades (per covered pixel and distinct sample
      * triangle, interpolated as the shading loop does), for the proxy filter below. */
@@ -612,47 +682,75 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split)
         if (lane == 0) { s_bnd[warp][0] = mn[0]; s_bnd[warp][1] = mn[1]; s_bnd[warp][2] = mn[2]; s_bnd[warp][3] = mx[0]; s_bnd[warp][4] = mx[1]; s_bnd[warp][5] = mx[2]; }
     }
 
-    /* D3: per light, the first 16 proxies that see it and can reach it (5936-5990) */
-    for (int i = warp; i < SFTG_MAX_TILE_LIGHTS; i += TILE_THREADS / 32) {
-        int n = 0;
-        if (i < ntl && F->shadows && F->n_proxies > 0) {
-            const sftg_point_light L = F->point[s_lights[i]];
-            for (uint32_t base = 0; base < F->n_proxies && n < SFTG_MAX_LIGHT_PROXIES; base += 32) {
-                const uint32_t p = base + lane;
-                bool take = false; uint8_t vs = 0;
-                v3 cc, ab, Wv; float br = 0.f, d2 = 0.f;
-                sftg_proxy px;
-                if (p < F->n_proxies) {
-                    px = F->proxies[p];
-                    vs = light_vis[(size_t)p * 64 + s_lights[i]];
-                    if (vs) {
-                        cc = mk3((px.posa[0] + px.posb[0]) * 0.5f, (px.posa[1] + px.posb[1]) * 0.5f, (px.posa[2] + px.posb[2]) * 0.5f);
-                        ab = mk3(px.posb[0] - px.posa[0], px.posb[1] - px.posa[1], px.posb[2] - px.posa[2]);
-                        const float cl = fsqrt(sdot(ab, ab));
-                        br = px.radius + (cl * 0.5f);
-                        const float cr = br + L.radius;
-                        Wv = sub3(cc, mk3(L.pos[0], L.pos[1], L.pos[2]));
-                        d2 = sdot(Wv, Wv);
-                        take = d2 <= cr * cr;
-                    }
-                }
-                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, take);
-                const int rank = __popc(bal & ((1u << lane) - 1u));
-                if (take && n + rank < SFTG_MAX_LIGHT_PROXIES) {
-                    proxy_cache* q = &pcache[i * SFTG_MAX_LIGHT_PROXIES + n + rank];
-                    q->pa[0] = px.posa[0]; q->pa[1] = px.posa[1]; q->pa[2] = px.posa[2];
-                    q->pb[0] = px.posb[0]; q->pb[1] = px.posb[1]; q->pb[2] = px.posb[2];
-                    q->ab[0] = ab.x; q->ab[1] = ab.y; q->ab[2] = ab.z;
-                    q->W[0] = Wv.x; q->W[1] = Wv.y; q->W[2] = Wv.z;
-                    q->abdab = sdot(ab, ab); q->wdw = d2; q->rb2 = br * br; q->pr = px.radius; q->pr2 = px.radius * px.radius;
-                    s_btw[i * SFTG_MAX_LIGHT_PROXIES + n + rank] = make_float4(Wv.x, Wv.y, Wv.z, d2);
-                    s_rb2[i * SFTG_MAX_LIGHT_PROXIES + n + rank] = q->rb2;
-                    q->vis_mult = (float)vs * 0.3333333f;
-                }
-                n = min(SFTG_MAX_LIGHT_PROXIES, n + __popc(bal));
-            }
+    if (records) {
+        /* D3's proxy cache (5936-5990): the tile's selected proxies, one thread per (light, slot), the
+         * entries computed as the selection computed them */
+        for (int t = tid; t < SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES; t += TILE_THREADS) {
+            const int i = t / SFTG_MAX_LIGHT_PROXIES, k = t % SFTG_MAX_LIGHT_PROXIES;
+            if (i >= ntl || k >= s_npc[i]) continue;
+            const uint32_t p = TL->proxy[i][k];
+            const sftg_point_light L = F->point[s_lights[i]];   /* s_pl is read only after the next barrier */
+            const sftg_proxy px = F->proxies[p];
+            const uint8_t vs = light_vis[(size_t)p * 64 + s_lights[i]];
+            const v3 cc = mk3((px.posa[0] + px.posb[0]) * 0.5f, (px.posa[1] + px.posb[1]) * 0.5f, (px.posa[2] + px.posb[2]) * 0.5f);
+            const v3 ab = mk3(px.posb[0] - px.posa[0], px.posb[1] - px.posa[1], px.posb[2] - px.posa[2]);
+            const float cl = fsqrt(sdot(ab, ab));
+            const float br = px.radius + (cl * 0.5f);
+            const v3 Wv = sub3(cc, mk3(L.pos[0], L.pos[1], L.pos[2]));
+            const float d2 = sdot(Wv, Wv);
+            proxy_cache* q = &pcache[t];
+            q->pa[0] = px.posa[0]; q->pa[1] = px.posa[1]; q->pa[2] = px.posa[2];
+            q->pb[0] = px.posb[0]; q->pb[1] = px.posb[1]; q->pb[2] = px.posb[2];
+            q->ab[0] = ab.x; q->ab[1] = ab.y; q->ab[2] = ab.z;
+            q->W[0] = Wv.x; q->W[1] = Wv.y; q->W[2] = Wv.z;
+            q->abdab = sdot(ab, ab); q->wdw = d2; q->rb2 = br * br; q->pr = px.radius; q->pr2 = px.radius * px.radius;
+            q->vis_mult = (float)vs * 0.3333333f;
+            s_btw[t] = make_float4(Wv.x, Wv.y, Wv.z, d2);
+            s_rb2[t] = q->rb2;
         }
-        if (lane == 0) s_npc[i] = (uint8_t)n;
+    } else {
+        /* D3: per light, the first 16 proxies that see it and can reach it (5936-5990) */
+        for (int i = warp; i < SFTG_MAX_TILE_LIGHTS; i += TILE_THREADS / 32) {
+            int n = 0;
+            if (i < ntl && F->shadows && F->n_proxies > 0) {
+                const sftg_point_light L = F->point[s_lights[i]];
+                for (uint32_t base = 0; base < F->n_proxies && n < SFTG_MAX_LIGHT_PROXIES; base += 32) {
+                    const uint32_t p = base + lane;
+                    bool take = false; uint8_t vs = 0;
+                    v3 cc, ab, Wv; float br = 0.f, d2 = 0.f;
+                    sftg_proxy px;
+                    if (p < F->n_proxies) {
+                        px = F->proxies[p];
+                        vs = light_vis[(size_t)p * 64 + s_lights[i]];
+                        if (vs) {
+                            cc = mk3((px.posa[0] + px.posb[0]) * 0.5f, (px.posa[1] + px.posb[1]) * 0.5f, (px.posa[2] + px.posb[2]) * 0.5f);
+                            ab = mk3(px.posb[0] - px.posa[0], px.posb[1] - px.posa[1], px.posb[2] - px.posa[2]);
+                            const float cl = fsqrt(sdot(ab, ab));
+                            br = px.radius + (cl * 0.5f);
+                            const float cr = br + L.radius;
+                            Wv = sub3(cc, mk3(L.pos[0], L.pos[1], L.pos[2]));
+                            d2 = sdot(Wv, Wv);
+                            take = d2 <= cr * cr;
+                        }
+                    }
+                    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, take);
+                    const int rank = __popc(bal & ((1u << lane) - 1u));
+                    if (take && n + rank < SFTG_MAX_LIGHT_PROXIES) {
+                        proxy_cache* q = &pcache[i * SFTG_MAX_LIGHT_PROXIES + n + rank];
+                        q->pa[0] = px.posa[0]; q->pa[1] = px.posa[1]; q->pa[2] = px.posa[2];
+                        q->pb[0] = px.posb[0]; q->pb[1] = px.posb[1]; q->pb[2] = px.posb[2];
+                        q->ab[0] = ab.x; q->ab[1] = ab.y; q->ab[2] = ab.z;
+                        q->W[0] = Wv.x; q->W[1] = Wv.y; q->W[2] = Wv.z;
+                        q->abdab = sdot(ab, ab); q->wdw = d2; q->rb2 = br * br; q->pr = px.radius; q->pr2 = px.radius * px.radius;
+                        s_btw[i * SFTG_MAX_LIGHT_PROXIES + n + rank] = make_float4(Wv.x, Wv.y, Wv.z, d2);
+                        s_rb2[i * SFTG_MAX_LIGHT_PROXIES + n + rank] = q->rb2;
+                        q->vis_mult = (float)vs * 0.3333333f;
+                    }
+                    n = min(SFTG_MAX_LIGHT_PROXIES, n + __popc(bal));
+                }
+            }
+            if (lane == 0) s_npc[i] = (uint8_t)n;
+        }
     }
     __syncthreads();
 
@@ -1205,10 +1303,14 @@ void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, in
     else k_raster<4><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
 }
 
-void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, cudaStream_t st, const sftg_tile_args& A) {
+void sftg_launch_tile_lights(uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
+    if (tiles) k_tile_lights<<<tiles, TILE_THREADS, 0, st>>>(A, tile0);
+}
+
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, bool records, cudaStream_t st, const sftg_tile_args& A) {
     if (!tiles) return;
     const uint32_t grid = tiles * (uint32_t)split;
-    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split);
-    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split);
-    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split);
+    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split, records);
+    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split, records);
+    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split, records);
 }
