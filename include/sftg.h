@@ -189,8 +189,8 @@ typedef struct sftg_tuning {
 int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out);
 int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* tuning);
 /* Times the given views with each candidate setting (median of reps renders per candidate,
- * coordinate search: job width, then per sample count slab rows, raster bands, resolve split and
- * where the tile light lists are made), keeps the
+ * coordinate search: job width, then per sample count slab rows, raster bands, and resolve split
+ * with where the tile light lists are made, jointly), keeps the
  * fastest in the context and copies it to *out (optional). */
 int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, int32_t reps, sftg_tuning* out);
 

@@ -1451,21 +1451,17 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
             if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 3, &t))) { ctx->tuning = best; return rc; }
             if (t < bt) { bt = t; best.raster_bands[si] = bands[k]; }
         }
+        /* resolve split and where the tile light lists are made, jointly: per-tile lists take the
+         * split-fold selection work out of every CTA, which favours higher splits */
         const int splits[5] = { 4, 8, 16, 2, 1 };
         bt = 1e30f;
-        for (int k = 0; k < 5; k++) {
-            ctx->tuning = best; ctx->tuning.resolve_split[si] = splits[k];
-            float t;
-            if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
-            if (t < bt) { bt = t; best.resolve_split[si] = splits[k]; }
-        }
-        bt = 1e30f;
-        for (int k = 1; k <= 2; k++) {
-            ctx->tuning = best; ctx->tuning.tile_lights[si] = k;
-            float t;
-            if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
-            if (t < bt) { bt = t; best.tile_lights[si] = k; }
-        }
+        for (int k = 0; k < 5; k++)
+            for (int m = 1; m <= 2; m++) {
+                ctx->tuning = best; ctx->tuning.resolve_split[si] = splits[k]; ctx->tuning.tile_lights[si] = m;
+                float t;
+                if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
+                if (t < bt) { bt = t; best.resolve_split[si] = splits[k]; best.tile_lights[si] = m; }
+            }
     }
     ctx->tuning = best;
     if (out) *out = best;
