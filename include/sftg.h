@@ -185,12 +185,15 @@ typedef struct sftg_tuning {
                                      its resolve CTAs, 2 = once per tile by a launch before the resolve (its CTAs read
                                      the result), 0 = 2 where the range has 16 CTAs per tile and at least 256 tiles,
                                      else 1 (default) */
+    int32_t tile_queue;           /* bit 0 raster, bit 1 resolve: set, the phase is one persistent launch of as many CTAs
+                                     as are resident at once, which take its (tile, band) / (tile, part) items, heaviest
+                                     tiles first, from a device counter; clear (default 0), one CTA per item */
 } sftg_tuning;
 int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out);
 int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* tuning);
 /* Times the given views with each candidate setting (median of reps renders per candidate,
  * coordinate search: job width, then per sample count slab rows, raster bands, and resolve split
- * with where the tile light lists are made, jointly), keeps the
+ * with where the tile light lists are made, jointly, then the persistent tile queue), keeps the
  * fastest in the context and copies it to *out (optional). */
 int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* frames, uint32_t n_views, int32_t reps, sftg_tuning* out);
 

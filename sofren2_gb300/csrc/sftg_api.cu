@@ -109,7 +109,7 @@ struct sftg_ctx {
     uint32_t blas_items = 0, blas_launches = 0; /* and its triangles and kernels */
     cudaEvent_t ev_blas[2] = { nullptr, nullptr };
     bool use_graphs = true;
-    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0, { 0, 0, 0 }, { 0, 0, 0 } };   /* measured best on the single-view workloads */
+    sftg_tuning tuning = { { 16, 8, 16 }, { 8, 8, 4 }, 1, 0, { 0, 0, 0 }, { 0, 0, 0 }, 0 };   /* measured best on the single-view workloads */
     /* transient models (one frame's dynamic meshes): pool marks where they start */
     bool tr_live = false, tr_pinned = false;
     uint32_t tr_meshlets = 0, tr_skin = 0, tr_blas = 0;
@@ -488,6 +488,7 @@ struct batch_bufs {
     uint32_t* tile_order; uint32_t* order_scratch;
     uint8_t* tile_nlights;   /* per tile: its light list length (debug views) */
     sftg_tile_lights* tile_lights;   /* per tile: lights and selected proxies, shared by its resolve CTAs */
+    uint32_t* queue;         /* item counters of the persistent raster and resolve launches, one per launch */
     bool any_overlay;        /* a view asks for a tile overlay (debug modes 2-4) */
     uint64_t* tile_pay;
     uint8_t* light_vis;
@@ -674,7 +675,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     acc((size_t)total_prox * 64 + 64); acc((size_t)total_packets * sftg_packet_bytes() + 64);
     acc((max_pairs * (1 + SFTG_OCC_ITEMS_PER_PAIR) + 1) * 8); acc(64); acc(((n_rec + total_tiles + total_stiles) / SFTG_SCAN_ELEMS_PER_BLOCK + 16) * 4); acc(64); acc(64);
     acc(vis_total * 8); acc((size_t)(total_tiles + 1) * sftg_raster_bands() * sizeof(float2));
-    acc((size_t)total_tiles * sizeof(sftg_tile_lights));
+    acc((size_t)total_tiles * sizeof(sftg_tile_lights)); acc(64);
     const int W0 = fds[0].width, H0 = fds[0].height, S0 = fds[0].samples;
     if (want_debug) { acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)total_tiles * S0 * 4096 * 4); acc((size_t)W0 * H0 * 16 * 4); }
     /* growth: the lane's previous batch has finished (a lane takes a batch only once the last
@@ -734,6 +735,7 @@ static int build_batch(sftg_ctx* ctx, sftg_lane& ln, const sftg_frame_desc* fds,
     B.vis = bp.take<float2>(vis_total);
     B.zrange = bp.take<float2>((size_t)(total_tiles + 1) * sftg_raster_bands());   /* per raster band of each tile */
     B.tile_lights = bp.take<sftg_tile_lights>(total_tiles);
+    B.queue = bp.take<uint32_t>(16);
     B.vis_depth = nullptr; B.vis_id = nullptr; B.shadow = nullptr;
     if (want_debug) {
         B.vis_depth = bp.take<float>((size_t)total_tiles * S0 * 4096);
@@ -902,7 +904,12 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
         CK(cudaStreamWaitEvent(st, ln.ev_merge[k], 0));
         return 0;
     };
-    int prc = per_range(0, [&](int si, cudaStream_t s) { sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], ctx->tuning.raster_bands[si], s, A); });
+    const bool queue_raster = (ctx->tuning.tile_queue & 1) != 0, queue_resolve = (ctx->tuning.tile_queue & 2) != 0;
+    if (ctx->tuning.tile_queue) CK(cudaMemsetAsync(B.queue, 0, 64, st));   /* counters: raster 0-2, resolve 3-5 */
+    int prc = per_range(0, [&](int si, cudaStream_t s) {
+        sftg_launch_raster(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.raster_slab_rows[si], ctx->tuning.raster_bands[si],
+                           queue_raster ? B.queue + si : nullptr, s, A);
+    });
     if (prc) return prc;
     CK(cudaGetLastError());
     CK(record_event(ln.ev[4], st));
@@ -918,7 +925,10 @@ static int launch_batch(sftg_ctx* ctx, sftg_lane& ln, const batch_bufs& B) {
             ln.launches++;
         }
     }
-    prc = per_range(1, [&](int si, cudaStream_t s) { sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], records[si], s, A); });
+    prc = per_range(1, [&](int si, cudaStream_t s) {
+        sftg_launch_resolve(1 << si, B.s_tile0[si], B.s_tiles[si], ctx->tuning.resolve_split[si], records[si],
+                            queue_resolve ? B.queue + 3 + si : nullptr, s, A);
+    });
     if (prc) return prc;
     if (B.any_overlay) { sftg_launch_debug_overlay(B.total_tiles, st, A); ln.launches++; }
     CK(cudaGetLastError());
@@ -938,7 +948,7 @@ static uint64_t batch_key(const sftg_ctx* ctx, const batch_bufs& B) {
     const uint32_t ov = B.any_overlay ? 1u : 0u;
     h = fnv(h, &ov, sizeof(ov));
     const void* ptrs[] = { B.frames, B.jobs, B.tile_view, B.packet_view, B.prox_view, B.stile_view, B.stile_count, B.stile_start,
-                           B.stile_list, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights, B.tile_lights,
+                           B.stile_list, B.ss, B.recs, B.clip_cnt, B.clip_base, B.tile_nlights, B.tile_lights, B.queue,
                            B.mrect, B.clips, B.clip_rect, B.tile_count, B.tile_start, B.tile_order, B.order_scratch, B.tile_pay,
                            B.light_vis, B.packets, B.pairs, B.n_pairs, B.scan_tmp, B.status, B.totals, B.vis, B.zrange,
                            B.vis_depth, B.vis_id, B.shadow };
@@ -1382,7 +1392,8 @@ static bool tuning_valid(const sftg_tuning* t) {
         if (!(rb == 0 || rb == 1 || rb == 2 || rb == 4)) return false;
         if (t->tile_lights[k] < 0 || t->tile_lights[k] > 2) return false;
     }
-    return t->geom_job_width >= 1 && t->geom_job_width <= 8 && (t->occl_ray_prune == 0 || t->occl_ray_prune == 1);
+    return t->geom_job_width >= 1 && t->geom_job_width <= 8 && (t->occl_ray_prune == 0 || t->occl_ray_prune == 1) &&
+           t->tile_queue >= 0 && t->tile_queue <= 3;
 }
 
 extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
@@ -1393,7 +1404,7 @@ extern "C" int sftg_get_tuning(const sftg_ctx* ctx, sftg_tuning* out) {
 
 extern "C" int sftg_set_tuning(sftg_ctx* ctx, const sftg_tuning* t) {
     if (!ctx || !t) return SFTG_E_ARG;
-    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8, raster bands 0/1/2/4, tile lights 0/1/2)");
+    if (!tuning_valid(t)) return set_err(ctx, SFTG_E_ARG, "tuning out of range (split 1/2/4/8/16, slab rows 4..64, job width 1..8, raster bands 0/1/2/4, tile lights 0/1/2, tile queue 0-3)");
     ctx->tuning = *t;
     return SFTG_OK;
 }
@@ -1404,7 +1415,7 @@ static int time_phase(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n, int
     for (int r = 0; r < reps; r++) {
         const int rc = batch_common(ctx, fds, n, nullptr, nullptr, nullptr, nullptr);
         if (rc) return rc;
-        t.push_back(ctx->timings[phase]);
+        t.push_back(phase < 0 ? ctx->timings[3] + ctx->timings[4] : ctx->timings[phase]);   /* -1: raster + resolve */
     }
     std::sort(t.begin(), t.end());
     *out = t[t.size() / 2];
@@ -1413,8 +1424,9 @@ static int time_phase(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n, int
 
 /* Coordinate search over the knobs that change only scheduling, never results: the geometry
  * job width against the geometry phase, then per sample count the raster slab height and the
- * raster bands against the raster phase and the resolve split against the resolve phase, each
- * measured on the views with that sample count.  Leaves the best setting in the context. */
+ * raster bands against the raster phase and the resolve split with the tile light lists against
+ * the resolve phase, each measured on the views with that sample count, then the persistent tile
+ * queue against raster + resolve of all views.  Leaves the best setting in the context. */
 extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t n_views, int32_t reps, sftg_tuning* out) {
     if (!ctx || !fds || !n_views) return SFTG_E_ARG;
     if (reps < 1) reps = 5;
@@ -1462,6 +1474,15 @@ extern "C" int sftg_autotune(sftg_ctx* ctx, const sftg_frame_desc* fds, uint32_t
                 if ((rc = time_phase(ctx, sub.data(), (uint32_t)sub.size(), reps, 4, &t))) { ctx->tuning = best; return rc; }
                 if (t < bt) { bt = t; best.resolve_split[si] = splits[k]; best.tile_lights[si] = m; }
             }
+    }
+    {   /* the persistent tile queue, against raster + resolve of all views */
+        float bt = 1e30f;
+        for (int q = 0; q <= 3; q++) {
+            ctx->tuning = best; ctx->tuning.tile_queue = q;
+            float t;
+            if ((rc = time_phase(ctx, fds, n_views, reps, -1, &t))) { ctx->tuning = best; return rc; }
+            if (t < bt) { bt = t; best.tile_queue = q; }
+        }
     }
     ctx->tuning = best;
     if (out) *out = best;

@@ -85,9 +85,13 @@ int sftg_raster_bands(void);   /* raster CTAs (row bands) per 64x64 tile */
 int sftg_launch_tile_order(const sftg_frame* frames, const uint16_t* tile_view, const uint32_t* tile_count, uint32_t n_tiles,
                             uint32_t* scratch, uint32_t* order, cudaStream_t st);
 /* slab_rows: rows of one raster work item (4..64); split: resolve CTAs per tile (1, 2, 4, 8 or 16) */
-void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, int bands, cudaStream_t st, const sftg_tile_args& A);
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, int bands, uint32_t* queue, cudaStream_t st,
+                        const sftg_tile_args& A);
 void sftg_launch_tile_lights(uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
-void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, bool records, cudaStream_t st, const sftg_tile_args& A);
+/* queue: null for one CTA per (tile, part) item, else a zeroed counter for one persistent launch
+ * whose CTAs take the items in launch order (k_resolve_queue); likewise for the raster */
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, bool records, uint32_t* queue, cudaStream_t st,
+                         const sftg_tile_args& A);
 /* tile overlays of the debug views 2-4 (sft__debug_draw_tile_overlay), after every resolve */
 void sftg_launch_debug_overlay(uint32_t tiles, cudaStream_t st, const sftg_tile_args& A);
 

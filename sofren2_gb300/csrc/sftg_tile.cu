@@ -345,8 +345,7 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
  * tile's depth range over valid samples (sofren2.c:5820-5853), which the resolve needs for its
  * light culling. */
 template <int S>
-__global__ void __launch_bounds__(RASTER_THREADS)
-k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
+SFTG_D void raster_item(const sftg_tile_args& A, uint32_t tile0, int slab_rows, int fixed_bands, uint32_t item)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = (unsigned long long*)smem;                  /* S planes, a band uses the first band_px of each */
@@ -358,8 +357,8 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
      * still walking a long slab (items touch keys only through atomicMax: order is free) */
     const uint32_t items_cap = (uint32_t)SETUP_CAP * (uint32_t)((raster_plan<S>::rows + slab_rows - 1) / slab_rows);
     __shared__ float s_red[2][RASTER_THREADS / 32];
-    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x / RASTER_BANDS];   /* batch-wide tile index, heaviest first */
-    const int band = (int)(blockIdx.x % RASTER_BANDS);
+    const uint32_t gtile = A.tile_order[tile0 + item / RASTER_BANDS];   /* batch-wide tile index, heaviest first */
+    const int band = (int)(item % RASTER_BANDS);
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
     const float* ss = A.ss + (size_t)F->ss_base * SFTG_SS_FLOATS;
@@ -490,6 +489,32 @@ k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
     }
 }
 
+/* one CTA per (tile, band) item */
+template <int S>
+__global__ void __launch_bounds__(RASTER_THREADS)
+k_raster(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands)
+{
+    raster_item<S>(A, tile0, slab_rows, fixed_bands, blockIdx.x);
+}
+
+/* Persistent form: as many CTAs as fit on the GPU at once, each taking the next (tile, band) item
+ * in launch order (heaviest tiles first) from a counter until all n_items are taken.  The loop
+ * ends after at most n_items + grid counter reads: nothing waits on another CTA. */
+template <int S>
+__global__ void __launch_bounds__(RASTER_THREADS, 2)   /* the 64 registers k_raster gets: 2 CTAs per SM */
+k_raster_queue(const sftg_tile_args A, uint32_t tile0, int slab_rows, int fixed_bands, uint32_t n_items, uint32_t* next)
+{
+    __shared__ uint32_t s_item;
+    for (;;) {
+        __syncthreads();   /* the previous item is done with shared memory, and s_item has been read */
+        if (threadIdx.x == 0) s_item = atomicAdd(next, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= n_items) break;
+        raster_item<S>(A, tile0, slab_rows, fixed_bands, item);
+    }
+}
+
 /* ---------------------------------------------------------------- resolve */
 /* D2 (5855-5934), one warp: the first SFTG_MAX_TILE_LIGHTS point lights in index order whose
  * depth range meets the tile's [zmin, zmax] and whose screen rectangle meets the tile.  Their
@@ -602,8 +627,7 @@ SFTG_D int block_of(int part, int split, int nblk, int b) { return S == 4 ? b * 
 /* One CTA per quarter tile: tile light list (5855-5934) and proxy cache (5936-5990), then one
  * 8-thread group per 4x2 block for the per-triangle shading and MSAA resolve (6029-6745). */
 template <int S>
-__global__ void __launch_bounds__(TILE_THREADS, S == 1 ? 3 : 4)   /* 64 registers at 2x and 4x, 80 at 1x: measured best */
-k_resolve(const sftg_tile_args A, uint32_t tile0, int split, bool records)
+SFTG_D void resolve_item(const sftg_tile_args& A, uint32_t tile0, int split, bool records, uint32_t item)
 {
     __shared__ proxy_cache pcache[SFTG_MAX_TILE_LIGHTS * SFTG_MAX_LIGHT_PROXIES];
     /* the per-lane "between" test's operands of each cached proxy, in pcache's order: W (proxy
@@ -615,8 +639,8 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split, bool records)
     __shared__ int s_nlights;
     __shared__ uint8_t s_npc[SFTG_MAX_TILE_LIGHTS];
 
-    const uint32_t gtile = A.tile_order[tile0 + blockIdx.x / (uint32_t)split];   /* batch-wide tile index, heaviest first */
-    const int part = (int)(blockIdx.x % (uint32_t)split);
+    const uint32_t gtile = A.tile_order[tile0 + item / (uint32_t)split];   /* batch-wide tile index, heaviest first */
+    const int part = (int)(item % (uint32_t)split);
     const int nblk = TILE_BLOCKS / split;
     const sftg_frame* F = A.frames + A.tile_view[gtile];
     const int tile = (int)(gtile - F->tile_base);
@@ -1136,6 +1160,30 @@ k_resolve(const sftg_tile_args A, uint32_t tile0, int split, bool records)
     }
 }
 
+/* one CTA per (tile, part) item */
+template <int S>
+__global__ void __launch_bounds__(TILE_THREADS, S == 1 ? 3 : 4)   /* 64 registers at 2x and 4x, 80 at 1x: measured best */
+k_resolve(const sftg_tile_args A, uint32_t tile0, int split, bool records)
+{
+    resolve_item<S>(A, tile0, split, records, blockIdx.x);
+}
+
+/* Persistent form, as k_raster_queue: CTAs take (tile, part) items in launch order from a counter. */
+template <int S>
+__global__ void __launch_bounds__(TILE_THREADS, S == 1 ? 3 : 4)
+k_resolve_queue(const sftg_tile_args A, uint32_t tile0, int split, bool records, uint32_t n_items, uint32_t* next)
+{
+    __shared__ uint32_t s_item;
+    for (;;) {
+        __syncthreads();   /* the previous item is done with shared memory, and s_item has been read */
+        if (threadIdx.x == 0) s_item = atomicAdd(next, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= n_items) break;
+        resolve_item<S>(A, tile0, split, records, item);
+    }
+}
+
 /* ---------------------------------------------------------------- tile order
  * The reference's workers take tiles in descending payload count (sofren2.c:6815-6857) so the
  * heaviest start first.  Here the same idea keeps the tail of the raster and resolve grids
@@ -1290,27 +1338,57 @@ cudaError_t sftg_tile_configure(int max_dynamic_smem) {
         if (S_[k] == 1) e = cudaFuncSetAttribute(k_raster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
         if (S_[k] == 2) e = cudaFuncSetAttribute(k_raster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
         if (S_[k] == 4) e = cudaFuncSetAttribute(k_raster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        if (e != cudaSuccess) break;
+        if (S_[k] == 1) e = cudaFuncSetAttribute(k_raster_queue<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        if (S_[k] == 2) e = cudaFuncSetAttribute(k_raster_queue<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        if (S_[k] == 4) e = cudaFuncSetAttribute(k_raster_queue<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
     }
     return e;
 }
 
-void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, int bands, cudaStream_t st, const sftg_tile_args& A) {
+/* CTAs of a persistent launch: as many as are resident at once on all SMs (at least 1), never more
+ * than there are items */
+template <class K>
+static uint32_t queue_grid(K kernel, int threads, size_t smem, uint32_t n_items) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    const uint64_t g = (uint64_t)(sms > 0 ? sms : 1) * (uint64_t)(per_sm > 0 ? per_sm : 1);
+    return (uint32_t)(g < n_items ? g : n_items);
+}
+
+void sftg_launch_raster(int S, uint32_t tile0, uint32_t tiles, int slab_rows, int bands, uint32_t* queue, cudaStream_t st,
+                        const sftg_tile_args& A) {
     if (!tiles) return;
     const size_t sm = raster_smem(S, slab_rows);
-    const uint32_t grid = tiles * RASTER_BANDS;
-    if (S == 1) k_raster<1><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
-    else if (S == 2) k_raster<2><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
-    else k_raster<4><<<grid, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
+    const uint32_t items = tiles * RASTER_BANDS;
+    if (queue) {
+        if (S == 1) k_raster_queue<1><<<queue_grid(k_raster_queue<1>, RASTER_THREADS, sm, items), RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands, items, queue);
+        else if (S == 2) k_raster_queue<2><<<queue_grid(k_raster_queue<2>, RASTER_THREADS, sm, items), RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands, items, queue);
+        else k_raster_queue<4><<<queue_grid(k_raster_queue<4>, RASTER_THREADS, sm, items), RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands, items, queue);
+        return;
+    }
+    if (S == 1) k_raster<1><<<items, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
+    else if (S == 2) k_raster<2><<<items, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
+    else k_raster<4><<<items, RASTER_THREADS, sm, st>>>(A, tile0, slab_rows, bands);
 }
 
 void sftg_launch_tile_lights(uint32_t tile0, uint32_t tiles, cudaStream_t st, const sftg_tile_args& A) {
     if (tiles) k_tile_lights<<<tiles, TILE_THREADS, 0, st>>>(A, tile0);
 }
 
-void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, bool records, cudaStream_t st, const sftg_tile_args& A) {
+void sftg_launch_resolve(int S, uint32_t tile0, uint32_t tiles, int split, bool records, uint32_t* queue, cudaStream_t st,
+                         const sftg_tile_args& A) {
     if (!tiles) return;
-    const uint32_t grid = tiles * (uint32_t)split;
-    if (S == 1) k_resolve<1><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split, records);
-    else if (S == 2) k_resolve<2><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split, records);
-    else k_resolve<4><<<grid, TILE_THREADS, 0, st>>>(A, tile0, split, records);
+    const uint32_t items = tiles * (uint32_t)split;
+    if (queue) {
+        if (S == 1) k_resolve_queue<1><<<queue_grid(k_resolve_queue<1>, TILE_THREADS, 0, items), TILE_THREADS, 0, st>>>(A, tile0, split, records, items, queue);
+        else if (S == 2) k_resolve_queue<2><<<queue_grid(k_resolve_queue<2>, TILE_THREADS, 0, items), TILE_THREADS, 0, st>>>(A, tile0, split, records, items, queue);
+        else k_resolve_queue<4><<<queue_grid(k_resolve_queue<4>, TILE_THREADS, 0, items), TILE_THREADS, 0, st>>>(A, tile0, split, records, items, queue);
+        return;
+    }
+    if (S == 1) k_resolve<1><<<items, TILE_THREADS, 0, st>>>(A, tile0, split, records);
+    else if (S == 2) k_resolve<2><<<items, TILE_THREADS, 0, st>>>(A, tile0, split, records);
+    else k_resolve<4><<<items, TILE_THREADS, 0, st>>>(A, tile0, split, records);
 }

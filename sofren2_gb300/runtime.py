@@ -262,14 +262,16 @@ class Renderer:
         return self.tuning()
 
     def tuning(self) -> dict:
-        t = np.zeros(14, np.int32)   # struct sftg_tuning (include/sftg.h)
+        t = np.zeros(15, np.int32)   # struct sftg_tuning (include/sftg.h)
         self.lib.sftg_get_tuning(self.lib.sft_get_gpu_context(), _ptr(t))
         return {"resolve_split": t[0:3].tolist(), "raster_slab_rows": t[3:6].tolist(), "geom_job_width": int(t[6]),
-                "occl_ray_prune": int(t[7]), "raster_bands": t[8:11].tolist(), "tile_lights": t[11:14].tolist()}
+                "occl_ray_prune": int(t[7]), "raster_bands": t[8:11].tolist(), "tile_lights": t[11:14].tolist(),
+                "tile_queue": int(t[14])}
 
     def set_tuning(self, resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=1, occl_ray_prune=0,
-                   raster_bands=(0, 0, 0), tile_lights=(0, 0, 0)) -> None:
-        t = np.array([*resolve_split, *raster_slab_rows, geom_job_width, occl_ray_prune, *raster_bands, *tile_lights], np.int32)
+                   raster_bands=(0, 0, 0), tile_lights=(0, 0, 0), tile_queue=0) -> None:
+        t = np.array([*resolve_split, *raster_slab_rows, geom_job_width, occl_ray_prune, *raster_bands, *tile_lights, tile_queue],
+                     np.int32)
         if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
             raise ValueError("tuning out of range")
 

@@ -87,9 +87,11 @@ def test_golden_cases_in_one_batch(renderer, golden):
 
 TUNINGS = [
     dict(resolve_split=(1, 2, 8), raster_slab_rows=(4, 16, 64), geom_job_width=1, raster_bands=(1, 2, 4), tile_lights=(2, 1, 2)),
-    dict(resolve_split=(8, 1, 2), raster_slab_rows=(64, 4, 16), geom_job_width=3, raster_bands=(4, 1, 2), tile_lights=(1, 2, 1)),
+    dict(resolve_split=(8, 1, 2), raster_slab_rows=(64, 4, 16), geom_job_width=3, raster_bands=(4, 1, 2), tile_lights=(1, 2, 1),
+         tile_queue=3),
     dict(resolve_split=(2, 8, 1), raster_slab_rows=(16, 64, 4), geom_job_width=5, raster_bands=(2, 4, 1), tile_lights=(2, 2, 2)),
-    dict(resolve_split=(16, 16, 16), raster_slab_rows=(4, 4, 4), geom_job_width=8, tile_lights=(1, 1, 1)),
+    dict(resolve_split=(16, 16, 16), raster_slab_rows=(4, 4, 4), geom_job_width=8, tile_lights=(1, 1, 1), tile_queue=1),
+    dict(resolve_split=(4, 4, 4), raster_slab_rows=(8, 8, 8), geom_job_width=2, tile_lights=(2, 2, 1), tile_queue=2),
     dict(resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=8, occl_ray_prune=1),
 ]
 
