@@ -126,6 +126,11 @@ class SftxServeStats(C.Structure):
                 ("max_inflight", C.c_uint64)]
 
 
+# struct sftg_tuning (include/sftg.h), field by field in order: (name, int32 count)
+TUNING_LAYOUT = (("resolve_split", 3), ("raster_slab_rows", 3), ("geom_job_width", 1), ("occl_ray_prune", 1),
+                 ("raster_bands", 3), ("tile_lights", 3), ("tile_queue", 1))
+
+
 def request_device_bytes(width: int, height: int, samples: int, meshlets: int) -> int:
     """Device memory a request holds while in flight: visibility buffer (8 B per sample), colour,
     screen-space cache and batch records per meshlet, tile lists and clip pool at a generous
@@ -262,16 +267,23 @@ class Renderer:
         return self.tuning()
 
     def tuning(self) -> dict:
-        t = np.zeros(15, np.int32)   # struct sftg_tuning (include/sftg.h)
+        t = np.zeros(sum(n for _, n in TUNING_LAYOUT), np.int32)
         self.lib.sftg_get_tuning(self.lib.sft_get_gpu_context(), _ptr(t))
-        return {"resolve_split": t[0:3].tolist(), "raster_slab_rows": t[3:6].tolist(), "geom_job_width": int(t[6]),
-                "occl_ray_prune": int(t[7]), "raster_bands": t[8:11].tolist(), "tile_lights": t[11:14].tolist(),
-                "tile_queue": int(t[14])}
+        out, k = {}, 0
+        for name, n in TUNING_LAYOUT:
+            out[name] = t[k:k + n].tolist() if n > 1 else int(t[k])
+            k += n
+        return out
 
     def set_tuning(self, resolve_split=(16, 8, 16), raster_slab_rows=(8, 8, 4), geom_job_width=1, occl_ray_prune=0,
                    raster_bands=(0, 0, 0), tile_lights=(0, 0, 0), tile_queue=0) -> None:
-        t = np.array([*resolve_split, *raster_slab_rows, geom_job_width, occl_ray_prune, *raster_bands, *tile_lights, tile_queue],
-                     np.int32)
+        vals = dict(resolve_split=resolve_split, raster_slab_rows=raster_slab_rows, geom_job_width=geom_job_width,
+                    occl_ray_prune=occl_ray_prune, raster_bands=raster_bands, tile_lights=tile_lights, tile_queue=tile_queue)
+        flat = []
+        for name, n in TUNING_LAYOUT:
+            v = vals[name]
+            flat += list(v) if n > 1 else [v]
+        t = np.array(flat, np.int32)
         if self.lib.sftg_set_tuning(self.lib.sft_get_gpu_context(), _ptr(t)) != 0:
             raise ValueError("tuning out of range")
 

@@ -1,6 +1,7 @@
 """The C ABI and host pieces that need no GPU: every function declared in include/*.h is
-exported by libsofren2_gb300.so, and the measured RCPPS/RSQRTPS tables reproduce the x86
-instructions (checked against the instructions themselves where the host is x86-64)."""
+exported by libsofren2_gb300.so, the Python binding's sftg_tuning layout is the header's, and the
+measured RCPPS/RSQRTPS tables reproduce the x86 instructions (checked against the instructions
+themselves where the host is x86-64)."""
 import ctypes as C
 import os
 import platform
@@ -103,3 +104,27 @@ def test_serve_and_lane_calls_reject_bad_arguments(lib_path):
         f = getattr(lib, fn)
         f.restype = C.c_int
         assert f(*args) == -2, fn   # SFTG_E_ARG
+
+
+def test_tuning_layout_matches_the_header(tmp_path):
+    """runtime.TUNING_LAYOUT (the ctypes view of struct sftg_tuning) against the header, compiled:
+    every field's offset and count, and the struct's size."""
+    from sofren2_gb300.runtime import TUNING_LAYOUT
+    cc = "gcc"
+    names = [n for n, _ in TUNING_LAYOUT]
+    prog = ["#include <stddef.h>", "#include <stdio.h>", '#include "sftg.h"', "int main(void) {",
+            '    printf("%zu\\n", sizeof(sftg_tuning));']
+    for n in names:
+        prog.append(f'    printf("%zu %zu\\n", offsetof(sftg_tuning, {n}), sizeof(((sftg_tuning*)0)->{n}));')
+    prog += ["    return 0;", "}"]
+    src = tmp_path / "tuning_layout.c"
+    src.write_text("\n".join(prog) + "\n")
+    exe = tmp_path / "tuning_layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    assert int(out[0]) == 4 * sum(n for _, n in TUNING_LAYOUT)
+    k = 0
+    for (name, n), line in zip(TUNING_LAYOUT, out[1:]):
+        off, size = map(int, line.split())
+        assert (off, size) == (4 * k, 4 * n), name
+        k += n
