@@ -131,8 +131,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# One k_resolve launch of the workload, from a full ncu capture of that launch on a GB300 (the 6th
-# launch of `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`, summarised in
+# The resolve phase of one frame of the workload (k_resolve, and k_tile_lights where the range makes
+# its light lists once per tile), from full ncu captures on a GB300 (`-k regex:"k_resolve|k_tile_lights"`
+# on `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`, summarised in
 # profiles/k_resolve_*.md, same kernel code as this build's): DRAM bytes (dram__bytes_read.sum +
 # dram__bytes_write.sum), warp instructions issued (smsp__inst_executed.sum), and the issue-active
 # and FMA-pipe fractions ncu measured over the kernel's active cycles.
@@ -144,188 +145,6 @@ RESOLVE_PROFILE = {
                             "fma_pipe": 0.204, "profile": "profiles/k_resolve_atrium_1080p_4x.md"},
     "static_640x360_1x": {"traffic": 2486528, "instructions": 5135702, "issue_active": 0.312, "fma_pipe": 0.072,
                           "profile": "profiles/k_resolve_static_640x360_1x.md"},
-}
-SERVE_RATES = (100, 500, 1000, 1500, 2000, 5000)   # requests/s offered
-SERVE_BUDGET = 150 << 30                      # device-memory admission budget, bytes
-
-
-def max_over_ranks(values: list[float], device: str = "cpu") -> list[float]:
-    """Element-wise max of per-rank timings over the process group (identity without one): the
-    job's time is its slowest rank's."""
-    import torch
-    import torch.distributed as dist
-    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
-        return list(values)
-    t = torch.tensor(values, dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return [float(x) for x in t.tolist()]
-
-
-def job_throughput(units_per_rank: int, world: int, ms_max: float) -> float:
-    """Whole-job rate: the units every rank processed over the slowest rank's time."""
-    return units_per_rank * world / (ms_max * 1e-3)
-
-
-def _peaks() -> dict:
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured", "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0))}
-    return {"hbm_gbs": 6800.0, "src": "fallback", "sm_max_mhz": 2070.0}
-
-
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
-
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
-
-    def __init__(self, index: int):
-        self.index, self.proc, self.lines = index, None, []
-
-    def start(self):
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except OSError:
-            self.proc = None
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def stop(self) -> dict:
-        if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 7:
-                continue
-            try:
-                sm.append(float(parts[0])); mx.append(float(parts[1]))
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[3:7]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
-
-
-# One k_resolve launch of the workload, from a full ncu capture of that launch on a GB300 (the 6th
-# launch of `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`, summarised in
-# profiles/k_resolve_*.md, same kernel code as this build's): DRAM bytes (dram__bytes_read.sum +
-# dram__bytes_write.sum), warp instructions issued (smsp__inst_executed.sum), and the issue-active
-# and FMA-pipe fractions ncu measured over the kernel's active cycles.
-RESOLVE_PROFILE = {
-    "skinned_1080p_2xmsaa": {"traffic": 38164736 + 26880, "instructions": 150391476, "issue_active": 0.594, "fma_pipe": 0.221,
-                             "profile": "profiles/k_resolve_skinned_1080p_2x.md"},
-    "atrium_1080p_4xmsaa": {"traffic": 74964992 + 3102464, "instructions": 387640116, "issue_active": 0.590, "fma_pipe": 0.203,
-                            "profile": "profiles/k_resolve_atrium_1080p_4x.md"},
-    "static_640x360_1x": {"traffic": 2486528, "instructions": 5135702, "issue_active": 0.312, "fma_pipe": 0.072,
-                          "profile": "profiles/k_resolve_static_640x360_1x.md"},
-}
-SERVE_RATES = (100, 500, 1000, 1500, 2000, 5000)   # requests/s offered
-SERVE_BUDGET = 150 << 30                      # device-memory admission budget, bytes
-
-
-def max_over_ranks(values: list[float], device: str = "cpu") -> list[float]:
-    """Element-wise max of per-rank timings over the process group (identity without one): the
-    job's time is its slowest rank's."""
-    import torch
-    import torch.distributed as dist
-    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
-        return list(values)
-    t = torch.tensor(values, dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return [float(x) for x in t.tolist()]
-
-
-def job_throughput(units_per_rank: int, world: int, ms_max: float) -> float:
-    """Whole-job rate: the units every rank processed over the slowest rank's time."""
-    return units_per_rank * world / (ms_max * 1e-3)
-
-
-def _peaks() -> dict:
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured", "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0))}
-    return {"hbm_gbs": 6800.0, "src": "fallback", "sm_max_mhz": 2070.0}
-
-
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
-
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
-
-    def __init__(self, index: int):
-        self.index, self.proc, self.lines = index, None, []
-
-    def start(self):
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except OSError:
-            self.proc = None
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def stop(self) -> dict:
-        if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 7:
-                continue
-            try:
-                sm.append(float(parts[0])); mx.append(float(parts[1]))
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[3:7]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
-
-
-# One k_resolve launch of the workload, from a full ncu capture of that launch on a GB300 (the 6th
-# launch of `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`, summarised in
-# profiles/k_resolve_*.md, same kernel code as this build's): DRAM bytes (dram__bytes_read.sum +
-# dram__bytes_write.sum), warp instructions issued (smsp__inst_executed.sum), and the issue-active
-# and FMA-pipe fractions ncu measured over the kernel's active cycles.
-RESOLVE_PROFILE = {
-    "skinned_1080p_2xmsaa": {"traffic": 38543616 + 44544, "instructions": 155414816, "issue_active": 0.590, "fma_pipe": 0.219,
-                             "profile": "profiles/k_resolve_skinned_1080p_2x.md"},
-    "atrium_1080p_4xmsaa": {"traffic": 76679424 + 3172096, "instructions": 389862714, "issue_active": 0.596, "fma_pipe": 0.205,
-                            "profile": "profiles/k_resolve_atrium_1080p_4x.md"},
-    "static_640x360_1x": {"traffic": 2722560, "instructions": 5232418, "issue_active": 0.300, "fma_pipe": 0.067,
-                          "profile": "profiles/launches_static_640x360_1x.md"},
 }
 
 
