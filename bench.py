@@ -134,7 +134,7 @@ class ClockSampler:
 # The resolve phase of one frame of the workload (k_resolve, and k_tile_lights where the range makes
 # its light lists once per tile), from full ncu captures on a GB300 (`-k regex:"k_resolve|k_tile_lights"`
 # on `bench.py --steps 2 --warmup 3 --config N --no-cpu-baseline`, summarised in
-# profiles/k_resolve_*.md, same kernel code as this build's): DRAM bytes (dram__bytes_read.sum +
+# profiles/k_resolve_*.md, same kernel code as the library's): DRAM bytes (dram__bytes_read.sum +
 # dram__bytes_write.sum), warp instructions issued (smsp__inst_executed.sum), and the issue-active
 # and FMA-pipe fractions ncu measured over the kernel's active cycles.
 RESOLVE_PROFILE = {

@@ -111,7 +111,7 @@ static sft_model* build_model(const sfts_scene* sc, const sfts_model* src, const
             memcpy(ms->inds[j].inds, sl->inds, 512);
 #else
             /* the blob holds the AVX2 build's swizzle (batches of 8 triangles: v0 x8, v1 x8, v2 x8,
-             * pad x8); this build's batches are SFT_SIMD_WIDTH triangles wide (sofren2.c:2419-2438) */
+             * pad x8); the NEON build's batches are SFT_SIMD_WIDTH triangles wide (sofren2.c:2419-2438) */
             for (u32 t = 0; t < 128; t++)
                 for (u32 v = 0; v < 4; v++)
                     ms->inds[j].inds[(t / SFT_SIMD_WIDTH) * SFT_SIMD_WIDTH * 4 + v * SFT_SIMD_WIDTH + t % SFT_SIMD_WIDTH] =

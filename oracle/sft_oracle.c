@@ -2,7 +2,7 @@
  * sofren2 per-frame render path: CPU ORACLE (test infrastructure only).
  *
  * A portable scalar restatement of the reference's AVX2 path (sofren2.c), used as the
- * checker for the CUDA implementation and as the "port" CPU baseline.  It is not part of
+ * oracle that the CUDA implementation is tested against and as the "port" CPU baseline.  It is not part of
  * the shipped library and the library never links or calls it.
  *
  * Parity anchor: the restatement is pinned against the unmodified reference compiled

@@ -76,12 +76,12 @@ def build_library(force: bool = False) -> str:
 
 
 def reference_dir() -> str:
-    """Where the reference's sources are read from to build the checkers: SFT_REFERENCE_DIR, else
-    the build container's checkout of the reference project."""
+    """Where the reference's sources are read from to build the reference harnesses:
+    SFT_REFERENCE_DIR, else the checkout of the reference project beside this one's build host."""
     return os.environ.get("SFT_REFERENCE_DIR") or "/root/reference"
 
 
-def build_checkers() -> None:
+def build_oracle_and_reference() -> None:
     """CPU oracle always; the reference harness only where the reference sources exist (x86-64 + AVX2)."""
     oracle_dir = os.path.join(ROOT, "oracle")
     _run(["make", "-s", "-C", oracle_dir, "oracle"])
@@ -100,5 +100,5 @@ def build_checkers() -> None:
 if __name__ == "__main__":
     lib = build_library(force="--force" in sys.argv)
     print(lib)
-    if "--checkers" in sys.argv:
-        build_checkers()
+    if "--oracle" in sys.argv:
+        build_oracle_and_reference()
