@@ -1,7 +1,7 @@
 """Builds libsofren2_gb300.so (CUDA kernels for sm_103a + the C host runtime) in-tree.
 
     python -m sofren2_gb300.build            # library only
-    python -m sofren2_gb300.build --checkers # also the CPU oracle (and the reference, when present)
+    python -m sofren2_gb300.build --oracle   # also the CPU oracle (and the reference, when present)
 
 Device code is compiled with -fmad=false: the render path reproduces the reference's
 floating-point results bit for bit, so every fused multiply-add is written explicitly.
