@@ -340,10 +340,10 @@ SFTG_D void sample_nearest(const sftg_frame* F, int ti, int lod, float cu, float
 }
 
 /* ---------------------------------------------------------------- raster */
-/* One CTA per tile: the tile's payload list into a shared-memory visibility buffer (64-bit
- * z/order words), decoded into the global visibility buffer (float2: depth, vid bits) plus the
- * tile's depth range over valid samples (sofren2.c:5820-5853), which the resolve needs for its
- * light culling. */
+/* One (tile, band) item, run by one CTA: the tile's payload list into a shared-memory visibility
+ * buffer (64-bit z/order words) for the band's rows, decoded into the global visibility buffer
+ * (float2: depth, vid bits) plus the band's depth range over valid samples (sofren2.c:5820-5853),
+ * which the resolve needs for its light culling (a tile's range is the union of its bands'). */
 template <int S>
 SFTG_D void raster_item(const sftg_tile_args& A, uint32_t tile0, int slab_rows, int fixed_bands, uint32_t item)
 {
