@@ -65,6 +65,33 @@ def test_gpu_equals_oracle_random(renderer, seed, samples):
     assert not bad, (res, first_vid_mismatch(ref, out, cols, samples))
 
 
+@pytest.mark.parametrize("seed", [31, 32])
+@pytest.mark.parametrize("samples", [1, 4])
+def test_gpu_equals_oracle_random_atrium(renderer, seed, samples):
+    """Fresh seeds of the lightmapped atrium (pillars, arches, lightmap pages, skinned humanoids,
+    10 point lights) at a small size: the lightmap shading path against the oracle."""
+    sc = scenes.atrium_scene(width=256, height=160, seed=seed, nx=6, nz=4, levels=2, arch_segments=6, n_tex=4, tex_size=64,
+                             lm_size=128, n_lights=10, n_chars=2, char_tex=64, floor_quads=(24, 12))
+    blob = sc.to_bytes()
+    o = Oracle(blob)
+    try:
+        ref = o.render_dump(0, samples)
+    finally:
+        o.close()
+    assert ref["invalid_packets"] == 0
+    h = renderer.load_scene(blob)
+    try:
+        renderer.set_samples(samples)
+        tss, npx = runtime.scene_counts(sc)
+        out = renderer.render_debug(h, 0, tss, npx)
+    finally:
+        renderer.free_scene(h)
+    res = compare_frames(ref, out, samples, len(sc.frames[0].point_lights))
+    bad = {k: v for k, v in res.items() if k not in ("color_max_lsb", "tlas") and v != 0}
+    cols = (sc.frames[0].width + 63) // 64
+    assert not bad, (res, first_vid_mismatch(ref, out, cols, samples))
+
+
 def test_gpu_shadow_factors_equal_oracle(renderer):
     """Per-pixel shadow intensity of every tile light (1x) is identical to the FP32 oracle
     (the tolerance stated for shadow factors is 1e-5 absolute).  The FP32 values against an FP64

@@ -83,6 +83,36 @@ def test_oracle_equals_reference_random(seed, samples):
     assert not bad, res
 
 
+def _skinned(seed):
+    from sofren2_gb300 import scenes
+    return scenes.skinned_characters_scene(width=256, height=160, seed=seed, n_chars=3, n_lights=6, tex_size=64)
+
+
+def _atrium(seed):
+    from sofren2_gb300 import scenes
+    return scenes.atrium_scene(width=256, height=160, seed=seed, nx=6, nz=4, levels=2, arch_segments=6, n_tex=4, tex_size=64,
+                               lm_size=128, n_lights=10, n_chars=2, char_tex=64, floor_quads=(24, 12))
+
+
+@pytest.mark.skipif(not reference_available(1), reason="reference not compiled here (oracle/_ref, x86-64 with AVX2)")
+@pytest.mark.parametrize("kind,samples", [("skinned", 2), ("atrium", 4)])
+@pytest.mark.parametrize("seed", [31, 32])
+def test_oracle_equals_reference_random_workload_shapes(kind, samples, seed):
+    """Fresh seeds of the two 1080p workloads' scene families at a small size: skinned humanoids
+    with capsule proxies at 2x, and the lightmapped atrium with skinned humanoids at 4x."""
+    sc = (_skinned if kind == "skinned" else _atrium)(seed)
+    blob = sc.to_bytes()
+    r = reference_dump(blob, samples)[0]
+    o = Oracle(blob)
+    try:
+        g = o.render_dump(0, samples)
+    finally:
+        o.close()
+    res = compare_frames(r, g, samples, len(sc.frames[0].point_lights))
+    bad = {k: v for k, v in res.items() if k != "color_max_lsb" and v != 0}
+    assert not bad, res
+
+
 def test_oracle_detects_undefined_packet_frustum():
     """A light inside a proxy batch's bounding box leaves the reference's packet frustum
     uninitialised (sofren2.c:4044-4048); the oracle counts those packets so parity scenes can
