@@ -76,9 +76,10 @@ def build_library(force: bool = False) -> str:
 
 
 def reference_dir() -> str:
-    """Where the reference's sources are read from to build the reference harnesses:
-    SFT_REFERENCE_DIR, else the checkout of the reference project beside this one's build host."""
-    return os.environ.get("SFT_REFERENCE_DIR") or "/root/reference"
+    """Where the reference's sources are read from to (re)build the reference harnesses: the
+    directory named by SFT_REFERENCE_DIR, or "" when it is not set.  Harnesses built earlier stay
+    in oracle/_ref and keep serving the tests without it."""
+    return os.environ.get("SFT_REFERENCE_DIR", "")
 
 
 def build_oracle_and_reference() -> None:
@@ -86,7 +87,7 @@ def build_oracle_and_reference() -> None:
     oracle_dir = os.path.join(ROOT, "oracle")
     _run(["make", "-s", "-C", oracle_dir, "oracle"])
     ref_dir = reference_dir()
-    if os.path.exists(os.path.join(ref_dir, "sofren2.c")) and os.uname().machine == "x86_64":
+    if ref_dir and os.path.exists(os.path.join(ref_dir, "sofren2.c")) and os.uname().machine == "x86_64":
         _run(["make", "-s", "-C", oracle_dir, "ref", f"REF_DIR={ref_dir}"])
     # the reference's own render path for the timed CPU baseline, native to this host (NEON on
     # aarch64), from the copy of its source that `make ref` left beside the builds

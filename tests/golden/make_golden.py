@@ -28,6 +28,8 @@ from oracle_lib import reference_dump  # noqa: E402
 def main(names: list[str]) -> None:
     from sofren2_gb300.build import reference_dir
     ref_dir = reference_dir()
+    if not ref_dir:
+        raise SystemExit("set SFT_REFERENCE_DIR to the reference project's checkout")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={ref_dir}"], check=True)
     path = os.path.join(HERE, "golden.json")
     golden = json.load(open(path)) if os.path.exists(path) else {}
